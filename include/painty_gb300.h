@@ -1,0 +1,199 @@
+/*
+ * painty_gb300.h -- C ABI of the GB300-native Kubelka-Munk paint path.
+ *
+ * A drop-in for lindemeier/painty's paint-rendering hot path: the imprint brush's stamp
+ * deposition onto the wet/dry canvas layers, the volume-weighted K,S mixing of pickup and
+ * deposit, and the per-pixel Kubelka-Munk layer composite onto the substrate reflectance.
+ * The C++ facade in painty_gb300.hpp mirrors painty's Canvas / FootprintBrush / Renderer
+ * classes on top of these entry points.
+ *
+ * Conventions
+ *  - Every call returns painty_status; nothing throws across this boundary.
+ *    painty_last_error() gives a message for the calling thread's last failure.
+ *  - Handles own device memory; the caller owns host buffers. Host images are row-major with
+ *    a top-left origin (painty's cv::Mat_ layout, no y-flip).
+ *  - `stream` is a cudaStream_t (NULL = the legacy default stream). Calls that take host
+ *    buffers are synchronous with respect to those buffers: they return once the host
+ *    memory may be reused (upload) or holds the result (download).
+ *  - A handle may be used from one thread at a time.
+ *  - Storage formats: F32 (default), F16 / BF16 (K and S in that type, volume in FP16; all
+ *    arithmetic in FP32), F64 (double storage and arithmetic: the parity mode whose stamping
+ *    reproduces painty's double-precision CPU results bit for bit).
+ */
+#ifndef PAINTY_GB300_H
+#define PAINTY_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PAINTY_GB300_ABI_VERSION 1
+
+typedef enum painty_status {
+  PAINTY_OK = 0,
+  PAINTY_ERR_INVALID_ARGUMENT = 1, /* painty throws std::invalid_argument */
+  PAINTY_ERR_OUT_OF_MEMORY = 2,
+  PAINTY_ERR_CUDA = 3,
+  PAINTY_ERR_UNSUPPORTED = 4,
+  PAINTY_ERR_BUDGET = 5,    /* serving: request larger than the memory budget */
+  PAINTY_ERR_TIMEOUT = 6,   /* a bounded device wait ran out */
+  PAINTY_ERR_CANCELLED = 7, /* serving: request cancelled before it ran */
+  PAINTY_ERR_STATE = 8      /* handle in the wrong state for the call */
+} painty_status;
+
+typedef enum painty_storage {
+  PAINTY_STORAGE_F32 = 0,
+  PAINTY_STORAGE_F16 = 1,
+  PAINTY_STORAGE_BF16 = 2,
+  PAINTY_STORAGE_F64 = 3
+} painty_storage;
+
+/* Host buffer formats. INTERLEAVED = pixel-major channels (cv::Mat_<vec3>);
+ * PLANAR = one full rows*cols plane per channel. One-channel planes read the same either way. */
+typedef enum painty_host_format {
+  PAINTY_HOST_F64_INTERLEAVED = 0,
+  PAINTY_HOST_F32_INTERLEAVED = 1,
+  PAINTY_HOST_F64_PLANAR = 2,
+  PAINTY_HOST_F32_PLANAR = 3
+} painty_host_format;
+
+/* Planes of a paint layer / canvas. */
+typedef enum painty_plane {
+  PAINTY_PLANE_K = 0,  /* absorption, 3 channels */
+  PAINTY_PLANE_S = 1,  /* scattering, 3 channels */
+  PAINTY_PLANE_V = 2,  /* paint volume (layer thickness), 1 channel */
+  PAINTY_PLANE_R0 = 3, /* canvas only: substrate reflectance, 3 channels */
+  PAINTY_PLANE_H = 4   /* canvas only: height map, 1 channel */
+} painty_plane;
+
+typedef struct painty_layer painty_layer;   /* PaintLayer<vec3>  (K, S, V) */
+typedef struct painty_image painty_image;   /* Mat<vec3> reflectance image on the device */
+typedef struct painty_canvas painty_canvas; /* Canvas<vec3>: wet layer + R0 + h */
+typedef struct painty_brush painty_brush;   /* FootprintBrush<vec3> */
+
+/* ------------------------------------------------------------------ library */
+int32_t painty_abi_version(void);
+const char* painty_status_string(painty_status s);
+const char* painty_last_error(void);
+/* Number of this library's kernel launches so far in this process (all devices). */
+int64_t painty_kernel_launch_count(void);
+
+/* ------------------------------------------------------------------ layers
+ * replaces PaintLayer<vec>::PaintLayer(rows, cols) + clear()  (painty/renderer/PaintLayer.hxx:27-30, 68-74) */
+painty_status painty_layer_create(int32_t rows, int32_t cols, painty_storage storage,
+                                  painty_layer** out);
+painty_status painty_layer_destroy(painty_layer* layer);
+/* replaces PaintLayer::clear (PaintLayer.hxx:68-74) */
+painty_status painty_layer_clear(painty_layer* layer, void* stream);
+/* replaces writes through getK_buffer/getS_buffer/getV_buffer (PaintLayer.hxx:32-54) */
+painty_status painty_layer_upload(painty_layer* layer, painty_plane plane, const void* host,
+                                  painty_host_format fmt, void* stream);
+painty_status painty_layer_download(const painty_layer* layer, painty_plane plane, void* host,
+                                    painty_host_format fmt, void* stream);
+/* replaces PaintLayer::copyTo (PaintLayer.hxx:103-111); same size and storage */
+painty_status painty_layer_copy(const painty_layer* src, painty_layer* dst, void* stream);
+painty_status painty_layer_info(const painty_layer* layer, int32_t* rows, int32_t* cols,
+                                painty_storage* storage);
+
+/* ------------------------------------------------------------------ images (R0, R1)
+ * F32 or F64 storage. */
+painty_status painty_image_create(int32_t rows, int32_t cols, painty_storage storage,
+                                  painty_image** out);
+painty_status painty_image_destroy(painty_image* img);
+painty_status painty_image_fill(painty_image* img, double r, double g, double b, void* stream);
+painty_status painty_image_upload(painty_image* img, const void* host, painty_host_format fmt,
+                                  void* stream);
+painty_status painty_image_download(const painty_image* img, void* host,
+                                    painty_host_format fmt, void* stream);
+
+/* ------------------------------------------------------------------ composite
+ * replaces PaintLayer::composeOnto applied to layers[0..L-1] in order
+ * (painty/renderer/PaintLayer.hxx:81-96, per pixel painty/core/KubelkaMunk.hxx:25-83),
+ * fused into one pass: out = KM(layer L-1, ... KM(layer 0, r0)). `out` may be `r0`
+ * (in place, as composeOnto). Layers share size; out/r0 storage F32, or F64 with F64 layers. */
+painty_status painty_compose_layers(const painty_layer* const* layers, int32_t L,
+                                    const painty_image* r0, painty_image* out, void* stream);
+/* The same one layer per launch (the plain drop-in composeOnto, R0 read and written per layer). */
+painty_status painty_compose_layers_unfused(const painty_layer* const* layers, int32_t L,
+                                            const painty_image* r0, painty_image* out,
+                                            void* stream);
+
+/* ------------------------------------------------------------------ canvas
+ * replaces Canvas<vec>::Canvas(rows, cols) (painty/renderer/Canvas.hxx:26-35): wet layer
+ * cleared, R0 = background 1.0, h = 0. */
+painty_status painty_canvas_create(int32_t rows, int32_t cols, painty_storage storage,
+                                   painty_canvas** out);
+painty_status painty_canvas_destroy(painty_canvas* canvas);
+/* replaces Canvas::clear (Canvas.hxx:37-58) */
+painty_status painty_canvas_clear(painty_canvas* canvas, void* stream);
+/* plane K/S/V: the wet layer; R0: substrate (replaces Canvas::setBackground, :80-87); H */
+painty_status painty_canvas_upload(painty_canvas* canvas, painty_plane plane, const void* host,
+                                   painty_host_format fmt, void* stream);
+painty_status painty_canvas_download(const painty_canvas* canvas, painty_plane plane,
+                                     void* host, painty_host_format fmt, void* stream);
+/* Borrowed handles (valid while the canvas lives): Canvas::getPaintLayer, Canvas::getR0 */
+painty_status painty_canvas_layer(painty_canvas* canvas, painty_layer** out);
+painty_status painty_canvas_r0(painty_canvas* canvas, painty_image** out);
+painty_status painty_canvas_info(const painty_canvas* canvas, int32_t* rows, int32_t* cols,
+                                 painty_storage* storage);
+/* replaces Renderer<vec>::compose(canvas) (painty/renderer/Renderer.hxx:26-53) */
+painty_status painty_canvas_compose(const painty_canvas* canvas, painty_image* out, void* stream);
+/* replaces Canvas::dryCanvas (Canvas.hxx:105-121): h += V, R0 = KM(K,S,R0,V), wet = 0 */
+painty_status painty_canvas_dry(painty_canvas* canvas, void* stream);
+
+/* ------------------------------------------------------------------ imprint brush
+ * replaces FootprintBrush<vec>::FootprintBrush(radius) (painty/renderer/FootprintBrush.hxx:29-37).
+ * `footprint` (fh x fw, row-major, values in [0,1]) stands in for data/footprint/footprint.png:
+ * setRadius resamples it to the brush width (bilinear, pixel-centre aligned, BORDER_REFLECT)
+ * and pads it to cover all rotations (FootprintBrush.hxx:46-63). */
+painty_status painty_brush_create(double radius, const double* footprint, int32_t fh,
+                                  int32_t fw, painty_brush** out);
+painty_status painty_brush_destroy(painty_brush* brush);
+/* replaces FootprintBrush::setRadius (:46-63); no change unless |radius - current| >= 0.5 */
+painty_status painty_brush_set_radius(painty_brush* brush, double radius);
+/* replaces setPickupRate / setDepositionRate (:182-188) */
+painty_status painty_brush_set_rates(painty_brush* brush, double pickup_rate,
+                                     double deposition_rate);
+painty_status painty_brush_get_rates(const painty_brush* brush, double* pickup_rate,
+                                     double* deposition_rate);
+/* replaces setUseSnapshotBuffer (:202-204) */
+painty_status painty_brush_set_snapshot(painty_brush* brush, int32_t use);
+/* replaces dip (:150-154): clears the pickup map, sets the paint {K, S} */
+painty_status painty_brush_dip(painty_brush* brush, const double K[3], const double S[3],
+                               void* stream);
+/* replaces updateSnapshot(canvas) (:168-172) */
+painty_status painty_brush_update_snapshot(painty_brush* brush, const painty_canvas* canvas,
+                                           void* stream);
+/* F = footprint side, S = pickup-map side (getFootprint / getPickupMap sizes) */
+painty_status painty_brush_info(const painty_brush* brush, double* radius, int32_t* F,
+                                int32_t* S);
+/* getFootprint (:178-180): F*F doubles */
+painty_status painty_brush_footprint(const painty_brush* brush, double* host);
+/* getPickupMap (:174-176): plane K/S (S*S*3 interleaved) or V (S*S) */
+painty_status painty_brush_download_pickup(const painty_brush* brush, painty_plane plane,
+                                           void* host, painty_host_format fmt, void* stream);
+
+/* replaces FootprintBrush::imprint(center, theta, canvas) (:73-143) */
+painty_status painty_imprint(painty_canvas* canvas, painty_brush* brush, double cx, double cy,
+                             double theta, void* stream);
+/* n imprints in order; cx_cy_theta = n triples (host) */
+painty_status painty_stamps(painty_canvas* canvas, painty_brush* brush,
+                            const double* cx_cy_theta, int64_t n, void* stream);
+/* replaces FootprintBrush::paintStroke(path, canvas) (:206-268): Catmull-Rom through the
+ * path, a stamp every `spacing` of chord length per segment (1.0 = the reference), angle
+ * from the spline derivative. path_xy = n (x, y) pairs (host). Returns the stamp count. */
+painty_status painty_stroke(painty_canvas* canvas, painty_brush* brush, const double* path_xy,
+                            int32_t n, double spacing, int64_t* stamps_out, void* stream);
+
+/* ------------------------------------------------------------------ mixing (host)
+ * replaces PaintMixer::mixSinglePaint (painty/mixer/src/PaintMixer.cxx:327-355) */
+painty_status painty_mix_paint(const double* weights, int32_t n, const double* palette_K,
+                               const double* palette_S, double K[3], double S[3]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PAINTY_GB300_H */

@@ -1,0 +1,425 @@
+"""Python binding of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this module, as the
+checker. It loads oracle/_build/liboracle.so (the double-precision restatement of painty's
+paint path, oracle/painty_oracle.cpp) and, where it was built, oracle/_ref/libpainty_ref.so
+(painty's own headers compiled against the repository's Eigen/OpenCV stand-ins).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "liboracle.so"
+REF_LIB = HERE / "_ref" / "libpainty_ref.so"
+REFERENCE_ROOT = Path("/root/reference")
+
+_P, _I32, _I64, _D = C.c_void_p, C.c_int32, C.c_int64, C.c_double
+
+
+def build(ref: bool = False) -> None:
+    """make -C oracle (and `make ref` when the reference checkout is present)."""
+    subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    if ref and (REFERENCE_ROOT / "painty").is_dir():
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={REFERENCE_ROOT}"], check=True)
+
+
+def _load(path: Path):
+    if not path.exists():
+        build(ref=path == REF_LIB)
+    return C.CDLL(str(path))
+
+
+def _p(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+class _Lib:
+    def __init__(self, lib, pre: str):
+        self.lib, self.pre = lib, pre
+
+    def f(self, name, *args, res=None):
+        fn = getattr(self.lib, f"{self.pre}_{name}")
+        fn.argtypes = list(args)
+        fn.restype = res
+        return fn
+
+
+class Oracle:
+    """The restated oracle (prefix orc_)."""
+
+    def __init__(self):
+        self.lib = _load(LIB)
+        L = _Lib(self.lib, "orc")
+        self.coth = L.f("coth", _D, res=_D)
+        self._cr = L.f("compute_reflectance", _P, _P, _P, _D, _P)
+        self._km64 = L.f("km_fp64", _P, _P, _P, _D, _P, _P)
+        self.catmull_rom_1d = L.f("catmull_rom_1d", _D, _D, _D, _D, _D, res=_D)
+        self._spline = L.f("spline_catmull_rom", _P, _I32, _D, _P)
+        self._interp = L.f("interpolate", _P, _I32, _I32, _D, _D, res=_D)
+        self._compose = L.f("compose_layers", _I64, _I32, _P, _P, _P, _P, _P, _I32, _I32)
+        self._compose32 = L.f("compose_layers_f32_soa", _I64, _I32, _P, _P, _P, _P, _P, _I32)
+        self._cc = L.f("canvas_create", _I32, _I32, res=_P)
+        self._cd = L.f("canvas_destroy", _P)
+        self._cp = L.f("canvas_plane", _P, _I32, res=_P)
+        self._cdry = L.f("canvas_dry", _P)
+        self._ccomp = L.f("canvas_compose", _P, _P)
+        self._bc = L.f("brush_create", _D, _P, _I32, _I32, res=_P)
+        self._bd = L.f("brush_destroy", _P)
+        self._bsr = L.f("brush_set_radius", _P, _D)
+        self._brates = L.f("brush_set_rates", _P, _D, _D)
+        self._bsnap = L.f("brush_set_snapshot", _P, _I32)
+        self._bdip = L.f("brush_dip", _P, _P, _P)
+        self._bupd = L.f("brush_update_snapshot", _P, _P)
+        self._bimp = L.f("brush_imprint", _P, _P, _D, _D, _D)
+        self._bstamps = L.f("brush_stamps", _P, _P, _P, _I64)
+        self._bstroke = L.f("brush_paint_stroke", _P, _P, _P, _I32, _D, res=_I64)
+        self._sstamps = L.f("stroke_stamps", _P, _I32, _D, _P, _I64, res=_I64)
+        self._binfo = L.f("brush_info", _P, C.POINTER(_I32), C.POINTER(_I32), res=_D)
+        self._bfp = L.f("brush_footprint", _P, res=_P)
+        self._bpick = L.f("brush_pickup", _P, _I32, res=_P)
+        self._mix = L.f("mix_single_paint", _P, _I32, _P, _P, _P, _P)
+        self._lab = L.f("rgb2lab", _P, _P)
+        self._de = L.f("ciede2000", _P, _P, res=_D)
+        self._deimg = L.f("delta_e_images", _I64, _P, _P, C.POINTER(_D), _I32, res=_D)
+        self._resample = L.f("resample", _P, _I32, _I32, _I32, _I32, _P)
+
+    # -- math
+    def compute_reflectance(self, K, S, R0, d):
+        K, S, R0 = (np.ascontiguousarray(x, dtype=np.float64) for x in (K, S, R0))
+        out = np.zeros(3)
+        self._cr(_p(K), _p(S), _p(R0), float(d), _p(out))
+        return out
+
+    def km_fp64(self, K, S, R0, d):
+        K, S, R0 = (np.ascontiguousarray(x, dtype=np.float64) for x in (K, S, R0))
+        R, T = np.zeros(3), np.zeros(3)
+        self._km64(_p(K), _p(S), _p(R0), float(d), _p(R), _p(T))
+        return R, T
+
+    def spline_catmull_rom(self, pts, u):
+        pts = np.ascontiguousarray(pts, dtype=np.float64)
+        out = np.zeros(2)
+        self._spline(_p(pts), len(pts), float(u), _p(out))
+        return out
+
+    def interpolate(self, img, x, y):
+        img = np.ascontiguousarray(img, dtype=np.float64)
+        return self._interp(_p(img), img.shape[0], img.shape[1], float(x), float(y))
+
+    def resample(self, img, rows, cols):
+        img = np.ascontiguousarray(img, dtype=np.float64)
+        out = np.zeros((rows, cols))
+        self._resample(_p(img), img.shape[0], img.shape[1], rows, cols, _p(out))
+        return out
+
+    def compose_layers(self, K, S, V, R0, mode: int = 0, threads: int = 1):
+        """K, S: (L, npix, 3); V: (L, npix); R0: (npix, 3) -> (npix, 3). mode 1 = FP64 oracle."""
+        K, S, V, R0 = (np.ascontiguousarray(x, dtype=np.float64) for x in (K, S, V, R0))
+        L, npix = V.shape
+        out = np.zeros((npix, 3))
+        self._compose(npix, L, _p(K), _p(S), _p(V), _p(R0), _p(out), mode, threads)
+        return out
+
+    def compose_layers_f32_planar(self, K, S, V, R0, threads: int = 1):
+        """The reference composite over float32 planar stacks (timed CPU baseline)."""
+        L = V.shape[0]
+        npix = V[0].size
+        out = np.empty((3,) + V.shape[1:], dtype=np.float32)
+        self._compose32(npix, L, _p(K), _p(S), _p(V), _p(R0), _p(out), threads)
+        return out
+
+    def mix_single_paint(self, w, K, S):
+        w, K, S = (np.ascontiguousarray(x, dtype=np.float64) for x in (w, K, S))
+        k, s = np.zeros(3), np.zeros(3)
+        self._mix(_p(w), len(w), _p(K), _p(S), _p(k), _p(s))
+        return k, s
+
+    def rgb2lab(self, rgb):
+        rgb = np.ascontiguousarray(rgb, dtype=np.float64)
+        out = np.zeros(3)
+        self._lab(_p(rgb), _p(out))
+        return out
+
+    def ciede2000(self, a, b):
+        a, b = (np.ascontiguousarray(x, dtype=np.float64) for x in (a, b))
+        return self._de(_p(a), _p(b))
+
+    def delta_e(self, rgb_a, rgb_b, threads: int = 8):
+        """(max, mean) CIEDE2000 between two linear-RGB images (..., 3)."""
+        a = np.ascontiguousarray(rgb_a, dtype=np.float64).reshape(-1, 3)
+        b = np.ascontiguousarray(rgb_b, dtype=np.float64).reshape(-1, 3)
+        mean = _D()
+        mx = self._deimg(a.shape[0], _p(a), _p(b), C.byref(mean), threads)
+        return mx, mean.value
+
+    def stroke_stamps(self, path, spacing):
+        path = np.ascontiguousarray(path, dtype=np.float64)
+        n = self._sstamps(_p(path), len(path), float(spacing), None, 0)
+        out = np.zeros((max(n, 1), 3))
+        self._sstamps(_p(path), len(path), float(spacing), _p(out), n)
+        return out[:n]
+
+    # -- objects
+    def canvas(self, rows, cols):
+        return OCanvas(self, rows, cols)
+
+    def brush(self, radius, footprint):
+        return OBrush(self, radius, footprint)
+
+
+class OCanvas:
+    def __init__(self, o: Oracle, rows: int, cols: int):
+        self.o, self.rows, self.cols = o, rows, cols
+        self.h = o._cc(rows, cols)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.o._cd(self.h)
+            self.h = None
+
+    def plane(self, which: str) -> np.ndarray:
+        idx = {"K": 0, "S": 1, "V": 2, "R0": 3, "h": 4}[which]
+        n = self.rows * self.cols * (1 if which in ("V", "h") else 3)
+        arr = np.ctypeslib.as_array(C.cast(self.o._cp(self.h, idx), C.POINTER(_D)), (n,))
+        return arr.reshape((self.rows, self.cols) if which in ("V", "h") else
+                           (self.rows, self.cols, 3))
+
+    def set(self, which: str, data) -> None:
+        self.plane(which)[...] = data
+
+    def get(self, which: str) -> np.ndarray:
+        return self.plane(which).copy()
+
+    def dry(self) -> None:
+        self.o._cdry(self.h)
+
+    def compose(self) -> np.ndarray:
+        out = np.zeros((self.rows, self.cols, 3))
+        self.o._ccomp(self.h, _p(out))
+        return out
+
+
+class OBrush:
+    def __init__(self, o: Oracle, radius: float, footprint: np.ndarray):
+        self.o = o
+        fp = np.ascontiguousarray(footprint, dtype=np.float64)
+        self.h = o._bc(float(radius), _p(fp), fp.shape[0], fp.shape[1])
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.o._bd(self.h)
+            self.h = None
+
+    def set_radius(self, r):
+        self.o._bsr(self.h, float(r))
+
+    def set_rates(self, pickup, deposition):
+        self.o._brates(self.h, float(pickup), float(deposition))
+
+    def set_snapshot(self, use: bool):
+        self.o._bsnap(self.h, 1 if use else 0)
+
+    def dip(self, K, S):
+        K, S = (np.ascontiguousarray(x, dtype=np.float64) for x in (K, S))
+        self.o._bdip(self.h, _p(K), _p(S))
+
+    def update_snapshot(self, canvas: OCanvas):
+        self.o._bupd(self.h, canvas.h)
+
+    def imprint(self, canvas: OCanvas, cx, cy, theta):
+        self.o._bimp(self.h, canvas.h, float(cx), float(cy), float(theta))
+
+    def stamps(self, canvas: OCanvas, s):
+        s = np.ascontiguousarray(s, dtype=np.float64).reshape(-1, 3)
+        self.o._bstamps(self.h, canvas.h, _p(s), s.shape[0])
+
+    def paint_stroke(self, canvas: OCanvas, path, spacing=1.0) -> int:
+        path = np.ascontiguousarray(path, dtype=np.float64)
+        return self.o._bstroke(self.h, canvas.h, _p(path), len(path), float(spacing))
+
+    def info(self):
+        F, S = _I32(), _I32()
+        r = self.o._binfo(self.h, C.byref(F), C.byref(S))
+        return r, F.value, S.value
+
+    def footprint(self):
+        _, F, _ = self.info()
+        return np.ctypeslib.as_array(C.cast(self.o._bfp(self.h), C.POINTER(_D)), (F, F)).copy()
+
+    def pickup(self, which: str):
+        _, _, S = self.info()
+        idx = {"K": 0, "S": 1, "V": 2}[which]
+        n = S * S * (1 if which == "V" else 3)
+        a = np.ctypeslib.as_array(C.cast(self.o._bpick(self.h, idx), C.POINTER(_D)), (n,))
+        return a.reshape((S, S) if which == "V" else (S, S, 3)).copy()
+
+
+class Reference:
+    """painty's own headers compiled against the stand-ins (prefix ref_); None if unbuilt."""
+
+    def __init__(self):
+        self.lib = _load(REF_LIB)
+        L = _Lib(self.lib, "ref")
+        self.coth = L.f("coth", _D, res=_D)
+        self._cr = L.f("compute_reflectance", _P, _P, _P, _D, _P)
+        self.catmull_rom_1d = L.f("catmull_rom_1d", _D, _D, _D, _D, _D, res=_D)
+        self._spline = L.f("spline_catmull_rom", _P, _I32, _D, _P)
+        self._interp = L.f("interpolate", _P, _I32, _I32, _D, _D, res=_D)
+        self._lab = L.f("rgb2lab", _P, _P)
+        self._de = L.f("ciede2000", _P, _P, res=_D)
+        self._cc = L.f("canvas_create", _I32, _I32, res=_P)
+        self._cd = L.f("canvas_destroy", _P)
+        self._cget = L.f("canvas_get", _P, _I32, _P)
+        self._cset = L.f("canvas_set", _P, _I32, _P)
+        self._cdry = L.f("canvas_dry", _P)
+        self._ccomp = L.f("canvas_compose", _P, _P)
+        self._bc = L.f("brush_create", _D, _P, _I32, _I32, res=_P)
+        self._bd = L.f("brush_destroy", _P)
+        self._bsr = L.f("brush_set_radius", _P, _D)
+        self._brates = L.f("brush_set_rates", _P, _D, _D)
+        self._bsnap = L.f("brush_set_snapshot", _P, _I32)
+        self._bdip = L.f("brush_dip", _P, _P, _P)
+        self._bupd = L.f("brush_update_snapshot", _P, _P)
+        self._bimp = L.f("brush_imprint", _P, _P, _D, _D, _D)
+        self._bstamps = L.f("brush_stamps", _P, _P, _P, _I64)
+        self._bstroke = L.f("brush_paint_stroke", _P, _P, _P, _I32, res=_I64)
+        self._binfo = L.f("brush_info", _P, C.POINTER(_I32), C.POINTER(_I32))
+        self._bfp = L.f("brush_footprint", _P, _P)
+        self._bpick = L.f("brush_pickup", _P, _I32, _P)
+
+    @staticmethod
+    def available() -> bool:
+        if REF_LIB.exists():
+            return True
+        if not (REFERENCE_ROOT / "painty").is_dir():
+            return False
+        try:
+            build(ref=True)
+        except Exception:
+            return False
+        return REF_LIB.exists()
+
+    def compute_reflectance(self, K, S, R0, d):
+        K, S, R0 = (np.ascontiguousarray(x, dtype=np.float64) for x in (K, S, R0))
+        out = np.zeros(3)
+        self._cr(_p(K), _p(S), _p(R0), float(d), _p(out))
+        return out
+
+    def spline_catmull_rom(self, pts, u):
+        pts = np.ascontiguousarray(pts, dtype=np.float64)
+        out = np.zeros(2)
+        self._spline(_p(pts), len(pts), float(u), _p(out))
+        return out
+
+    def interpolate(self, img, x, y):
+        img = np.ascontiguousarray(img, dtype=np.float64)
+        return self._interp(_p(img), img.shape[0], img.shape[1], float(x), float(y))
+
+    def rgb2lab(self, rgb):
+        rgb = np.ascontiguousarray(rgb, dtype=np.float64)
+        out = np.zeros(3)
+        self._lab(_p(rgb), _p(out))
+        return out
+
+    def ciede2000(self, a, b):
+        a, b = (np.ascontiguousarray(x, dtype=np.float64) for x in (a, b))
+        return self._de(_p(a), _p(b))
+
+    def canvas(self, rows, cols):
+        return RCanvas(self, rows, cols)
+
+    def brush(self, radius, footprint):
+        return RBrush(self, radius, footprint)
+
+
+class RCanvas:
+    def __init__(self, r: Reference, rows: int, cols: int):
+        self.r, self.rows, self.cols = r, rows, cols
+        self.h = r._cc(rows, cols)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.r._cd(self.h)
+            self.h = None
+
+    def get(self, which: str) -> np.ndarray:
+        idx = {"K": 0, "S": 1, "V": 2, "R0": 3, "h": 4}[which]
+        one = which in ("V", "h")
+        out = np.zeros((self.rows, self.cols) if one else (self.rows, self.cols, 3))
+        self.r._cget(self.h, idx, _p(out))
+        return out
+
+    def set(self, which: str, data) -> None:
+        idx = {"K": 0, "S": 1, "V": 2, "R0": 3, "h": 4}[which]
+        d = np.ascontiguousarray(data, dtype=np.float64)
+        self.r._cset(self.h, idx, _p(d))
+
+    def dry(self):
+        self.r._cdry(self.h)
+
+    def compose(self):
+        out = np.zeros((self.rows, self.cols, 3))
+        self.r._ccomp(self.h, _p(out))
+        return out
+
+
+class RBrush:
+    def __init__(self, r: Reference, radius: float, footprint: np.ndarray):
+        self.r = r
+        fp = np.ascontiguousarray(footprint, dtype=np.float64)
+        self.h = r._bc(float(radius), _p(fp), fp.shape[0], fp.shape[1])
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.r._bd(self.h)
+            self.h = None
+
+    def set_radius(self, v):
+        self.r._bsr(self.h, float(v))
+
+    def set_rates(self, p, d):
+        self.r._brates(self.h, float(p), float(d))
+
+    def set_snapshot(self, use):
+        self.r._bsnap(self.h, 1 if use else 0)
+
+    def dip(self, K, S):
+        K, S = (np.ascontiguousarray(x, dtype=np.float64) for x in (K, S))
+        self.r._bdip(self.h, _p(K), _p(S))
+
+    def update_snapshot(self, canvas):
+        self.r._bupd(self.h, canvas.h)
+
+    def imprint(self, canvas, cx, cy, theta):
+        self.r._bimp(self.h, canvas.h, float(cx), float(cy), float(theta))
+
+    def stamps(self, canvas, s):
+        s = np.ascontiguousarray(s, dtype=np.float64).reshape(-1, 3)
+        self.r._bstamps(self.h, canvas.h, _p(s), s.shape[0])
+
+    def paint_stroke(self, canvas, path) -> int:
+        path = np.ascontiguousarray(path, dtype=np.float64)
+        return self.r._bstroke(self.h, canvas.h, _p(path), len(path))
+
+    def info(self):
+        F, S = _I32(), _I32()
+        self.r._binfo(self.h, C.byref(F), C.byref(S))
+        return F.value, S.value
+
+    def footprint(self):
+        F, _ = self.info()
+        out = np.zeros((F, F))
+        self.r._bfp(self.h, _p(out))
+        return out
+
+    def pickup(self, which):
+        _, S = self.info()
+        idx = {"K": 0, "S": 1, "V": 2}[which]
+        out = np.zeros((S, S) if which == "V" else (S, S, 3))
+        self.r._bpick(self.h, idx, _p(out))
+        return out

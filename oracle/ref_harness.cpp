@@ -1,0 +1,224 @@
+// ref_harness.cpp -- TEST INFRASTRUCTURE ONLY.
+//
+// Compiles lindemeier/painty's own header-only hot-path code, unmodified, from the reference
+// checkout (include root passed by oracle/Makefile), against the repository's minimal Eigen
+// and OpenCV stand-ins in oracle/ref_shim/, and exposes it through a C API (prefix ref_) that
+// mirrors the oracle's (prefix orc_). Tests use it to pin the restated oracle bit for bit.
+// It exists only where the reference checkout exists; nothing on the product path uses it.
+//
+// What is the reference's code here: KubelkaMunk.hxx, Math.hxx (coth), Spline.hxx,
+// Color.hxx (CIEDE2000), image/Mat.hxx (Interpolate, PaddedMat), renderer/PaintLayer.hxx,
+// Canvas.hxx, FootprintBrush.hxx, Renderer.hxx. What is the harness's: the footprint
+// "image" source (painty::io::imRead below returns the registered full-size footprint),
+// and the stroke loop of FootprintBrush::paintStroke, re-driven here over the reference's
+// own CatmullRom/imprint because that loop reads path[SIZE_MAX] at i = 0
+// (FootprintBrush.hxx:252).
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "painty/core/Color.hxx"
+#include "painty/core/KubelkaMunk.hxx"
+#include "painty/core/Math.hxx"
+#include "painty/core/Spline.hxx"
+#include "painty/image/Mat.hxx"
+#include "painty/renderer/Canvas.hxx"
+#include "painty/renderer/FootprintBrush.hxx"
+#include "painty/renderer/PaintLayer.hxx"
+#include "painty/renderer/Renderer.hxx"
+
+using painty::vec2;
+using painty::vec3;
+
+namespace {
+painty::Mat<double> g_footprint_full;
+}
+
+namespace cv {
+void shim_resize_bilinear(const Mat_<double>& src, Mat_<double>& dst, int rows, int cols) {
+  Mat_<double> out(rows, cols);
+  const double sy = static_cast<double>(src.rows) / static_cast<double>(rows);
+  const double sx = static_cast<double>(src.cols) / static_cast<double>(cols);
+  for (int i = 0; i < rows; i++)
+    for (int j = 0; j < cols; j++) {
+      const vec2 pos = {(static_cast<double>(j) + 0.5) * sx - 0.5,
+                        (static_cast<double>(i) + 0.5) * sy - 0.5};
+      out(i, j) = painty::Interpolate(src, pos);
+    }
+  dst = out;
+}
+}  // namespace cv
+
+namespace painty {
+namespace io {
+void imRead(const std::string&, Mat<double>& gray, bool) { gray = g_footprint_full.clone(); }
+}  // namespace io
+}  // namespace painty
+
+struct ref_canvas {
+  painty::Canvas<vec3> c;
+  ref_canvas(int r, int cc) : c(r, cc) {}
+};
+struct ref_brush {
+  painty::FootprintBrush<vec3> b;
+  explicit ref_brush(double r) : b(r) {}
+};
+
+static vec3 v3(const double* p) { return vec3(p[0], p[1], p[2]); }
+
+extern "C" {
+
+double ref_coth(double x) { return painty::coth(x); }
+
+void ref_compute_reflectance(const double K[3], const double S[3], const double R0[3],
+                             double d, double out[3]) {
+  const vec3 r = painty::ComputeReflectance<double, 3>(v3(K), v3(S), v3(R0), d);
+  for (int i = 0; i < 3; i++) out[i] = r[i];
+}
+
+double ref_catmull_rom_1d(double p_1, double p0, double p1, double p2, double t) {
+  return painty::CatmullRom(p_1, p0, p1, p2, t);
+}
+
+void ref_spline_catmull_rom(const double* pts, int32_t n, double u, double out[2]) {
+  std::vector<vec2> v;
+  for (int i = 0; i < n; i++) v.emplace_back(pts[2 * i], pts[2 * i + 1]);
+  painty::SplineEval<std::vector<vec2>::const_iterator> s(v.cbegin(), v.cend());
+  const vec2 r = s.catmullRom(u);
+  out[0] = r[0];
+  out[1] = r[1];
+}
+
+double ref_interpolate(const double* img, int32_t rows, int32_t cols, double x, double y) {
+  painty::Mat<double> m(rows, cols);
+  for (int i = 0; i < rows * cols; i++) m(i) = img[i];
+  return painty::Interpolate(m, vec2(x, y));
+}
+
+void ref_rgb2lab(const double rgb[3], double lab[3]) {
+  painty::ColorConverter<double> conv;
+  vec3 out;
+  conv.rgb2lab(v3(rgb), out);
+  for (int i = 0; i < 3; i++) lab[i] = out[i];
+}
+
+double ref_ciede2000(const double a[3], const double b[3]) {
+  return painty::ColorConverter<double>::ColorDifferenceCIEDE2000(v3(a), v3(b));
+}
+
+ref_canvas* ref_canvas_create(int32_t rows, int32_t cols) { return new ref_canvas(rows, cols); }
+void ref_canvas_destroy(ref_canvas* c) { delete c; }
+
+// which: 0 K (npix*3), 1 S, 2 V (npix), 3 R0 (npix*3), 4 h (npix)
+void ref_canvas_get(ref_canvas* c, int32_t which, double* out) {
+  auto& L = c->c.getPaintLayer();
+  const int n = L.getRows() * L.getCols();
+  for (int i = 0; i < n; i++) {
+    switch (which) {
+      case 0: for (int ch = 0; ch < 3; ch++) out[i * 3 + ch] = L.getK_buffer()(i)[ch]; break;
+      case 1: for (int ch = 0; ch < 3; ch++) out[i * 3 + ch] = L.getS_buffer()(i)[ch]; break;
+      case 2: out[i] = L.getV_buffer()(i); break;
+      case 3: for (int ch = 0; ch < 3; ch++) out[i * 3 + ch] = c->c.getR0()(i)[ch]; break;
+      case 4: out[i] = c->c.get_h()(i); break;
+      default: break;
+    }
+  }
+}
+
+void ref_canvas_set(ref_canvas* c, int32_t which, const double* in) {
+  auto& L = c->c.getPaintLayer();
+  const int n = L.getRows() * L.getCols();
+  for (int i = 0; i < n; i++) {
+    switch (which) {
+      case 0: L.getK_buffer()(i) = v3(in + 3 * i); break;
+      case 1: L.getS_buffer()(i) = v3(in + 3 * i); break;
+      case 2: L.getV_buffer()(i) = in[i]; break;
+      case 3: c->c.getR0()(i) = v3(in + 3 * i); break;
+      case 4: c->c.get_h()(i) = in[i]; break;
+      default: break;
+    }
+  }
+}
+
+void ref_canvas_dry(ref_canvas* c) { c->c.dryCanvas(); }
+
+void ref_canvas_compose(ref_canvas* c, double* out) {
+  painty::Renderer<vec3> r;
+  const auto R = r.compose(c->c);
+  for (size_t i = 0; i < R.total(); i++)
+    for (int ch = 0; ch < 3; ch++) out[i * 3 + ch] = R(static_cast<int>(i))[ch];
+}
+
+ref_brush* ref_brush_create(double radius, const double* fp, int32_t fh, int32_t fw) {
+  g_footprint_full = painty::Mat<double>(fh, fw);
+  for (int i = 0; i < fh * fw; i++) g_footprint_full(i) = fp[i];
+  return new ref_brush(radius);
+}
+void ref_brush_destroy(ref_brush* b) { delete b; }
+void ref_brush_set_radius(ref_brush* b, double r) { b->b.setRadius(r); }
+void ref_brush_set_rates(ref_brush* b, double pickup, double deposit) {
+  b->b.setPickupRate(pickup);
+  b->b.setDepositionRate(deposit);
+}
+void ref_brush_set_snapshot(ref_brush* b, int32_t use) { b->b.setUseSnapshotBuffer(use != 0); }
+void ref_brush_dip(ref_brush* b, const double K[3], const double S[3]) {
+  b->b.dip({v3(K), v3(S)});
+}
+void ref_brush_update_snapshot(ref_brush* b, ref_canvas* c) { b->b.updateSnapshot(c->c); }
+void ref_brush_imprint(ref_brush* b, ref_canvas* c, double cx, double cy, double theta) {
+  b->b.imprint(vec2(cx, cy), theta, c->c);
+}
+void ref_brush_stamps(ref_brush* b, ref_canvas* c, const double* s, int64_t n) {
+  for (int64_t i = 0; i < n; i++) b->b.imprint(vec2(s[3 * i], s[3 * i + 1]), s[3 * i + 2], c->c);
+}
+
+// FootprintBrush.hxx:251-267 with painty's CatmullRom / CatmullRomDerivativeFirst and
+// imprint, path[0] for the predecessor of the first segment.
+int64_t ref_brush_paint_stroke(ref_brush* b, ref_canvas* c, const double* path, int32_t n) {
+  if (n < 2) return 0;
+  std::vector<vec2> p;
+  for (int i = 0; i < n; i++) p.emplace_back(path[2 * i], path[2 * i + 1]);
+  int64_t count = 0;
+  for (size_t i = 0; i + 1 < p.size(); i++) {
+    const auto p_pre = p[i == 0 ? 0 : i - 1];
+    const auto p_0 = p[i];
+    const auto p_1 = p[i + 1];
+    const auto p_next = p[std::min(i + 2, p.size() - 1)];
+    const auto dist = (p_1 - p_0).norm();
+    for (int32_t pd = 1; pd <= static_cast<int32_t>(dist); pd++) {
+      const auto t = static_cast<double>(pd) / dist;
+      const auto dir = painty::CatmullRomDerivativeFirst(p_pre, p_0, p_1, p_next, t);
+      b->b.imprint(painty::CatmullRom(p_pre, p_0, p_1, p_next, t), std::atan2(dir[1], dir[0]),
+                   c->c);
+      count++;
+    }
+  }
+  return count;
+}
+
+// F (footprint side) and S (pickup-map side)
+void ref_brush_info(ref_brush* b, int32_t* F, int32_t* S) {
+  *F = b->b.getFootprint().rows;
+  *S = b->b.getPickupMap().getRows();
+}
+void ref_brush_footprint(ref_brush* b, double* out) {
+  const auto& f = b->b.getFootprint();
+  for (size_t i = 0; i < f.total(); i++) out[i] = f(static_cast<int>(i));
+}
+// which: 0 K (S*S*3), 1 S, 2 V
+void ref_brush_pickup(ref_brush* b, int32_t which, double* out) {
+  const auto& L = b->b.getPickupMap();
+  const int n = L.getRows() * L.getCols();
+  for (int i = 0; i < n; i++) {
+    switch (which) {
+      case 0: for (int ch = 0; ch < 3; ch++) out[i * 3 + ch] = L.getK_buffer()(i)[ch]; break;
+      case 1: for (int ch = 0; ch < 3; ch++) out[i * 3 + ch] = L.getS_buffer()(i)[ch]; break;
+      case 2: out[i] = L.getV_buffer()(i); break;
+      default: break;
+    }
+  }
+}
+
+}  // extern "C"

@@ -1,0 +1,417 @@
+"""painty_gb300 -- GB300-native Kubelka-Munk paint path (Python host mirror of the C ABI).
+
+Mirrors lindemeier/painty's renderer classes over the C ABI in include/painty_gb300.h:
+
+    Canvas          painty/renderer/Canvas.hxx        (wet layer, substrate R0, height map)
+    PaintLayer      painty/renderer/PaintLayer.hxx    (K, S, V planes)
+    Image           Mat<vec3> reflectance on the device (R0 / composite output)
+    FootprintBrush  painty/renderer/FootprintBrush.hxx
+    Renderer        painty/renderer/Renderer.hxx      (compose)
+    mix_single_paint painty/mixer/src/PaintMixer.cxx:327-355
+
+Errors map to painty's exception types: invalid arguments raise ValueError (painty throws
+std::invalid_argument), CUDA failures raise RuntimeError, allocation failures MemoryError.
+
+The compiled library is required: importing this package without it raises ImportError.
+There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = _HERE / "_lib" / "libpainty_gb300.so"
+
+if not LIB_PATH.exists():
+    raise ImportError(
+        f"painty_gb300 native library not found at {LIB_PATH}; build it with "
+        "`python -m painty_gb300.build` (CUDA toolkit required; there is no CPU fallback)")
+
+_lib = C.CDLL(str(LIB_PATH))
+
+STORAGE = {"f32": 0, "f16": 1, "bf16": 2, "f64": 3}
+HOST_F64_INTERLEAVED, HOST_F32_INTERLEAVED, HOST_F64_PLANAR, HOST_F32_PLANAR = 0, 1, 2, 3
+PLANE = {"K": 0, "S": 1, "V": 2, "R0": 3, "h": 4}
+
+_P, _I32, _I64, _D = C.c_void_p, C.c_int32, C.c_int64, C.c_double
+
+
+def _sig(name, *args, res=C.c_int):
+    f = getattr(_lib, name)
+    f.argtypes = list(args)
+    f.restype = res
+    return f
+
+
+_sig("painty_abi_version", res=_I32)
+_sig("painty_status_string", C.c_int, res=C.c_char_p)
+_sig("painty_last_error", res=C.c_char_p)
+_sig("painty_kernel_launch_count", res=_I64)
+_sig("painty_layer_create", _I32, _I32, C.c_int, C.POINTER(_P))
+_sig("painty_layer_destroy", _P)
+_sig("painty_layer_clear", _P, _P)
+_sig("painty_layer_upload", _P, C.c_int, _P, C.c_int, _P)
+_sig("painty_layer_download", _P, C.c_int, _P, C.c_int, _P)
+_sig("painty_layer_copy", _P, _P, _P)
+_sig("painty_layer_info", _P, C.POINTER(_I32), C.POINTER(_I32), C.POINTER(C.c_int))
+_sig("painty_image_create", _I32, _I32, C.c_int, C.POINTER(_P))
+_sig("painty_image_destroy", _P)
+_sig("painty_image_fill", _P, _D, _D, _D, _P)
+_sig("painty_image_upload", _P, _P, C.c_int, _P)
+_sig("painty_image_download", _P, _P, C.c_int, _P)
+_sig("painty_compose_layers", _P, _I32, _P, _P, _P)
+_sig("painty_compose_layers_unfused", _P, _I32, _P, _P, _P)
+_sig("painty_canvas_create", _I32, _I32, C.c_int, C.POINTER(_P))
+_sig("painty_canvas_destroy", _P)
+_sig("painty_canvas_clear", _P, _P)
+_sig("painty_canvas_upload", _P, C.c_int, _P, C.c_int, _P)
+_sig("painty_canvas_download", _P, C.c_int, _P, C.c_int, _P)
+_sig("painty_canvas_layer", _P, C.POINTER(_P))
+_sig("painty_canvas_r0", _P, C.POINTER(_P))
+_sig("painty_canvas_info", _P, C.POINTER(_I32), C.POINTER(_I32), C.POINTER(C.c_int))
+_sig("painty_canvas_compose", _P, _P, _P)
+_sig("painty_canvas_dry", _P, _P)
+_sig("painty_brush_create", _D, _P, _I32, _I32, C.POINTER(_P))
+_sig("painty_brush_destroy", _P)
+_sig("painty_brush_set_radius", _P, _D)
+_sig("painty_brush_set_rates", _P, _D, _D)
+_sig("painty_brush_get_rates", _P, C.POINTER(_D), C.POINTER(_D))
+_sig("painty_brush_set_snapshot", _P, _I32)
+_sig("painty_brush_dip", _P, _P, _P, _P)
+_sig("painty_brush_update_snapshot", _P, _P, _P)
+_sig("painty_brush_info", _P, C.POINTER(_D), C.POINTER(_I32), C.POINTER(_I32))
+_sig("painty_brush_footprint", _P, _P)
+_sig("painty_brush_download_pickup", _P, C.c_int, _P, C.c_int, _P)
+_sig("painty_imprint", _P, _P, _D, _D, _D, _P)
+_sig("painty_stamps", _P, _P, _P, _I64, _P)
+_sig("painty_stroke", _P, _P, _P, _I32, _D, C.POINTER(_I64), _P)
+_sig("painty_mix_paint", _P, _I32, _P, _P, _P, _P)
+
+ABI_VERSION = _lib.painty_abi_version()
+
+
+class PaintyError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(msg)
+        self.status = status
+
+
+class PaintyValueError(PaintyError, ValueError):
+    pass
+
+
+def _check(status: int) -> None:
+    if status == 0:
+        return
+    msg = f"{_lib.painty_status_string(status).decode()}: {_lib.painty_last_error().decode()}"
+    if status == 1:
+        raise PaintyValueError(status, msg)
+    if status == 2:
+        raise MemoryError(msg)
+    raise PaintyError(status, msg)
+
+
+def kernel_launch_count() -> int:
+    """Kernel launches this library has issued in this process."""
+    return int(_lib.painty_kernel_launch_count())
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+def _stream(stream) -> int | None:
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return int(getattr(stream, "cuda_stream", stream))
+
+
+def _host_fmt(a: np.ndarray, planar: bool) -> int:
+    if a.dtype == np.float64:
+        return HOST_F64_PLANAR if planar else HOST_F64_INTERLEAVED
+    if a.dtype == np.float32:
+        return HOST_F32_PLANAR if planar else HOST_F32_INTERLEAVED
+    raise TypeError("host buffers are float32 or float64")
+
+
+def _shape3(rows, cols, planar):
+    return (3, rows, cols) if planar else (rows, cols, 3)
+
+
+class PaintLayer:
+    """painty::PaintLayer<vec3> on the device (PaintLayer.hxx:21-145)."""
+
+    def __init__(self, rows: int, cols: int, storage: str = "f32", *, _handle=None, _owner=None):
+        self.storage = storage
+        if _handle is not None:
+            self._h = _handle
+            self._owned = False
+            self._owner = _owner
+        else:
+            h = _P()
+            _check(_lib.painty_layer_create(rows, cols, STORAGE[storage], C.byref(h)))
+            self._h = h.value
+            self._owned = True
+        r, c, s = _I32(), _I32(), C.c_int()
+        _check(_lib.painty_layer_info(self._h, C.byref(r), C.byref(c), C.byref(s)))
+        self.rows, self.cols = r.value, c.value
+
+    def __del__(self):
+        if getattr(self, "_owned", False) and self._h:
+            _lib.painty_layer_destroy(self._h)
+            self._h = None
+
+    def getRows(self) -> int:
+        return self.rows
+
+    def getCols(self) -> int:
+        return self.cols
+
+    def clear(self, stream=None) -> None:
+        _check(_lib.painty_layer_clear(self._h, _stream(stream)))
+
+    def upload(self, plane: str, data: np.ndarray, planar: bool = False, stream=None) -> None:
+        data = np.ascontiguousarray(data)
+        _check(_lib.painty_layer_upload(self._h, PLANE[plane], _ptr(data),
+                                        _host_fmt(data, planar), _stream(stream)))
+
+    def download(self, plane: str, dtype=np.float64, planar: bool = False, stream=None):
+        shape = (self.rows, self.cols) if plane == "V" else _shape3(self.rows, self.cols, planar)
+        out = np.empty(shape, dtype=dtype)
+        _check(_lib.painty_layer_download(self._h, PLANE[plane], _ptr(out),
+                                          _host_fmt(out, planar), _stream(stream)))
+        return out
+
+    def set(self, K: np.ndarray, S: np.ndarray, V: np.ndarray, stream=None) -> None:
+        self.upload("K", K, stream=stream)
+        self.upload("S", S, stream=stream)
+        self.upload("V", V, stream=stream)
+
+    def getK_buffer(self):
+        return self.download("K")
+
+    def getS_buffer(self):
+        return self.download("S")
+
+    def getV_buffer(self):
+        return self.download("V")
+
+    def copyTo(self, other: "PaintLayer", stream=None) -> None:
+        _check(_lib.painty_layer_copy(self._h, other._h, _stream(stream)))
+
+    def composeOnto(self, R0: "Image", stream=None) -> None:
+        """PaintLayer::composeOnto (PaintLayer.hxx:81-96): R0 <- KM(K, S, R0, V) in place."""
+        compose_layers([self], R0, R0, stream=stream)
+
+
+class Image:
+    """A 3-channel reflectance image (painty Mat<vec3>) on the device; F32 or F64."""
+
+    def __init__(self, rows: int, cols: int, storage: str = "f32", *, _handle=None, _owner=None):
+        self.rows, self.cols, self.storage = rows, cols, storage
+        if _handle is not None:
+            self._h, self._owned, self._owner = _handle, False, _owner
+        else:
+            h = _P()
+            _check(_lib.painty_image_create(rows, cols, STORAGE[storage], C.byref(h)))
+            self._h, self._owned = h.value, True
+
+    def __del__(self):
+        if getattr(self, "_owned", False) and self._h:
+            _lib.painty_image_destroy(self._h)
+            self._h = None
+
+    def fill(self, r: float, g: float, b: float, stream=None) -> None:
+        _check(_lib.painty_image_fill(self._h, r, g, b, _stream(stream)))
+
+    def upload(self, data: np.ndarray, planar: bool = False, stream=None) -> None:
+        data = np.ascontiguousarray(data)
+        _check(_lib.painty_image_upload(self._h, _ptr(data), _host_fmt(data, planar),
+                                        _stream(stream)))
+
+    def download(self, dtype=np.float64, planar: bool = False, out=None, stream=None):
+        if out is None:
+            out = np.empty(_shape3(self.rows, self.cols, planar), dtype=dtype)
+        _check(_lib.painty_image_download(self._h, _ptr(out), _host_fmt(out, planar),
+                                          _stream(stream)))
+        return out
+
+
+def compose_layers(layers, r0: Image, out: Image, fused: bool = True, stream=None) -> None:
+    """out = KM(layer L-1, ... KM(layer 0, r0)) -- PaintLayer::composeOnto over a stack."""
+    arr = (_P * max(1, len(layers)))(*[l._h for l in layers])
+    fn = _lib.painty_compose_layers if fused else _lib.painty_compose_layers_unfused
+    _check(fn(arr, len(layers), r0._h, out._h, _stream(stream)))
+
+
+class Canvas:
+    """painty::Canvas<vec3> (Canvas.hxx:20-198) on the device."""
+
+    def __init__(self, rows: int, cols: int, storage: str = "f32"):
+        h = _P()
+        _check(_lib.painty_canvas_create(rows, cols, STORAGE[storage], C.byref(h)))
+        self._h = h.value
+        self.rows, self.cols, self.storage = rows, cols, storage
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            _lib.painty_canvas_destroy(self._h)
+            self._h = None
+
+    def clear(self, stream=None) -> None:
+        _check(_lib.painty_canvas_clear(self._h, _stream(stream)))
+
+    def upload(self, plane: str, data: np.ndarray, planar: bool = False, stream=None) -> None:
+        data = np.ascontiguousarray(data)
+        _check(_lib.painty_canvas_upload(self._h, PLANE[plane], _ptr(data),
+                                         _host_fmt(data, planar), _stream(stream)))
+
+    def download(self, plane: str, dtype=np.float64, planar: bool = False, stream=None):
+        one = plane in ("V", "h")
+        shape = (self.rows, self.cols) if one else _shape3(self.rows, self.cols, planar)
+        out = np.empty(shape, dtype=dtype)
+        _check(_lib.painty_canvas_download(self._h, PLANE[plane], _ptr(out),
+                                           _host_fmt(out, planar), _stream(stream)))
+        return out
+
+    def setBackground(self, background: np.ndarray) -> None:
+        """Canvas::setBackground (Canvas.hxx:80-87): clear, then R0 = background."""
+        self.clear()
+        self.upload("R0", background)
+
+    def getR0(self):
+        return self.download("R0")
+
+    def get_h(self):
+        return self.download("h")
+
+    def getPaintLayer(self) -> PaintLayer:
+        h = _P()
+        _check(_lib.painty_canvas_layer(self._h, C.byref(h)))
+        return PaintLayer(0, 0, self.storage, _handle=h.value, _owner=self)
+
+    def r0_image(self) -> Image:
+        h = _P()
+        _check(_lib.painty_canvas_r0(self._h, C.byref(h)))
+        return Image(self.rows, self.cols, "f64" if self.storage == "f64" else "f32",
+                     _handle=h.value, _owner=self)
+
+    def dryCanvas(self, stream=None) -> None:
+        _check(_lib.painty_canvas_dry(self._h, _stream(stream)))
+
+
+class Renderer:
+    """painty::Renderer<vec3>::compose (Renderer.hxx:26-53)."""
+
+    def compose(self, canvas: Canvas, out: Image | None = None, stream=None) -> Image:
+        if out is None:
+            out = Image(canvas.rows, canvas.cols, "f64" if canvas.storage == "f64" else "f32")
+        _check(_lib.painty_canvas_compose(canvas._h, out._h, _stream(stream)))
+        return out
+
+
+class FootprintBrush:
+    """painty::FootprintBrush<vec3> (FootprintBrush.hxx:22-502).
+
+    `footprint` is the full-size footprint image (values in [0, 1]) that stands in for
+    data/footprint/footprint.png.
+    """
+
+    def __init__(self, radius: float, footprint: np.ndarray):
+        fp = np.ascontiguousarray(footprint, dtype=np.float64)
+        h = _P()
+        _check(_lib.painty_brush_create(float(radius), _ptr(fp), fp.shape[0], fp.shape[1],
+                                        C.byref(h)))
+        self._h = h.value
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            _lib.painty_brush_destroy(self._h)
+            self._h = None
+
+    def setRadius(self, radius: float) -> None:
+        _check(_lib.painty_brush_set_radius(self._h, float(radius)))
+
+    def setPickupRate(self, rate: float) -> None:
+        _, dep = self.rates()
+        _check(_lib.painty_brush_set_rates(self._h, float(rate), dep))
+
+    def setDepositionRate(self, rate: float) -> None:
+        pick, _ = self.rates()
+        _check(_lib.painty_brush_set_rates(self._h, pick, float(rate)))
+
+    def rates(self):
+        p, d = _D(), _D()
+        _check(_lib.painty_brush_get_rates(self._h, C.byref(p), C.byref(d)))
+        return p.value, d.value
+
+    def getPickupRate(self) -> float:
+        return self.rates()[0]
+
+    def getDepositionRate(self) -> float:
+        return self.rates()[1]
+
+    def setUseSnapshotBuffer(self, use: bool) -> None:
+        _check(_lib.painty_brush_set_snapshot(self._h, 1 if use else 0))
+
+    def dip(self, paint) -> None:
+        K = np.ascontiguousarray(paint[0], dtype=np.float64)
+        S = np.ascontiguousarray(paint[1], dtype=np.float64)
+        _check(_lib.painty_brush_dip(self._h, _ptr(K), _ptr(S), None))
+
+    def updateSnapshot(self, canvas: Canvas, stream=None) -> None:
+        _check(_lib.painty_brush_update_snapshot(self._h, canvas._h, _stream(stream)))
+
+    def info(self):
+        r, F, S = _D(), _I32(), _I32()
+        _check(_lib.painty_brush_info(self._h, C.byref(r), C.byref(F), C.byref(S)))
+        return r.value, F.value, S.value
+
+    def getFootprint(self) -> np.ndarray:
+        _, F, _ = self.info()
+        out = np.empty((F, F), dtype=np.float64)
+        _check(_lib.painty_brush_footprint(self._h, _ptr(out)))
+        return out
+
+    def getPickupMap(self, plane: str, dtype=np.float64) -> np.ndarray:
+        _, _, S = self.info()
+        shape = (S, S) if plane == "V" else (S, S, 3)
+        out = np.empty(shape, dtype=dtype)
+        _check(_lib.painty_brush_download_pickup(self._h, PLANE[plane], _ptr(out),
+                                                 _host_fmt(out, False), None))
+        return out
+
+    def imprint(self, center, theta: float, canvas: Canvas, stream=None) -> None:
+        _check(_lib.painty_imprint(canvas._h, self._h, float(center[0]), float(center[1]),
+                                   float(theta), _stream(stream)))
+
+    def stamps(self, cx_cy_theta: np.ndarray, canvas: Canvas, stream=None) -> None:
+        s = np.ascontiguousarray(cx_cy_theta, dtype=np.float64).reshape(-1, 3)
+        _check(_lib.painty_stamps(canvas._h, self._h, _ptr(s), s.shape[0], _stream(stream)))
+
+    def paintStroke(self, path: np.ndarray, canvas: Canvas, spacing: float = 1.0,
+                    stream=None) -> int:
+        p = np.ascontiguousarray(path, dtype=np.float64).reshape(-1, 2)
+        n = _I64()
+        _check(_lib.painty_stroke(canvas._h, self._h, _ptr(p), p.shape[0], float(spacing),
+                                  C.byref(n), _stream(stream)))
+        return n.value
+
+
+def mix_single_paint(weights: np.ndarray, palette_K: np.ndarray, palette_S: np.ndarray):
+    """PaintMixer::mixSinglePaint (PaintMixer.cxx:327-355): (K, S) of the weighted mix."""
+    w = np.ascontiguousarray(weights, dtype=np.float64)
+    pk = np.ascontiguousarray(palette_K, dtype=np.float64)
+    ps = np.ascontiguousarray(palette_S, dtype=np.float64)
+    if pk.shape != (w.size, 3) or ps.shape != (w.size, 3):
+        raise ValueError("Palette size does not match underlying size.")
+    K = np.zeros(3)
+    S = np.zeros(3)
+    _check(_lib.painty_mix_paint(_ptr(w), w.size, _ptr(pk), _ptr(ps), _ptr(K), _ptr(S)))
+    return K, S

@@ -1,0 +1,77 @@
+"""Builds the painty_gb300 CUDA library in-tree for sm_103a.
+
+    python -m painty_gb300.build          # -> painty_gb300/_lib/libpainty_gb300.so
+
+One nvcc job per translation unit, run in parallel, then one link. No CPU fallback is built:
+the library is CUDA-only and every entry point launches its own kernels.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent
+CSRC = HERE / "csrc"
+OUT_DIR = HERE / "_lib"
+LIB = OUT_DIR / "libpainty_gb300.so"
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and Path(cand).exists():
+            return cand
+    raise RuntimeError("nvcc not found: the CUDA toolkit is required to build painty_gb300")
+
+
+def cuda_lib_dir() -> str:
+    return str(Path(nvcc()).resolve().parent.parent / "lib64")
+
+
+def sources() -> list[Path]:
+    return sorted(CSRC.glob("*.cu"))
+
+
+def _compile(src: Path, obj: Path) -> None:
+    cmd = [nvcc(), *ARCH, "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
+           "-Xcompiler", "-Wall", "--expt-relaxed-constexpr", "-I", str(ROOT / "include"),
+           "-I", str(CSRC), "-c", str(src), "-o", str(obj)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {src.name}:\n{r.stdout}\n{r.stderr}")
+
+
+def build(verbose: bool = False) -> Path:
+    OUT_DIR.mkdir(exist_ok=True)
+    objs = []
+    jobs = []
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(len(sources()), os.cpu_count() or 4))) as ex:
+        for src in sources():
+            obj = OUT_DIR / (src.stem + ".o")
+            objs.append(obj)
+            jobs.append(ex.submit(_compile, src, obj))
+        for j in jobs:
+            j.result()
+    libdir = cuda_lib_dir()
+    tmp = LIB.with_suffix(".so.tmp")
+    cmd = [nvcc(), *ARCH, "-shared", "-cudart", "shared", "-o", str(tmp), *map(str, objs),
+           "-Xlinker", f"-rpath={libdir}", "-L", libdir]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, LIB)
+    for o in objs:
+        o.unlink(missing_ok=True)
+    if verbose:
+        print(f"built {LIB}")
+    return LIB
+
+
+if __name__ == "__main__":
+    build(verbose=True)
+    sys.exit(0)

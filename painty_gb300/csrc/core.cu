@@ -1,0 +1,869 @@
+// core.cu -- library plumbing, layers / images / canvases, plane transfers, and the fused
+// multi-layer Kubelka-Munk composite and drying kernels.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "device_common.cuh"
+#include "internal.h"
+
+namespace pg {
+
+namespace {
+thread_local std::string g_last_error;
+std::atomic<int64_t> g_launches{0};
+std::atomic<uint64_t> g_canvas_ids{1};
+}  // namespace
+
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+void count_launch(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+[[noreturn]] void fail(painty_status s, const std::string& msg) { throw Error(s, msg); }
+
+void check_cuda(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return;
+  if (e == cudaErrorMemoryAllocation) {
+    cudaGetLastError();
+    fail(PAINTY_ERR_OUT_OF_MEMORY, std::string(what) + ": " + cudaGetErrorString(e));
+  }
+  fail(PAINTY_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+bool valid_storage(painty_storage s) {
+  return s == PAINTY_STORAGE_F32 || s == PAINTY_STORAGE_F16 || s == PAINTY_STORAGE_BF16 ||
+         s == PAINTY_STORAGE_F64;
+}
+size_t ks_bytes(painty_storage s) {
+  switch (s) {
+    case PAINTY_STORAGE_F16:
+    case PAINTY_STORAGE_BF16: return 2;
+    case PAINTY_STORAGE_F64: return 8;
+    default: return 4;
+  }
+}
+size_t v_bytes(painty_storage s) { return ks_bytes(s); }  // F16 and BF16 keep V in FP16
+DevType ks_type(painty_storage s) {
+  switch (s) {
+    case PAINTY_STORAGE_F16: return DT_F16;
+    case PAINTY_STORAGE_BF16: return DT_BF16;
+    case PAINTY_STORAGE_F64: return DT_F64;
+    default: return DT_F32;
+  }
+}
+DevType v_type(painty_storage s) {
+  switch (s) {
+    case PAINTY_STORAGE_F16:
+    case PAINTY_STORAGE_BF16: return DT_F16;
+    case PAINTY_STORAGE_F64: return DT_F64;
+    default: return DT_F32;
+  }
+}
+DevType r_type(painty_storage s) { return s == PAINTY_STORAGE_F64 ? DT_F64 : DT_F32; }
+
+static size_t dt_size(DevType t) { return t == DT_F64 ? 8 : (t == DT_F32 ? 4 : 2); }
+static size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+
+void* device_alloc(size_t bytes) {
+  void* p = nullptr;
+  if (bytes == 0) return nullptr;
+  PG_CUDA(cudaMalloc(&p, bytes));
+  return p;
+}
+void device_free(void* p) {
+  if (p) cudaFree(p);
+}
+
+size_t layer_bytes(int32_t rows, int32_t cols, painty_storage s) {
+  const size_t pe = static_cast<size_t>(rows) * pitch_for(cols);
+  return 6 * align256(pe * ks_bytes(s)) + align256(pe * v_bytes(s));
+}
+void layer_layout(painty_layer& L, int32_t rows, int32_t cols, painty_storage s, void* base) {
+  L.rows = rows;
+  L.cols = cols;
+  L.pitch = pitch_for(cols);
+  L.storage = s;
+  L.base = base;
+  L.bytes = layer_bytes(rows, cols, s);
+  const size_t ksb = align256(static_cast<size_t>(L.plane_elems()) * ks_bytes(s));
+  char* p = static_cast<char*>(base);
+  for (int c = 0; c < 3; c++) L.K[c] = p + c * ksb;
+  for (int c = 0; c < 3; c++) L.S[c] = p + (3 + c) * ksb;
+  L.V = p + 6 * ksb;
+}
+size_t image_bytes(int32_t rows, int32_t cols, painty_storage s) {
+  const size_t pe = static_cast<size_t>(rows) * pitch_for(cols);
+  return 3 * align256(pe * r_bytes(s));
+}
+void image_layout(painty_image& I, int32_t rows, int32_t cols, painty_storage s, void* base) {
+  I.rows = rows;
+  I.cols = cols;
+  I.pitch = pitch_for(cols);
+  I.storage = s;
+  I.base = base;
+  I.bytes = image_bytes(rows, cols, s);
+  const size_t rb = align256(static_cast<size_t>(I.plane_elems()) * r_bytes(s));
+  for (int c = 0; c < 3; c++) I.R[c] = static_cast<char*>(base) + c * rb;
+}
+
+// ------------------------------------------------------------------ transfer kernels
+namespace {
+
+struct PlanePtrs {
+  void* p[3];
+};
+
+template <class TD, class TS>
+__device__ __forceinline__ TD convert(TS v);
+template <> __device__ __forceinline__ float convert<float, float>(float v) { return v; }
+template <> __device__ __forceinline__ float convert<float, double>(double v) { return static_cast<float>(v); }
+template <> __device__ __forceinline__ double convert<double, double>(double v) { return v; }
+template <> __device__ __forceinline__ double convert<double, float>(float v) { return v; }
+template <> __device__ __forceinline__ __half convert<__half, float>(float v) { return __float2half_rn(v); }
+template <> __device__ __forceinline__ __half convert<__half, double>(double v) { return __double2half(v); }
+template <> __device__ __forceinline__ __nv_bfloat16 convert<__nv_bfloat16, float>(float v) { return __float2bfloat16_rn(v); }
+template <> __device__ __forceinline__ __nv_bfloat16 convert<__nv_bfloat16, double>(double v) { return __double2bfloat16(v); }
+template <> __device__ __forceinline__ float convert<float, __half>(__half v) { return __half2float(v); }
+template <> __device__ __forceinline__ double convert<double, __half>(__half v) { return __half2float(v); }
+template <> __device__ __forceinline__ float convert<float, __nv_bfloat16>(__nv_bfloat16 v) { return __bfloat162float(v); }
+template <> __device__ __forceinline__ double convert<double, __nv_bfloat16>(__nv_bfloat16 v) { return __bfloat162float(v); }
+
+// staging (host layout, contiguous) -> pitched planes
+template <class TD, class TS>
+__global__ void scatter_kernel(const TS* __restrict__ src, PlanePtrs dst, int nch,
+                               int interleaved, int32_t rows, int32_t cols, int64_t pitch) {
+  const int64_t n = static_cast<int64_t>(rows) * cols;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n * nch;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t p, c;
+    if (interleaved) {
+      p = i / nch;
+      c = i - p * nch;
+    } else {
+      c = i / n;
+      p = i - c * n;
+    }
+    const int64_t r = p / cols, col = p - r * cols;
+    static_cast<TD*>(dst.p[c])[r * pitch + col] = convert<TD, TS>(src[i]);
+  }
+}
+
+// pitched planes -> staging (host layout)
+template <class TD, class TS>
+__global__ void gather_kernel(PlanePtrs src, TD* __restrict__ dst, int nch, int interleaved,
+                              int32_t rows, int32_t cols, int64_t pitch) {
+  const int64_t n = static_cast<int64_t>(rows) * cols;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n * nch;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t p, c;
+    if (interleaved) {
+      p = i / nch;
+      c = i - p * nch;
+    } else {
+      c = i / n;
+      p = i - c * n;
+    }
+    const int64_t r = p / cols, col = p - r * cols;
+    dst[i] = convert<TD, TS>(static_cast<const TS*>(src.p[c])[r * pitch + col]);
+  }
+}
+
+template <class T>
+__global__ void fill_kernel(PlanePtrs dst, int nch, int64_t elems, double v0, double v1,
+                            double v2) {
+  const double v[3] = {v0, v1, v2};
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < elems * nch;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = i / elems;
+    static_cast<T*>(dst.p[c])[i - c * elems] = convert<T, double>(v[c]);
+  }
+}
+
+int grid_for(int64_t n, int block) {
+  const int64_t g = (n + block - 1) / block;
+  return static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(g, 152 * 32)));
+}
+
+bool host_is_f64(painty_host_format f) {
+  return f == PAINTY_HOST_F64_INTERLEAVED || f == PAINTY_HOST_F64_PLANAR;
+}
+bool host_is_interleaved(painty_host_format f) {
+  return f == PAINTY_HOST_F64_INTERLEAVED || f == PAINTY_HOST_F32_INTERLEAVED;
+}
+
+template <class TS>
+void launch_scatter(DevType dt, const TS* src, PlanePtrs dst, int nch, int il, int32_t rows,
+                    int32_t cols, int64_t pitch, cudaStream_t st) {
+  const int64_t n = static_cast<int64_t>(rows) * cols * nch;
+  const int g = grid_for(n, 256);
+  switch (dt) {
+    case DT_F32: scatter_kernel<float, TS><<<g, 256, 0, st>>>(src, dst, nch, il, rows, cols, pitch); break;
+    case DT_F16: scatter_kernel<__half, TS><<<g, 256, 0, st>>>(src, dst, nch, il, rows, cols, pitch); break;
+    case DT_BF16: scatter_kernel<__nv_bfloat16, TS><<<g, 256, 0, st>>>(src, dst, nch, il, rows, cols, pitch); break;
+    case DT_F64: scatter_kernel<double, TS><<<g, 256, 0, st>>>(src, dst, nch, il, rows, cols, pitch); break;
+  }
+  count_launch();
+  PG_CUDA(cudaGetLastError());
+}
+
+template <class TD>
+void launch_gather(DevType dt, PlanePtrs src, TD* dst, int nch, int il, int32_t rows,
+                   int32_t cols, int64_t pitch, cudaStream_t st) {
+  const int64_t n = static_cast<int64_t>(rows) * cols * nch;
+  const int g = grid_for(n, 256);
+  switch (dt) {
+    case DT_F32: gather_kernel<TD, float><<<g, 256, 0, st>>>(src, dst, nch, il, rows, cols, pitch); break;
+    case DT_F16: gather_kernel<TD, __half><<<g, 256, 0, st>>>(src, dst, nch, il, rows, cols, pitch); break;
+    case DT_BF16: gather_kernel<TD, __nv_bfloat16><<<g, 256, 0, st>>>(src, dst, nch, il, rows, cols, pitch); break;
+    case DT_F64: gather_kernel<TD, double><<<g, 256, 0, st>>>(src, dst, nch, il, rows, cols, pitch); break;
+  }
+  count_launch();
+  PG_CUDA(cudaGetLastError());
+}
+
+}  // namespace
+
+void upload_planes(void* const* planes, int nch, DevType dt, int32_t rows, int32_t cols,
+                   int64_t pitch, const void* host, painty_host_format fmt, cudaStream_t st) {
+  PG_REQUIRE(host != nullptr, "host buffer is null");
+  PG_REQUIRE(fmt >= PAINTY_HOST_F64_INTERLEAVED && fmt <= PAINTY_HOST_F32_PLANAR,
+             "unknown host format");
+  const bool f64 = host_is_f64(fmt);
+  const size_t hes = f64 ? 8 : 4;
+  const size_t n = static_cast<size_t>(rows) * cols;
+  // Fast path: planar host data of the device element type -> one 2D copy per plane.
+  if (!host_is_interleaved(fmt) || nch == 1) {
+    if ((dt == DT_F32 && !f64) || (dt == DT_F64 && f64)) {
+      for (int c = 0; c < nch; c++)
+        PG_CUDA(cudaMemcpy2DAsync(planes[c], pitch * hes,
+                                  static_cast<const char*>(host) + c * n * hes, cols * hes,
+                                  cols * hes, rows, cudaMemcpyHostToDevice, st));
+      PG_CUDA(cudaStreamSynchronize(st));
+      return;
+    }
+  }
+  void* staging = nullptr;
+  PG_CUDA(cudaMallocAsync(&staging, n * nch * hes, st));
+  PG_CUDA(cudaMemcpyAsync(staging, host, n * nch * hes, cudaMemcpyHostToDevice, st));
+  PlanePtrs pp{{planes[0], nch > 1 ? planes[1] : nullptr, nch > 2 ? planes[2] : nullptr}};
+  const int il = host_is_interleaved(fmt) ? 1 : 0;
+  if (f64)
+    launch_scatter<double>(dt, static_cast<const double*>(staging), pp, nch, il, rows, cols,
+                           pitch, st);
+  else
+    launch_scatter<float>(dt, static_cast<const float*>(staging), pp, nch, il, rows, cols,
+                          pitch, st);
+  PG_CUDA(cudaFreeAsync(staging, st));
+  PG_CUDA(cudaStreamSynchronize(st));
+}
+
+void download_planes(const void* const* planes, int nch, DevType dt, int32_t rows,
+                     int32_t cols, int64_t pitch, void* host, painty_host_format fmt,
+                     cudaStream_t st) {
+  PG_REQUIRE(host != nullptr, "host buffer is null");
+  PG_REQUIRE(fmt >= PAINTY_HOST_F64_INTERLEAVED && fmt <= PAINTY_HOST_F32_PLANAR,
+             "unknown host format");
+  const bool f64 = host_is_f64(fmt);
+  const size_t hes = f64 ? 8 : 4;
+  const size_t n = static_cast<size_t>(rows) * cols;
+  if (!host_is_interleaved(fmt) || nch == 1) {
+    if ((dt == DT_F32 && !f64) || (dt == DT_F64 && f64)) {
+      for (int c = 0; c < nch; c++)
+        PG_CUDA(cudaMemcpy2DAsync(static_cast<char*>(host) + c * n * hes, cols * hes,
+                                  planes[c], pitch * hes, cols * hes, rows,
+                                  cudaMemcpyDeviceToHost, st));
+      PG_CUDA(cudaStreamSynchronize(st));
+      return;
+    }
+  }
+  void* staging = nullptr;
+  PG_CUDA(cudaMallocAsync(&staging, n * nch * hes, st));
+  PlanePtrs pp{{const_cast<void*>(planes[0]), nch > 1 ? const_cast<void*>(planes[1]) : nullptr,
+                nch > 2 ? const_cast<void*>(planes[2]) : nullptr}};
+  const int il = host_is_interleaved(fmt) ? 1 : 0;
+  if (f64)
+    launch_gather<double>(dt, pp, static_cast<double*>(staging), nch, il, rows, cols, pitch, st);
+  else
+    launch_gather<float>(dt, pp, static_cast<float*>(staging), nch, il, rows, cols, pitch, st);
+  PG_CUDA(cudaMemcpyAsync(host, staging, n * nch * hes, cudaMemcpyDeviceToHost, st));
+  PG_CUDA(cudaFreeAsync(staging, st));
+  PG_CUDA(cudaStreamSynchronize(st));
+}
+
+void fill_planes(void* const* planes, int nch, DevType dt, int64_t elems, const double* v,
+                 cudaStream_t st) {
+  PlanePtrs pp{{planes[0], nch > 1 ? planes[1] : nullptr, nch > 2 ? planes[2] : nullptr}};
+  const int g = grid_for(elems * nch, 256);
+  const double v0 = v[0], v1 = nch > 1 ? v[1] : 0.0, v2 = nch > 2 ? v[2] : 0.0;
+  switch (dt) {
+    case DT_F32: fill_kernel<float><<<g, 256, 0, st>>>(pp, nch, elems, v0, v1, v2); break;
+    case DT_F16: fill_kernel<__half><<<g, 256, 0, st>>>(pp, nch, elems, v0, v1, v2); break;
+    case DT_BF16: fill_kernel<__nv_bfloat16><<<g, 256, 0, st>>>(pp, nch, elems, v0, v1, v2); break;
+    case DT_F64: fill_kernel<double><<<g, 256, 0, st>>>(pp, nch, elems, v0, v1, v2); break;
+  }
+  count_launch();
+  PG_CUDA(cudaGetLastError());
+}
+
+void copy_planes_async(void* const* dst, const void* const* src, int nch, size_t plane_bytes,
+                       cudaStream_t st) {
+  for (int c = 0; c < nch; c++)
+    PG_CUDA(cudaMemcpyAsync(dst[c], src[c], plane_bytes, cudaMemcpyDeviceToDevice, st));
+}
+
+// ------------------------------------------------------------------ composite kernel
+namespace {
+
+constexpr int kMaxLayersPerLaunch = 16;
+
+template <class TK, class TV, class TR>
+struct ComposeArgs {
+  const TK* K[kMaxLayersPerLaunch][3];
+  const TK* S[kMaxLayersPerLaunch][3];
+  const TV* V[kMaxLayersPerLaunch];
+  const TR* r0[3];
+  TR* out[3];
+  int32_t L;
+  int64_t groups;  // plane elements / 8
+};
+
+// One thread owns 8 consecutive plane elements (pixels): 128-bit streaming loads of each
+// layer's 7 planes, the KM recurrence R <- KM(K_l, S_l, R, V_l) through all L layers in
+// registers, one store of R. Per pixel this reads 7 L + 3 planes and writes 3 exactly once.
+template <class TK, class TV, class TR>
+__global__ void __launch_bounds__(256) km_composite_kernel(
+  const __grid_constant__ ComposeArgs<TK, TV, TR> a) {
+  using M = typename MathOf<TR>::type;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t g = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; g < a.groups;
+       g += stride) {
+    const int64_t e = g * 8;
+    M r[3][8];
+#pragma unroll
+    for (int c = 0; c < 3; c++) load8(a.r0[c] + e, r[c]);
+    for (int l = 0; l < a.L; l++) {
+      M v[8];
+      load8(a.V[l] + e, v);
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        M k[8], s[8];
+        load8(a.K[l][c] + e, k);
+        load8(a.S[l][c] + e, s);
+#pragma unroll
+        for (int i = 0; i < 8; i++) r[c][i] = km_reflectance(k[i], s[i], r[c][i], v[i]);
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; c++) store8(a.out[c] + e, r[c]);
+  }
+}
+
+template <class TK, class TV, class TR>
+void compose_typed(const painty_layer* const* layers, int32_t L, const painty_image* r0,
+                   painty_image* out, cudaStream_t st) {
+  const int64_t elems = r0->plane_elems();
+  int dev = 0, sms = 0;
+  PG_CUDA(cudaGetDevice(&dev));
+  PG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  for (int32_t l0 = 0; l0 < L || (L == 0 && l0 == 0); l0 += kMaxLayersPerLaunch) {
+    ComposeArgs<TK, TV, TR> a{};
+    const int32_t n = std::min<int32_t>(kMaxLayersPerLaunch, L - l0);
+    for (int32_t i = 0; i < n; i++) {
+      const painty_layer* ly = layers[l0 + i];
+      for (int c = 0; c < 3; c++) {
+        a.K[i][c] = static_cast<const TK*>(ly->K[c]);
+        a.S[i][c] = static_cast<const TK*>(ly->S[c]);
+      }
+      a.V[i] = static_cast<const TV*>(ly->V);
+    }
+    const painty_image* src = l0 == 0 ? r0 : out;
+    for (int c = 0; c < 3; c++) {
+      a.r0[c] = static_cast<const TR*>(src->R[c]);
+      a.out[c] = static_cast<TR*>(out->R[c]);
+    }
+    a.L = std::max<int32_t>(n, 0);
+    a.groups = elems / 8;
+    const int64_t blocks_needed = (a.groups + 255) / 256;
+    const int grid = static_cast<int>(std::min<int64_t>(blocks_needed, int64_t(sms) * 8));
+    km_composite_kernel<TK, TV, TR><<<std::max(grid, 1), 256, 0, st>>>(a);
+    count_launch();
+    PG_CUDA(cudaGetLastError());
+    if (L == 0) break;
+  }
+}
+
+}  // namespace
+
+void launch_compose(const painty_layer* const* layers, int32_t L, const painty_image* r0,
+                    painty_image* out, cudaStream_t st) {
+  PG_REQUIRE(r0 && out, "null image");
+  PG_REQUIRE(L >= 0, "negative layer count");
+  PG_REQUIRE(r0->rows == out->rows && r0->cols == out->cols, "image sizes differ");
+  PG_REQUIRE(r0->storage == out->storage, "image storages differ");
+  const painty_storage s = L > 0 ? layers[0]->storage : PAINTY_STORAGE_F32;
+  for (int32_t l = 0; l < L; l++) {
+    PG_REQUIRE(layers[l] != nullptr, "null layer");
+    PG_REQUIRE(layers[l]->rows == r0->rows && layers[l]->cols == r0->cols,
+               "layer size differs from the substrate (painty reallocates R0 here; pass an "
+               "image of the layer's size)");
+    PG_REQUIRE(layers[l]->storage == s, "layers have different storage formats");
+  }
+  if (L == 0) {
+    if (out != r0) {
+      const void* src[3] = {r0->R[0], r0->R[1], r0->R[2]};
+      copy_planes_async(out->R, src, 3, r0->plane_elems() * r_bytes(r0->storage), st);
+    }
+    return;
+  }
+  if (s == PAINTY_STORAGE_F64) {
+    PG_REQUIRE(r0->storage == PAINTY_STORAGE_F64, "F64 layers compose onto an F64 image");
+    compose_typed<double, double, double>(layers, L, r0, out, st);
+    return;
+  }
+  PG_REQUIRE(r0->storage == PAINTY_STORAGE_F32, "F32/F16/BF16 layers compose onto an F32 image");
+  switch (s) {
+    case PAINTY_STORAGE_F32: compose_typed<float, float, float>(layers, L, r0, out, st); break;
+    case PAINTY_STORAGE_F16: compose_typed<__half, __half, float>(layers, L, r0, out, st); break;
+    case PAINTY_STORAGE_BF16:
+      compose_typed<__nv_bfloat16, __half, float>(layers, L, r0, out, st);
+      break;
+    default: fail(PAINTY_ERR_INVALID_ARGUMENT, "bad storage");
+  }
+}
+
+// ------------------------------------------------------------------ drying kernel
+namespace {
+// Canvas::dryCanvas (painty/renderer/Canvas.hxx:105-121): h += V; R0 = KM(K, S, R0, V);
+// K = S = V = 0. One pass over the wet layer, R0 and h.
+struct PtrTriple {
+  void* p[3];
+};
+
+template <class TK, class TV, class TR>
+__global__ void __launch_bounds__(256) km_dry_kernel(PtrTriple wk, PtrTriple ws, TV* v, TV* h,
+                                                       PtrTriple r0, int64_t elems) {
+  using M = typename MathOf<TR>::type;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < elems;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const M vol = ld_elem<M>(v + i);
+    st_elem<M>(h + i, ld_elem<M>(h + i) + vol);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      TK* kp = static_cast<TK*>(wk.p[c]);
+      TK* sp = static_cast<TK*>(ws.p[c]);
+      TR* rp = static_cast<TR*>(r0.p[c]);
+      const M r = km_reflectance(ld_elem<M>(kp + i), ld_elem<M>(sp + i), ld_elem<M>(rp + i), vol);
+      st_elem<M>(rp + i, r);
+      st_elem<M>(kp + i, M(0));
+      st_elem<M>(sp + i, M(0));
+    }
+    st_elem<M>(v + i, M(0));
+  }
+}
+
+template <class TK, class TV, class TR>
+void dry_typed(painty_canvas* c, cudaStream_t st) {
+  const int64_t elems = c->wet.plane_elems();
+  PtrTriple wk{{c->wet.K[0], c->wet.K[1], c->wet.K[2]}};
+  PtrTriple ws{{c->wet.S[0], c->wet.S[1], c->wet.S[2]}};
+  PtrTriple r0{{c->r0.R[0], c->r0.R[1], c->r0.R[2]}};
+  const int g = grid_for(elems, 256);
+  km_dry_kernel<TK, TV, TR><<<g, 256, 0, st>>>(wk, ws, static_cast<TV*>(c->wet.V),
+                                                 static_cast<TV*>(c->h), r0, elems);
+  count_launch();
+  PG_CUDA(cudaGetLastError());
+}
+}  // namespace
+
+}  // namespace pg
+
+// ====================================================================== C ABI
+using pg::guard;
+
+extern "C" {
+
+int32_t painty_abi_version(void) { return PAINTY_GB300_ABI_VERSION; }
+
+const char* painty_status_string(painty_status s) {
+  switch (s) {
+    case PAINTY_OK: return "ok";
+    case PAINTY_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case PAINTY_ERR_OUT_OF_MEMORY: return "out of memory";
+    case PAINTY_ERR_CUDA: return "CUDA error";
+    case PAINTY_ERR_UNSUPPORTED: return "unsupported";
+    case PAINTY_ERR_BUDGET: return "over memory budget";
+    case PAINTY_ERR_TIMEOUT: return "device wait timed out";
+    case PAINTY_ERR_CANCELLED: return "cancelled";
+    case PAINTY_ERR_STATE: return "invalid state";
+  }
+  return "unknown status";
+}
+
+const char* painty_last_error(void) { return pg::g_last_error.c_str(); }
+
+int64_t painty_kernel_launch_count(void) { return pg::g_launches.load(); }
+
+// ---------------------------------------------------------------- layers
+painty_status painty_layer_create(int32_t rows, int32_t cols, painty_storage storage,
+                                  painty_layer** out) {
+  return guard([&] {
+    PG_REQUIRE(out != nullptr, "out is null");
+    PG_REQUIRE(rows > 0 && cols > 0, "rows and cols must be positive");
+    PG_REQUIRE(pg::valid_storage(storage), "unknown storage format");
+    auto* L = new painty_layer();
+    try {
+      void* base = pg::device_alloc(pg::layer_bytes(rows, cols, storage));
+      pg::layer_layout(*L, rows, cols, storage, base);
+      PG_CUDA(cudaMemset(base, 0, L->bytes));
+    } catch (...) {
+      if (L->base) pg::device_free(L->base);
+      delete L;
+      throw;
+    }
+    *out = L;
+  });
+}
+
+painty_status painty_layer_destroy(painty_layer* layer) {
+  return guard([&] {
+    if (!layer) return;
+    PG_REQUIRE(layer->owned, "borrowed layer handles are not destroyed");
+    pg::device_free(layer->base);
+    delete layer;
+  });
+}
+
+painty_status painty_layer_clear(painty_layer* layer, void* stream) {
+  return guard([&] {
+    PG_REQUIRE(layer != nullptr, "layer is null");
+    PG_CUDA(cudaMemsetAsync(layer->base, 0, layer->bytes, pg::as_stream(stream)));
+  });
+}
+
+static void layer_plane_ptrs(const painty_layer* L, painty_plane plane, void** p, int* nch,
+                             pg::DevType* dt) {
+  switch (plane) {
+    case PAINTY_PLANE_K:
+      for (int c = 0; c < 3; c++) p[c] = L->K[c];
+      *nch = 3;
+      *dt = pg::ks_type(L->storage);
+      return;
+    case PAINTY_PLANE_S:
+      for (int c = 0; c < 3; c++) p[c] = L->S[c];
+      *nch = 3;
+      *dt = pg::ks_type(L->storage);
+      return;
+    case PAINTY_PLANE_V:
+      p[0] = L->V;
+      *nch = 1;
+      *dt = pg::v_type(L->storage);
+      return;
+    default: pg::fail(PAINTY_ERR_INVALID_ARGUMENT, "a layer has planes K, S and V");
+  }
+}
+
+painty_status painty_layer_upload(painty_layer* layer, painty_plane plane, const void* host,
+                                  painty_host_format fmt, void* stream) {
+  return guard([&] {
+    PG_REQUIRE(layer != nullptr, "layer is null");
+    void* p[3] = {nullptr, nullptr, nullptr};
+    int nch = 0;
+    pg::DevType dt;
+    layer_plane_ptrs(layer, plane, p, &nch, &dt);
+    pg::upload_planes(p, nch, dt, layer->rows, layer->cols, layer->pitch, host, fmt,
+                      pg::as_stream(stream));
+  });
+}
+
+painty_status painty_layer_download(const painty_layer* layer, painty_plane plane, void* host,
+                                    painty_host_format fmt, void* stream) {
+  return guard([&] {
+    PG_REQUIRE(layer != nullptr, "layer is null");
+    void* p[3] = {nullptr, nullptr, nullptr};
+    int nch = 0;
+    pg::DevType dt;
+    layer_plane_ptrs(layer, plane, p, &nch, &dt);
+    const void* cp[3] = {p[0], p[1], p[2]};
+    pg::download_planes(cp, nch, dt, layer->rows, layer->cols, layer->pitch, host, fmt,
+                        pg::as_stream(stream));
+  });
+}
+
+painty_status painty_layer_copy(const painty_layer* src, painty_layer* dst, void* stream) {
+  return guard([&] {
+    PG_REQUIRE(src && dst, "layer is null");
+    PG_REQUIRE(src->rows == dst->rows && src->cols == dst->cols && src->storage == dst->storage,
+               "layers differ in size or storage");
+    PG_CUDA(cudaMemcpyAsync(dst->base, src->base, src->bytes, cudaMemcpyDeviceToDevice,
+                            pg::as_stream(stream)));
+  });
+}
+
+painty_status painty_layer_info(const painty_layer* layer, int32_t* rows, int32_t* cols,
+                                painty_storage* storage) {
+  return guard([&] {
+    PG_REQUIRE(layer != nullptr, "layer is null");
+    if (rows) *rows = layer->rows;
+    if (cols) *cols = layer->cols;
+    if (storage) *storage = layer->storage;
+  });
+}
+
+// ---------------------------------------------------------------- images
+painty_status painty_image_create(int32_t rows, int32_t cols, painty_storage storage,
+                                  painty_image** out) {
+  return guard([&] {
+    PG_REQUIRE(out != nullptr, "out is null");
+    PG_REQUIRE(rows > 0 && cols > 0, "rows and cols must be positive");
+    PG_REQUIRE(storage == PAINTY_STORAGE_F32 || storage == PAINTY_STORAGE_F64,
+               "images are F32 or F64");
+    auto* I = new painty_image();
+    try {
+      void* base = pg::device_alloc(pg::image_bytes(rows, cols, storage));
+      pg::image_layout(*I, rows, cols, storage, base);
+      PG_CUDA(cudaMemset(base, 0, I->bytes));
+    } catch (...) {
+      if (I->base) pg::device_free(I->base);
+      delete I;
+      throw;
+    }
+    *out = I;
+  });
+}
+
+painty_status painty_image_destroy(painty_image* img) {
+  return guard([&] {
+    if (!img) return;
+    PG_REQUIRE(img->owned, "borrowed image handles are not destroyed");
+    pg::device_free(img->base);
+    delete img;
+  });
+}
+
+painty_status painty_image_fill(painty_image* img, double r, double g, double b, void* stream) {
+  return guard([&] {
+    PG_REQUIRE(img != nullptr, "image is null");
+    const double v[3] = {r, g, b};
+    pg::fill_planes(img->R, 3, pg::r_type(img->storage), img->plane_elems(), v,
+                    pg::as_stream(stream));
+  });
+}
+
+painty_status painty_image_upload(painty_image* img, const void* host, painty_host_format fmt,
+                                  void* stream) {
+  return guard([&] {
+    PG_REQUIRE(img != nullptr, "image is null");
+    pg::upload_planes(img->R, 3, pg::r_type(img->storage), img->rows, img->cols, img->pitch,
+                      host, fmt, pg::as_stream(stream));
+  });
+}
+
+painty_status painty_image_download(const painty_image* img, void* host, painty_host_format fmt,
+                                    void* stream) {
+  return guard([&] {
+    PG_REQUIRE(img != nullptr, "image is null");
+    const void* p[3] = {img->R[0], img->R[1], img->R[2]};
+    pg::download_planes(p, 3, pg::r_type(img->storage), img->rows, img->cols, img->pitch, host,
+                        fmt, pg::as_stream(stream));
+  });
+}
+
+// ---------------------------------------------------------------- composite
+painty_status painty_compose_layers(const painty_layer* const* layers, int32_t L,
+                                    const painty_image* r0, painty_image* out, void* stream) {
+  return guard([&] {
+    PG_REQUIRE(L == 0 || layers != nullptr, "layers is null");
+    pg::launch_compose(layers, L, r0, out, pg::as_stream(stream));
+  });
+}
+
+painty_status painty_compose_layers_unfused(const painty_layer* const* layers, int32_t L,
+                                            const painty_image* r0, painty_image* out,
+                                            void* stream) {
+  return guard([&] {
+    PG_REQUIRE(L == 0 || layers != nullptr, "layers is null");
+    if (L == 0) {
+      pg::launch_compose(layers, 0, r0, out, pg::as_stream(stream));
+      return;
+    }
+    pg::launch_compose(layers, 1, r0, out, pg::as_stream(stream));
+    for (int32_t l = 1; l < L; l++) pg::launch_compose(layers + l, 1, out, out, pg::as_stream(stream));
+  });
+}
+
+// ---------------------------------------------------------------- canvas
+painty_status painty_canvas_create(int32_t rows, int32_t cols, painty_storage storage,
+                                   painty_canvas** out) {
+  return guard([&] {
+    PG_REQUIRE(out != nullptr, "out is null");
+    PG_REQUIRE(rows > 0 && cols > 0, "rows and cols must be positive");
+    PG_REQUIRE(pg::valid_storage(storage), "unknown storage format");
+    auto* c = new painty_canvas();
+    const painty_storage rs = storage == PAINTY_STORAGE_F64 ? PAINTY_STORAGE_F64 : PAINTY_STORAGE_F32;
+    const size_t lb = pg::layer_bytes(rows, cols, storage);
+    const size_t ib = pg::image_bytes(rows, cols, rs);
+    const size_t hb = static_cast<size_t>(rows) * pg::pitch_for(cols) * pg::v_bytes(storage);
+    try {
+      c->bytes = lb + ib + (hb + 255) / 256 * 256;
+      c->base = pg::device_alloc(c->bytes);
+      pg::layer_layout(c->wet, rows, cols, storage, c->base);
+      c->wet.owned = false;
+      pg::image_layout(c->r0, rows, cols, rs, static_cast<char*>(c->base) + lb);
+      c->r0.owned = false;
+      c->h = static_cast<char*>(c->base) + lb + ib;
+      c->id = pg::g_canvas_ids.fetch_add(1);
+      PG_CUDA(cudaMemset(c->base, 0, c->bytes));
+      const double one[3] = {1.0, 1.0, 1.0};  // Canvas.hxx:33 background
+      pg::fill_planes(c->r0.R, 3, pg::r_type(rs), c->r0.plane_elems(), one, nullptr);
+      PG_CUDA(cudaStreamSynchronize(nullptr));
+    } catch (...) {
+      if (c->base) pg::device_free(c->base);
+      delete c;
+      throw;
+    }
+    *out = c;
+  });
+}
+
+painty_status painty_canvas_destroy(painty_canvas* c) {
+  return guard([&] {
+    if (!c) return;
+    pg::device_free(c->base);
+    delete c;
+  });
+}
+
+painty_status painty_canvas_clear(painty_canvas* c, void* stream) {
+  return guard([&] {
+    PG_REQUIRE(c != nullptr, "canvas is null");
+    const cudaStream_t st = pg::as_stream(stream);
+    PG_CUDA(cudaMemsetAsync(c->wet.base, 0, c->wet.bytes, st));
+    const size_t hb = static_cast<size_t>(c->wet.plane_elems()) * pg::v_bytes(c->wet.storage);
+    PG_CUDA(cudaMemsetAsync(c->h, 0, hb, st));
+    const double one[3] = {1.0, 1.0, 1.0};
+    pg::fill_planes(c->r0.R, 3, pg::r_type(c->r0.storage), c->r0.plane_elems(), one, st);
+    c->version++;
+  });
+}
+
+painty_status painty_canvas_upload(painty_canvas* c, painty_plane plane, const void* host,
+                                   painty_host_format fmt, void* stream) {
+  return guard([&] {
+    PG_REQUIRE(c != nullptr, "canvas is null");
+    const cudaStream_t st = pg::as_stream(stream);
+    c->version++;
+    if (plane == PAINTY_PLANE_R0) {
+      pg::upload_planes(c->r0.R, 3, pg::r_type(c->r0.storage), c->wet.rows, c->wet.cols,
+                        c->wet.pitch, host, fmt, st);
+    } else if (plane == PAINTY_PLANE_H) {
+      void* p[1] = {c->h};
+      pg::upload_planes(p, 1, pg::v_type(c->wet.storage), c->wet.rows, c->wet.cols,
+                        c->wet.pitch, host, fmt, st);
+    } else {
+      void* p[3] = {nullptr, nullptr, nullptr};
+      int nch = 0;
+      pg::DevType dt;
+      layer_plane_ptrs(&c->wet, plane, p, &nch, &dt);
+      pg::upload_planes(p, nch, dt, c->wet.rows, c->wet.cols, c->wet.pitch, host, fmt, st);
+    }
+  });
+}
+
+painty_status painty_canvas_download(const painty_canvas* c, painty_plane plane, void* host,
+                                     painty_host_format fmt, void* stream) {
+  return guard([&] {
+    PG_REQUIRE(c != nullptr, "canvas is null");
+    const cudaStream_t st = pg::as_stream(stream);
+    if (plane == PAINTY_PLANE_R0) {
+      const void* p[3] = {c->r0.R[0], c->r0.R[1], c->r0.R[2]};
+      pg::download_planes(p, 3, pg::r_type(c->r0.storage), c->wet.rows, c->wet.cols,
+                          c->wet.pitch, host, fmt, st);
+    } else if (plane == PAINTY_PLANE_H) {
+      const void* p[1] = {c->h};
+      pg::download_planes(p, 1, pg::v_type(c->wet.storage), c->wet.rows, c->wet.cols,
+                          c->wet.pitch, host, fmt, st);
+    } else {
+      void* p[3] = {nullptr, nullptr, nullptr};
+      int nch = 0;
+      pg::DevType dt;
+      layer_plane_ptrs(&c->wet, plane, p, &nch, &dt);
+      const void* cp[3] = {p[0], p[1], p[2]};
+      pg::download_planes(cp, nch, dt, c->wet.rows, c->wet.cols, c->wet.pitch, host, fmt, st);
+    }
+  });
+}
+
+painty_status painty_canvas_layer(painty_canvas* c, painty_layer** out) {
+  return guard([&] {
+    PG_REQUIRE(c && out, "null argument");
+    *out = &c->wet;
+  });
+}
+
+painty_status painty_canvas_r0(painty_canvas* c, painty_image** out) {
+  return guard([&] {
+    PG_REQUIRE(c && out, "null argument");
+    *out = &c->r0;
+  });
+}
+
+painty_status painty_canvas_info(const painty_canvas* c, int32_t* rows, int32_t* cols,
+                                 painty_storage* storage) {
+  return guard([&] {
+    PG_REQUIRE(c != nullptr, "canvas is null");
+    if (rows) *rows = c->wet.rows;
+    if (cols) *cols = c->wet.cols;
+    if (storage) *storage = c->wet.storage;
+  });
+}
+
+painty_status painty_canvas_compose(const painty_canvas* c, painty_image* out, void* stream) {
+  return guard([&] {
+    PG_REQUIRE(c != nullptr, "canvas is null");
+    const painty_layer* L[1] = {&c->wet};
+    pg::launch_compose(L, 1, &c->r0, out, pg::as_stream(stream));
+  });
+}
+
+painty_status painty_canvas_dry(painty_canvas* c, void* stream) {
+  return guard([&] {
+    PG_REQUIRE(c != nullptr, "canvas is null");
+    const cudaStream_t st = pg::as_stream(stream);
+    c->version++;
+    switch (c->wet.storage) {
+      case PAINTY_STORAGE_F32: pg::dry_typed<float, float, float>(c, st); break;
+      case PAINTY_STORAGE_F16: pg::dry_typed<__half, __half, float>(c, st); break;
+      case PAINTY_STORAGE_BF16: pg::dry_typed<__nv_bfloat16, __half, float>(c, st); break;
+      case PAINTY_STORAGE_F64: pg::dry_typed<double, double, double>(c, st); break;
+    }
+  });
+}
+
+// ---------------------------------------------------------------- mixing
+painty_status painty_mix_paint(const double* w, int32_t n, const double* palK,
+                               const double* palS, double K[3], double S[3]) {
+  return guard([&] {
+    PG_REQUIRE(w && palK && palS && K && S, "null argument");
+    PG_REQUIRE(n > 0, "palette size must be positive");
+    // PaintMixer.cxx:327-355: normalise when |sum w - 1| >= 10e-6, then K,S = sum w_i K_i,S_i
+    double norm = 1.0, wsum = 0.0;
+    for (int i = 0; i < n; i++) wsum += w[i];
+    if (!(std::fabs(wsum - 1.0) < 10e-6)) norm = 1. / wsum;
+    for (int i = 0; i < 3; i++) {
+      K[i] = 0.0;
+      S[i] = 0.0;
+    }
+    for (int l = 0; l < n; l++)
+      for (int i = 0; i < 3; i++) {
+        K[i] += norm * w[l] * palK[l * 3 + i];
+        S[i] += norm * w[l] * palS[l * 3 + i];
+      }
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,181 @@
+// device_common.cuh -- element types, vector loads/stores and the Kubelka-Munk math.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace pg {
+
+// ------------------------------------------------------------------ element conversion
+__device__ __forceinline__ float to_f(float x) { return x; }
+__device__ __forceinline__ float to_f(__half x) { return __half2float(x); }
+__device__ __forceinline__ float to_f(__nv_bfloat16 x) { return __bfloat162float(x); }
+__device__ __forceinline__ double to_d(double x) { return x; }
+
+template <class T>
+__device__ __forceinline__ T from_f(float x);
+template <>
+__device__ __forceinline__ float from_f<float>(float x) { return x; }
+template <>
+__device__ __forceinline__ __half from_f<__half>(float x) { return __float2half_rn(x); }
+template <>
+__device__ __forceinline__ __nv_bfloat16 from_f<__nv_bfloat16>(float x) {
+  return __float2bfloat16_rn(x);
+}
+
+// Math type for a storage type: double for double storage, float otherwise.
+template <class T> struct MathOf { using type = float; };
+template <> struct MathOf<double> { using type = double; };
+
+template <class M, class T>
+__device__ __forceinline__ M ld_elem(const T* p) { return static_cast<M>(to_f(*p)); }
+template <>
+__device__ __forceinline__ double ld_elem<double, double>(const double* p) { return *p; }
+template <class M, class T>
+__device__ __forceinline__ void st_elem(T* p, M v) { *p = from_f<T>(static_cast<float>(v)); }
+template <>
+__device__ __forceinline__ void st_elem<double, double>(double* p, double v) { *p = v; }
+
+// ------------------------------------------------------------------ 8-element vector I/O
+// Streaming (read-once) 128-bit loads that do not allocate in L1, and streaming stores.
+__device__ __forceinline__ uint4 ld_stream_u4(const void* p) {
+  uint4 r;
+  asm volatile("ld.global.nc.L1::no_allocate.v4.u32 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+               : "l"(p));
+  return r;
+}
+__device__ __forceinline__ void st_stream_u4(void* p, uint4 v) {
+  asm volatile("st.global.cs.v4.u32 [%0], {%1,%2,%3,%4};" ::"l"(p), "r"(v.x), "r"(v.y),
+               "r"(v.z), "r"(v.w)
+               : "memory");
+}
+
+__device__ __forceinline__ void load8(const float* p, float (&o)[8]) {
+  const uint4 a = ld_stream_u4(p), b = ld_stream_u4(p + 4);
+  o[0] = __uint_as_float(a.x); o[1] = __uint_as_float(a.y);
+  o[2] = __uint_as_float(a.z); o[3] = __uint_as_float(a.w);
+  o[4] = __uint_as_float(b.x); o[5] = __uint_as_float(b.y);
+  o[6] = __uint_as_float(b.z); o[7] = __uint_as_float(b.w);
+}
+__device__ __forceinline__ void load8(const __half* p, float (&o)[8]) {
+  const uint4 a = ld_stream_u4(p);
+  const uint32_t w[4] = {a.x, a.y, a.z, a.w};
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const float2 f = __half22float2(*reinterpret_cast<const __half2*>(&w[i]));
+    o[2 * i] = f.x;
+    o[2 * i + 1] = f.y;
+  }
+}
+__device__ __forceinline__ void load8(const __nv_bfloat16* p, float (&o)[8]) {
+  const uint4 a = ld_stream_u4(p);
+  const uint32_t w[4] = {a.x, a.y, a.z, a.w};
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w[i]));
+    o[2 * i] = f.x;
+    o[2 * i + 1] = f.y;
+  }
+}
+__device__ __forceinline__ void load8(const double* p, double (&o)[8]) {
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    const uint4 a = ld_stream_u4(p + 2 * i);
+    o[2 * i] = __hiloint2double(a.y, a.x);
+    o[2 * i + 1] = __hiloint2double(a.w, a.z);
+  }
+}
+__device__ __forceinline__ void store8(float* p, const float (&v)[8]) {
+  st_stream_u4(p, make_uint4(__float_as_uint(v[0]), __float_as_uint(v[1]),
+                             __float_as_uint(v[2]), __float_as_uint(v[3])));
+  st_stream_u4(p + 4, make_uint4(__float_as_uint(v[4]), __float_as_uint(v[5]),
+                                 __float_as_uint(v[6]), __float_as_uint(v[7])));
+}
+__device__ __forceinline__ void store8(double* p, const double (&v)[8]) {
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    st_stream_u4(p + 2 * i, make_uint4(__double2loint(v[2 * i]), __double2hiint(v[2 * i]),
+                                       __double2loint(v[2 * i + 1]),
+                                       __double2hiint(v[2 * i + 1])));
+  }
+}
+
+// ------------------------------------------------------------------ hardware approximations
+__device__ __forceinline__ float ex2_approx(float x) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// ------------------------------------------------------------------ Kubelka-Munk
+// Reflectance of a layer (K, S, thickness d) over a substrate of reflectance R0, with the
+// semantics of painty's ComputeReflectance (painty/core/KubelkaMunk.hxx:25-83): R0 when
+// |d| < 1e4*DBL_EPSILON, S replaced by 1e-11 when |S| <= 1e4*DBL_EPSILON.
+//
+// FP32 evaluation, rearranged to avoid cancellation and to need 3 MUFU operations:
+//   with b = sqrt(a^2 - 1), a = 1 + K/S, x = b S d, and beta = S b = sqrt(K (2S + K)),
+//   A = S (1 - R0) - R0 K, B = S (1 - R0) + K, e = exp(-2x):
+//     R = (A (1 - e) + R0 beta (1 + e)) / (B (1 - e) + beta (1 + e))
+//   and for |x| < 0.05, with g = x coth x = 1 + x^2/3 - x^4/45 (+ O(x^6) < 4e-11):
+//     R = (A d + R0 g) / (B d + g)
+// Both are the reference's (1 - R0 (a - b coth x)) / (a - R0 + b coth x) multiplied through
+// by S (1 - e) or by S d / g. The series form is finite at K = 0, where the reference's
+// 0 * coth(0) is NaN. Physical inputs (K, S >= 0, d >= 0) are assumed.
+__device__ __forceinline__ float km_reflectance(float K, float S, float R0, float d) {
+  constexpr float kEps = 2.220446049250313e-12f;  // 1e4 * DBL_EPSILON
+  if (fabsf(d) < kEps) return R0;
+  S = fabsf(S) > kEps ? S : 1e-11f;
+  const float beta = sqrtf(fmaxf(K * (2.0f * S + K), 0.0f));
+  const float x = beta * d;
+  const float omr = 1.0f - R0;
+  const float A = fmaf(S, omr, -R0 * K);
+  const float B = fmaf(S, omr, K);
+  float num, den;
+  if (x < 0.05f) {
+    const float x2 = x * x;
+    const float g = fmaf(x2, fmaf(x2, -1.0f / 45.0f, 1.0f / 3.0f), 1.0f);
+    num = fmaf(A, d, R0 * g);
+    den = fmaf(B, d, g);
+  } else {
+    const float e = ex2_approx(-2.8853900817779268f * x);  // exp(-2x) = 2^(-2x log2 e)
+    const float u = 1.0f - e;
+    const float v = beta * (1.0f + e);
+    num = fmaf(A, u, R0 * v);
+    den = fmaf(B, u, v);
+  }
+  return __fdividef(num, den);
+}
+
+// painty's coth (painty/core/Math.hxx:157-169) and ComputeReflectance in double, in the
+// reference's own operation order; for the F64 parity storage mode.
+__device__ __forceinline__ double coth_ref(double x) {
+  if (x > 20.0) return 1.0;
+  if (fabs(x) > 0.0) {
+    const double res = cosh(x) / sinh(x);
+    return isnan(res) ? 1.0 : res;
+  }
+  return __longlong_as_double(0x7ff0000000000000ULL);
+}
+__device__ __forceinline__ double km_reflectance(double K, double S_in, double R0, double d) {
+  constexpr double kEps = 2.220446049250313e-12;
+  if (fabs(d) < kEps) return R0;
+  const double S = fabs(S_in) > kEps ? S_in : 0.00000000001;
+  const double K_S = __ddiv_rn(K, S);
+  const double a = __dadd_rn(1.0, K_S);
+  const double v = __dadd_rn(__dmul_rn(a, a), -1.0);
+  const double b = v < 0.0 ? 0.0 : __dsqrt_rn(v);
+  const double bSh = __dmul_rn(__dmul_rn(b, S), d);
+  const double bc = __dmul_rn(b, coth_ref(bSh));
+  return __ddiv_rn(__dadd_rn(1.0, -__dmul_rn(R0, __dadd_rn(a, -bc))),
+                   __dadd_rn(__dadd_rn(a, -R0), bc));
+}
+
+}  // namespace pg

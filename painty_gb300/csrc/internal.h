@@ -1,0 +1,127 @@
+// internal.h -- host-side definitions shared by the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+
+#include "painty_gb300.h"
+
+namespace pg {
+
+struct Error : std::runtime_error {
+  painty_status status;
+  Error(painty_status s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+[[noreturn]] void fail(painty_status s, const std::string& msg);
+void check_cuda(cudaError_t e, const char* what);
+#define PG_CUDA(x) ::pg::check_cuda((x), #x)
+#define PG_REQUIRE(cond, msg) \
+  do {                        \
+    if (!(cond)) ::pg::fail(PAINTY_ERR_INVALID_ARGUMENT, (msg)); \
+  } while (0)
+
+void set_last_error(const std::string& msg);
+void count_launch(int64_t n = 1);
+
+// Runs fn, converting exceptions to a status code and recording the message.
+template <class Fn>
+painty_status guard(Fn&& fn) {
+  try {
+    fn();
+    return PAINTY_OK;
+  } catch (const Error& e) {
+    set_last_error(e.what());
+    return e.status;
+  } catch (const std::bad_alloc&) {
+    set_last_error("host allocation failed");
+    return PAINTY_ERR_OUT_OF_MEMORY;
+  } catch (const std::exception& e) {
+    set_last_error(e.what());
+    return PAINTY_ERR_INVALID_ARGUMENT;
+  }
+}
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// Element sizes: K/S planes, V (and h) planes, reflectance planes.
+size_t ks_bytes(painty_storage s);
+size_t v_bytes(painty_storage s);
+inline size_t r_bytes(painty_storage s) { return s == PAINTY_STORAGE_F64 ? 8 : 4; }
+bool valid_storage(painty_storage s);
+
+// Row pitch in elements: a multiple of 64 elements (>= 128 bytes for every element type), so
+// each row starts 128-byte aligned and plane sizes are multiples of 8 elements.
+inline int64_t pitch_for(int32_t cols) { return (static_cast<int64_t>(cols) + 63) / 64 * 64; }
+
+void* device_alloc(size_t bytes);
+void device_free(void* p);
+
+}  // namespace pg
+
+// Opaque handle types of the C ABI.
+struct painty_layer {
+  int32_t rows = 0, cols = 0;
+  int64_t pitch = 0;
+  painty_storage storage = PAINTY_STORAGE_F32;
+  void* base = nullptr;  // one allocation holding the 7 planes
+  size_t bytes = 0;
+  void* K[3] = {nullptr, nullptr, nullptr};
+  void* S[3] = {nullptr, nullptr, nullptr};
+  void* V = nullptr;
+  bool owned = true;
+  int64_t plane_elems() const { return static_cast<int64_t>(rows) * pitch; }
+};
+
+struct painty_image {
+  int32_t rows = 0, cols = 0;
+  int64_t pitch = 0;
+  painty_storage storage = PAINTY_STORAGE_F32;  // F32 or F64
+  void* base = nullptr;
+  size_t bytes = 0;
+  void* R[3] = {nullptr, nullptr, nullptr};
+  bool owned = true;
+  int64_t plane_elems() const { return static_cast<int64_t>(rows) * pitch; }
+};
+
+struct painty_canvas {
+  painty_layer wet;  // borrowed view: owned = false
+  painty_image r0;   // borrowed view: owned = false
+  void* h = nullptr;  // height map, V element type
+  void* base = nullptr;
+  size_t bytes = 0;
+  uint64_t id = 0;       // process-unique
+  uint64_t version = 0;  // bumped by every write that does not go through a stamp
+};
+
+namespace pg {
+// Layout helpers (defined in core.cu).
+void layer_layout(painty_layer& L, int32_t rows, int32_t cols, painty_storage s, void* base);
+size_t layer_bytes(int32_t rows, int32_t cols, painty_storage s);
+void image_layout(painty_image& I, int32_t rows, int32_t cols, painty_storage s, void* base);
+size_t image_bytes(int32_t rows, int32_t cols, painty_storage s);
+
+// Plane transfer between a host buffer and `nch` device planes of element type `dev_type`
+// (0 f32, 1 f16, 2 bf16, 3 f64) with the given pitch. Synchronous w.r.t. the host buffer.
+enum DevType { DT_F32 = 0, DT_F16 = 1, DT_BF16 = 2, DT_F64 = 3 };
+DevType ks_type(painty_storage s);
+DevType v_type(painty_storage s);
+DevType r_type(painty_storage s);
+void upload_planes(void* const* planes, int nch, DevType dt, int32_t rows, int32_t cols,
+                   int64_t pitch, const void* host, painty_host_format fmt, cudaStream_t st);
+void download_planes(const void* const* planes, int nch, DevType dt, int32_t rows,
+                     int32_t cols, int64_t pitch, void* host, painty_host_format fmt,
+                     cudaStream_t st);
+void fill_planes(void* const* planes, int nch, DevType dt, int64_t elems, const double* values,
+                 cudaStream_t st);
+void copy_planes_async(void* const* dst, const void* const* src, int nch, size_t plane_bytes,
+                       cudaStream_t st);
+
+// KM composite launcher (core.cu). layers: L pointers; r0 and out may alias.
+void launch_compose(const painty_layer* const* layers, int32_t L, const painty_image* r0,
+                    painty_image* out, cudaStream_t st);
+}  // namespace pg

@@ -1,0 +1,129 @@
+"""Seeded synthetic workloads for the paint path (no files, no network).
+
+The reference paints from a scanned footprint PNG, measured pigments and user strokes; these
+generators stand in for them with fixed seeds:
+
+* footprint_image   64x64 imprint footprint: radial falloff x value noise, values in [0, 1]
+* pigments          base pigments, K ~ U[0.01, 5], S ~ U[0.05, 3] per channel
+* stroke_paints     per-stroke paint: Dirichlet(0.3) weights mixed as PaintMixer::mixSinglePaint
+* strokes           Catmull-Rom control polygons (8 points uniform on the canvas), radii
+* composite_stack   L stacked paint layers for the composite stress case
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+
+def footprint_image(seed: int = 7, size: int = 64, cells: int = 8) -> np.ndarray:
+    """Radial falloff (1 - (d/R)^2, clipped) times smoothstep-interpolated value noise."""
+    rng = np.random.default_rng(seed)
+    lattice = rng.random((cells + 1, cells + 1))
+    coord = (np.arange(size) + 0.5) / size * cells
+    i0 = np.minimum(coord.astype(np.int64), cells - 1)
+    t = coord - i0
+    t = t * t * (3.0 - 2.0 * t)
+    a = lattice[i0][:, i0]
+    b = lattice[i0][:, i0 + 1]
+    c = lattice[i0 + 1][:, i0]
+    d = lattice[i0 + 1][:, i0 + 1]
+    tx = t[None, :]
+    ty = t[:, None]
+    noise = (a * (1 - tx) + b * tx) * (1 - ty) + (c * (1 - tx) + d * tx) * ty
+    r = size / 2.0
+    yy, xx = np.mgrid[0:size, 0:size]
+    dist = np.hypot(xx + 0.5 - r, yy + 0.5 - r) / r
+    falloff = np.clip(1.0 - dist * dist, 0.0, 1.0)
+    return np.ascontiguousarray(falloff * noise)
+
+
+def pigments(seed: int = 11, n: int = 14):
+    rng = np.random.default_rng(seed)
+    K = rng.uniform(0.01, 5.0, (n, 3))
+    S = rng.uniform(0.05, 3.0, (n, 3))
+    return K, S
+
+
+def mix_single_paint_np(weights: np.ndarray, K: np.ndarray, S: np.ndarray):
+    """PaintMixer::mixSinglePaint (PaintMixer.cxx:327-355) with its accumulation order."""
+    wsum = 0.0
+    for w in weights:
+        wsum += float(w)
+    norm = 1.0 if abs(wsum - 1.0) < 10e-6 else 1.0 / wsum
+    k = np.zeros(3)
+    s = np.zeros(3)
+    for l in range(len(weights)):
+        for i in range(3):
+            k[i] += norm * float(weights[l]) * K[l, i]
+            s[i] += norm * float(weights[l]) * S[l, i]
+    return k, s
+
+
+@dataclass
+class Stroke:
+    path: np.ndarray  # (n, 2) control points, x then y
+    radius: float
+    K: np.ndarray
+    S: np.ndarray
+    spacing: float
+
+
+def strokes(width: int, height: int, n: int, seed: int = 3, rmin: float = 8.0,
+            rmax: float = 32.0, points: int = 8, log_radius: bool = False,
+            spacing_factor: float = 0.25, pigment_seed: int = 11) -> list[Stroke]:
+    """Strokes through `points` control points uniform on the canvas; radius U[rmin, rmax]
+    (log-uniform with log_radius); paint = Dirichlet(0.3) mix of the base pigments; stamp
+    spacing spacing_factor * radius."""
+    rng = np.random.default_rng(seed)
+    PK, PS = pigments(pigment_seed)
+    out = []
+    for _ in range(n):
+        path = np.stack([rng.uniform(0, width, points), rng.uniform(0, height, points)], axis=1)
+        if log_radius:
+            r = float(np.exp(rng.uniform(np.log(rmin), np.log(rmax))))
+        else:
+            r = float(rng.uniform(rmin, rmax))
+        w = rng.dirichlet(np.full(len(PK), 0.3))
+        k, s = mix_single_paint_np(w, PK, PS)
+        out.append(Stroke(np.ascontiguousarray(path), r, k, s, spacing_factor * r))
+    return out
+
+
+def substrate(rows: int, cols: int, seed: int = 5, lo: float = 0.80, hi: float = 0.95):
+    """R0 ~ U[lo, hi] per channel per pixel, interleaved (rows, cols, 3)."""
+    rng = np.random.default_rng(seed)
+    return rng.uniform(lo, hi, (rows, cols, 3))
+
+
+def composite_stack(rows: int, cols: int, layers: int = 8, seed: int = 1,
+                    dtype=np.float32):
+    """Planar layer stack for the composite stress case.
+
+    Returns K, S of shape (L, 3, rows, cols), V of shape (L, rows, cols) and R0 of shape
+    (3, rows, cols): K ~ U[0.01, 5], S ~ U[0.05, 3], h ~ U[0, 0.5] with 20% of pixels at
+    h = 0 and 5% with h ~ U[1e-7, 1e-4] (the small-argument branch), R0 ~ U[0.8, 0.95].
+    """
+    rng = np.random.default_rng(seed)
+    K = rng.uniform(0.01, 5.0, (layers, 3, rows, cols)).astype(dtype)
+    S = rng.uniform(0.05, 3.0, (layers, 3, rows, cols)).astype(dtype)
+    V = rng.uniform(0.0, 0.5, (layers, rows, cols))
+    sel = rng.random((layers, rows, cols))
+    V[sel < 0.20] = 0.0
+    small = (sel >= 0.20) & (sel < 0.25)
+    V[small] = rng.uniform(1e-7, 1e-4, int(small.sum()))
+    V = V.astype(dtype)
+    R0 = rng.uniform(0.8, 0.95, (3, rows, cols)).astype(dtype)
+    return K, S, V, R0
+
+
+def paint_config0(canvas, brush, strokes_list, on_stroke=None):
+    """Config-0 style painting: per stroke setRadius, dip, paintStroke at the stroke spacing."""
+    total = 0
+    for i, s in enumerate(strokes_list):
+        brush.setRadius(s.radius)
+        brush.dip((s.K, s.S))
+        total += brush.paintStroke(s.path, canvas, spacing=s.spacing)
+        if on_stroke is not None:
+            on_stroke(i)
+    return total

@@ -1,0 +1,122 @@
+"""KM composite kernel vs the oracle (GPU)."""
+import numpy as np
+import pytest
+
+from painty_gb300 import workloads
+from tests.gpu_helpers import gpu_compose, oracle_compose
+
+pytestmark = pytest.mark.gpu
+
+# FP32 storage and arithmetic vs painty's double ComputeReflectance on the same inputs
+F32_ABS_TOL = 1e-5
+# FP16/BF16 storage (K, S, V rounded on store) vs the FP64 oracle, as CIEDE2000
+HALF_DELTA_E = 0.5
+
+
+@pytest.mark.parametrize("shape,L", [((61, 203), 8), ((64, 64), 1), ((17, 5), 3)])
+def test_f32_matches_reference(pg, oracle, shape, L):
+    K, S, V, R0 = workloads.composite_stack(*shape, layers=L, seed=L)
+    got = gpu_compose(pg, K, S, V, R0, "f32")
+    want = oracle_compose(oracle, K, S, V, R0, mode=0)
+    err = np.abs(got - want).max()
+    assert err <= F32_ABS_TOL, err
+
+
+def test_f32_small_thickness_branch(pg, oracle):
+    """Thickness in [1e-7, 1e-4] (the series branch) and exactly 0 (R0 passthrough)."""
+    rows, cols, L = 32, 96, 4
+    K, S, V, R0 = workloads.composite_stack(rows, cols, layers=L, seed=9)
+    rng = np.random.default_rng(1)
+    V = np.where(rng.random(V.shape) < 0.5, rng.uniform(1e-7, 1e-4, V.shape), 0.0).astype(np.float32)
+    got = gpu_compose(pg, K, S, V, R0, "f32")
+    want = oracle_compose(oracle, K, S, V, R0, mode=0)
+    assert np.abs(got - want).max() <= F32_ABS_TOL
+    # pixels with all layers at h = 0 are exactly R0
+    zero = (V == 0).all(axis=0)
+    assert np.array_equal(got[:, zero], R0[:, zero].astype(np.float64))
+
+
+def test_f64_matches_reference(pg, oracle):
+    K, S, V, R0 = workloads.composite_stack(40, 70, layers=5, seed=3, dtype=np.float64)
+    got = gpu_compose(pg, K, S, V, R0, "f64")
+    want = oracle_compose(oracle, K, S, V, R0, mode=0)
+    assert np.abs(got - want).max() <= 1e-13
+
+
+@pytest.mark.parametrize("storage", ["f16", "bf16"])
+def test_half_storage_delta_e(pg, oracle, storage):
+    K, S, V, R0 = workloads.composite_stack(48, 160, layers=8, seed=4, dtype=np.float64)
+    got = gpu_compose(pg, K, S, V, R0, storage)
+    want = oracle_compose(oracle, K, S, V, R0, mode=1)
+    de_max, de_mean = oracle.delta_e(np.moveaxis(got, 0, -1), np.moveaxis(want, 0, -1))
+    assert de_max < HALF_DELTA_E, (de_max, de_mean)
+
+
+def test_fused_equals_unfused_bitwise(pg):
+    K, S, V, R0 = workloads.composite_stack(33, 130, layers=8, seed=5)
+    a = gpu_compose(pg, K, S, V, R0, "f32", fused=True)
+    b = gpu_compose(pg, K, S, V, R0, "f32", fused=False)
+    assert np.array_equal(a, b)
+
+
+def test_more_layers_than_one_launch(pg, oracle):
+    K, S, V, R0 = workloads.composite_stack(16, 72, layers=19, seed=6)
+    got = gpu_compose(pg, K, S, V, R0, "f32")
+    want = oracle_compose(oracle, K, S, V, R0, mode=0)
+    assert np.abs(got - want).max() <= 2 * F32_ABS_TOL
+
+
+def test_inplace_and_zero_layers(pg):
+    K, S, V, R0 = workloads.composite_stack(16, 40, layers=3, seed=7)
+    a = gpu_compose(pg, K, S, V, R0, "f32")
+    b = gpu_compose(pg, K, S, V, R0, "f32", inplace=True)
+    assert np.array_equal(a, b)
+    z = gpu_compose(pg, K[:0], S[:0], V[:0], R0, "f32")
+    assert np.array_equal(z, R0.astype(np.float64))
+
+
+def test_fp32_vs_fp64_oracle_delta_e(pg, oracle):
+    K, S, V, R0 = workloads.composite_stack(64, 128, layers=8, seed=8)
+    got = gpu_compose(pg, K, S, V, R0, "f32")
+    want = oracle_compose(oracle, K, S, V, R0, mode=1)
+    de_max, _ = oracle.delta_e(np.moveaxis(got, 0, -1), np.moveaxis(want, 0, -1))
+    assert de_max < 0.01
+
+
+def test_canvas_compose_and_dry(pg, oracle):
+    rows, cols = 23, 57
+    rng = np.random.default_rng(2)
+    K = rng.uniform(0.01, 5, (rows, cols, 3))
+    S = rng.uniform(0.05, 3, (rows, cols, 3))
+    V = np.where(rng.random((rows, cols)) < 0.3, 0.0, rng.uniform(0, 2, (rows, cols)))
+    R0 = rng.uniform(0.8, 0.95, (rows, cols, 3))
+    for storage, tol in (("f64", 1e-13), ("f32", 2e-5)):
+        c = pg.Canvas(rows, cols, storage)
+        oc = oracle.canvas(rows, cols)
+        for p, a in (("K", K), ("S", S), ("V", V), ("R0", R0)):
+            c.upload(p, a)
+            oc.set(p, a)
+        out = pg.Renderer().compose(c).download()
+        assert np.abs(out - oc.compose()).max() <= tol
+        c.dryCanvas()
+        oc.dry()
+        assert np.abs(c.getR0() - oc.get("R0")).max() <= tol
+        assert np.abs(c.get_h() - oc.get("h")).max() <= 1e-6
+        assert not c.download("V").any() and not c.download("K").any()
+
+
+def test_upload_download_roundtrip(pg):
+    rows, cols = 19, 77
+    rng = np.random.default_rng(3)
+    a = rng.random((rows, cols, 3))
+    for storage in ("f32", "f64"):
+        ly = pg.PaintLayer(rows, cols, storage)
+        ly.upload("K", a)
+        back = ly.download("K")
+        tol = 0 if storage == "f64" else 1e-7
+        assert np.abs(back - a).max() <= tol
+        ly.upload("S", a.astype(np.float32))
+        np.testing.assert_array_equal(ly.download("S", dtype=np.float32), a.astype(np.float32))
+        planar = np.ascontiguousarray(np.moveaxis(a, -1, 0))
+        ly.upload("K", planar, planar=True)
+        assert np.abs(ly.download("K") - a).max() <= tol
