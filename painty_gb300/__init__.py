@@ -29,7 +29,7 @@ LIB_PATH = _HERE / "_lib" / "libpainty_gb300.so"
 if not LIB_PATH.exists():
     raise ImportError(
         f"painty_gb300 native library not found at {LIB_PATH}; build it with "
-        "`python -m painty_gb300.build` (CUDA toolkit required; there is no CPU fallback)")
+        "`python painty_gb300/build.py` (CUDA toolkit required; there is no CPU fallback)")
 
 _lib = C.CDLL(str(LIB_PATH))
 

@@ -1,6 +1,8 @@
 """Builds the painty_gb300 CUDA library in-tree for sm_103a.
 
-    python -m painty_gb300.build          # -> painty_gb300/_lib/libpainty_gb300.so
+    python painty_gb300/build.py           # -> painty_gb300/_lib/libpainty_gb300.so
+
+(Run it as a script: importing the package itself requires the built library.)
 
 One nvcc job per translation unit, run in parallel, then one link. No CPU fallback is built:
 the library is CUDA-only and every entry point launches its own kernels.
