@@ -39,9 +39,11 @@ def sources() -> list[Path]:
     return sorted(CSRC.glob("*.cu"))
 
 
+# Host code is built without floating-point contraction so the footprint resample and the
+# stroke expansion give the same bits on x86-64 and aarch64 (and as painty's double code).
 def _compile(src: Path, obj: Path) -> None:
     cmd = [nvcc(), *ARCH, "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
-           "-Xcompiler", "-Wall", "--expt-relaxed-constexpr", "-I", str(ROOT / "include"),
+           "-Xcompiler", "-Wall", "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr", "-I", str(ROOT / "include"),
            "-I", str(CSRC), "-c", str(src), "-o", str(obj)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

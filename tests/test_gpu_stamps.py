@@ -215,3 +215,13 @@ def test_invalid_stamp_rejected(pg):
         b.imprint((float("nan"), 1.0), 0.0, c)
     with pytest.raises(ValueError):
         b.paintStroke(np.array([[0.0, 0.0], [5.0, 5.0]]), c, spacing=0.0)
+
+
+def test_host_setup_matches_oracle(pg, oracle):
+    """Footprint resample and stroke expansion (host code) give the oracle's exact bits."""
+    fp = workloads.footprint_image(seed=7)
+    for r in (0.7, 3.2, 8.0, 19.6, 31.1, 64.0):
+        b = pg.FootprintBrush(r, fp)
+        ob = oracle.brush(r, fp)
+        assert b.info() == ob.info()
+        assert np.array_equal(b.getFootprint(), ob.footprint()), r
