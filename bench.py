@@ -61,7 +61,7 @@ def _traffic_from_profile():
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    Q = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -69,6 +69,15 @@ class ClockSampler:
         self.index = index
         self.proc = None
         self.file = None
+        self.window = None  # (t0, t1) wall-clock bounds of the timed region
+
+    def wait_ready(self, timeout: float = 5.0) -> None:
+        """Blocks until the sampler has written its first line (it takes a moment to start)."""
+        t = time.time()
+        while self.proc is not None and time.time() - t < timeout:
+            if Path(self.file.name).stat().st_size > 0:
+                return
+            time.sleep(0.05)
 
     def __enter__(self):
         try:
@@ -92,23 +101,35 @@ class ClockSampler:
     def summary(self):
         if self.proc is None or self.file is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        import datetime
+
         rows = []
         for line in Path(self.file.name).read_text().splitlines():
             f = [x.strip() for x in line.split(",")]
             if len(f) < 9:
                 continue
             try:
-                rows.append((float(f[1]), float(f[2]), f[5], f[6], f[7], f[8]))
+                ts = datetime.datetime.strptime(f[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                rows.append((ts, float(f[1]), float(f[2]), f[5], f[6], f[7], f[8]))
             except ValueError:
                 continue
         os.unlink(self.file.name)
+        where = "timed region"
+        if self.window is not None:
+            t0, t1 = self.window
+            inside = [r for r in rows if t0 - 0.05 <= r[0] <= t1 + 0.15]
+            if not inside:  # region shorter than the sampling period: nearest samples after it
+                inside = [r for r in rows if t1 <= r[0] <= t1 + 0.5][:2]
+                where = "first samples after the timed region"
+            rows = inside
+        rows = [r[1:] for r in rows]
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
         sm = sorted(r[0] for r in rows)
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[i] for r in rows for i in range(4) if r[2 + i] == "Active"})
         return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": max(r[1] for r in rows),
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(rows), "window": where}
 
 
 def _dist():
@@ -181,13 +202,16 @@ def run_ours(args):
         torch.cuda.synchronize()
 
     # ---- device-resident composite
+    clocks = ClockSampler(local).__enter__()
+    clocks.wait_ready()
     for _ in range(args.warmup):
         pg.compose_layers(layers, r0, out, stream=stream)
     barrier()
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     l0 = pg.kernel_launch_count()
-    with ClockSampler(local) as clocks:
+    wall0 = time.time()
+    if True:
         t0 = torch.cuda.Event(enable_timing=True)
         t1 = torch.cuda.Event(enable_timing=True)
         t0.record(stream)
@@ -197,6 +221,9 @@ def run_ours(args):
             ends[i].record(stream)
         t1.record(stream)
         barrier()
+    clocks.window = (wall0, time.time())
+    time.sleep(0.2)
+    clocks.__exit__(None, None, None)
     launches = pg.kernel_launch_count() - l0
     total_ms = t0.elapsed_time(t1)
     per = [s.elapsed_time(e) for s, e in zip(starts, ends)]
@@ -264,7 +291,7 @@ def run_ours(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded, generated on the device)",
-            "config": {"workload": "KM composite 4096x4096, 8 stacked FP32 layers -> RGB",
+            "config": {"workload": f"KM composite {ROWS}x{COLS}, {LAYERS} stacked FP32 layers -> RGB",
                        "rows": ROWS, "cols": COLS, "layers": LAYERS, "storage": "f32",
                        "l2": "inputs 4.2 GB per step > 129 MB L2 (no flush needed)",
                        "parallelism": f"replicas{ws}"},
@@ -377,7 +404,7 @@ def run_reference(args):
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-        "config": {"workload": "KM composite 4096x4096, 8 stacked FP32 layers -> RGB",
+        "config": {"workload": f"KM composite {ROWS}x{COLS}, {LAYERS} stacked FP32 layers -> RGB",
                    "rows": ROWS, "cols": COLS, "layers": LAYERS},
         "cpu_baseline": {"value": round(value, 3), "unit": "Mpix/s", "cores": cores,
                          "kind": "port", "sample": sample},
@@ -389,14 +416,17 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=500)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--rows", type=int, default=ROWS, help="composite rows (profiling cases)")
+    ap.add_argument("--cols", type=int, default=COLS, help="composite cols (profiling cases)")
     ap.add_argument("--no-stamps", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    globals()["ROWS"], globals()["COLS"] = args.rows, args.cols
     if args.impl == "reference":
         run_reference(args)
     else:
