@@ -193,6 +193,58 @@ painty_status painty_stroke(painty_canvas* canvas, painty_brush* brush, const do
 painty_status painty_mix_paint(const double* weights, int32_t n, const double* palette_K,
                                const double* palette_S, double K[3], double S[3]);
 
+/* ------------------------------------------------------------------ allocation-free stamping
+ * No counterpart in the reference (painty's brush owns its buffers; this entry exists for
+ * callers that cannot allocate device memory).
+ *
+ * Some callers cannot call cudaMalloc: a plugin whose host application owns every byte of
+ * device memory and hands out fixed buffers, a real-time paint loop that must not pay the
+ * device-wide synchronisation an allocation can cause, or code that runs while another
+ * thread captures a CUDA graph. painty_stamps allocates on first use (snapshot, pickup map,
+ * scratch); this entry point allocates nothing. The caller passes every input and output as
+ * its own device memory, and the only scratch -- an owner table of map_side^2 ints and a
+ * status word -- is a fixed array inside the library (about 258 KB, held on every GPU that
+ * loads the library until the process exits).
+ *
+ * Semantics are painty_stamps' on an F32 canvas: stamps applied in order, each one
+ * FootprintBrush::imprint. Limits: map_side <= PAINTY_NOALLOC_MAX_MAP_SIDE (radius about 90);
+ * larger sizes return PAINTY_ERR_INVALID_ARGUMENT. The first call on a device looks up the
+ * scratch address; make it before any stream capture. Calls share the scratch: calls that
+ * overlap on the GPU (other streams, other threads) race, so serialise them. The call returns
+ * after the stamps ran (it reads the kernel's status word).
+ *
+ * Buffers (device memory, FP32):
+ *   canvas_*:   the wet layer, rows x pitch elements per plane (pitch >= cols)
+ *   snapshot_*: the pickup source (FootprintBrush's snapshot buffer), same geometry; all NULL
+ *               to pick up from the canvas. The caller initialises it (a copy of the canvas,
+ *               as painty does on first use) and keeps it between calls.
+ *   pickup_*:   the pickup map, map_side x map_side per plane; zero it to dip the brush
+ *   footprint:  footprint_side x footprint_side heights (painty_brush_footprint, as float)
+ *   stamps:     n records of 4 doubles: cx, cy, cos(-theta), sin(-theta)
+ * Brush values: radius (the brush's current radius), rates, capacity (painty uses 1.0) and the
+ * dipped paint. */
+#define PAINTY_NOALLOC_MAX_MAP_SIDE 257
+typedef struct painty_stamp_buffers_f32 {
+  float* canvas_K[3];
+  float* canvas_S[3];
+  float* canvas_V;
+  float* snapshot_K[3];
+  float* snapshot_S[3];
+  float* snapshot_V;
+  float* pickup_K[3];
+  float* pickup_S[3];
+  float* pickup_V;
+  const float* footprint;
+  const double* stamps;
+  int64_t n;
+  int32_t rows, cols;
+  int64_t pitch;
+  int32_t footprint_side, map_side;
+  double radius, pickup_rate, deposition_rate, capacity;
+  double paint_K[3], paint_S[3];
+} painty_stamp_buffers_f32;
+painty_status painty_stamps_f32_noalloc(const painty_stamp_buffers_f32* buffers, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

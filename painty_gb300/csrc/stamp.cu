@@ -40,6 +40,8 @@
 #include <climits>
 #include <cmath>
 #include <cstring>
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "device_common.cuh"
@@ -654,6 +656,42 @@ void expand_stroke(const double* path, int32_t n, double spacing, std::vector<St
 
 }  // namespace pg
 
+// ====================================================================== allocation-free stamping
+// Scratch of painty_stamps_f32_noalloc: the per-stamp owner table (map_side^2 ints, up to
+// 257^2) followed by one status word. Every GPU that loads this library holds it (about
+// 258 KB) until the process exits. All calls share it; calls that overlap on the GPU race.
+constexpr int kNoAllocMaxMapSide = 257;
+constexpr int kNoAllocOwnerCells = kNoAllocMaxMapSide * kNoAllocMaxMapSide;
+static __device__ __align__(256) int g_noalloc_scratch[kNoAllocOwnerCells + 64];
+
+namespace pg {
+namespace {
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+// Device address of the scratch array on the current device. The host-side symbol is only a
+// stand-in, so the address is looked up once per device, with that device current.
+int* noalloc_scratch() {
+  int dev = 0;
+  PG_CUDA(cudaGetDevice(&dev));
+  PG_REQUIRE(dev >= 0 && dev < kNoAllocMaxDevices, "device ordinal out of range");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+      cudaGetLastError();
+      fail(PAINTY_ERR_CUDA, std::string("cudaGetSymbolAddress(no-alloc scratch): ") +
+                              cudaGetErrorString(e));
+    }
+    g_noalloc_addr[dev] = p;
+  }
+  return static_cast<int*>(g_noalloc_addr[dev]);
+}
+}  // namespace
+}  // namespace pg
+
 using pg::guard;
 
 extern "C" {
@@ -828,6 +866,81 @@ painty_status painty_stroke(painty_canvas* c, painty_brush* b, const double* pat
     pg::expand_stroke(path, n, spacing, r);
     if (stamps_out) *stamps_out = static_cast<int64_t>(r.size());
     pg::run_stamps(c, b, r, pg::as_stream(stream));
+  });
+}
+
+// Runs the stamp kernel on caller-owned buffers without allocating: the owner table and the
+// status word live in g_noalloc_scratch. The first call on a device looks up the scratch
+// address (make it before any stream capture). Synchronous: returns after the stamps ran.
+painty_status painty_stamps_f32_noalloc(const painty_stamp_buffers_f32* b, void* stream) {
+  return guard([&] {
+    PG_REQUIRE(b != nullptr, "buffers is null");
+    PG_REQUIRE(b->n >= 0, "negative stamp count");
+    PG_REQUIRE(b->rows > 0 && b->cols > 0 && b->pitch >= b->cols, "bad canvas geometry");
+    PG_REQUIRE(b->footprint_side > 0 && (b->footprint_side & 1) == 1,
+               "footprint side must be odd and positive");
+    PG_REQUIRE(b->map_side >= b->footprint_side && b->map_side <= b->footprint_side + 1,
+               "map side must be the footprint side or one more");
+    PG_REQUIRE(b->map_side <= kNoAllocMaxMapSide,
+               "pickup map side above the allocation-free maximum of 257 (radius about 90)");
+    PG_REQUIRE(static_cast<int64_t>(b->footprint_side) * b->footprint_side <=
+                 int64_t(pg::kMaxPixelsPerThread) * pg::kStampThreads,
+               "footprint side above 256");
+    for (int i = 0; i < 3; i++)
+      PG_REQUIRE(b->canvas_K[i] && b->canvas_S[i] && b->pickup_K[i] && b->pickup_S[i],
+                 "null plane");
+    PG_REQUIRE(b->canvas_V && b->pickup_V && b->footprint, "null plane");
+    const bool snap = b->snapshot_V != nullptr;
+    if (snap)
+      for (int i = 0; i < 3; i++)
+        PG_REQUIRE(b->snapshot_K[i] && b->snapshot_S[i], "partial snapshot planes");
+    if (b->n == 0) return;
+    PG_REQUIRE(b->stamps != nullptr, "stamps is null");
+    const cudaStream_t st = pg::as_stream(stream);
+    int* scratch = pg::noalloc_scratch();
+    unsigned* status = reinterpret_cast<unsigned*>(scratch + kNoAllocOwnerCells);
+    PG_CUDA(cudaMemsetAsync(status, 0, sizeof(unsigned), st));
+    pg::StampArgs<float, float> a{};
+    for (int i = 0; i < 3; i++) {
+      a.cK[i] = b->canvas_K[i];
+      a.cS[i] = b->canvas_S[i];
+      a.sK[i] = snap ? b->snapshot_K[i] : b->canvas_K[i];
+      a.sS[i] = snap ? b->snapshot_S[i] : b->canvas_S[i];
+      a.pK[i] = b->pickup_K[i];
+      a.pS[i] = b->pickup_S[i];
+      a.paintK[i] = static_cast<float>(b->paint_K[i]);
+      a.paintS[i] = static_cast<float>(b->paint_S[i]);
+    }
+    a.cV = b->canvas_V;
+    a.sV = snap ? b->snapshot_V : b->canvas_V;
+    a.pV = b->pickup_V;
+    a.footprint = b->footprint;
+    a.stamps = reinterpret_cast<const pg::StampRec*>(b->stamps);
+    a.n = b->n;
+    a.rows = b->rows;
+    a.cols = b->cols;
+    a.pitch = b->pitch;
+    a.F = b->footprint_side;
+    a.S = b->map_side;
+    a.wr = (b->footprint_side - 1) / 2;
+    a.radius = b->radius;
+    a.pickupRate = static_cast<float>(b->pickup_rate);
+    a.depositionRate = static_cast<float>(b->deposition_rate);
+    a.capacity = static_cast<float>(b->capacity);
+    a.use_snapshot = snap ? 1 : 0;
+    a.owner_global = scratch;
+    a.status = status;
+    const size_t dyn = static_cast<size_t>(b->footprint_side) * (2 * sizeof(int) + 2);
+    auto kern = pg::stamp_kernel<float, float>;
+    PG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(dyn)));
+    kern<<<1, pg::kStampThreads, dyn, st>>>(a);
+    pg::count_launch();
+    PG_CUDA(cudaGetLastError());
+    unsigned hs = 0;
+    PG_CUDA(cudaMemcpyAsync(&hs, status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    PG_CUDA(cudaStreamSynchronize(st));
+    if (hs != 0) pg::fail(PAINTY_ERR_CUDA, "stamp kernel reported an internal error");
   });
 }
 
