@@ -169,6 +169,16 @@ def generate_stack_device(torch, seed: int):
     return host
 
 
+def run_stamps_only(args):
+    """The stamping case alone (profiling runs): prints its stamps object."""
+    import torch
+
+    import painty_gb300 as pg
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    print(json.dumps(run_stamps_config0(pg, torch, args.strokes)), flush=True)
+
+
 def run_ours(args):
     import torch
 
@@ -318,12 +328,12 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def run_stamps_config0(pg, torch):
+def run_stamps_config0(pg, torch, nstrokes: int = 200):
     """1024x768 FP32 canvas, 200 strokes, r ~ U[8,32], spacing 0.25 r, through the C ABI."""
     from painty_gb300 import workloads
 
     rows, cols = 768, 1024
-    strokes = workloads.strokes(cols, rows, 200, seed=3)
+    strokes = workloads.strokes(cols, rows, nstrokes, seed=3)
     fp = workloads.footprint_image(seed=7)
     r0 = workloads.substrate(rows, cols, seed=5)
     canvas = pg.Canvas(rows, cols, "f32")
@@ -422,6 +432,8 @@ def main():
     ap.add_argument("--rows", type=int, default=ROWS, help="composite rows (profiling cases)")
     ap.add_argument("--cols", type=int, default=COLS, help="composite cols (profiling cases)")
     ap.add_argument("--no-stamps", action="store_true")
+    ap.add_argument("--stamps-only", action="store_true", help="only the stamping case")
+    ap.add_argument("--strokes", type=int, default=200, help="strokes in the stamping case")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -429,6 +441,8 @@ def main():
     globals()["ROWS"], globals()["COLS"] = args.rows, args.cols
     if args.impl == "reference":
         run_reference(args)
+    elif args.stamps_only:
+        run_stamps_only(args)
     else:
         run_ours(args)
 

@@ -332,45 +332,77 @@ struct ComposeArgs {
   int64_t groups;  // plane elements / 8
 };
 
-// One thread owns 8 consecutive plane elements (pixels): 128-bit streaming loads of each
-// layer's 7 planes, the KM recurrence R <- KM(K_l, S_l, R, V_l) through all L layers in
-// registers, one store of R. Per pixel this reads 7 L + 3 planes and writes 3 exactly once.
+// One thread owns PIX consecutive pixels, PIX = 16 bytes of the K/S element type (4 for F32,
+// 8 for F16/BF16, 2 for F64): 16-byte streaming loads of each layer's 7 planes, the KM
+// recurrence R <- KM(K_l, S_l, R, V_l) through all L layers in registers, one streaming store
+// of R. Per pixel this reads 7 L + 3 planes and writes 3, each exactly once. The grid is one
+// wave of resident blocks walking the planes with a grid stride.
 template <class TK, class TV, class TR>
 __global__ void __launch_bounds__(256) km_composite_kernel(
   const __grid_constant__ ComposeArgs<TK, TV, TR> a) {
   using M = typename MathOf<TR>::type;
+  constexpr int PIX = 16 / sizeof(TK);
+  const int64_t groups = a.groups;
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-  for (int64_t g = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; g < a.groups;
+  for (int64_t g = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; g < groups;
        g += stride) {
-    const int64_t e = g * 8;
-    M r[3][8];
+    const int64_t e = g * PIX;
+    M r[3][PIX];
 #pragma unroll
-    for (int c = 0; c < 3; c++) load8(a.r0[c] + e, r[c]);
+    for (int c = 0; c < 3; c++) {
+      TR t[PIX];
+      load_vec<PIX>(a.r0[c] + e, t);
+#pragma unroll
+      for (int i = 0; i < PIX; i++) r[c][i] = static_cast<M>(t[i]);
+    }
     for (int l = 0; l < a.L; l++) {
-      M v[8];
-      load8(a.V[l] + e, v);
+      TV v[PIX];
+      TK k[3][PIX], s[3][PIX];
+      load_vec<PIX>(a.V[l] + e, v);
 #pragma unroll
       for (int c = 0; c < 3; c++) {
-        M k[8], s[8];
-        load8(a.K[l][c] + e, k);
-        load8(a.S[l][c] + e, s);
-#pragma unroll
-        for (int i = 0; i < 8; i++) r[c][i] = km_reflectance(k[i], s[i], r[c][i], v[i]);
+        load_vec<PIX>(a.K[l][c] + e, k[c]);
+        load_vec<PIX>(a.S[l][c] + e, s[c]);
       }
+#pragma unroll
+      for (int c = 0; c < 3; c++)
+#pragma unroll
+        for (int i = 0; i < PIX; i++)
+          r[c][i] = km_reflectance(ld_elem<M>(&k[c][i]), ld_elem<M>(&s[c][i]), r[c][i],
+                                   ld_elem<M>(&v[i]));
     }
 #pragma unroll
-    for (int c = 0; c < 3; c++) store8(a.out[c] + e, r[c]);
+    for (int c = 0; c < 3; c++) {
+      TR t[PIX];
+#pragma unroll
+      for (int i = 0; i < PIX; i++) t[i] = static_cast<TR>(r[c][i]);
+      store_vec<PIX>(a.out[c] + e, t);
+    }
   }
+}
+
+template <class Kern>
+int resident_grid(Kern kern, int block) {
+  static int cached[64] = {0};
+  int dev = 0;
+  PG_CUDA(cudaGetDevice(&dev));
+  if (dev < 64 && cached[dev] > 0) return cached[dev];
+  int sms = 0, per_sm = 0;
+  PG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  PG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, 0));
+  const int g = std::max(1, sms * std::max(1, per_sm));
+  if (dev < 64) cached[dev] = g;
+  return g;
 }
 
 template <class TK, class TV, class TR>
 void compose_typed(const painty_layer* const* layers, int32_t L, const painty_image* r0,
                    painty_image* out, cudaStream_t st) {
-  const int64_t elems = r0->plane_elems();
-  int dev = 0, sms = 0;
-  PG_CUDA(cudaGetDevice(&dev));
-  PG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  for (int32_t l0 = 0; l0 < L || (L == 0 && l0 == 0); l0 += kMaxLayersPerLaunch) {
+  constexpr int PIX = 16 / sizeof(TK);
+  const int64_t elems = r0->plane_elems();  // a multiple of 64 elements
+  auto kern = km_composite_kernel<TK, TV, TR>;
+  const int wave = resident_grid(kern, 256);
+  for (int32_t l0 = 0; l0 < L; l0 += kMaxLayersPerLaunch) {
     ComposeArgs<TK, TV, TR> a{};
     const int32_t n = std::min<int32_t>(kMaxLayersPerLaunch, L - l0);
     for (int32_t i = 0; i < n; i++) {
@@ -386,14 +418,13 @@ void compose_typed(const painty_layer* const* layers, int32_t L, const painty_im
       a.r0[c] = static_cast<const TR*>(src->R[c]);
       a.out[c] = static_cast<TR*>(out->R[c]);
     }
-    a.L = std::max<int32_t>(n, 0);
-    a.groups = elems / 8;
+    a.L = n;
+    a.groups = elems / PIX;
     const int64_t blocks_needed = (a.groups + 255) / 256;
-    const int grid = static_cast<int>(std::min<int64_t>(blocks_needed, int64_t(sms) * 8));
-    km_composite_kernel<TK, TV, TR><<<std::max(grid, 1), 256, 0, st>>>(a);
+    const int grid = static_cast<int>(std::min<int64_t>(blocks_needed, wave));
+    kern<<<std::max(grid, 1), 256, 0, st>>>(a);
     count_launch();
     PG_CUDA(cudaGetLastError());
-    if (L == 0) break;
   }
 }
 

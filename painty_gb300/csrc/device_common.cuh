@@ -38,7 +38,7 @@ __device__ __forceinline__ void st_elem(T* p, M v) { *p = from_f<T>(static_cast<
 template <>
 __device__ __forceinline__ void st_elem<double, double>(double* p, double v) { *p = v; }
 
-// ------------------------------------------------------------------ 8-element vector I/O
+// ------------------------------------------------------------------ streaming 16-byte I/O
 // Streaming (read-once) 128-bit loads that do not allocate in L1, and streaming stores.
 __device__ __forceinline__ uint4 ld_stream_u4(const void* p) {
   uint4 r;
@@ -53,54 +53,29 @@ __device__ __forceinline__ void st_stream_u4(void* p, uint4 v) {
                : "memory");
 }
 
-__device__ __forceinline__ void load8(const float* p, float (&o)[8]) {
-  const uint4 a = ld_stream_u4(p), b = ld_stream_u4(p + 4);
-  o[0] = __uint_as_float(a.x); o[1] = __uint_as_float(a.y);
-  o[2] = __uint_as_float(a.z); o[3] = __uint_as_float(a.w);
-  o[4] = __uint_as_float(b.x); o[5] = __uint_as_float(b.y);
-  o[6] = __uint_as_float(b.z); o[7] = __uint_as_float(b.w);
-}
-__device__ __forceinline__ void load8(const __half* p, float (&o)[8]) {
-  const uint4 a = ld_stream_u4(p);
-  const uint32_t w[4] = {a.x, a.y, a.z, a.w};
+// ------------------------------------------------------------------ N-element vector I/O
+// N elements of T as 16-byte streaming loads / stores (N * sizeof(T) a multiple of 16).
+template <int N, class T>
+__device__ __forceinline__ void load_vec(const T* p, T (&o)[N]) {
+  static_assert((N * sizeof(T)) % 16 == 0, "whole 16-byte vectors");
+  constexpr int V = N * sizeof(T) / 16;
+  uint4 raw[V];
 #pragma unroll
-  for (int i = 0; i < 4; i++) {
-    const float2 f = __half22float2(*reinterpret_cast<const __half2*>(&w[i]));
-    o[2 * i] = f.x;
-    o[2 * i + 1] = f.y;
-  }
-}
-__device__ __forceinline__ void load8(const __nv_bfloat16* p, float (&o)[8]) {
-  const uint4 a = ld_stream_u4(p);
-  const uint32_t w[4] = {a.x, a.y, a.z, a.w};
+  for (int v = 0; v < V; v++) raw[v] = ld_stream_u4(reinterpret_cast<const char*>(p) + 16 * v);
+  const T* e = reinterpret_cast<const T*>(raw);
 #pragma unroll
-  for (int i = 0; i < 4; i++) {
-    const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w[i]));
-    o[2 * i] = f.x;
-    o[2 * i + 1] = f.y;
-  }
+  for (int i = 0; i < N; i++) o[i] = e[i];
 }
-__device__ __forceinline__ void load8(const double* p, double (&o)[8]) {
+template <int N, class T>
+__device__ __forceinline__ void store_vec(T* p, const T (&v)[N]) {
+  static_assert((N * sizeof(T)) % 16 == 0, "whole 16-byte vectors");
+  constexpr int V = N * sizeof(T) / 16;
+  uint4 raw[V];
+  T* e = reinterpret_cast<T*>(raw);
 #pragma unroll
-  for (int i = 0; i < 4; i++) {
-    const uint4 a = ld_stream_u4(p + 2 * i);
-    o[2 * i] = __hiloint2double(a.y, a.x);
-    o[2 * i + 1] = __hiloint2double(a.w, a.z);
-  }
-}
-__device__ __forceinline__ void store8(float* p, const float (&v)[8]) {
-  st_stream_u4(p, make_uint4(__float_as_uint(v[0]), __float_as_uint(v[1]),
-                             __float_as_uint(v[2]), __float_as_uint(v[3])));
-  st_stream_u4(p + 4, make_uint4(__float_as_uint(v[4]), __float_as_uint(v[5]),
-                                 __float_as_uint(v[6]), __float_as_uint(v[7])));
-}
-__device__ __forceinline__ void store8(double* p, const double (&v)[8]) {
+  for (int i = 0; i < N; i++) e[i] = v[i];
 #pragma unroll
-  for (int i = 0; i < 4; i++) {
-    st_stream_u4(p + 2 * i, make_uint4(__double2loint(v[2 * i]), __double2hiint(v[2 * i]),
-                                       __double2loint(v[2 * i + 1]),
-                                       __double2hiint(v[2 * i + 1])));
-  }
+  for (int w = 0; w < V; w++) st_stream_u4(reinterpret_cast<char*>(p) + 16 * w, raw[w]);
 }
 
 // ------------------------------------------------------------------ hardware approximations
@@ -114,6 +89,11 @@ __device__ __forceinline__ float rcp_approx(float x) {
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
   return r;
 }
+__device__ __forceinline__ float rsqrt_approx(float x) {
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
 
 // ------------------------------------------------------------------ Kubelka-Munk
 // Reflectance of a layer (K, S, thickness d) over a substrate of reflectance R0, with the
@@ -123,35 +103,30 @@ __device__ __forceinline__ float rcp_approx(float x) {
 // FP32 evaluation, rearranged to avoid cancellation and to need 3 MUFU operations:
 //   with b = sqrt(a^2 - 1), a = 1 + K/S, x = b S d, and beta = S b = sqrt(K (2S + K)),
 //   A = S (1 - R0) - R0 K, B = S (1 - R0) + K, e = exp(-2x):
-//     R = (A (1 - e) + R0 beta (1 + e)) / (B (1 - e) + beta (1 + e))
-//   and for |x| < 0.05, with g = x coth x = 1 + x^2/3 - x^4/45 (+ O(x^6) < 4e-11):
-//     R = (A d + R0 g) / (B d + g)
+//     R = (A u + R0 w) / (B u + w),   (u, w) = (1 - e, beta (1 + e))
+//   and for x < 0.05, with g = x coth x = 1 + x^2/3 - x^4/45 (+ O(x^6) < 4e-11):
+//     (u, w) = (d, g)
 // Both are the reference's (1 - R0 (a - b coth x)) / (a - R0 + b coth x) multiplied through
 // by S (1 - e) or by S d / g. The series form is finite at K = 0, where the reference's
-// 0 * coth(0) is NaN. Physical inputs (K, S >= 0, d >= 0) are assumed.
+// 0 * coth(0) is NaN. Branch-free: both forms are evaluated and selected. Physical inputs
+// (K, S >= 0, d >= 0) are assumed.
 __device__ __forceinline__ float km_reflectance(float K, float S, float R0, float d) {
   constexpr float kEps = 2.220446049250313e-12f;  // 1e4 * DBL_EPSILON
-  if (fabsf(d) < kEps) return R0;
   S = fabsf(S) > kEps ? S : 1e-11f;
-  const float beta = sqrtf(fmaxf(K * (2.0f * S + K), 0.0f));
+  const float q = fmaxf(K * (2.0f * S + K), 1e-30f);
+  const float beta = q * rsqrt_approx(q);
   const float x = beta * d;
   const float omr = 1.0f - R0;
   const float A = fmaf(S, omr, -R0 * K);
   const float B = fmaf(S, omr, K);
-  float num, den;
-  if (x < 0.05f) {
-    const float x2 = x * x;
-    const float g = fmaf(x2, fmaf(x2, -1.0f / 45.0f, 1.0f / 3.0f), 1.0f);
-    num = fmaf(A, d, R0 * g);
-    den = fmaf(B, d, g);
-  } else {
-    const float e = ex2_approx(-2.8853900817779268f * x);  // exp(-2x) = 2^(-2x log2 e)
-    const float u = 1.0f - e;
-    const float v = beta * (1.0f + e);
-    num = fmaf(A, u, R0 * v);
-    den = fmaf(B, u, v);
-  }
-  return __fdividef(num, den);
+  const float e = ex2_approx(-2.8853900817779268f * x);  // exp(-2x) = 2^(-2x log2 e)
+  const float x2 = x * x;
+  const float g = fmaf(x2, fmaf(x2, -1.0f / 45.0f, 1.0f / 3.0f), 1.0f);
+  const bool series = x < 0.05f;
+  const float u = series ? d : 1.0f - e;
+  const float w = series ? g : beta * (1.0f + e);
+  const float r = fmaf(A, u, R0 * w) * rcp_approx(fmaf(B, u, w));
+  return fabsf(d) < kEps ? R0 : r;
 }
 
 // painty's coth (painty/core/Math.hxx:157-169) and ComputeReflectance in double, in the

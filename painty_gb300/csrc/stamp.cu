@@ -86,7 +86,7 @@ struct StampArgs {
   TK* sK[3];  // pickup source: snapshot planes, or the canvas planes without a snapshot
   TK* sS[3];
   TV* sV;
-  M* pK[3];  // pickup map, S*S per plane
+  M* pK[3];  // pickup map in global memory, S*S per plane (the brush's state)
   M* pS[3];
   M* pV;
   const M* footprint;  // F*F
@@ -95,23 +95,35 @@ struct StampArgs {
   int32_t rows, cols;
   int64_t pitch;
   int32_t F, S, wr;
+  // Stamp pixels with dc^2 + dr^2 > support2 map to cells whose footprint is 0 (the rotated
+  // and rounded cell lies within 0.71 px of the rotated point) and change nothing.
+  int32_t support2;
   double radius;
   M pickupRate, depositionRate, capacity;
   M paintK[3], paintS[3];
   int32_t use_snapshot;
-  int* owner_global;  // S*S ints when the owner table does not fit in shared memory
+  // Snapshot dirty map (rows x pitch bytes): 1 where the snapshot may differ from the canvas.
+  // The ring refresh copies only dirty pixels (copying an equal pixel is a no-op); pixels a
+  // stamp changes are marked. NULL: refresh the whole ring.
+  uint8_t* dirty;
+  int32_t pickup_zero;    // the map starts cleared (a dip or new radius since the last run)
+  int32_t pickup_smem;    // stage the pickup map in shared memory for the launch
+  int32_t footprint_smem; // stage the footprint in shared memory
+  int* owner_global;      // S*S ints when the owner table does not fit in shared memory
   unsigned* status;
 };
 
-struct StampShared {
+constexpr int kParamChunk = 32;  // stamps whose parameters are derived together
+
+struct StampParams {
   double cx, cy, c, s;
   float cf, sf;
   int tl[2], br[2], tla[2], bra[2];
-  int c0, r0;  // first index of the duplicated column / row, -1 if none
 };
 
-// Reference map coordinate round(fl(fl(u*c - v*s) + w)) (sgn = +1) or
-// round(fl(fl(u*s + v*c) + w)) style, given as a = u*ca, b = v*cb in the caller's order.
+// Reference map coordinate round(fl(fl(u*ca -/+ v*cb) + w)): the FP32 value `fast` decides
+// unless it lies within 2e-4 of a rounding tie (its error is below 4e-5), then the
+// reference's double operations are repeated.
 __device__ __forceinline__ int map_coord(float fast, int u, double ca, int v, double cb,
                                          bool minus, int w) {
   const float fr = fast - floorf(fast);
@@ -122,47 +134,80 @@ __device__ __forceinline__ int map_coord(float fast, int u, double ca, int v, do
   return static_cast<int>(round(__dadd_rn(r, static_cast<double>(w))));
 }
 
-template <class M>
-__device__ __forceinline__ void blend3(M va, const M (&a)[3], M vb, const M (&b)[3], M (&r)[3]) {
-  using A = Arith<M>;
-  const M tot = A::add(va, vb);
-  if (tot > M(0.001)) {
+// blend (FootprintBrush.hxx:331-340): (va a + vb b) / (va + vb) when va + vb > MinVolume.
+// FP64 divides as the reference; FP32 multiplies by the correctly rounded reciprocal.
+__device__ __forceinline__ void blend3(double va, const double (&a)[3], double vb,
+                                       const double (&b)[3], double (&r)[3]) {
+  const double tot = __dadd_rn(va, vb);
+  if (tot > 0.001) {
 #pragma unroll
-    for (int i = 0; i < 3; i++) r[i] = A::div(A::add(A::mul(va, a[i]), A::mul(vb, b[i])), tot);
+    for (int i = 0; i < 3; i++)
+      r[i] = __ddiv_rn(__dadd_rn(__dmul_rn(va, a[i]), __dmul_rn(vb, b[i])), tot);
+  } else {
+#pragma unroll
+    for (int i = 0; i < 3; i++) r[i] = a[i];
+  }
+}
+__device__ __forceinline__ void blend3(float va, const float (&a)[3], float vb,
+                                       const float (&b)[3], float (&r)[3]) {
+  const float tot = va + vb;
+  if (tot > 0.001f) {
+    const float inv = __frcp_rn(tot);
+#pragma unroll
+    for (int i = 0; i < 3; i++) r[i] = fmaf(va, a[i], vb * b[i]) * inv;
   } else {
 #pragma unroll
     for (int i = 0; i < 3; i++) r[i] = a[i];
   }
 }
 
-// pickupPaint then depositPaint for one stamp pixel (FootprintBrush.hxx:349-431)
-template <class TK, class TV>
-__device__ __forceinline__ void process_pixel(const StampArgs<TK, TV>& a, int xc, int yc, int mx,
-                                              int my) {
-  using M = typename MathOf<TK>::type;
+// Plane p (K r,g,b, S r,g,b, V) of the pickup map in global memory.
+template <class TK, class TV, class M>
+__device__ __forceinline__ M* pickup_plane(const StampArgs<TK, TV>& a, int p) {
+  return p < 3 ? a.pK[p] : (p < 6 ? a.pS[p - 3] : a.pV);
+}
+
+// pickupPaint then depositPaint for one stamp pixel (FootprintBrush.hxx:349-431); fp > 0.
+// PS: the pickup map is staged in shared memory at `pbase` (7 planes `cells` apart).
+template <bool PS, class TK, class TV, class M>
+__device__ __forceinline__ void process_pixel(const StampArgs<TK, TV>& a, M* pbase, int cells,
+                                              M fp, int64_t c, int m) {
   using A = Arith<M>;
-  const M fp = (my < a.F && mx < a.F) ? a.footprint[my * a.F + mx] : M(0);
-  if (!(fp > M(0))) return;
-  const int64_t c = static_cast<int64_t>(yc) * a.pitch + xc;
-  const int m = my * a.S + mx;
-  M vp = a.pV[m];
-  M kp[3], sp[3];
+  auto cell = [&](int p) -> M& {
+    if constexpr (PS) return pbase[p * cells + m];
+    else return pickup_plane<TK, TV, M>(a, p)[m];
+  };
+  // independent loads first: pickup cell, pickup source, canvas pixel
+  M vp = cell(6);
+  M kp[3], sp[3], ck[3], cs[3];
 #pragma unroll
   for (int i = 0; i < 3; i++) {
-    kp[i] = a.pK[i][m];
-    sp[i] = a.pS[i][m];
+    kp[i] = cell(i);
+    sp[i] = cell(3 + i);
+    ck[i] = ld_elem<M>(a.cK[i] + c);
+    cs[i] = ld_elem<M>(a.cS[i] + c);
   }
-  // pickupPaint
   const M vsrc = ld_elem<M>(a.sV + c);
+  M vcan = ld_elem<M>(a.cV + c);
+  // pickupPaint
   const M vleave = A::mul(A::mul(a.pickupRate, vsrc), fp);
   bool pk_changed = false;
   if (vleave > M(0.001)) {
     st_elem<M>(a.sV + c, A::sub(vsrc, vleave));
     M ks[3], ss[3], nk[3], ns[3];
+    if (a.use_snapshot) {
 #pragma unroll
-    for (int i = 0; i < 3; i++) {
-      ks[i] = ld_elem<M>(a.sK[i] + c);
-      ss[i] = ld_elem<M>(a.sS[i] + c);
+      for (int i = 0; i < 3; i++) {
+        ks[i] = ld_elem<M>(a.sK[i] + c);
+        ss[i] = ld_elem<M>(a.sS[i] + c);
+      }
+    } else {  // the pickup source is the canvas itself
+#pragma unroll
+      for (int i = 0; i < 3; i++) {
+        ks[i] = ck[i];
+        ss[i] = cs[i];
+      }
+      vcan = ld_elem<M>(a.cV + c);  // the stored remainder
     }
     blend3(vp, kp, vleave, ks, nk);
     blend3(vp, sp, vleave, ss, ns);
@@ -181,22 +226,16 @@ __device__ __forceinline__ void process_pixel(const StampArgs<TK, TV>& a, int xc
   blend3(vp, kp, vfree, a.paintK, ksrc);
   blend3(vp, sp, vfree, a.paintS, ssrc);
   const M pleave = A::mul(A::mul(a.depositionRate, vp), fp);
-  a.pV[m] = A::sub(vp, pleave);
+  cell(6) = A::sub(vp, pleave);
   if (pk_changed) {
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-      a.pK[i][m] = kp[i];
-      a.pS[i][m] = sp[i];
+      cell(i) = kp[i];
+      cell(3 + i) = sp[i];
     }
   }
-  const M vcan = ld_elem<M>(a.cV + c);
   const M vb = A::mul(a.capacity, fp);
-  M ck[3], cs[3], nk[3], ns[3];
-#pragma unroll
-  for (int i = 0; i < 3; i++) {
-    ck[i] = ld_elem<M>(a.cK[i] + c);
-    cs[i] = ld_elem<M>(a.cS[i] + c);
-  }
+  M nk[3], ns[3];
   blend3(vb, ksrc, vcan, ck, nk);
   blend3(vb, ssrc, vcan, cs, ns);
 #pragma unroll
@@ -205,171 +244,383 @@ __device__ __forceinline__ void process_pixel(const StampArgs<TK, TV>& a, int xc
     st_elem<M>(a.cS[i] + c, ns[i]);
   }
   st_elem<M>(a.cV + c, A::add(vb, vcan));
+  if (a.dirty) a.dirty[c] = 1;
 }
 
 struct PixelInfo {
   int xc, yc, mx, my;
-  bool valid;
+  bool live;  // inside canvas and map, and a positive footprint: the pixel changes state
 };
 
-template <class TK, class TV>
-__device__ __forceinline__ PixelInfo pixel_info(const StampArgs<TK, TV>& a,
-                                                const StampShared& sh, const int* xs,
-                                                const int* ys, int idx) {
+// Stamp pixel (row, col) of the F x F box: canvas pixel, pickup-map cell, footprint height.
+template <class TK, class TV, class M>
+__device__ __forceinline__ PixelInfo pixel_info(const StampArgs<TK, TV>& a, const StampParams& sp,
+                                                const int* xs, const int* ys, const M* fps,
+                                                int row, int col, M* fp_out) {
   PixelInfo p;
-  const int row = idx / a.F, col = idx - (idx / a.F) * a.F;
   const int dr = row - a.wr, dc = col - a.wr;
   p.xc = xs[col];
   p.yc = ys[row];
   const float dcf = static_cast<float>(dc), drf = static_cast<float>(dr);
   const float wrf = static_cast<float>(a.wr);
-  const float fx = fmaf(-drf, sh.sf, dcf * sh.cf) + wrf;  // col*cos - row*sin + wr
-  const float fy = fmaf(drf, sh.cf, dcf * sh.sf) + wrf;   // col*sin + row*cos + hr
-  p.mx = map_coord(fx, dc, sh.c, dr, sh.s, true, a.wr);
-  p.my = map_coord(fy, dc, sh.s, dr, sh.c, false, a.wr);
-  p.valid = p.yc >= 0 && p.xc >= 0 && p.xc < a.cols && p.yc < a.rows && p.my >= 0 &&
-            p.mx >= 0 && p.mx < a.S && p.my < a.S;
+  const float fx = fmaf(-drf, sp.sf, dcf * sp.cf) + wrf;  // col*cos - row*sin + wr
+  const float fy = fmaf(drf, sp.cf, dcf * sp.sf) + wrf;   // col*sin + row*cos + hr
+  p.mx = map_coord(fx, dc, sp.c, dr, sp.s, true, a.wr);
+  p.my = map_coord(fy, dc, sp.s, dr, sp.c, false, a.wr);
+  const bool inside = p.yc >= 0 && p.xc >= 0 && p.xc < a.cols && p.yc < a.rows && p.my >= 0 &&
+                      p.mx >= 0 && p.mx < a.S && p.my < a.S;
+  M fp = M(0);
+  if (inside && p.mx < a.F && p.my < a.F) fp = fps[p.my * a.F + p.mx];
+  *fp_out = fp;
+  p.live = inside && fp > M(0);
   return p;
 }
 
-// Earlier pixels on the same canvas pixel must be done (left/top edge duplicates).
-__device__ __forceinline__ bool canvas_ready(const StampShared& sh, const uint8_t* done_c0,
-                                             const uint8_t* done_r0, int row, int col) {
+// Earlier pixels on the same canvas pixel (left/top edge duplicates) finished in an earlier
+// wave. done_c[row] / done_r[col] hold the 1-based wave in which pixel (c0, row) / (col, r0)
+// finished (c0, r0: the first of the duplicated column / row), 0 while pending.
+__device__ __forceinline__ bool canvas_ready(const int* xs, const int* ys, int F,
+                                             const uint16_t* done_c, const uint16_t* done_r,
+                                             int row, int col, int wave) {
+  auto fin = [wave](uint16_t d) { return d != 0 && d <= wave; };
+  const bool dupx_prev = col > 0 && xs[col - 1] == xs[col];  // col == c0 + 1
+  const bool dupy_prev = row > 0 && ys[row - 1] == ys[row];  // row == r0 + 1
   bool ok = true;
-  if (sh.c0 >= 0 && col == sh.c0 + 1) ok = ok && done_c0[row];
-  if (sh.r0 >= 0 && row == sh.r0 + 1) {
-    ok = ok && done_r0[col];
-    if (sh.c0 >= 0 && col == sh.c0) ok = ok && done_r0[sh.c0 + 1];
-    if (sh.c0 >= 0 && col == sh.c0 + 1) ok = ok && done_r0[sh.c0];
+  if (dupx_prev) ok = ok && fin(done_c[row]);
+  if (dupy_prev) {
+    ok = ok && fin(done_r[col]);
+    if (col + 1 < F && xs[col] == xs[col + 1]) ok = ok && fin(done_r[col + 1]);  // up-right
+    if (dupx_prev) ok = ok && fin(done_r[col - 1]);                                // up-left
   }
   return ok;
 }
 
+__device__ __forceinline__ void mark_done(const int* xs, const int* ys, int F, uint16_t* done_c,
+                                          uint16_t* done_r, int row, int col, uint16_t v) {
+  if (col + 1 < F && xs[col] == xs[col + 1]) done_c[row] = v;
+  if (row + 1 < F && ys[row] == ys[row + 1]) done_r[col] = v;
+}
+
+// FootprintBrush.hxx:291-305 box and snapshot-ring bounds, in the reference's double ops
+__device__ __forceinline__ StampParams derive_params(const StampRec& st, int wr, double radius,
+                                                     int rows, int cols) {
+  StampParams p;
+  p.cx = st.cx;
+  p.cy = st.cy;
+  p.c = st.c;
+  p.s = st.s;
+  p.cf = static_cast<float>(st.c);
+  p.sf = static_cast<float>(st.s);
+  const double w = wr;
+  p.tl[0] = static_cast<int>(__dsub_rn(st.cx, w));
+  p.tl[1] = static_cast<int>(__dsub_rn(st.cy, w));
+  p.br[0] = static_cast<int>(__dadd_rn(st.cx, w));
+  p.br[1] = static_cast<int>(__dadd_rn(st.cy, w));
+  p.tla[0] = max(static_cast<int>(__dsub_rn(__dsub_rn(st.cx, w), radius)), 0);
+  p.tla[1] = max(static_cast<int>(__dsub_rn(__dsub_rn(st.cy, w), radius)), 0);
+  p.bra[0] = min(static_cast<int>(__dadd_rn(__dadd_rn(st.cx, w), radius)), cols - 1);
+  p.bra[1] = min(static_cast<int>(__dadd_rn(__dadd_rn(st.cy, w), radius)), rows - 1);
+  return p;
+}
+
+__host__ __device__ constexpr size_t align_up(size_t x, size_t a) {
+  return (x + a - 1) / a * a;
+}
+
+// Dynamic shared memory layout of stamp_kernel (all offsets 16-byte aligned).
+struct StampSmem {
+  size_t fp, pick, own, xs, ys, done_c, done_r, queue, total;
+};
+constexpr int kRefreshQueue = 2048;  // snapshot-refresh queue entries (canvas offsets)
+template <class M>
+__host__ __device__ inline StampSmem stamp_smem_layout(int F, int S, bool fp_smem,
+                                                       bool pick_smem, bool own_smem) {
+  StampSmem L{};
+  size_t o = 0;
+  L.fp = o;
+  if (fp_smem) o = align_up(o + size_t(F) * F * sizeof(M), 16);
+  L.pick = o;
+  if (pick_smem) o = align_up(o + size_t(7) * S * S * sizeof(M), 16);
+  L.own = o;
+  if (own_smem) o = align_up(o + size_t(S) * S * sizeof(int), 16);
+  L.xs = o;
+  o = align_up(o + size_t(F) * sizeof(int), 16);
+  L.ys = o;
+  o = align_up(o + size_t(F) * sizeof(int), 16);
+  L.done_c = o;
+  o = align_up(o + size_t(F) * sizeof(uint16_t), 16);
+  L.done_r = o;
+  o = align_up(o + size_t(F) * sizeof(uint16_t), 16);
+  L.queue = o;
+  o = align_up(o + size_t(kRefreshQueue) * sizeof(int), 16);
+  L.total = o;
+  return L;
+}
+
+constexpr int kEpochMax = 32767;  // owner keys: ((kEpochMax - epoch) << 16) | pixel index
+constexpr int kWarps = kStampThreads / 32;
+
+// Snapshot refresh, pass 1: scan the dirty bytes of ring row segment [lo, hi] four at a
+// time (one 32-bit word per lane) and queue the dirty pixels (canvas offsets) in shared
+// memory; a pixel's dirty byte is cleared only once it is queued, so entries past the queue's
+// end stay dirty (and flag an overflow) for the next scan. Requires a dirty map.
 template <class TK, class TV>
+__device__ __forceinline__ void scan_segment(const StampArgs<TK, TV>& a, int row, int lo, int hi,
+                                             int lane, int* queue, int* qcount, int* qover) {
+  const int64_t rb = static_cast<int64_t>(row) * a.pitch;
+  for (int w0 = (lo & ~3); w0 <= hi; w0 += 4 * 32) {
+    const int w = w0 + 4 * lane;
+    uint32_t word = 0, take = 0;
+    if (w <= hi) {
+      word = *reinterpret_cast<const uint32_t*>(a.dirty + rb + w);
+#pragma unroll
+      for (int b = 0; b < 4; b++) {
+        const int col = w + b;
+        if (col >= lo && col <= hi && ((word >> (8 * b)) & 0xffu)) take |= 1u << b;
+      }
+    }
+    const int n = __popc(take);
+    int incl = n;  // warp inclusive prefix sum of the counts
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d) incl += v;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    int base = 0;
+    if (lane == 31 && total > 0) base = atomicAdd(qcount, total);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    int slot = base + incl - n;
+    uint32_t cleared = word;
+    for (int b = 0; b < 4; b++) {
+      if (!((take >> b) & 1u)) continue;
+      if (slot < kRefreshQueue) {
+        queue[slot] = static_cast<int>(rb + w + b);
+        cleared &= ~(0xffu << (8 * b));
+      } else {
+        *qover = 1;
+      }
+      slot++;
+    }
+    if (take && cleared != word) *reinterpret_cast<uint32_t*>(a.dirty + rb + w) = cleared;
+  }
+}
+
+// Snapshot refresh without a dirty map: copy every pixel of the segment.
+template <class TK, class TV>
+__device__ __forceinline__ void copy_segment(const StampArgs<TK, TV>& a, int row, int lo, int hi,
+                                             int lane) {
+  const int64_t rb = static_cast<int64_t>(row) * a.pitch;
+  for (int col = lo + lane; col <= hi; col += 32) {
+    const int64_t o = rb + col;
+#pragma unroll
+    for (int ch = 0; ch < 3; ch++) {
+      a.sK[ch][o] = a.cK[ch][o];
+      a.sS[ch][o] = a.cS[ch][o];
+    }
+    a.sV[o] = a.cV[o];
+  }
+}
+
+// Snapshot refresh, pass 2: copy the queued pixels canvas -> snapshot (7 planes).
+template <class TK, class TV>
+__device__ __forceinline__ void copy_queued(const StampArgs<TK, TV>& a, const int* queue,
+                                            int count, int tid, int T) {
+  for (int q = tid; q < count; q += T) {
+    const int64_t o = queue[q];
+    TK k[3], s[3];
+#pragma unroll
+    for (int ch = 0; ch < 3; ch++) {
+      k[ch] = a.cK[ch][o];
+      s[ch] = a.cS[ch][o];
+    }
+    const TV v = a.cV[o];
+#pragma unroll
+    for (int ch = 0; ch < 3; ch++) {
+      a.sK[ch][o] = k[ch];
+      a.sS[ch][o] = s[ch];
+    }
+    a.sV[o] = v;
+  }
+}
+
+// The ring of a stamp: rows of the grown box, the strict interior of the box excepted
+// (FootprintBrush.hxx:307-318); one warp per row. With a dirty map the dirty pixels are
+// queued (copied by copy_queued); without one every ring pixel is copied here.
+template <class TK, class TV>
+__device__ __forceinline__ void scan_ring(const StampArgs<TK, TV>& a, const StampParams& sp,
+                                          int warp, int lane, int nwarps, int* queue,
+                                          int* qcount, int* qover) {
+  for (int row = sp.tla[1] + warp; row <= sp.bra[1]; row += nwarps) {
+    const bool interior_row = row > sp.tl[1] && row < sp.br[1];
+    const int lo0 = sp.tla[0], hi0 = interior_row ? min(sp.tl[0], sp.bra[0]) : sp.bra[0];
+    const int lo1 = max(sp.br[0], sp.tla[0]), hi1 = interior_row ? sp.bra[0] : -1;
+    if (a.dirty) {
+      scan_segment(a, row, lo0, hi0, lane, queue, qcount, qover);
+      scan_segment(a, row, lo1, hi1, lane, queue, qcount, qover);
+    } else {
+      copy_segment(a, row, lo0, hi0, lane);
+      copy_segment(a, row, lo1, hi1, lane);
+    }
+  }
+}
+
+// One CTA applies the stamps in order. Pixel slots: warp w owns box rows w, w+32, ...; lane l
+// owns columns l, l+32, ...; slot j = jr * NC + jc (jr-th row, jc-th column of the thread).
+// PS: pickup map staged in shared memory. BIG: footprint and owner table in global memory
+// (maps too large for shared memory); otherwise both are in shared memory.
+template <bool PS, bool BIG, class TK, class TV>
 __global__ void __launch_bounds__(kStampThreads, 1) stamp_kernel(const __grid_constant__ StampArgs<TK, TV> a) {
+  using M = typename MathOf<TK>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ StampShared sh;
+  __shared__ StampParams sparams[kParamChunk];
   const int tid = threadIdx.x;
   const int T = blockDim.x;
+  const int warp = tid >> 5, lane = tid & 31;
   const int F = a.F, S = a.S;
   const int npix = F * F;
-  int* own = a.owner_global ? a.owner_global : reinterpret_cast<int*>(smem_raw);
-  const size_t own_bytes = a.owner_global ? 0 : static_cast<size_t>(S) * S * sizeof(int);
-  int* xs = reinterpret_cast<int*>(smem_raw + own_bytes);
-  int* ys = xs + F;
-  uint8_t* done_c0 = reinterpret_cast<uint8_t*>(ys + F);
-  uint8_t* done_r0 = done_c0 + F;
+  const int cells = S * S;
+  const int NC = (F + 31) / 32;
+  const StampSmem L = stamp_smem_layout<M>(F, S, !BIG, PS, !BIG);
+  const M* fps = !BIG ? reinterpret_cast<M*>(smem_raw + L.fp) : a.footprint;
+  M* pbase = PS ? reinterpret_cast<M*>(smem_raw + L.pick) : nullptr;
+  int* own = BIG ? a.owner_global : reinterpret_cast<int*>(smem_raw + L.own);
+  int* xs = reinterpret_cast<int*>(smem_raw + L.xs);
+  int* ys = reinterpret_cast<int*>(smem_raw + L.ys);
+  uint16_t* done_c = reinterpret_cast<uint16_t*>(smem_raw + L.done_c);
+  uint16_t* done_r = reinterpret_cast<uint16_t*>(smem_raw + L.done_r);
+  int* queue = reinterpret_cast<int*>(smem_raw + L.queue);
+  __shared__ int s_qcount, s_qover;
+
+  // launch prologue: footprint and pickup map staged, owner table reset
+  if (!BIG) {
+    M* f = reinterpret_cast<M*>(smem_raw + L.fp);
+    for (int i = tid; i < npix; i += T) f[i] = a.footprint[i];
+  }
+  for (int i = tid; i < 7 * cells; i += T) {
+    const int p = i / cells, m = i - p * cells;
+    if (PS)
+      pbase[i] = a.pickup_zero ? M(0) : pickup_plane<TK, TV, M>(a, p)[m];
+    else if (a.pickup_zero)
+      pickup_plane<TK, TV, M>(a, p)[m] = M(0);
+  }
+  for (int i = tid; i < cells; i += T) own[i] = INT_MAX;
+  if (tid == 0) {
+    s_qcount = 0;
+    s_qover = 0;
+  }
+  int epoch = 0;
 
   for (int64_t k = 0; k < a.n; k++) {
-    if (tid == 0) {
-      const StampRec st = a.stamps[k];
-      sh.cx = st.cx;
-      sh.cy = st.cy;
-      sh.c = st.c;
-      sh.s = st.s;
-      sh.cf = static_cast<float>(st.c);
-      sh.sf = static_cast<float>(st.s);
-      const double w = a.wr;
-      // FootprintBrush.hxx:291-305
-      sh.tl[0] = static_cast<int>(__dsub_rn(st.cx, w));
-      sh.tl[1] = static_cast<int>(__dsub_rn(st.cy, w));
-      sh.br[0] = static_cast<int>(__dadd_rn(st.cx, w));
-      sh.br[1] = static_cast<int>(__dadd_rn(st.cy, w));
-      sh.tla[0] = max(static_cast<int>(__dsub_rn(__dsub_rn(st.cx, w), a.radius)), 0);
-      sh.tla[1] = max(static_cast<int>(__dsub_rn(__dsub_rn(st.cy, w), a.radius)), 0);
-      sh.bra[0] = min(static_cast<int>(__dadd_rn(__dadd_rn(st.cx, w), a.radius)), a.cols - 1);
-      sh.bra[1] = min(static_cast<int>(__dadd_rn(__dadd_rn(st.cy, w), a.radius)), a.rows - 1);
-      sh.c0 = -1;
-      sh.r0 = -1;
-    }
-    __syncthreads();
-    // canvas coordinates per column / row; owner table reset; done flags reset
-    for (int i = tid; i < F; i += T) {
-      xs[i] = static_cast<int>(__dadd_rn(static_cast<double>(i - a.wr), sh.cx));
-      ys[i] = static_cast<int>(__dadd_rn(static_cast<double>(i - a.wr), sh.cy));
-      done_c0[i] = 0;
-      done_r0[i] = 0;
-    }
-    for (int i = tid; i < S * S; i += T) own[i] = INT_MAX;
-    // snapshot refresh around the footprint box (FootprintBrush.hxx:307-318)
-    if (a.use_snapshot) {
-      const int w = sh.bra[0] - sh.tla[0] + 1, h = sh.bra[1] - sh.tla[1] + 1;
-      if (w > 0 && h > 0) {
-        const int total = w * h;
-        for (int i = tid; i < total; i += T) {
-          const int row = sh.tla[1] + i / w, col = sh.tla[0] + i % w;
-          if (row > sh.tl[1] && row < sh.br[1] && col > sh.tl[0] && col < sh.br[0]) continue;
-          const int64_t o = static_cast<int64_t>(row) * a.pitch + col;
-#pragma unroll
-          for (int ch = 0; ch < 3; ch++) {
-            a.sK[ch][o] = a.cK[ch][o];
-            a.sS[ch][o] = a.cS[ch][o];
-          }
-          a.sV[o] = a.cV[o];
-        }
-      }
-    }
-    __syncthreads();
-    for (int i = tid; i + 1 < F; i += T) {
-      if (xs[i] == xs[i + 1]) sh.c0 = i;
-      if (ys[i] == ys[i + 1]) sh.r0 = i;
-    }
-    __syncthreads();
-    // first claim: every valid pixel bids for its map cell
-    uint64_t rem = 0;
-    for (int j = 0; j < kMaxPixelsPerThread; j++) {
-      const int idx = j * T + tid;
-      if (idx >= npix) break;
-      const PixelInfo p = pixel_info(a, sh, xs, ys, idx);
-      const int row = idx / F, col = idx - row * F;
-      if (p.valid) {
-        rem |= (1ull << j);
-        atomicMin(&own[p.my * S + p.mx], idx);
-      } else {
-        if (col == sh.c0) done_c0[row] = 1;
-        if (row == sh.r0) done_r0[col] = 1;
-      }
-    }
-    __syncthreads();
-    for (int wave = 0;; wave++) {
-      uint64_t processed = 0;
-      for (uint64_t bits = rem; bits; bits &= bits - 1) {
-        const int j = __ffsll(static_cast<long long>(bits)) - 1;
-        const int idx = j * T + tid;
-        const PixelInfo p = pixel_info(a, sh, xs, ys, idx);
-        const int row = idx / F, col = idx - row * F;
-        if (own[p.my * S + p.mx] == idx && canvas_ready(sh, done_c0, done_r0, row, col)) {
-          process_pixel(a, p.xc, p.yc, p.mx, p.my);
-          processed |= (1ull << j);
-        }
+    const int slot = static_cast<int>(k % kParamChunk);
+    if (slot == 0) {  // derive the next chunk of stamp parameters in parallel
+      __syncthreads();
+      const int64_t j = k + tid;
+      if (tid < kParamChunk && j < a.n)
+        sparams[tid] = derive_params(a.stamps[j], a.wr, a.radius, a.rows, a.cols);
+      if (epoch > kEpochMax - 2 * kMaxWaves) {  // owner keys about to wrap: reset
+        for (int i = tid; i < cells; i += T) own[i] = INT_MAX;
+        epoch = 0;
       }
       __syncthreads();
-      rem &= ~processed;
-      for (uint64_t bits = processed; bits; bits &= bits - 1) {
-        const int j = __ffsll(static_cast<long long>(bits)) - 1;
-        const int idx = j * T + tid;
-        const int row = idx / F, col = idx - row * F;
-        if (col == sh.c0) done_c0[row] = 1;
-        if (row == sh.r0) done_r0[col] = 1;
+    }
+    const StampParams& sp = sparams[slot];
+    // phase A: per column / row canvas coordinates (double, as the reference), done flags
+    // reset, snapshot ring scanned for dirty pixels
+    for (int i = tid; i < F; i += T) {
+      xs[i] = static_cast<int>(__dadd_rn(static_cast<double>(i - a.wr), sp.cx));
+      ys[i] = static_cast<int>(__dadd_rn(static_cast<double>(i - a.wr), sp.cy));
+      done_c[i] = 0;
+      done_r[i] = 0;
+    }
+    if (a.use_snapshot) scan_ring(a, sp, warp, lane, kWarps, queue, &s_qcount, &s_qover);
+    __syncthreads();
+    // phase B: queued snapshot copies; live pixels (inside the support disc, canvas and map,
+    // positive footprint) classified and bidding for their map cells (wave 1)
+    if (a.use_snapshot) copy_queued(a, queue, min(s_qcount, kRefreshQueue), tid, T);
+    int wave = 1;
+    int key_hi = (kEpochMax - epoch) << 16;
+    epoch++;
+    uint64_t rem = 0;
+    for (int row = warp, jr = 0; row < F; row += kWarps, jr++) {
+      const int dr = row - a.wr;
+      for (int col = lane, jc = 0; col < F; col += 32, jc++) {
+        const int dc = col - a.wr;
+        bool live = false;
+        if (dc * dc + dr * dr <= a.support2) {
+          M fp;
+          const PixelInfo p = pixel_info(a, sp, xs, ys, fps, row, col, &fp);
+          if (p.live) {
+            live = true;
+            atomicMin(&own[p.my * S + p.mx], key_hi | (row * F + col));
+          }
+        }
+        if (live)
+          rem |= 1ull << (jr * NC + jc);
+        else
+          mark_done(xs, ys, F, done_c, done_r, row, col, 1);  // done "before" wave 1
       }
-      for (uint64_t bits = rem; bits; bits &= bits - 1) {
-        const int j = __ffsll(static_cast<long long>(bits)) - 1;
-        const PixelInfo p = pixel_info(a, sh, xs, ys, j * T + tid);
-        own[p.my * S + p.mx] = INT_MAX;
-      }
-      const int any = __syncthreads_or(rem != 0);
-      if (!any) break;
-      if (wave + 1 >= kMaxWaves) {  // cannot happen; guards the loop bound
+    }
+    __syncthreads();
+    // The refresh queue overflowed: drain the rest before painting. Each round clears the
+    // dirty bytes of the pixels it queued, so the rounds end; the cap only guards the loop.
+    for (int round = 0; s_qover; round++) {
+      if (round > (sp.bra[1] - sp.tla[1] + 2) * (sp.bra[0] - sp.tla[0] + 2) / kRefreshQueue + 2) {
         if (tid == 0) atomicOr(a.status, kStatusWaveCap);
         break;
       }
-      for (uint64_t bits = rem; bits; bits &= bits - 1) {
-        const int j = __ffsll(static_cast<long long>(bits)) - 1;
-        const int idx = j * T + tid;
-        const PixelInfo p = pixel_info(a, sh, xs, ys, idx);
-        atomicMin(&own[p.my * S + p.mx], idx);
+      __syncthreads();
+      if (tid == 0) {
+        s_qcount = 0;
+        s_qover = 0;
       }
       __syncthreads();
+      scan_ring(a, sp, warp, lane, kWarps, queue, &s_qcount, &s_qover);
+      __syncthreads();
+      copy_queued(a, queue, min(s_qcount, kRefreshQueue), tid, T);
+      __syncthreads();
+    }
+    if (tid == 0) s_qcount = 0;
+    for (;;) {
+      for (uint64_t bits = rem; bits; bits &= bits - 1) {
+        const int j = __ffsll(static_cast<long long>(bits)) - 1;
+        const int row = warp + kWarps * (j / NC), col = lane + 32 * (j % NC);
+        M fp;
+        const PixelInfo p = pixel_info(a, sp, xs, ys, fps, row, col, &fp);
+        if (own[p.my * S + p.mx] == (key_hi | (row * F + col)) &&
+            canvas_ready(xs, ys, F, done_c, done_r, row, col, wave)) {
+          process_pixel<PS, TK, TV, M>(a, pbase, cells, fp,
+                                       static_cast<int64_t>(p.yc) * a.pitch + p.xc,
+                                       p.my * S + p.mx);
+          rem &= ~(1ull << j);
+          mark_done(xs, ys, F, done_c, done_r, row, col, static_cast<uint16_t>(wave + 1));
+        }
+      }
+      const int any = __syncthreads_or(rem != 0);
+      if (!any) break;
+      if (wave >= kMaxWaves) {  // cannot happen: the lowest remaining pixel always runs
+        if (tid == 0) atomicOr(a.status, kStatusWaveCap);
+        break;
+      }
+      wave++;
+      key_hi = (kEpochMax - epoch) << 16;
+      epoch++;
+      for (uint64_t bits = rem; bits; bits &= bits - 1) {  // bid for the map cell
+        const int j = __ffsll(static_cast<long long>(bits)) - 1;
+        const int row = warp + kWarps * (j / NC), col = lane + 32 * (j % NC);
+        M fp;
+        const PixelInfo p = pixel_info(a, sp, xs, ys, fps, row, col, &fp);
+        atomicMin(&own[p.my * S + p.mx], key_hi | (row * F + col));
+      }
+      __syncthreads();
+    }
+  }
+  // launch epilogue: the brush keeps its pickup map
+  if (PS) {
+    __syncthreads();
+    for (int i = tid; i < 7 * cells; i += T) {
+      const int p = i / cells, m = i - p * cells;
+      pickup_plane<TK, TV, M>(a, p)[m] = pbase[i];
     }
   }
 }
@@ -382,6 +633,7 @@ struct painty_brush {
   double radius = 0.0;  // FootprintBrush.hxx:437
   int32_t sizeMap = 0;  // :443
   int32_t F = 0;
+  int32_t support2 = 0;  // squared stamp-pixel radius beyond which the footprint is zero
   std::vector<double> full;
   int32_t fh = 0, fw = 0;
   std::vector<double> footprint;  // F*F
@@ -404,6 +656,11 @@ struct painty_brush {
   // snapshot (FootprintBrush.hxx:471): canvas-sized layer, allocated at first use
   painty_layer snapshot;
   bool has_snapshot = false;
+  // snapshot dirty map (canvas rows x pitch bytes) and the canvas state it describes
+  void* d_dirty = nullptr;
+  size_t d_dirty_bytes = 0;
+  uint64_t dirty_canvas = 0;
+  uint64_t dirty_version = 0;
   void* d_stamps = nullptr;
   size_t d_stamps_bytes = 0;
   unsigned* d_status = nullptr;
@@ -431,6 +688,21 @@ double interpolate(const double* in, int rows, int cols, double px, double py) {
          (in[y1 * cols + x0] * (1.0 - a) + in[y1 * cols + x1] * a) * c;
 }
 
+// Squared radius bound (in stamp pixels) of the footprint's support: a stamp pixel at
+// distance d from the centre maps to a cell at distance >= d - sqrt(0.5) (rotation keeps d,
+// rounding moves each coordinate by <= 0.5), so pixels with d > R + 0.71 see a zero footprint.
+int32_t support_radius2(const double* fp, int F) {
+  const int wr = (F - 1) / 2;
+  double R = -1.0;
+  for (int i = 0; i < F; i++)
+    for (int j = 0; j < F; j++)
+      if (fp[static_cast<size_t>(i) * F + j] > 0.0)
+        R = std::max(R, std::sqrt(double((i - wr) * (i - wr) + (j - wr) * (j - wr))));
+  if (R < 0.0) return -1;  // an all-zero footprint: every stamp pixel is a no-op
+  const double b = R + 0.7072;
+  return static_cast<int32_t>(std::floor(b * b)) + 1;
+}
+
 // FootprintBrush::setRadius (FootprintBrush.hxx:46-63). The footprint image is resampled to
 // width x width by a pixel-centre aligned bilinear resample (in place of OpenCV's
 // Lanczos-4 resize) and zero-padded by (sizeMap - width) / 2 on each side.
@@ -448,6 +720,7 @@ void set_radius(painty_brush* b, double radius) {
       b->footprint[static_cast<size_t>(i + pad) * b->F + (j + pad)] =
         interpolate(b->full.data(), b->fh, b->fw, (static_cast<double>(j) + 0.5) * sx - 0.5,
                     (static_cast<double>(i) + 0.5) * sy - 0.5);
+  b->support2 = support_radius2(b->footprint.data(), b->F);
   b->footprint_stale = true;
   b->pickup_clear = true;
 }
@@ -462,15 +735,39 @@ void ensure(void** p, size_t* cap, size_t bytes) {
 }
 
 int max_dyn_smem() {
-  int dev = 0, v = 0;
+  static int cached[64] = {0};
+  int dev = 0;
   PG_CUDA(cudaGetDevice(&dev));
+  if (dev < 64 && cached[dev] > 0) return cached[dev];
+  int v = 0;
   PG_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  if (dev < 64) cached[dev] = v;
   return v;
+}
+
+// Shared-memory plan for a launch. The small variant keeps the footprint and the owner table
+// in shared memory (BIG = false); maps too large for that keep both in global memory. The
+// pickup map (7 planes) is staged in shared memory when it fits beside them.
+struct SmemPlan {
+  bool big, pick;
+  StampSmem layout;
+};
+template <class M>
+SmemPlan plan_smem(int F, int S, bool allow_small) {
+  const size_t limit = static_cast<size_t>(max_dyn_smem()) - sizeof(StampParams) * kParamChunk - 512;
+  const bool cand[4][2] = {{false, true}, {false, false}, {true, true}, {true, false}};
+  for (const auto& c : cand) {
+    const bool big = c[0], pick = c[1];
+    if (!big && !allow_small) continue;
+    const StampSmem L = stamp_smem_layout<M>(F, S, !big, pick, !big);
+    if (L.total <= limit) return SmemPlan{big, pick, L};
+  }
+  fail(PAINTY_ERR_UNSUPPORTED, "stamp kernel shared memory plan failed");
 }
 
 template <class TK, class TV>
 void launch_stamps(painty_canvas* c, painty_brush* b, const StampRec* d_stamps, int64_t n,
-                   cudaStream_t st) {
+                   bool pickup_zero, cudaStream_t st) {
   using M = typename MathOf<TK>::type;
   StampArgs<TK, TV> a{};
   for (int i = 0; i < 3; i++) {
@@ -507,20 +804,24 @@ void launch_stamps(painty_canvas* c, painty_brush* b, const StampRec* d_stamps, 
     a.paintS[i] = static_cast<M>(b->paintS[i]);
   }
   a.use_snapshot = b->useSnapshot ? 1 : 0;
+  a.dirty = b->useSnapshot ? static_cast<uint8_t*>(b->d_dirty) : nullptr;
+  a.pickup_zero = pickup_zero ? 1 : 0;
   a.status = b->d_status;
-  const size_t small = static_cast<size_t>(b->F) * (2 * sizeof(int) + 2);
-  const size_t own = cells * sizeof(int);
-  const int limit = max_dyn_smem() - static_cast<int>(sizeof(StampShared)) - 1024;
-  size_t dyn = small + own;
-  if (dyn > static_cast<size_t>(limit)) {
-    ensure(&b->d_owner, &b->d_owner_bytes, own);
+  a.support2 = b->support2;
+  const SmemPlan plan = plan_smem<M>(b->F, b->sizeMap, true);
+  const bool big = plan.big;
+  if (big) {
+    ensure(&b->d_owner, &b->d_owner_bytes, cells * sizeof(int));
     a.owner_global = static_cast<int*>(b->d_owner);
-    dyn = small;
   }
-  auto kern = stamp_kernel<TK, TV>;
+  a.footprint_smem = big ? 0 : 1;
+  a.pickup_smem = plan.pick ? 1 : 0;
+  auto kern = plan.pick ? (big ? stamp_kernel<true, true, TK, TV> : stamp_kernel<true, false, TK, TV>)
+                        : (big ? stamp_kernel<false, true, TK, TV> : stamp_kernel<false, false, TK, TV>);
+  const StampSmem Lk = plan.layout;
   PG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               static_cast<int>(dyn)));
-  kern<<<1, kStampThreads, dyn, st>>>(a);
+                               static_cast<int>(Lk.total)));
+  kern<<<1, kStampThreads, Lk.total, st>>>(a);
   count_launch();
   PG_CUDA(cudaGetLastError());
 }
@@ -553,16 +854,14 @@ void run_stamps(painty_canvas* c, painty_brush* b, const std::vector<StampRec>& 
     }
     b->footprint_stale = false;
   }
-  // pickup map
+  // pickup map: cleared by the kernel itself when a dip / new radius is pending
   const size_t pk_bytes = static_cast<size_t>(b->sizeMap) * b->sizeMap * 7 * msz;
   if (b->d_pickup_bytes < pk_bytes) {
     ensure(&b->d_pickup, &b->d_pickup_bytes, pk_bytes);
     b->pickup_clear = true;
   }
-  if (b->pickup_clear) {
-    PG_CUDA(cudaMemsetAsync(b->d_pickup, 0, pk_bytes, st));
-    b->pickup_clear = false;
-  }
+  const bool pickup_zero = b->pickup_clear;
+  b->pickup_clear = false;
   if (!b->d_status) {
     b->d_status = static_cast<unsigned*>(device_alloc(sizeof(unsigned)));
     PG_CUDA(cudaMemsetAsync(b->d_status, 0, sizeof(unsigned), st));
@@ -578,6 +877,17 @@ void run_stamps(painty_canvas* c, painty_brush* b, const std::vector<StampRec>& 
       b->has_snapshot = true;
       PG_CUDA(cudaMemcpyAsync(b->snapshot.base, c->wet.base, c->wet.bytes,
                               cudaMemcpyDeviceToDevice, st));
+      // a fresh copy: snapshot == canvas everywhere
+      ensure(&b->d_dirty, &b->d_dirty_bytes, static_cast<size_t>(c->wet.plane_elems()));
+      PG_CUDA(cudaMemsetAsync(b->d_dirty, 0, c->wet.plane_elems(), st));
+      b->dirty_canvas = c->id;
+      b->dirty_version = c->version;
+    }
+    // the canvas changed outside this brush's stamps since its last run (or another canvas
+    // was painted): every pixel may differ from the snapshot
+    if (b->dirty_canvas != c->id || b->dirty_version != c->version) {
+      ensure(&b->d_dirty, &b->d_dirty_bytes, static_cast<size_t>(c->wet.plane_elems()));
+      PG_CUDA(cudaMemsetAsync(b->d_dirty, 1, c->wet.plane_elems(), st));
     }
   }
   // stamps
@@ -587,11 +897,17 @@ void run_stamps(painty_canvas* c, painty_brush* b, const std::vector<StampRec>& 
   const auto* ds = static_cast<const StampRec*>(b->d_stamps);
   const int64_t n = static_cast<int64_t>(recs.size());
   switch (c->wet.storage) {
-    case PAINTY_STORAGE_F32: launch_stamps<float, float>(c, b, ds, n, st); break;
-    case PAINTY_STORAGE_F16: launch_stamps<__half, __half>(c, b, ds, n, st); break;
-    case PAINTY_STORAGE_BF16: launch_stamps<__nv_bfloat16, __half>(c, b, ds, n, st); break;
-    case PAINTY_STORAGE_F64: launch_stamps<double, double>(c, b, ds, n, st); break;
+    case PAINTY_STORAGE_F32: launch_stamps<float, float>(c, b, ds, n, pickup_zero, st); break;
+    case PAINTY_STORAGE_F16: launch_stamps<__half, __half>(c, b, ds, n, pickup_zero, st); break;
+    case PAINTY_STORAGE_BF16:
+      launch_stamps<__nv_bfloat16, __half>(c, b, ds, n, pickup_zero, st);
+      break;
+    case PAINTY_STORAGE_F64: launch_stamps<double, double>(c, b, ds, n, pickup_zero, st); break;
   }
+  // other writers of this canvas must invalidate this brush's snapshot bookkeeping
+  c->version++;
+  b->dirty_canvas = c->id;
+  b->dirty_version = c->version;
   // the stamp records live in a reused buffer: finish before returning
   unsigned status = 0;
   PG_CUDA(cudaMemcpyAsync(&status, b->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
@@ -719,6 +1035,7 @@ painty_status painty_brush_destroy(painty_brush* b) {
     pg::device_free(b->d_owner);
     pg::device_free(b->d_stamps);
     pg::device_free(b->d_status);
+    pg::device_free(b->d_dirty);
     if (b->has_snapshot) pg::device_free(b->snapshot.base);
     delete b;
   });
@@ -784,6 +1101,10 @@ painty_status painty_brush_update_snapshot(painty_brush* b, const painty_canvas*
     }
     PG_CUDA(cudaMemcpyAsync(b->snapshot.base, c->wet.base, c->wet.bytes,
                             cudaMemcpyDeviceToDevice, st));
+    pg::ensure(&b->d_dirty, &b->d_dirty_bytes, static_cast<size_t>(c->wet.plane_elems()));
+    PG_CUDA(cudaMemsetAsync(b->d_dirty, 0, c->wet.plane_elems(), st));
+    b->dirty_canvas = c->id;
+    b->dirty_version = c->version;
     PG_CUDA(cudaStreamSynchronize(st));
   });
 }
@@ -928,13 +1249,22 @@ painty_status painty_stamps_f32_noalloc(const painty_stamp_buffers_f32* b, void*
     a.depositionRate = static_cast<float>(b->deposition_rate);
     a.capacity = static_cast<float>(b->capacity);
     a.use_snapshot = snap ? 1 : 0;
+    a.dirty = nullptr;  // no dirty map: the whole ring is refreshed, as painty does
+    a.pickup_zero = 0;
     a.owner_global = scratch;
     a.status = status;
-    const size_t dyn = static_cast<size_t>(b->footprint_side) * (2 * sizeof(int) + 2);
-    auto kern = pg::stamp_kernel<float, float>;
+    const pg::SmemPlan plan = pg::plan_smem<float>(b->footprint_side, b->map_side, false);
+    a.pickup_smem = plan.pick ? 1 : 0;
+    a.footprint_smem = 0;
+    a.support2 = 2 * b->footprint_side * b->footprint_side;  // no cull: every box pixel
+    a.footprint = b->footprint;  // global: the owner table is the scratch array
+    auto kern = a.pickup_smem ? pg::stamp_kernel<true, true, float, float>
+                              : pg::stamp_kernel<false, true, float, float>;
+    const pg::StampSmem Lk = pg::stamp_smem_layout<float>(b->footprint_side, b->map_side,
+                                                          false, a.pickup_smem != 0, false);
     PG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(dyn)));
-    kern<<<1, pg::kStampThreads, dyn, st>>>(a);
+                                 static_cast<int>(Lk.total)));
+    kern<<<1, pg::kStampThreads, Lk.total, st>>>(a);
     pg::count_launch();
     PG_CUDA(cudaGetLastError());
     unsigned hs = 0;
