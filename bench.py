@@ -291,8 +291,12 @@ def run_ours(args):
 
     stamps = None
     cpu = None
+    precision = composite_precision(pg, torch, Kh, Sh, Vh, R0h, max(3, min(args.steps, 100)))
+    batch = None
     if rank == 0 and not args.no_stamps:
         stamps = run_stamps_config0(pg, torch)
+        batch = {s_: run_batch(pg, torch, s_, args.batch_canvases, args.batch_max_strokes)
+                 for s_ in ("f32", "f16")}
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(Kh, Sh, Vh, R0h)
     if rank == 0:
@@ -320,8 +324,11 @@ def run_ours(args):
         }
         if cpu is not None:
             line["cpu_baseline"] = cpu
+        line["composite_half_storage"] = precision
         if stamps is not None:
             line["stamps"] = stamps
+        if batch is not None:
+            line["stamps_batched"] = batch
         print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist
@@ -359,6 +366,77 @@ def run_stamps_config0(pg, torch, nstrokes: int = 200):
             "config": "1024x768 FP32, 200 strokes, r U[8,32], spacing 0.25 r, snapshot on, "
                       "deposit 0.1, pickup 0.05, final composite; through the C ABI",
             "gpu_launches": pg.kernel_launch_count() - l0}
+
+
+def run_batch(pg, torch, storage: str, ncanvas: int, max_strokes):
+    """The batching workload (config-2 distributions) in one painty_paint_batch launch."""
+    from painty_gb300 import workloads
+
+    specs, strokes = workloads.batch_canvases(ncanvas, seed=2, max_strokes=max_strokes)
+    fp = workloads.footprint_image(seed=7)
+    canvases, brushes = [], []
+    for rows, cols, r0 in specs:
+        c = pg.Canvas(rows, cols, storage)
+        c.upload("R0", r0)
+        b = pg.FootprintBrush(8.0, fp)
+        b.setPickupRate(0.05)
+        b.setDepositionRate(0.1)
+        canvases.append(c)
+        brushes.append(b)
+    torch.cuda.synchronize()
+    l0 = pg.kernel_launch_count()
+    t = time.perf_counter()
+    n = pg.paint_batch(canvases, brushes, strokes)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t
+    px = sum(r * c for r, c, _ in specs)
+    return {"metric": "stamps/s", "value": round(n / dt, 1), "unit": "stamps/s", "stamps": n,
+            "s": round(dt, 3), "storage": storage, "gpu_launches": pg.kernel_launch_count() - l0,
+            "config": f"{ncanvas} canvases (side logU[256,2048], aspect U[0.5,2], "
+                      f"{pg_canvas_px(px)}), {len(strokes)} strokes (logU[50,2000] per canvas"
+                      f"{'' if max_strokes is None else f', at most {max_strokes}'}), "
+                      "r logU[4,64], spacing 0.25 r; one persistent launch"}
+
+
+def pg_canvas_px(px):
+    return f"{px / 1e6:.0f} Mpx"
+
+
+def composite_precision(pg, torch, Kh, Sh, Vh, R0h, steps: int):
+    """Fused composite with FP16 / BF16 layer storage on the same workload: Mpix/s."""
+    out = {}
+    npix = ROWS * COLS
+    for storage in ("f16", "bf16"):
+        layers = []
+        for l in range(LAYERS):
+            ly = pg.PaintLayer(ROWS, COLS, storage)
+            ly.upload("K", Kh[l], planar=True)
+            ly.upload("S", Sh[l], planar=True)
+            ly.upload("V", Vh[l], planar=True)
+            layers.append(ly)
+        r0 = pg.Image(ROWS, COLS)
+        r0.upload(R0h, planar=True)
+        img = pg.Image(ROWS, COLS)
+        stream = torch.cuda.Stream()
+        for _ in range(3):
+            pg.compose_layers(layers, r0, img, stream=stream)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            pg.compose_layers(layers, r0, img, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        bytes_px = 14 * LAYERS + 24
+        peak, _ = _peaks()
+        gbs = bytes_px * npix / (ms / 1e3) / 1e9
+        out[storage] = {"value": round(npix / (ms / 1e3) / 1e6, 2), "unit": "Mpix/s",
+                        "kernel_ms": round(ms, 4), "achieved_gbs": round(gbs, 1),
+                        "frac": round(gbs / peak, 4), "bytes_per_px": bytes_px}
+        del layers
+    return out
 
 
 def cpu_baseline(Kh, Sh, Vh, R0h, target_s: float = 8.0):
@@ -433,6 +511,10 @@ def main():
     ap.add_argument("--cols", type=int, default=COLS, help="composite cols (profiling cases)")
     ap.add_argument("--no-stamps", action="store_true")
     ap.add_argument("--stamps-only", action="store_true", help="only the stamping case")
+    ap.add_argument("--batch-canvases", type=int, default=152,
+                    help="canvases in the batched stamping case")
+    ap.add_argument("--batch-max-strokes", type=int, default=200,
+                    help="cap on strokes per canvas in the batched stamping case")
     ap.add_argument("--strokes", type=int, default=200, help="strokes in the stamping case")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()

@@ -188,6 +188,81 @@ painty_status painty_stamps(painty_canvas* canvas, painty_brush* brush,
 painty_status painty_stroke(painty_canvas* canvas, painty_brush* brush, const double* path_xy,
                             int32_t n, double spacing, int64_t* stamps_out, void* stream);
 
+/* ------------------------------------------------------------------ batched painting
+ * Many canvases, each with its own brush, painted in one persistent launch. For every canvas,
+ * its strokes (in array order) are applied as painty's
+ *     brush.setRadius(radius); brush.dip({K, S}); brush.paintStroke(path, canvas)
+ * (FootprintBrush.hxx:46-63, 150-154, 206-268) with stamps every `spacing` of chord length
+ * (1.0 = painty). Canvases are independent and run concurrently, heaviest first; a canvas's
+ * strokes run in order. Results equal the sequential calls, except that the stamp angles'
+ * atan2/cos/sin come from the device's double functions (within 1-2 ulp of libm's).
+ * All canvases share one storage format; a brush belongs to one canvas of the batch. */
+typedef struct painty_stroke_desc {
+  int32_t canvas;      /* index into canvases[] */
+  int32_t npoints;     /* control points, at most 512 */
+  int64_t first_point; /* first (x, y) pair in points[] */
+  double radius;       /* setRadius before the stroke */
+  double spacing;      /* stamp spacing along each segment's chord */
+  double K[3], S[3];   /* dip before the stroke */
+} painty_stroke_desc;
+painty_status painty_paint_batch(painty_canvas* const* canvases, painty_brush* const* brushes,
+                                 int32_t ncanvas, const painty_stroke_desc* strokes, int64_t nstrokes,
+                                 const double* points, int64_t npoints, int64_t* stamps_out,
+                                 void* stream);
+
+/* ------------------------------------------------------------------ serving
+ * A continuous-batching render server (no counterpart in painty, whose SbrRenderThread runs
+ * one stroke at a time on a GL thread: painty/renderer/SbrRenderThread.hxx:50-74). Requests
+ * paint strokes on a new canvas or continue a canvas an earlier request created; a worker
+ * thread paints a slice of every admitted request per step in one batched launch, so
+ * requests that arrive while others run join at the next step. Canvases stay resident
+ * between requests within a device-memory budget (idle canvases are moved to host memory,
+ * least recently used first, and restored when continued). A canvas's requests run in
+ * submission order; each completes with its canvas's KM composite in the caller's buffer.
+ * Every canvas gets its own brush (the server's footprint and rates, snapshot on). */
+typedef struct painty_server painty_server;
+typedef struct painty_server_options {
+  uint64_t budget_bytes;   /* device memory for resident canvases (state, snapshot, maps) */
+  painty_storage storage;  /* canvas storage format */
+  int32_t max_active;      /* requests painted at once (<= 0: 256) */
+  int64_t step_stamps;     /* stamps per request per step (<= 0: 16384) */
+  double pickup_rate, deposition_rate;
+  const double* footprint; /* brush footprint image (copied) */
+  int32_t footprint_rows, footprint_cols;
+} painty_server_options;
+typedef struct painty_request {
+  uint64_t canvas_id;      /* 0: a new canvas of rows x cols; else continue that canvas */
+  int32_t rows, cols;
+  const float* r0;         /* new canvas substrate, rows*cols*3 interleaved (NULL: 1.0) */
+  const painty_stroke_desc* strokes; /* `canvas` ignored; copied at submit */
+  int64_t nstrokes;
+  const double* points;    /* copied at submit */
+  int64_t npoints;
+  float* out_rgb;          /* composite result, rows*cols*3 interleaved (NULL: none); must
+                              stay valid until the request finishes */
+} painty_request;
+typedef struct painty_server_counters {
+  int64_t submitted, completed, failed, cancelled;
+  int64_t steps, stamps, evictions, restores;
+  uint64_t resident_bytes, peak_resident_bytes;
+  int64_t active, pending, canvases;
+} painty_server_counters;
+painty_status painty_server_create(const painty_server_options* options, painty_server** out);
+/* Non-blocking. Returns the request id and its canvas id (new canvases get one here). */
+painty_status painty_server_submit(painty_server* server, const painty_request* request,
+                                   uint64_t* request_id, uint64_t* canvas_id);
+/* Blocks until the request finished (timeout_s < 0: no limit); returns its status:
+ * PAINTY_OK, PAINTY_ERR_BUDGET (canvas larger than the budget), PAINTY_ERR_CANCELLED, or
+ * PAINTY_ERR_TIMEOUT when it has not finished in time. */
+painty_status painty_server_wait(painty_server* server, uint64_t request_id, double timeout_s,
+                                 double* latency_s, int64_t* stamps);
+/* Cancels a request: before it runs it is dropped; while it runs it stops at the next step
+ * (its canvas keeps the strokes painted so far). */
+painty_status painty_server_cancel(painty_server* server, uint64_t request_id);
+painty_status painty_server_stats(painty_server* server, painty_server_counters* out);
+/* Stops the worker after its current step; unfinished requests end as cancelled. */
+painty_status painty_server_destroy(painty_server* server);
+
 /* ------------------------------------------------------------------ mixing (host)
  * replaces PaintMixer::mixSinglePaint (painty/mixer/src/PaintMixer.cxx:327-355) */
 painty_status painty_mix_paint(const double* weights, int32_t n, const double* palette_K,

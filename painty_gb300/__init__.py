@@ -90,6 +90,12 @@ _sig("painty_imprint", _P, _P, _D, _D, _D, _P)
 _sig("painty_stamps", _P, _P, _P, _I64, _P)
 _sig("painty_stroke", _P, _P, _P, _I32, _D, C.POINTER(_I64), _P)
 _sig("painty_mix_paint", _P, _I32, _P, _P, _P, _P)
+_sig("painty_paint_batch", _P, _P, _I32, _P, _I64, _P, _I64, C.POINTER(_I64), _P)
+
+# painty_stroke_desc (include/painty_gb300.h)
+STROKE_DESC = np.dtype([("canvas", np.int32), ("npoints", np.int32), ("first_point", np.int64),
+                        ("radius", np.float64), ("spacing", np.float64),
+                        ("K", np.float64, 3), ("S", np.float64, 3)])
 
 ABI_VERSION = _lib.painty_abi_version()
 
@@ -415,3 +421,133 @@ def mix_single_paint(weights: np.ndarray, palette_K: np.ndarray, palette_S: np.n
     S = np.zeros(3)
     _check(_lib.painty_mix_paint(_ptr(w), w.size, _ptr(pk), _ptr(ps), _ptr(K), _ptr(S)))
     return K, S
+
+
+def paint_batch(canvases, brushes, strokes, stream=None) -> int:
+    """Paints many canvases in one launch (painty_paint_batch).
+
+    strokes: iterable of (canvas_index, path (n, 2), radius, spacing, K (3), S (3)). For each
+    canvas its strokes are applied in order as brush.setRadius, brush.dip, brush.paintStroke.
+    Returns the number of stamps.
+    """
+    strokes = list(strokes)
+    desc = np.zeros(len(strokes), dtype=STROKE_DESC)
+    paths = []
+    offset = 0
+    for i, (ci, path, radius, spacing, K, S) in enumerate(strokes):
+        p = np.ascontiguousarray(path, dtype=np.float64).reshape(-1, 2)
+        desc[i] = (ci, p.shape[0], offset, radius, spacing, K, S)
+        paths.append(p)
+        offset += p.shape[0]
+    pts = np.ascontiguousarray(np.concatenate(paths) if paths else np.zeros((0, 2)))
+    carr = (_P * len(canvases))(*[c._h for c in canvases])
+    barr = (_P * len(brushes))(*[b._h for b in brushes])
+    n = _I64()
+    _check(_lib.painty_paint_batch(carr, barr, len(canvases), desc.ctypes.data, len(strokes),
+                                   pts.ctypes.data, pts.shape[0], C.byref(n), _stream(stream)))
+    return n.value
+
+
+class _ServerOptions(C.Structure):
+    _fields_ = [("budget_bytes", C.c_uint64), ("storage", C.c_int), ("max_active", C.c_int32),
+                ("step_stamps", C.c_int64), ("pickup_rate", C.c_double),
+                ("deposition_rate", C.c_double), ("footprint", C.c_void_p),
+                ("footprint_rows", C.c_int32), ("footprint_cols", C.c_int32)]
+
+
+class _Request(C.Structure):
+    _fields_ = [("canvas_id", C.c_uint64), ("rows", C.c_int32), ("cols", C.c_int32),
+                ("r0", C.c_void_p), ("strokes", C.c_void_p), ("nstrokes", C.c_int64),
+                ("points", C.c_void_p), ("npoints", C.c_int64), ("out_rgb", C.c_void_p)]
+
+
+class _Counters(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in ("submitted", "completed", "failed", "cancelled", "steps",
+                                          "stamps", "evictions", "restores")] + \
+               [("resident_bytes", C.c_uint64), ("peak_resident_bytes", C.c_uint64)] + \
+               [(n, C.c_int64) for n in ("active", "pending", "canvases")]
+
+
+_sig("painty_server_create", C.POINTER(_ServerOptions), C.POINTER(_P))
+_sig("painty_server_submit", _P, C.POINTER(_Request), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64))
+_sig("painty_server_wait", _P, C.c_uint64, _D, C.POINTER(_D), C.POINTER(_I64))
+_sig("painty_server_cancel", _P, C.c_uint64)
+_sig("painty_server_stats", _P, C.POINTER(_Counters))
+_sig("painty_server_destroy", _P)
+
+
+def _strokes_to_desc(strokes):
+    desc = np.zeros(len(strokes), dtype=STROKE_DESC)
+    paths, offset = [], 0
+    for i, (path, radius, spacing, K, S) in enumerate(strokes):
+        p = np.ascontiguousarray(path, dtype=np.float64).reshape(-1, 2)
+        desc[i] = (0, p.shape[0], offset, radius, spacing, K, S)
+        paths.append(p)
+        offset += p.shape[0]
+    pts = np.ascontiguousarray(np.concatenate(paths) if paths else np.zeros((0, 2)))
+    return desc, pts
+
+
+class Server:
+    """Continuous-batching render server (painty_server_*): requests paint strokes on a new
+    canvas or continue one; results are the canvases' KM composites."""
+
+    def __init__(self, budget_bytes: int, footprint: np.ndarray, storage: str = "f16",
+                 pickup_rate: float = 0.05, deposition_rate: float = 0.1, max_active: int = 256,
+                 step_stamps: int = 16384):
+        self._fp = np.ascontiguousarray(footprint, dtype=np.float64)
+        o = _ServerOptions(int(budget_bytes), STORAGE[storage], max_active, step_stamps,
+                           pickup_rate, deposition_rate, self._fp.ctypes.data,
+                           self._fp.shape[0], self._fp.shape[1])
+        h = _P()
+        _check(_lib.painty_server_create(C.byref(o), C.byref(h)))
+        self._h = h.value
+        self._dims = {}
+        self._live = {}  # request id -> buffers that must outlive the request
+
+    def submit(self, strokes, canvas_id: int = 0, rows: int = 0, cols: int = 0, r0=None,
+               want_result: bool = True):
+        """strokes: [(path, radius, spacing, K, S)]; returns (request_id, canvas_id)."""
+        desc, pts = _strokes_to_desc(strokes)
+        if canvas_id:
+            rows, cols = self._dims.get(canvas_id, (0, 0))
+        r0a = None if r0 is None else np.ascontiguousarray(r0, dtype=np.float32)
+        out = np.empty((rows, cols, 3), dtype=np.float32) if want_result else None
+        req = _Request(canvas_id, rows, cols, None if r0a is None else r0a.ctypes.data,
+                       desc.ctypes.data, len(desc), pts.ctypes.data, pts.shape[0],
+                       None if out is None else out.ctypes.data)
+        rid, cid = C.c_uint64(), C.c_uint64()
+        _check(_lib.painty_server_submit(self._h, C.byref(req), C.byref(rid), C.byref(cid)))
+        self._dims.setdefault(cid.value, (rows, cols))
+        self._live[rid.value] = out
+        return rid.value, cid.value
+
+    def wait(self, request_id: int, timeout: float = -1.0):
+        """Blocks until the request finished; returns (result image or None, latency s,
+        stamps). Raises on a failed, cancelled or unfinished request."""
+        lat, st = _D(), _I64()
+        status = _lib.painty_server_wait(self._h, request_id, timeout, C.byref(lat), C.byref(st))
+        out = self._live.get(request_id)
+        if status != 6:  # not a timeout: the request is over
+            self._live.pop(request_id, None)
+        _check(status)
+        return out, lat.value, st.value
+
+    def cancel(self, request_id: int) -> None:
+        _check(_lib.painty_server_cancel(self._h, request_id))
+
+    def stats(self) -> dict:
+        c = _Counters()
+        _check(_lib.painty_server_stats(self._h, C.byref(c)))
+        return {n: getattr(c, n) for n, _ in _Counters._fields_}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            _check(_lib.painty_server_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

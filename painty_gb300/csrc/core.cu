@@ -111,6 +111,25 @@ void image_layout(painty_image& I, int32_t rows, int32_t cols, painty_storage s,
   for (int c = 0; c < 3; c++) I.R[c] = static_cast<char*>(base) + c * rb;
 }
 
+void canvas_relayout(painty_canvas* c, void* base) {
+  const int32_t rows = c->wet.rows, cols = c->wet.cols;
+  const painty_storage st = c->wet.storage;
+  const painty_storage rs = c->r0.storage;
+  c->base = base;
+  if (!base) {  // evicted: views point nowhere until the canvas is restored
+    for (int i = 0; i < 3; i++) c->wet.K[i] = c->wet.S[i] = c->r0.R[i] = nullptr;
+    c->wet.V = c->h = c->wet.base = c->r0.base = nullptr;
+    return;
+  }
+  const size_t lb = layer_bytes(rows, cols, st);
+  const size_t ib = image_bytes(rows, cols, rs);
+  layer_layout(c->wet, rows, cols, st, base);
+  c->wet.owned = false;
+  image_layout(c->r0, rows, cols, rs, static_cast<char*>(base) + lb);
+  c->r0.owned = false;
+  c->h = static_cast<char*>(base) + lb + ib;
+}
+
 // ------------------------------------------------------------------ transfer kernels
 namespace {
 

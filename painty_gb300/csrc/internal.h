@@ -5,6 +5,9 @@
 
 #include <atomic>
 #include <cstdint>
+#include <map>
+#include <utility>
+#include <vector>
 #include <stdexcept>
 #include <string>
 
@@ -98,12 +101,57 @@ struct painty_canvas {
   uint64_t version = 0;  // bumped by every write that does not go through a stamp
 };
 
+// FootprintBrush<vec3> (painty/renderer/FootprintBrush.hxx:22-502): host copy of the brush
+// parameters and the device buffers it owns.
+struct painty_brush {
+  double radius = 0.0;  // FootprintBrush.hxx:437
+  int32_t sizeMap = 0;  // :443
+  int32_t F = 0;
+  int32_t support2 = 0;  // squared stamp-pixel radius beyond which the footprint is zero
+  int32_t width = 0;     // footprint width before padding (2 ceil(r) + 1)
+  // footprints already built from `full`, by width: (padded footprint, support2)
+  std::map<int32_t, std::pair<std::vector<double>, int32_t>> fp_cache;
+  std::vector<double> full;
+  int32_t fh = 0, fw = 0;
+  std::vector<double> footprint;  // F*F
+  bool useSnapshot = true;        // :477
+  double capacity = 1.0;          // :483
+  double pickupRate = 0.9;        // :489
+  double depositionRate = 0.05;   // :495
+  double paintK[3] = {0, 0, 0};
+  double paintS[3] = {0, 0, 0};
+  // device state; `math64` is fixed by the first canvas the brush paints
+  int bound = -1;  // -1 unbound, 0 FP32 math, 1 FP64 math
+  void* d_footprint = nullptr;
+  size_t d_footprint_bytes = 0;
+  bool footprint_stale = true;
+  void* d_pickup = nullptr;  // 7 planes of S*S
+  size_t d_pickup_bytes = 0;
+  bool pickup_clear = true;
+  void* d_owner = nullptr;
+  size_t d_owner_bytes = 0;
+  // snapshot (FootprintBrush.hxx:471): canvas-sized layer, allocated at first use
+  painty_layer snapshot;
+  bool has_snapshot = false;
+  // snapshot dirty map (canvas rows x pitch bytes) and the canvas state it describes
+  void* d_dirty = nullptr;
+  size_t d_dirty_bytes = 0;
+  uint64_t dirty_canvas = 0;
+  uint64_t dirty_version = 0;
+  void* d_stamps = nullptr;
+  size_t d_stamps_bytes = 0;
+  unsigned* d_status = nullptr;
+};
+
 namespace pg {
 // Layout helpers (defined in core.cu).
 void layer_layout(painty_layer& L, int32_t rows, int32_t cols, painty_storage s, void* base);
 size_t layer_bytes(int32_t rows, int32_t cols, painty_storage s);
 void image_layout(painty_image& I, int32_t rows, int32_t cols, painty_storage s, void* base);
 size_t image_bytes(int32_t rows, int32_t cols, painty_storage s);
+// Points a canvas's plane views into a new device allocation of the canvas layout (nullptr:
+// no allocation, as for a canvas whose state was moved to host memory).
+void canvas_relayout(painty_canvas* c, void* base);
 
 // Plane transfer between a host buffer and `nch` device planes of element type `dev_type`
 // (0 f32, 1 f16, 2 bf16, 3 f64) with the given pitch. Synchronous w.r.t. the host buffer.
@@ -120,6 +168,13 @@ void fill_planes(void* const* planes, int nch, DevType dt, int64_t elems, const 
                  cudaStream_t st);
 void copy_planes_async(void* const* dst, const void* const* src, int nch, size_t plane_bytes,
                        cudaStream_t st);
+
+// Batched painting (stamp.cu): painty_paint_batch after argument checks.
+void paint_batch(painty_canvas* const* canvases, painty_brush* const* brushes, int32_t nc,
+                 const painty_stroke_desc* strokes, int64_t ns, const double* points,
+                 int64_t npoints, int64_t* stamps_out, cudaStream_t st);
+// Stamps painty's paintStroke puts on a path at the given chord spacing (host count).
+int64_t stroke_stamp_count(const double* path, int32_t n, double spacing);
 
 // KM composite launcher (core.cu). layers: L pointers; r0 and out may alias.
 void launch_compose(const painty_layer* const* layers, int32_t L, const painty_image* r0,

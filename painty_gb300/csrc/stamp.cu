@@ -40,6 +40,8 @@
 #include <climits>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <type_traits>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -467,13 +469,24 @@ __device__ __forceinline__ void scan_ring(const StampArgs<TK, TV>& a, const Stam
 
 // One CTA applies the stamps in order. Pixel slots: warp w owns box rows w, w+32, ...; lane l
 // owns columns l, l+32, ...; slot j = jr * NC + jc (jr-th row, jc-th column of the thread).
-// PS: pickup map staged in shared memory. BIG: footprint and owner table in global memory
-// (maps too large for shared memory); otherwise both are in shared memory.
-template <bool PS, bool BIG, class TK, class TV>
-__global__ void __launch_bounds__(kStampThreads, 1) stamp_kernel(const __grid_constant__ StampArgs<TK, TV> a) {
+// Stamps of a host-built record list (imprint / painty_stamps / painty_stroke).
+struct RecordSource {
+  const StampRec* recs;
+  int64_t n;
+  __device__ __forceinline__ int64_t count() const { return n; }
+  __device__ __forceinline__ StampRec get(int64_t k) const { return recs[k]; }
+};
+
+// One stroke's stamps applied in order by the whole CTA (the kernel body shared by the
+// single-canvas and the batched kernels). `a` may live in shared or parameter memory.
+template <bool PS, bool BIG, class TK, class TV, class Src>
+__device__ __forceinline__ void run_stroke(const StampArgs<TK, TV>& a, const Src& src,
+                                           unsigned char* smem_raw, StampParams* sparams,
+                                           int* s_q) {
   using M = typename MathOf<TK>::type;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ StampParams sparams[kParamChunk];
+  int& s_qcount = s_q[0];
+  int& s_qover = s_q[1];
+  const int64_t nstamps = src.count();
   const int tid = threadIdx.x;
   const int T = blockDim.x;
   const int warp = tid >> 5, lane = tid & 31;
@@ -490,7 +503,6 @@ __global__ void __launch_bounds__(kStampThreads, 1) stamp_kernel(const __grid_co
   uint16_t* done_c = reinterpret_cast<uint16_t*>(smem_raw + L.done_c);
   uint16_t* done_r = reinterpret_cast<uint16_t*>(smem_raw + L.done_r);
   int* queue = reinterpret_cast<int*>(smem_raw + L.queue);
-  __shared__ int s_qcount, s_qover;
 
   // launch prologue: footprint and pickup map staged, owner table reset
   if (!BIG) {
@@ -511,13 +523,13 @@ __global__ void __launch_bounds__(kStampThreads, 1) stamp_kernel(const __grid_co
   }
   int epoch = 0;
 
-  for (int64_t k = 0; k < a.n; k++) {
+  for (int64_t k = 0; k < nstamps; k++) {
     const int slot = static_cast<int>(k % kParamChunk);
     if (slot == 0) {  // derive the next chunk of stamp parameters in parallel
       __syncthreads();
       const int64_t j = k + tid;
-      if (tid < kParamChunk && j < a.n)
-        sparams[tid] = derive_params(a.stamps[j], a.wr, a.radius, a.rows, a.cols);
+      if (tid < kParamChunk && j < nstamps)
+        sparams[tid] = derive_params(src.get(j), a.wr, a.radius, a.rows, a.cols);
       if (epoch > kEpochMax - 2 * kMaxWaves) {  // owner keys about to wrap: reset
         for (int i = tid; i < cells; i += T) own[i] = INT_MAX;
         epoch = 0;
@@ -615,12 +627,219 @@ __global__ void __launch_bounds__(kStampThreads, 1) stamp_kernel(const __grid_co
       __syncthreads();
     }
   }
-  // launch epilogue: the brush keeps its pickup map
+  // epilogue: the brush keeps its pickup map
+  __syncthreads();
   if (PS) {
-    __syncthreads();
     for (int i = tid; i < 7 * cells; i += T) {
       const int p = i / cells, m = i - p * cells;
       pickup_plane<TK, TV, M>(a, p)[m] = pbase[i];
+    }
+    __syncthreads();
+  }
+}
+
+// PS: pickup map staged in shared memory. BIG: footprint and owner table in global memory
+// (maps too large for shared memory); otherwise both are in shared memory.
+template <bool PS, bool BIG, class TK, class TV>
+__global__ void __launch_bounds__(kStampThreads, 1) stamp_kernel(const __grid_constant__ StampArgs<TK, TV> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ StampParams sparams[kParamChunk];
+  __shared__ int s_q[2];
+  run_stroke<PS, BIG>(a, RecordSource{a.stamps, a.n}, smem_raw, sparams, s_q);
+}
+
+// ---------------------------------------------------------------------- batched painting
+constexpr int kMaxPathPoints = 512;  // control points per stroke in the batched kernel
+
+// Spline.hxx:27-73 in painty's operation order, without contraction (device side).
+__device__ __forceinline__ double cr_pos(double p_1, double p0, double p1, double p2, double t) {
+  const double t2 = __dmul_rn(t, t), t3 = __dmul_rn(t2, t);
+  const double b1 = __dsub_rn(__dadd_rn(__dmul_rn(-0.5, t), __dmul_rn(1.0, t2)), __dmul_rn(0.5, t3));
+  const double b2 = __dadd_rn(__dadd_rn(1.0, __dmul_rn(-2.5, t2)), __dmul_rn(1.5, t3));
+  const double b3 = __dadd_rn(__dadd_rn(__dmul_rn(0.5, t), __dmul_rn(2.0, t2)), __dmul_rn(-1.5, t3));
+  const double b4 = __dadd_rn(__dmul_rn(-0.5, t2), __dmul_rn(0.5, t3));
+  return __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(p_1, b1), __dmul_rn(p0, b2)), __dmul_rn(p1, b3)),
+                   __dmul_rn(p2, b4));
+}
+__device__ __forceinline__ double cr_deriv(double p_1, double p0, double p1, double p2, double t) {
+  const double t2 = __dmul_rn(t, t);
+  const double b1 = __dmul_rn(0.5, __dsub_rn(__dadd_rn(__dmul_rn(-3.0, t2), __dmul_rn(4.0, t)), 1.0));
+  const double b2 = __dmul_rn(-t, __dadd_rn(__dadd_rn(-1.0, __dmul_rn(-4.5, t)), 6.0));
+  const double b3 = __dmul_rn(__dsub_rn(t, 1.0), __dsub_rn(__dmul_rn(-4.5, t), 0.5));
+  const double b4 = __dmul_rn(__dmul_rn(0.5, t), __dsub_rn(__dmul_rn(3.0, t), 2.0));
+  return __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(p_1, b1), __dmul_rn(p0, b2)), __dmul_rn(p1, b3)),
+                   __dmul_rn(p2, b4));
+}
+
+// Stamps of FootprintBrush::paintStroke (FootprintBrush.hxx:251-267) over a path with chord
+// spacing `spacing`, generated on the device: stamp pd of segment i sits at t = pd*spacing/dist.
+// The angle's atan2 / cos / sin are the device's double functions (within 1-2 ulp of libm's).
+struct PathSource {
+  const double* pts;  // (x, y) pairs
+  int npts;
+  double spacing;
+  const int64_t* seg_end;  // inclusive prefix sums of the per-segment stamp counts
+  int64_t n;
+  __device__ __forceinline__ int64_t count() const { return n; }
+  __device__ __forceinline__ StampRec get(int64_t k) const {
+    int lo = 0, hi = npts - 2;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (seg_end[mid] > k) hi = mid; else lo = mid + 1;
+    }
+    const int i = lo;
+    const int64_t pd = k - (i > 0 ? seg_end[i - 1] : 0) + 1;
+    const double* pp = pts + 2 * (i > 0 ? i - 1 : 0);
+    const double* p0 = pts + 2 * i;
+    const double* p1 = pts + 2 * (i + 1);
+    const double* pn = pts + 2 * min(i + 2, npts - 1);
+    const double dx = __dsub_rn(p1[0], p0[0]), dy = __dsub_rn(p1[1], p0[1]);
+    const double dist = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+    const double t = __ddiv_rn(__dmul_rn(static_cast<double>(pd), spacing), dist);
+    const double dirx = cr_deriv(pp[0], p0[0], p1[0], pn[0], t);
+    const double diry = cr_deriv(pp[1], p0[1], p1[1], pn[1], t);
+    const double theta = atan2(diry, dirx);
+    StampRec r;
+    r.cx = cr_pos(pp[0], p0[0], p1[0], pn[0], t);
+    r.cy = cr_pos(pp[1], p0[1], p1[1], pn[1], t);
+    r.c = cos(-theta);
+    r.s = sin(-theta);
+    return r;
+  }
+};
+
+template <class TK, class TV>
+struct BatchCanvas {
+  TK* cK[3];
+  TK* cS[3];
+  TV* cV;
+  TK* sK[3];
+  TK* sS[3];
+  TV* sV;
+  uint8_t* dirty;
+  int32_t rows, cols;
+  int64_t pitch;
+  int32_t use_snapshot;
+  int32_t nstrokes;
+  int64_t first_stroke;
+  double pickup_rate, deposition_rate, capacity;
+  void* brush_pickup;  // the brush's own pickup map: the canvas's last stroke paints into it
+};
+
+struct BatchStroke {
+  int64_t first_point;
+  int32_t npoints;
+  int32_t F, S, wr, support2;
+  int32_t plan;  // bit 0: pickup map in shared memory; bit 1: footprint and owners global
+  int64_t fp_offset;
+  double radius, spacing;
+  double K[3], Sc[3];
+};
+
+template <class TK, class TV>
+struct BatchArgs {
+  using M = typename MathOf<TK>::type;
+  const BatchCanvas<TK, TV>* canvases;
+  const BatchStroke* strokes;
+  const double* points;
+  const M* footprints;
+  const int32_t* order;  // canvases, heaviest first
+  int32_t ncanvas;
+  int* counter;
+  M* scratch_pickup;  // per CTA: 7 planes of Smax^2
+  int* scratch_owner; // per CTA: Smax^2
+  int64_t pickup_stride, owner_stride;
+  unsigned* status;
+};
+
+// Persistent batched painting: each CTA claims canvases (heaviest first) and applies their
+// strokes in order, each as setRadius + dip + paintStroke on the canvas's brush.
+template <class TK, class TV>
+__global__ void __launch_bounds__(kStampThreads, 1) batch_kernel(const __grid_constant__ BatchArgs<TK, TV> b) {
+  using M = typename MathOf<TK>::type;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ StampParams sparams[kParamChunk];
+  __shared__ int s_q[2];
+  __shared__ StampArgs<TK, TV> sa;
+  __shared__ int s_item;
+  __shared__ int64_t seg_end[kMaxPathPoints];
+  const int tid = threadIdx.x, T = blockDim.x;
+  for (;;) {
+    __syncthreads();
+    if (tid == 0) {
+      const int i = atomicAdd(b.counter, 1);
+      s_item = i < b.ncanvas ? b.order[i] : -1;
+    }
+    __syncthreads();
+    const int ci = s_item;
+    if (ci < 0) return;
+    const BatchCanvas<TK, TV>& cv = b.canvases[ci];
+    for (int32_t k = 0; k < cv.nstrokes; k++) {
+      const BatchStroke& st = b.strokes[cv.first_stroke + k];
+      const int nseg = st.npoints - 1;
+      __syncthreads();
+      if (tid == 0) {
+        const bool last = k + 1 == cv.nstrokes;
+        const int64_t cells = static_cast<int64_t>(st.S) * st.S;
+        M* pk = last ? static_cast<M*>(cv.brush_pickup)
+                     : b.scratch_pickup + static_cast<int64_t>(blockIdx.x) * b.pickup_stride;
+        for (int i = 0; i < 3; i++) {
+          sa.cK[i] = cv.cK[i];
+          sa.cS[i] = cv.cS[i];
+          sa.sK[i] = cv.sK[i];
+          sa.sS[i] = cv.sS[i];
+          sa.pK[i] = pk + i * cells;
+          sa.pS[i] = pk + (3 + i) * cells;
+          sa.paintK[i] = static_cast<M>(st.K[i]);
+          sa.paintS[i] = static_cast<M>(st.Sc[i]);
+        }
+        sa.cV = cv.cV;
+        sa.sV = cv.sV;
+        sa.pV = pk + 6 * cells;
+        sa.footprint = b.footprints + st.fp_offset;
+        sa.stamps = nullptr;
+        sa.n = 0;
+        sa.rows = cv.rows;
+        sa.cols = cv.cols;
+        sa.pitch = cv.pitch;
+        sa.F = st.F;
+        sa.S = st.S;
+        sa.wr = st.wr;
+        sa.support2 = st.support2;
+        sa.radius = st.radius;
+        sa.pickupRate = static_cast<M>(cv.pickup_rate);
+        sa.depositionRate = static_cast<M>(cv.deposition_rate);
+        sa.capacity = static_cast<M>(cv.capacity);
+        sa.use_snapshot = cv.use_snapshot;
+        sa.dirty = cv.use_snapshot ? cv.dirty : nullptr;
+        sa.pickup_zero = 1;  // dip: the pickup map starts clean
+        sa.pickup_smem = st.plan & 1;
+        sa.footprint_smem = (st.plan & 2) ? 0 : 1;
+        sa.owner_global = (st.plan & 2)
+                            ? b.scratch_owner + static_cast<int64_t>(blockIdx.x) * b.owner_stride
+                            : nullptr;
+        sa.status = b.status;
+      }
+      const double* pts = b.points + 2 * st.first_point;
+      for (int i = tid; i < nseg; i += T) {  // stamps per segment (paintStroke's loop bound)
+        const double dx = __dsub_rn(pts[2 * (i + 1)], pts[2 * i]);
+        const double dy = __dsub_rn(pts[2 * (i + 1) + 1], pts[2 * i + 1]);
+        const double dist = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+        seg_end[i] = static_cast<int64_t>(static_cast<int>(__ddiv_rn(dist, st.spacing)));
+      }
+      __syncthreads();
+      if (tid == 0)
+        for (int i = 1; i < nseg; i++) seg_end[i] += seg_end[i - 1];
+      __syncthreads();
+      const int64_t n = nseg > 0 ? seg_end[nseg - 1] : 0;
+      if (n == 0) continue;
+      const PathSource src{pts, st.npoints, st.spacing, seg_end, n};
+      switch (st.plan) {
+        case 0: run_stroke<false, false>(sa, src, smem_raw, sparams, s_q); break;
+        case 1: run_stroke<true, false>(sa, src, smem_raw, sparams, s_q); break;
+        case 2: run_stroke<false, true>(sa, src, smem_raw, sparams, s_q); break;
+        default: run_stroke<true, true>(sa, src, smem_raw, sparams, s_q); break;
+      }
     }
   }
 }
@@ -629,42 +848,6 @@ __global__ void __launch_bounds__(kStampThreads, 1) stamp_kernel(const __grid_co
 }  // namespace pg
 
 // ====================================================================== brush
-struct painty_brush {
-  double radius = 0.0;  // FootprintBrush.hxx:437
-  int32_t sizeMap = 0;  // :443
-  int32_t F = 0;
-  int32_t support2 = 0;  // squared stamp-pixel radius beyond which the footprint is zero
-  std::vector<double> full;
-  int32_t fh = 0, fw = 0;
-  std::vector<double> footprint;  // F*F
-  bool useSnapshot = true;        // :477
-  double capacity = 1.0;          // :483
-  double pickupRate = 0.9;        // :489
-  double depositionRate = 0.05;   // :495
-  double paintK[3] = {0, 0, 0};
-  double paintS[3] = {0, 0, 0};
-  // device state; `math64` is fixed by the first canvas the brush paints
-  int bound = -1;  // -1 unbound, 0 FP32 math, 1 FP64 math
-  void* d_footprint = nullptr;
-  size_t d_footprint_bytes = 0;
-  bool footprint_stale = true;
-  void* d_pickup = nullptr;  // 7 planes of S*S
-  size_t d_pickup_bytes = 0;
-  bool pickup_clear = true;
-  void* d_owner = nullptr;
-  size_t d_owner_bytes = 0;
-  // snapshot (FootprintBrush.hxx:471): canvas-sized layer, allocated at first use
-  painty_layer snapshot;
-  bool has_snapshot = false;
-  // snapshot dirty map (canvas rows x pitch bytes) and the canvas state it describes
-  void* d_dirty = nullptr;
-  size_t d_dirty_bytes = 0;
-  uint64_t dirty_canvas = 0;
-  uint64_t dirty_version = 0;
-  void* d_stamps = nullptr;
-  size_t d_stamps_bytes = 0;
-  unsigned* d_status = nullptr;
-};
 
 namespace pg {
 namespace {
@@ -706,21 +889,35 @@ int32_t support_radius2(const double* fp, int F) {
 // FootprintBrush::setRadius (FootprintBrush.hxx:46-63). The footprint image is resampled to
 // width x width by a pixel-centre aligned bilinear resample (in place of OpenCV's
 // Lanczos-4 resize) and zero-padded by (sizeMap - width) / 2 on each side.
+// The padded footprint of a brush width (cached per width: the resample depends on it only).
+const std::pair<std::vector<double>, int32_t>& footprint_for(painty_brush* b, int width) {
+  auto it = b->fp_cache.find(width);
+  if (it != b->fp_cache.end()) return it->second;
+  const int sizeMap = static_cast<int>(std::ceil(std::sqrt(2.0) * width));
+  const int pad = (sizeMap - width) / 2;
+  const int F = width + 2 * pad;
+  std::vector<double> fp(static_cast<size_t>(F) * F, 0.0);
+  const double sy = static_cast<double>(b->fh) / width, sx = static_cast<double>(b->fw) / width;
+  for (int i = 0; i < width; i++)
+    for (int j = 0; j < width; j++)
+      fp[static_cast<size_t>(i + pad) * F + (j + pad)] =
+        interpolate(b->full.data(), b->fh, b->fw, (static_cast<double>(j) + 0.5) * sx - 0.5,
+                    (static_cast<double>(i) + 0.5) * sy - 0.5);
+  const int32_t s2 = support_radius2(fp.data(), F);
+  return b->fp_cache.emplace(width, std::make_pair(std::move(fp), s2)).first->second;
+}
+
 void set_radius(painty_brush* b, double radius) {
   if (std::fabs(b->radius - radius) < 0.5) return;
   b->radius = radius;
   const int width = static_cast<int>(2.0 * std::ceil(radius) + 1.0);
+  b->width = width;
   b->sizeMap = static_cast<int>(std::ceil(std::sqrt(2.0) * width));
   const int pad = (b->sizeMap - width) / 2;
   b->F = width + 2 * pad;
-  b->footprint.assign(static_cast<size_t>(b->F) * b->F, 0.0);
-  const double sy = static_cast<double>(b->fh) / width, sx = static_cast<double>(b->fw) / width;
-  for (int i = 0; i < width; i++)
-    for (int j = 0; j < width; j++)
-      b->footprint[static_cast<size_t>(i + pad) * b->F + (j + pad)] =
-        interpolate(b->full.data(), b->fh, b->fw, (static_cast<double>(j) + 0.5) * sx - 0.5,
-                    (static_cast<double>(i) + 0.5) * sy - 0.5);
-  b->support2 = support_radius2(b->footprint.data(), b->F);
+  const auto& fp = footprint_for(b, width);
+  b->footprint = fp.first;
+  b->support2 = fp.second;
   b->footprint_stale = true;
   b->pickup_clear = true;
 }
@@ -753,8 +950,7 @@ struct SmemPlan {
   StampSmem layout;
 };
 template <class M>
-SmemPlan plan_smem(int F, int S, bool allow_small) {
-  const size_t limit = static_cast<size_t>(max_dyn_smem()) - sizeof(StampParams) * kParamChunk - 512;
+SmemPlan plan_smem_limit(int F, int S, size_t limit, bool allow_small = true) {
   const bool cand[4][2] = {{false, true}, {false, false}, {true, true}, {true, false}};
   for (const auto& c : cand) {
     const bool big = c[0], pick = c[1];
@@ -763,6 +959,12 @@ SmemPlan plan_smem(int F, int S, bool allow_small) {
     if (L.total <= limit) return SmemPlan{big, pick, L};
   }
   fail(PAINTY_ERR_UNSUPPORTED, "stamp kernel shared memory plan failed");
+}
+
+template <class M>
+SmemPlan plan_smem(int F, int S, bool allow_small) {
+  const size_t limit = static_cast<size_t>(max_dyn_smem()) - sizeof(StampParams) * kParamChunk - 512;
+  return plan_smem_limit<M>(F, S, limit, allow_small);
 }
 
 template <class TK, class TV>
@@ -826,6 +1028,31 @@ void launch_stamps(painty_canvas* c, painty_brush* b, const StampRec* d_stamps, 
   PG_CUDA(cudaGetLastError());
 }
 
+// Snapshot buffer for painting canvas c with brush b (FootprintBrush.hxx:280-284: a full copy
+// when the sizes differ) and its dirty map: clean after a full copy; all dirty when the canvas
+// changed outside this brush's stamps since its last run, or another canvas was painted.
+void prepare_snapshot(painty_canvas* c, painty_brush* b, cudaStream_t st) {
+  if (!b->useSnapshot) return;
+  if (!b->has_snapshot || b->snapshot.rows != c->wet.rows || b->snapshot.cols != c->wet.cols ||
+      b->snapshot.storage != c->wet.storage) {
+    if (b->has_snapshot) device_free(b->snapshot.base);
+    b->has_snapshot = false;
+    void* base = device_alloc(layer_bytes(c->wet.rows, c->wet.cols, c->wet.storage));
+    layer_layout(b->snapshot, c->wet.rows, c->wet.cols, c->wet.storage, base);
+    b->has_snapshot = true;
+    PG_CUDA(cudaMemcpyAsync(b->snapshot.base, c->wet.base, c->wet.bytes,
+                            cudaMemcpyDeviceToDevice, st));
+    ensure(&b->d_dirty, &b->d_dirty_bytes, static_cast<size_t>(c->wet.plane_elems()));
+    PG_CUDA(cudaMemsetAsync(b->d_dirty, 0, c->wet.plane_elems(), st));
+    b->dirty_canvas = c->id;
+    b->dirty_version = c->version;
+  }
+  if (b->dirty_canvas != c->id || b->dirty_version != c->version) {
+    ensure(&b->d_dirty, &b->d_dirty_bytes, static_cast<size_t>(c->wet.plane_elems()));
+    PG_CUDA(cudaMemsetAsync(b->d_dirty, 1, c->wet.plane_elems(), st));
+  }
+}
+
 // Prepares device state and runs n stamps (host records) on the canvas.
 void run_stamps(painty_canvas* c, painty_brush* b, const std::vector<StampRec>& recs,
                 cudaStream_t st) {
@@ -866,30 +1093,7 @@ void run_stamps(painty_canvas* c, painty_brush* b, const std::vector<StampRec>& 
     b->d_status = static_cast<unsigned*>(device_alloc(sizeof(unsigned)));
     PG_CUDA(cudaMemsetAsync(b->d_status, 0, sizeof(unsigned), st));
   }
-  // snapshot (FootprintBrush.hxx:280-284: full copy when the sizes differ)
-  if (b->useSnapshot) {
-    if (!b->has_snapshot || b->snapshot.rows != c->wet.rows || b->snapshot.cols != c->wet.cols ||
-        b->snapshot.storage != c->wet.storage) {
-      if (b->has_snapshot) device_free(b->snapshot.base);
-      b->has_snapshot = false;
-      void* base = device_alloc(layer_bytes(c->wet.rows, c->wet.cols, c->wet.storage));
-      layer_layout(b->snapshot, c->wet.rows, c->wet.cols, c->wet.storage, base);
-      b->has_snapshot = true;
-      PG_CUDA(cudaMemcpyAsync(b->snapshot.base, c->wet.base, c->wet.bytes,
-                              cudaMemcpyDeviceToDevice, st));
-      // a fresh copy: snapshot == canvas everywhere
-      ensure(&b->d_dirty, &b->d_dirty_bytes, static_cast<size_t>(c->wet.plane_elems()));
-      PG_CUDA(cudaMemsetAsync(b->d_dirty, 0, c->wet.plane_elems(), st));
-      b->dirty_canvas = c->id;
-      b->dirty_version = c->version;
-    }
-    // the canvas changed outside this brush's stamps since its last run (or another canvas
-    // was painted): every pixel may differ from the snapshot
-    if (b->dirty_canvas != c->id || b->dirty_version != c->version) {
-      ensure(&b->d_dirty, &b->d_dirty_bytes, static_cast<size_t>(c->wet.plane_elems()));
-      PG_CUDA(cudaMemsetAsync(b->d_dirty, 1, c->wet.plane_elems(), st));
-    }
-  }
+  prepare_snapshot(c, b, st);
   // stamps
   const size_t sbytes = recs.size() * sizeof(StampRec);
   ensure(&b->d_stamps, &b->d_stamps_bytes, sbytes);
@@ -914,6 +1118,241 @@ void run_stamps(painty_canvas* c, painty_brush* b, const std::vector<StampRec>& 
   PG_CUDA(cudaStreamSynchronize(st));
   if (status != 0) fail(PAINTY_ERR_CUDA, "stamp kernel reported an internal error");
 }
+
+
+// ---------------------------------------------------------------------- batched painting (host)
+template <class TK, class TV>
+void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushes, int32_t nc,
+                     const painty_stroke_desc* strokes, int64_t ns, const double* points,
+                     int64_t npoints, int64_t* stamps_out, cudaStream_t st) {
+  using M = typename MathOf<TK>::type;
+  const bool f64 = std::is_same<M, double>::value;
+  const size_t msz = sizeof(M);
+  // strokes grouped by canvas, in order
+  std::vector<std::vector<int64_t>> per(nc);
+  for (int64_t i = 0; i < ns; i++) per[strokes[i].canvas].push_back(i);
+  // launch shared-memory budget: the opt-in maximum minus the kernel's static shared memory
+  cudaFuncAttributes fa{};
+  PG_CUDA(cudaFuncGetAttributes(&fa, batch_kernel<TK, TV>));
+  const size_t limit = static_cast<size_t>(max_dyn_smem()) - fa.sharedSizeBytes - 256;
+  std::vector<BatchStroke> bs;
+  bs.reserve(static_cast<size_t>(ns));
+  std::vector<M> fptable;
+  std::map<std::pair<const painty_brush*, int32_t>, int64_t> fp_off;
+  std::vector<double> work(nc, 0.0);
+  int32_t smax = 1;
+  size_t dyn = 0;
+  int64_t total_stamps = 0;
+  std::vector<int64_t> first(nc, 0);
+  for (int32_t c = 0; c < nc; c++) {
+    painty_brush* b = brushes[c];
+    first[c] = static_cast<int64_t>(bs.size());
+    for (int64_t si : per[c]) {
+      const painty_stroke_desc& sk = strokes[si];
+      set_radius(b, sk.radius);  // FootprintBrush::setRadius: new footprint only on a 0.5 change
+      PG_REQUIRE(b->sizeMap > 0 && b->F > 0, "brush radius gives an empty footprint");
+      PG_REQUIRE(static_cast<int64_t>(b->F) * b->F <= int64_t(kMaxPixelsPerThread) * kStampThreads,
+                 "brush radius above the supported maximum (footprint side 256)");
+      const auto key = std::make_pair(static_cast<const painty_brush*>(b), b->width);
+      auto it = fp_off.find(key);
+      if (it == fp_off.end()) {
+        it = fp_off.emplace(key, static_cast<int64_t>(fptable.size())).first;
+        for (double v : b->footprint) fptable.push_back(static_cast<M>(v));
+      }
+      BatchStroke x{};
+      x.first_point = sk.first_point;
+      x.npoints = sk.npoints;
+      x.F = b->F;
+      x.S = b->sizeMap;
+      x.wr = (b->F - 1) / 2;
+      x.support2 = b->support2;
+      x.fp_offset = it->second;
+      x.radius = b->radius;
+      x.spacing = sk.spacing;
+      for (int i = 0; i < 3; i++) {
+        x.K[i] = sk.K[i];
+        x.Sc[i] = sk.S[i];
+      }
+      const SmemPlan plan = plan_smem_limit<M>(b->F, b->sizeMap, limit);
+      x.plan = (plan.pick ? 1 : 0) | (plan.big ? 2 : 0);
+      dyn = std::max(dyn, plan.layout.total);
+      smax = std::max(smax, b->sizeMap);
+      // stamp count (paintStroke's loop bounds) and a work estimate for the ordering
+      const int64_t n = stroke_stamp_count(points + 2 * sk.first_point, sk.npoints, sk.spacing);
+      total_stamps += n;
+      work[c] += static_cast<double>(n) * (0.4 * b->F * b->F + 4.0 * b->F * (b->radius + 1));
+      bs.push_back(x);
+      for (int i = 0; i < 3; i++) {  // dip
+        b->paintK[i] = sk.K[i];
+        b->paintS[i] = sk.S[i];
+      }
+    }
+  }
+  if (stamps_out) *stamps_out = total_stamps;
+  // canvases, brushes' device state
+  std::vector<BatchCanvas<TK, TV>> bc(nc);
+  for (int32_t c = 0; c < nc; c++) {
+    painty_canvas* cv = canvases[c];
+    painty_brush* b = brushes[c];
+    const int mode = f64 ? 1 : 0;
+    if (b->bound < 0) b->bound = mode;
+    PG_REQUIRE(b->bound == mode,
+               "a brush paints either F64 canvases or F32/F16/BF16 canvases, not both");
+    if (!b->d_status) {
+      b->d_status = static_cast<unsigned*>(device_alloc(sizeof(unsigned)));
+      PG_CUDA(cudaMemsetAsync(b->d_status, 0, sizeof(unsigned), st));
+    }
+    const size_t pk_bytes = static_cast<size_t>(b->sizeMap) * b->sizeMap * 7 * msz;
+    ensure(&b->d_pickup, &b->d_pickup_bytes, pk_bytes);
+    if (!per[c].empty()) prepare_snapshot(cv, b, st);
+    BatchCanvas<TK, TV>& x = bc[c];
+    for (int i = 0; i < 3; i++) {
+      x.cK[i] = static_cast<TK*>(cv->wet.K[i]);
+      x.cS[i] = static_cast<TK*>(cv->wet.S[i]);
+      const painty_layer& src = b->useSnapshot ? b->snapshot : cv->wet;
+      x.sK[i] = static_cast<TK*>(src.K[i]);
+      x.sS[i] = static_cast<TK*>(src.S[i]);
+    }
+    x.cV = static_cast<TV*>(cv->wet.V);
+    x.sV = static_cast<TV*>(b->useSnapshot ? b->snapshot.V : cv->wet.V);
+    x.dirty = b->useSnapshot ? static_cast<uint8_t*>(b->d_dirty) : nullptr;
+    x.rows = cv->wet.rows;
+    x.cols = cv->wet.cols;
+    x.pitch = cv->wet.pitch;
+    x.use_snapshot = b->useSnapshot ? 1 : 0;
+    x.nstrokes = static_cast<int32_t>(per[c].size());
+    x.first_stroke = first[c];
+    x.pickup_rate = b->pickupRate;
+    x.deposition_rate = b->depositionRate;
+    x.capacity = b->capacity;
+    x.brush_pickup = b->d_pickup;
+  }
+  // heaviest canvases first
+  std::vector<int32_t> order(nc);
+  for (int32_t c = 0; c < nc; c++) order[c] = c;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int32_t a, int32_t b2) { return work[a] > work[b2]; });
+  // device copies of the descriptors (stream-ordered, freed after the launch)
+  int dev = 0, sms = 0;
+  PG_CUDA(cudaGetDevice(&dev));
+  PG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int grid = std::max(1, std::min(sms, nc));
+  auto upload = [&](const void* h, size_t bytes) -> void* {
+    void* d = nullptr;
+    PG_CUDA(cudaMallocAsync(&d, std::max<size_t>(bytes, 16), st));
+    if (bytes) PG_CUDA(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, st));
+    return d;
+  };
+  void* d_canvas = upload(bc.data(), bc.size() * sizeof(bc[0]));
+  void* d_strokes = upload(bs.data(), bs.size() * sizeof(BatchStroke));
+  void* d_points = upload(points, static_cast<size_t>(npoints) * 2 * sizeof(double));
+  void* d_fp = upload(fptable.data(), fptable.size() * sizeof(M));
+  void* d_order = upload(order.data(), order.size() * sizeof(int32_t));
+  const int64_t pstride = static_cast<int64_t>(7) * smax * smax;
+  const int64_t ostride = static_cast<int64_t>(smax) * smax;
+  void* d_scratch_p = nullptr;
+  void* d_scratch_o = nullptr;
+  void* d_counter = nullptr;
+  PG_CUDA(cudaMallocAsync(&d_scratch_p, grid * pstride * msz, st));
+  PG_CUDA(cudaMallocAsync(&d_scratch_o, grid * ostride * sizeof(int), st));
+  PG_CUDA(cudaMallocAsync(&d_counter, sizeof(int) + sizeof(unsigned), st));
+  PG_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(int) + sizeof(unsigned), st));
+  BatchArgs<TK, TV> a{};
+  a.canvases = static_cast<const BatchCanvas<TK, TV>*>(d_canvas);
+  a.strokes = static_cast<const BatchStroke*>(d_strokes);
+  a.points = static_cast<const double*>(d_points);
+  a.footprints = static_cast<const M*>(d_fp);
+  a.order = static_cast<const int32_t*>(d_order);
+  a.ncanvas = nc;
+  a.counter = static_cast<int*>(d_counter);
+  a.status = reinterpret_cast<unsigned*>(static_cast<int*>(d_counter) + 1);
+  a.scratch_pickup = static_cast<M*>(d_scratch_p);
+  a.scratch_owner = static_cast<int*>(d_scratch_o);
+  a.pickup_stride = pstride;
+  a.owner_stride = ostride;
+  auto kern = batch_kernel<TK, TV>;
+  PG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               static_cast<int>(dyn)));
+  kern<<<grid, kStampThreads, dyn, st>>>(a);
+  count_launch();
+  PG_CUDA(cudaGetLastError());
+  unsigned status = 0;
+  PG_CUDA(cudaMemcpyAsync(&status, a.status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+  for (void* d : {d_canvas, d_strokes, d_points, d_fp, d_order, d_scratch_p, d_scratch_o, d_counter})
+    PG_CUDA(cudaFreeAsync(d, st));
+  PG_CUDA(cudaStreamSynchronize(st));
+  for (int32_t c = 0; c < nc; c++) {
+    if (per[c].empty()) continue;
+    painty_brush* b = brushes[c];
+    canvases[c]->version++;
+    b->dirty_canvas = canvases[c]->id;
+    b->dirty_version = canvases[c]->version;
+    b->pickup_clear = false;  // the last stroke's pickup map is in the brush's buffer
+  }
+  if (status != 0) fail(PAINTY_ERR_CUDA, "batched stamp kernel reported an internal error");
+}
+
+}  // namespace
+
+int64_t stroke_stamp_count(const double* p, int32_t npts, double spacing) {
+  int64_t n = 0;
+  for (int32_t i = 0; i + 1 < npts; i++) {
+    const double dx = p[2 * (i + 1)] - p[2 * i], dy = p[2 * (i + 1) + 1] - p[2 * i + 1];
+    n += static_cast<int>(std::sqrt(dx * dx + dy * dy) / spacing);
+  }
+  return n;
+}
+
+void paint_batch(painty_canvas* const* canvases, painty_brush* const* brushes, int32_t ncanvas,
+                 const painty_stroke_desc* strokes, int64_t nstrokes, const double* points,
+                 int64_t npoints, int64_t* stamps_out, cudaStream_t st) {
+  PG_REQUIRE(ncanvas > 0 && canvases && brushes, "no canvases");
+  PG_REQUIRE(nstrokes >= 0 && (nstrokes == 0 || strokes), "strokes is null");
+  PG_REQUIRE(npoints >= 0 && (npoints == 0 || points), "points is null");
+  const painty_storage storage = canvases[0] ? canvases[0]->wet.storage : PAINTY_STORAGE_F32;
+  for (int32_t c = 0; c < ncanvas; c++) {
+    PG_REQUIRE(canvases[c] && brushes[c], "null canvas or brush");
+    PG_REQUIRE(canvases[c]->wet.storage == storage, "canvases of one batch share a storage format");
+    PG_REQUIRE(static_cast<int64_t>(canvases[c]->wet.rows) * canvases[c]->wet.pitch < (int64_t(1) << 31),
+               "canvas too large for the batched kernel");
+  }
+  {
+    std::vector<const void*> seen_c(canvases, canvases + ncanvas), seen_b(brushes, brushes + ncanvas);
+    std::sort(seen_c.begin(), seen_c.end());
+    std::sort(seen_b.begin(), seen_b.end());
+    PG_REQUIRE(std::adjacent_find(seen_c.begin(), seen_c.end()) == seen_c.end() &&
+                 std::adjacent_find(seen_b.begin(), seen_b.end()) == seen_b.end(),
+               "each canvas of a batch has its own brush");
+  }
+  for (int64_t i = 0; i < 2 * npoints; i++)
+    PG_REQUIRE(std::isfinite(points[i]), "path coordinates must be finite");
+  for (int64_t i = 0; i < nstrokes; i++) {
+    const painty_stroke_desc& s = strokes[i];
+    PG_REQUIRE(s.canvas >= 0 && s.canvas < ncanvas, "stroke canvas index out of range");
+    PG_REQUIRE(s.npoints >= 0 && s.npoints <= kMaxPathPoints,
+               "stroke paths hold at most 512 points in a batch");
+    PG_REQUIRE(s.first_point >= 0 && s.first_point + s.npoints <= npoints,
+               "stroke points out of range");
+    PG_REQUIRE(std::isfinite(s.radius) && s.radius >= 0.0, "radius must be finite and >= 0");
+    PG_REQUIRE(std::isfinite(s.spacing) && s.spacing > 0.0, "spacing must be positive");
+  }
+  switch (storage) {
+    case PAINTY_STORAGE_F32:
+      run_batch_typed<float, float>(canvases, brushes, ncanvas, strokes, nstrokes, points, npoints, stamps_out, st);
+      break;
+    case PAINTY_STORAGE_F16:
+      run_batch_typed<__half, __half>(canvases, brushes, ncanvas, strokes, nstrokes, points, npoints, stamps_out, st);
+      break;
+    case PAINTY_STORAGE_BF16:
+      run_batch_typed<__nv_bfloat16, __half>(canvases, brushes, ncanvas, strokes, nstrokes, points, npoints, stamps_out, st);
+      break;
+    case PAINTY_STORAGE_F64:
+      run_batch_typed<double, double>(canvases, brushes, ncanvas, strokes, nstrokes, points, npoints, stamps_out, st);
+      break;
+  }
+}
+
+namespace {
 
 StampRec make_rec(double cx, double cy, double theta) {
   PG_REQUIRE(std::isfinite(cx) && std::isfinite(cy) && std::isfinite(theta),
@@ -1271,6 +1710,16 @@ painty_status painty_stamps_f32_noalloc(const painty_stamp_buffers_f32* b, void*
     PG_CUDA(cudaMemcpyAsync(&hs, status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     PG_CUDA(cudaStreamSynchronize(st));
     if (hs != 0) pg::fail(PAINTY_ERR_CUDA, "stamp kernel reported an internal error");
+  });
+}
+
+painty_status painty_paint_batch(painty_canvas* const* canvases, painty_brush* const* brushes,
+                                 int32_t ncanvas, const painty_stroke_desc* strokes, int64_t nstrokes,
+                                 const double* points, int64_t npoints, int64_t* stamps_out,
+                                 void* stream) {
+  return guard([&] {
+    pg::paint_batch(canvases, brushes, ncanvas, strokes, nstrokes, points, npoints, stamps_out,
+                    pg::as_stream(stream));
   });
 }
 

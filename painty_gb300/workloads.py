@@ -127,3 +127,31 @@ def paint_config0(canvas, brush, strokes_list, on_stroke=None):
         if on_stroke is not None:
             on_stroke(i)
     return total
+
+
+def batch_canvases(n: int, seed: int = 2, smin: float = 256, smax: float = 2048,
+                   strokes_min: int = 50, strokes_max: int = 2000, rmin: float = 4.0,
+                   rmax: float = 64.0, max_strokes=None, pigment_seed: int = 11):
+    """The batching workload: n canvases with side log-uniform in [smin, smax] and aspect
+    U[0.5, 2]; strokes per canvas log-uniform in [strokes_min, strokes_max] (optionally capped
+    at max_strokes); radius log-uniform in [rmin, rmax]; 8 uniform control points; spacing
+    0.25 r; Dirichlet(0.3) paints. Returns [(rows, cols, R0 (rows, cols, 3))] and strokes as
+    (canvas, path, radius, spacing, K, S)."""
+    rng = np.random.default_rng(seed)
+    PK, PS = pigments(pigment_seed)
+    canvases, strokes_out = [], []
+    for c in range(n):
+        side = float(np.exp(rng.uniform(np.log(smin), np.log(smax))))
+        asp = rng.uniform(0.5, 2.0)
+        cols, rows = int(side * np.sqrt(asp)), int(side / np.sqrt(asp))
+        ns = int(np.exp(rng.uniform(np.log(strokes_min), np.log(strokes_max))))
+        if max_strokes is not None:
+            ns = min(ns, max_strokes)
+        canvases.append((rows, cols, rng.uniform(0.80, 0.95, (rows, cols, 3)).astype(np.float32)))
+        for _ in range(ns):
+            path = np.stack([rng.uniform(0, cols, 8), rng.uniform(0, rows, 8)], axis=1)
+            r = float(np.exp(rng.uniform(np.log(rmin), np.log(rmax))))
+            w = rng.dirichlet(np.full(len(PK), 0.3))
+            k, s = mix_single_paint_np(w, PK, PS)
+            strokes_out.append((c, path, r, 0.25 * r, k, s))
+    return canvases, strokes_out

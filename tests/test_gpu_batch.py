@@ -1,0 +1,145 @@
+"""Batched painting (painty_paint_batch) vs sequential painty calls and the oracle (GPU)."""
+import numpy as np
+import pytest
+
+from painty_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def _canvases(rng, n, smin=40, smax=160):
+    out = []
+    for _ in range(n):
+        side = float(np.exp(rng.uniform(np.log(smin), np.log(smax))))
+        asp = rng.uniform(0.5, 2.0)
+        out.append((max(8, int(side / np.sqrt(asp))), max(8, int(side * np.sqrt(asp)))))
+    return out
+
+
+def _session(rng, sizes, strokes_per=(2, 6), rmin=1.5, rmax=20.0):
+    strokes = []
+    for ci, (rows, cols) in enumerate(sizes):
+        for _ in range(int(rng.integers(*strokes_per))):
+            path = np.stack([rng.uniform(-5, cols + 5, 6), rng.uniform(-5, rows + 5, 6)], axis=1)
+            r = float(np.exp(rng.uniform(np.log(rmin), np.log(rmax))))
+            strokes.append((ci, path, r, 0.25 * r if rng.random() < 0.7 else 1.0,
+                            rng.uniform(0.01, 5, 3), rng.uniform(0.05, 3, 3)))
+    # interleave the canvases at random, each canvas's strokes keeping their order
+    queues = {}
+    for s in strokes:
+        queues.setdefault(s[0], []).append(s)
+    seq = []
+    while queues:
+        ci = list(queues)[int(rng.integers(len(queues)))]
+        seq.append(queues[ci].pop(0))
+        if not queues[ci]:
+            del queues[ci]
+    return seq
+
+
+def _setup(pg, sizes, storage, rng_seed=7, snap=True):
+    rng = np.random.default_rng(rng_seed)
+    fp = workloads.footprint_image(seed=7)
+    cs, bs, r0s = [], [], []
+    for rows, cols in sizes:
+        c = pg.Canvas(rows, cols, storage)
+        r0 = rng.uniform(0.8, 0.95, (rows, cols, 3))
+        c.upload("R0", r0)
+        b = pg.FootprintBrush(3.0, fp)
+        b.setPickupRate(0.05)
+        b.setDepositionRate(0.1)
+        b.setUseSnapshotBuffer(snap)
+        cs.append(c)
+        bs.append(b)
+        r0s.append(r0)
+    return cs, bs, r0s
+
+
+@pytest.mark.parametrize("snap", [True, False])
+def test_batch_f64_equals_sequential_and_oracle(pg, oracle, snap):
+    rng = np.random.default_rng(11 + snap)
+    sizes = _canvases(rng, 7)
+    strokes = _session(rng, sizes)
+    cs, bs, r0s = _setup(pg, sizes, "f64", snap=snap)
+    n = pg.paint_batch(cs, bs, strokes)
+    # sequential painty calls through the single-canvas entry points
+    cs2, bs2, _ = _setup(pg, sizes, "f64", snap=snap)
+    n2 = 0
+    for ci, path, r, spacing, K, S in strokes:
+        bs2[ci].setRadius(r)
+        bs2[ci].dip((K, S))
+        n2 += bs2[ci].paintStroke(path, cs2[ci], spacing=spacing)
+    assert n == n2
+    fp = workloads.footprint_image(seed=7)
+    for ci, (rows, cols) in enumerate(sizes):
+        oc = oracle.canvas(rows, cols)
+        oc.set("R0", r0s[ci])
+        ob = oracle.brush(3.0, fp)
+        ob.set_rates(0.05, 0.1)
+        ob.set_snapshot(snap)
+        for cj, path, r, spacing, K, S in strokes:
+            if cj != ci:
+                continue
+            ob.set_radius(r)
+            ob.dip(K, S)
+            ob.paint_stroke(oc, path, spacing)
+        for p in ("K", "S", "V"):
+            a = cs[ci].download(p)
+            assert np.array_equal(a, cs2[ci].download(p)), (ci, p)
+            assert np.array_equal(a, oc.get(p)), (ci, p, "oracle")
+        # the brush keeps the last stroke's pickup map, as the sequential calls leave it
+        assert np.array_equal(bs[ci].getPickupMap("V"), bs2[ci].getPickupMap("V"))
+        assert bs[ci].info() == bs2[ci].info()
+
+
+def test_batch_f32_close_to_sequential(pg):
+    rng = np.random.default_rng(5)
+    sizes = _canvases(rng, 12, 64, 300)
+    strokes = _session(rng, sizes, (3, 9), 2.0, 40.0)
+    cs, bs, _ = _setup(pg, sizes, "f32")
+    pg.paint_batch(cs, bs, strokes)
+    cs2, bs2, _ = _setup(pg, sizes, "f32")
+    for ci, path, r, spacing, K, S in strokes:
+        bs2[ci].setRadius(r)
+        bs2[ci].dip((K, S))
+        bs2[ci].paintStroke(path, cs2[ci], spacing=spacing)
+    for ci in range(len(sizes)):
+        for p in ("K", "S", "V"):
+            a, b = cs[ci].download(p), cs2[ci].download(p)
+            rel = np.abs(a - b) / np.maximum(np.abs(b), 1.0)
+            assert rel.max() <= 1e-4, (ci, p, rel.max())
+
+
+def test_batch_then_single_calls_continue(pg, oracle):
+    """After a batch, the canvas and brush continue exactly as after sequential calls."""
+    rng = np.random.default_rng(9)
+    sizes = [(50, 70)]
+    strokes = _session(rng, sizes, (3, 4))
+    cs, bs, r0s = _setup(pg, sizes, "f64")
+    pg.paint_batch(cs, bs, strokes)
+    extra = np.array([[10.5, 12.5, 0.3], [20.25, 18.0, 1.0]])
+    bs[0].stamps(extra, cs[0])
+    fp = workloads.footprint_image(seed=7)
+    oc = oracle.canvas(50, 70)
+    oc.set("R0", r0s[0])
+    ob = oracle.brush(3.0, fp)
+    ob.set_rates(0.05, 0.1)
+    for _, path, r, spacing, K, S in strokes:
+        ob.set_radius(r)
+        ob.dip(K, S)
+        ob.paint_stroke(oc, path, spacing)
+    ob.stamps(oc, extra)
+    for p in ("K", "S", "V"):
+        assert np.array_equal(cs[0].download(p), oc.get(p)), p
+
+
+def test_batch_rejects_bad_input(pg):
+    fp = workloads.footprint_image(seed=7)
+    c = pg.Canvas(20, 20)
+    b = pg.FootprintBrush(3.0, fp)
+    with pytest.raises(ValueError):
+        pg.paint_batch([c], [b], [(1, np.zeros((2, 2)), 3.0, 1.0, np.ones(3), np.ones(3))])
+    with pytest.raises(ValueError):
+        pg.paint_batch([c, c], [b, b], [])
+    with pytest.raises(ValueError):
+        pg.paint_batch([c], [b], [(0, np.zeros((2, 2)), 3.0, 0.0, np.ones(3), np.ones(3))])
