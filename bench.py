@@ -169,6 +169,15 @@ def generate_stack_device(torch, seed: int):
     return host
 
 
+def run_serve_only(args):
+    import torch
+
+    import painty_gb300 as pg
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    print(json.dumps(run_serve(pg, torch, args.serve_rate, args.serve_seconds)), flush=True)
+
+
 def run_stamps_only(args):
     """The stamping case alone (profiling runs): prints its stamps object."""
     import torch
@@ -293,10 +302,12 @@ def run_ours(args):
     cpu = None
     precision = composite_precision(pg, torch, Kh, Sh, Vh, R0h, max(3, min(args.steps, 100)))
     batch = None
+    serve = None
     if rank == 0 and not args.no_stamps:
         stamps = run_stamps_config0(pg, torch)
         batch = {s_: run_batch(pg, torch, s_, args.batch_canvases, args.batch_max_strokes)
                  for s_ in ("f32", "f16")}
+        serve = run_serve(pg, torch, args.serve_rate, args.serve_seconds)
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(Kh, Sh, Vh, R0h)
     if rank == 0:
@@ -329,6 +340,8 @@ def run_ours(args):
             line["stamps"] = stamps
         if batch is not None:
             line["stamps_batched"] = batch
+        if serve is not None:
+            line["serving"] = serve
         print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist
@@ -396,6 +409,91 @@ def run_batch(pg, torch, storage: str, ncanvas: int, max_strokes):
                       f"{pg_canvas_px(px)}), {len(strokes)} strokes (logU[50,2000] per canvas"
                       f"{'' if max_strokes is None else f', at most {max_strokes}'}), "
                       "r logU[4,64], spacing 0.25 r; one persistent launch"}
+
+
+def run_serve(pg, torch, rate: float, seconds: float, seed: int = 4, budget_gb: float = 120.0,
+              storage: str = "f16"):
+    """Serving: Poisson arrivals at `rate` req/s for `seconds`; each request a canvas of side
+    log-uniform in [512, 4096] (aspect 1) with 1-500 strokes (geometric, mean 60) from the
+    plain case's generators; 30% continue an earlier canvas; FP16 state under the budget."""
+    import threading
+
+    from painty_gb300 import workloads
+
+    rng = np.random.default_rng(seed)
+    PK, PS = workloads.pigments()
+    fp = workloads.footprint_image(seed=7)
+    substrate = rng.uniform(0.8, 0.95, (4096, 4096, 3)).astype(np.float32)
+    n = max(1, int(rng.poisson(rate * seconds)))
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
+    plan = []  # (t, continue_index or -1, rows, cols, strokes)
+    for i in range(n):
+        cont = -1
+        if i > 0 and rng.random() < 0.30:
+            cont = int(rng.integers(0, i))
+            while plan[cont][1] >= 0:  # continue the canvas an earlier request created
+                cont = plan[cont][1]
+            rows, cols = plan[cont][2], plan[cont][3]
+        else:
+            rows = cols = int(np.exp(rng.uniform(np.log(512), np.log(4096))))
+        ns = min(500, int(rng.geometric(1.0 / 60.0)))
+        strokes = []
+        for _ in range(ns):
+            path = np.stack([rng.uniform(0, cols, 8), rng.uniform(0, rows, 8)], axis=1)
+            r = float(rng.uniform(8, 32))
+            w = rng.dirichlet(np.full(len(PK), 0.3))
+            k = (w / w.sum()) @ PK
+            s_ = (w / w.sum()) @ PS
+            strokes.append((path, r, 0.25 * r, k, s_))
+        plan.append((float(arrivals[i]), cont, rows, cols, strokes))
+    srv = pg.Server(int(budget_gb * (1 << 30)), fp, storage=storage, step_stamps=16384)
+    rids = [None] * n
+    cids = [None] * n
+    t0 = time.perf_counter()
+
+    def client():
+        for i, (t, cont, rows, cols, strokes) in enumerate(plan):
+            dt = t - (time.perf_counter() - t0)
+            if dt > 0:
+                time.sleep(dt)
+            if cont >= 0:
+                while cids[cont] is None:
+                    time.sleep(0.0005)
+                rids[i], cids[i] = srv.submit(strokes, canvas_id=cids[cont])
+            else:
+                r0 = np.ascontiguousarray(substrate[:rows, :cols])
+                rids[i], cids[i] = srv.submit(strokes, rows=rows, cols=cols, r0=r0)
+
+    th = threading.Thread(target=client)
+    th.start()
+    th.join()
+    lat, stamps = [], 0
+    for i in range(n):
+        _, l, st = srv.wait(rids[i], -1)
+        lat.append(l)
+        stamps += st
+    wall = time.perf_counter() - t0
+    stats = srv.stats()
+    srv.close()
+    lat = np.array(lat)
+    offered = sum(
+        int(sum(pg_stroke_stamps(p, sp) for p, _, sp, _, _ in strokes)) for *_, strokes in plan)
+    return {"metric": "request latency", "p50_s": round(float(np.percentile(lat, 50)), 4),
+            "p99_s": round(float(np.percentile(lat, 99)), 4),
+            "throughput_req_s": round(n / wall, 2), "stamps_per_s": round(stamps / wall, 1),
+            "requests": n, "arrival_rate": rate, "arrival_window_s": seconds,
+            "offered_stamps_per_s": round(offered / seconds, 1),
+            "wall_s": round(wall, 2), "storage": storage, "budget_gb": budget_gb,
+            "evictions": stats["evictions"], "restores": stats["restores"],
+            "steps": stats["steps"], "peak_resident_gb": round(stats["peak_resident_bytes"] / 2**30, 2),
+            "config": "Poisson arrivals; canvas side logU[512,4096]; 1-500 strokes (geometric, "
+                      "mean 60), r U[8,32], spacing 0.25 r; 30% continue an earlier canvas; "
+                      "composite returned per request"}
+
+
+def pg_stroke_stamps(path, spacing):
+    d = np.linalg.norm(np.diff(path, axis=0), axis=1)
+    return int(np.sum(np.floor(d / spacing)))
 
 
 def pg_canvas_px(px):
@@ -517,6 +615,9 @@ def main():
                     help="cap on strokes per canvas in the batched stamping case")
     ap.add_argument("--strokes", type=int, default=200, help="strokes in the stamping case")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--serve-only", action="store_true", help="only the serving case")
+    ap.add_argument("--serve-rate", type=float, default=20.0, help="serving arrivals per second")
+    ap.add_argument("--serve-seconds", type=float, default=5.0, help="serving arrival window")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -525,6 +626,8 @@ def main():
         run_reference(args)
     elif args.stamps_only:
         run_stamps_only(args)
+    elif args.serve_only:
+        run_serve_only(args)
     else:
         run_ours(args)
 
