@@ -125,6 +125,7 @@ void canvas_relayout(painty_canvas* c, void* base) {
   const size_t ib = image_bytes(rows, cols, rs);
   layer_layout(c->wet, rows, cols, st, base);
   c->wet.owned = false;
+  c->wet.writes = &c->version;
   image_layout(c->r0, rows, cols, rs, static_cast<char*>(base) + lb);
   c->r0.owned = false;
   c->h = static_cast<char*>(base) + lb + ib;
@@ -592,6 +593,7 @@ painty_status painty_layer_clear(painty_layer* layer, void* stream) {
   return guard([&] {
     PG_REQUIRE(layer != nullptr, "layer is null");
     PG_CUDA(cudaMemsetAsync(layer->base, 0, layer->bytes, pg::as_stream(stream)));
+    layer->touch();
   });
 }
 
@@ -627,6 +629,7 @@ painty_status painty_layer_upload(painty_layer* layer, painty_plane plane, const
     layer_plane_ptrs(layer, plane, p, &nch, &dt);
     pg::upload_planes(p, nch, dt, layer->rows, layer->cols, layer->pitch, host, fmt,
                       pg::as_stream(stream));
+    layer->touch();
   });
 }
 
@@ -651,6 +654,7 @@ painty_status painty_layer_copy(const painty_layer* src, painty_layer* dst, void
                "layers differ in size or storage");
     PG_CUDA(cudaMemcpyAsync(dst->base, src->base, src->bytes, cudaMemcpyDeviceToDevice,
                             pg::as_stream(stream)));
+    dst->touch();
   });
 }
 
@@ -763,6 +767,7 @@ painty_status painty_canvas_create(int32_t rows, int32_t cols, painty_storage st
       c->base = pg::device_alloc(c->bytes);
       pg::layer_layout(c->wet, rows, cols, storage, c->base);
       c->wet.owned = false;
+      c->wet.writes = &c->version;
       pg::image_layout(c->r0, rows, cols, rs, static_cast<char*>(c->base) + lb);
       c->r0.owned = false;
       c->h = static_cast<char*>(c->base) + lb + ib;

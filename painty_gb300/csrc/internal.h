@@ -77,6 +77,11 @@ struct painty_layer {
   void* S[3] = {nullptr, nullptr, nullptr};
   void* V = nullptr;
   bool owned = true;
+  // a canvas's wet layer: the canvas's write counter, bumped by every write through the layer
+  uint64_t* writes = nullptr;
+  void touch() const {
+    if (writes) ++*writes;
+  }
   int64_t plane_elems() const { return static_cast<int64_t>(rows) * pitch; }
 };
 
@@ -133,14 +138,16 @@ struct painty_brush {
   // snapshot (FootprintBrush.hxx:471): canvas-sized layer, allocated at first use
   painty_layer snapshot;
   bool has_snapshot = false;
-  // snapshot dirty map (canvas rows x pitch bytes) and the canvas state it describes
-  void* d_dirty = nullptr;
-  size_t d_dirty_bytes = 0;
-  uint64_t dirty_canvas = 0;
-  uint64_t dirty_version = 0;
+  // snapshot-ring state on the device (box and grown box of the last stamp painted with the
+  // snapshot) and the canvas state it describes; ring_pending: a reset mode for the next run
+  // (-1 none)
+  uint64_t ring_canvas = 0;
+  uint64_t ring_version = 0;
+  int ring_pending = -1;
   void* d_stamps = nullptr;
   size_t d_stamps_bytes = 0;
-  unsigned* d_status = nullptr;
+  unsigned* d_status = nullptr;  // 16 words: [0] kernel status, [8..15] the ring state
+  int* d_ring() const { return reinterpret_cast<int*>(d_status) + 8; }
 };
 
 namespace pg {

@@ -63,7 +63,7 @@ struct ServerCanvas {
   size_t bytes = 0;  // device bytes when resident
   std::vector<float> r0;  // substrate until the canvas is created
   std::deque<uint64_t> waiting;  // its unfinished requests, in submission order
-  HostBlob save_canvas, save_snapshot, save_dirty;
+  HostBlob save_canvas, save_snapshot;
 };
 
 struct ServerRequest {
@@ -111,10 +111,10 @@ size_t canvas_device_bytes(const painty_server* s, int32_t rows, int32_t cols) {
   const size_t pe = static_cast<size_t>(rows) * pg::pitch_for(cols);
   return pg::layer_bytes(rows, cols, st) + pg::image_bytes(rows, cols, rs) +
          pe * pg::v_bytes(st) + pg::layer_bytes(rows, cols, st) /* snapshot */ +
-         pe /* dirty map */ + (4u << 20) /* pickup map, footprint, scratch */;
+         (4u << 20) /* pickup map, footprint, scratch */;
 }
 
-// Moves a canvas's device state (canvas planes, the brush's snapshot and dirty map) to
+// Moves a canvas's device state (canvas planes and the brush's snapshot) to
 // pinned host memory and frees it on the device.
 void evict(painty_server* s, ServerCanvas* c) {
   painty_canvas* cv = c->cv;
@@ -126,9 +126,6 @@ void evict(painty_server* s, ServerCanvas* c) {
     c->save_snapshot.ensure(b->snapshot.bytes);
     PG_CUDA(cudaMemcpyAsync(c->save_snapshot.p, b->snapshot.base, b->snapshot.bytes,
                             cudaMemcpyDeviceToHost, s->stream));
-    const size_t db = static_cast<size_t>(b->snapshot.plane_elems());
-    c->save_dirty.ensure(db);
-    PG_CUDA(cudaMemcpyAsync(c->save_dirty.p, b->d_dirty, db, cudaMemcpyDeviceToHost, s->stream));
   }
   PG_CUDA(cudaStreamSynchronize(s->stream));
   pg::device_free(cv->base);
@@ -136,9 +133,6 @@ void evict(painty_server* s, ServerCanvas* c) {
   if (b->has_snapshot) {
     pg::device_free(b->snapshot.base);
     b->snapshot.base = nullptr;
-    pg::device_free(b->d_dirty);
-    b->d_dirty = nullptr;
-    b->d_dirty_bytes = 0;
   }
   c->resident = false;
 }
@@ -154,10 +148,6 @@ void restore(painty_server* s, ServerCanvas* c) {
     PG_CUDA(cudaMemcpyAsync(sb, c->save_snapshot.p, b->snapshot.bytes, cudaMemcpyHostToDevice,
                             s->stream));
     pg::layer_layout(b->snapshot, b->snapshot.rows, b->snapshot.cols, b->snapshot.storage, sb);
-    const size_t db = static_cast<size_t>(b->snapshot.plane_elems());
-    b->d_dirty = pg::device_alloc(db);
-    b->d_dirty_bytes = db;
-    PG_CUDA(cudaMemcpyAsync(b->d_dirty, c->save_dirty.p, db, cudaMemcpyHostToDevice, s->stream));
   }
   PG_CUDA(cudaStreamSynchronize(s->stream));
   c->resident = true;

@@ -104,10 +104,15 @@ struct StampArgs {
   M pickupRate, depositionRate, capacity;
   M paintK[3], paintS[3];
   int32_t use_snapshot;
-  // Snapshot dirty map (rows x pitch bytes): 1 where the snapshot may differ from the canvas.
-  // The ring refresh copies only dirty pixels (copying an equal pixel is a no-op); pixels a
-  // stamp changes are marked. NULL: refresh the whole ring.
-  uint8_t* dirty;
+  // Snapshot-ring state (8 ints in device memory, may be NULL): the box and the grown box of
+  // the last stamp this brush applied with a snapshot, read before the first stamp and
+  // written after the last. ring_reset overrides it: kRingKeep uses it, kRingUnknown
+  // refreshes the whole first ring, kRingClean treats the snapshot as equal to the canvas.
+  int* ring;
+  int32_t ring_reset;
+  // Box pixels inside the support disc, listed (row-major) in shared memory for the launch,
+  // with a per-stamp cell map of the box; 0: no list, every stamp paints in waves
+  int32_t ndisc;
   int32_t pickup_zero;    // the map starts cleared (a dip or new radius since the last run)
   int32_t pickup_smem;    // stage the pickup map in shared memory for the launch
   int32_t footprint_smem; // stage the footprint in shared memory
@@ -136,31 +141,28 @@ __device__ __forceinline__ int map_coord(float fast, int u, double ca, int v, do
   return static_cast<int>(round(__dadd_rn(r, static_cast<double>(w))));
 }
 
-// blend (FootprintBrush.hxx:331-340): (va a + vb b) / (va + vb) when va + vb > MinVolume.
-// FP64 divides as the reference; FP32 multiplies by the correctly rounded reciprocal.
-__device__ __forceinline__ void blend3(double va, const double (&a)[3], double vb,
-                                       const double (&b)[3], double (&r)[3]) {
+// blend (FootprintBrush.hxx:331-340) of the K and S triples together (same volumes):
+// (va a + vb b) / (va + vb) when va + vb > MinVolume, else a. FP64 divides as the reference;
+// FP32 multiplies by the hardware reciprocal (relative error ~1e-7), branch-free.
+__device__ __forceinline__ void blend6(double va, const double (&a)[6], double vb,
+                                       const double (&b)[6], double (&r)[6]) {
   const double tot = __dadd_rn(va, vb);
   if (tot > 0.001) {
 #pragma unroll
-    for (int i = 0; i < 3; i++)
+    for (int i = 0; i < 6; i++)
       r[i] = __ddiv_rn(__dadd_rn(__dmul_rn(va, a[i]), __dmul_rn(vb, b[i])), tot);
   } else {
 #pragma unroll
-    for (int i = 0; i < 3; i++) r[i] = a[i];
+    for (int i = 0; i < 6; i++) r[i] = a[i];
   }
 }
-__device__ __forceinline__ void blend3(float va, const float (&a)[3], float vb,
-                                       const float (&b)[3], float (&r)[3]) {
+__device__ __forceinline__ void blend6(float va, const float (&a)[6], float vb,
+                                       const float (&b)[6], float (&r)[6]) {
   const float tot = va + vb;
-  if (tot > 0.001f) {
-    const float inv = __frcp_rn(tot);
+  const bool mix = tot > 0.001f;
+  const float inv = rcp_approx(tot);
 #pragma unroll
-    for (int i = 0; i < 3; i++) r[i] = fmaf(va, a[i], vb * b[i]) * inv;
-  } else {
-#pragma unroll
-    for (int i = 0; i < 3; i++) r[i] = a[i];
-  }
+  for (int i = 0; i < 6; i++) r[i] = mix ? fmaf(va, a[i], vb * b[i]) * inv : a[i];
 }
 
 // Plane p (K r,g,b, S r,g,b, V) of the pickup map in global memory.
@@ -171,82 +173,72 @@ __device__ __forceinline__ M* pickup_plane(const StampArgs<TK, TV>& a, int p) {
 
 // pickupPaint then depositPaint for one stamp pixel (FootprintBrush.hxx:349-431); fp > 0.
 // PS: the pickup map is staged in shared memory at `pbase` (7 planes `cells` apart).
+// Triples are handled as K r,g,b then S r,g,b.
 template <bool PS, class TK, class TV, class M>
 __device__ __forceinline__ void process_pixel(const StampArgs<TK, TV>& a, M* pbase, int cells,
-                                              M fp, int64_t c, int m) {
+                                              M fp, int c, int m) {
   using A = Arith<M>;
   auto cell = [&](int p) -> M& {
     if constexpr (PS) return pbase[p * cells + m];
     else return pickup_plane<TK, TV, M>(a, p)[m];
   };
-  // independent loads first: pickup cell, pickup source, canvas pixel
+  // every load first (one round trip): pickup cell, canvas pixel, snapshot pixel
   M vp = cell(6);
-  M kp[3], sp[3], ck[3], cs[3];
+  M pk[6], cn[6], sn[6];
 #pragma unroll
   for (int i = 0; i < 3; i++) {
-    kp[i] = cell(i);
-    sp[i] = cell(3 + i);
-    ck[i] = ld_elem<M>(a.cK[i] + c);
-    cs[i] = ld_elem<M>(a.cS[i] + c);
+    pk[i] = cell(i);
+    pk[3 + i] = cell(3 + i);
+    cn[i] = ld_elem<M>(a.cK[i] + c);
+    cn[3 + i] = ld_elem<M>(a.cS[i] + c);
   }
   const M vsrc = ld_elem<M>(a.sV + c);
   M vcan = ld_elem<M>(a.cV + c);
-  // pickupPaint
-  const M vleave = A::mul(A::mul(a.pickupRate, vsrc), fp);
-  bool pk_changed = false;
-  if (vleave > M(0.001)) {
-    st_elem<M>(a.sV + c, A::sub(vsrc, vleave));
-    M ks[3], ss[3], nk[3], ns[3];
-    if (a.use_snapshot) {
-#pragma unroll
-      for (int i = 0; i < 3; i++) {
-        ks[i] = ld_elem<M>(a.sK[i] + c);
-        ss[i] = ld_elem<M>(a.sS[i] + c);
-      }
-    } else {  // the pickup source is the canvas itself
-#pragma unroll
-      for (int i = 0; i < 3; i++) {
-        ks[i] = ck[i];
-        ss[i] = cs[i];
-      }
-      vcan = ld_elem<M>(a.cV + c);  // the stored remainder
-    }
-    blend3(vp, kp, vleave, ks, nk);
-    blend3(vp, sp, vleave, ss, ns);
+  if (a.use_snapshot) {
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-      kp[i] = nk[i];
-      sp[i] = ns[i];
+      sn[i] = ld_elem<M>(a.sK[i] + c);
+      sn[3 + i] = ld_elem<M>(a.sS[i] + c);
+    }
+  } else {  // the pickup source is the canvas itself
+#pragma unroll
+    for (int i = 0; i < 6; i++) sn[i] = cn[i];
+  }
+  // pickupPaint
+  const M vleave = A::mul(A::mul(a.pickupRate, vsrc), fp);
+  if (vleave > M(0.001)) {
+    st_elem<M>(a.sV + c, A::sub(vsrc, vleave));
+    if (!a.use_snapshot) vcan = ld_elem<M>(a.cV + c);  // the stored remainder
+    M np[6];
+    blend6(vp, pk, vleave, sn, np);
+#pragma unroll
+    for (int i = 0; i < 6; i++) {
+      pk[i] = np[i];
+      cell(i) = np[i];
     }
     vp = A::add(vp, vleave);
-    pk_changed = true;
   }
   // depositPaint
   const M dfree = A::sub(a.capacity, vp);
   const M vfree = (M(0) < dfree) ? dfree : M(0);  // std::max(0.0, x)
-  M ksrc[3], ssrc[3];
-  blend3(vp, kp, vfree, a.paintK, ksrc);
-  blend3(vp, sp, vfree, a.paintS, ssrc);
-  const M pleave = A::mul(A::mul(a.depositionRate, vp), fp);
-  cell(6) = A::sub(vp, pleave);
-  if (pk_changed) {
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-      cell(i) = kp[i];
-      cell(3 + i) = sp[i];
-    }
-  }
-  const M vb = A::mul(a.capacity, fp);
-  M nk[3], ns[3];
-  blend3(vb, ksrc, vcan, ck, nk);
-  blend3(vb, ssrc, vcan, cs, ns);
+  M paint[6], src[6];
 #pragma unroll
   for (int i = 0; i < 3; i++) {
-    st_elem<M>(a.cK[i] + c, nk[i]);
-    st_elem<M>(a.cS[i] + c, ns[i]);
+    paint[i] = a.paintK[i];
+    paint[3 + i] = a.paintS[i];
+  }
+  blend6(vp, pk, vfree, paint, src);
+  const M pleave = A::mul(A::mul(a.depositionRate, vp), fp);
+  cell(6) = A::sub(vp, pleave);
+  const M vb = A::mul(a.capacity, fp);
+  M out[6];
+  blend6(vb, src, vcan, cn, out);
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    st_elem<M>(a.cK[i] + c, out[i]);
+    st_elem<M>(a.cS[i] + c, out[3 + i]);
   }
   st_elem<M>(a.cV + c, A::add(vb, vcan));
-  if (a.dirty) a.dirty[c] = 1;
 }
 
 struct PixelInfo {
@@ -254,21 +246,27 @@ struct PixelInfo {
   bool live;  // inside canvas and map, and a positive footprint: the pixel changes state
 };
 
+// Pickup-map cell of stamp pixel (dc, dr) (offsets from the box centre): the reference's
+// round(R(-theta) (dc, dr)) + wr, through map_coord.
+__device__ __forceinline__ void map_cell(const StampParams& sp, int dc, int dr, int wr, int* mx,
+                                         int* my) {
+  const float dcf = static_cast<float>(dc), drf = static_cast<float>(dr);
+  const float wrf = static_cast<float>(wr);
+  const float fx = fmaf(-drf, sp.sf, dcf * sp.cf) + wrf;  // col*cos - row*sin + wr
+  const float fy = fmaf(drf, sp.cf, dcf * sp.sf) + wrf;   // col*sin + row*cos + hr
+  *mx = map_coord(fx, dc, sp.c, dr, sp.s, true, wr);
+  *my = map_coord(fy, dc, sp.s, dr, sp.c, false, wr);
+}
+
 // Stamp pixel (row, col) of the F x F box: canvas pixel, pickup-map cell, footprint height.
 template <class TK, class TV, class M>
 __device__ __forceinline__ PixelInfo pixel_info(const StampArgs<TK, TV>& a, const StampParams& sp,
                                                 const int* xs, const int* ys, const M* fps,
                                                 int row, int col, M* fp_out) {
   PixelInfo p;
-  const int dr = row - a.wr, dc = col - a.wr;
   p.xc = xs[col];
   p.yc = ys[row];
-  const float dcf = static_cast<float>(dc), drf = static_cast<float>(dr);
-  const float wrf = static_cast<float>(a.wr);
-  const float fx = fmaf(-drf, sp.sf, dcf * sp.cf) + wrf;  // col*cos - row*sin + wr
-  const float fy = fmaf(drf, sp.cf, dcf * sp.sf) + wrf;   // col*sin + row*cos + hr
-  p.mx = map_coord(fx, dc, sp.c, dr, sp.s, true, a.wr);
-  p.my = map_coord(fy, dc, sp.s, dr, sp.c, false, a.wr);
+  map_cell(sp, col - a.wr, row - a.wr, a.wr, &p.mx, &p.my);
   const bool inside = p.yc >= 0 && p.xc >= 0 && p.xc < a.cols && p.yc < a.rows && p.my >= 0 &&
                       p.mx >= 0 && p.mx < a.S && p.my < a.S;
   M fp = M(0);
@@ -329,13 +327,14 @@ __host__ __device__ constexpr size_t align_up(size_t x, size_t a) {
   return (x + a - 1) / a * a;
 }
 
-// Dynamic shared memory layout of stamp_kernel (all offsets 16-byte aligned).
+// Dynamic shared memory layout of stamp_kernel (all offsets 16-byte aligned). The per-stamp
+// arrays (canvas columns / rows of the box, edge-duplicate flags) are double-buffered: the
+// next stamp is set up while the current one is painted.
 struct StampSmem {
-  size_t fp, pick, own, xs, ys, done_c, done_r, queue, total;
+  size_t fp, pick, own, xs, ys, done_c, done_r, disc, cellmap, total;
 };
-constexpr int kRefreshQueue = 2048;  // snapshot-refresh queue entries (canvas offsets)
 template <class M>
-__host__ __device__ inline StampSmem stamp_smem_layout(int F, int S, bool fp_smem,
+__host__ __device__ inline StampSmem stamp_smem_layout(int F, int S, int ndisc, bool fp_smem,
                                                        bool pick_smem, bool own_smem) {
   StampSmem L{};
   size_t o = 0;
@@ -346,15 +345,17 @@ __host__ __device__ inline StampSmem stamp_smem_layout(int F, int S, bool fp_sme
   L.own = o;
   if (own_smem) o = align_up(o + size_t(S) * S * sizeof(int), 16);
   L.xs = o;
-  o = align_up(o + size_t(F) * sizeof(int), 16);
+  o = align_up(o + size_t(2) * F * sizeof(int), 16);
   L.ys = o;
-  o = align_up(o + size_t(F) * sizeof(int), 16);
+  o = align_up(o + size_t(2) * F * sizeof(int), 16);
   L.done_c = o;
-  o = align_up(o + size_t(F) * sizeof(uint16_t), 16);
+  o = align_up(o + size_t(2) * F * sizeof(uint16_t), 16);
   L.done_r = o;
-  o = align_up(o + size_t(F) * sizeof(uint16_t), 16);
-  L.queue = o;
-  o = align_up(o + size_t(kRefreshQueue) * sizeof(int), 16);
+  o = align_up(o + size_t(2) * F * sizeof(uint16_t), 16);
+  L.disc = o;
+  if (ndisc > 0) o = align_up(o + size_t(ndisc) * sizeof(uint32_t), 16);
+  L.cellmap = o;
+  if (ndisc > 0) o = align_up(o + size_t(F) * F * sizeof(int), 16);
   L.total = o;
   return L;
 }
@@ -362,113 +363,142 @@ __host__ __device__ inline StampSmem stamp_smem_layout(int F, int S, bool fp_sme
 constexpr int kEpochMax = 32767;  // owner keys: ((kEpochMax - epoch) << 16) | pixel index
 constexpr int kWarps = kStampThreads / 32;
 
-// Snapshot refresh, pass 1: scan the dirty bytes of ring row segment [lo, hi] four at a
-// time (one 32-bit word per lane) and queue the dirty pixels (canvas offsets) in shared
-// memory; a pixel's dirty byte is cleared only once it is queued, so entries past the queue's
-// end stay dirty (and flag an overflow) for the next scan. Requires a dirty map.
-template <class TK, class TV>
-__device__ __forceinline__ void scan_segment(const StampArgs<TK, TV>& a, int row, int lo, int hi,
-                                             int lane, int* queue, int* qcount, int* qover) {
-  const int64_t rb = static_cast<int64_t>(row) * a.pitch;
-  for (int w0 = (lo & ~3); w0 <= hi; w0 += 4 * 32) {
-    const int w = w0 + 4 * lane;
-    uint32_t word = 0, take = 0;
-    if (w <= hi) {
-      word = *reinterpret_cast<const uint32_t*>(a.dirty + rb + w);
+// ---------------------------------------------------------------------- snapshot ring
+// painty refreshes the snapshot from the canvas over a ring around every stamp: the box grown
+// by the radius, the strict interior of the box excepted (FootprintBrush.hxx:291-318). Only
+// part of a ring can differ from the snapshot. A pixel of ring j outside box j-1 that was
+// inside grown box j-1 lay in ring j-1 (the grown box minus an interior inside the box), so
+// it was refreshed by stamp j-1 and not written since (a stamp writes canvas and snapshot
+// only inside its box). Ring j therefore needs copying only where it meets box j-1 or leaves
+// grown box j-1; the rest would be a copy of equal values. The two parts are disjoint (box
+// j-1 within the canvas lies inside grown box j-1) and are cut into at most 20 rectangles.
+constexpr int kRingKeep = 0, kRingUnknown = 1, kRingClean = 2;
+constexpr int kRefreshRects = 20;
+
+struct IRect {
+  int x0, y0, x1, y1;  // inclusive; empty when x0 > x1 or y0 > y1
+};
+
+struct RefreshList {
+  int4 rect[kRefreshRects];
+  int pre[kRefreshRects + 1];  // prefix sums of the rectangle areas
+};
+
+// Static shared state of the stamp loop.
+struct StampShared {
+  RefreshList rl[2];  // double-buffered with the per-stamp arrays
+  int prev[8];        // box, grown box of the stamp before the current parameter chunk
+};
+
+__device__ __forceinline__ bool rect_empty(const IRect& r) { return r.x0 > r.x1 || r.y0 > r.y1; }
+
+// Piece i (0 top, 1 bottom, 2 left, 3 right) of X with H cut out; X itself as piece 0 when
+// H misses X.
+__device__ __forceinline__ IRect rect_piece(const IRect& X, const IRect& H, int i) {
+  const IRect none{0, 0, -1, -1};
+  if (rect_empty(X)) return none;
+  const int hx0 = max(H.x0, X.x0), hx1 = min(H.x1, X.x1);
+  const int hy0 = max(H.y0, X.y0), hy1 = min(H.y1, X.y1);
+  if (hx0 > hx1 || hy0 > hy1) return i == 0 ? X : none;
+  switch (i) {
+    case 0: return IRect{X.x0, X.y0, X.x1, hy0 - 1};
+    case 1: return IRect{X.x0, hy1 + 1, X.x1, X.y1};
+    case 2: return IRect{X.x0, hy0, hx0 - 1, hy1};
+    default: return IRect{hx1 + 1, hy0, X.x1, hy1};
+  }
+}
+
+// Box (canvas pixels a stamp may write) and grown box (clipped) of a stamp as 8 ints.
+__device__ __forceinline__ void stamp_rects(const StampParams& sp, int* out) {
+  out[0] = sp.tl[0];
+  out[1] = sp.tl[1];
+  out[2] = sp.br[0];
+  out[3] = sp.br[1];
+  out[4] = sp.tla[0];
+  out[5] = sp.tla[1];
+  out[6] = sp.bra[0];
+  out[7] = sp.bra[1];
+}
+
+// Warp 0: the rectangles of ring pixels to copy for the stamp `sp`, given the previous
+// stamp's box and grown box (prev[0..7]).
+__device__ __forceinline__ void build_refresh(const StampParams& sp, const int* prev, int lane,
+                                              RefreshList* rl) {
+  const IRect G{sp.tla[0], sp.tla[1], sp.bra[0], sp.bra[1]};
+  const IRect I{sp.tl[0] + 1, sp.tl[1] + 1, sp.br[0] - 1, sp.br[1] - 1};
+  const IRect Bp{prev[0], prev[1], prev[2], prev[3]};
+  const IRect Gp{prev[4], prev[5], prev[6], prev[7]};
+  IRect r{0, 0, -1, -1};
+  if (lane < 4) {  // ring pixels inside the previous box
+    const IRect X{max(Bp.x0, G.x0), max(Bp.y0, G.y0), min(Bp.x1, G.x1), min(Bp.y1, G.y1)};
+    r = rect_piece(X, I, lane);
+  } else if (lane < kRefreshRects) {  // ring pixels outside the previous grown box
+    const IRect X = rect_piece(G, Gp, (lane - 4) >> 2);
+    r = rect_piece(X, I, (lane - 4) & 3);
+  }
+  const int area = rect_empty(r) ? 0 : (r.x1 - r.x0 + 1) * (r.y1 - r.y0 + 1);
+  int incl = area;
 #pragma unroll
-      for (int b = 0; b < 4; b++) {
-        const int col = w + b;
-        if (col >= lo && col <= hi && ((word >> (8 * b)) & 0xffu)) take |= 1u << b;
+  for (int d = 1; d < 32; d <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += v;
+  }
+  if (lane < kRefreshRects) {
+    rl->rect[lane] = make_int4(r.x0, r.y0, r.x1, r.y1);
+    rl->pre[lane + 1] = incl;
+  }
+  if (lane == 0) rl->pre[0] = 0;
+}
+
+// All threads: copy the listed ring pixels canvas -> snapshot (7 planes), four pixels per
+// thread in flight.
+template <class TK, class TV>
+__device__ __forceinline__ void refresh_ring(const StampArgs<TK, TV>& a, const RefreshList& rl,
+                                             int tid, int T) {
+  const int total = rl.pre[kRefreshRects];
+  constexpr int U = 2;
+  for (int base = 0; base < total; base += U * T) {
+    int64_t off[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int idx = base + u * T + tid;
+      off[u] = -1;
+      if (idx < total) {
+        int r = 0;
+#pragma unroll
+        for (int q = 1; q < kRefreshRects; q++) r += idx >= rl.pre[q] ? 1 : 0;
+        const int4 R = rl.rect[r];
+        const int w = R.z - R.x + 1;
+        const int local = idx - rl.pre[r];
+        const int dy = local / w;
+        off[u] = static_cast<int64_t>(R.y + dy) * a.pitch + (R.x + local - dy * w);
       }
     }
-    const int n = __popc(take);
-    int incl = n;  // warp inclusive prefix sum of the counts
+    TK k[U][3], s[U][3];
+    TV v[U];
 #pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      const int v = __shfl_up_sync(0xffffffffu, incl, d);
-      if (lane >= d) incl += v;
-    }
-    const int total = __shfl_sync(0xffffffffu, incl, 31);
-    int base = 0;
-    if (lane == 31 && total > 0) base = atomicAdd(qcount, total);
-    base = __shfl_sync(0xffffffffu, base, 31);
-    int slot = base + incl - n;
-    uint32_t cleared = word;
-    for (int b = 0; b < 4; b++) {
-      if (!((take >> b) & 1u)) continue;
-      if (slot < kRefreshQueue) {
-        queue[slot] = static_cast<int>(rb + w + b);
-        cleared &= ~(0xffu << (8 * b));
-      } else {
-        *qover = 1;
+    for (int u = 0; u < U; u++) {
+      if (off[u] < 0) continue;
+#pragma unroll
+      for (int ch = 0; ch < 3; ch++) {
+        k[u][ch] = a.cK[ch][off[u]];
+        s[u][ch] = a.cS[ch][off[u]];
       }
-      slot++;
+      v[u] = a.cV[off[u]];
     }
-    if (take && cleared != word) *reinterpret_cast<uint32_t*>(a.dirty + rb + w) = cleared;
-  }
-}
-
-// Snapshot refresh without a dirty map: copy every pixel of the segment.
-template <class TK, class TV>
-__device__ __forceinline__ void copy_segment(const StampArgs<TK, TV>& a, int row, int lo, int hi,
-                                             int lane) {
-  const int64_t rb = static_cast<int64_t>(row) * a.pitch;
-  for (int col = lo + lane; col <= hi; col += 32) {
-    const int64_t o = rb + col;
 #pragma unroll
-    for (int ch = 0; ch < 3; ch++) {
-      a.sK[ch][o] = a.cK[ch][o];
-      a.sS[ch][o] = a.cS[ch][o];
-    }
-    a.sV[o] = a.cV[o];
-  }
-}
-
-// Snapshot refresh, pass 2: copy the queued pixels canvas -> snapshot (7 planes).
-template <class TK, class TV>
-__device__ __forceinline__ void copy_queued(const StampArgs<TK, TV>& a, const int* queue,
-                                            int count, int tid, int T) {
-  for (int q = tid; q < count; q += T) {
-    const int64_t o = queue[q];
-    TK k[3], s[3];
+    for (int u = 0; u < U; u++) {
+      if (off[u] < 0) continue;
 #pragma unroll
-    for (int ch = 0; ch < 3; ch++) {
-      k[ch] = a.cK[ch][o];
-      s[ch] = a.cS[ch][o];
-    }
-    const TV v = a.cV[o];
-#pragma unroll
-    for (int ch = 0; ch < 3; ch++) {
-      a.sK[ch][o] = k[ch];
-      a.sS[ch][o] = s[ch];
-    }
-    a.sV[o] = v;
-  }
-}
-
-// The ring of a stamp: rows of the grown box, the strict interior of the box excepted
-// (FootprintBrush.hxx:307-318); one warp per row. With a dirty map the dirty pixels are
-// queued (copied by copy_queued); without one every ring pixel is copied here.
-template <class TK, class TV>
-__device__ __forceinline__ void scan_ring(const StampArgs<TK, TV>& a, const StampParams& sp,
-                                          int warp, int lane, int nwarps, int* queue,
-                                          int* qcount, int* qover) {
-  for (int row = sp.tla[1] + warp; row <= sp.bra[1]; row += nwarps) {
-    const bool interior_row = row > sp.tl[1] && row < sp.br[1];
-    const int lo0 = sp.tla[0], hi0 = interior_row ? min(sp.tl[0], sp.bra[0]) : sp.bra[0];
-    const int lo1 = max(sp.br[0], sp.tla[0]), hi1 = interior_row ? sp.bra[0] : -1;
-    if (a.dirty) {
-      scan_segment(a, row, lo0, hi0, lane, queue, qcount, qover);
-      scan_segment(a, row, lo1, hi1, lane, queue, qcount, qover);
-    } else {
-      copy_segment(a, row, lo0, hi0, lane);
-      copy_segment(a, row, lo1, hi1, lane);
+      for (int ch = 0; ch < 3; ch++) {
+        a.sK[ch][off[u]] = k[u][ch];
+        a.sS[ch][off[u]] = s[u][ch];
+      }
+      a.sV[off[u]] = v[u];
     }
   }
 }
 
-// One CTA applies the stamps in order. Pixel slots: warp w owns box rows w, w+32, ...; lane l
-// owns columns l, l+32, ...; slot j = jr * NC + jc (jr-th row, jc-th column of the thread).
 // Stamps of a host-built record list (imprint / painty_stamps / painty_stroke).
 struct RecordSource {
   const StampRec* recs;
@@ -477,34 +507,212 @@ struct RecordSource {
   __device__ __forceinline__ StampRec get(int64_t k) const { return recs[k]; }
 };
 
+// Painting of a stamp without edge duplicates. A stamp pixel changes state only through its
+// pickup-map cell (where the footprint is positive) and its canvas pixel. Canvas pixels of
+// different stamp pixels differ unless truncation maps two box columns (rows) at the canvas's
+// left (top) edge to one (`dup` stamps, painted in waves). Otherwise stamp pixels conflict
+// only through cells, and the pixels of one cell lie within sqrt(2) of each other (each lies
+// within sqrt(1/2) of the cell's rotated centre: rounding moves a map coordinate by at most
+// 1/2), so they are 8-neighbours. Each cell's first pixel in painty's row-major order
+// (no earlier neighbour maps to the cell) paints itself and then its later neighbours that
+// map to the cell, in row-major order; cells are independent.
+//
+// Pass 1: cell of every support-disc pixel (packed my << 16 | mx; -1 when the pixel changes
+// nothing: outside the canvas or the map, or a zero footprint).
+template <class TK, class TV, class M>
+__device__ __forceinline__ void classify_disc(const StampArgs<TK, TV>& a, const StampParams& sp,
+                                              const int* xs, const int* ys, const M* fps,
+                                              const uint32_t* disc, int ndisc, int* cellmap,
+                                              int tid, int T) {
+  const int F = a.F;
+  for (int i = tid; i < ndisc; i += T) {
+    const uint32_t e = disc[i];
+    const int row = static_cast<int>(e >> 16), col = static_cast<int>(e & 0xffffu);
+    M fp;
+    const PixelInfo p = pixel_info(a, sp, xs, ys, fps, row, col, &fp);
+    cellmap[row * F + col] = p.live ? ((p.my << 16) | p.mx) : -1;
+  }
+}
+
+// Pass 2: first pixels paint their cell's pixels.
+template <bool PS, class TK, class TV, class M>
+__device__ __forceinline__ void paint_disc(const StampArgs<TK, TV>& a, const int* xs, const int* ys,
+                                        const M* fps, M* pbase, const uint32_t* disc, int ndisc,
+                                        const int* cellmap, int tid, int T) {
+  const int F = a.F, S = a.S;
+  const int cells = S * S;
+  const int pitch32 = static_cast<int>(a.pitch);  // planes hold fewer than 2^31 elements
+  for (int i = tid; i < ndisc; i += T) {
+    const uint32_t e = disc[i];
+    const int row = static_cast<int>(e >> 16), col = static_cast<int>(e & 0xffffu);
+    const int* cm = cellmap + row * F + col;
+    const int m = cm[0];
+    if (m < 0) continue;
+    const bool l = col > 0, r = col + 1 < F, u = row > 0, d = row + 1 < F;
+    if ((l && cm[-1] == m) || (u && cm[-F] == m) || (u && l && cm[-F - 1] == m) ||
+        (u && r && cm[-F + 1] == m))
+      continue;  // a later pixel of its cell
+    // later pixels of the cell, row-major: right, down-left, down, down-right
+    unsigned follow = 0;
+    if (r && cm[1] == m) follow |= 1u;
+    if (d && l && cm[F - 1] == m) follow |= 2u;
+    if (d && cm[F] == m) follow |= 4u;
+    if (d && r && cm[F + 1] == m) follow |= 8u;
+    const int mx = m & 0xffff, my = m >> 16;
+    const M fp = fps[my * F + mx];
+    const int cell = my * S + mx;
+    process_pixel<PS, TK, TV, M>(a, pbase, cells, fp, ys[row] * pitch32 + xs[col], cell);
+    for (; follow; follow &= follow - 1) {
+      const int q = __ffs(follow) - 1;
+      const int rr = row + (q == 0 ? 0 : 1);
+      const int cc = col + (q == 0 ? 1 : q - 2);
+      process_pixel<PS, TK, TV, M>(a, pbase, cells, fp, ys[rr] * pitch32 + xs[cc], cell);
+    }
+  }
+}
+
+// Painting of a stamp with edge duplicates, in waves: live pixels bid (atomicMin on
+// epoch-tagged row-major indices) for their cells and run when they hold their cell's lowest
+// remaining index and their earlier duplicates (done_c / done_r) finished. Called by the
+// whole CTA; returns the next epoch. Out of line: rare, and it keeps the cell path's
+// registers free.
+template <bool PS, class TK, class TV, class M>
+__device__ __noinline__ int paint_waves(const StampArgs<TK, TV>& a, const StampParams& sp,
+                                        const int* xs, const int* ys, uint16_t* done_c,
+                                        uint16_t* done_r, const M* fps, M* pbase, int* own,
+                                        int epoch) {
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int F = a.F, S = a.S;
+  const int cells = S * S;
+  const int NC = (F + 31) / 32;
+  uint64_t rem = 0;
+  int wave = 1;
+  int key_hi = (kEpochMax - epoch) << 16;
+  epoch++;
+  for (int row = warp, jr = 0; row < F; row += kWarps, jr++) {
+    const int dr = row - a.wr;
+    for (int col = lane, jc = 0; col < F; col += 32, jc++) {
+      const int dc = col - a.wr;
+      bool lv = false;
+      if (dc * dc + dr * dr <= a.support2) {
+        M fp;
+        const PixelInfo p = pixel_info(a, sp, xs, ys, fps, row, col, &fp);
+        if (p.live) {
+          lv = true;
+          atomicMin(&own[p.my * S + p.mx], key_hi | (row * F + col));
+        }
+      }
+      if (lv)
+        rem |= 1ull << (jr * NC + jc);
+      else
+        mark_done(xs, ys, F, done_c, done_r, row, col, 1);  // done "before" wave 1
+    }
+  }
+  __syncthreads();
+  for (;;) {
+    for (uint64_t bits = rem; bits; bits &= bits - 1) {
+      const int j = __ffsll(static_cast<long long>(bits)) - 1;
+      const int row = warp + kWarps * (j / NC), col = lane + 32 * (j % NC);
+      M fp;
+      const PixelInfo p = pixel_info(a, sp, xs, ys, fps, row, col, &fp);
+      if (own[p.my * S + p.mx] == (key_hi | (row * F + col)) &&
+          canvas_ready(xs, ys, F, done_c, done_r, row, col, wave)) {
+        process_pixel<PS, TK, TV, M>(a, pbase, cells, fp,
+                                     p.yc * static_cast<int>(a.pitch) + p.xc, p.my * S + p.mx);
+        rem &= ~(1ull << j);
+        mark_done(xs, ys, F, done_c, done_r, row, col, static_cast<uint16_t>(wave + 1));
+      }
+    }
+    const int any = __syncthreads_or(rem != 0);
+    if (!any) break;
+    if (wave >= kMaxWaves) {  // cannot happen: the lowest remaining pixel always runs
+      if (tid == 0) atomicOr(a.status, kStatusWaveCap);
+      break;
+    }
+    wave++;
+    key_hi = (kEpochMax - epoch) << 16;
+    epoch++;
+    for (uint64_t bits = rem; bits; bits &= bits - 1) {  // bid for the map cell
+      const int j = __ffsll(static_cast<long long>(bits)) - 1;
+      const int row = warp + kWarps * (j / NC), col = lane + 32 * (j % NC);
+      M fp;
+      const PixelInfo p = pixel_info(a, sp, xs, ys, fps, row, col, &fp);
+      atomicMin(&own[p.my * S + p.mx], key_hi | (row * F + col));
+    }
+    __syncthreads();
+  }
+  return epoch;
+}
+
+// Per-stamp setup of stamp k into buffer `buf`: canvas columns / rows of the box (double, as
+// the reference), duplicate flags reset, the ring rectangles (warp 0). Returns whether this
+// thread saw an edge duplicate.
+template <class TK, class TV>
+__device__ __forceinline__ int setup_stamp(const StampArgs<TK, TV>& a, const StampParams* sparams,
+                                           int64_t k, int* xs, int* ys, uint16_t* done_c,
+                                           uint16_t* done_r, StampShared* sh, RefreshList* rl,
+                                           int tid, int T) {
+  const int slot = static_cast<int>(k % kParamChunk);
+  const StampParams& sp = sparams[slot];
+  const int F = a.F;
+  int dup = 0;
+  for (int i = tid; i < F; i += T) {
+    const int x = static_cast<int>(__dadd_rn(static_cast<double>(i - a.wr), sp.cx));
+    const int y = static_cast<int>(__dadd_rn(static_cast<double>(i - a.wr), sp.cy));
+    xs[i] = x;
+    ys[i] = y;
+    done_c[i] = 0;
+    done_r[i] = 0;
+    if (i + 1 < F) {
+      const int x1 = static_cast<int>(__dadd_rn(static_cast<double>(i + 1 - a.wr), sp.cx));
+      const int y1 = static_cast<int>(__dadd_rn(static_cast<double>(i + 1 - a.wr), sp.cy));
+      dup |= (x == x1) | (y == y1);
+    }
+  }
+  if (a.use_snapshot && (tid >> 5) == 0) {
+    int prev[8];
+    if (slot > 0)
+      stamp_rects(sparams[slot - 1], prev);
+    else
+      for (int i = 0; i < 8; i++) prev[i] = sh->prev[i];
+    build_refresh(sp, prev, tid & 31, rl);
+  }
+  return dup;
+}
+
 // One stroke's stamps applied in order by the whole CTA (the kernel body shared by the
 // single-canvas and the batched kernels). `a` may live in shared or parameter memory.
+// Per stamp: ring refresh | paint | (next stamp's setup alongside) -- two barriers. Stamps
+// with edge duplicates paint in waves instead: pixels bid for their cells (atomicMin on
+// epoch-tagged row-major indices) and run when they hold their cell's lowest remaining index
+// and their earlier duplicates are done.
 template <bool PS, bool BIG, class TK, class TV, class Src>
 __device__ __forceinline__ void run_stroke(const StampArgs<TK, TV>& a, const Src& src,
                                            unsigned char* smem_raw, StampParams* sparams,
-                                           int* s_q) {
+                                           StampShared* sh) {
   using M = typename MathOf<TK>::type;
-  int& s_qcount = s_q[0];
-  int& s_qover = s_q[1];
   const int64_t nstamps = src.count();
   const int tid = threadIdx.x;
   const int T = blockDim.x;
-  const int warp = tid >> 5, lane = tid & 31;
+  const int lane = tid & 31;
+  auto warp_id = [tid]() { return tid >> 5; };
   const int F = a.F, S = a.S;
   const int npix = F * F;
   const int cells = S * S;
-  const int NC = (F + 31) / 32;
-  const StampSmem L = stamp_smem_layout<M>(F, S, !BIG, PS, !BIG);
+  const StampSmem L = stamp_smem_layout<M>(F, S, a.ndisc, !BIG, PS, !BIG);
   const M* fps = !BIG ? reinterpret_cast<M*>(smem_raw + L.fp) : a.footprint;
   M* pbase = PS ? reinterpret_cast<M*>(smem_raw + L.pick) : nullptr;
   int* own = BIG ? a.owner_global : reinterpret_cast<int*>(smem_raw + L.own);
-  int* xs = reinterpret_cast<int*>(smem_raw + L.xs);
-  int* ys = reinterpret_cast<int*>(smem_raw + L.ys);
-  uint16_t* done_c = reinterpret_cast<uint16_t*>(smem_raw + L.done_c);
-  uint16_t* done_r = reinterpret_cast<uint16_t*>(smem_raw + L.done_r);
-  int* queue = reinterpret_cast<int*>(smem_raw + L.queue);
+  int* xs_b = reinterpret_cast<int*>(smem_raw + L.xs);
+  int* ys_b = reinterpret_cast<int*>(smem_raw + L.ys);
+  uint16_t* dc_b = reinterpret_cast<uint16_t*>(smem_raw + L.done_c);
+  uint16_t* dr_b = reinterpret_cast<uint16_t*>(smem_raw + L.done_r);
+  uint32_t* disc = reinterpret_cast<uint32_t*>(smem_raw + L.disc);
+  int* cellmap = reinterpret_cast<int*>(smem_raw + L.cellmap);
+  const int ndisc = a.ndisc;
 
-  // launch prologue: footprint and pickup map staged, owner table reset
+  // launch prologue: footprint and pickup map staged, owner table reset, ring state
   if (!BIG) {
     M* f = reinterpret_cast<M*>(smem_raw + L.fp);
     for (int i = tid; i < npix; i += T) f[i] = a.footprint[i];
@@ -517,118 +725,105 @@ __device__ __forceinline__ void run_stroke(const StampArgs<TK, TV>& a, const Src
       pickup_plane<TK, TV, M>(a, p)[m] = M(0);
   }
   for (int i = tid; i < cells; i += T) own[i] = INT_MAX;
-  if (tid == 0) {
-    s_qcount = 0;
-    s_qover = 0;
+  if (tid == 0) {  // the stamp before the first: from the brush's ring state or the reset mode
+    const int big = 1 << 30;
+    const int unknown[8] = {0, 0, -1, -1, 0, 0, -1, -1};
+    const int clean[8] = {0, 0, -1, -1, -big, -big, big, big};
+    for (int i = 0; i < 8; i++)
+      sh->prev[i] = (a.ring_reset == kRingKeep && a.ring) ? a.ring[i]
+                    : a.ring_reset == kRingClean          ? clean[i]
+                                                          : unknown[i];
   }
+  // support-disc pixels, row-major (warp 0: per-row column intervals, prefix sums), and a
+  // cell map whose pixels outside the disc read as "changes nothing"
+  if (ndisc > 0) {
+    for (int i = tid; i < F * F; i += T) cellmap[i] = -1;
+    if (warp_id() == 0) {
+      int base = 0;
+      for (int r0 = 0; r0 < F; r0 += 32) {
+        const int row = r0 + lane;
+        int lo = 0, n = 0;
+        if (row < F) {
+          const int dr = row - a.wr;
+          const int rem2 = a.support2 - dr * dr;
+          if (rem2 >= 0) {
+            int h = static_cast<int>(sqrtf(static_cast<float>(rem2)));
+            while ((h + 1) * (h + 1) <= rem2) h++;
+            while (h > 0 && h * h > rem2) h--;
+            lo = max(a.wr - h, 0);
+            n = min(a.wr + h, F - 1) - lo + 1;
+          }
+        }
+        int incl = n;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          const int v = __shfl_up_sync(0xffffffffu, incl, d);
+          if (lane >= d) incl += v;
+        }
+        const int start = base + incl - n;
+        for (int j = 0; j < n && start + j < ndisc; j++)
+          disc[start + j] = (static_cast<uint32_t>(row) << 16) | static_cast<uint32_t>(lo + j);
+        base += __shfl_sync(0xffffffffu, incl, 31);
+      }
+      if (lane == 0 && base != ndisc) atomicOr(a.status, kStatusWaveCap);
+    }
+  }
+  // parameters of the first chunk, setup of the first stamp
+  if (tid < kParamChunk && tid < nstamps)
+    sparams[tid] = derive_params(src.get(tid), a.wr, a.radius, a.rows, a.cols);
+  __syncthreads();
   int epoch = 0;
+  int dup = 0;
+  if (nstamps > 0)
+    dup = setup_stamp(a, sparams, 0, xs_b, ys_b, dc_b, dr_b, sh, &sh->rl[0], tid, T);
+  dup = __syncthreads_or(dup);
 
   for (int64_t k = 0; k < nstamps; k++) {
     const int slot = static_cast<int>(k % kParamChunk);
-    if (slot == 0) {  // derive the next chunk of stamp parameters in parallel
-      __syncthreads();
-      const int64_t j = k + tid;
-      if (tid < kParamChunk && j < nstamps)
-        sparams[tid] = derive_params(src.get(j), a.wr, a.radius, a.rows, a.cols);
-      if (epoch > kEpochMax - 2 * kMaxWaves) {  // owner keys about to wrap: reset
-        for (int i = tid; i < cells; i += T) own[i] = INT_MAX;
-        epoch = 0;
-      }
-      __syncthreads();
-    }
+    const int buf = static_cast<int>(k & 1);
     const StampParams& sp = sparams[slot];
-    // phase A: per column / row canvas coordinates (double, as the reference), done flags
-    // reset, snapshot ring scanned for dirty pixels
-    for (int i = tid; i < F; i += T) {
-      xs[i] = static_cast<int>(__dadd_rn(static_cast<double>(i - a.wr), sp.cx));
-      ys[i] = static_cast<int>(__dadd_rn(static_cast<double>(i - a.wr), sp.cy));
-      done_c[i] = 0;
-      done_r[i] = 0;
-    }
-    if (a.use_snapshot) scan_ring(a, sp, warp, lane, kWarps, queue, &s_qcount, &s_qover);
+    const int* xs = xs_b + buf * F;
+    const int* ys = ys_b + buf * F;
+    uint16_t* done_c = dc_b + buf * F;
+    uint16_t* done_r = dr_b + buf * F;
+    // ring refresh and the cell map, then painting (in waves with edge duplicates)
+    const bool by_cells = !dup && ndisc > 0;
+    if (a.use_snapshot) refresh_ring(a, sh->rl[buf], tid, T);
+    if (by_cells) classify_disc(a, sp, xs, ys, fps, disc, ndisc, cellmap, tid, T);
     __syncthreads();
-    // phase B: queued snapshot copies; live pixels (inside the support disc, canvas and map,
-    // positive footprint) classified and bidding for their map cells (wave 1)
-    if (a.use_snapshot) copy_queued(a, queue, min(s_qcount, kRefreshQueue), tid, T);
-    int wave = 1;
-    int key_hi = (kEpochMax - epoch) << 16;
-    epoch++;
-    uint64_t rem = 0;
-    for (int row = warp, jr = 0; row < F; row += kWarps, jr++) {
-      const int dr = row - a.wr;
-      for (int col = lane, jc = 0; col < F; col += 32, jc++) {
-        const int dc = col - a.wr;
-        bool live = false;
-        if (dc * dc + dr * dr <= a.support2) {
-          M fp;
-          const PixelInfo p = pixel_info(a, sp, xs, ys, fps, row, col, &fp);
-          if (p.live) {
-            live = true;
-            atomicMin(&own[p.my * S + p.mx], key_hi | (row * F + col));
-          }
+    if (by_cells)
+      paint_disc<PS, TK, TV, M>(a, xs, ys, fps, pbase, disc, ndisc, cellmap, tid, T);
+    else
+      epoch = paint_waves<PS, TK, TV, M>(a, sp, xs, ys, done_c, done_r, fps, pbase, own, epoch);
+    // the next stamp's setup (into the other buffer), alongside painting
+    int nd = 0;
+    if (k + 1 < nstamps) {
+      if ((k + 1) % kParamChunk == 0) {  // derive the next chunk of stamp parameters
+        if (tid == 0) stamp_rects(sparams[kParamChunk - 1], sh->prev);
+        __syncthreads();
+        const int64_t j = k + 1 + tid;
+        if (tid < kParamChunk && j < nstamps)
+          sparams[tid] = derive_params(src.get(j), a.wr, a.radius, a.rows, a.cols);
+        if (epoch > kEpochMax - 2 * kMaxWaves) {  // owner keys about to wrap: reset
+          for (int i = tid; i < cells; i += T) own[i] = INT_MAX;
+          epoch = 0;
         }
-        if (live)
-          rem |= 1ull << (jr * NC + jc);
-        else
-          mark_done(xs, ys, F, done_c, done_r, row, col, 1);  // done "before" wave 1
+        __syncthreads();
       }
+      const int nb = buf ^ 1;
+      nd = setup_stamp(a, sparams, k + 1, xs_b + nb * F, ys_b + nb * F, dc_b + nb * F,
+                       dr_b + nb * F, sh, &sh->rl[nb], tid, T);
     }
-    __syncthreads();
-    // The refresh queue overflowed: drain the rest before painting. Each round clears the
-    // dirty bytes of the pixels it queued, so the rounds end; the cap only guards the loop.
-    for (int round = 0; s_qover; round++) {
-      if (round > (sp.bra[1] - sp.tla[1] + 2) * (sp.bra[0] - sp.tla[0] + 2) / kRefreshQueue + 2) {
-        if (tid == 0) atomicOr(a.status, kStatusWaveCap);
-        break;
-      }
-      __syncthreads();
-      if (tid == 0) {
-        s_qcount = 0;
-        s_qover = 0;
-      }
-      __syncthreads();
-      scan_ring(a, sp, warp, lane, kWarps, queue, &s_qcount, &s_qover);
-      __syncthreads();
-      copy_queued(a, queue, min(s_qcount, kRefreshQueue), tid, T);
-      __syncthreads();
-    }
-    if (tid == 0) s_qcount = 0;
-    for (;;) {
-      for (uint64_t bits = rem; bits; bits &= bits - 1) {
-        const int j = __ffsll(static_cast<long long>(bits)) - 1;
-        const int row = warp + kWarps * (j / NC), col = lane + 32 * (j % NC);
-        M fp;
-        const PixelInfo p = pixel_info(a, sp, xs, ys, fps, row, col, &fp);
-        if (own[p.my * S + p.mx] == (key_hi | (row * F + col)) &&
-            canvas_ready(xs, ys, F, done_c, done_r, row, col, wave)) {
-          process_pixel<PS, TK, TV, M>(a, pbase, cells, fp,
-                                       static_cast<int64_t>(p.yc) * a.pitch + p.xc,
-                                       p.my * S + p.mx);
-          rem &= ~(1ull << j);
-          mark_done(xs, ys, F, done_c, done_r, row, col, static_cast<uint16_t>(wave + 1));
-        }
-      }
-      const int any = __syncthreads_or(rem != 0);
-      if (!any) break;
-      if (wave >= kMaxWaves) {  // cannot happen: the lowest remaining pixel always runs
-        if (tid == 0) atomicOr(a.status, kStatusWaveCap);
-        break;
-      }
-      wave++;
-      key_hi = (kEpochMax - epoch) << 16;
-      epoch++;
-      for (uint64_t bits = rem; bits; bits &= bits - 1) {  // bid for the map cell
-        const int j = __ffsll(static_cast<long long>(bits)) - 1;
-        const int row = warp + kWarps * (j / NC), col = lane + 32 * (j % NC);
-        M fp;
-        const PixelInfo p = pixel_info(a, sp, xs, ys, fps, row, col, &fp);
-        atomicMin(&own[p.my * S + p.mx], key_hi | (row * F + col));
-      }
-      __syncthreads();
-    }
+    dup = __syncthreads_or(nd);
   }
-  // epilogue: the brush keeps its pickup map
+  // epilogue: the brush keeps its pickup map and the ring state
   __syncthreads();
+  if (tid == 0 && a.ring && a.use_snapshot) {
+    if (nstamps > 0)
+      stamp_rects(sparams[static_cast<int>((nstamps - 1) % kParamChunk)], a.ring);
+    else
+      for (int i = 0; i < 8; i++) a.ring[i] = sh->prev[i];
+  }
   if (PS) {
     for (int i = tid; i < 7 * cells; i += T) {
       const int p = i / cells, m = i - p * cells;
@@ -644,8 +839,8 @@ template <bool PS, bool BIG, class TK, class TV>
 __global__ void __launch_bounds__(kStampThreads, 1) stamp_kernel(const __grid_constant__ StampArgs<TK, TV> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ StampParams sparams[kParamChunk];
-  __shared__ int s_q[2];
-  run_stroke<PS, BIG>(a, RecordSource{a.stamps, a.n}, smem_raw, sparams, s_q);
+  __shared__ StampShared sh;
+  run_stroke<PS, BIG>(a, RecordSource{a.stamps, a.n}, smem_raw, sparams, &sh);
 }
 
 // ---------------------------------------------------------------------- batched painting
@@ -716,7 +911,8 @@ struct BatchCanvas {
   TK* sK[3];
   TK* sS[3];
   TV* sV;
-  uint8_t* dirty;
+  int* ring;           // the brush's snapshot-ring state
+  int32_t ring_reset;  // for the canvas's first stroke with stamps
   int32_t rows, cols;
   int64_t pitch;
   int32_t use_snapshot;
@@ -730,6 +926,7 @@ struct BatchStroke {
   int64_t first_point;
   int32_t npoints;
   int32_t F, S, wr, support2;
+  int32_t ndisc;  // support-disc list length (0: waves only)
   int32_t plan;  // bit 0: pickup map in shared memory; bit 1: footprint and owners global
   int64_t fp_offset;
   double radius, spacing;
@@ -759,7 +956,7 @@ __global__ void __launch_bounds__(kStampThreads, 1) batch_kernel(const __grid_co
   using M = typename MathOf<TK>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ StampParams sparams[kParamChunk];
-  __shared__ int s_q[2];
+  __shared__ StampShared sh;
   __shared__ StampArgs<TK, TV> sa;
   __shared__ int s_item;
   __shared__ int64_t seg_end[kMaxPathPoints];
@@ -774,6 +971,7 @@ __global__ void __launch_bounds__(kStampThreads, 1) batch_kernel(const __grid_co
     const int ci = s_item;
     if (ci < 0) return;
     const BatchCanvas<TK, TV>& cv = b.canvases[ci];
+    bool ran = false;  // a stroke with stamps has run on this canvas (uniform over the CTA)
     for (int32_t k = 0; k < cv.nstrokes; k++) {
       const BatchStroke& st = b.strokes[cv.first_stroke + k];
       const int nseg = st.npoints - 1;
@@ -806,12 +1004,14 @@ __global__ void __launch_bounds__(kStampThreads, 1) batch_kernel(const __grid_co
         sa.S = st.S;
         sa.wr = st.wr;
         sa.support2 = st.support2;
+        sa.ndisc = st.ndisc;
         sa.radius = st.radius;
         sa.pickupRate = static_cast<M>(cv.pickup_rate);
         sa.depositionRate = static_cast<M>(cv.deposition_rate);
         sa.capacity = static_cast<M>(cv.capacity);
         sa.use_snapshot = cv.use_snapshot;
-        sa.dirty = cv.use_snapshot ? cv.dirty : nullptr;
+        sa.ring = cv.ring;
+        sa.ring_reset = ran ? kRingKeep : cv.ring_reset;
         sa.pickup_zero = 1;  // dip: the pickup map starts clean
         sa.pickup_smem = st.plan & 1;
         sa.footprint_smem = (st.plan & 2) ? 0 : 1;
@@ -832,14 +1032,21 @@ __global__ void __launch_bounds__(kStampThreads, 1) batch_kernel(const __grid_co
         for (int i = 1; i < nseg; i++) seg_end[i] += seg_end[i - 1];
       __syncthreads();
       const int64_t n = nseg > 0 ? seg_end[nseg - 1] : 0;
-      if (n == 0) continue;
+      if (n == 0) {  // no stamps: a last stroke still leaves the brush a clean pickup map
+        if (k + 1 == cv.nstrokes) {
+          const int64_t pc = static_cast<int64_t>(7) * st.S * st.S;
+          for (int64_t i = tid; i < pc; i += T) static_cast<M*>(cv.brush_pickup)[i] = M(0);
+        }
+        continue;
+      }
       const PathSource src{pts, st.npoints, st.spacing, seg_end, n};
       switch (st.plan) {
-        case 0: run_stroke<false, false>(sa, src, smem_raw, sparams, s_q); break;
-        case 1: run_stroke<true, false>(sa, src, smem_raw, sparams, s_q); break;
-        case 2: run_stroke<false, true>(sa, src, smem_raw, sparams, s_q); break;
-        default: run_stroke<true, true>(sa, src, smem_raw, sparams, s_q); break;
+        case 0: run_stroke<false, false>(sa, src, smem_raw, sparams, &sh); break;
+        case 1: run_stroke<true, false>(sa, src, smem_raw, sparams, &sh); break;
+        case 2: run_stroke<false, true>(sa, src, smem_raw, sparams, &sh); break;
+        default: run_stroke<true, true>(sa, src, smem_raw, sparams, &sh); break;
       }
+      ran = true;
     }
   }
 }
@@ -945,31 +1152,47 @@ int max_dyn_smem() {
 // Shared-memory plan for a launch. The small variant keeps the footprint and the owner table
 // in shared memory (BIG = false); maps too large for that keep both in global memory. The
 // pickup map (7 planes) is staged in shared memory when it fits beside them.
+// The support-disc list and cell map (ndisc > 0) are kept when some variant fits with them.
 struct SmemPlan {
   bool big, pick;
+  int ndisc;
   StampSmem layout;
 };
 template <class M>
-SmemPlan plan_smem_limit(int F, int S, size_t limit, bool allow_small = true) {
+SmemPlan plan_smem_limit(int F, int S, int ndisc, size_t limit, bool allow_small = true) {
   const bool cand[4][2] = {{false, true}, {false, false}, {true, true}, {true, false}};
-  for (const auto& c : cand) {
-    const bool big = c[0], pick = c[1];
-    if (!big && !allow_small) continue;
-    const StampSmem L = stamp_smem_layout<M>(F, S, !big, pick, !big);
-    if (L.total <= limit) return SmemPlan{big, pick, L};
+  for (int nd : {ndisc, 0}) {
+    for (const auto& c : cand) {
+      const bool big = c[0], pick = c[1];
+      if (!big && !allow_small) continue;
+      const StampSmem L = stamp_smem_layout<M>(F, S, nd, !big, pick, !big);
+      if (L.total <= limit) return SmemPlan{big, pick, nd, L};
+    }
+    if (ndisc == 0) break;
   }
   fail(PAINTY_ERR_UNSUPPORTED, "stamp kernel shared memory plan failed");
 }
 
 template <class M>
-SmemPlan plan_smem(int F, int S, bool allow_small) {
-  const size_t limit = static_cast<size_t>(max_dyn_smem()) - sizeof(StampParams) * kParamChunk - 512;
-  return plan_smem_limit<M>(F, S, limit, allow_small);
+SmemPlan plan_smem(int F, int S, int ndisc, bool allow_small) {
+  const size_t limit = static_cast<size_t>(max_dyn_smem()) - sizeof(StampParams) * kParamChunk -
+                       sizeof(StampShared) - 512;
+  return plan_smem_limit<M>(F, S, ndisc, limit, allow_small);
+}
+
+// Box pixels (F x F, centre wr) with dc^2 + dr^2 <= support2: the kernel's support-disc list.
+int32_t disc_count(int F, int32_t support2) {
+  const int wr = (F - 1) / 2;
+  int32_t n = 0;
+  for (int r = 0; r < F; r++)
+    for (int c = 0; c < F; c++)
+      n += (c - wr) * (c - wr) + (r - wr) * (r - wr) <= support2 ? 1 : 0;
+  return n;
 }
 
 template <class TK, class TV>
 void launch_stamps(painty_canvas* c, painty_brush* b, const StampRec* d_stamps, int64_t n,
-                   bool pickup_zero, cudaStream_t st) {
+                   bool pickup_zero, int ring_reset, cudaStream_t st) {
   using M = typename MathOf<TK>::type;
   StampArgs<TK, TV> a{};
   for (int i = 0; i < 3; i++) {
@@ -1006,11 +1229,13 @@ void launch_stamps(painty_canvas* c, painty_brush* b, const StampRec* d_stamps, 
     a.paintS[i] = static_cast<M>(b->paintS[i]);
   }
   a.use_snapshot = b->useSnapshot ? 1 : 0;
-  a.dirty = b->useSnapshot ? static_cast<uint8_t*>(b->d_dirty) : nullptr;
+  a.ring = b->d_ring();
+  a.ring_reset = ring_reset;
   a.pickup_zero = pickup_zero ? 1 : 0;
   a.status = b->d_status;
   a.support2 = b->support2;
-  const SmemPlan plan = plan_smem<M>(b->F, b->sizeMap, true);
+  const SmemPlan plan = plan_smem<M>(b->F, b->sizeMap, disc_count(b->F, b->support2), true);
+  a.ndisc = plan.ndisc;
   const bool big = plan.big;
   if (big) {
     ensure(&b->d_owner, &b->d_owner_bytes, cells * sizeof(int));
@@ -1029,10 +1254,12 @@ void launch_stamps(painty_canvas* c, painty_brush* b, const StampRec* d_stamps, 
 }
 
 // Snapshot buffer for painting canvas c with brush b (FootprintBrush.hxx:280-284: a full copy
-// when the sizes differ) and its dirty map: clean after a full copy; all dirty when the canvas
-// changed outside this brush's stamps since its last run, or another canvas was painted.
-void prepare_snapshot(painty_canvas* c, painty_brush* b, cudaStream_t st) {
-  if (!b->useSnapshot) return;
+// when the sizes differ) and the ring reset mode of the run: clean after a full copy; unknown
+// when the canvas changed outside this brush's snapshot runs since its last one, or another
+// canvas was painted; otherwise the device ring state carries over.
+int prepare_snapshot(painty_canvas* c, painty_brush* b, cudaStream_t st) {
+  if (!b->useSnapshot) return kRingUnknown;
+  int mode = kRingKeep;
   if (!b->has_snapshot || b->snapshot.rows != c->wet.rows || b->snapshot.cols != c->wet.cols ||
       b->snapshot.storage != c->wet.storage) {
     if (b->has_snapshot) device_free(b->snapshot.base);
@@ -1042,15 +1269,22 @@ void prepare_snapshot(painty_canvas* c, painty_brush* b, cudaStream_t st) {
     b->has_snapshot = true;
     PG_CUDA(cudaMemcpyAsync(b->snapshot.base, c->wet.base, c->wet.bytes,
                             cudaMemcpyDeviceToDevice, st));
-    ensure(&b->d_dirty, &b->d_dirty_bytes, static_cast<size_t>(c->wet.plane_elems()));
-    PG_CUDA(cudaMemsetAsync(b->d_dirty, 0, c->wet.plane_elems(), st));
-    b->dirty_canvas = c->id;
-    b->dirty_version = c->version;
+    mode = kRingClean;
+  } else if (b->ring_canvas != c->id || b->ring_version != c->version) {
+    mode = kRingUnknown;
+  } else if (b->ring_pending >= 0) {
+    mode = b->ring_pending;
   }
-  if (b->dirty_canvas != c->id || b->dirty_version != c->version) {
-    ensure(&b->d_dirty, &b->d_dirty_bytes, static_cast<size_t>(c->wet.plane_elems()));
-    PG_CUDA(cudaMemsetAsync(b->d_dirty, 1, c->wet.plane_elems(), st));
-  }
+  b->ring_pending = -1;
+  return mode;
+}
+
+// Device status word and ring state of a brush.
+void ensure_status(painty_brush* b, cudaStream_t st) {
+  if (b->d_status) return;
+  b->d_status = static_cast<unsigned*>(device_alloc(16 * sizeof(unsigned)));
+  PG_CUDA(cudaMemsetAsync(b->d_status, 0, 16 * sizeof(unsigned), st));
+  b->ring_canvas = 0;  // the ring state holds nothing yet
 }
 
 // Prepares device state and runs n stamps (host records) on the canvas.
@@ -1061,6 +1295,8 @@ void run_stamps(painty_canvas* c, painty_brush* b, const std::vector<StampRec>& 
   PG_REQUIRE(b->sizeMap > 0 && b->F > 0, "brush radius gives an empty footprint");
   PG_REQUIRE(static_cast<int64_t>(b->F) * b->F <= int64_t(kMaxPixelsPerThread) * kStampThreads,
              "brush radius above the supported maximum (footprint side 256)");
+  PG_REQUIRE(static_cast<int64_t>(c->wet.rows) * c->wet.pitch < (int64_t(1) << 31),
+             "canvas too large for stamping (a plane holds 2^31 elements or more)");
   const bool f64 = c->wet.storage == PAINTY_STORAGE_F64;
   const int mode = f64 ? 1 : 0;
   if (b->bound < 0) b->bound = mode;
@@ -1089,11 +1325,8 @@ void run_stamps(painty_canvas* c, painty_brush* b, const std::vector<StampRec>& 
   }
   const bool pickup_zero = b->pickup_clear;
   b->pickup_clear = false;
-  if (!b->d_status) {
-    b->d_status = static_cast<unsigned*>(device_alloc(sizeof(unsigned)));
-    PG_CUDA(cudaMemsetAsync(b->d_status, 0, sizeof(unsigned), st));
-  }
-  prepare_snapshot(c, b, st);
+  ensure_status(b, st);
+  const int ring_reset = prepare_snapshot(c, b, st);
   // stamps
   const size_t sbytes = recs.size() * sizeof(StampRec);
   ensure(&b->d_stamps, &b->d_stamps_bytes, sbytes);
@@ -1101,17 +1334,26 @@ void run_stamps(painty_canvas* c, painty_brush* b, const std::vector<StampRec>& 
   const auto* ds = static_cast<const StampRec*>(b->d_stamps);
   const int64_t n = static_cast<int64_t>(recs.size());
   switch (c->wet.storage) {
-    case PAINTY_STORAGE_F32: launch_stamps<float, float>(c, b, ds, n, pickup_zero, st); break;
-    case PAINTY_STORAGE_F16: launch_stamps<__half, __half>(c, b, ds, n, pickup_zero, st); break;
-    case PAINTY_STORAGE_BF16:
-      launch_stamps<__nv_bfloat16, __half>(c, b, ds, n, pickup_zero, st);
+    case PAINTY_STORAGE_F32:
+      launch_stamps<float, float>(c, b, ds, n, pickup_zero, ring_reset, st);
       break;
-    case PAINTY_STORAGE_F64: launch_stamps<double, double>(c, b, ds, n, pickup_zero, st); break;
+    case PAINTY_STORAGE_F16:
+      launch_stamps<__half, __half>(c, b, ds, n, pickup_zero, ring_reset, st);
+      break;
+    case PAINTY_STORAGE_BF16:
+      launch_stamps<__nv_bfloat16, __half>(c, b, ds, n, pickup_zero, ring_reset, st);
+      break;
+    case PAINTY_STORAGE_F64:
+      launch_stamps<double, double>(c, b, ds, n, pickup_zero, ring_reset, st);
+      break;
   }
-  // other writers of this canvas must invalidate this brush's snapshot bookkeeping
+  // other writers of this canvas (including this brush without its snapshot) invalidate the
+  // ring state
   c->version++;
-  b->dirty_canvas = c->id;
-  b->dirty_version = c->version;
+  if (b->useSnapshot) {
+    b->ring_canvas = c->id;
+    b->ring_version = c->version;
+  }
   // the stamp records live in a reused buffer: finish before returning
   unsigned status = 0;
   PG_CUDA(cudaMemcpyAsync(&status, b->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
@@ -1173,7 +1415,8 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
         x.K[i] = sk.K[i];
         x.Sc[i] = sk.S[i];
       }
-      const SmemPlan plan = plan_smem_limit<M>(b->F, b->sizeMap, limit);
+      const SmemPlan plan = plan_smem_limit<M>(b->F, b->sizeMap, disc_count(b->F, b->support2), limit);
+      x.ndisc = plan.ndisc;
       x.plan = (plan.pick ? 1 : 0) | (plan.big ? 2 : 0);
       dyn = std::max(dyn, plan.layout.total);
       smax = std::max(smax, b->sizeMap);
@@ -1198,13 +1441,10 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
     if (b->bound < 0) b->bound = mode;
     PG_REQUIRE(b->bound == mode,
                "a brush paints either F64 canvases or F32/F16/BF16 canvases, not both");
-    if (!b->d_status) {
-      b->d_status = static_cast<unsigned*>(device_alloc(sizeof(unsigned)));
-      PG_CUDA(cudaMemsetAsync(b->d_status, 0, sizeof(unsigned), st));
-    }
+    ensure_status(b, st);
     const size_t pk_bytes = static_cast<size_t>(b->sizeMap) * b->sizeMap * 7 * msz;
     ensure(&b->d_pickup, &b->d_pickup_bytes, pk_bytes);
-    if (!per[c].empty()) prepare_snapshot(cv, b, st);
+    const int ring_reset = per[c].empty() ? kRingKeep : prepare_snapshot(cv, b, st);
     BatchCanvas<TK, TV>& x = bc[c];
     for (int i = 0; i < 3; i++) {
       x.cK[i] = static_cast<TK*>(cv->wet.K[i]);
@@ -1215,7 +1455,8 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
     }
     x.cV = static_cast<TV*>(cv->wet.V);
     x.sV = static_cast<TV*>(b->useSnapshot ? b->snapshot.V : cv->wet.V);
-    x.dirty = b->useSnapshot ? static_cast<uint8_t*>(b->d_dirty) : nullptr;
+    x.ring = b->d_ring();
+    x.ring_reset = ring_reset;
     x.rows = cv->wet.rows;
     x.cols = cv->wet.cols;
     x.pitch = cv->wet.pitch;
@@ -1285,8 +1526,10 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
     if (per[c].empty()) continue;
     painty_brush* b = brushes[c];
     canvases[c]->version++;
-    b->dirty_canvas = canvases[c]->id;
-    b->dirty_version = canvases[c]->version;
+    if (b->useSnapshot) {
+      b->ring_canvas = canvases[c]->id;
+      b->ring_version = canvases[c]->version;
+    }
     b->pickup_clear = false;  // the last stroke's pickup map is in the brush's buffer
   }
   if (status != 0) fail(PAINTY_ERR_CUDA, "batched stamp kernel reported an internal error");
@@ -1474,7 +1717,6 @@ painty_status painty_brush_destroy(painty_brush* b) {
     pg::device_free(b->d_owner);
     pg::device_free(b->d_stamps);
     pg::device_free(b->d_status);
-    pg::device_free(b->d_dirty);
     if (b->has_snapshot) pg::device_free(b->snapshot.base);
     delete b;
   });
@@ -1540,10 +1782,9 @@ painty_status painty_brush_update_snapshot(painty_brush* b, const painty_canvas*
     }
     PG_CUDA(cudaMemcpyAsync(b->snapshot.base, c->wet.base, c->wet.bytes,
                             cudaMemcpyDeviceToDevice, st));
-    pg::ensure(&b->d_dirty, &b->d_dirty_bytes, static_cast<size_t>(c->wet.plane_elems()));
-    PG_CUDA(cudaMemsetAsync(b->d_dirty, 0, c->wet.plane_elems(), st));
-    b->dirty_canvas = c->id;
-    b->dirty_version = c->version;
+    b->ring_canvas = c->id;  // snapshot == canvas: the next run refreshes nothing stale
+    b->ring_version = c->version;
+    b->ring_pending = pg::kRingClean;
     PG_CUDA(cudaStreamSynchronize(st));
   });
 }
@@ -1637,6 +1878,8 @@ painty_status painty_stamps_f32_noalloc(const painty_stamp_buffers_f32* b, void*
     PG_REQUIRE(b != nullptr, "buffers is null");
     PG_REQUIRE(b->n >= 0, "negative stamp count");
     PG_REQUIRE(b->rows > 0 && b->cols > 0 && b->pitch >= b->cols, "bad canvas geometry");
+    PG_REQUIRE(static_cast<int64_t>(b->rows) * b->pitch < (int64_t(1) << 31),
+               "canvas too large for stamping (a plane holds 2^31 elements or more)");
     PG_REQUIRE(b->footprint_side > 0 && (b->footprint_side & 1) == 1,
                "footprint side must be odd and positive");
     PG_REQUIRE(b->map_side >= b->footprint_side && b->map_side <= b->footprint_side + 1,
@@ -1688,18 +1931,21 @@ painty_status painty_stamps_f32_noalloc(const painty_stamp_buffers_f32* b, void*
     a.depositionRate = static_cast<float>(b->deposition_rate);
     a.capacity = static_cast<float>(b->capacity);
     a.use_snapshot = snap ? 1 : 0;
-    a.dirty = nullptr;  // no dirty map: the whole ring is refreshed, as painty does
+    a.ring = nullptr;  // no state kept between calls: the first stamp refreshes its whole ring
+    a.ring_reset = pg::kRingUnknown;
     a.pickup_zero = 0;
     a.owner_global = scratch;
     a.status = status;
-    const pg::SmemPlan plan = pg::plan_smem<float>(b->footprint_side, b->map_side, false);
+    a.support2 = 2 * b->footprint_side * b->footprint_side;  // no cull: every box pixel
+    const pg::SmemPlan plan = pg::plan_smem<float>(
+        b->footprint_side, b->map_side, pg::disc_count(b->footprint_side, a.support2), false);
+    a.ndisc = plan.ndisc;
     a.pickup_smem = plan.pick ? 1 : 0;
     a.footprint_smem = 0;
-    a.support2 = 2 * b->footprint_side * b->footprint_side;  // no cull: every box pixel
     a.footprint = b->footprint;  // global: the owner table is the scratch array
     auto kern = a.pickup_smem ? pg::stamp_kernel<true, true, float, float>
                               : pg::stamp_kernel<false, true, float, float>;
-    const pg::StampSmem Lk = pg::stamp_smem_layout<float>(b->footprint_side, b->map_side,
+    const pg::StampSmem Lk = pg::stamp_smem_layout<float>(b->footprint_side, b->map_side, a.ndisc,
                                                           false, a.pickup_smem != 0, false);
     PG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(Lk.total)));
