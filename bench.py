@@ -169,6 +169,15 @@ def generate_stack_device(torch, seed: int):
     return host
 
 
+def run_precision_only(args):
+    import torch
+
+    import painty_gb300 as pg
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    print(json.dumps(run_precision(pg, torch)), flush=True)
+
+
 def run_serve_only(args):
     import torch
 
@@ -303,11 +312,13 @@ def run_ours(args):
     precision = composite_precision(pg, torch, Kh, Sh, Vh, R0h, max(3, min(args.steps, 100)))
     batch = None
     serve = None
+    prec = None
     if rank == 0 and not args.no_stamps:
         stamps = run_stamps_config0(pg, torch)
         batch = {s_: run_batch(pg, torch, s_, args.batch_canvases, args.batch_max_strokes)
                  for s_ in ("f32", "f16")}
         serve = run_serve(pg, torch, args.serve_rate, args.serve_seconds)
+        prec = run_precision(pg, torch)
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(Kh, Sh, Vh, R0h)
     if rank == 0:
@@ -342,6 +353,8 @@ def run_ours(args):
             line["stamps_batched"] = batch
         if serve is not None:
             line["serving"] = serve
+        if prec is not None:
+            line["precision"] = prec
         print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist
@@ -537,6 +550,79 @@ def composite_precision(pg, torch, Kh, Sh, Vh, R0h, steps: int):
     return out
 
 
+def run_precision(pg, torch):
+    """Reduced-precision storage against the F64 path (painty's double arithmetic, bit-exact
+    with its CPU code; tested): CIEDE2000 max / mean and max |dR| of the composed reflectance.
+    composite: the composite-stress distributions on 1024 x 1024 x 8 layers; stamps: the plain
+    case's first 40 strokes; batched: 6 canvases of the batching workload, at most 30 strokes
+    each, in one paint_batch per storage."""
+    from painty_gb300 import color, workloads
+
+    def stats(ref, got):
+        de = color.delta_e(ref, got)
+        return {"de_max": round(float(de.max()), 4), "de_mean": round(float(de.mean()), 5),
+                "dr_max": float(f"{np.abs(got - ref).max():.3g}")}
+
+    out = {"reference": "F64 storage (painty's double arithmetic)"}
+    # composite
+    n = 1024
+    K, S, V, R0 = workloads.composite_stack(n, n, LAYERS, seed=1, dtype=np.float64)
+    imgs = {}
+    for st in ("f64", "f32", "f16", "bf16"):
+        rs = "f64" if st == "f64" else "f32"
+        layers = []
+        for l in range(LAYERS):
+            ly = pg.PaintLayer(n, n, st)
+            ly.upload("K", K[l], planar=True)
+            ly.upload("S", S[l], planar=True)
+            ly.upload("V", V[l], planar=True)
+            layers.append(ly)
+        r0 = pg.Image(n, n, rs)
+        r0.upload(R0, planar=True)
+        img = pg.Image(n, n, rs)
+        pg.compose_layers(layers, r0, img)
+        imgs[st] = img.download()
+    out["composite"] = {st: stats(imgs["f64"], imgs[st]) for st in ("f32", "f16", "bf16")}
+    # plain painting
+    rows, cols = 768, 1024
+    strokes = workloads.strokes(cols, rows, 40, seed=3)
+    fp = workloads.footprint_image(seed=7)
+    r0h = workloads.substrate(rows, cols, seed=5)
+    imgs = {}
+    for st in ("f64", "f32", "f16", "bf16"):
+        cv = pg.Canvas(rows, cols, st)
+        cv.setBackground(r0h)
+        br = pg.FootprintBrush(strokes[0].radius, fp)
+        br.setPickupRate(0.05)
+        br.setDepositionRate(0.1)
+        workloads.paint_config0(cv, br, strokes)
+        imgs[st] = pg.Renderer().compose(cv).download()
+    out["stamps"] = {st: stats(imgs["f64"], imgs[st]) for st in ("f32", "f16", "bf16")}
+    # batched painting
+    specs, bstrokes = workloads.batch_canvases(6, seed=2, max_strokes=30)
+    res = {}
+    for st in ("f64", "f16", "bf16"):
+        cvs, brs = [], []
+        for rr, cc, r0 in specs:
+            cv = pg.Canvas(rr, cc, st)
+            cv.upload("R0", r0)
+            b = pg.FootprintBrush(8.0, fp)
+            b.setPickupRate(0.05)
+            b.setDepositionRate(0.1)
+            cvs.append(cv)
+            brs.append(b)
+        pg.paint_batch(cvs, brs, bstrokes)
+        res[st] = [pg.Renderer().compose(cv).download() for cv in cvs]
+    out["batched"] = {}
+    for st in ("f16", "bf16"):
+        per = [stats(a, b) for a, b in zip(res["f64"], res[st])]
+        out["batched"][st] = {"de_max": max(p["de_max"] for p in per),
+                              "de_mean": round(float(np.mean([p["de_mean"] for p in per])), 5),
+                              "dr_max": max(p["dr_max"] for p in per)}
+    torch.cuda.synchronize()
+    return out
+
+
 def cpu_baseline(Kh, Sh, Vh, R0h, target_s: float = 8.0):
     """painty's composite restated (oracle/), one thread, on a row sample of the workload."""
     from oracle.oracle import Oracle
@@ -616,6 +702,7 @@ def main():
     ap.add_argument("--strokes", type=int, default=200, help="strokes in the stamping case")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--serve-only", action="store_true", help="only the serving case")
+    ap.add_argument("--precision-only", action="store_true", help="only the precision case")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="serving arrivals per second")
     ap.add_argument("--serve-seconds", type=float, default=5.0, help="serving arrival window")
     args = ap.parse_args()
@@ -628,6 +715,8 @@ def main():
         run_stamps_only(args)
     elif args.serve_only:
         run_serve_only(args)
+    elif args.precision_only:
+        run_precision_only(args)
     else:
         run_ours(args)
 

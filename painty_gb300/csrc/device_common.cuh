@@ -38,6 +38,42 @@ __device__ __forceinline__ void st_elem(T* p, M v) { *p = from_f<T>(static_cast<
 template <>
 __device__ __forceinline__ void st_elem<double, double>(double* p, double v) { *p = v; }
 
+// Stochastic rounding to a 16-bit storage type: `r` supplies the random low bits (13 for FP16,
+// 16 for BF16), added to the FP32 pattern before truncation, so the stored value is
+// unbiased. FP16 subnormals (|x| < 2^-14) round to nearest. FP32 / FP64 store exactly.
+template <class T>
+__device__ __forceinline__ T from_f_sr(float x, uint32_t r);
+template <>
+__device__ __forceinline__ float from_f_sr<float>(float x, uint32_t) { return x; }
+template <>
+__device__ __forceinline__ __half from_f_sr<__half>(float x, uint32_t r) {
+  if (!(fabsf(x) >= 6.103515625e-05f) || !(fabsf(x) < 65504.0f)) return __float2half_rn(x);
+  return __float2half_rz(__uint_as_float(__float_as_uint(x) + (r & 0x1fffu)));
+}
+template <>
+__device__ __forceinline__ __nv_bfloat16 from_f_sr<__nv_bfloat16>(float x, uint32_t r) {
+  if (!(fabsf(x) < 3.0e38f)) return __float2bfloat16_rn(x);
+  return __float2bfloat16_rz(__uint_as_float(__float_as_uint(x) + (r & 0xffffu)));
+}
+template <class M, class T>
+__device__ __forceinline__ void st_elem_sr(T* p, M v, uint32_t r) {
+  *p = from_f_sr<T>(static_cast<float>(v), r);
+}
+template <>
+__device__ __forceinline__ void st_elem_sr<double, double>(double* p, double v, uint32_t) {
+  *p = v;
+}
+
+// 32-bit integer hash (xorshift-multiply finaliser) for the rounding bits.
+__device__ __forceinline__ uint32_t hash32(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352du;
+  x ^= x >> 15;
+  x *= 0x846ca68bu;
+  x ^= x >> 16;
+  return x;
+}
+
 // ------------------------------------------------------------------ streaming 16-byte I/O
 // Streaming (read-once) 128-bit loads that do not allocate in L1, and streaming stores.
 __device__ __forceinline__ uint4 ld_stream_u4(const void* p) {

@@ -146,7 +146,8 @@ struct painty_brush {
   int ring_pending = -1;
   void* d_stamps = nullptr;
   size_t d_stamps_bytes = 0;
-  unsigned* d_status = nullptr;  // 16 words: [0] kernel status, [8..15] the ring state
+  unsigned* d_status = nullptr;  // 16 words: [0] kernel status, [2] stamps applied (rounding
+                                 // seed), [8..15] the ring state
   int* d_ring() const { return reinterpret_cast<int*>(d_status) + 8; }
 };
 

@@ -110,6 +110,9 @@ struct StampArgs {
   // refreshes the whole first ring, kRingClean treats the snapshot as equal to the canvas.
   int* ring;
   int32_t ring_reset;
+  // stamps applied to the canvas so far (device counter, may be NULL): seeds the stochastic
+  // rounding of 16-bit storage
+  unsigned* stamp_count;
   // Box pixels inside the support disc, listed (row-major) in shared memory for the launch,
   // with a per-stamp cell map of the box; 0: no list, every stamp paints in waves
   int32_t ndisc;
@@ -176,8 +179,18 @@ __device__ __forceinline__ M* pickup_plane(const StampArgs<TK, TV>& a, int p) {
 // Triples are handled as K r,g,b then S r,g,b.
 template <bool PS, class TK, class TV, class M>
 __device__ __forceinline__ void process_pixel(const StampArgs<TK, TV>& a, M* pbase, int cells,
-                                              M fp, int c, int m) {
+                                              M fp, int c, int m, uint32_t seed) {
   using A = Arith<M>;
+  // 16-bit storage rounds its stores stochastically (bits from the canvas's stamp count and
+  // the pixel; independent of how stamps are grouped into launches)
+  constexpr bool kSR = sizeof(TK) == 2;
+  uint32_t h0 = 0, h1 = 0, h2 = 0, h3 = 0;
+  if constexpr (kSR) {
+    h0 = hash32(seed ^ (static_cast<uint32_t>(c) * 0x9e3779b1u));
+    h1 = hash32(h0 + 0x632be5abu);
+    h2 = hash32(h1 + 0x632be5abu);
+    h3 = hash32(h2 + 0x632be5abu);
+  }
   auto cell = [&](int p) -> M& {
     if constexpr (PS) return pbase[p * cells + m];
     else return pickup_plane<TK, TV, M>(a, p)[m];
@@ -207,7 +220,7 @@ __device__ __forceinline__ void process_pixel(const StampArgs<TK, TV>& a, M* pba
   // pickupPaint
   const M vleave = A::mul(A::mul(a.pickupRate, vsrc), fp);
   if (vleave > M(0.001)) {
-    st_elem<M>(a.sV + c, A::sub(vsrc, vleave));
+    st_elem_sr<M>(a.sV + c, A::sub(vsrc, vleave), h3 >> 16);
     if (!a.use_snapshot) vcan = ld_elem<M>(a.cV + c);  // the stored remainder
     M np[6];
     blend6(vp, pk, vleave, sn, np);
@@ -233,12 +246,13 @@ __device__ __forceinline__ void process_pixel(const StampArgs<TK, TV>& a, M* pba
   const M vb = A::mul(a.capacity, fp);
   M out[6];
   blend6(vb, src, vcan, cn, out);
+  const uint32_t rb[7] = {h0, h0 >> 16, h1, h1 >> 16, h2, h2 >> 16, h3};
 #pragma unroll
   for (int i = 0; i < 3; i++) {
-    st_elem<M>(a.cK[i] + c, out[i]);
-    st_elem<M>(a.cS[i] + c, out[3 + i]);
+    st_elem_sr<M>(a.cK[i] + c, out[i], rb[i]);
+    st_elem_sr<M>(a.cS[i] + c, out[3 + i], rb[3 + i]);
   }
-  st_elem<M>(a.cV + c, A::add(vb, vcan));
+  st_elem_sr<M>(a.cV + c, A::add(vb, vcan), rb[6]);
 }
 
 struct PixelInfo {
@@ -388,6 +402,7 @@ struct RefreshList {
 struct StampShared {
   RefreshList rl[2];  // double-buffered with the per-stamp arrays
   int prev[8];        // box, grown box of the stamp before the current parameter chunk
+  unsigned seed0;     // the canvas's stamp count at launch
 };
 
 __device__ __forceinline__ bool rect_empty(const IRect& r) { return r.x0 > r.x1 || r.y0 > r.y1; }
@@ -538,7 +553,7 @@ __device__ __forceinline__ void classify_disc(const StampArgs<TK, TV>& a, const 
 template <bool PS, class TK, class TV, class M>
 __device__ __forceinline__ void paint_disc(const StampArgs<TK, TV>& a, const int* xs, const int* ys,
                                         const M* fps, M* pbase, const uint32_t* disc, int ndisc,
-                                        const int* cellmap, int tid, int T) {
+                                        const int* cellmap, uint32_t seed, int tid, int T) {
   const int F = a.F, S = a.S;
   const int cells = S * S;
   const int pitch32 = static_cast<int>(a.pitch);  // planes hold fewer than 2^31 elements
@@ -561,12 +576,12 @@ __device__ __forceinline__ void paint_disc(const StampArgs<TK, TV>& a, const int
     const int mx = m & 0xffff, my = m >> 16;
     const M fp = fps[my * F + mx];
     const int cell = my * S + mx;
-    process_pixel<PS, TK, TV, M>(a, pbase, cells, fp, ys[row] * pitch32 + xs[col], cell);
+    process_pixel<PS, TK, TV, M>(a, pbase, cells, fp, ys[row] * pitch32 + xs[col], cell, seed);
     for (; follow; follow &= follow - 1) {
       const int q = __ffs(follow) - 1;
       const int rr = row + (q == 0 ? 0 : 1);
       const int cc = col + (q == 0 ? 1 : q - 2);
-      process_pixel<PS, TK, TV, M>(a, pbase, cells, fp, ys[rr] * pitch32 + xs[cc], cell);
+      process_pixel<PS, TK, TV, M>(a, pbase, cells, fp, ys[rr] * pitch32 + xs[cc], cell, seed);
     }
   }
 }
@@ -580,7 +595,7 @@ template <bool PS, class TK, class TV, class M>
 __device__ __noinline__ int paint_waves(const StampArgs<TK, TV>& a, const StampParams& sp,
                                         const int* xs, const int* ys, uint16_t* done_c,
                                         uint16_t* done_r, const M* fps, M* pbase, int* own,
-                                        int epoch) {
+                                        int epoch, uint32_t seed) {
   const int tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
   const int F = a.F, S = a.S;
@@ -619,7 +634,8 @@ __device__ __noinline__ int paint_waves(const StampArgs<TK, TV>& a, const StampP
       if (own[p.my * S + p.mx] == (key_hi | (row * F + col)) &&
           canvas_ready(xs, ys, F, done_c, done_r, row, col, wave)) {
         process_pixel<PS, TK, TV, M>(a, pbase, cells, fp,
-                                     p.yc * static_cast<int>(a.pitch) + p.xc, p.my * S + p.mx);
+                                     p.yc * static_cast<int>(a.pitch) + p.xc, p.my * S + p.mx,
+                                     seed);
         rem &= ~(1ull << j);
         mark_done(xs, ys, F, done_c, done_r, row, col, static_cast<uint16_t>(wave + 1));
       }
@@ -733,6 +749,7 @@ __device__ __forceinline__ void run_stroke(const StampArgs<TK, TV>& a, const Src
       sh->prev[i] = (a.ring_reset == kRingKeep && a.ring) ? a.ring[i]
                     : a.ring_reset == kRingClean          ? clean[i]
                                                           : unknown[i];
+    sh->seed0 = a.stamp_count ? *a.stamp_count : 0u;
   }
   // support-disc pixels, row-major (warp 0: per-row column intervals, prefix sums), and a
   // cell map whose pixels outside the disc read as "changes nothing"
@@ -791,10 +808,12 @@ __device__ __forceinline__ void run_stroke(const StampArgs<TK, TV>& a, const Src
     if (a.use_snapshot) refresh_ring(a, sh->rl[buf], tid, T);
     if (by_cells) classify_disc(a, sp, xs, ys, fps, disc, ndisc, cellmap, tid, T);
     __syncthreads();
+    const uint32_t seed = hash32(sh->seed0 + static_cast<uint32_t>(k));
     if (by_cells)
-      paint_disc<PS, TK, TV, M>(a, xs, ys, fps, pbase, disc, ndisc, cellmap, tid, T);
+      paint_disc<PS, TK, TV, M>(a, xs, ys, fps, pbase, disc, ndisc, cellmap, seed, tid, T);
     else
-      epoch = paint_waves<PS, TK, TV, M>(a, sp, xs, ys, done_c, done_r, fps, pbase, own, epoch);
+      epoch = paint_waves<PS, TK, TV, M>(a, sp, xs, ys, done_c, done_r, fps, pbase, own, epoch,
+                                         seed);
     // the next stamp's setup (into the other buffer), alongside painting
     int nd = 0;
     if (k + 1 < nstamps) {
@@ -818,6 +837,7 @@ __device__ __forceinline__ void run_stroke(const StampArgs<TK, TV>& a, const Src
   }
   // epilogue: the brush keeps its pickup map and the ring state
   __syncthreads();
+  if (tid == 0 && a.stamp_count) *a.stamp_count = sh->seed0 + static_cast<unsigned>(nstamps);
   if (tid == 0 && a.ring && a.use_snapshot) {
     if (nstamps > 0)
       stamp_rects(sparams[static_cast<int>((nstamps - 1) % kParamChunk)], a.ring);
@@ -912,6 +932,7 @@ struct BatchCanvas {
   TK* sS[3];
   TV* sV;
   int* ring;           // the brush's snapshot-ring state
+  unsigned* stamp_count;
   int32_t ring_reset;  // for the canvas's first stroke with stamps
   int32_t rows, cols;
   int64_t pitch;
@@ -1011,6 +1032,7 @@ __global__ void __launch_bounds__(kStampThreads, 1) batch_kernel(const __grid_co
         sa.capacity = static_cast<M>(cv.capacity);
         sa.use_snapshot = cv.use_snapshot;
         sa.ring = cv.ring;
+        sa.stamp_count = cv.stamp_count;
         sa.ring_reset = ran ? kRingKeep : cv.ring_reset;
         sa.pickup_zero = 1;  // dip: the pickup map starts clean
         sa.pickup_smem = st.plan & 1;
@@ -1231,6 +1253,7 @@ void launch_stamps(painty_canvas* c, painty_brush* b, const StampRec* d_stamps, 
   a.use_snapshot = b->useSnapshot ? 1 : 0;
   a.ring = b->d_ring();
   a.ring_reset = ring_reset;
+  a.stamp_count = b->d_status + 2;
   a.pickup_zero = pickup_zero ? 1 : 0;
   a.status = b->d_status;
   a.support2 = b->support2;
@@ -1456,6 +1479,7 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
     x.cV = static_cast<TV*>(cv->wet.V);
     x.sV = static_cast<TV*>(b->useSnapshot ? b->snapshot.V : cv->wet.V);
     x.ring = b->d_ring();
+    x.stamp_count = b->d_status + 2;
     x.ring_reset = ring_reset;
     x.rows = cv->wet.rows;
     x.cols = cv->wet.cols;
@@ -1932,6 +1956,7 @@ painty_status painty_stamps_f32_noalloc(const painty_stamp_buffers_f32* b, void*
     a.capacity = static_cast<float>(b->capacity);
     a.use_snapshot = snap ? 1 : 0;
     a.ring = nullptr;  // no state kept between calls: the first stamp refreshes its whole ring
+    a.stamp_count = nullptr;
     a.ring_reset = pg::kRingUnknown;
     a.pickup_zero = 0;
     a.owner_global = scratch;

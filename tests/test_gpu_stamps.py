@@ -13,9 +13,10 @@ pytestmark = pytest.mark.gpu
 F32_REL_TOL = 2e-3   # per-value relative error of K, S, V after a stroke sequence (FP32)
 F32_DELTA_E = 0.05   # CIEDE2000 of the composed canvas, FP32 storage vs the double oracle
 F16_DELTA_E = 0.5    # CIEDE2000 of the composed canvas, FP16 storage vs the double oracle
-# BF16 keeps 8 significant bits; a pixel re-blended by every stamp over it drifts by up to
-# about one CIEDE2000 unit on this case (measured 1.04 max, 0.23 mean): the bound documents it.
-BF16_DELTA_E = 1.5
+# BF16 keeps 8 significant bits; a pixel re-blended by every stamp over it drifts. With the
+# stochastic rounding of 16-bit stores this case measures 1.50 max, 0.31 mean (round-to-nearest:
+# 1.04 here, but twice the stochastic error on long painting sessions): the bound documents it.
+BF16_DELTA_E = 2.0
 
 
 def _gpu_replay(pg, fx, name, storage="f64"):
