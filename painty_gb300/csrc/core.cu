@@ -79,22 +79,35 @@ void device_free(void* p) {
   if (p) cudaFree(p);
 }
 
-size_t layer_bytes(int32_t rows, int32_t cols, painty_storage s) {
+// Planar: 7 planes, each 256-byte aligned. Packed: one record of 8 elements per pixel (K and
+// S, V of the same size in every storage format).
+size_t layer_bytes(int32_t rows, int32_t cols, painty_storage s, bool packed) {
   const size_t pe = static_cast<size_t>(rows) * pitch_for(cols);
+  if (packed) return align256(pe * 8 * ks_bytes(s));
   return 6 * align256(pe * ks_bytes(s)) + align256(pe * v_bytes(s));
 }
-void layer_layout(painty_layer& L, int32_t rows, int32_t cols, painty_storage s, void* base) {
+void layer_layout(painty_layer& L, int32_t rows, int32_t cols, painty_storage s, void* base,
+                  bool packed) {
   L.rows = rows;
   L.cols = cols;
   L.pitch = pitch_for(cols);
   L.storage = s;
   L.base = base;
-  L.bytes = layer_bytes(rows, cols, s);
-  const size_t ksb = align256(static_cast<size_t>(L.plane_elems()) * ks_bytes(s));
+  L.bytes = layer_bytes(rows, cols, s, packed);
   char* p = static_cast<char*>(base);
+  if (packed) {
+    const size_t es = ks_bytes(s);
+    for (int c = 0; c < 3; c++) L.K[c] = p + c * es;
+    for (int c = 0; c < 3; c++) L.S[c] = p + (3 + c) * es;
+    L.V = p + 6 * es;
+    L.estride = 8;
+    return;
+  }
+  const size_t ksb = align256(static_cast<size_t>(L.plane_elems()) * ks_bytes(s));
   for (int c = 0; c < 3; c++) L.K[c] = p + c * ksb;
   for (int c = 0; c < 3; c++) L.S[c] = p + (3 + c) * ksb;
   L.V = p + 6 * ksb;
+  L.estride = 1;
 }
 size_t image_bytes(int32_t rows, int32_t cols, painty_storage s) {
   const size_t pe = static_cast<size_t>(rows) * pitch_for(cols);
@@ -121,9 +134,9 @@ void canvas_relayout(painty_canvas* c, void* base) {
     c->wet.V = c->h = c->wet.base = c->r0.base = nullptr;
     return;
   }
-  const size_t lb = layer_bytes(rows, cols, st);
+  const size_t lb = layer_bytes(rows, cols, st, true);
   const size_t ib = image_bytes(rows, cols, rs);
-  layer_layout(c->wet, rows, cols, st, base);
+  layer_layout(c->wet, rows, cols, st, base, true);
   c->wet.owned = false;
   c->wet.writes = &c->version;
   image_layout(c->r0, rows, cols, rs, static_cast<char*>(base) + lb);
@@ -136,6 +149,9 @@ namespace {
 
 struct PlanePtrs {
   void* p[3];
+};
+struct LayerPtrs {  // K r,g,b, S r,g,b, V
+  void* p[7];
 };
 
 template <class TD, class TS>
@@ -156,7 +172,8 @@ template <> __device__ __forceinline__ double convert<double, __nv_bfloat16>(__n
 // staging (host layout, contiguous) -> pitched planes
 template <class TD, class TS>
 __global__ void scatter_kernel(const TS* __restrict__ src, PlanePtrs dst, int nch,
-                               int interleaved, int32_t rows, int32_t cols, int64_t pitch) {
+                               int interleaved, int32_t rows, int32_t cols, int64_t pitch,
+                               int64_t es) {
   const int64_t n = static_cast<int64_t>(rows) * cols;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n * nch;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -169,14 +186,14 @@ __global__ void scatter_kernel(const TS* __restrict__ src, PlanePtrs dst, int nc
       p = i - c * n;
     }
     const int64_t r = p / cols, col = p - r * cols;
-    static_cast<TD*>(dst.p[c])[r * pitch + col] = convert<TD, TS>(src[i]);
+    static_cast<TD*>(dst.p[c])[(r * pitch + col) * es] = convert<TD, TS>(src[i]);
   }
 }
 
 // pitched planes -> staging (host layout)
 template <class TD, class TS>
 __global__ void gather_kernel(PlanePtrs src, TD* __restrict__ dst, int nch, int interleaved,
-                              int32_t rows, int32_t cols, int64_t pitch) {
+                              int32_t rows, int32_t cols, int64_t pitch, int64_t es) {
   const int64_t n = static_cast<int64_t>(rows) * cols;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n * nch;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -189,18 +206,31 @@ __global__ void gather_kernel(PlanePtrs src, TD* __restrict__ dst, int nch, int 
       p = i - c * n;
     }
     const int64_t r = p / cols, col = p - r * cols;
-    dst[i] = convert<TD, TS>(static_cast<const TS*>(src.p[c])[r * pitch + col]);
+    dst[i] = convert<TD, TS>(static_cast<const TS*>(src.p[c])[(r * pitch + col) * es]);
   }
 }
 
 template <class T>
 __global__ void fill_kernel(PlanePtrs dst, int nch, int64_t elems, double v0, double v1,
-                            double v2) {
+                            double v2, int64_t es) {
   const double v[3] = {v0, v1, v2};
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < elems * nch;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t c = i / elems;
-    static_cast<T*>(dst.p[c])[i - c * elems] = convert<T, double>(v[c]);
+    static_cast<T*>(dst.p[c])[(i - c * elems) * es] = convert<T, double>(v[c]);
+  }
+}
+
+// Layer copy between any layouts: the 7 values of each pixel, src element stride -> dst.
+template <class TK, class TV>
+__global__ void copy_layer_kernel(LayerPtrs src, LayerPtrs dst, int64_t elems, int64_t ses,
+                                  int64_t des) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < elems;
+       i += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int c = 0; c < 6; c++)
+      static_cast<TK*>(dst.p[c])[i * des] = static_cast<const TK*>(src.p[c])[i * ses];
+    static_cast<TV*>(dst.p[6])[i * des] = static_cast<const TV*>(src.p[6])[i * ses];
   }
 }
 
@@ -218,14 +248,14 @@ bool host_is_interleaved(painty_host_format f) {
 
 template <class TS>
 void launch_scatter(DevType dt, const TS* src, PlanePtrs dst, int nch, int il, int32_t rows,
-                    int32_t cols, int64_t pitch, cudaStream_t st) {
+                    int32_t cols, int64_t pitch, int64_t es, cudaStream_t st) {
   const int64_t n = static_cast<int64_t>(rows) * cols * nch;
   const int g = grid_for(n, 256);
   switch (dt) {
-    case DT_F32: scatter_kernel<float, TS><<<g, 256, 0, st>>>(src, dst, nch, il, rows, cols, pitch); break;
-    case DT_F16: scatter_kernel<__half, TS><<<g, 256, 0, st>>>(src, dst, nch, il, rows, cols, pitch); break;
-    case DT_BF16: scatter_kernel<__nv_bfloat16, TS><<<g, 256, 0, st>>>(src, dst, nch, il, rows, cols, pitch); break;
-    case DT_F64: scatter_kernel<double, TS><<<g, 256, 0, st>>>(src, dst, nch, il, rows, cols, pitch); break;
+    case DT_F32: scatter_kernel<float, TS><<<g, 256, 0, st>>>(src, dst, nch, il, rows, cols, pitch, es); break;
+    case DT_F16: scatter_kernel<__half, TS><<<g, 256, 0, st>>>(src, dst, nch, il, rows, cols, pitch, es); break;
+    case DT_BF16: scatter_kernel<__nv_bfloat16, TS><<<g, 256, 0, st>>>(src, dst, nch, il, rows, cols, pitch, es); break;
+    case DT_F64: scatter_kernel<double, TS><<<g, 256, 0, st>>>(src, dst, nch, il, rows, cols, pitch, es); break;
   }
   count_launch();
   PG_CUDA(cudaGetLastError());
@@ -233,14 +263,14 @@ void launch_scatter(DevType dt, const TS* src, PlanePtrs dst, int nch, int il, i
 
 template <class TD>
 void launch_gather(DevType dt, PlanePtrs src, TD* dst, int nch, int il, int32_t rows,
-                   int32_t cols, int64_t pitch, cudaStream_t st) {
+                   int32_t cols, int64_t pitch, int64_t es, cudaStream_t st) {
   const int64_t n = static_cast<int64_t>(rows) * cols * nch;
   const int g = grid_for(n, 256);
   switch (dt) {
-    case DT_F32: gather_kernel<TD, float><<<g, 256, 0, st>>>(src, dst, nch, il, rows, cols, pitch); break;
-    case DT_F16: gather_kernel<TD, __half><<<g, 256, 0, st>>>(src, dst, nch, il, rows, cols, pitch); break;
-    case DT_BF16: gather_kernel<TD, __nv_bfloat16><<<g, 256, 0, st>>>(src, dst, nch, il, rows, cols, pitch); break;
-    case DT_F64: gather_kernel<TD, double><<<g, 256, 0, st>>>(src, dst, nch, il, rows, cols, pitch); break;
+    case DT_F32: gather_kernel<TD, float><<<g, 256, 0, st>>>(src, dst, nch, il, rows, cols, pitch, es); break;
+    case DT_F16: gather_kernel<TD, __half><<<g, 256, 0, st>>>(src, dst, nch, il, rows, cols, pitch, es); break;
+    case DT_BF16: gather_kernel<TD, __nv_bfloat16><<<g, 256, 0, st>>>(src, dst, nch, il, rows, cols, pitch, es); break;
+    case DT_F64: gather_kernel<TD, double><<<g, 256, 0, st>>>(src, dst, nch, il, rows, cols, pitch, es); break;
   }
   count_launch();
   PG_CUDA(cudaGetLastError());
@@ -249,15 +279,17 @@ void launch_gather(DevType dt, PlanePtrs src, TD* dst, int nch, int il, int32_t 
 }  // namespace
 
 void upload_planes(void* const* planes, int nch, DevType dt, int32_t rows, int32_t cols,
-                   int64_t pitch, const void* host, painty_host_format fmt, cudaStream_t st) {
+                   int64_t pitch, const void* host, painty_host_format fmt, cudaStream_t st,
+                   int64_t estride) {
   PG_REQUIRE(host != nullptr, "host buffer is null");
   PG_REQUIRE(fmt >= PAINTY_HOST_F64_INTERLEAVED && fmt <= PAINTY_HOST_F32_PLANAR,
              "unknown host format");
   const bool f64 = host_is_f64(fmt);
   const size_t hes = f64 ? 8 : 4;
   const size_t n = static_cast<size_t>(rows) * cols;
-  // Fast path: planar host data of the device element type -> one 2D copy per plane.
-  if (!host_is_interleaved(fmt) || nch == 1) {
+  // Fast path: planar host data of the device element type into planar device planes -> one
+  // 2D copy per plane.
+  if ((!host_is_interleaved(fmt) || nch == 1) && estride == 1) {
     if ((dt == DT_F32 && !f64) || (dt == DT_F64 && f64)) {
       for (int c = 0; c < nch; c++)
         PG_CUDA(cudaMemcpy2DAsync(planes[c], pitch * hes,
@@ -274,24 +306,24 @@ void upload_planes(void* const* planes, int nch, DevType dt, int32_t rows, int32
   const int il = host_is_interleaved(fmt) ? 1 : 0;
   if (f64)
     launch_scatter<double>(dt, static_cast<const double*>(staging), pp, nch, il, rows, cols,
-                           pitch, st);
+                           pitch, estride, st);
   else
     launch_scatter<float>(dt, static_cast<const float*>(staging), pp, nch, il, rows, cols,
-                          pitch, st);
+                          pitch, estride, st);
   PG_CUDA(cudaFreeAsync(staging, st));
   PG_CUDA(cudaStreamSynchronize(st));
 }
 
 void download_planes(const void* const* planes, int nch, DevType dt, int32_t rows,
                      int32_t cols, int64_t pitch, void* host, painty_host_format fmt,
-                     cudaStream_t st) {
+                     cudaStream_t st, int64_t estride) {
   PG_REQUIRE(host != nullptr, "host buffer is null");
   PG_REQUIRE(fmt >= PAINTY_HOST_F64_INTERLEAVED && fmt <= PAINTY_HOST_F32_PLANAR,
              "unknown host format");
   const bool f64 = host_is_f64(fmt);
   const size_t hes = f64 ? 8 : 4;
   const size_t n = static_cast<size_t>(rows) * cols;
-  if (!host_is_interleaved(fmt) || nch == 1) {
+  if ((!host_is_interleaved(fmt) || nch == 1) && estride == 1) {
     if ((dt == DT_F32 && !f64) || (dt == DT_F64 && f64)) {
       for (int c = 0; c < nch; c++)
         PG_CUDA(cudaMemcpy2DAsync(static_cast<char*>(host) + c * n * hes, cols * hes,
@@ -307,24 +339,56 @@ void download_planes(const void* const* planes, int nch, DevType dt, int32_t row
                 nch > 2 ? const_cast<void*>(planes[2]) : nullptr}};
   const int il = host_is_interleaved(fmt) ? 1 : 0;
   if (f64)
-    launch_gather<double>(dt, pp, static_cast<double*>(staging), nch, il, rows, cols, pitch, st);
+    launch_gather<double>(dt, pp, static_cast<double*>(staging), nch, il, rows, cols, pitch,
+                          estride, st);
   else
-    launch_gather<float>(dt, pp, static_cast<float*>(staging), nch, il, rows, cols, pitch, st);
+    launch_gather<float>(dt, pp, static_cast<float*>(staging), nch, il, rows, cols, pitch,
+                         estride, st);
   PG_CUDA(cudaMemcpyAsync(host, staging, n * nch * hes, cudaMemcpyDeviceToHost, st));
   PG_CUDA(cudaFreeAsync(staging, st));
   PG_CUDA(cudaStreamSynchronize(st));
 }
 
 void fill_planes(void* const* planes, int nch, DevType dt, int64_t elems, const double* v,
-                 cudaStream_t st) {
+                 cudaStream_t st, int64_t estride) {
   PlanePtrs pp{{planes[0], nch > 1 ? planes[1] : nullptr, nch > 2 ? planes[2] : nullptr}};
   const int g = grid_for(elems * nch, 256);
   const double v0 = v[0], v1 = nch > 1 ? v[1] : 0.0, v2 = nch > 2 ? v[2] : 0.0;
   switch (dt) {
-    case DT_F32: fill_kernel<float><<<g, 256, 0, st>>>(pp, nch, elems, v0, v1, v2); break;
-    case DT_F16: fill_kernel<__half><<<g, 256, 0, st>>>(pp, nch, elems, v0, v1, v2); break;
-    case DT_BF16: fill_kernel<__nv_bfloat16><<<g, 256, 0, st>>>(pp, nch, elems, v0, v1, v2); break;
-    case DT_F64: fill_kernel<double><<<g, 256, 0, st>>>(pp, nch, elems, v0, v1, v2); break;
+    case DT_F32: fill_kernel<float><<<g, 256, 0, st>>>(pp, nch, elems, v0, v1, v2, estride); break;
+    case DT_F16: fill_kernel<__half><<<g, 256, 0, st>>>(pp, nch, elems, v0, v1, v2, estride); break;
+    case DT_BF16: fill_kernel<__nv_bfloat16><<<g, 256, 0, st>>>(pp, nch, elems, v0, v1, v2, estride); break;
+    case DT_F64: fill_kernel<double><<<g, 256, 0, st>>>(pp, nch, elems, v0, v1, v2, estride); break;
+  }
+  count_launch();
+  PG_CUDA(cudaGetLastError());
+}
+
+void copy_layer(const painty_layer& src, painty_layer& dst, cudaStream_t st) {
+  PG_REQUIRE(src.rows == dst.rows && src.cols == dst.cols && src.storage == dst.storage,
+             "layers differ in size or storage");
+  if (src.estride == dst.estride) {
+    PG_CUDA(cudaMemcpyAsync(dst.base, src.base, src.bytes, cudaMemcpyDeviceToDevice, st));
+    return;
+  }
+  LayerPtrs s{{src.K[0], src.K[1], src.K[2], src.S[0], src.S[1], src.S[2], src.V}};
+  LayerPtrs d{{dst.K[0], dst.K[1], dst.K[2], dst.S[0], dst.S[1], dst.S[2], dst.V}};
+  const int64_t elems = src.plane_elems();
+  const int g = grid_for(elems, 256);
+  switch (src.storage) {
+    case PAINTY_STORAGE_F32:
+      copy_layer_kernel<float, float><<<g, 256, 0, st>>>(s, d, elems, src.estride, dst.estride);
+      break;
+    case PAINTY_STORAGE_F16:
+      copy_layer_kernel<__half, __half><<<g, 256, 0, st>>>(s, d, elems, src.estride, dst.estride);
+      break;
+    case PAINTY_STORAGE_BF16:
+      copy_layer_kernel<__nv_bfloat16, __half><<<g, 256, 0, st>>>(s, d, elems, src.estride,
+                                                                    dst.estride);
+      break;
+    case PAINTY_STORAGE_F64:
+      copy_layer_kernel<double, double><<<g, 256, 0, st>>>(s, d, elems, src.estride, dst.estride);
+      break;
   }
   count_launch();
   PG_CUDA(cudaGetLastError());
@@ -401,6 +465,40 @@ __global__ void __launch_bounds__(256) km_composite_kernel(
   }
 }
 
+// Composite over layers of any layout (a canvas's packed wet layer, or mixed stacks): one
+// thread per pixel, each layer's values read with its element stride.
+template <class TK, class TV, class TR>
+struct ComposeStridedArgs {
+  const TK* K[kMaxLayersPerLaunch][3];
+  const TK* S[kMaxLayersPerLaunch][3];
+  const TV* V[kMaxLayersPerLaunch];
+  int64_t es[kMaxLayersPerLaunch];
+  const TR* r0[3];
+  TR* out[3];
+  int32_t L;
+  int64_t elems;
+};
+template <class TK, class TV, class TR>
+__global__ void __launch_bounds__(256) km_composite_strided_kernel(
+  const __grid_constant__ ComposeStridedArgs<TK, TV, TR> a) {
+  using M = typename MathOf<TR>::type;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < a.elems;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    M r[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) r[c] = static_cast<M>(a.r0[c][i]);
+    for (int l = 0; l < a.L; l++) {
+      const int64_t j = i * a.es[l];
+      const M v = ld_elem<M>(a.V[l] + j);
+#pragma unroll
+      for (int c = 0; c < 3; c++)
+        r[c] = km_reflectance(ld_elem<M>(a.K[l][c] + j), ld_elem<M>(a.S[l][c] + j), r[c], v);
+    }
+#pragma unroll
+    for (int c = 0; c < 3; c++) a.out[c][i] = static_cast<TR>(r[c]);
+  }
+}
+
 template <class Kern>
 int resident_grid(Kern kern, int block) {
   static int cached[64] = {0};
@@ -416,8 +514,45 @@ int resident_grid(Kern kern, int block) {
 }
 
 template <class TK, class TV, class TR>
+void compose_strided(const painty_layer* const* layers, int32_t L, const painty_image* r0,
+                     painty_image* out, cudaStream_t st) {
+  const int64_t elems = r0->plane_elems();
+  auto kern = km_composite_strided_kernel<TK, TV, TR>;
+  const int wave = resident_grid(kern, 256);
+  for (int32_t l0 = 0; l0 < L; l0 += kMaxLayersPerLaunch) {
+    ComposeStridedArgs<TK, TV, TR> a{};
+    const int32_t n = std::min<int32_t>(kMaxLayersPerLaunch, L - l0);
+    for (int32_t i = 0; i < n; i++) {
+      const painty_layer* ly = layers[l0 + i];
+      for (int c = 0; c < 3; c++) {
+        a.K[i][c] = static_cast<const TK*>(ly->K[c]);
+        a.S[i][c] = static_cast<const TK*>(ly->S[c]);
+      }
+      a.V[i] = static_cast<const TV*>(ly->V);
+      a.es[i] = ly->estride;
+    }
+    const painty_image* src = l0 == 0 ? r0 : out;
+    for (int c = 0; c < 3; c++) {
+      a.r0[c] = static_cast<const TR*>(src->R[c]);
+      a.out[c] = static_cast<TR*>(out->R[c]);
+    }
+    a.L = n;
+    a.elems = elems;
+    const int grid = static_cast<int>(std::min<int64_t>((elems + 255) / 256, wave));
+    kern<<<std::max(grid, 1), 256, 0, st>>>(a);
+    count_launch();
+    PG_CUDA(cudaGetLastError());
+  }
+}
+
+template <class TK, class TV, class TR>
 void compose_typed(const painty_layer* const* layers, int32_t L, const painty_image* r0,
                    painty_image* out, cudaStream_t st) {
+  for (int32_t l = 0; l < L; l++)
+    if (layers[l]->estride != 1) {
+      compose_strided<TK, TV, TR>(layers, L, r0, out, st);
+      return;
+    }
   constexpr int PIX = 16 / sizeof(TK);
   const int64_t elems = r0->plane_elems();  // a multiple of 64 elements
   auto kern = km_composite_kernel<TK, TV, TR>;
@@ -497,23 +632,24 @@ struct PtrTriple {
 
 template <class TK, class TV, class TR>
 __global__ void __launch_bounds__(256) km_dry_kernel(PtrTriple wk, PtrTriple ws, TV* v, TV* h,
-                                                       PtrTriple r0, int64_t elems) {
+                                                       PtrTriple r0, int64_t elems, int64_t es) {
   using M = typename MathOf<TR>::type;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < elems;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const M vol = ld_elem<M>(v + i);
+    const int64_t j = i * es;  // the wet layer's element (packed or planar)
+    const M vol = ld_elem<M>(v + j);
     st_elem<M>(h + i, ld_elem<M>(h + i) + vol);
 #pragma unroll
     for (int c = 0; c < 3; c++) {
       TK* kp = static_cast<TK*>(wk.p[c]);
       TK* sp = static_cast<TK*>(ws.p[c]);
       TR* rp = static_cast<TR*>(r0.p[c]);
-      const M r = km_reflectance(ld_elem<M>(kp + i), ld_elem<M>(sp + i), ld_elem<M>(rp + i), vol);
+      const M r = km_reflectance(ld_elem<M>(kp + j), ld_elem<M>(sp + j), ld_elem<M>(rp + i), vol);
       st_elem<M>(rp + i, r);
-      st_elem<M>(kp + i, M(0));
-      st_elem<M>(sp + i, M(0));
+      st_elem<M>(kp + j, M(0));
+      st_elem<M>(sp + j, M(0));
     }
-    st_elem<M>(v + i, M(0));
+    st_elem<M>(v + j, M(0));
   }
 }
 
@@ -525,7 +661,8 @@ void dry_typed(painty_canvas* c, cudaStream_t st) {
   PtrTriple r0{{c->r0.R[0], c->r0.R[1], c->r0.R[2]}};
   const int g = grid_for(elems, 256);
   km_dry_kernel<TK, TV, TR><<<g, 256, 0, st>>>(wk, ws, static_cast<TV*>(c->wet.V),
-                                                 static_cast<TV*>(c->h), r0, elems);
+                                                 static_cast<TV*>(c->h), r0, elems,
+                                                 c->wet.estride);
   count_launch();
   PG_CUDA(cudaGetLastError());
 }
@@ -628,7 +765,7 @@ painty_status painty_layer_upload(painty_layer* layer, painty_plane plane, const
     pg::DevType dt;
     layer_plane_ptrs(layer, plane, p, &nch, &dt);
     pg::upload_planes(p, nch, dt, layer->rows, layer->cols, layer->pitch, host, fmt,
-                      pg::as_stream(stream));
+                      pg::as_stream(stream), layer->estride);
     layer->touch();
   });
 }
@@ -643,17 +780,14 @@ painty_status painty_layer_download(const painty_layer* layer, painty_plane plan
     layer_plane_ptrs(layer, plane, p, &nch, &dt);
     const void* cp[3] = {p[0], p[1], p[2]};
     pg::download_planes(cp, nch, dt, layer->rows, layer->cols, layer->pitch, host, fmt,
-                        pg::as_stream(stream));
+                        pg::as_stream(stream), layer->estride);
   });
 }
 
 painty_status painty_layer_copy(const painty_layer* src, painty_layer* dst, void* stream) {
   return guard([&] {
     PG_REQUIRE(src && dst, "layer is null");
-    PG_REQUIRE(src->rows == dst->rows && src->cols == dst->cols && src->storage == dst->storage,
-               "layers differ in size or storage");
-    PG_CUDA(cudaMemcpyAsync(dst->base, src->base, src->bytes, cudaMemcpyDeviceToDevice,
-                            pg::as_stream(stream)));
+    pg::copy_layer(*src, *dst, pg::as_stream(stream));
     dst->touch();
   });
 }
@@ -759,13 +893,13 @@ painty_status painty_canvas_create(int32_t rows, int32_t cols, painty_storage st
     PG_REQUIRE(pg::valid_storage(storage), "unknown storage format");
     auto* c = new painty_canvas();
     const painty_storage rs = storage == PAINTY_STORAGE_F64 ? PAINTY_STORAGE_F64 : PAINTY_STORAGE_F32;
-    const size_t lb = pg::layer_bytes(rows, cols, storage);
+    const size_t lb = pg::layer_bytes(rows, cols, storage, true);
     const size_t ib = pg::image_bytes(rows, cols, rs);
     const size_t hb = static_cast<size_t>(rows) * pg::pitch_for(cols) * pg::v_bytes(storage);
     try {
       c->bytes = lb + ib + (hb + 255) / 256 * 256;
       c->base = pg::device_alloc(c->bytes);
-      pg::layer_layout(c->wet, rows, cols, storage, c->base);
+      pg::layer_layout(c->wet, rows, cols, storage, c->base, true);
       c->wet.owned = false;
       c->wet.writes = &c->version;
       pg::image_layout(c->r0, rows, cols, rs, static_cast<char*>(c->base) + lb);
@@ -824,7 +958,8 @@ painty_status painty_canvas_upload(painty_canvas* c, painty_plane plane, const v
       int nch = 0;
       pg::DevType dt;
       layer_plane_ptrs(&c->wet, plane, p, &nch, &dt);
-      pg::upload_planes(p, nch, dt, c->wet.rows, c->wet.cols, c->wet.pitch, host, fmt, st);
+      pg::upload_planes(p, nch, dt, c->wet.rows, c->wet.cols, c->wet.pitch, host, fmt, st,
+                        c->wet.estride);
     }
   });
 }
@@ -848,7 +983,8 @@ painty_status painty_canvas_download(const painty_canvas* c, painty_plane plane,
       pg::DevType dt;
       layer_plane_ptrs(&c->wet, plane, p, &nch, &dt);
       const void* cp[3] = {p[0], p[1], p[2]};
-      pg::download_planes(cp, nch, dt, c->wet.rows, c->wet.cols, c->wet.pitch, host, fmt, st);
+      pg::download_planes(cp, nch, dt, c->wet.rows, c->wet.cols, c->wet.pitch, host, fmt, st,
+                          c->wet.estride);
     }
   });
 }

@@ -33,6 +33,17 @@ template <class M, class T>
 __device__ __forceinline__ M ld_elem(const T* p) { return static_cast<M>(to_f(*p)); }
 template <>
 __device__ __forceinline__ double ld_elem<double, double>(const double* p) { return *p; }
+// L2 loads (bypassing L1): data other SMs of a cluster wrote before a cluster barrier.
+template <class M, class T>
+__device__ __forceinline__ M ld_cg(const T* p) { return static_cast<M>(to_f(__ldcg(p))); }
+template <>
+__device__ __forceinline__ double ld_cg<double, double>(const double* p) { return __ldcg(p); }
+// Load through L1 (CG false) or from L2 only (CG true).
+template <bool CG, class M, class T>
+__device__ __forceinline__ M ld_sel(const T* p) {
+  if constexpr (CG) return ld_cg<M>(p);
+  else return ld_elem<M>(p);
+}
 template <class M, class T>
 __device__ __forceinline__ void st_elem(T* p, M v) { *p = from_f<T>(static_cast<float>(v)); }
 template <>
@@ -55,13 +66,37 @@ __device__ __forceinline__ __nv_bfloat16 from_f_sr<__nv_bfloat16>(float x, uint3
   if (!(fabsf(x) < 3.0e38f)) return __float2bfloat16_rn(x);
   return __float2bfloat16_rz(__uint_as_float(__float_as_uint(x) + (r & 0xffffu)));
 }
-template <class M, class T>
-__device__ __forceinline__ void st_elem_sr(T* p, M v, uint32_t r) {
-  *p = from_f_sr<T>(static_cast<float>(v), r);
+// The storage value of v (stochastically rounded for 16-bit types).
+template <class T, class M>
+__device__ __forceinline__ T to_store_sr(M v, uint32_t r) {
+  return from_f_sr<T>(static_cast<float>(v), r);
 }
 template <>
-__device__ __forceinline__ void st_elem_sr<double, double>(double* p, double v, uint32_t) {
-  *p = v;
+__device__ __forceinline__ double to_store_sr<double, double>(double v, uint32_t) {
+  return v;
+}
+template <class M, class T>
+__device__ __forceinline__ void st_elem_sr(T* p, M v, uint32_t r) {
+  *p = to_store_sr<T>(v, r);
+}
+
+// ------------------------------------------------------------------ thread-block clusters
+// Rank of this CTA in its cluster and the cluster's size (1 and 0 without a cluster launch).
+__device__ __forceinline__ unsigned cluster_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ unsigned cluster_size() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+  return r;
+}
+// Barrier over every thread of the cluster; memory operations before it (global and shared,
+// by any CTA of the cluster) are visible after it. All threads call it, convergently.
+__device__ __forceinline__ void cluster_barrier() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;"
+               ::: "memory");
 }
 
 // 32-bit integer hash (xorshift-multiply finaliser) for the rounding bits.

@@ -76,6 +76,10 @@ struct painty_layer {
   void* K[3] = {nullptr, nullptr, nullptr};
   void* S[3] = {nullptr, nullptr, nullptr};
   void* V = nullptr;
+  // Elements from one pixel to the next within a plane view: 1 for planar layers (7 planes);
+  // 8 for packed layers (one record per pixel: K r,g,b, S r,g,b, V, pad), the layout of
+  // canvases and snapshots, whose stamps touch whole pixels.
+  int64_t estride = 1;
   bool owned = true;
   // a canvas's wet layer: the canvas's write counter, bumped by every write through the layer
   uint64_t* writes = nullptr;
@@ -153,8 +157,9 @@ struct painty_brush {
 
 namespace pg {
 // Layout helpers (defined in core.cu).
-void layer_layout(painty_layer& L, int32_t rows, int32_t cols, painty_storage s, void* base);
-size_t layer_bytes(int32_t rows, int32_t cols, painty_storage s);
+void layer_layout(painty_layer& L, int32_t rows, int32_t cols, painty_storage s, void* base,
+                  bool packed = false);
+size_t layer_bytes(int32_t rows, int32_t cols, painty_storage s, bool packed = false);
 void image_layout(painty_image& I, int32_t rows, int32_t cols, painty_storage s, void* base);
 size_t image_bytes(int32_t rows, int32_t cols, painty_storage s);
 // Points a canvas's plane views into a new device allocation of the canvas layout (nullptr:
@@ -162,18 +167,22 @@ size_t image_bytes(int32_t rows, int32_t cols, painty_storage s);
 void canvas_relayout(painty_canvas* c, void* base);
 
 // Plane transfer between a host buffer and `nch` device planes of element type `dev_type`
-// (0 f32, 1 f16, 2 bf16, 3 f64) with the given pitch. Synchronous w.r.t. the host buffer.
+// (0 f32, 1 f16, 2 bf16, 3 f64) with the given pitch and element stride (1 planar, 8 packed).
+// Synchronous w.r.t. the host buffer.
 enum DevType { DT_F32 = 0, DT_F16 = 1, DT_BF16 = 2, DT_F64 = 3 };
 DevType ks_type(painty_storage s);
 DevType v_type(painty_storage s);
 DevType r_type(painty_storage s);
 void upload_planes(void* const* planes, int nch, DevType dt, int32_t rows, int32_t cols,
-                   int64_t pitch, const void* host, painty_host_format fmt, cudaStream_t st);
+                   int64_t pitch, const void* host, painty_host_format fmt, cudaStream_t st,
+                   int64_t estride = 1);
 void download_planes(const void* const* planes, int nch, DevType dt, int32_t rows,
                      int32_t cols, int64_t pitch, void* host, painty_host_format fmt,
-                     cudaStream_t st);
+                     cudaStream_t st, int64_t estride = 1);
 void fill_planes(void* const* planes, int nch, DevType dt, int64_t elems, const double* values,
-                 cudaStream_t st);
+                 cudaStream_t st, int64_t estride = 1);
+// Copies a layer's 7 planes into another of the same size and storage (any layouts).
+void copy_layer(const painty_layer& src, painty_layer& dst, cudaStream_t st);
 void copy_planes_async(void* const* dst, const void* const* src, int nch, size_t plane_bytes,
                        cudaStream_t st);
 

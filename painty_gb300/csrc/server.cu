@@ -109,8 +109,8 @@ size_t canvas_device_bytes(const painty_server* s, int32_t rows, int32_t cols) {
   const painty_storage st = s->opt.storage;
   const painty_storage rs = st == PAINTY_STORAGE_F64 ? PAINTY_STORAGE_F64 : PAINTY_STORAGE_F32;
   const size_t pe = static_cast<size_t>(rows) * pg::pitch_for(cols);
-  return pg::layer_bytes(rows, cols, st) + pg::image_bytes(rows, cols, rs) +
-         pe * pg::v_bytes(st) + pg::layer_bytes(rows, cols, st) /* snapshot */ +
+  return pg::layer_bytes(rows, cols, st, true) + pg::image_bytes(rows, cols, rs) +
+         pe * pg::v_bytes(st) + pg::layer_bytes(rows, cols, st, true) /* snapshot */ +
          (4u << 20) /* pickup map, footprint, scratch */;
 }
 
@@ -147,7 +147,8 @@ void restore(painty_server* s, ServerCanvas* c) {
     void* sb = pg::device_alloc(b->snapshot.bytes);
     PG_CUDA(cudaMemcpyAsync(sb, c->save_snapshot.p, b->snapshot.bytes, cudaMemcpyHostToDevice,
                             s->stream));
-    pg::layer_layout(b->snapshot, b->snapshot.rows, b->snapshot.cols, b->snapshot.storage, sb);
+    pg::layer_layout(b->snapshot, b->snapshot.rows, b->snapshot.cols, b->snapshot.storage, sb,
+                     true);
   }
   PG_CUDA(cudaStreamSynchronize(s->stream));
   c->resident = true;

@@ -40,7 +40,9 @@
 #include <climits>
 #include <cmath>
 #include <cstring>
+#include <cstdlib>
 #include <map>
+#include <queue>
 #include <type_traits>
 #include <mutex>
 #include <string>
@@ -88,6 +90,9 @@ struct StampArgs {
   TK* sK[3];  // pickup source: snapshot planes, or the canvas planes without a snapshot
   TK* sS[3];
   TV* sV;
+  // Packed layers (the PK kernels): pixel records of the canvas and of the pickup source
+  void* crec;
+  void* srec;
   M* pK[3];  // pickup map in global memory, S*S per plane (the brush's state)
   M* pS[3];
   M* pV;
@@ -123,7 +128,8 @@ struct StampArgs {
   unsigned* status;
 };
 
-constexpr int kParamChunk = 32;  // stamps whose parameters are derived together
+constexpr int kParamChunk = 32;               // stamps whose parameters are derived together
+constexpr int kParamRing = 2 * kParamChunk;   // parameter slots: the current and the next chunk
 
 struct StampParams {
   double cx, cy, c, s;
@@ -174,12 +180,48 @@ __device__ __forceinline__ M* pickup_plane(const StampArgs<TK, TV>& a, int p) {
   return p < 3 ? a.pK[p] : (p < 6 ? a.pS[p - 3] : a.pV);
 }
 
+// The record of one pixel of a packed layer: 8 elements of the storage size (K r,g,b, S r,g,b,
+// V, pad) read and written as 16-byte words.
+template <class TK, class TV>
+union PixRec {
+  static constexpr int kWords = 8 * sizeof(TK) / 16;
+  uint4 w[kWords];
+  TK k[8];
+  TV v[8];
+};
+template <bool CG, class TK, class TV>
+__device__ __forceinline__ PixRec<TK, TV> load_rec(const void* base, int c) {
+  using R = PixRec<TK, TV>;
+  const uint4* p = static_cast<const uint4*>(base) + static_cast<int64_t>(c) * R::kWords;
+  R r;
+#pragma unroll
+  for (int i = 0; i < R::kWords; i++) {
+    if constexpr (CG) r.w[i] = __ldcg(p + i);
+    else r.w[i] = p[i];
+  }
+  return r;
+}
+template <class TK, class TV>
+__device__ __forceinline__ void store_rec(void* base, int c, const PixRec<TK, TV>& r) {
+  using R = PixRec<TK, TV>;
+  uint4* p = static_cast<uint4*>(base) + static_cast<int64_t>(c) * R::kWords;
+#pragma unroll
+  for (int i = 0; i < R::kWords; i++) p[i] = r.w[i];
+}
+template <class TK, class TV>
+__device__ __forceinline__ TV* rec_v(void* base, int c) {
+  return reinterpret_cast<TV*>(static_cast<char*>(base) + static_cast<int64_t>(c) * 8 * sizeof(TK)) + 6;
+}
+
 // pickupPaint then depositPaint for one stamp pixel (FootprintBrush.hxx:349-431); fp > 0.
-// PS: the pickup map is staged in shared memory at `pbase` (7 planes `cells` apart).
-// Triples are handled as K r,g,b then S r,g,b.
-template <bool PS, class TK, class TV, class M>
+// PS: the pickup map is staged in shared memory at `pbase` (7 planes `cells` apart). CG:
+// global loads from L2 only (other CTAs of a cluster write the same planes). snap: the next
+// stamp's ring refresh of this pixel, done here -- the snapshot receives the values just stored.
+// PK: packed layers (pixel records); otherwise planar planes. Triples are handled as K r,g,b
+// then S r,g,b.
+template <bool PS, bool CG, bool PK, class TK, class TV, class M>
 __device__ __forceinline__ void process_pixel(const StampArgs<TK, TV>& a, M* pbase, int cells,
-                                              M fp, int c, int m, uint32_t seed) {
+                                              M fp, int c, int m, uint32_t seed, bool snap) {
   using A = Arith<M>;
   // 16-bit storage rounds its stores stochastically (bits from the canvas's stamp count and
   // the pixel; independent of how stamps are grouped into launches)
@@ -195,33 +237,60 @@ __device__ __forceinline__ void process_pixel(const StampArgs<TK, TV>& a, M* pba
     if constexpr (PS) return pbase[p * cells + m];
     else return pickup_plane<TK, TV, M>(a, p)[m];
   };
-  // every load first (one round trip): pickup cell, canvas pixel, snapshot pixel
-  M vp = cell(6);
+  // every load first (one round trip): pickup cell, canvas pixel, snapshot pixel; global
+  // loads from L2 (another CTA of a cluster may have written them)
+  auto pick = [&](int p) -> M {
+    if constexpr (PS) return pbase[p * cells + m];
+    else return ld_sel<CG, M>(pickup_plane<TK, TV, M>(a, p) + m);
+  };
+  M vp = pick(6);
   M pk[6], cn[6], sn[6];
+  M vsrc, vcan;
 #pragma unroll
-  for (int i = 0; i < 3; i++) {
-    pk[i] = cell(i);
-    pk[3 + i] = cell(3 + i);
-    cn[i] = ld_elem<M>(a.cK[i] + c);
-    cn[3 + i] = ld_elem<M>(a.cS[i] + c);
-  }
-  const M vsrc = ld_elem<M>(a.sV + c);
-  M vcan = ld_elem<M>(a.cV + c);
-  if (a.use_snapshot) {
+  for (int i = 0; i < 6; i++) pk[i] = pick(i);
+  if constexpr (PK) {
+    const PixRec<TK, TV> cr = load_rec<CG, TK, TV>(a.crec, c);
+#pragma unroll
+    for (int i = 0; i < 6; i++) cn[i] = ld_elem<M>(&cr.k[i]);
+    vcan = ld_elem<M>(&cr.v[6]);
+    if (a.use_snapshot) {
+      const PixRec<TK, TV> sr = load_rec<CG, TK, TV>(a.srec, c);
+#pragma unroll
+      for (int i = 0; i < 6; i++) sn[i] = ld_elem<M>(&sr.k[i]);
+      vsrc = ld_elem<M>(&sr.v[6]);
+    } else {  // the pickup source is the canvas itself
+#pragma unroll
+      for (int i = 0; i < 6; i++) sn[i] = cn[i];
+      vsrc = vcan;
+    }
+  } else {
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-      sn[i] = ld_elem<M>(a.sK[i] + c);
-      sn[3 + i] = ld_elem<M>(a.sS[i] + c);
+      cn[i] = ld_sel<CG, M>(a.cK[i] + c);
+      cn[3 + i] = ld_sel<CG, M>(a.cS[i] + c);
     }
-  } else {  // the pickup source is the canvas itself
+    vsrc = ld_sel<CG, M>(a.sV + c);
+    vcan = ld_sel<CG, M>(a.cV + c);
+    if (a.use_snapshot) {
 #pragma unroll
-    for (int i = 0; i < 6; i++) sn[i] = cn[i];
+      for (int i = 0; i < 3; i++) {
+        sn[i] = ld_sel<CG, M>(a.sK[i] + c);
+        sn[3 + i] = ld_sel<CG, M>(a.sS[i] + c);
+      }
+    } else {  // the pickup source is the canvas itself
+#pragma unroll
+      for (int i = 0; i < 6; i++) sn[i] = cn[i];
+    }
   }
   // pickupPaint
   const M vleave = A::mul(A::mul(a.pickupRate, vsrc), fp);
   if (vleave > M(0.001)) {
-    st_elem_sr<M>(a.sV + c, A::sub(vsrc, vleave), h3 >> 16);
-    if (!a.use_snapshot) vcan = ld_elem<M>(a.cV + c);  // the stored remainder
+    const TV left = to_store_sr<TV>(A::sub(vsrc, vleave), h3 >> 16);
+    if constexpr (PK)
+      *rec_v<TK, TV>(a.srec, c) = left;
+    else
+      a.sV[c] = left;
+    if (!a.use_snapshot) vcan = ld_elem<M>(&left);  // the stored remainder
     M np[6];
     blend6(vp, pk, vleave, sn, np);
 #pragma unroll
@@ -247,12 +316,31 @@ __device__ __forceinline__ void process_pixel(const StampArgs<TK, TV>& a, M* pba
   M out[6];
   blend6(vb, src, vcan, cn, out);
   const uint32_t rb[7] = {h0, h0 >> 16, h1, h1 >> 16, h2, h2 >> 16, h3};
+  if constexpr (PK) {
+    PixRec<TK, TV> r;
 #pragma unroll
-  for (int i = 0; i < 3; i++) {
-    st_elem_sr<M>(a.cK[i] + c, out[i], rb[i]);
-    st_elem_sr<M>(a.cS[i] + c, out[3 + i], rb[3 + i]);
+    for (int i = 0; i < PixRec<TK, TV>::kWords; i++) r.w[i] = make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+    for (int i = 0; i < 6; i++) r.k[i] = to_store_sr<TK>(out[i], rb[i]);
+    r.v[6] = to_store_sr<TV>(A::add(vb, vcan), rb[6]);
+    store_rec<TK, TV>(a.crec, c, r);
+    if (snap) store_rec<TK, TV>(a.srec, c, r);
+  } else {
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      const TK k = to_store_sr<TK>(out[i], rb[i]);
+      const TK s = to_store_sr<TK>(out[3 + i], rb[3 + i]);
+      a.cK[i][c] = k;
+      a.cS[i][c] = s;
+      if (snap) {
+        a.sK[i][c] = k;
+        a.sS[i][c] = s;
+      }
+    }
+    const TV v = to_store_sr<TV>(A::add(vb, vcan), rb[6]);
+    a.cV[c] = v;
+    if (snap) a.sV[c] = v;
   }
-  st_elem_sr<M>(a.cV + c, A::add(vb, vcan), rb[6]);
 }
 
 struct PixelInfo {
@@ -342,8 +430,9 @@ __host__ __device__ constexpr size_t align_up(size_t x, size_t a) {
 }
 
 // Dynamic shared memory layout of stamp_kernel (all offsets 16-byte aligned). The per-stamp
-// arrays (canvas columns / rows of the box, edge-duplicate flags) are double-buffered: the
-// next stamp is set up while the current one is painted.
+// arrays (canvas columns / rows of the box, edge-duplicate flags) have kStampBufs buffers and
+// the cell map two: while stamp k is painted, stamp k+1 is classified and stamp k+2 set up.
+constexpr int kStampBufs = 3;
 struct StampSmem {
   size_t fp, pick, own, xs, ys, done_c, done_r, disc, cellmap, total;
 };
@@ -359,17 +448,17 @@ __host__ __device__ inline StampSmem stamp_smem_layout(int F, int S, int ndisc, 
   L.own = o;
   if (own_smem) o = align_up(o + size_t(S) * S * sizeof(int), 16);
   L.xs = o;
-  o = align_up(o + size_t(2) * F * sizeof(int), 16);
+  o = align_up(o + size_t(kStampBufs) * F * sizeof(int), 16);
   L.ys = o;
-  o = align_up(o + size_t(2) * F * sizeof(int), 16);
+  o = align_up(o + size_t(kStampBufs) * F * sizeof(int), 16);
   L.done_c = o;
-  o = align_up(o + size_t(2) * F * sizeof(uint16_t), 16);
+  o = align_up(o + size_t(kStampBufs) * F * sizeof(uint16_t), 16);
   L.done_r = o;
-  o = align_up(o + size_t(2) * F * sizeof(uint16_t), 16);
+  o = align_up(o + size_t(kStampBufs) * F * sizeof(uint16_t), 16);
   L.disc = o;
   if (ndisc > 0) o = align_up(o + size_t(ndisc) * sizeof(uint32_t), 16);
   L.cellmap = o;
-  if (ndisc > 0) o = align_up(o + size_t(F) * F * sizeof(int), 16);
+  if (ndisc > 0) o = align_up(o + size_t(2) * F * F * sizeof(int), 16);
   L.total = o;
   return L;
 }
@@ -465,14 +554,21 @@ __device__ __forceinline__ void build_refresh(const StampParams& sp, const int* 
   if (lane == 0) rl->pre[0] = 0;
 }
 
-// All threads: copy the listed ring pixels canvas -> snapshot (7 planes), four pixels per
-// thread in flight.
-template <class TK, class TV>
+// All threads of a CTA: copy its share (of `csize`) of the listed ring pixels canvas ->
+// snapshot (7 planes), two pixels per thread in flight. `skip` (may be NULL): the current
+// stamp's cell map, its box starting at canvas (x0, y0); pixels it paints (cell >= 0) are
+// copied by their painter instead, and the rest of the list is not touched by the stamp, so
+// the copy runs beside its painting.
+template <bool CG, bool PK, class TK, class TV>
 __device__ __forceinline__ void refresh_ring(const StampArgs<TK, TV>& a, const RefreshList& rl,
-                                             int tid, int T) {
-  const int total = rl.pre[kRefreshRects];
+                                             int tid, int T, int crank, int csize,
+                                             const int* skip, int x0, int y0) {
+  const int all = rl.pre[kRefreshRects];
+  const int first = static_cast<int>(static_cast<int64_t>(all) * crank / csize);
+  const int total = static_cast<int>(static_cast<int64_t>(all) * (crank + 1) / csize);
+  const int F = a.F;
   constexpr int U = 2;
-  for (int base = 0; base < total; base += U * T) {
+  for (int base = first; base < total; base += U * T) {
     int64_t off[U];
 #pragma unroll
     for (int u = 0; u < U; u++) {
@@ -486,8 +582,24 @@ __device__ __forceinline__ void refresh_ring(const StampArgs<TK, TV>& a, const R
         const int w = R.z - R.x + 1;
         const int local = idx - rl.pre[r];
         const int dy = local / w;
-        off[u] = static_cast<int64_t>(R.y + dy) * a.pitch + (R.x + local - dy * w);
+        const int y = R.y + dy, x = R.x + local - dy * w;
+        bool take = true;
+        if (skip) {
+          const int bx = x - x0, by = y - y0;
+          take = !(bx >= 0 && by >= 0 && bx < F && by < F && skip[by * F + bx] >= 0);
+        }
+        if (take) off[u] = static_cast<int64_t>(y) * a.pitch + x;
       }
+    }
+    if constexpr (PK) {  // whole pixel records
+      PixRec<TK, TV> r[U];
+#pragma unroll
+      for (int u = 0; u < U; u++)
+        if (off[u] >= 0) r[u] = load_rec<CG, TK, TV>(a.crec, static_cast<int>(off[u]));
+#pragma unroll
+      for (int u = 0; u < U; u++)
+        if (off[u] >= 0) store_rec<TK, TV>(a.srec, static_cast<int>(off[u]), r[u]);
+      continue;
     }
     TK k[U][3], s[U][3];
     TV v[U];
@@ -496,10 +608,18 @@ __device__ __forceinline__ void refresh_ring(const StampArgs<TK, TV>& a, const R
       if (off[u] < 0) continue;
 #pragma unroll
       for (int ch = 0; ch < 3; ch++) {
-        k[u][ch] = a.cK[ch][off[u]];
-        s[u][ch] = a.cS[ch][off[u]];
+        if constexpr (CG) {
+          k[u][ch] = __ldcg(a.cK[ch] + off[u]);
+          s[u][ch] = __ldcg(a.cS[ch] + off[u]);
+        } else {
+          k[u][ch] = a.cK[ch][off[u]];
+          s[u][ch] = a.cS[ch][off[u]];
+        }
       }
-      v[u] = a.cV[off[u]];
+      if constexpr (CG)
+        v[u] = __ldcg(a.cV + off[u]);
+      else
+        v[u] = a.cV[off[u]];
     }
 #pragma unroll
     for (int u = 0; u < U; u++) {
@@ -549,15 +669,28 @@ __device__ __forceinline__ void classify_disc(const StampArgs<TK, TV>& a, const 
   }
 }
 
-// Pass 2: first pixels paint their cell's pixels.
-template <bool PS, class TK, class TV, class M>
+// Pass 2: first pixels paint their cell's pixels (this CTA's share of the disc). `nxt`: the
+// next stamp's parameters, or NULL for the last stamp -- painted pixels inside the next ring
+// are refreshed into the snapshot as they are written (the next refresh would copy exactly
+// these values).
+template <bool PS, bool CG, bool PK, class TK, class TV, class M>
 __device__ __forceinline__ void paint_disc(const StampArgs<TK, TV>& a, const int* xs, const int* ys,
                                         const M* fps, M* pbase, const uint32_t* disc, int ndisc,
-                                        const int* cellmap, uint32_t seed, int tid, int T) {
+                                        const int* cellmap, uint32_t seed, int tid, int T,
+                                        int crank, int csize, const StampParams* nxt) {
   const int F = a.F, S = a.S;
   const int cells = S * S;
   const int pitch32 = static_cast<int>(a.pitch);  // planes hold fewer than 2^31 elements
-  for (int i = tid; i < ndisc; i += T) {
+  const int first = ndisc * crank / csize, last = ndisc * (crank + 1) / csize;
+  const bool snapping = nxt != nullptr && a.use_snapshot;
+  // canvas pixel (x, y) lies in the next stamp's ring: its grown box minus the box's interior
+  auto in_ring = [&](int x, int y) -> bool {
+    if (!snapping) return false;
+    const bool g = x >= nxt->tla[0] && x <= nxt->bra[0] && y >= nxt->tla[1] && y <= nxt->bra[1];
+    const bool i = x > nxt->tl[0] && x < nxt->br[0] && y > nxt->tl[1] && y < nxt->br[1];
+    return g && !i;
+  };
+  for (int i = first + tid; i < last; i += T) {
     const uint32_t e = disc[i];
     const int row = static_cast<int>(e >> 16), col = static_cast<int>(e & 0xffffu);
     const int* cm = cellmap + row * F + col;
@@ -576,12 +709,14 @@ __device__ __forceinline__ void paint_disc(const StampArgs<TK, TV>& a, const int
     const int mx = m & 0xffff, my = m >> 16;
     const M fp = fps[my * F + mx];
     const int cell = my * S + mx;
-    process_pixel<PS, TK, TV, M>(a, pbase, cells, fp, ys[row] * pitch32 + xs[col], cell, seed);
+    process_pixel<PS, CG, PK, TK, TV, M>(a, pbase, cells, fp, ys[row] * pitch32 + xs[col], cell,
+                                         seed, in_ring(xs[col], ys[row]));
     for (; follow; follow &= follow - 1) {
       const int q = __ffs(follow) - 1;
       const int rr = row + (q == 0 ? 0 : 1);
       const int cc = col + (q == 0 ? 1 : q - 2);
-      process_pixel<PS, TK, TV, M>(a, pbase, cells, fp, ys[rr] * pitch32 + xs[cc], cell, seed);
+      process_pixel<PS, CG, PK, TK, TV, M>(a, pbase, cells, fp, ys[rr] * pitch32 + xs[cc],
+                                           cell, seed, in_ring(xs[cc], ys[rr]));
     }
   }
 }
@@ -591,7 +726,7 @@ __device__ __forceinline__ void paint_disc(const StampArgs<TK, TV>& a, const int
 // remaining index and their earlier duplicates (done_c / done_r) finished. Called by the
 // whole CTA; returns the next epoch. Out of line: rare, and it keeps the cell path's
 // registers free.
-template <bool PS, class TK, class TV, class M>
+template <bool PS, bool CG, bool PK, class TK, class TV, class M>
 __device__ __noinline__ int paint_waves(const StampArgs<TK, TV>& a, const StampParams& sp,
                                         const int* xs, const int* ys, uint16_t* done_c,
                                         uint16_t* done_r, const M* fps, M* pbase, int* own,
@@ -601,6 +736,11 @@ __device__ __noinline__ int paint_waves(const StampArgs<TK, TV>& a, const StampP
   const int F = a.F, S = a.S;
   const int cells = S * S;
   const int NC = (F + 31) / 32;
+  if (epoch > kEpochMax - 2 * kMaxWaves) {  // owner keys about to wrap: reset the table
+    for (int i = tid; i < cells; i += blockDim.x) own[i] = INT_MAX;
+    epoch = 0;
+    __syncthreads();
+  }
   uint64_t rem = 0;
   int wave = 1;
   int key_hi = (kEpochMax - epoch) << 16;
@@ -633,9 +773,9 @@ __device__ __noinline__ int paint_waves(const StampArgs<TK, TV>& a, const StampP
       const PixelInfo p = pixel_info(a, sp, xs, ys, fps, row, col, &fp);
       if (own[p.my * S + p.mx] == (key_hi | (row * F + col)) &&
           canvas_ready(xs, ys, F, done_c, done_r, row, col, wave)) {
-        process_pixel<PS, TK, TV, M>(a, pbase, cells, fp,
-                                     p.yc * static_cast<int>(a.pitch) + p.xc, p.my * S + p.mx,
-                                     seed);
+        process_pixel<PS, CG, PK, TK, TV, M>(a, pbase, cells, fp,
+                                             p.yc * static_cast<int>(a.pitch) + p.xc,
+                                             p.my * S + p.mx, seed, false);
         rem &= ~(1ull << j);
         mark_done(xs, ys, F, done_c, done_r, row, col, static_cast<uint16_t>(wave + 1));
       }
@@ -661,16 +801,13 @@ __device__ __noinline__ int paint_waves(const StampArgs<TK, TV>& a, const StampP
   return epoch;
 }
 
-// Per-stamp setup of stamp k into buffer `buf`: canvas columns / rows of the box (double, as
-// the reference), duplicate flags reset, the ring rectangles (warp 0). Returns whether this
-// thread saw an edge duplicate.
+// Per-stamp setup of a stamp: canvas columns / rows of the box (double, as the reference),
+// duplicate flags reset, the ring rectangles (warp 0) given the previous stamp's box and
+// grown box `prev`. Returns whether this thread saw an edge duplicate.
 template <class TK, class TV>
-__device__ __forceinline__ int setup_stamp(const StampArgs<TK, TV>& a, const StampParams* sparams,
-                                           int64_t k, int* xs, int* ys, uint16_t* done_c,
-                                           uint16_t* done_r, StampShared* sh, RefreshList* rl,
-                                           int tid, int T) {
-  const int slot = static_cast<int>(k % kParamChunk);
-  const StampParams& sp = sparams[slot];
+__device__ __forceinline__ int setup_stamp(const StampArgs<TK, TV>& a, const StampParams& sp,
+                                           const int* prev, int* xs, int* ys, uint16_t* done_c,
+                                           uint16_t* done_r, RefreshList* rl, int tid, int T) {
   const int F = a.F;
   int dup = 0;
   for (int i = tid; i < F; i += T) {
@@ -686,24 +823,20 @@ __device__ __forceinline__ int setup_stamp(const StampArgs<TK, TV>& a, const Sta
       dup |= (x == x1) | (y == y1);
     }
   }
-  if (a.use_snapshot && (tid >> 5) == 0) {
-    int prev[8];
-    if (slot > 0)
-      stamp_rects(sparams[slot - 1], prev);
-    else
-      for (int i = 0; i < 8; i++) prev[i] = sh->prev[i];
-    build_refresh(sp, prev, tid & 31, rl);
-  }
+  if (a.use_snapshot && (tid >> 5) == 0) build_refresh(sp, prev, tid & 31, rl);
   return dup;
 }
 
-// One stroke's stamps applied in order by the whole CTA (the kernel body shared by the
-// single-canvas and the batched kernels). `a` may live in shared or parameter memory.
-// Per stamp: ring refresh | paint | (next stamp's setup alongside) -- two barriers. Stamps
-// with edge duplicates paint in waves instead: pixels bid for their cells (atomicMin on
-// epoch-tagged row-major indices) and run when they hold their cell's lowest remaining index
-// and their earlier duplicates are done.
-template <bool PS, bool BIG, class TK, class TV, class Src>
+// One stroke's stamps applied in order by the whole CTA -- or by a cluster of CTAs, each
+// painting and refreshing its share (the pickup map is then in global memory: PS false, CG
+// true). The kernel body shared by the single-canvas and the batched kernels; `a` may live in
+// shared or parameter memory.
+//
+// One barrier per stamp. Phase k paints stamp k (by cells, or in waves when it has edge
+// duplicates), refreshes stamp k+1's ring beside it (the pixels stamp k paints are refreshed
+// by their painter), classifies stamp k+1's support disc and sets up stamp k+2. After a wave-
+// painted stamp the next ring is refreshed in a phase of its own.
+template <bool PS, bool BIG, bool CG, bool PK, class TK, class TV, class Src>
 __device__ __forceinline__ void run_stroke(const StampArgs<TK, TV>& a, const Src& src,
                                            unsigned char* smem_raw, StampParams* sparams,
                                            StampShared* sh) {
@@ -725,36 +858,70 @@ __device__ __forceinline__ void run_stroke(const StampArgs<TK, TV>& a, const Src
   uint16_t* dc_b = reinterpret_cast<uint16_t*>(smem_raw + L.done_c);
   uint16_t* dr_b = reinterpret_cast<uint16_t*>(smem_raw + L.done_r);
   uint32_t* disc = reinterpret_cast<uint32_t*>(smem_raw + L.disc);
-  int* cellmap = reinterpret_cast<int*>(smem_raw + L.cellmap);
+  int* cm_b = reinterpret_cast<int*>(smem_raw + L.cellmap);
   const int ndisc = a.ndisc;
+  const int crank = static_cast<int>(cluster_rank()), csize = static_cast<int>(cluster_size());
+  auto csync = [csize]() {
+    if (csize > 1)
+      cluster_barrier();
+    else
+      __syncthreads();
+  };
+  if (tid == 0 && (PS || !CG) && csize > 1) atomicOr(a.status, kStatusWaveCap);  // host bug
+  auto par = [&](int64_t k) -> StampParams& { return sparams[static_cast<int>(k % kParamRing)]; };
+  auto xs_of = [&](int64_t k) { return xs_b + static_cast<int>(k % kStampBufs) * F; };
+  auto ys_of = [&](int64_t k) { return ys_b + static_cast<int>(k % kStampBufs) * F; };
+  auto dc_of = [&](int64_t k) { return dc_b + static_cast<int>(k % kStampBufs) * F; };
+  auto dr_of = [&](int64_t k) { return dr_b + static_cast<int>(k % kStampBufs) * F; };
+  auto cm_of = [&](int64_t k) { return cm_b + static_cast<int>(k & 1) * npix; };
+  auto rl_of = [&](int64_t k) { return &sh->rl[k & 1]; };
+  // rectangles of stamp k - 1 (the brush's ring state before the first stamp)
+  auto prev_of = [&](int64_t k, int* out) {
+    if (k == 0)
+      for (int i = 0; i < 8; i++) out[i] = sh->prev[i];
+    else
+      stamp_rects(par(k - 1), out);
+  };
+  auto derive_chunk = [&](int64_t k0) {  // parameters of stamps k0 .. k0 + 31 (threads < 32)
+    const int64_t j = k0 + tid;
+    if (tid < kParamChunk && j < nstamps)
+      par(j) = derive_params(src.get(j), a.wr, a.radius, a.rows, a.cols);
+  };
+  auto setup = [&](int64_t k) -> int {
+    int prev[8];
+    prev_of(k, prev);
+    return setup_stamp(a, par(k), prev, xs_of(k), ys_of(k), dc_of(k), dr_of(k), rl_of(k), tid,
+                       T);
+  };
 
   // launch prologue: footprint and pickup map staged, owner table reset, ring state
   if (!BIG) {
     M* f = reinterpret_cast<M*>(smem_raw + L.fp);
     for (int i = tid; i < npix; i += T) f[i] = a.footprint[i];
   }
-  for (int i = tid; i < 7 * cells; i += T) {
+  for (int i = tid + crank * T; i < 7 * cells; i += T * csize) {
     const int p = i / cells, m = i - p * cells;
     if (PS)
       pbase[i] = a.pickup_zero ? M(0) : pickup_plane<TK, TV, M>(a, p)[m];
     else if (a.pickup_zero)
       pickup_plane<TK, TV, M>(a, p)[m] = M(0);
   }
-  for (int i = tid; i < cells; i += T) own[i] = INT_MAX;
+  if (!BIG || crank == 0)
+    for (int i = tid; i < cells; i += T) own[i] = INT_MAX;
   if (tid == 0) {  // the stamp before the first: from the brush's ring state or the reset mode
     const int big = 1 << 30;
     const int unknown[8] = {0, 0, -1, -1, 0, 0, -1, -1};
     const int clean[8] = {0, 0, -1, -1, -big, -big, big, big};
     for (int i = 0; i < 8; i++)
-      sh->prev[i] = (a.ring_reset == kRingKeep && a.ring) ? a.ring[i]
+      sh->prev[i] = (a.ring_reset == kRingKeep && a.ring) ? __ldcg(a.ring + i)
                     : a.ring_reset == kRingClean          ? clean[i]
                                                           : unknown[i];
-    sh->seed0 = a.stamp_count ? *a.stamp_count : 0u;
+    sh->seed0 = a.stamp_count ? __ldcg(a.stamp_count) : 0u;
   }
-  // support-disc pixels, row-major (warp 0: per-row column intervals, prefix sums), and a
-  // cell map whose pixels outside the disc read as "changes nothing"
+  // support-disc pixels, row-major (warp 0: per-row column intervals, prefix sums), and cell
+  // maps whose pixels outside the disc read as "changes nothing"
   if (ndisc > 0) {
-    for (int i = tid; i < F * F; i += T) cellmap[i] = -1;
+    for (int i = tid; i < 2 * npix; i += T) cm_b[i] = -1;
     if (warp_id() == 0) {
       int base = 0;
       for (int r0 = 0; r0 < F; r0 += 32) {
@@ -785,62 +952,56 @@ __device__ __forceinline__ void run_stroke(const StampArgs<TK, TV>& a, const Src
       if (lane == 0 && base != ndisc) atomicOr(a.status, kStatusWaveCap);
     }
   }
-  // parameters of the first chunk, setup of the first stamp
-  if (tid < kParamChunk && tid < nstamps)
-    sparams[tid] = derive_params(src.get(tid), a.wr, a.radius, a.rows, a.cols);
-  __syncthreads();
+  derive_chunk(0);
+  csync();  // parameters, disc list; a cleared pickup map is visible to the whole cluster
+  // stamps 0 and 1 set up, stamp 0's ring refreshed and its disc classified
+  int dup0 = 0, dup1 = 0;
+  if (nstamps > 0) dup0 = __syncthreads_or(setup(0));
+  if (nstamps > 1) dup1 = __syncthreads_or(setup(1));
+  if (nstamps > 0) {
+    if (a.use_snapshot)
+      refresh_ring<CG, PK>(a, *rl_of(0), tid, T, crank, csize, nullptr, 0, 0);
+    if (!dup0 && ndisc > 0)
+      classify_disc(a, par(0), xs_of(0), ys_of(0), fps, disc, ndisc, cm_of(0), tid, T);
+  }
+  csync();
   int epoch = 0;
-  int dup = 0;
-  if (nstamps > 0)
-    dup = setup_stamp(a, sparams, 0, xs_b, ys_b, dc_b, dr_b, sh, &sh->rl[0], tid, T);
-  dup = __syncthreads_or(dup);
-
   for (int64_t k = 0; k < nstamps; k++) {
-    const int slot = static_cast<int>(k % kParamChunk);
-    const int buf = static_cast<int>(k & 1);
-    const StampParams& sp = sparams[slot];
-    const int* xs = xs_b + buf * F;
-    const int* ys = ys_b + buf * F;
-    uint16_t* done_c = dc_b + buf * F;
-    uint16_t* done_r = dr_b + buf * F;
-    // ring refresh and the cell map, then painting (in waves with edge duplicates)
-    const bool by_cells = !dup && ndisc > 0;
-    if (a.use_snapshot) refresh_ring(a, sh->rl[buf], tid, T);
-    if (by_cells) classify_disc(a, sp, xs, ys, fps, disc, ndisc, cellmap, tid, T);
-    __syncthreads();
+    const StampParams& sp = par(k);
+    const bool has_next = k + 1 < nstamps;
     const uint32_t seed = hash32(sh->seed0 + static_cast<uint32_t>(k));
-    if (by_cells)
-      paint_disc<PS, TK, TV, M>(a, xs, ys, fps, pbase, disc, ndisc, cellmap, seed, tid, T);
-    else
-      epoch = paint_waves<PS, TK, TV, M>(a, sp, xs, ys, done_c, done_r, fps, pbase, own, epoch,
-                                         seed);
-    // the next stamp's setup (into the other buffer), alongside painting
-    int nd = 0;
-    if (k + 1 < nstamps) {
-      if ((k + 1) % kParamChunk == 0) {  // derive the next chunk of stamp parameters
-        if (tid == 0) stamp_rects(sparams[kParamChunk - 1], sh->prev);
-        __syncthreads();
-        const int64_t j = k + 1 + tid;
-        if (tid < kParamChunk && j < nstamps)
-          sparams[tid] = derive_params(src.get(j), a.wr, a.radius, a.rows, a.cols);
-        if (epoch > kEpochMax - 2 * kMaxWaves) {  // owner keys about to wrap: reset
-          for (int i = tid; i < cells; i += T) own[i] = INT_MAX;
-          epoch = 0;
-        }
-        __syncthreads();
-      }
-      const int nb = buf ^ 1;
-      nd = setup_stamp(a, sparams, k + 1, xs_b + nb * F, ys_b + nb * F, dc_b + nb * F,
-                       dr_b + nb * F, sh, &sh->rl[nb], tid, T);
+    if (!dup0 && ndisc > 0) {
+      paint_disc<PS, CG, PK, TK, TV, M>(a, xs_of(k), ys_of(k), fps, pbase, disc, ndisc, cm_of(k),
+                                        seed, tid, T, crank, csize,
+                                        has_next ? &par(k + 1) : nullptr);
+      if (has_next && a.use_snapshot)
+        refresh_ring<CG, PK>(a, *rl_of(k + 1), tid, T, crank, csize, cm_of(k), xs_of(k)[0],
+                             ys_of(k)[0]);
+    } else {
+      if (crank == 0)  // edge duplicates: the first CTA alone, in waves
+        epoch = paint_waves<PS, CG, PK, TK, TV, M>(a, sp, xs_of(k), ys_of(k), dc_of(k), dr_of(k),
+                                                   fps, pbase, own, epoch, seed);
+      csync();
+      if (has_next && a.use_snapshot)
+        refresh_ring<CG, PK>(a, *rl_of(k + 1), tid, T, crank, csize, nullptr, 0, 0);
     }
-    dup = __syncthreads_or(nd);
+    if (has_next && !dup1 && ndisc > 0)
+      classify_disc(a, par(k + 1), xs_of(k + 1), ys_of(k + 1), fps, disc, ndisc, cm_of(k + 1),
+                    tid, T);
+    if ((k + 3) % kParamChunk == 0) derive_chunk(k + 3);  // read from phase k + 1 on
+    int nd = 0;
+    if (k + 2 < nstamps) nd = setup(k + 2);
+    nd = __syncthreads_or(nd);
+    if (csize > 1) cluster_barrier();  // this phase's writes before the next phase's reads
+    dup0 = dup1;
+    dup1 = nd;
   }
   // epilogue: the brush keeps its pickup map and the ring state
-  __syncthreads();
-  if (tid == 0 && a.stamp_count) *a.stamp_count = sh->seed0 + static_cast<unsigned>(nstamps);
-  if (tid == 0 && a.ring && a.use_snapshot) {
+  if (tid == 0 && crank == 0 && a.stamp_count)
+    *a.stamp_count = sh->seed0 + static_cast<unsigned>(nstamps);
+  if (tid == 0 && crank == 0 && a.ring && a.use_snapshot) {
     if (nstamps > 0)
-      stamp_rects(sparams[static_cast<int>((nstamps - 1) % kParamChunk)], a.ring);
+      stamp_rects(par(nstamps - 1), a.ring);
     else
       for (int i = 0; i < 8; i++) a.ring[i] = sh->prev[i];
   }
@@ -849,18 +1010,19 @@ __device__ __forceinline__ void run_stroke(const StampArgs<TK, TV>& a, const Src
       const int p = i / cells, m = i - p * cells;
       pickup_plane<TK, TV, M>(a, p)[m] = pbase[i];
     }
-    __syncthreads();
   }
+  csync();  // the ring state and pickup map are written before any CTA reads them again
 }
 
 // PS: pickup map staged in shared memory. BIG: footprint and owner table in global memory
-// (maps too large for shared memory); otherwise both are in shared memory.
-template <bool PS, bool BIG, class TK, class TV>
+// (maps too large for shared memory); otherwise both are in shared memory. CG: a cluster
+// launch (global loads from L2).
+template <bool PS, bool BIG, bool CG, bool PK, class TK, class TV>
 __global__ void __launch_bounds__(kStampThreads, 1) stamp_kernel(const __grid_constant__ StampArgs<TK, TV> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ StampParams sparams[kParamChunk];
+  __shared__ StampParams sparams[kParamRing];
   __shared__ StampShared sh;
-  run_stroke<PS, BIG>(a, RecordSource{a.stamps, a.n}, smem_raw, sparams, &sh);
+  run_stroke<PS, BIG, CG, PK>(a, RecordSource{a.stamps, a.n}, smem_raw, sparams, &sh);
 }
 
 // ---------------------------------------------------------------------- batched painting
@@ -931,6 +1093,8 @@ struct BatchCanvas {
   TK* sK[3];
   TK* sS[3];
   TV* sV;
+  void* crec;          // packed canvas and pickup-source records
+  void* srec;
   int* ring;           // the brush's snapshot-ring state
   unsigned* stamp_count;
   int32_t ring_reset;  // for the canvas's first stroke with stamps
@@ -964,8 +1128,9 @@ struct BatchArgs {
   const int32_t* order;  // canvases, heaviest first
   int32_t ncanvas;
   int* counter;
-  M* scratch_pickup;  // per CTA: 7 planes of Smax^2
-  int* scratch_owner; // per CTA: Smax^2
+  int* claims;        // per cluster: the canvas it claimed last
+  M* scratch_pickup;  // per cluster: 7 planes of Smax^2
+  int* scratch_owner; // per cluster: Smax^2
   int64_t pickup_stride, owner_stride;
   unsigned* status;
 };
@@ -976,19 +1141,27 @@ template <class TK, class TV>
 __global__ void __launch_bounds__(kStampThreads, 1) batch_kernel(const __grid_constant__ BatchArgs<TK, TV> b) {
   using M = typename MathOf<TK>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ StampParams sparams[kParamChunk];
+  __shared__ StampParams sparams[kParamRing];
   __shared__ StampShared sh;
   __shared__ StampArgs<TK, TV> sa;
   __shared__ int s_item;
   __shared__ int64_t seg_end[kMaxPathPoints];
   const int tid = threadIdx.x, T = blockDim.x;
+  // a cluster (or a lone CTA) paints one canvas at a time; its first CTA claims the canvas
+  const int crank = static_cast<int>(cluster_rank()), csize = static_cast<int>(cluster_size());
+  const int cid = static_cast<int>(blockIdx.x) / csize;
   for (;;) {
     __syncthreads();
-    if (tid == 0) {
+    if (tid == 0 && crank == 0) {
       const int i = atomicAdd(b.counter, 1);
-      s_item = i < b.ncanvas ? b.order[i] : -1;
+      b.claims[cid] = i < b.ncanvas ? b.order[i] : -1;
     }
-    __syncthreads();
+    if (csize > 1) cluster_barrier();
+    if (tid == 0) s_item = __ldcg(b.claims + cid);
+    if (csize > 1)
+      cluster_barrier();  // every CTA has the claim before the next one overwrites it
+    else
+      __syncthreads();
     const int ci = s_item;
     if (ci < 0) return;
     const BatchCanvas<TK, TV>& cv = b.canvases[ci];
@@ -1001,7 +1174,7 @@ __global__ void __launch_bounds__(kStampThreads, 1) batch_kernel(const __grid_co
         const bool last = k + 1 == cv.nstrokes;
         const int64_t cells = static_cast<int64_t>(st.S) * st.S;
         M* pk = last ? static_cast<M*>(cv.brush_pickup)
-                     : b.scratch_pickup + static_cast<int64_t>(blockIdx.x) * b.pickup_stride;
+                     : b.scratch_pickup + static_cast<int64_t>(cid) * b.pickup_stride;
         for (int i = 0; i < 3; i++) {
           sa.cK[i] = cv.cK[i];
           sa.cS[i] = cv.cS[i];
@@ -1014,6 +1187,8 @@ __global__ void __launch_bounds__(kStampThreads, 1) batch_kernel(const __grid_co
         }
         sa.cV = cv.cV;
         sa.sV = cv.sV;
+        sa.crec = cv.crec;
+        sa.srec = cv.srec;
         sa.pV = pk + 6 * cells;
         sa.footprint = b.footprints + st.fp_offset;
         sa.stamps = nullptr;
@@ -1038,7 +1213,7 @@ __global__ void __launch_bounds__(kStampThreads, 1) batch_kernel(const __grid_co
         sa.pickup_smem = st.plan & 1;
         sa.footprint_smem = (st.plan & 2) ? 0 : 1;
         sa.owner_global = (st.plan & 2)
-                            ? b.scratch_owner + static_cast<int64_t>(blockIdx.x) * b.owner_stride
+                            ? b.scratch_owner + static_cast<int64_t>(cid) * b.owner_stride
                             : nullptr;
         sa.status = b.status;
       }
@@ -1055,18 +1230,25 @@ __global__ void __launch_bounds__(kStampThreads, 1) batch_kernel(const __grid_co
       __syncthreads();
       const int64_t n = nseg > 0 ? seg_end[nseg - 1] : 0;
       if (n == 0) {  // no stamps: a last stroke still leaves the brush a clean pickup map
-        if (k + 1 == cv.nstrokes) {
+        if (k + 1 == cv.nstrokes && crank == 0) {
           const int64_t pc = static_cast<int64_t>(7) * st.S * st.S;
           for (int64_t i = tid; i < pc; i += T) static_cast<M*>(cv.brush_pickup)[i] = M(0);
         }
         continue;
       }
       const PathSource src{pts, st.npoints, st.spacing, seg_end, n};
-      switch (st.plan) {
-        case 0: run_stroke<false, false>(sa, src, smem_raw, sparams, &sh); break;
-        case 1: run_stroke<true, false>(sa, src, smem_raw, sparams, &sh); break;
-        case 2: run_stroke<false, true>(sa, src, smem_raw, sparams, &sh); break;
-        default: run_stroke<true, true>(sa, src, smem_raw, sparams, &sh); break;
+      if (csize > 1) {  // clusters: the pickup map in global memory, loads from L2
+        if (st.plan & 2)
+          run_stroke<false, true, true, true>(sa, src, smem_raw, sparams, &sh);
+        else
+          run_stroke<false, false, true, true>(sa, src, smem_raw, sparams, &sh);
+      } else {
+        switch (st.plan) {
+          case 0: run_stroke<false, false, false, true>(sa, src, smem_raw, sparams, &sh); break;
+          case 1: run_stroke<true, false, false, true>(sa, src, smem_raw, sparams, &sh); break;
+          case 2: run_stroke<false, true, false, true>(sa, src, smem_raw, sparams, &sh); break;
+          default: run_stroke<true, true, false, true>(sa, src, smem_raw, sparams, &sh); break;
+        }
       }
       ran = true;
     }
@@ -1181,12 +1363,14 @@ struct SmemPlan {
   StampSmem layout;
 };
 template <class M>
-SmemPlan plan_smem_limit(int F, int S, int ndisc, size_t limit, bool allow_small = true) {
+SmemPlan plan_smem_limit(int F, int S, int ndisc, size_t limit, bool allow_small = true,
+                         bool allow_pick = true) {
   const bool cand[4][2] = {{false, true}, {false, false}, {true, true}, {true, false}};
   for (int nd : {ndisc, 0}) {
     for (const auto& c : cand) {
       const bool big = c[0], pick = c[1];
       if (!big && !allow_small) continue;
+      if (pick && !allow_pick) continue;
       const StampSmem L = stamp_smem_layout<M>(F, S, nd, !big, pick, !big);
       if (L.total <= limit) return SmemPlan{big, pick, nd, L};
     }
@@ -1196,10 +1380,64 @@ SmemPlan plan_smem_limit(int F, int S, int ndisc, size_t limit, bool allow_small
 }
 
 template <class M>
-SmemPlan plan_smem(int F, int S, int ndisc, bool allow_small) {
-  const size_t limit = static_cast<size_t>(max_dyn_smem()) - sizeof(StampParams) * kParamChunk -
+SmemPlan plan_smem(int F, int S, int ndisc, bool allow_small, bool allow_pick = true) {
+  const size_t limit = static_cast<size_t>(max_dyn_smem()) - sizeof(StampParams) * kParamRing -
                        sizeof(StampShared) - 512;
-  return plan_smem_limit<M>(F, S, ndisc, limit, allow_small);
+  return plan_smem_limit<M>(F, S, ndisc, limit, allow_small, allow_pick);
+}
+
+// Launch of a stamp-path kernel with `cluster` CTAs per thread-block cluster (1: a plain
+// launch).
+template <class Arg>
+void launch_clustered(void (*kern)(Arg), int grid, int cluster, size_t smem, cudaStream_t st,
+                      const Arg& arg) {
+  if (cluster <= 1) {
+    kern<<<grid, kStampThreads, smem, st>>>(arg);
+    return;
+  }
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(static_cast<unsigned>(grid));
+  cfg.blockDim = dim3(kStampThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = static_cast<unsigned>(cluster);
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  PG_CUDA(cudaLaunchKernelEx(&cfg, kern, arg));
+}
+
+// Clusters of `cluster` stamp CTAs (smem bytes each) that fit on the device at once.
+template <class Arg>
+int max_clusters(void (*kern)(Arg), int cluster, size_t smem) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(static_cast<unsigned>(cluster));
+  cfg.blockDim = dim3(kStampThreads);
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = static_cast<unsigned>(cluster);
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+// Cluster size from the environment (PAINTY_STAMP_CLUSTER / PAINTY_BATCH_CLUSTER), 0 if unset.
+int env_cluster(const char* name) {
+  const char* v = std::getenv(name);
+  if (!v || !*v) return 0;
+  const int n = std::atoi(v);
+  return (n == 1 || n == 2 || n == 4 || n == 8) ? n : 0;
 }
 
 // Box pixels (F x F, centre wr) with dc^2 + dr^2 <= support2: the kernel's support-disc list.
@@ -1226,6 +1464,8 @@ void launch_stamps(painty_canvas* c, painty_brush* b, const StampRec* d_stamps, 
   }
   a.cV = static_cast<TV*>(c->wet.V);
   a.sV = static_cast<TV*>(b->useSnapshot ? b->snapshot.V : c->wet.V);
+  a.crec = c->wet.base;
+  a.srec = b->useSnapshot ? b->snapshot.base : c->wet.base;
   const size_t cells = static_cast<size_t>(b->sizeMap) * b->sizeMap;
   M* pk = static_cast<M*>(b->d_pickup);
   for (int i = 0; i < 3; i++) {
@@ -1257,21 +1497,37 @@ void launch_stamps(painty_canvas* c, painty_brush* b, const StampRec* d_stamps, 
   a.pickup_zero = pickup_zero ? 1 : 0;
   a.status = b->d_status;
   a.support2 = b->support2;
-  const SmemPlan plan = plan_smem<M>(b->F, b->sizeMap, disc_count(b->F, b->support2), true);
+  // one canvas: a cluster of CTAs shares each stamp when the stamp is large enough to split
+  // (the pickup map is then in global memory); a lone CTA stages it in shared memory
+  const int nd = disc_count(b->F, b->support2);
+  int cl = env_cluster("PAINTY_STAMP_CLUSTER");
+  if (cl == 0) cl = nd >= 4096 ? 4 : nd >= 1536 ? 2 : 1;
+  SmemPlan plan{};
+  void (*kern)(StampArgs<TK, TV>) = nullptr;
+  for (;;) {
+    plan = plan_smem<M>(b->F, b->sizeMap, nd, true, cl == 1);
+    if (cl > 1)
+      kern = plan.big ? stamp_kernel<false, true, true, true, TK, TV>
+                      : stamp_kernel<false, false, true, true, TK, TV>;
+    else
+      kern = plan.pick ? (plan.big ? stamp_kernel<true, true, false, true, TK, TV>
+                                   : stamp_kernel<true, false, false, true, TK, TV>)
+                       : (plan.big ? stamp_kernel<false, true, false, true, TK, TV>
+                                   : stamp_kernel<false, false, false, true, TK, TV>);
+    PG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(plan.layout.total)));
+    if (cl == 1 || max_clusters(kern, cl, plan.layout.total) >= 1) break;
+    cl /= 2;
+  }
   a.ndisc = plan.ndisc;
-  const bool big = plan.big;
-  if (big) {
+  if (plan.big) {
     ensure(&b->d_owner, &b->d_owner_bytes, cells * sizeof(int));
     a.owner_global = static_cast<int*>(b->d_owner);
   }
-  a.footprint_smem = big ? 0 : 1;
+  a.footprint_smem = plan.big ? 0 : 1;
   a.pickup_smem = plan.pick ? 1 : 0;
-  auto kern = plan.pick ? (big ? stamp_kernel<true, true, TK, TV> : stamp_kernel<true, false, TK, TV>)
-                        : (big ? stamp_kernel<false, true, TK, TV> : stamp_kernel<false, false, TK, TV>);
   const StampSmem Lk = plan.layout;
-  PG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               static_cast<int>(Lk.total)));
-  kern<<<1, kStampThreads, Lk.total, st>>>(a);
+  launch_clustered(kern, cl, cl, Lk.total, st, a);
   count_launch();
   PG_CUDA(cudaGetLastError());
 }
@@ -1287,8 +1543,8 @@ int prepare_snapshot(painty_canvas* c, painty_brush* b, cudaStream_t st) {
       b->snapshot.storage != c->wet.storage) {
     if (b->has_snapshot) device_free(b->snapshot.base);
     b->has_snapshot = false;
-    void* base = device_alloc(layer_bytes(c->wet.rows, c->wet.cols, c->wet.storage));
-    layer_layout(b->snapshot, c->wet.rows, c->wet.cols, c->wet.storage, base);
+    void* base = device_alloc(layer_bytes(c->wet.rows, c->wet.cols, c->wet.storage, true));
+    layer_layout(b->snapshot, c->wet.rows, c->wet.cols, c->wet.storage, base, true);
     b->has_snapshot = true;
     PG_CUDA(cudaMemcpyAsync(b->snapshot.base, c->wet.base, c->wet.bytes,
                             cudaMemcpyDeviceToDevice, st));
@@ -1386,6 +1642,32 @@ void run_stamps(painty_canvas* c, painty_brush* b, const std::vector<StampRec>& 
 
 
 // ---------------------------------------------------------------------- batched painting (host)
+// Stamp cost model for choosing the cluster size of a batch (GB300, 1024-thread CTAs, SM
+// cycles per stamp): kStampFixed + kStampPerPixel * disc / cluster, plus kClusterSync when a
+// cluster of CTAs shares each stamp (two cluster barriers and the split's imbalance).
+constexpr double kStampFixed = 7000.0;
+constexpr double kStampPerPixel = 12.0;
+constexpr double kClusterSync = 1500.0;
+
+// Makespan of painting canvases with loads (stamps N, stamp-pixels P) on `slots` clusters of
+// `cl` CTAs, heaviest canvas first onto the least-loaded cluster (the kernel's claim order).
+double batch_makespan(const std::vector<double>& N, const std::vector<double>& P,
+                      const std::vector<int32_t>& order, int slots, int cl) {
+  if (slots < 1) return 1e300;
+  std::priority_queue<double, std::vector<double>, std::greater<double>> q;
+  for (int i = 0; i < slots; i++) q.push(0.0);
+  double span = 0.0;
+  for (int32_t c : order) {
+    const double t = N[c] * (kStampFixed + (cl > 1 ? kClusterSync : 0.0)) +
+                     kStampPerPixel * P[c] / cl;
+    const double end = q.top() + t;
+    q.pop();
+    q.push(end);
+    span = std::max(span, end);
+  }
+  return span;
+}
+
 template <class TK, class TV>
 void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushes, int32_t nc,
                      const painty_stroke_desc* strokes, int64_t ns, const double* points,
@@ -1404,7 +1686,10 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   bs.reserve(static_cast<size_t>(ns));
   std::vector<M> fptable;
   std::map<std::pair<const painty_brush*, int32_t>, int64_t> fp_off;
-  std::vector<double> work(nc, 0.0);
+  std::vector<double> work(nc, 0.0), loadN(nc, 0.0), loadP(nc, 0.0);
+  std::vector<int32_t> disc_of;  // per stroke: support-disc pixels
+  disc_of.reserve(static_cast<size_t>(ns));
+  std::map<std::pair<int32_t, int32_t>, int32_t> disc_cache;
   int32_t smax = 1;
   size_t dyn = 0;
   int64_t total_stamps = 0;
@@ -1438,15 +1723,17 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
         x.K[i] = sk.K[i];
         x.Sc[i] = sk.S[i];
       }
-      const SmemPlan plan = plan_smem_limit<M>(b->F, b->sizeMap, disc_count(b->F, b->support2), limit);
-      x.ndisc = plan.ndisc;
-      x.plan = (plan.pick ? 1 : 0) | (plan.big ? 2 : 0);
-      dyn = std::max(dyn, plan.layout.total);
+      const auto dk = std::make_pair(b->F, b->support2);
+      auto di = disc_cache.find(dk);
+      if (di == disc_cache.end()) di = disc_cache.emplace(dk, disc_count(b->F, b->support2)).first;
+      disc_of.push_back(di->second);
       smax = std::max(smax, b->sizeMap);
-      // stamp count (paintStroke's loop bounds) and a work estimate for the ordering
+      // stamp count (paintStroke's loop bounds) and the load estimates
       const int64_t n = stroke_stamp_count(points + 2 * sk.first_point, sk.npoints, sk.spacing);
       total_stamps += n;
-      work[c] += static_cast<double>(n) * (0.4 * b->F * b->F + 4.0 * b->F * (b->radius + 1));
+      loadN[c] += static_cast<double>(n);
+      loadP[c] += static_cast<double>(n) * di->second;
+      work[c] = loadN[c] * kStampFixed + kStampPerPixel * loadP[c];
       bs.push_back(x);
       for (int i = 0; i < 3; i++) {  // dip
         b->paintK[i] = sk.K[i];
@@ -1478,6 +1765,8 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
     }
     x.cV = static_cast<TV*>(cv->wet.V);
     x.sV = static_cast<TV*>(b->useSnapshot ? b->snapshot.V : cv->wet.V);
+    x.crec = cv->wet.base;
+    x.srec = b->useSnapshot ? b->snapshot.base : cv->wet.base;
     x.ring = b->d_ring();
     x.stamp_count = b->d_status + 2;
     x.ring_reset = ring_reset;
@@ -1497,11 +1786,39 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   for (int32_t c = 0; c < nc; c++) order[c] = c;
   std::stable_sort(order.begin(), order.end(),
                    [&](int32_t a, int32_t b2) { return work[a] > work[b2]; });
+  // cluster size (autotuned by the cost model unless PAINTY_BATCH_CLUSTER sets it) and the
+  // strokes' shared-memory plans (clusters keep the pickup map in global memory)
+  auto kern = batch_kernel<TK, TV>;
+  auto plan_all = [&](int cl) {
+    dyn = 0;
+    for (size_t i = 0; i < bs.size(); i++) {
+      const SmemPlan plan = plan_smem_limit<M>(bs[i].F, bs[i].S, disc_of[i], limit, true, cl == 1);
+      bs[i].ndisc = plan.ndisc;
+      bs[i].plan = (plan.pick ? 1 : 0) | (plan.big ? 2 : 0);
+      dyn = std::max(dyn, plan.layout.total);
+    }
+    PG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(std::max<size_t>(dyn, 16))));
+  };
+  const int forced = env_cluster("PAINTY_BATCH_CLUSTER");
+  int cl = 1, slots = 0;
+  double best = 1e300;
+  for (int c2 : {1, 2, 4}) {
+    if (forced && c2 != forced) continue;
+    plan_all(c2);
+    const int fits = max_clusters(kern, c2, std::max<size_t>(dyn, 16));
+    const int sl = std::min(fits, nc);
+    const double span = batch_makespan(loadN, loadP, order, sl, c2);
+    if (sl >= 1 && span < best) {
+      best = span;
+      cl = c2;
+      slots = sl;
+    }
+  }
+  PG_REQUIRE(slots >= 1, "no stamp cluster fits on the device");
+  plan_all(cl);
+  const int grid = slots * cl;
   // device copies of the descriptors (stream-ordered, freed after the launch)
-  int dev = 0, sms = 0;
-  PG_CUDA(cudaGetDevice(&dev));
-  PG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const int grid = std::max(1, std::min(sms, nc));
   auto upload = [&](const void* h, size_t bytes) -> void* {
     void* d = nullptr;
     PG_CUDA(cudaMallocAsync(&d, std::max<size_t>(bytes, 16), st));
@@ -1518,10 +1835,10 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   void* d_scratch_p = nullptr;
   void* d_scratch_o = nullptr;
   void* d_counter = nullptr;
-  PG_CUDA(cudaMallocAsync(&d_scratch_p, grid * pstride * msz, st));
-  PG_CUDA(cudaMallocAsync(&d_scratch_o, grid * ostride * sizeof(int), st));
-  PG_CUDA(cudaMallocAsync(&d_counter, sizeof(int) + sizeof(unsigned), st));
-  PG_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(int) + sizeof(unsigned), st));
+  PG_CUDA(cudaMallocAsync(&d_scratch_p, slots * pstride * msz, st));
+  PG_CUDA(cudaMallocAsync(&d_scratch_o, slots * ostride * sizeof(int), st));
+  PG_CUDA(cudaMallocAsync(&d_counter, sizeof(int) * (2 + slots), st));
+  PG_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(int) * (2 + slots), st));
   BatchArgs<TK, TV> a{};
   a.canvases = static_cast<const BatchCanvas<TK, TV>*>(d_canvas);
   a.strokes = static_cast<const BatchStroke*>(d_strokes);
@@ -1531,14 +1848,12 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   a.ncanvas = nc;
   a.counter = static_cast<int*>(d_counter);
   a.status = reinterpret_cast<unsigned*>(static_cast<int*>(d_counter) + 1);
+  a.claims = static_cast<int*>(d_counter) + 2;
   a.scratch_pickup = static_cast<M*>(d_scratch_p);
   a.scratch_owner = static_cast<int*>(d_scratch_o);
   a.pickup_stride = pstride;
   a.owner_stride = ostride;
-  auto kern = batch_kernel<TK, TV>;
-  PG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               static_cast<int>(dyn)));
-  kern<<<grid, kStampThreads, dyn, st>>>(a);
+  launch_clustered(kern, grid, cl, std::max<size_t>(dyn, 16), st, a);
   count_launch();
   PG_CUDA(cudaGetLastError());
   unsigned status = 0;
@@ -1800,8 +2115,8 @@ painty_status painty_brush_update_snapshot(painty_brush* b, const painty_canvas*
         b->snapshot.storage != c->wet.storage) {
       if (b->has_snapshot) pg::device_free(b->snapshot.base);
       b->has_snapshot = false;
-      void* base = pg::device_alloc(pg::layer_bytes(c->wet.rows, c->wet.cols, c->wet.storage));
-      pg::layer_layout(b->snapshot, c->wet.rows, c->wet.cols, c->wet.storage, base);
+      void* base = pg::device_alloc(pg::layer_bytes(c->wet.rows, c->wet.cols, c->wet.storage, true));
+      pg::layer_layout(b->snapshot, c->wet.rows, c->wet.cols, c->wet.storage, base, true);
       b->has_snapshot = true;
     }
     PG_CUDA(cudaMemcpyAsync(b->snapshot.base, c->wet.base, c->wet.bytes,
@@ -1968,8 +2283,8 @@ painty_status painty_stamps_f32_noalloc(const painty_stamp_buffers_f32* b, void*
     a.pickup_smem = plan.pick ? 1 : 0;
     a.footprint_smem = 0;
     a.footprint = b->footprint;  // global: the owner table is the scratch array
-    auto kern = a.pickup_smem ? pg::stamp_kernel<true, true, float, float>
-                              : pg::stamp_kernel<false, true, float, float>;
+    auto kern = a.pickup_smem ? pg::stamp_kernel<true, true, false, false, float, float>
+                              : pg::stamp_kernel<false, true, false, false, float, float>;
     const pg::StampSmem Lk = pg::stamp_smem_layout<float>(b->footprint_side, b->map_side, a.ndisc,
                                                           false, a.pickup_smem != 0, false);
     PG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
