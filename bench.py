@@ -178,6 +178,17 @@ def run_precision_only(args):
     print(json.dumps(run_precision(pg, torch)), flush=True)
 
 
+def run_batch_only(args):
+    import torch
+
+    import painty_gb300 as pg
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    for s_ in ("f32", "f16"):
+        print(json.dumps(run_batch(pg, torch, s_, args.batch_canvases, args.batch_max_strokes)),
+              flush=True)
+
+
 def run_serve_only(args):
     import torch
 
@@ -416,8 +427,10 @@ def run_batch(pg, torch, storage: str, ncanvas: int, max_strokes):
     torch.cuda.synchronize()
     dt = time.perf_counter() - t
     px = sum(r * c for r, c, _ in specs)
+    cl, nclusters = pg.batch_last_shape()
     return {"metric": "stamps/s", "value": round(n / dt, 1), "unit": "stamps/s", "stamps": n,
             "s": round(dt, 3), "storage": storage, "gpu_launches": pg.kernel_launch_count() - l0,
+            "ctas_per_canvas": cl, "clusters": nclusters,
             "config": f"{ncanvas} canvases (side logU[256,2048], aspect U[0.5,2], "
                       f"{pg_canvas_px(px)}), {len(strokes)} strokes (logU[50,2000] per canvas"
                       f"{'' if max_strokes is None else f', at most {max_strokes}'}), "
@@ -703,6 +716,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--serve-only", action="store_true", help="only the serving case")
     ap.add_argument("--precision-only", action="store_true", help="only the precision case")
+    ap.add_argument("--batch-only", action="store_true", help="only the batched stamping case")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="serving arrivals per second")
     ap.add_argument("--serve-seconds", type=float, default=5.0, help="serving arrival window")
     args = ap.parse_args()
@@ -717,6 +731,8 @@ def main():
         run_serve_only(args)
     elif args.precision_only:
         run_precision_only(args)
+    elif args.batch_only:
+        run_batch_only(args)
     else:
         run_ours(args)
 

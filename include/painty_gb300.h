@@ -210,6 +210,12 @@ painty_status painty_paint_batch(painty_canvas* const* canvases, painty_brush* c
                                  const double* points, int64_t npoints, int64_t* stamps_out,
                                  void* stream);
 
+/* The launch shape the last painty_paint_batch on this thread chose: CTAs per canvas (a
+ * thread-block cluster sharing each stamp; picked by a makespan model of the batch unless the
+ * environment variable PAINTY_BATCH_CLUSTER sets it) and the number of clusters launched.
+ * No counterpart in painty. */
+painty_status painty_batch_last_shape(int32_t* cluster, int32_t* clusters);
+
 /* ------------------------------------------------------------------ serving
  * A continuous-batching render server (no counterpart in painty, whose SbrRenderThread runs
  * one stroke at a time on a GL thread: painty/renderer/SbrRenderThread.hxx:50-74). Requests

@@ -91,6 +91,7 @@ _sig("painty_stamps", _P, _P, _P, _I64, _P)
 _sig("painty_stroke", _P, _P, _P, _I32, _D, C.POINTER(_I64), _P)
 _sig("painty_mix_paint", _P, _I32, _P, _P, _P, _P)
 _sig("painty_paint_batch", _P, _P, _I32, _P, _I64, _P, _I64, C.POINTER(_I64), _P)
+_sig("painty_batch_last_shape", C.POINTER(_I32), C.POINTER(_I32))
 
 # painty_stroke_desc (include/painty_gb300.h)
 STROKE_DESC = np.dtype([("canvas", np.int32), ("npoints", np.int32), ("first_point", np.int64),
@@ -446,6 +447,13 @@ def paint_batch(canvases, brushes, strokes, stream=None) -> int:
     _check(_lib.painty_paint_batch(carr, barr, len(canvases), desc.ctypes.data, len(strokes),
                                    pts.ctypes.data, pts.shape[0], C.byref(n), _stream(stream)))
     return n.value
+
+
+def batch_last_shape():
+    """(CTAs per canvas, clusters) of the last paint_batch on this thread."""
+    cl, n = _I32(), _I32()
+    _check(_lib.painty_batch_last_shape(C.byref(cl), C.byref(n)))
+    return cl.value, n.value
 
 
 class _ServerOptions(C.Structure):

@@ -96,6 +96,7 @@ struct StampArgs {
   M* pK[3];  // pickup map in global memory, S*S per plane (the brush's state)
   M* pS[3];
   M* pV;
+  M* prec;   // PK kernels: the pickup map as cell records of 8 values (K r,g,b, S r,g,b, V, pad)
   const M* footprint;  // F*F
   const StampRec* stamps;
   int64_t n;
@@ -213,6 +214,14 @@ __device__ __forceinline__ TV* rec_v(void* base, int c) {
   return reinterpret_cast<TV*>(static_cast<char*>(base) + static_cast<int64_t>(c) * 8 * sizeof(TK)) + 6;
 }
 
+// A pickup-map cell record (K r,g,b, S r,g,b, V, pad) as 16-byte words.
+template <class M>
+union CellRec {
+  static constexpr int kWords = 8 * sizeof(M) / 16;
+  uint4 w[kWords];
+  M v[8];
+};
+
 // pickupPaint then depositPaint for one stamp pixel (FootprintBrush.hxx:349-431); fp > 0.
 // PS: the pickup map is staged in shared memory at `pbase` (7 planes `cells` apart). CG:
 // global loads from L2 only (other CTAs of a cluster write the same planes). snap: the next
@@ -233,21 +242,37 @@ __device__ __forceinline__ void process_pixel(const StampArgs<TK, TV>& a, M* pba
     h2 = hash32(h1 + 0x632be5abu);
     h3 = hash32(h2 + 0x632be5abu);
   }
+  // the pickup cell: planar planes (!PK) or a cell record (PK), in shared (PS) or global memory
   auto cell = [&](int p) -> M& {
     if constexpr (PS) return pbase[p * cells + m];
     else return pickup_plane<TK, TV, M>(a, p)[m];
   };
+  CellRec<M> crec_{};
+  M* const cell_rec = PK ? (PS ? pbase : a.prec) + static_cast<int64_t>(m) * 8 : nullptr;
   // every load first (one round trip): pickup cell, canvas pixel, snapshot pixel; global
   // loads from L2 (another CTA of a cluster may have written them)
-  auto pick = [&](int p) -> M {
-    if constexpr (PS) return pbase[p * cells + m];
-    else return ld_sel<CG, M>(pickup_plane<TK, TV, M>(a, p) + m);
-  };
-  M vp = pick(6);
+  M vp;
   M pk[6], cn[6], sn[6];
   M vsrc, vcan;
+  if constexpr (PK) {
+    const uint4* w = reinterpret_cast<const uint4*>(cell_rec);
 #pragma unroll
-  for (int i = 0; i < 6; i++) pk[i] = pick(i);
+    for (int i = 0; i < CellRec<M>::kWords; i++) {
+      if constexpr (PS || !CG) crec_.w[i] = w[i];
+      else crec_.w[i] = __ldcg(w + i);
+    }
+#pragma unroll
+    for (int i = 0; i < 6; i++) pk[i] = crec_.v[i];
+    vp = crec_.v[6];
+  } else {
+    auto pick = [&](int p) -> M {
+      if constexpr (PS) return pbase[p * cells + m];
+      else return ld_sel<CG, M>(pickup_plane<TK, TV, M>(a, p) + m);
+    };
+    vp = pick(6);
+#pragma unroll
+    for (int i = 0; i < 6; i++) pk[i] = pick(i);
+  }
   if constexpr (PK) {
     const PixRec<TK, TV> cr = load_rec<CG, TK, TV>(a.crec, c);
 #pragma unroll
@@ -296,7 +321,7 @@ __device__ __forceinline__ void process_pixel(const StampArgs<TK, TV>& a, M* pba
 #pragma unroll
     for (int i = 0; i < 6; i++) {
       pk[i] = np[i];
-      cell(i) = np[i];
+      if constexpr (!PK) cell(i) = np[i];
     }
     vp = A::add(vp, vleave);
   }
@@ -311,7 +336,16 @@ __device__ __forceinline__ void process_pixel(const StampArgs<TK, TV>& a, M* pba
   }
   blend6(vp, pk, vfree, paint, src);
   const M pleave = A::mul(A::mul(a.depositionRate, vp), fp);
-  cell(6) = A::sub(vp, pleave);
+  if constexpr (PK) {
+#pragma unroll
+    for (int i = 0; i < 6; i++) crec_.v[i] = pk[i];
+    crec_.v[6] = A::sub(vp, pleave);
+    uint4* w = reinterpret_cast<uint4*>(cell_rec);
+#pragma unroll
+    for (int i = 0; i < CellRec<M>::kWords; i++) w[i] = crec_.w[i];
+  } else {
+    cell(6) = A::sub(vp, pleave);
+  }
   const M vb = A::mul(a.capacity, fp);
   M out[6];
   blend6(vb, src, vcan, cn, out);
@@ -438,13 +472,14 @@ struct StampSmem {
 };
 template <class M>
 __host__ __device__ inline StampSmem stamp_smem_layout(int F, int S, int ndisc, bool fp_smem,
-                                                       bool pick_smem, bool own_smem) {
+                                                       bool pick_smem, bool own_smem,
+                                                       int pick_vals = 8) {
   StampSmem L{};
   size_t o = 0;
   L.fp = o;
   if (fp_smem) o = align_up(o + size_t(F) * F * sizeof(M), 16);
   L.pick = o;
-  if (pick_smem) o = align_up(o + size_t(7) * S * S * sizeof(M), 16);
+  if (pick_smem) o = align_up(o + size_t(pick_vals) * S * S * sizeof(M), 16);
   L.own = o;
   if (own_smem) o = align_up(o + size_t(S) * S * sizeof(int), 16);
   L.xs = o;
@@ -575,13 +610,17 @@ __device__ __forceinline__ void refresh_ring(const StampArgs<TK, TV>& a, const R
       const int idx = base + u * T + tid;
       off[u] = -1;
       if (idx < total) {
-        int r = 0;
+        int r = 0;  // the rectangle holding idx: pre[r] <= idx < pre[r + 1] (binary search)
 #pragma unroll
-        for (int q = 1; q < kRefreshRects; q++) r += idx >= rl.pre[q] ? 1 : 0;
+        for (int step = 16; step > 0; step >>= 1)
+          if (r + step < kRefreshRects && idx >= rl.pre[r + step]) r += step;
         const int4 R = rl.rect[r];
         const int w = R.z - R.x + 1;
         const int local = idx - rl.pre[r];
-        const int dy = local / w;
+        // local / w through a float reciprocal (local < 2^22), corrected to the exact quotient
+        int dy = static_cast<int>(static_cast<float>(local) * __frcp_rn(static_cast<float>(w)));
+        if (dy * w > local) dy--;
+        if ((dy + 1) * w <= local) dy++;
         const int y = R.y + dy, x = R.x + local - dy * w;
         bool take = true;
         if (skip) {
@@ -849,7 +888,7 @@ __device__ __forceinline__ void run_stroke(const StampArgs<TK, TV>& a, const Src
   const int F = a.F, S = a.S;
   const int npix = F * F;
   const int cells = S * S;
-  const StampSmem L = stamp_smem_layout<M>(F, S, a.ndisc, !BIG, PS, !BIG);
+  const StampSmem L = stamp_smem_layout<M>(F, S, a.ndisc, !BIG, PS, !BIG, PK ? 8 : 7);
   const M* fps = !BIG ? reinterpret_cast<M*>(smem_raw + L.fp) : a.footprint;
   M* pbase = PS ? reinterpret_cast<M*>(smem_raw + L.pick) : nullptr;
   int* own = BIG ? a.owner_global : reinterpret_cast<int*>(smem_raw + L.own);
@@ -899,12 +938,21 @@ __device__ __forceinline__ void run_stroke(const StampArgs<TK, TV>& a, const Src
     M* f = reinterpret_cast<M*>(smem_raw + L.fp);
     for (int i = tid; i < npix; i += T) f[i] = a.footprint[i];
   }
-  for (int i = tid + crank * T; i < 7 * cells; i += T * csize) {
-    const int p = i / cells, m = i - p * cells;
-    if (PS)
-      pbase[i] = a.pickup_zero ? M(0) : pickup_plane<TK, TV, M>(a, p)[m];
-    else if (a.pickup_zero)
-      pickup_plane<TK, TV, M>(a, p)[m] = M(0);
+  if constexpr (PK) {  // cell records
+    for (int i = tid + crank * T; i < 8 * cells; i += T * csize) {
+      if (PS)
+        pbase[i] = a.pickup_zero ? M(0) : a.prec[i];
+      else if (a.pickup_zero)
+        a.prec[i] = M(0);
+    }
+  } else {
+    for (int i = tid + crank * T; i < 7 * cells; i += T * csize) {
+      const int p = i / cells, m = i - p * cells;
+      if (PS)
+        pbase[i] = a.pickup_zero ? M(0) : pickup_plane<TK, TV, M>(a, p)[m];
+      else if (a.pickup_zero)
+        pickup_plane<TK, TV, M>(a, p)[m] = M(0);
+    }
   }
   if (!BIG || crank == 0)
     for (int i = tid; i < cells; i += T) own[i] = INT_MAX;
@@ -1006,9 +1054,13 @@ __device__ __forceinline__ void run_stroke(const StampArgs<TK, TV>& a, const Src
       for (int i = 0; i < 8; i++) a.ring[i] = sh->prev[i];
   }
   if (PS) {
-    for (int i = tid; i < 7 * cells; i += T) {
-      const int p = i / cells, m = i - p * cells;
-      pickup_plane<TK, TV, M>(a, p)[m] = pbase[i];
+    if constexpr (PK) {
+      for (int i = tid; i < 8 * cells; i += T) a.prec[i] = pbase[i];
+    } else {
+      for (int i = tid; i < 7 * cells; i += T) {
+        const int p = i / cells, m = i - p * cells;
+        pickup_plane<TK, TV, M>(a, p)[m] = pbase[i];
+      }
     }
   }
   csync();  // the ring state and pickup map are written before any CTA reads them again
@@ -1129,7 +1181,7 @@ struct BatchArgs {
   int32_t ncanvas;
   int* counter;
   int* claims;        // per cluster: the canvas it claimed last
-  M* scratch_pickup;  // per cluster: 7 planes of Smax^2
+  M* scratch_pickup;  // per cluster: Smax^2 cell records
   int* scratch_owner; // per cluster: Smax^2
   int64_t pickup_stride, owner_stride;
   unsigned* status;
@@ -1180,8 +1232,8 @@ __global__ void __launch_bounds__(kStampThreads, 1) batch_kernel(const __grid_co
           sa.cS[i] = cv.cS[i];
           sa.sK[i] = cv.sK[i];
           sa.sS[i] = cv.sS[i];
-          sa.pK[i] = pk + i * cells;
-          sa.pS[i] = pk + (3 + i) * cells;
+          sa.pK[i] = nullptr;
+          sa.pS[i] = nullptr;
           sa.paintK[i] = static_cast<M>(st.K[i]);
           sa.paintS[i] = static_cast<M>(st.Sc[i]);
         }
@@ -1189,7 +1241,9 @@ __global__ void __launch_bounds__(kStampThreads, 1) batch_kernel(const __grid_co
         sa.sV = cv.sV;
         sa.crec = cv.crec;
         sa.srec = cv.srec;
-        sa.pV = pk + 6 * cells;
+        sa.pV = nullptr;
+        sa.prec = pk;
+        (void)cells;
         sa.footprint = b.footprints + st.fp_offset;
         sa.stamps = nullptr;
         sa.n = 0;
@@ -1467,12 +1521,7 @@ void launch_stamps(painty_canvas* c, painty_brush* b, const StampRec* d_stamps, 
   a.crec = c->wet.base;
   a.srec = b->useSnapshot ? b->snapshot.base : c->wet.base;
   const size_t cells = static_cast<size_t>(b->sizeMap) * b->sizeMap;
-  M* pk = static_cast<M*>(b->d_pickup);
-  for (int i = 0; i < 3; i++) {
-    a.pK[i] = pk + i * cells;
-    a.pS[i] = pk + (3 + i) * cells;
-  }
-  a.pV = pk + 6 * cells;
+  a.prec = static_cast<M*>(b->d_pickup);  // cell records
   a.footprint = static_cast<const M*>(b->d_footprint);
   a.stamps = d_stamps;
   a.n = n;
@@ -1597,7 +1646,7 @@ void run_stamps(painty_canvas* c, painty_brush* b, const std::vector<StampRec>& 
     b->footprint_stale = false;
   }
   // pickup map: cleared by the kernel itself when a dip / new radius is pending
-  const size_t pk_bytes = static_cast<size_t>(b->sizeMap) * b->sizeMap * 7 * msz;
+  const size_t pk_bytes = static_cast<size_t>(b->sizeMap) * b->sizeMap * 8 * msz;
   if (b->d_pickup_bytes < pk_bytes) {
     ensure(&b->d_pickup, &b->d_pickup_bytes, pk_bytes);
     b->pickup_clear = true;
@@ -1648,6 +1697,8 @@ void run_stamps(painty_canvas* c, painty_brush* b, const std::vector<StampRec>& 
 constexpr double kStampFixed = 7000.0;
 constexpr double kStampPerPixel = 12.0;
 constexpr double kClusterSync = 1500.0;
+
+thread_local int32_t g_last_batch_shape[2] = {0, 0};  // cluster size, clusters
 
 // Makespan of painting canvases with loads (stamps N, stamp-pixels P) on `slots` clusters of
 // `cl` CTAs, heaviest canvas first onto the least-loaded cluster (the kernel's claim order).
@@ -1752,7 +1803,7 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
     PG_REQUIRE(b->bound == mode,
                "a brush paints either F64 canvases or F32/F16/BF16 canvases, not both");
     ensure_status(b, st);
-    const size_t pk_bytes = static_cast<size_t>(b->sizeMap) * b->sizeMap * 7 * msz;
+    const size_t pk_bytes = static_cast<size_t>(b->sizeMap) * b->sizeMap * 8 * msz;
     ensure(&b->d_pickup, &b->d_pickup_bytes, pk_bytes);
     const int ring_reset = per[c].empty() ? kRingKeep : prepare_snapshot(cv, b, st);
     BatchCanvas<TK, TV>& x = bc[c];
@@ -1816,6 +1867,8 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
     }
   }
   PG_REQUIRE(slots >= 1, "no stamp cluster fits on the device");
+  g_last_batch_shape[0] = cl;
+  g_last_batch_shape[1] = slots;
   plan_all(cl);
   const int grid = slots * cl;
   // device copies of the descriptors (stream-ordered, freed after the launch)
@@ -1830,7 +1883,7 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   void* d_points = upload(points, static_cast<size_t>(npoints) * 2 * sizeof(double));
   void* d_fp = upload(fptable.data(), fptable.size() * sizeof(M));
   void* d_order = upload(order.data(), order.size() * sizeof(int32_t));
-  const int64_t pstride = static_cast<int64_t>(7) * smax * smax;
+  const int64_t pstride = static_cast<int64_t>(8) * smax * smax;
   const int64_t ostride = static_cast<int64_t>(smax) * smax;
   void* d_scratch_p = nullptr;
   void* d_scratch_o = nullptr;
@@ -2160,17 +2213,17 @@ painty_status painty_brush_download_pickup(const painty_brush* b, painty_plane p
       std::memset(host, 0, nvals * (host64 ? 8 : 4));
       return;
     }
-    char* base = static_cast<char*>(b->d_pickup);
+    char* base = static_cast<char*>(b->d_pickup);  // cell records of 8 values
     if (plane == PAINTY_PLANE_V) {
-      const void* p[1] = {base + 6 * cells * msz};
-      pg::download_planes(p, 1, dt, S, S, S, host, fmt, pg::as_stream(stream));
+      const void* p[1] = {base + 6 * msz};
+      pg::download_planes(p, 1, dt, S, S, S, host, fmt, pg::as_stream(stream), 8);
     } else {
       PG_REQUIRE(plane == PAINTY_PLANE_K || plane == PAINTY_PLANE_S, "pickup planes are K, S, V");
       const int off = plane == PAINTY_PLANE_K ? 0 : 3;
-      const void* p[3] = {base + (off + 0) * cells * msz, base + (off + 1) * cells * msz,
-                          base + (off + 2) * cells * msz};
-      pg::download_planes(p, 3, dt, S, S, S, host, fmt, pg::as_stream(stream));
+      const void* p[3] = {base + (off + 0) * msz, base + (off + 1) * msz, base + (off + 2) * msz};
+      pg::download_planes(p, 3, dt, S, S, S, host, fmt, pg::as_stream(stream), 8);
     }
+    (void)cells;
   });
 }
 
@@ -2296,6 +2349,13 @@ painty_status painty_stamps_f32_noalloc(const painty_stamp_buffers_f32* b, void*
     PG_CUDA(cudaMemcpyAsync(&hs, status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     PG_CUDA(cudaStreamSynchronize(st));
     if (hs != 0) pg::fail(PAINTY_ERR_CUDA, "stamp kernel reported an internal error");
+  });
+}
+
+painty_status painty_batch_last_shape(int32_t* cluster, int32_t* clusters) {
+  return guard([&] {
+    if (cluster) *cluster = pg::g_last_batch_shape[0];
+    if (clusters) *clusters = pg::g_last_batch_shape[1];
   });
 }
 
