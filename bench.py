@@ -324,10 +324,11 @@ def run_ours(args):
     batch = None
     serve = None
     prec = None
+    if not args.no_stamps:
+        batch = {s_: run_batch(pg, torch, s_, args.batch_canvases, args.batch_max_strokes,
+                               rank, ws) for s_ in ("f32", "f16")}
     if rank == 0 and not args.no_stamps:
         stamps = run_stamps_config0(pg, torch)
-        batch = {s_: run_batch(pg, torch, s_, args.batch_canvases, args.batch_max_strokes)
-                 for s_ in ("f32", "f16")}
         serve = run_serve(pg, torch, args.serve_rate, args.serve_seconds)
         prec = run_precision(pg, torch)
     if rank == 0 and not args.no_cpu:
@@ -405,11 +406,22 @@ def run_stamps_config0(pg, torch, nstrokes: int = 200):
             "gpu_launches": pg.kernel_launch_count() - l0}
 
 
-def run_batch(pg, torch, storage: str, ncanvas: int, max_strokes):
-    """The batching workload (config-2 distributions) in one painty_paint_batch launch."""
-    from painty_gb300 import workloads
+def run_batch(pg, torch, storage: str, ncanvas: int, max_strokes, rank: int = 0,
+              world: int = 1):
+    """The batching workload (config-2 distributions) in one painty_paint_batch launch per GPU;
+    with several ranks each paints its share of the canvases (longest-processing-time split
+    by estimated work), and the job's rate is all stamps over the slowest rank's time."""
+    from painty_gb300 import sharding, workloads
 
     specs, strokes = workloads.batch_canvases(ncanvas, seed=2, max_strokes=max_strokes)
+    if world > 1:
+        work = np.zeros(len(specs))
+        for c, path, r, sp, _, _ in strokes:
+            work[c] += sharding.stroke_work(path, r, sp)
+        mine = sharding.canvas_shard(work, rank, world)
+        index = {c: i for i, c in enumerate(mine)}
+        specs = [specs[c] for c in mine]
+        strokes = [(index[s[0]],) + tuple(s[1:]) for s in strokes if s[0] in index]
     fp = workloads.footprint_image(seed=7)
     canvases, brushes = [], []
     for rows, cols, r0 in specs:
@@ -421,11 +433,22 @@ def run_batch(pg, torch, storage: str, ncanvas: int, max_strokes):
         canvases.append(c)
         brushes.append(b)
     torch.cuda.synchronize()
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
     l0 = pg.kernel_launch_count()
     t = time.perf_counter()
-    n = pg.paint_batch(canvases, brushes, strokes)
+    n = pg.paint_batch(canvases, brushes, strokes) if strokes else 0
     torch.cuda.synchronize()
     dt = time.perf_counter() - t
+    if world > 1:
+        import torch.distributed as dist
+        v = torch.tensor([dt, float(n)], device="cuda", dtype=torch.float64)
+        t_ = v[:1].clone()
+        dist.all_reduce(t_, op=dist.ReduceOp.MAX)
+        n_ = v[1:].clone()
+        dist.all_reduce(n_, op=dist.ReduceOp.SUM)
+        dt, n = float(t_.item()), int(n_.item())
     px = sum(r * c for r, c, _ in specs)
     cl, nclusters = pg.batch_last_shape()
     return {"metric": "stamps/s", "value": round(n / dt, 1), "unit": "stamps/s", "stamps": n,

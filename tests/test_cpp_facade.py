@@ -1,0 +1,66 @@
+"""The C++ facade (include/painty_gb300.hpp): compiles against the C ABI, translates statuses
+into painty's exception types, and paints the same result as the Python binding."""
+import os
+import shutil
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from painty_gb300 import workloads
+
+ROOT = Path(__file__).resolve().parents[1]
+LIB = ROOT / "painty_gb300" / "_lib"
+
+
+def _cuda_lib():
+    for c in ("/usr/local/cuda/lib64", "/usr/local/cuda/targets/sbsa-linux/lib",
+              "/usr/local/cuda/targets/x86_64-linux/lib"):
+        if Path(c, "libcudart.so").exists():
+            return c
+    return "/usr/local/cuda/lib64"
+
+
+@pytest.fixture(scope="module")
+def demo(tmp_path_factory, pg):
+    if shutil.which("g++") is None:
+        pytest.skip("no C++ compiler")
+    exe = tmp_path_factory.mktemp("cpp") / "facade_demo"
+    cmd = ["g++", "-std=c++17", "-O1", "-Wall", "-Werror", f"-I{ROOT / 'include'}",
+           str(ROOT / "tests" / "cpp" / "facade_demo.cpp"), "-o", str(exe), f"-L{LIB}",
+           "-lpainty_gb300", f"-Wl,-rpath,{LIB}", f"-Wl,-rpath,{_cuda_lib()}"]
+    subprocess.run(cmd, check=True, capture_output=True)
+    return exe
+
+
+def test_facade_translates_argument_errors(demo):
+    r = subprocess.run([str(demo), "errors"], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "errors ok" in r.stdout
+
+
+@pytest.mark.gpu
+def test_facade_paints_like_python_binding(demo, pg, tmp_path):
+    rows, cols = 70, 90
+    fp = workloads.footprint_image(seed=7)
+    s = workloads.strokes(cols, rows, 1, seed=29, rmin=5, rmax=12)[0]
+    r0 = workloads.substrate(rows, cols, seed=5)
+    buf = np.concatenate([[rows, cols, fp.shape[0], fp.shape[1]], fp.ravel(), [len(s.path)],
+                          s.path.ravel(), [s.radius, s.spacing, 0.05, 0.1], s.K, s.S, r0.ravel()])
+    inp, out = tmp_path / "in.bin", tmp_path / "out.bin"
+    buf.astype(np.float64).tofile(inp)
+    r = subprocess.run([str(demo), "paint", str(inp), str(out)], capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    got = np.fromfile(out, dtype=np.float64)
+    c = pg.Canvas(rows, cols, "f64")
+    c.setBackground(r0)
+    b = pg.FootprintBrush(s.radius, fp)
+    b.setPickupRate(0.05)
+    b.setDepositionRate(0.1)
+    b.dip((s.K, s.S))
+    n = b.paintStroke(s.path, c, spacing=s.spacing)
+    want = [np.array([n], dtype=np.float64), c.download("K").ravel(), c.download("S").ravel(),
+            c.download("V").ravel(), pg.Renderer().compose(c).download().ravel()]
+    assert np.array_equal(got, np.concatenate(want))
