@@ -171,6 +171,61 @@ class Oracle:
     def brush(self, radius, footprint):
         return OBrush(self, radius, footprint)
 
+    def texture_brush(self, texture):
+        return _TBrush(self.lib, "orc", texture)
+
+
+class _TBrush:
+    """TextureBrush<vec3> with the given thickness texture (orc_ or ref_ prefix)."""
+
+    def __init__(self, lib, pre: str, texture):
+        L = _Lib(lib, pre)
+        self._create = L.f("tbrush_create", _P, _I32, _I32, res=_P)
+        self._destroy = L.f("tbrush_destroy", _P)
+        self._radius = L.f("tbrush_set_radius", _P, _D)
+        self._dip = L.f("tbrush_dip", _P, _P, _P)
+        self._smudge = L.f("tbrush_set_smudge", _P, _I32)
+        self._scale = L.f("tbrush_set_thickness_scale", _P, _D)
+        self._stroke = L.f("tbrush_paint_stroke", _P, _P, _P, _I32,
+                           res=_I64 if pre == "orc" else None)
+        self.pre = pre
+        if pre == "orc":
+            self._map = L.f("tbrush_smudge_map", _P, _I32, C.POINTER(_I32), res=_P)
+        tex = np.ascontiguousarray(texture, dtype=np.float64)
+        self.h = self._create(_p(tex), tex.shape[0], tex.shape[1])
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self._destroy(self.h)
+            self.h = None
+
+    def set_radius(self, r):
+        self._radius(self.h, float(r))
+
+    def dip(self, K, S):
+        K, S = (np.ascontiguousarray(x, dtype=np.float64) for x in (K, S))
+        self._dip(self.h, _p(K), _p(S))
+
+    def enable_smudge(self, on: bool):
+        self._smudge(self.h, 1 if on else 0)
+
+    def set_thickness_scale(self, s):
+        self._scale(self.h, float(s))
+
+    def paint_stroke(self, canvas, path):
+        path = np.ascontiguousarray(path, dtype=np.float64)
+        return self._stroke(self.h, canvas.h, _p(path), len(path))
+
+    def smudge_map(self, which: str):
+        side = _I32()
+        idx = {"K": 0, "S": 1, "V": 2}[which]
+        ptr = self._map(self.h, idx, C.byref(side))
+        n = side.value
+        if n == 0:
+            return np.zeros((0, 0) if which == "V" else (0, 0, 3))
+        a = np.ctypeslib.as_array(C.cast(ptr, C.POINTER(_D)), (n * n * (1 if which == "V" else 3),))
+        return a.reshape((n, n) if which == "V" else (n, n, 3)).copy()
+
 
 class OCanvas:
     def __init__(self, o: Oracle, rows: int, cols: int):
@@ -335,6 +390,9 @@ class Reference:
 
     def brush(self, radius, footprint):
         return RBrush(self, radius, footprint)
+
+    def texture_brush(self, texture):
+        return _TBrush(self.lib, "ref", texture)
 
 
 class RCanvas:

@@ -749,3 +749,354 @@ double orc_delta_e_images(int64_t npix, const double* a, const double* b, double
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- texture brush
+// TextureBrush<vec3> (painty/renderer/TextureBrush.hxx:20-237) with its Smudge<vec3>
+// (painty/renderer/Smudge.hxx:16-229). The thickness texture stands in for
+// BrushStrokeSample::getThicknessMap(), which painty loads from a sample directory.
+namespace {
+
+struct V2 {
+  double x, y;
+};
+
+// SplineEval::catmullRom / catmullRomDerivativeFirst over all points (Spline.hxx:183-231):
+// x = (n-1) u, index = int(x), t = x - floor(x), control points clamped to the ends.
+V2 spline_eval(const std::vector<V2>& p, double u, bool deriv) {
+  const auto n = static_cast<int64_t>(p.size());
+  const double x = static_cast<double>(n - 1) * u;
+  const int32_t index = static_cast<int32_t>(x);
+  const double t = x - std::floor(x);
+  auto at = [&](int32_t i) -> const V2& {
+    if (i < 0) return p.front();
+    if (i >= static_cast<int32_t>(n)) return p.back();
+    return p[static_cast<size_t>(i)];
+  };
+  const V2 &a = at(index - 1), &b = at(index), &c = at(index + 1), &d = at(index + 2);
+  if (deriv)
+    return {catmull_rom_deriv(a.x, b.x, c.x, d.x, t), catmull_rom_deriv(a.y, b.y, c.y, d.y, t)};
+  return {catmull_rom(a.x, b.x, c.x, d.x, t), catmull_rom(a.y, b.y, c.y, d.y, t)};
+}
+
+double norm2(const V2& v) { return std::sqrt(v.x * v.x + v.y * v.y); }
+V2 normalized2(const V2& v) {  // Eigen normalized(): v / sqrt(squaredNorm) when positive
+  const double n = v.x * v.x + v.y * v.y;
+  if (n > 0.0) {
+    const double r = std::sqrt(n);
+    return {v.x / r, v.y / r};
+  }
+  return v;
+}
+
+// generalizedBarycentricCoordinatesInterpolate (painty/core/Math.hxx:72-147) for vec2 values
+V2 barycentric_interpolate(const std::vector<V2>& polygon, const V2& pos,
+                           const std::vector<V2>& values) {
+  const size_t n = polygon.size();
+  constexpr double Eps = std::numeric_limits<double>::epsilon() * 100.0;
+  if (n == 1U) return values.front();
+  std::vector<V2> sv(n);
+  for (size_t i = 0; i < n; ++i) sv[i] = {polygon[i].x - pos.x, polygon[i].y - pos.y};
+  std::vector<double> r(n), A(n), D(n);
+  for (size_t i = 0; i < n; ++i) {
+    const V2 si1 = (i == n - 1) ? sv[0] : sv[i + 1];
+    const V2 si = sv[i];
+    r[i] = norm2(si);
+    if (std::fabs(r[i] - 0.0) < Eps) return values[i];
+    const double det = si.x * si1.y - si1.x * si.y;
+    A[i] = det / 2.0;
+    D[i] = si.x * si1.x + si.y * si1.y;
+    if (std::fabs(A[i] - 0.0) < Eps && D[i] < 0.0) {
+      const double ri1 = norm2(si1);
+      const V2 fi1 = (i == n - 1) ? values.front() : values[i + 1];
+      const double k = 1.0 / (r[i] + ri1);
+      return {(ri1 * values[i].x + r[i] * fi1.x) * k, (ri1 * values[i].y + r[i] * fi1.y) * k};
+    }
+  }
+  V2 f = {0.0, 0.0};
+  double W = 0.0;
+  for (size_t i = 0; i < n; ++i) {
+    double w = 0.0;
+    const double A_1 = (i == 0) ? A.back() : A[i - 1];
+    if (A_1 != 0.0) {
+      const double r_1 = (i == 0) ? r.back() : r[i - 1];
+      const double D_1 = (i == 0) ? D.back() : D[i - 1];
+      w = w + (r_1 - D_1 / r[i]) / A_1;
+    }
+    if (A[i] != 0.0) {
+      const double ri1 = (i == n - 1) ? r[0] : r[i + 1];
+      w = w + (ri1 - D[i] / r[i]) / A[i];
+    }
+    f = {f.x + w * values[i].x, f.y + w * values[i].y};
+    W = W + w;
+  }
+  if (!(std::fabs(W - 0.0) < Eps)) {
+    const double k = 1.0 / W;
+    return {f.x * k, f.y * k};
+  }
+  return values.front();
+}
+
+// Mat.hxx:68-103, three channels of an interleaved layer plane
+void interpolate3(const std::vector<double>& in, int rows, int cols, double px, double py,
+                  double out[3]) {
+  const int x = static_cast<int>(std::floor(px));
+  const int y = static_cast<int>(std::floor(py));
+  const int x0 = border_reflect(x, cols), x1 = border_reflect(x + 1, cols);
+  const int y0 = border_reflect(y, rows), y1 = border_reflect(y + 1, rows);
+  const double a = px - static_cast<double>(x);
+  const double c = py - static_cast<double>(y);
+  for (int k = 0; k < 3; k++) {
+    auto v = [&](int yy, int xx) { return in[(static_cast<size_t>(yy) * cols + xx) * 3 + k]; };
+    out[k] = (v(y0, x0) * (1.0 - a) + v(y0, x1) * a) * (1.0 - c) +
+             (v(y1, x0) * (1.0 - a) + v(y1, x1) * a) * c;
+  }
+}
+
+}  // namespace
+
+struct orc_tbrush {
+  std::vector<double> tex;  // thickness texture (th x tw)
+  int th = 0, tw = 0;
+  double radius = 0.0;           // TextureBrush.hxx:228
+  double thicknessScale = 1.0;   // BrushBase.hxx _thicknessScale
+  double paint[2][3] = {{0.1, 0.1, 0.1}, {0.1, 0.1, 0.1}};  // TextureBrush.hxx:28-30
+  bool useSmudge = true;         // TextureBrush.hxx:236
+  // Smudge (Smudge.hxx:147-158)
+  int maxSize = 0;
+  Layer pickSrc, pickDst;
+  double rotation = 0.0;
+  double smPickupRate = 0.1, smDepositionRate = 0.1;
+  void make_smudge(int32_t size) {  // Smudge.hxx:22-36
+    maxSize = size;
+    pickSrc.resize(size, size);
+    pickDst.resize(size, size);
+    if ((maxSize % 2) == 0) maxSize++;
+    pickSrc.clear();
+    pickDst.clear();
+    rotation = 0.0;
+  }
+};
+
+namespace {
+
+double normalize_angle(double angle) {  // Smudge.hxx:201-211
+  constexpr double HALF_PI = 0.5 * 3.14159265358979323846;
+  constexpr double PI = 3.14159265358979323846;
+  double a = angle;
+  while (a <= -HALF_PI) a += PI;
+  while (a > HALF_PI) a -= PI;
+  return a;
+}
+
+// Smudge::updateOrientation (Smudge.hxx:160-199)
+void smudge_orient(orc_tbrush* b, const V2& heading) {
+  const double theta = std::atan2(heading.y, heading.x);
+  const double dtheta = normalize_angle(theta - b->rotation);
+  b->rotation = theta;
+  b->pickDst.copy_to(b->pickSrc);
+  const double cx = b->maxSize / 2.0, cy = b->maxSize / 2.0;
+  const double sn = std::sin(dtheta), cs = std::cos(dtheta);
+  Layer& d = b->pickDst;
+  const Layer& sr = b->pickSrc;
+  for (int x = 0; x < d.cols; x++)
+    for (int y = 0; y < d.rows; y++) {
+      const double px = x - cx, py = y - cy;
+      const double qx = px * cs - py * sn + cx;
+      const double qy = px * sn + py * cs + cy;
+      const size_t o = d.idx(y, x);
+      if (qx < 0 || qy < 0 || qx >= d.cols || qy >= d.rows) {
+        for (int k = 0; k < 3; k++) {
+          d.K[o * 3 + k] = sr.K[o * 3 + k];
+          d.S[o * 3 + k] = sr.S[o * 3 + k];
+        }
+        d.V[o] = sr.V[o];
+      } else {
+        d.V[o] = interpolate(sr.V.data(), sr.rows, sr.cols, qx, qy);
+        interpolate3(sr.K, sr.rows, sr.cols, qx, qy, &d.K[o * 3]);
+        interpolate3(sr.S, sr.rows, sr.cols, qx, qy, &d.S[o * 3]);
+      }
+    }
+}
+
+// Smudge::smudge (Smudge.hxx:38-145)
+void smudge_run(orc_tbrush* b, orc_canvas* c, const V2& boundMin, const std::vector<V2>& verts,
+                double length, const std::vector<double>& tmap, int trows, int tcols) {
+  double maxD = 0.0;
+  for (double m : tmap) maxD = std::max(m, maxD);
+  if (maxD <= 0.) return;
+  Layer& pm = b->pickDst;
+  Layer& cw = c->wet;
+  for (double u = 0.0; u <= 1.0; u += 1. / length) {
+    const V2 center = spline_eval(verts, u, false);
+    const V2 t = normalized2(spline_eval(verts, u, true));
+    smudge_orient(b, t);
+    const double radius = b->maxSize * 0.5;
+    const int32_t roi_x = static_cast<int32_t>(center.x - pm.cols / 2.0);
+    const int32_t roi_y = static_cast<int32_t>(center.y - pm.rows / 2.0);
+    for (int x = 0; x < pm.cols; x++)
+      for (int y = 0; y < pm.rows; y++) {
+        const int cpx = x + roi_x, cpy = y + roi_y;
+        const int tpx = static_cast<int32_t>(cpx - boundMin.x);
+        const int tpy = static_cast<int32_t>(cpy - boundMin.y);
+        if (cpx < 0 || cpy < 0 || cpx >= cw.cols || cpy >= cw.rows) continue;
+        if (tpx < 0 || tpy < 0 || tpx >= tcols || tpy >= trows) continue;
+        const double dx = center.x - static_cast<double>(cpx);
+        const double dy = center.y - static_cast<double>(cpy);
+        if (std::sqrt(dx * dx + dy * dy) > radius) continue;
+        const double D = tmap[static_cast<size_t>(tpy) * tcols + tpx];
+        if (D <= 0.0) continue;
+        const size_t co = cw.idx(cpy, cpx), po = pm.idx(y, x);
+        const double cV = cw.V[co], pV = pm.V[po];
+        const double cVl = cV * b->smDepositionRate * D / maxD;
+        const double cVr = cV - cVl;
+        const double pVl = pV * b->smPickupRate * D / maxD;
+        const double pVr = pV - pVl;
+        double canvasK[3], canvasS[3], pickK[3], pickS[3];
+        for (int k = 0; k < 3; k++) {
+          canvasK[k] = cw.K[co * 3 + k];
+          canvasS[k] = cw.S[co * 3 + k];
+          pickK[k] = pm.K[po * 3 + k];
+          pickS[k] = pm.S[po * 3 + k];
+        }
+        constexpr double MinVolume = 0.001;
+        const double pVnew = pVr + cVl;
+        if (pVnew > MinVolume) {
+          const double pVnew_ = 1.0 / pVnew;
+          for (int k = 0; k < 3; k++) {
+            pm.K[po * 3 + k] = pVnew_ * (pVr * pickK[k] + cVl * canvasK[k]);
+            pm.S[po * 3 + k] = pVnew_ * (pVr * pickS[k] + cVl * canvasS[k]);
+          }
+          pm.V[po] = std::max(pVnew, 0.0);
+        }
+        const double cVnew = cVr + pVl;
+        if (cVnew > MinVolume) {
+          const double cVnew_ = 1. / cVnew;
+          for (int k = 0; k < 3; k++) {
+            cw.K[co * 3 + k] = cVnew_ * (cVr * canvasK[k] + pVl * pickK[k]);
+            cw.S[co * 3 + k] = cVnew_ * (cVr * canvasS[k] + pVl * pickS[k]);
+          }
+          cw.V[co] = std::max(cVnew, 0.0);
+        }
+      }
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+orc_tbrush* orc_tbrush_create(const double* tex, int32_t th, int32_t tw) {
+  auto* b = new orc_tbrush();
+  b->tex.assign(tex, tex + static_cast<size_t>(th) * tw);
+  b->th = th;
+  b->tw = tw;
+  b->make_smudge(static_cast<int32_t>(2.0 * b->radius));  // TextureBrush.hxx:25-31
+  return b;
+}
+void orc_tbrush_destroy(orc_tbrush* b) { delete b; }
+void orc_tbrush_set_radius(orc_tbrush* b, double radius) {  // TextureBrush.hxx:33-41
+  if (!(std::fabs(b->radius - radius) < 0.5)) {
+    b->radius = radius;
+    if (b->useSmudge) b->make_smudge(static_cast<int32_t>(2.0 * radius));
+  }
+}
+void orc_tbrush_dip(orc_tbrush* b, const double K[3], const double S[3]) {  // :48-50
+  for (int k = 0; k < 3; k++) {
+    b->paint[0][k] = K[k];
+    b->paint[1][k] = S[k];
+  }
+}
+void orc_tbrush_set_smudge(orc_tbrush* b, int32_t on) { b->useSmudge = on != 0; }  // :207-209
+void orc_tbrush_set_thickness_scale(orc_tbrush* b, double s) { b->thicknessScale = s; }
+// the smudge pickup map (which: 0 K, 1 S, 2 V) and its side
+const double* orc_tbrush_smudge_map(const orc_tbrush* b, int32_t which, int32_t* side) {
+  if (side) *side = b->pickDst.rows;
+  return which == 0 ? b->pickDst.K.data() : which == 1 ? b->pickDst.S.data() : b->pickDst.V.data();
+}
+
+// TextureBrush::paintStroke (TextureBrush.hxx:52-205); returns the pixels painted
+int64_t orc_tbrush_paint_stroke(orc_tbrush* b, orc_canvas* c, const double* path, int32_t n) {
+  if (n < 2) return 0;
+  std::vector<V2> arg(static_cast<size_t>(n));
+  for (int32_t i = 0; i < n; i++) arg[i] = {path[2 * i], path[2 * i + 1]};
+  std::vector<V2> v;
+  {
+    const V2 d = normalized2({arg[1].x - arg[0].x, arg[1].y - arg[0].y});
+    v.push_back({arg[0].x - d.x * b->radius, arg[0].y - d.y * b->radius});
+  }
+  v.insert(v.end(), arg.begin(), arg.end());
+  {
+    const V2 d = normalized2({arg[n - 1].x - arg[n - 2].x, arg[n - 1].y - arg[n - 2].y});
+    v.push_back({arg[n - 1].x + d.x * b->radius, arg[n - 1].y + d.y * b->radius});
+  }
+  Layer& cw = c->wet;
+  V2 bmin = v.front(), bmax = v.front();
+  for (const V2& p : v) {
+    bmin.x = std::min(bmin.x, p.x);
+    bmin.y = std::min(bmin.y, p.y);
+    bmax.x = std::max(bmax.x, p.x);
+    bmax.y = std::max(bmax.y, p.y);
+  }
+  bmin.x = std::max(bmin.x - b->radius, 0.0);
+  bmax.x = std::min(bmax.x + b->radius, static_cast<double>(cw.cols - 1));
+  bmin.y = std::max(bmin.y - b->radius, 0.0);
+  bmax.y = std::min(bmax.y + b->radius, static_cast<double>(cw.rows - 1));
+  double length = 0.0;
+  for (size_t i = 1; i < v.size(); ++i) length += norm2({v[i].x - v[i - 1].x, v[i].y - v[i - 1].y});
+  // the outline: right side reversed, then left side; uv (u, 1) then (u, 0)
+  std::vector<V2> up, down, upUv, downUv;
+  for (size_t i = 0; i < v.size(); ++i) {
+    const double u = static_cast<double>(i) / static_cast<double>(v.size() - 1);
+    const V2 cpt = spline_eval(v, u, false);
+    const V2 t = normalized2(spline_eval(v, u, true));
+    const V2 d = {-t.y, t.x};
+    up.push_back({cpt.x - b->radius * d.x, cpt.y - b->radius * d.y});
+    down.push_back({cpt.x + b->radius * d.x, cpt.y + b->radius * d.y});
+    upUv.push_back({u, 0.0});
+    downUv.push_back({u, 1.0});
+  }
+  up.insert(up.begin(), down.rbegin(), down.rend());
+  upUv.insert(upUv.begin(), downUv.rbegin(), downUv.rend());
+  const int trows = static_cast<int32_t>(bmax.y - bmin.y + 1);
+  const int tcols = static_cast<int32_t>(bmax.x - bmin.x + 1);
+  std::vector<double> tmap(static_cast<size_t>(std::max(trows, 0)) * std::max(tcols, 0), 0.0);
+  std::vector<std::pair<int, int>> pixels;
+  for (int x = static_cast<int32_t>(bmin.x); x <= static_cast<int32_t>(bmax.x); x++)
+    for (int y = static_cast<int32_t>(bmin.y); y <= static_cast<int32_t>(bmax.y); y++) {
+      if (x < 0 || x >= cw.cols || y < 0 || y >= cw.rows) continue;
+      V2 tp = barycentric_interpolate(up, {static_cast<double>(x), static_cast<double>(y)}, upUv);
+      if (tp.x < 0.0 || tp.x > 1.0 || tp.y < 0.0 || tp.y > 1.0) continue;
+      tp.x *= b->tw;
+      tp.y *= b->th;
+      const double Vtex = b->thicknessScale * interpolate(b->tex.data(), b->th, b->tw, tp.x, tp.y);
+      if (Vtex > 0.0) {
+        const int sx = x - static_cast<int32_t>(bmin.x), sy = y - static_cast<int32_t>(bmin.y);
+        if (sx >= 0 && sy >= 0 && sx < tcols && sy < trows) {
+          tmap[static_cast<size_t>(sy) * tcols + sx] = Vtex;
+          pixels.emplace_back(x, y);
+        }
+      }
+    }
+  if (b->useSmudge) smudge_run(b, c, bmin, v, length, tmap, trows, tcols);
+  for (const auto& px : pixels) {
+    const int x = px.first, y = px.second;
+    if (x < 0 || y < 0 || x >= cw.cols || y >= cw.rows) continue;
+    const int ty = std::min(trows - 1, std::max(y - static_cast<int32_t>(bmin.y), 0));
+    const int tx = std::min(tcols - 1, std::max(x - static_cast<int32_t>(bmin.x), 0));
+    const double Vtex = tmap[static_cast<size_t>(ty) * tcols + tx];
+    const size_t o = cw.idx(y, x);
+    const double Vcan = cw.V[o];
+    const double Vsum = Vcan + Vtex;
+    if (Vsum > 0.0) {
+      const double sc = 1.0 / Vsum;
+      for (int k = 0; k < 3; k++) {
+        cw.K[o * 3 + k] = (Vcan * cw.K[o * 3 + k] + Vtex * b->paint[0][k]) * sc;
+        cw.S[o * 3 + k] = (Vcan * cw.S[o * 3 + k] + Vtex * b->paint[1][k]) * sc;
+      }
+      cw.V[o] = std::max(Vtex, Vcan);
+    }
+  }
+  return static_cast<int64_t>(pixels.size());
+}
+
+}  // extern "C"

@@ -112,6 +112,17 @@ double orc_ciede2000(const double lab1[3], const double lab2[3]);
 double orc_delta_e_images(int64_t npix, const double* rgb_a, const double* rgb_b,
                           double* mean_out, int32_t nthreads);
 
+/* TextureBrush<vec3> (TextureBrush.hxx) with its Smudge; the texture is the thickness map. */
+typedef struct orc_tbrush orc_tbrush;
+orc_tbrush* orc_tbrush_create(const double* tex, int32_t th, int32_t tw);
+void orc_tbrush_destroy(orc_tbrush* b);
+void orc_tbrush_set_radius(orc_tbrush* b, double radius);
+void orc_tbrush_dip(orc_tbrush* b, const double K[3], const double S[3]);
+void orc_tbrush_set_smudge(orc_tbrush* b, int32_t on);
+void orc_tbrush_set_thickness_scale(orc_tbrush* b, double s);
+const double* orc_tbrush_smudge_map(const orc_tbrush* b, int32_t which, int32_t* side);
+int64_t orc_tbrush_paint_stroke(orc_tbrush* b, orc_canvas* c, const double* path_xy, int32_t n);
+
 #ifdef __cplusplus
 }
 #endif

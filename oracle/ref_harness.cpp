@@ -28,12 +28,14 @@
 #include "painty/renderer/FootprintBrush.hxx"
 #include "painty/renderer/PaintLayer.hxx"
 #include "painty/renderer/Renderer.hxx"
+#include "painty/renderer/TextureBrush.hxx"
 
 using painty::vec2;
 using painty::vec3;
 
 namespace {
 painty::Mat<double> g_footprint_full;
+painty::Mat<double> g_texture;  // the thickness texture the next TextureBrush loads
 }
 
 namespace cv {
@@ -55,11 +57,22 @@ namespace painty {
 namespace io {
 void imRead(const std::string&, Mat<double>& gray, bool) { gray = g_footprint_full.clone(); }
 }  // namespace io
+
+// The harness's stand-ins for the two out-of-line classes TextureBrush.hxx needs
+// (painty/renderer/src/BrushStrokeSample.cxx, painty/image/src/TextureWarp.cxx load stroke
+// samples from disk): the sample's thickness map is the registered texture.
+TextureWarp::TextureWarp() {}
+BrushStrokeSample::BrushStrokeSample(const std::string&) { _thickness_map = g_texture.clone(); }
+const Mat<double>& BrushStrokeSample::getThicknessMap() const { return _thickness_map; }
 }  // namespace painty
 
 struct ref_canvas {
   painty::Canvas<vec3> c;
   ref_canvas(int r, int cc) : c(r, cc) {}
+};
+struct ref_tbrush {
+  painty::TextureBrush<vec3> b;
+  ref_tbrush() : b("sample") {}
 };
 struct ref_brush {
   painty::FootprintBrush<vec3> b;
@@ -219,6 +232,26 @@ void ref_brush_pickup(ref_brush* b, int32_t which, double* out) {
       default: break;
     }
   }
+}
+
+// TextureBrush<vec3> (TextureBrush.hxx) with the registered thickness texture
+ref_tbrush* ref_tbrush_create(const double* tex, int32_t th, int32_t tw) {
+  g_texture = painty::Mat<double>(th, tw);
+  for (int32_t i = 0; i < th; i++)
+    for (int32_t j = 0; j < tw; j++) g_texture(i, j) = tex[static_cast<size_t>(i) * tw + j];
+  return new ref_tbrush();
+}
+void ref_tbrush_destroy(ref_tbrush* b) { delete b; }
+void ref_tbrush_set_radius(ref_tbrush* b, double r) { b->b.setRadius(r); }
+void ref_tbrush_dip(ref_tbrush* b, const double K[3], const double S[3]) {
+  b->b.dip({v3(K), v3(S)});
+}
+void ref_tbrush_set_smudge(ref_tbrush* b, int32_t on) { b->b.enableSmudge(on != 0); }
+void ref_tbrush_set_thickness_scale(ref_tbrush* b, double s) { b->b.setThicknessScale(s); }
+void ref_tbrush_paint_stroke(ref_tbrush* b, ref_canvas* c, const double* path, int32_t n) {
+  std::vector<vec2> v;
+  for (int32_t i = 0; i < n; i++) v.emplace_back(path[2 * i], path[2 * i + 1]);
+  b->b.paintStroke(v, c->c);
 }
 
 }  // extern "C"

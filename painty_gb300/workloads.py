@@ -38,6 +38,24 @@ def footprint_image(seed: int = 7, size: int = 64, cells: int = 8) -> np.ndarray
     return np.ascontiguousarray(falloff * noise)
 
 
+def stroke_texture(seed: int = 13, rows: int = 32, cols: int = 128, cells: int = 8) -> np.ndarray:
+    """Thickness texture of a brush-stroke sample (stands in for painty's scanned stroke
+    samples): a bristle profile across the width (rows) times smoothed value noise along the
+    length, values in [0, 1], tapering to 0 at the stroke's ends and sides."""
+    rng = np.random.default_rng(seed)
+    across = (np.arange(rows) + 0.5) / rows
+    bristles = 0.6 + 0.4 * rng.random(rows)
+    side = np.clip(1.0 - (2.0 * across - 1.0) ** 4, 0.0, 1.0) * bristles
+    lattice = rng.random(cells + 1)
+    x = (np.arange(cols) + 0.5) / cols * cells
+    i0 = np.minimum(x.astype(np.int64), cells - 1)
+    t = x - i0
+    t = t * t * (3.0 - 2.0 * t)
+    along = lattice[i0] * (1 - t) + lattice[i0 + 1] * t
+    along *= np.clip(np.minimum(x, cells - x) / 0.75, 0.0, 1.0)
+    return np.ascontiguousarray(side[:, None] * along[None, :])
+
+
 def pigments(seed: int = 11, n: int = 14):
     rng = np.random.default_rng(seed)
     K = rng.uniform(0.01, 5.0, (n, 3))
