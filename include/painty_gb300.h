@@ -216,6 +216,42 @@ painty_status painty_paint_batch(painty_canvas* const* canvases, painty_brush* c
  * No counterpart in painty. */
 painty_status painty_batch_last_shape(int32_t* cluster, int32_t* clusters);
 
+/* ------------------------------------------------------------------ texture brush
+ * TextureBrush<vec3> (painty/renderer/TextureBrush.hxx:20-237) with its Smudge<vec3>
+ * (painty/renderer/Smudge.hxx:16-229). The texture is the brush-stroke sample's thickness
+ * map (BrushStrokeSample::getThicknessMap), rows x cols doubles, row-major; painty's
+ * constructor loads it from the sample directory, which this interface leaves to the
+ * caller. A brush binds to F64 canvases or to F32/F16/BF16 canvases at its first stroke. */
+typedef struct painty_texture_brush painty_texture_brush;
+/* replaces TextureBrush(sampleDir) (:25-31): paint {0.1, 0.1, 0.1} x2, smudge on, radius 0 */
+painty_status painty_texture_brush_create(const double* texture, int32_t rows, int32_t cols,
+                                          painty_texture_brush** out);
+painty_status painty_texture_brush_destroy(painty_texture_brush* brush);
+/* replaces setRadius (:33-41): no change unless |radius - current| >= 0.5; a change makes a
+ * new smudge of side int(2 radius) (clear pickup map, rotation 0) */
+painty_status painty_texture_brush_set_radius(painty_texture_brush* brush, double radius);
+/* replaces dip (:48-50) */
+painty_status painty_texture_brush_dip(painty_texture_brush* brush, const double K[3],
+                                       const double S[3]);
+/* replaces enableSmudge (:207-209) */
+painty_status painty_texture_brush_set_smudge(painty_texture_brush* brush, int32_t enable);
+/* replaces BrushBase::setThicknessScale (painty/renderer/BrushBase.hxx:31-33) */
+painty_status painty_texture_brush_set_thickness_scale(painty_texture_brush* brush,
+                                                       double scale);
+/* replaces paintStroke(verts, canvas) (:52-205): path_xy = n (x, y) pairs (host, n >= 2 to
+ * paint). painted_out (may be null) receives the pixels the stroke deposited on. A stroke
+ * whose bounds lie off the canvas paints nothing (painty fails on it). Synchronises the
+ * stream. */
+painty_status painty_texture_brush_paint_stroke(painty_canvas* canvas,
+                                                painty_texture_brush* brush,
+                                                const double* path_xy, int32_t n,
+                                                int64_t* painted_out, void* stream);
+/* the smudge pickup map (Smudge.hxx _pickupMapDst): plane K/S (side*side*3 interleaved) or
+ * V (side*side) doubles; side_out receives the side; host may be null to query it */
+painty_status painty_texture_brush_smudge_map(const painty_texture_brush* brush,
+                                              painty_plane plane, double* host,
+                                              int32_t* side_out, void* stream);
+
 /* ------------------------------------------------------------------ serving
  * A continuous-batching render server (no counterpart in painty, whose SbrRenderThread runs
  * one stroke at a time on a GL thread: painty/renderer/SbrRenderThread.hxx:50-74). Requests

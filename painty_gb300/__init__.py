@@ -92,6 +92,14 @@ _sig("painty_stroke", _P, _P, _P, _I32, _D, C.POINTER(_I64), _P)
 _sig("painty_mix_paint", _P, _I32, _P, _P, _P, _P)
 _sig("painty_paint_batch", _P, _P, _I32, _P, _I64, _P, _I64, C.POINTER(_I64), _P)
 _sig("painty_batch_last_shape", C.POINTER(_I32), C.POINTER(_I32))
+_sig("painty_texture_brush_create", _P, _I32, _I32, C.POINTER(_P))
+_sig("painty_texture_brush_destroy", _P)
+_sig("painty_texture_brush_set_radius", _P, _D)
+_sig("painty_texture_brush_dip", _P, _P, _P)
+_sig("painty_texture_brush_set_smudge", _P, _I32)
+_sig("painty_texture_brush_set_thickness_scale", _P, _D)
+_sig("painty_texture_brush_paint_stroke", _P, _P, _P, _I32, C.POINTER(_I64), _P)
+_sig("painty_texture_brush_smudge_map", _P, C.c_int, _P, C.POINTER(_I32), _P)
 
 # painty_stroke_desc (include/painty_gb300.h)
 STROKE_DESC = np.dtype([("canvas", np.int32), ("npoints", np.int32), ("first_point", np.int64),
@@ -409,6 +417,59 @@ class FootprintBrush:
         _check(_lib.painty_stroke(canvas._h, self._h, _ptr(p), p.shape[0], float(spacing),
                                   C.byref(n), _stream(stream)))
         return n.value
+
+
+class TextureBrush:
+    """painty::TextureBrush<vec3> (TextureBrush.hxx:20-237) with its Smudge (Smudge.hxx).
+
+    `texture` is the brush-stroke sample's thickness map (rows x cols, values >= 0) that
+    stands in for the sample directory painty's constructor reads.
+    """
+
+    def __init__(self, texture: np.ndarray):
+        t = np.ascontiguousarray(texture, dtype=np.float64)
+        h = _P()
+        _check(_lib.painty_texture_brush_create(_ptr(t), t.shape[0], t.shape[1], C.byref(h)))
+        self._h = h.value
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            _lib.painty_texture_brush_destroy(self._h)
+            self._h = None
+
+    def setRadius(self, radius: float) -> None:
+        _check(_lib.painty_texture_brush_set_radius(self._h, float(radius)))
+
+    def dip(self, paint) -> None:
+        K = np.ascontiguousarray(paint[0], dtype=np.float64)
+        S = np.ascontiguousarray(paint[1], dtype=np.float64)
+        _check(_lib.painty_texture_brush_dip(self._h, _ptr(K), _ptr(S)))
+
+    def enableSmudge(self, enable: bool) -> None:
+        _check(_lib.painty_texture_brush_set_smudge(self._h, 1 if enable else 0))
+
+    def setThicknessScale(self, scale: float) -> None:
+        _check(_lib.painty_texture_brush_set_thickness_scale(self._h, float(scale)))
+
+    def paintStroke(self, path: np.ndarray, canvas: Canvas, stream=None) -> int:
+        """Paints the stroke; returns the number of pixels it deposited on."""
+        p = np.ascontiguousarray(path, dtype=np.float64).reshape(-1, 2)
+        n = _I64()
+        _check(_lib.painty_texture_brush_paint_stroke(canvas._h, self._h, _ptr(p), p.shape[0],
+                                                      C.byref(n), _stream(stream)))
+        return n.value
+
+    def getSmudgeMap(self, plane: str) -> np.ndarray:
+        """The smudge pickup map's K / S (side, side, 3) or V (side, side)."""
+        side = _I32()
+        _check(_lib.painty_texture_brush_smudge_map(self._h, PLANE[plane], None, C.byref(side),
+                                                    None))
+        n = side.value
+        out = np.empty((n, n) if plane == "V" else (n, n, 3), dtype=np.float64)
+        if n:
+            _check(_lib.painty_texture_brush_smudge_map(self._h, PLANE[plane], _ptr(out),
+                                                        C.byref(side), None))
+        return out
 
 
 def mix_single_paint(weights: np.ndarray, palette_K: np.ndarray, palette_S: np.ndarray):

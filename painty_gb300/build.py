@@ -41,10 +41,17 @@ def sources() -> list[Path]:
 
 # Host code is built without floating-point contraction so the footprint resample and the
 # stroke expansion give the same bits on x86-64 and aarch64 (and as painty's double code).
+# Translation units listed in NO_FMAD also keep device code free of fused multiply-adds: their
+# double kernels repeat painty's arithmetic as written (the others use explicit intrinsics).
+NO_FMAD = {"texture.cu"}
+
+
 def _compile(src: Path, obj: Path) -> None:
     cmd = [nvcc(), *ARCH, "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-Wall", "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr", "-I", str(ROOT / "include"),
            "-I", str(CSRC), "-c", str(src), "-o", str(obj)]
+    if src.name in NO_FMAD:
+        cmd.insert(1, "--fmad=false")
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src.name}:\n{r.stdout}\n{r.stderr}")

@@ -181,39 +181,6 @@ __device__ __forceinline__ M* pickup_plane(const StampArgs<TK, TV>& a, int p) {
   return p < 3 ? a.pK[p] : (p < 6 ? a.pS[p - 3] : a.pV);
 }
 
-// The record of one pixel of a packed layer: 8 elements of the storage size (K r,g,b, S r,g,b,
-// V, pad) read and written as 16-byte words.
-template <class TK, class TV>
-union PixRec {
-  static constexpr int kWords = 8 * sizeof(TK) / 16;
-  uint4 w[kWords];
-  TK k[8];
-  TV v[8];
-};
-template <bool CG, class TK, class TV>
-__device__ __forceinline__ PixRec<TK, TV> load_rec(const void* base, int c) {
-  using R = PixRec<TK, TV>;
-  const uint4* p = static_cast<const uint4*>(base) + static_cast<int64_t>(c) * R::kWords;
-  R r;
-#pragma unroll
-  for (int i = 0; i < R::kWords; i++) {
-    if constexpr (CG) r.w[i] = __ldcg(p + i);
-    else r.w[i] = p[i];
-  }
-  return r;
-}
-template <class TK, class TV>
-__device__ __forceinline__ void store_rec(void* base, int c, const PixRec<TK, TV>& r) {
-  using R = PixRec<TK, TV>;
-  uint4* p = static_cast<uint4*>(base) + static_cast<int64_t>(c) * R::kWords;
-#pragma unroll
-  for (int i = 0; i < R::kWords; i++) p[i] = r.w[i];
-}
-template <class TK, class TV>
-__device__ __forceinline__ TV* rec_v(void* base, int c) {
-  return reinterpret_cast<TV*>(static_cast<char*>(base) + static_cast<int64_t>(c) * 8 * sizeof(TK)) + 6;
-}
-
 // A pickup-map cell record (K r,g,b, S r,g,b, V, pad) as 16-byte words.
 template <class M>
 union CellRec {

@@ -1,0 +1,845 @@
+// texture.cu -- the texture brush: painty's TextureBrush<vec3> with its Smudge<vec3>
+// (painty/renderer/TextureBrush.hxx:20-237, painty/renderer/Smudge.hxx:16-229) on the GPU.
+//
+// A stroke is three launches:
+//  1. thickness: every pixel of the stroke's bounding box finds its texture coordinates by
+//     generalized barycentric interpolation over the stroke outline (Math.hxx:72-147), samples
+//     the thickness texture bilinearly and records the thickness map and its maximum;
+//  2. smudge: one CTA walks the spine in painty's u steps; each step rotates the smudge pickup
+//     map to the new heading (bilinear) and exchanges paint between it and the canvas pixels
+//     under it (every cell and canvas pixel once per step, so a step is parallel);
+//  3. deposit: each painted pixel blends the brush paint in by volume, V = max(Vtex, Vcan).
+// The spine, the outline and the per-step rotations are computed on the host with painty's
+// double arithmetic (this file's device code is built without fused multiply-adds, so F64
+// storage reproduces painty bit for bit). Outline geometry and texture sampling are double in
+// every storage mode; the smudge and the deposit run in the storage's math type.
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <type_traits>
+#include <vector>
+
+#include "device_common.cuh"
+#include "internal.h"
+
+// TextureBrush<vec3>: host copy of the brush and its device buffers.
+struct painty_texture_brush {
+  std::vector<double> tex;  // thickness texture (th x tw), painty's BrushStrokeSample map
+  int32_t th = 0, tw = 0;
+  double radius = 0.0;          // TextureBrush.hxx:228
+  double thicknessScale = 1.0;  // BrushBase.hxx _thicknessScale
+  double paintK[3] = {0.1, 0.1, 0.1}, paintS[3] = {0.1, 0.1, 0.1};  // TextureBrush.hxx:28-30
+  bool useSmudge = true;        // TextureBrush.hxx:236
+  // Smudge (Smudge.hxx:22-36, 147-158): maps side x side, maxSize made odd
+  int32_t side = 0, maxSize = 1;
+  double rotation = 0.0;
+  bool maps_zero = true;  // the device maps must be cleared before their next use
+  int bound = -1;         // -1 unbound, 0 FP32 math, 1 FP64 math
+  void* d_tex = nullptr;
+  void* d_maps = nullptr;  // two maps of 7 planes of side^2 cells; the first is the state
+  size_t d_maps_bytes = 0;
+  void make_smudge(int32_t size) {
+    side = size;
+    maxSize = (size % 2) == 0 ? size + 1 : size;
+    rotation = 0.0;
+    maps_zero = true;
+  }
+};
+
+namespace pg {
+namespace {
+
+constexpr int kSmudgeThreads = 1024;
+constexpr int kTexThreads = 256;
+
+struct D2 {
+  double x, y;
+};
+
+// ---------------------------------------------------------------------- host geometry
+// Spline.hxx:27-73 and SplineEval (:183-231) in painty's operation order
+double cr_pos_h(double p_1, double p0, double p1, double p2, double t) {
+  constexpr double tau = 0.5;
+  const double t2 = t * t, t3 = t2 * t;
+  const double b1 = -tau * t + 2.0 * tau * t2 - tau * t3;
+  const double b2 = 1.0 + (tau - 3.0) * t2 + (2.0 - tau) * t3;
+  const double b3 = tau * t + (3.0 - 2.0 * tau) * t2 + (tau - 2.0) * t3;
+  const double b4 = -tau * t2 + tau * t3;
+  return p_1 * b1 + p0 * b2 + p1 * b3 + p2 * b4;
+}
+double cr_der_h(double p_1, double p0, double p1, double p2, double t) {
+  constexpr double tau = 0.5;
+  const double t2 = t * t;
+  const double b1 = tau * (-3.0 * t2 + 4.0 * t - 1.0);
+  const double b2 = -t * (-2.0 * tau + 3.0 * (tau - 2.0) * t + 6.0);
+  const double b3 = (t - 1.0) * (3.0 * (tau - 2.0) * t - tau);
+  const double b4 = tau * t * (3.0 * t - 2.0);
+  return p_1 * b1 + p0 * b2 + p1 * b3 + p2 * b4;
+}
+D2 spline_h(const std::vector<D2>& p, double u, bool deriv) {
+  const auto n = static_cast<int64_t>(p.size());
+  const double x = static_cast<double>(n - 1) * u;
+  const int32_t index = static_cast<int32_t>(x);
+  const double t = x - std::floor(x);
+  auto at = [&](int32_t i) -> const D2& {
+    if (i < 0) return p.front();
+    if (i >= static_cast<int32_t>(n)) return p.back();
+    return p[static_cast<size_t>(i)];
+  };
+  const D2 &a = at(index - 1), &b = at(index), &c = at(index + 1), &d = at(index + 2);
+  if (deriv) return {cr_der_h(a.x, b.x, c.x, d.x, t), cr_der_h(a.y, b.y, c.y, d.y, t)};
+  return {cr_pos_h(a.x, b.x, c.x, d.x, t), cr_pos_h(a.y, b.y, c.y, d.y, t)};
+}
+D2 normalized_h(const D2& v) {  // Eigen normalized(): v / sqrt(squaredNorm), unchanged at 0
+  const double n = v.x * v.x + v.y * v.y;
+  if (n > 0.0) {
+    const double r = std::sqrt(n);
+    return {v.x / r, v.y / r};
+  }
+  return v;
+}
+double normalize_angle_h(double a) {  // Smudge.hxx:201-211
+  constexpr double PI = 3.14159265358979323846;
+  while (a <= -0.5 * PI) a += PI;
+  while (a > 0.5 * PI) a -= PI;
+  return a;
+}
+
+// ---------------------------------------------------------------------- device code
+// generalizedBarycentricCoordinatesInterpolate (Math.hxx:72-147) of the outline `poly` at
+// (px, py) with texture coordinates `uv` (n > 1 vertices, global memory).
+__device__ D2 barycentric_uv(const double2* poly, const double2* uv, int n, double px,
+                             double py) {
+  constexpr double Eps = 2.220446049250313080847e-16 * 100.0;
+  // pass 1: r, A, D and the early returns (on a vertex, or on an edge)
+  double rprev = 0.0, Aprev = 0.0, Dprev = 0.0;  // of vertex n-1 (filled at i = n-1)
+  double r0 = 0.0, A0 = 0.0, D0 = 0.0;
+  for (int i = 0; i < n; i++) {
+    const double2 pi = poly[i], pj = poly[i + 1 < n ? i + 1 : 0];
+    const double sx = pi.x - px, sy = pi.y - py;
+    const double tx = pj.x - px, ty = pj.y - py;
+    const double r = sqrt(sx * sx + sy * sy);
+    if (fabs(r - 0.0) < Eps) return {uv[i].x, uv[i].y};
+    const double det = sx * ty - tx * sy;
+    const double A = det / 2.0;
+    const double D = sx * tx + sy * ty;
+    if (fabs(A - 0.0) < Eps && D < 0.0) {
+      const double ri1 = sqrt(tx * tx + ty * ty);
+      const double2 fi1 = uv[i + 1 < n ? i + 1 : 0];
+      const double k = 1.0 / (r + ri1);
+      return {(ri1 * uv[i].x + r * fi1.x) * k, (ri1 * uv[i].y + r * fi1.y) * k};
+    }
+    if (i == 0) {
+      r0 = r;
+      A0 = A;
+      D0 = D;
+    }
+    if (i == n - 1) {
+      rprev = r;
+      Aprev = A;
+      Dprev = D;
+    }
+  }
+  // pass 2: weights, in painty's order
+  double fx = 0.0, fy = 0.0, W = 0.0;
+  double r_1 = rprev, A_1 = Aprev, D_1 = Dprev;  // of vertex i-1
+  double ri = r0, Ai = A0, Di = D0;
+  for (int i = 0; i < n; i++) {
+    // r, A, D of vertex i+1 (recomputed rather than stored)
+    double rn, An, Dn;
+    if (i + 1 < n) {
+      const double2 pi = poly[i + 1], pj = poly[i + 2 < n ? i + 2 : 0];
+      const double sx = pi.x - px, sy = pi.y - py;
+      const double tx = pj.x - px, ty = pj.y - py;
+      rn = sqrt(sx * sx + sy * sy);
+      An = (sx * ty - tx * sy) / 2.0;
+      Dn = sx * tx + sy * ty;
+    } else {
+      rn = r0;
+      An = A0;
+      Dn = D0;
+    }
+    double w = 0.0;
+    if (A_1 != 0.0) w = w + (r_1 - D_1 / ri) / A_1;
+    if (Ai != 0.0) w = w + (rn - Di / ri) / Ai;
+    fx = fx + w * uv[i].x;
+    fy = fy + w * uv[i].y;
+    W = W + w;
+    r_1 = ri;
+    A_1 = Ai;
+    D_1 = Di;
+    ri = rn;
+    Ai = An;
+    Di = Dn;
+  }
+  if (!(fabs(W - 0.0) < Eps)) {
+    const double k = 1.0 / W;
+    return {fx * k, fy * k};
+  }
+  return {uv[0].x, uv[0].y};
+}
+
+__device__ __forceinline__ int reflect_d(int p, int len) {  // OpenCV BORDER_REFLECT
+  if (len == 1) return 0;
+  for (int guard = 0; (p < 0 || p >= len) && guard < 64; guard++) p = p < 0 ? -p - 1 : len - 1 - (p - len);
+  return min(max(p, 0), len - 1);
+}
+
+// Mat.hxx:68-103: bilinear sample with BORDER_REFLECT (double)
+__device__ double interp_d(const double* img, int rows, int cols, double px, double py) {
+  const int x = static_cast<int>(floor(px)), y = static_cast<int>(floor(py));
+  const int x0 = reflect_d(x, cols), x1 = reflect_d(x + 1, cols);
+  const int y0 = reflect_d(y, rows), y1 = reflect_d(y + 1, rows);
+  const double a = px - static_cast<double>(x), c = py - static_cast<double>(y);
+  return (img[y0 * cols + x0] * (1.0 - a) + img[y0 * cols + x1] * a) * (1.0 - c) +
+         (img[y1 * cols + x0] * (1.0 - a) + img[y1 * cols + x1] * a) * c;
+}
+
+struct TexArgs {
+  const double2* poly;
+  const double2* uv;
+  int npoly;
+  const double* tex;
+  int th, tw;
+  double scale;
+  int x0, y0, nx, ny;     // the bounding-box loop (painty's int(boundMin) .. int(boundMax))
+  int bx, by;             // int(boundMin): thickness-map origin
+  int trows, tcols;       // thickness-map size
+  int rows, cols;         // canvas
+};
+
+// Launch 1: thickness map (math type M), its maximum (non-negative values compare as their
+// bit patterns) and the number of painted pixels; stats = {max bits, count}.
+template <class M>
+__global__ void __launch_bounds__(kTexThreads) tb_thickness_kernel(const TexArgs a, M* tmap,
+                                                                   unsigned long long* stats) {
+  using Bits = typename std::conditional<sizeof(M) == 8, unsigned long long, unsigned>::type;
+  const int64_t n = static_cast<int64_t>(a.nx) * a.ny;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  Bits vmax = 0;
+  unsigned count = 0;
+  // every thread runs the same trip count, so the warp reductions below see all lanes
+  for (int64_t base = static_cast<int64_t>(blockIdx.x) * blockDim.x; base < n; base += stride) {
+    const int64_t i = base + threadIdx.x;
+    if (i >= n) continue;
+    const int y = a.y0 + static_cast<int>(i / a.nx), x = a.x0 + static_cast<int>(i % a.nx);
+    if (x < 0 || x >= a.cols || y < 0 || y >= a.rows) continue;
+    D2 tp = barycentric_uv(a.poly, a.uv, a.npoly, static_cast<double>(x), static_cast<double>(y));
+    if (tp.x < 0.0 || tp.x > 1.0 || tp.y < 0.0 || tp.y > 1.0) continue;
+    tp.x *= a.tw;
+    tp.y *= a.th;
+    const double vtex = a.scale * interp_d(a.tex, a.th, a.tw, tp.x, tp.y);
+    if (!(vtex > 0.0)) continue;
+    const int s = x - a.bx, t = y - a.by;
+    if (s < 0 || t < 0 || s >= a.tcols || t >= a.trows) continue;
+    const M v = static_cast<M>(vtex);
+    if (!(v > M(0))) continue;
+    tmap[static_cast<int64_t>(t) * a.tcols + s] = v;
+    Bits vb;
+    if constexpr (sizeof(M) == 8) vb = static_cast<Bits>(__double_as_longlong(v));
+    else vb = __float_as_uint(v);
+    vmax = vb > vmax ? vb : vmax;
+    count++;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const Bits ov = __shfl_xor_sync(0xffffffffu, vmax, o);
+    vmax = ov > vmax ? ov : vmax;
+    count += __shfl_xor_sync(0xffffffffu, count, o);
+  }
+  if ((threadIdx.x & 31) == 0 && count > 0) {
+    if constexpr (sizeof(M) == 8) atomicMax(stats, vmax);
+    else atomicMax(reinterpret_cast<unsigned*>(stats), vmax);
+    atomicAdd(stats + 1, static_cast<unsigned long long>(count));
+  }
+}
+
+// One smudge step in the math type M: spine point, cos / sin of the heading change and the
+// map's top-left canvas pixel.
+template <class M>
+struct SmudgeStep {
+  M cx, cy;
+  M c, s;
+  int roi_x, roi_y;
+};
+
+template <class M>
+struct SmudgeArgs {
+  void* canvas;   // packed canvas records
+  int rows, cols;
+  int64_t pitch;
+  M* maps;        // two pickup maps of 7 planes (K r,g,b, S r,g,b, V) of side^2 cells each;
+                  // the first is the smudge's state between strokes
+  int side;
+  M ctr, radius;  // maxSize / 2 (the rotation centre) and maxSize * 0.5 (the exchange radius)
+  const M* tmap;
+  int trows, tcols;
+  // int(cp - boundMin) of painty, in integers: boundMin = b0 + f with f in [0, 1); m = cp - b0
+  // gives m - 1 for m >= 1 and f > 0, else m
+  int bx0, by0, bxf, byf;
+  const SmudgeStep<M>* steps;
+  int64_t nsteps;
+  const unsigned long long* maxbits;
+  M pickupRate, depositionRate;
+  uint32_t seed;  // stochastic rounding of 16-bit canvas stores (per stroke)
+};
+
+// Cells a thread exchanges per batch (its canvas loads are in flight together).
+template <class M> constexpr int kSmudgeBatch = sizeof(M) == 8 ? 2 : 4;
+
+// Launch 2: Smudge::smudge (Smudge.hxx:38-145) with updateOrientation (:160-199), one CTA
+// walking the steps in order. Per step the map is rotated from one buffer into the other
+// (painty copies dst to src, then rotates src into dst: cells that rotate in from outside keep
+// their own value), then each cell under the stroke exchanges paint with its canvas pixel.
+// SM: both maps staged in shared memory (loaded at the start, written back at the end).
+template <class TK, class TV, class M, bool SM>
+__global__ void __launch_bounds__(kSmudgeThreads, 1) tb_smudge_kernel(const __grid_constant__ SmudgeArgs<M> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int J = kSmudgeBatch<M>;
+  const int tid = threadIdx.x, T = blockDim.x;
+  const int side = a.side, cells = side * side;
+  M* cur;
+  M* nxt;
+  if constexpr (SM) {
+    cur = reinterpret_cast<M*>(smem_raw);
+    nxt = cur + 7 * cells;
+    for (int i = tid; i < 7 * cells; i += T) cur[i] = a.maps[i];
+    __syncthreads();
+  } else {
+    cur = a.maps;
+    nxt = a.maps + 7 * cells;
+  }
+  M maxD;
+  if constexpr (sizeof(M) == 8)
+    maxD = __longlong_as_double(static_cast<long long>(*a.maxbits));
+  else
+    maxD = __uint_as_float(static_cast<unsigned>(*a.maxbits));
+  // 1 / maxD: FP32 multiplies by it; FP64 divides as painty does
+  const M rmaxD = M(1) / maxD;
+  const M c0 = a.ctr, radius = a.radius, fside = static_cast<M>(side);
+  SmudgeStep<M> st = a.steps[0];
+  for (int64_t k = 0; k < a.nsteps; k++) {
+    // the next step's parameters load while this one runs
+    const SmudgeStep<M> st_next = a.steps[k + 1 < a.nsteps ? k + 1 : k];
+    // updateOrientation: nxt = cur rotated about the map centre
+    const M cs = st.c, sn = st.s;
+    for (int i = tid; i < cells; i += T) {
+      const int y = i / side, x = i - y * side;
+      const M px = static_cast<M>(x) - c0, py = static_cast<M>(y) - c0;
+      const M qx = px * cs - py * sn + c0;
+      const M qy = px * sn + py * cs + c0;
+      if (qx < M(0) || qy < M(0) || qx >= fside || qy >= fside) {
+#pragma unroll
+        for (int q = 0; q < 7; q++) nxt[q * cells + i] = cur[q * cells + i];
+      } else {
+        // 0 <= q < side: the BORDER_REFLECT neighbours are q's cell and the next one, which
+        // reflects back onto the last cell at the border
+        const int fx = static_cast<int>(floor(qx)), fy = static_cast<int>(floor(qy));
+        const int x0 = fx, x1 = min(fx + 1, side - 1);
+        const int y0 = fy, y1 = min(fy + 1, side - 1);
+        const M wa = qx - static_cast<M>(fx), wc = qy - static_cast<M>(fy);
+        const int o00 = y0 * side + x0, o01 = y0 * side + x1;
+        const int o10 = y1 * side + x0, o11 = y1 * side + x1;
+#pragma unroll
+        for (int q = 0; q < 7; q++) {
+          const M* s = cur + q * cells;
+          nxt[q * cells + i] = (s[o00] * (M(1) - wa) + s[o01] * wa) * (M(1) - wc) +
+                               (s[o10] * (M(1) - wa) + s[o11] * wa) * wc;
+        }
+      }
+    }
+    __syncthreads();
+    // paint exchange between the pickup map and the canvas under it; a cell and its canvas
+    // pixel are touched by no other cell of the step
+    for (int base = 0; base < cells; base += J * T) {
+      int cid[J], pix[J];
+      M D[J];
+#pragma unroll
+      for (int j = 0; j < J; j++) {
+        const int i = base + j * T + tid;
+        cid[j] = -1;
+        D[j] = M(0);
+        if (i >= cells) continue;
+        const int y = i / side, x = i - y * side;
+        const int cpx = x + st.roi_x, cpy = y + st.roi_y;
+        if (cpx < 0 || cpy < 0 || cpx >= a.cols || cpy >= a.rows) continue;
+        const int mx = cpx - a.bx0, my = cpy - a.by0;
+        const int tpx = (a.bxf && mx >= 1) ? mx - 1 : mx;
+        const int tpy = (a.byf && my >= 1) ? my - 1 : my;
+        if (tpx < 0 || tpy < 0 || tpx >= a.tcols || tpy >= a.trows) continue;
+        const M dx = st.cx - static_cast<M>(cpx);
+        const M dy = st.cy - static_cast<M>(cpy);
+        if (sqrt(dx * dx + dy * dy) > radius) continue;
+        D[j] = __ldg(a.tmap + static_cast<int64_t>(tpy) * a.tcols + tpx);
+        cid[j] = i;
+        pix[j] = static_cast<int>(static_cast<int64_t>(cpy) * a.pitch + cpx);
+      }
+      PixRec<TK, TV> cr[J];
+#pragma unroll
+      for (int j = 0; j < J; j++)
+        if (cid[j] >= 0 && D[j] > M(0)) cr[j] = load_rec<false, TK, TV>(a.canvas, pix[j]);
+#pragma unroll
+      for (int j = 0; j < J; j++) {
+        if (cid[j] < 0 || !(D[j] > M(0))) continue;
+        const int i = cid[j];
+        const M cV = ld_elem<M>(&cr[j].v[6]), pV = nxt[6 * cells + i];
+        M cVl, pVl;
+        if constexpr (sizeof(M) == 8) {
+          cVl = cV * a.depositionRate * D[j] / maxD;
+          pVl = pV * a.pickupRate * D[j] / maxD;
+        } else {
+          cVl = cV * a.depositionRate * D[j] * rmaxD;
+          pVl = pV * a.pickupRate * D[j] * rmaxD;
+        }
+        const M cVr = cV - cVl;
+        const M pVr = pV - pVl;
+        M cK[6], pK[6];
+#pragma unroll
+        for (int q = 0; q < 6; q++) {
+          cK[q] = ld_elem<M>(&cr[j].k[q]);
+          pK[q] = nxt[q * cells + i];
+        }
+        constexpr double MinVolume = 0.001;
+        const M pVnew = pVr + cVl;
+        if (pVnew > M(MinVolume)) {
+          const M inv = M(1) / pVnew;
+#pragma unroll
+          for (int q = 0; q < 6; q++) nxt[q * cells + i] = inv * (pVr * pK[q] + cVl * cK[q]);
+          nxt[6 * cells + i] = pVnew > M(0) ? pVnew : M(0);
+        }
+        const M cVnew = cVr + pVl;
+        if (cVnew > M(MinVolume)) {
+          // 16-bit storage rounds stochastically: a step moves a pixel by a small fraction of
+          // the difference, which round-to-nearest would drop (bits from stroke, step, pixel)
+          uint32_t h[4] = {0u, 0u, 0u, 0u};
+          if constexpr (sizeof(TK) == 2) {
+            h[0] = hash32(hash32(a.seed + static_cast<uint32_t>(k)) ^
+                          (static_cast<uint32_t>(pix[j]) * 0x9e3779b1u));
+#pragma unroll
+            for (int q = 1; q < 4; q++) h[q] = hash32(h[q - 1] + 0x632be5abu);
+          }
+          const M inv = M(1) / cVnew;
+#pragma unroll
+          for (int q = 0; q < 6; q++)
+            st_elem_sr<M>(&cr[j].k[q], inv * (cVr * cK[q] + pVl * pK[q]),
+                          (q & 1) ? h[q >> 1] >> 16 : h[q >> 1]);
+          st_elem_sr<M>(&cr[j].v[6], cVnew > M(0) ? cVnew : M(0), h[3]);
+          store_rec<TK, TV>(a.canvas, pix[j], cr[j]);
+        }
+      }
+    }
+    __syncthreads();
+    M* t = cur;
+    cur = nxt;
+    nxt = t;
+    st = st_next;
+  }
+  // the state map: write the current map back to the first global map
+  if (SM || cur != a.maps)
+    for (int i = tid; i < 7 * cells; i += T) a.maps[i] = cur[i];
+}
+
+template <class M>
+struct DepositArgs {
+  void* canvas;
+  int rows, cols;
+  int64_t pitch;
+  const M* tmap;
+  int trows, tcols;
+  int x0, y0, nx, ny, bx, by;
+  M K[3], S[3];
+};
+
+// Launch 3: the deposit over the painted pixels (TextureBrush.hxx:179-204)
+template <class TK, class TV, class M>
+__global__ void __launch_bounds__(kTexThreads) tb_deposit_kernel(const DepositArgs<M> a) {
+  const int64_t n = static_cast<int64_t>(a.nx) * a.ny;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int y = a.y0 + static_cast<int>(i / a.nx), x = a.x0 + static_cast<int>(i % a.nx);
+    if (x < 0 || x >= a.cols || y < 0 || y >= a.rows) continue;
+    const int s = x - a.bx, t = y - a.by;
+    if (s < 0 || t < 0 || s >= a.tcols || t >= a.trows) continue;
+    const M vtex = a.tmap[static_cast<int64_t>(t) * a.tcols + s];
+    if (!(vtex > M(0))) continue;  // not a painted pixel
+    const int c = static_cast<int>(static_cast<int64_t>(y) * a.pitch + x);
+    PixRec<TK, TV> r = load_rec<false, TK, TV>(a.canvas, c);
+    const M vcan = ld_elem<M>(&r.v[6]);
+    const M vsum = vcan + vtex;
+    if (!(vsum > M(0))) continue;
+    const M sc = M(1) / vsum;
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      const M kk = ld_elem<M>(&r.k[q]), ss = ld_elem<M>(&r.k[3 + q]);
+      st_elem<M>(&r.k[q], (vcan * kk + vtex * a.K[q]) * sc);
+      st_elem<M>(&r.k[3 + q], (vcan * ss + vtex * a.S[q]) * sc);
+    }
+    st_elem<M>(&r.v[6], vtex > vcan ? vtex : vcan);
+    store_rec<TK, TV>(a.canvas, c, r);
+  }
+}
+
+size_t align256(size_t n) { return (n + 255) / 256 * 256; }
+
+int max_dyn_smem() {
+  int dev = 0, v = 0;
+  PG_CUDA(cudaGetDevice(&dev));
+  PG_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  return v;
+}
+
+int grid_of(int64_t n, int block) {
+  return static_cast<int>(std::max<int64_t>(1, std::min<int64_t>((n + block - 1) / block, 152 * 16)));
+}
+
+// TextureBrush::paintStroke (TextureBrush.hxx:52-205); returns the pixels painted.
+template <class TK, class TV>
+int64_t paint_texture_stroke(painty_canvas* c, painty_texture_brush* b, const double* path,
+                             int32_t n, cudaStream_t st) {
+  using M = typename MathOf<TK>::type;
+  if (n < 2) return 0;
+  const int rows = c->wet.rows, cols = c->wet.cols;
+  std::vector<D2> arg(static_cast<size_t>(n));
+  for (int32_t i = 0; i < n; i++) arg[i] = {path[2 * i], path[2 * i + 1]};
+  std::vector<D2> v;
+  {
+    const D2 d = normalized_h({arg[1].x - arg[0].x, arg[1].y - arg[0].y});
+    v.push_back({arg[0].x - d.x * b->radius, arg[0].y - d.y * b->radius});
+  }
+  v.insert(v.end(), arg.begin(), arg.end());
+  {
+    const D2 d = normalized_h({arg[n - 1].x - arg[n - 2].x, arg[n - 1].y - arg[n - 2].y});
+    v.push_back({arg[n - 1].x + d.x * b->radius, arg[n - 1].y + d.y * b->radius});
+  }
+  D2 bmin = v.front(), bmax = v.front();
+  for (const D2& p : v) {
+    bmin.x = std::min(bmin.x, p.x);
+    bmin.y = std::min(bmin.y, p.y);
+    bmax.x = std::max(bmax.x, p.x);
+    bmax.y = std::max(bmax.y, p.y);
+  }
+  bmin.x = std::max(bmin.x - b->radius, 0.0);
+  bmax.x = std::min(bmax.x + b->radius, static_cast<double>(cols - 1));
+  bmin.y = std::max(bmin.y - b->radius, 0.0);
+  bmax.y = std::min(bmax.y + b->radius, static_cast<double>(rows - 1));
+  double length = 0.0;
+  for (size_t i = 1; i < v.size(); ++i) {
+    const double dx = v[i].x - v[i - 1].x, dy = v[i].y - v[i - 1].y;
+    length += std::sqrt(dx * dx + dy * dy);
+  }
+  // the smudge steps u by 1 / length: about length + 1 steps
+  PG_REQUIRE(!b->useSmudge || length < static_cast<double>(1 << 26),
+             "stroke too long for the smudge");
+  // outline: the right side reversed, then the left side; uv (u, 1) then (u, 0)
+  std::vector<double2> up, down, upUv, downUv;
+  for (size_t i = 0; i < v.size(); ++i) {
+    const double u = static_cast<double>(i) / static_cast<double>(v.size() - 1);
+    const D2 p = spline_h(v, u, false);
+    const D2 t = normalized_h(spline_h(v, u, true));
+    const D2 d = {-t.y, t.x};
+    up.push_back(make_double2(p.x - b->radius * d.x, p.y - b->radius * d.y));
+    down.push_back(make_double2(p.x + b->radius * d.x, p.y + b->radius * d.y));
+    upUv.push_back(make_double2(u, 0.0));
+    downUv.push_back(make_double2(u, 1.0));
+  }
+  up.insert(up.begin(), down.rbegin(), down.rend());
+  upUv.insert(upUv.begin(), downUv.rbegin(), downUv.rend());
+  const int trows = static_cast<int32_t>(bmax.y - bmin.y + 1);
+  const int tcols = static_cast<int32_t>(bmax.x - bmin.x + 1);
+  if (trows <= 0 || tcols <= 0) return 0;  // the bounds miss the canvas (painty fails here)
+  const int x0 = static_cast<int32_t>(bmin.x), x1 = static_cast<int32_t>(bmax.x);
+  const int y0 = static_cast<int32_t>(bmin.y), y1 = static_cast<int32_t>(bmax.y);
+  const int nx = x1 - x0 + 1, ny = y1 - y0 + 1;
+  if (nx <= 0 || ny <= 0) return 0;
+
+  // device buffers of the stroke (stream-ordered)
+  const int np = static_cast<int>(up.size());
+  const size_t tmap_bytes = static_cast<size_t>(trows) * tcols * sizeof(M);
+  char* d = nullptr;
+  const size_t off_poly = 0, off_uv = align256(np * sizeof(double2)),
+               off_max = off_uv + align256(np * sizeof(double2)),
+               off_tmap = off_max + 256, total = off_tmap + align256(tmap_bytes);
+  PG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&d), total, st));
+  PG_CUDA(cudaMemcpyAsync(d + off_poly, up.data(), np * sizeof(double2), cudaMemcpyHostToDevice, st));
+  PG_CUDA(cudaMemcpyAsync(d + off_uv, upUv.data(), np * sizeof(double2), cudaMemcpyHostToDevice, st));
+  PG_CUDA(cudaMemsetAsync(d + off_max, 0, 256 + align256(tmap_bytes), st));
+  auto* maxbits = reinterpret_cast<unsigned long long*>(d + off_max);
+  M* tmap = reinterpret_cast<M*>(d + off_tmap);
+
+  TexArgs ta{};
+  ta.poly = reinterpret_cast<const double2*>(d + off_poly);
+  ta.uv = reinterpret_cast<const double2*>(d + off_uv);
+  ta.npoly = np;
+  ta.tex = static_cast<const double*>(b->d_tex);
+  ta.th = b->th;
+  ta.tw = b->tw;
+  ta.scale = b->thicknessScale;
+  ta.x0 = x0;
+  ta.y0 = y0;
+  ta.nx = nx;
+  ta.ny = ny;
+  ta.bx = x0;
+  ta.by = y0;
+  ta.trows = trows;
+  ta.tcols = tcols;
+  ta.rows = rows;
+  ta.cols = cols;
+  const int64_t npx = static_cast<int64_t>(nx) * ny;
+  tb_thickness_kernel<M><<<grid_of(npx, kTexThreads), kTexThreads, 0, st>>>(ta, tmap, maxbits);
+  count_launch();
+  PG_CUDA(cudaGetLastError());
+
+  // the thickness maximum and the painted-pixel count
+  unsigned long long stats[2] = {0, 0};
+  PG_CUDA(cudaMemcpyAsync(stats, maxbits, sizeof(stats), cudaMemcpyDeviceToHost, st));
+  PG_CUDA(cudaStreamSynchronize(st));
+  const int64_t painted = static_cast<int64_t>(stats[1]);
+  if (painted == 0) {
+    PG_CUDA(cudaFreeAsync(d, st));
+    return 0;
+  }
+  // the smudge runs only where the map has paint (Smudge.hxx:41-47)
+  if (b->useSmudge) {
+    double maxD;
+    if constexpr (sizeof(M) == 8) {
+      std::memcpy(&maxD, &stats[0], 8);
+    } else {
+      float x;
+      const unsigned lo = static_cast<unsigned>(stats[0]);
+      std::memcpy(&x, &lo, 4);
+      maxD = x;
+    }
+    if (maxD > 0.0) {
+      std::vector<SmudgeStep<M>> steps;
+      const double msz = static_cast<double>(b->side);
+      for (double u = 0.0; u <= 1.0; u += 1. / length) {
+        const D2 ctr = spline_h(v, u, false);
+        const D2 t = normalized_h(spline_h(v, u, true));
+        const double theta = std::atan2(t.y, t.x);
+        const double dtheta = normalize_angle_h(theta - b->rotation);
+        b->rotation = theta;
+        SmudgeStep<M> s{};
+        s.cx = static_cast<M>(ctr.x);
+        s.cy = static_cast<M>(ctr.y);
+        s.c = static_cast<M>(std::cos(dtheta));
+        s.s = static_cast<M>(std::sin(dtheta));
+        s.roi_x = static_cast<int32_t>(ctr.x - msz / 2.0);
+        s.roi_y = static_cast<int32_t>(ctr.y - msz / 2.0);
+        steps.push_back(s);
+      }
+      const size_t cells = static_cast<size_t>(b->side) * b->side;
+      const size_t mbytes = 2 * cells * 7 * sizeof(M);
+      if (b->d_maps_bytes < mbytes || !b->d_maps) {
+        device_free(b->d_maps);
+        b->d_maps = device_alloc(std::max<size_t>(mbytes, 256));
+        b->d_maps_bytes = std::max<size_t>(mbytes, 256);
+        b->maps_zero = true;
+      }
+      if (b->maps_zero) {
+        PG_CUDA(cudaMemsetAsync(b->d_maps, 0, b->d_maps_bytes, st));
+        b->maps_zero = false;
+      }
+      SmudgeStep<M>* dsteps = nullptr;
+      PG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&dsteps),
+                              std::max<size_t>(steps.size(), 1) * sizeof(SmudgeStep<M>), st));
+      if (!steps.empty())
+        PG_CUDA(cudaMemcpyAsync(dsteps, steps.data(), steps.size() * sizeof(SmudgeStep<M>),
+                                cudaMemcpyHostToDevice, st));
+      SmudgeArgs<M> sa{};
+      sa.canvas = c->wet.base;
+      sa.rows = rows;
+      sa.cols = cols;
+      sa.pitch = c->wet.pitch;
+      sa.maps = static_cast<M*>(b->d_maps);
+      sa.side = b->side;
+      sa.ctr = static_cast<M>(b->maxSize / 2.0);
+      sa.radius = static_cast<M>(b->maxSize * 0.5);
+      sa.tmap = tmap;
+      sa.trows = trows;
+      sa.tcols = tcols;
+      sa.bx0 = static_cast<int>(std::floor(bmin.x));
+      sa.by0 = static_cast<int>(std::floor(bmin.y));
+      sa.bxf = bmin.x > std::floor(bmin.x) ? 1 : 0;
+      sa.byf = bmin.y > std::floor(bmin.y) ? 1 : 0;
+      sa.steps = dsteps;
+      sa.nsteps = static_cast<int64_t>(steps.size());
+      sa.maxbits = maxbits;
+      sa.pickupRate = static_cast<M>(0.1);      // Smudge.hxx:156
+      sa.depositionRate = static_cast<M>(0.1);  // Smudge.hxx:158
+      sa.seed = static_cast<uint32_t>(c->id * 0x9e3779b97f4a7c15ull + c->version);
+      if (!steps.empty() && cells > 0) {
+        // both maps in shared memory when they fit (side <= 64 in FP32, <= 45 in FP64)
+        const size_t smem = 2 * cells * 7 * sizeof(M);
+        if (smem <= static_cast<size_t>(max_dyn_smem())) {
+          auto kern = tb_smudge_kernel<TK, TV, M, true>;
+          PG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(smem)));
+          kern<<<1, kSmudgeThreads, smem, st>>>(sa);
+        } else {
+          tb_smudge_kernel<TK, TV, M, false><<<1, kSmudgeThreads, 0, st>>>(sa);
+        }
+        count_launch();
+        PG_CUDA(cudaGetLastError());
+      }
+      PG_CUDA(cudaFreeAsync(dsteps, st));
+    }
+  }
+
+  DepositArgs<M> da{};
+  da.canvas = c->wet.base;
+  da.rows = rows;
+  da.cols = cols;
+  da.pitch = c->wet.pitch;
+  da.tmap = tmap;
+  da.trows = trows;
+  da.tcols = tcols;
+  da.x0 = x0;
+  da.y0 = y0;
+  da.nx = nx;
+  da.ny = ny;
+  da.bx = x0;
+  da.by = y0;
+  for (int q = 0; q < 3; q++) {
+    da.K[q] = static_cast<M>(b->paintK[q]);
+    da.S[q] = static_cast<M>(b->paintS[q]);
+  }
+  tb_deposit_kernel<TK, TV, M><<<grid_of(npx, kTexThreads), kTexThreads, 0, st>>>(da);
+  count_launch();
+  PG_CUDA(cudaGetLastError());
+  PG_CUDA(cudaFreeAsync(d, st));
+  c->version++;
+  return painted;
+}
+
+}  // namespace
+}  // namespace pg
+
+using pg::guard;
+
+extern "C" {
+
+painty_status painty_texture_brush_create(const double* texture, int32_t rows, int32_t cols,
+                                          painty_texture_brush** out) {
+  return guard([&] {
+    PG_REQUIRE(out != nullptr, "out is null");
+    PG_REQUIRE(texture != nullptr && rows > 0 && cols > 0, "texture is empty");
+    auto* b = new painty_texture_brush();
+    b->tex.assign(texture, texture + static_cast<size_t>(rows) * cols);
+    b->th = rows;
+    b->tw = cols;
+    b->make_smudge(static_cast<int32_t>(2.0 * b->radius));  // TextureBrush.hxx:25-31
+    *out = b;
+  });
+}
+
+painty_status painty_texture_brush_destroy(painty_texture_brush* b) {
+  return guard([&] {
+    if (!b) return;
+    pg::device_free(b->d_tex);
+    pg::device_free(b->d_maps);
+    delete b;
+  });
+}
+
+painty_status painty_texture_brush_set_radius(painty_texture_brush* b, double radius) {
+  return guard([&] {
+    PG_REQUIRE(b != nullptr, "brush is null");
+    PG_REQUIRE(std::isfinite(radius) && radius >= 0.0, "radius must be finite and >= 0");
+    if (!(std::fabs(b->radius - radius) < 0.5)) {  // TextureBrush.hxx:33-41
+      b->radius = radius;
+      if (b->useSmudge) b->make_smudge(static_cast<int32_t>(2.0 * radius));
+    }
+  });
+}
+
+painty_status painty_texture_brush_dip(painty_texture_brush* b, const double K[3],
+                                       const double S[3]) {
+  return guard([&] {
+    PG_REQUIRE(b && K && S, "null argument");
+    for (int i = 0; i < 3; i++) {
+      b->paintK[i] = K[i];
+      b->paintS[i] = S[i];
+    }
+  });
+}
+
+painty_status painty_texture_brush_set_smudge(painty_texture_brush* b, int32_t enable) {
+  return guard([&] {
+    PG_REQUIRE(b != nullptr, "brush is null");
+    b->useSmudge = enable != 0;
+  });
+}
+
+painty_status painty_texture_brush_set_thickness_scale(painty_texture_brush* b, double scale) {
+  return guard([&] {
+    PG_REQUIRE(b != nullptr, "brush is null");
+    PG_REQUIRE(std::isfinite(scale), "scale must be finite");
+    b->thicknessScale = scale;
+  });
+}
+
+painty_status painty_texture_brush_paint_stroke(painty_canvas* c, painty_texture_brush* b,
+                                                const double* path_xy, int32_t n,
+                                                int64_t* painted_out, void* stream) {
+  return guard([&] {
+    PG_REQUIRE(c && b, "null handle");
+    PG_REQUIRE(n >= 0 && (n == 0 || path_xy), "path is null");
+    for (int64_t i = 0; i < 2 * static_cast<int64_t>(n); i++)
+      PG_REQUIRE(std::isfinite(path_xy[i]), "path coordinates must be finite");
+    PG_REQUIRE(static_cast<int64_t>(c->wet.rows) * c->wet.pitch < (int64_t(1) << 31),
+               "canvas too large for the texture brush");
+    const bool f64 = c->wet.storage == PAINTY_STORAGE_F64;
+    const int mode = f64 ? 1 : 0;
+    if (b->bound < 0) b->bound = mode;
+    PG_REQUIRE(b->bound == mode,
+               "a texture brush paints either F64 canvases or F32/F16/BF16 canvases, not both");
+    const cudaStream_t st = pg::as_stream(stream);
+    if (!b->d_tex) {
+      b->d_tex = pg::device_alloc(b->tex.size() * sizeof(double));
+      PG_CUDA(cudaMemcpyAsync(b->d_tex, b->tex.data(), b->tex.size() * sizeof(double),
+                              cudaMemcpyHostToDevice, st));
+    }
+    int64_t painted = 0;
+    switch (c->wet.storage) {
+      case PAINTY_STORAGE_F32:
+        painted = pg::paint_texture_stroke<float, float>(c, b, path_xy, n, st);
+        break;
+      case PAINTY_STORAGE_F16:
+        painted = pg::paint_texture_stroke<__half, __half>(c, b, path_xy, n, st);
+        break;
+      case PAINTY_STORAGE_BF16:
+        painted = pg::paint_texture_stroke<__nv_bfloat16, __half>(c, b, path_xy, n, st);
+        break;
+      case PAINTY_STORAGE_F64:
+        painted = pg::paint_texture_stroke<double, double>(c, b, path_xy, n, st);
+        break;
+    }
+    if (painted_out) *painted_out = painted;
+  });
+}
+
+painty_status painty_texture_brush_smudge_map(const painty_texture_brush* b,
+                                                   painty_plane plane, double* host,
+                                                   int32_t* side, void* stream) {
+  return guard([&] {
+    PG_REQUIRE(b != nullptr, "brush is null");
+    if (side) *side = b->side;
+    if (!host) return;
+    const size_t cells = static_cast<size_t>(b->side) * b->side;
+    const int nch = plane == PAINTY_PLANE_V ? 1 : 3;
+    PG_REQUIRE(plane == PAINTY_PLANE_K || plane == PAINTY_PLANE_S || plane == PAINTY_PLANE_V,
+               "smudge planes are K, S, V");
+    if (!b->d_maps || b->maps_zero || b->bound < 0) {
+      std::memset(host, 0, cells * nch * sizeof(double));
+      return;
+    }
+    const size_t msz = b->bound == 1 ? 8 : 4;
+    const int off = plane == PAINTY_PLANE_K ? 0 : plane == PAINTY_PLANE_S ? 3 : 6;
+    const char* base = static_cast<const char*>(b->d_maps);
+    const size_t pb = cells * msz;  // bytes per plane
+    const void* p[3] = {base + off * pb, base + (off + 1) * pb, base + (off + 2) * pb};
+    pg::download_planes(p, nch, b->bound == 1 ? pg::DT_F64 : pg::DT_F32, b->side, b->side,
+                        b->side, host, PAINTY_HOST_F64_INTERLEAVED, pg::as_stream(stream));
+  });
+}
+
+}  // extern "C"

@@ -33,7 +33,8 @@ def golden():
     import numpy as np
     kat = json.loads((ROOT / "tests/golden/kat.json").read_text())
     stamps = dict(np.load(ROOT / "tests/golden/stamps_ref.npz"))
-    return {"kat": kat, "stamps": stamps}
+    texture = dict(np.load(ROOT / "tests/golden/texture_ref.npz"))
+    return {"kat": kat, "stamps": stamps, "texture": texture}
 
 
 @pytest.fixture(scope="session")

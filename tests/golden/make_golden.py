@@ -9,6 +9,8 @@ stamps_ref.npz canvas and pickup-map planes after imprint sequences run by paint
                repository's Eigen/OpenCV stand-ins (oracle/_ref). The GPU tests compare the
                library's F64 mode against these bit for bit; the GPU machine has no reference
                checkout, so the fixtures travel with the tests.
+texture_ref.npz canvas planes after texture-brush stroke sessions (TextureBrush + Smudge) run
+               by painty's own TextureBrush.hxx through the same harness.
 """
 from __future__ import annotations
 
@@ -144,12 +146,56 @@ def stamps_fixture() -> dict:
     return arrays
 
 
+def texture_session(rng, rows, cols, n, rmin=4.0, rmax=18.0):
+    """n random strokes (2-5 control points, partly off the canvas) with radius and paint."""
+    out = []
+    for _ in range(n):
+        k = int(rng.integers(2, 6))
+        path = np.stack([rng.uniform(-10, cols + 10, k), rng.uniform(-10, rows + 10, k)], axis=1)
+        out.append((path, float(rng.uniform(rmin, rmax)), rng.uniform(0.01, 5, 3),
+                    rng.uniform(0.05, 3, 3)))
+    return out
+
+
+def texture_fixture() -> dict:
+    ref = Reference()
+    arrays = {}
+    cases = [
+        # name, rows, cols, smudge, thickness scale, texture seed, strokes
+        ("smudge", 48, 64, True, 1.0, 13, 5),
+        ("nosmudge", 40, 56, False, 1.5, 5, 4),
+    ]
+    rng = np.random.default_rng(77)
+    for name, rows, cols, smudge, scale, tseed, nstrokes in cases:
+        tex = workloads.stroke_texture(seed=tseed)
+        sess = texture_session(rng, rows, cols, nstrokes)
+        r0 = rng.uniform(0.8, 0.95, (rows, cols, 3))
+        c = ref.canvas(rows, cols)
+        c.set("R0", r0)
+        b = ref.texture_brush(tex)
+        b.enable_smudge(smudge)
+        b.set_thickness_scale(scale)
+        for i, (path, rad, K, S) in enumerate(sess):
+            b.set_radius(rad)
+            b.dip(K, S)
+            b.paint_stroke(c, path)
+            arrays[f"{name}/stroke{i}/path"] = path
+            arrays[f"{name}/stroke{i}/radius"] = np.array([rad])
+            arrays[f"{name}/stroke{i}/paint"] = np.stack([K, S])
+        arrays[f"{name}/meta"] = np.array([rows, cols, int(smudge), scale, tseed], dtype=np.float64)
+        arrays[f"{name}/r0"] = r0
+        for p in ("K", "S", "V"):
+            arrays[f"{name}/out_{p}"] = c.get(p)
+    return arrays
+
+
 def main() -> None:
     if not Reference.available():
         raise SystemExit("reference checkout / oracle/_ref build not available")
     (HERE / "kat.json").write_text(json.dumps(kat(), indent=1) + "\n")
     np.savez_compressed(HERE / "stamps_ref.npz", **stamps_fixture())
-    print("wrote kat.json, stamps_ref.npz")
+    np.savez_compressed(HERE / "texture_ref.npz", **texture_fixture())
+    print("wrote kat.json, stamps_ref.npz, texture_ref.npz")
 
 
 if __name__ == "__main__":

@@ -75,3 +75,45 @@ def test_texture_brush_off_canvas_is_a_no_op(oracle):
     c = _run(oracle, rows, cols, tex,
              [(np.array([[-50.0, -50.0], [-20.0, -30.0]]), 4.0, np.ones(3), np.ones(3))])
     assert not c.get("V").any()
+
+
+def replay_texture_fixture(o, fx, name, storage=None):
+    """Replays a texture-brush session of the golden fixture on the oracle (storage None) or on
+    the library's Canvas / TextureBrush (storage given; `o` is the package)."""
+    rows, cols, smudge, scale, tseed = fx[f"{name}/meta"]
+    rows, cols = int(rows), int(cols)
+    tex = workloads.stroke_texture(seed=int(tseed))
+    if storage is None:
+        c = o.canvas(rows, cols)
+        c.set("R0", fx[f"{name}/r0"])
+        b = o.texture_brush(tex)
+        b.enable_smudge(bool(smudge))
+        b.set_thickness_scale(scale)
+    else:
+        c = o.Canvas(rows, cols, storage)
+        c.upload("R0", fx[f"{name}/r0"])
+        b = o.TextureBrush(tex)
+        b.enableSmudge(bool(smudge))
+        b.setThicknessScale(scale)
+    i = 0
+    while f"{name}/stroke{i}/path" in fx:
+        K, S = fx[f"{name}/stroke{i}/paint"]
+        if storage is None:
+            b.set_radius(fx[f"{name}/stroke{i}/radius"][0])
+            b.dip(K, S)
+            b.paint_stroke(c, fx[f"{name}/stroke{i}/path"])
+        else:
+            b.setRadius(fx[f"{name}/stroke{i}/radius"][0])
+            b.dip((K, S))
+            b.paintStroke(fx[f"{name}/stroke{i}/path"], c)
+        i += 1
+    return c, b
+
+
+@pytest.mark.parametrize("name", ["smudge", "nosmudge"])
+def test_texture_brush_oracle_matches_golden(oracle, golden, name):
+    """The oracle against the committed reference outputs (runs without the reference)."""
+    fx = golden["texture"]
+    c, _ = replay_texture_fixture(oracle, fx, name)
+    for p in ("K", "S", "V"):
+        assert np.array_equal(c.get(p), fx[f"{name}/out_{p}"]), p
