@@ -66,7 +66,9 @@ typedef enum painty_plane {
   PAINTY_PLANE_S = 1,  /* scattering, 3 channels */
   PAINTY_PLANE_V = 2,  /* paint volume (layer thickness), 1 channel */
   PAINTY_PLANE_R0 = 3, /* canvas only: substrate reflectance, 3 channels */
-  PAINTY_PLANE_H = 4   /* canvas only: height map, 1 channel */
+  PAINTY_PLANE_H = 4,  /* canvas only: height map, 1 channel */
+  PAINTY_PLANE_VL = 5  /* canvas only: the GL path's lighting volume (S.a of painty's
+                          PaintLayerGpu, PaintTextureFootprintOnCanvas.compute.glsl:51-52) */
 } painty_plane;
 
 typedef struct painty_layer painty_layer;   /* PaintLayer<vec3>  (K, S, V) */
@@ -251,6 +253,69 @@ painty_status painty_texture_brush_paint_stroke(painty_canvas* canvas,
 painty_status painty_texture_brush_smudge_map(const painty_texture_brush* brush,
                                               painty_plane plane, double* host,
                                               int32_t* side_out, void* stream);
+
+/* ------------------------------------------------------------------ the GL canvas path
+ * painty's second renderer (CanvasGpu, PaintLayerGpu, TextureBrushGpu) keeps the canvas in
+ * rgba32f textures and paints with compute and raster shaders. These entry points run that
+ * path's arithmetic on the library's canvas (F32, F16 or BF16; float arithmetic): V is the
+ * textures' K.a and PAINTY_PLANE_VL their S.a. The shaders' thresholds differ from the CPU
+ * path's (|d| > 1e-5; any channel with |b S d| < 1e-5 keeps R0; no S floor), and their
+ * reflectance uses coth(bSd) where the CPU path has b coth(bSd). */
+/* replaces CanvasGpu::getComposed (CanvasGpu.cxx:91-95): out = the wet layer composed onto a
+ * copy of R0 by ComposeLayerOnSubstrate.compute.glsl:49-71; out is an F32 image */
+painty_status painty_canvas_compose_glsl(const painty_canvas* canvas, painty_image* out,
+                                         void* stream);
+/* replaces CanvasGpu::dryStep(step) (CanvasGpu.cxx:112-128, DryingStep.compute.glsl:122-147):
+ * min(V, portion) of the paint dries into R0, V keeps the rest */
+painty_status painty_canvas_dry_step(painty_canvas* canvas, float portion, void* stream);
+
+/* TextureBrushDictionary (painty/renderer/TextureBrushDictionary.hxx:17-39): brush textures
+ * in classes (radius token, length token), as painty reads them from data/textures/
+ * <radius>_<length>_*.png. lookup picks the class nearest the brush size (mean texture rows)
+ * and path length (mean cols), then a texture of the class at random: here from a
+ * std::mt19937 seeded at creation (painty seeds from std::random_device). */
+typedef struct painty_texture_dictionary painty_texture_dictionary;
+painty_status painty_texture_dictionary_create(uint32_t seed, painty_texture_dictionary** out);
+painty_status painty_texture_dictionary_destroy(painty_texture_dictionary* dict);
+/* one texture: a height map rows x cols (normalised min-max to [0, 1], as loadHeightMap,
+ * TextureBrushDictionary.cxx:112-120); index_out (may be null) receives its index */
+painty_status painty_texture_dictionary_add(painty_texture_dictionary* dict,
+                                            uint32_t radius_class, uint32_t length_class,
+                                            const double* height, int32_t rows, int32_t cols,
+                                            int32_t* index_out);
+/* replaces lookup(path, brushSize) (TextureBrushDictionary.cxx:66-110) */
+painty_status painty_texture_dictionary_lookup(painty_texture_dictionary* dict,
+                                               const double* path_xy, int32_t n,
+                                               double brush_size, int32_t* index_out);
+
+/* TextureBrushGpu (painty/renderer/TextureBrushGpu.hxx:21-64) over a dictionary that must
+ * outlive it. Radius 5 after creation (TextureBrushGpu.cxx:45); paint {0, 0}. */
+typedef struct painty_gpu_texture_brush painty_gpu_texture_brush;
+painty_status painty_gpu_texture_brush_create(painty_texture_dictionary* dict,
+                                              painty_gpu_texture_brush** out);
+painty_status painty_gpu_texture_brush_destroy(painty_gpu_texture_brush* brush);
+/* replaces setRadius (TextureBrushGpu.cxx:48-61) */
+painty_status painty_gpu_texture_brush_set_radius(painty_gpu_texture_brush* brush, double radius);
+/* replaces dip (:63-65) */
+painty_status painty_gpu_texture_brush_dip(painty_gpu_texture_brush* brush, const double K[3],
+                                           const double S[3]);
+painty_status painty_gpu_texture_brush_set_thickness_scale(painty_gpu_texture_brush* brush,
+                                                           double scale);
+/* replaces enableSmudge (:248-250); enabling returns PAINTY_ERR_UNSUPPORTED (the GL smudge
+ * pass has racing writes, so it has no result to reproduce; painty's default is off) */
+painty_status painty_gpu_texture_brush_set_smudge(painty_gpu_texture_brush* brush,
+                                                  int32_t enable);
+/* the dictionary index of the texture the last stroke used (-1 before the first) */
+painty_status painty_gpu_texture_brush_last_texture(const painty_gpu_texture_brush* brush,
+                                                    int32_t* index_out);
+/* replaces paintStroke(path, CanvasGpu&) (:74-167): the strip through the path's Catmull-Rom
+ * spline is rasterised with a dictionary texture into a canvas-sized warped texture, which is
+ * imprinted (V = Vcan + Vtex; K, S volume-weighted; lighting volume Vtex, or Vcan where
+ * Vtex = 0) over the stroke's bounds and cleared. n < 2 paints nothing. Asynchronous. */
+painty_status painty_gpu_texture_brush_paint_stroke(painty_canvas* canvas,
+                                                    painty_gpu_texture_brush* brush,
+                                                    const double* path_xy, int32_t n,
+                                                    void* stream);
 
 /* ------------------------------------------------------------------ serving
  * A continuous-batching render server (no counterpart in painty, whose SbrRenderThread runs

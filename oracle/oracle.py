@@ -171,6 +171,29 @@ class Oracle:
     def brush(self, radius, footprint):
         return OBrush(self, radius, footprint)
 
+    # -- the GL canvas path (float; K4 / S4 / R4: (rows, cols, 4) float32)
+    def glsl_compose(self, K4, S4, R4):
+        """CanvasGpu::getComposed: ComposeLayerOnSubstrate over a copy of R0."""
+        K4, S4, R4 = (np.ascontiguousarray(x, dtype=np.float32) for x in (K4, S4, R4))
+        out = np.empty_like(R4)
+        f = _Lib(self.lib, "orc").f("glsl_compose", _I64, _P, _P, _P, _P)
+        f(K4.size // 4, _p(K4), _p(S4), _p(R4), _p(out))
+        return out
+
+    def glsl_dry_step(self, K4, S4, R4, portion):
+        """CanvasGpu::dryStep on copies; returns (K4, R4)."""
+        K4, R4 = (np.array(x, dtype=np.float32, order="C") for x in (K4, R4))
+        S4 = np.ascontiguousarray(S4, dtype=np.float32)
+        f = _Lib(self.lib, "orc").f("glsl_dry_step", _I64, _P, _P, _P, C.c_float)
+        f(K4.size // 4, _p(K4), _p(S4), _p(R4), float(portion))
+        return K4, R4
+
+    def texture_dictionary(self, seed: int):
+        return _TDict(self.lib, seed)
+
+    def gpu_texture_brush(self):
+        return _GTBrush(self.lib)
+
     def texture_brush(self, texture):
         return _TBrush(self.lib, "orc", texture)
 
@@ -225,6 +248,71 @@ class _TBrush:
             return np.zeros((0, 0) if which == "V" else (0, 0, 3))
         a = np.ctypeslib.as_array(C.cast(ptr, C.POINTER(_D)), (n * n * (1 if which == "V" else 3),))
         return a.reshape((n, n) if which == "V" else (n, n, 3)).copy()
+
+
+class _TDict:
+    """TextureBrushDictionary with a seeded pick (orc_tdict)."""
+
+    def __init__(self, lib, seed: int):
+        L = _Lib(lib, "orc")
+        self._destroy = L.f("tdict_destroy", _P)
+        self._add = L.f("tdict_add", _P, C.c_uint32, C.c_uint32, _P, _I32, _I32, res=_I32)
+        self._lookup = L.f("tdict_lookup", _P, _P, _I32, _D, res=_I32)
+        self.h = L.f("tdict_create", C.c_uint32, res=_P)(seed)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self._destroy(self.h)
+            self.h = None
+
+    def add(self, radius_class, length_class, height):
+        h = np.ascontiguousarray(height, dtype=np.float64)
+        return self._add(self.h, radius_class, length_class, _p(h), h.shape[0], h.shape[1])
+
+    def lookup(self, path, brush_size):
+        p = np.ascontiguousarray(path, dtype=np.float64)
+        return self._lookup(self.h, _p(p), len(p), float(brush_size))
+
+
+class _GTBrush:
+    """TextureBrushGpu, smudge off (orc_gtbrush); paints float K4 / S4 arrays in place."""
+
+    def __init__(self, lib):
+        L = _Lib(lib, "orc")
+        self._destroy = L.f("gtbrush_destroy", _P)
+        self._radius = L.f("gtbrush_set_radius", _P, _D)
+        self._dip = L.f("gtbrush_dip", _P, _P, _P)
+        self._scale = L.f("gtbrush_set_thickness_scale", _P, _D)
+        self._last = L.f("gtbrush_last_texture", _P, res=_I32)
+        self._warped = L.f("gtbrush_warped", _P, res=_P)
+        self._stroke = L.f("gtbrush_paint_stroke", _P, _P, _I32, _I32, _P, _P, _P, _I32,
+                           res=_I32)
+        self.h = L.f("gtbrush_create", res=_P)()
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self._destroy(self.h)
+            self.h = None
+
+    def set_radius(self, r):
+        self._radius(self.h, float(r))
+
+    def dip(self, K, S):
+        K, S = (np.ascontiguousarray(x, dtype=np.float64) for x in (K, S))
+        self._dip(self.h, _p(K), _p(S))
+
+    def set_thickness_scale(self, s):
+        self._scale(self.h, float(s))
+
+    def last_texture(self):
+        return self._last(self.h)
+
+    def paint_stroke(self, dictionary, K4, S4, path):
+        """K4, S4: C-contiguous float32 (rows, cols, 4), painted in place."""
+        assert K4.dtype == np.float32 and K4.flags.c_contiguous and S4.flags.c_contiguous
+        p = np.ascontiguousarray(path, dtype=np.float64)
+        return self._stroke(self.h, dictionary.h, K4.shape[0], K4.shape[1], _p(K4), _p(S4),
+                            _p(p), len(p))
 
 
 class OCanvas:

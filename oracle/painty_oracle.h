@@ -123,6 +123,31 @@ void orc_tbrush_set_thickness_scale(orc_tbrush* b, double s);
 const double* orc_tbrush_smudge_map(const orc_tbrush* b, int32_t which, int32_t* side);
 int64_t orc_tbrush_paint_stroke(orc_tbrush* b, orc_canvas* c, const double* path_xy, int32_t n);
 
+/* ---- the GL canvas path (gl_path.cpp), float: K4/S4/R4 = npix pixels of 4 floats ---- */
+/* PaintLayerGpu::composeOnto of one layer onto a copy of R0 (CanvasGpu::getComposed) */
+void orc_glsl_compose(int64_t npix, const float* K4, const float* S4, const float* R4,
+                      float* out4);
+/* CanvasGpu::dryStep(portion) */
+void orc_glsl_dry_step(int64_t npix, float* K4, const float* S4, float* R4, float portion);
+/* TextureBrushDictionary with a seeded pick */
+typedef struct orc_tdict orc_tdict;
+orc_tdict* orc_tdict_create(uint32_t seed);
+void orc_tdict_destroy(orc_tdict* d);
+int32_t orc_tdict_add(orc_tdict* d, uint32_t radius_class, uint32_t length_class,
+                      const double* height, int32_t rows, int32_t cols);
+int32_t orc_tdict_lookup(orc_tdict* d, const double* path_xy, int32_t n, double brush_size);
+/* TextureBrushGpu (smudge off) */
+typedef struct orc_gtbrush orc_gtbrush;
+orc_gtbrush* orc_gtbrush_create(void);
+void orc_gtbrush_destroy(orc_gtbrush* b);
+void orc_gtbrush_set_radius(orc_gtbrush* b, double radius);
+void orc_gtbrush_dip(orc_gtbrush* b, const double K[3], const double S[3]);
+void orc_gtbrush_set_thickness_scale(orc_gtbrush* b, double s);
+int32_t orc_gtbrush_last_texture(const orc_gtbrush* b);
+const float* orc_gtbrush_warped(const orc_gtbrush* b);
+int32_t orc_gtbrush_paint_stroke(orc_gtbrush* b, orc_tdict* dict, int32_t rows, int32_t cols,
+                                 float* K4, float* S4, const double* path_xy, int32_t n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -35,7 +35,7 @@ _lib = C.CDLL(str(LIB_PATH))
 
 STORAGE = {"f32": 0, "f16": 1, "bf16": 2, "f64": 3}
 HOST_F64_INTERLEAVED, HOST_F32_INTERLEAVED, HOST_F64_PLANAR, HOST_F32_PLANAR = 0, 1, 2, 3
-PLANE = {"K": 0, "S": 1, "V": 2, "R0": 3, "h": 4}
+PLANE = {"K": 0, "S": 1, "V": 2, "R0": 3, "h": 4, "VL": 5}
 
 _P, _I32, _I64, _D = C.c_void_p, C.c_int32, C.c_int64, C.c_double
 
@@ -100,6 +100,20 @@ _sig("painty_texture_brush_set_smudge", _P, _I32)
 _sig("painty_texture_brush_set_thickness_scale", _P, _D)
 _sig("painty_texture_brush_paint_stroke", _P, _P, _P, _I32, C.POINTER(_I64), _P)
 _sig("painty_texture_brush_smudge_map", _P, C.c_int, _P, C.POINTER(_I32), _P)
+_sig("painty_canvas_compose_glsl", _P, _P, _P)
+_sig("painty_canvas_dry_step", _P, C.c_float, _P)
+_sig("painty_texture_dictionary_create", C.c_uint32, C.POINTER(_P))
+_sig("painty_texture_dictionary_destroy", _P)
+_sig("painty_texture_dictionary_add", _P, C.c_uint32, C.c_uint32, _P, _I32, _I32, C.POINTER(_I32))
+_sig("painty_texture_dictionary_lookup", _P, _P, _I32, _D, C.POINTER(_I32))
+_sig("painty_gpu_texture_brush_create", _P, C.POINTER(_P))
+_sig("painty_gpu_texture_brush_destroy", _P)
+_sig("painty_gpu_texture_brush_set_radius", _P, _D)
+_sig("painty_gpu_texture_brush_dip", _P, _P, _P)
+_sig("painty_gpu_texture_brush_set_thickness_scale", _P, _D)
+_sig("painty_gpu_texture_brush_set_smudge", _P, _I32)
+_sig("painty_gpu_texture_brush_last_texture", _P, C.POINTER(_I32))
+_sig("painty_gpu_texture_brush_paint_stroke", _P, _P, _P, _I32, _P)
 
 # painty_stroke_desc (include/painty_gb300.h)
 STROKE_DESC = np.dtype([("canvas", np.int32), ("npoints", np.int32), ("first_point", np.int64),
@@ -288,7 +302,7 @@ class Canvas:
                                          _host_fmt(data, planar), _stream(stream)))
 
     def download(self, plane: str, dtype=np.float64, planar: bool = False, stream=None):
-        one = plane in ("V", "h")
+        one = plane in ("V", "h", "VL")
         shape = (self.rows, self.cols) if one else _shape3(self.rows, self.cols, planar)
         out = np.empty(shape, dtype=dtype)
         _check(_lib.painty_canvas_download(self._h, PLANE[plane], _ptr(out),
@@ -305,6 +319,17 @@ class Canvas:
 
     def get_h(self):
         return self.download("h")
+
+    def getComposedGlsl(self, out: Image | None = None, stream=None) -> Image:
+        """CanvasGpu::getComposed (CanvasGpu.cxx:91-95): the GL path's composite."""
+        if out is None:
+            out = Image(self.rows, self.cols, "f32")
+        _check(_lib.painty_canvas_compose_glsl(self._h, out._h, _stream(stream)))
+        return out
+
+    def dryStep(self, step: float = 0.01, stream=None) -> None:
+        """CanvasGpu::dryStep (CanvasGpu.cxx:112-128)."""
+        _check(_lib.painty_canvas_dry_step(self._h, float(step), _stream(stream)))
 
     def getPaintLayer(self) -> PaintLayer:
         h = _P()
@@ -470,6 +495,74 @@ class TextureBrush:
             _check(_lib.painty_texture_brush_smudge_map(self._h, PLANE[plane], _ptr(out),
                                                         C.byref(side), None))
         return out
+
+
+class TextureBrushDictionary:
+    """painty::TextureBrushDictionary (TextureBrushDictionary.hxx:17-39) with a seeded pick."""
+
+    def __init__(self, seed: int = 0):
+        h = _P()
+        _check(_lib.painty_texture_dictionary_create(int(seed) & 0xffffffff, C.byref(h)))
+        self._h = h.value
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            _lib.painty_texture_dictionary_destroy(self._h)
+            self._h = None
+
+    def add(self, radius_class: int, length_class: int, height: np.ndarray) -> int:
+        """One texture of class (radius token, length token); returns its index."""
+        t = np.ascontiguousarray(height, dtype=np.float64)
+        i = _I32()
+        _check(_lib.painty_texture_dictionary_add(self._h, radius_class, length_class, _ptr(t),
+                                                  t.shape[0], t.shape[1], C.byref(i)))
+        return i.value
+
+    def lookup(self, path: np.ndarray, brush_size: float) -> int:
+        p = np.ascontiguousarray(path, dtype=np.float64).reshape(-1, 2)
+        i = _I32()
+        _check(_lib.painty_texture_dictionary_lookup(self._h, _ptr(p), p.shape[0],
+                                                     float(brush_size), C.byref(i)))
+        return i.value
+
+
+class TextureBrushGpu:
+    """painty::TextureBrushGpu (TextureBrushGpu.hxx:21-64) painting the GL canvas path."""
+
+    def __init__(self, dictionary: TextureBrushDictionary):
+        h = _P()
+        _check(_lib.painty_gpu_texture_brush_create(dictionary._h, C.byref(h)))
+        self._h = h.value
+        self._dict = dictionary  # the brush borrows it
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            _lib.painty_gpu_texture_brush_destroy(self._h)
+            self._h = None
+
+    def setRadius(self, radius: float) -> None:
+        _check(_lib.painty_gpu_texture_brush_set_radius(self._h, float(radius)))
+
+    def dip(self, paint) -> None:
+        K = np.ascontiguousarray(paint[0], dtype=np.float64)
+        S = np.ascontiguousarray(paint[1], dtype=np.float64)
+        _check(_lib.painty_gpu_texture_brush_dip(self._h, _ptr(K), _ptr(S)))
+
+    def setThicknessScale(self, scale: float) -> None:
+        _check(_lib.painty_gpu_texture_brush_set_thickness_scale(self._h, float(scale)))
+
+    def enableSmudge(self, enable: bool) -> None:
+        _check(_lib.painty_gpu_texture_brush_set_smudge(self._h, 1 if enable else 0))
+
+    def lastTexture(self) -> int:
+        i = _I32()
+        _check(_lib.painty_gpu_texture_brush_last_texture(self._h, C.byref(i)))
+        return i.value
+
+    def paintStroke(self, path: np.ndarray, canvas: Canvas, stream=None) -> None:
+        p = np.ascontiguousarray(path, dtype=np.float64).reshape(-1, 2)
+        _check(_lib.painty_gpu_texture_brush_paint_stroke(canvas._h, self._h, _ptr(p),
+                                                          p.shape[0], _stream(stream)))
 
 
 def mix_single_paint(weights: np.ndarray, palette_K: np.ndarray, palette_S: np.ndarray):

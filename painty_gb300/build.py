@@ -43,7 +43,7 @@ def sources() -> list[Path]:
 # stroke expansion give the same bits on x86-64 and aarch64 (and as painty's double code).
 # Translation units listed in NO_FMAD also keep device code free of fused multiply-adds: their
 # double kernels repeat painty's arithmetic as written (the others use explicit intrinsics).
-NO_FMAD = {"texture.cu"}
+NO_FMAD = {"texture.cu", "canvas_gpu.cu"}
 
 
 def _compile(src: Path, obj: Path) -> None:

@@ -953,6 +953,10 @@ painty_status painty_canvas_upload(painty_canvas* c, painty_plane plane, const v
       void* p[1] = {c->h};
       pg::upload_planes(p, 1, pg::v_type(c->wet.storage), c->wet.rows, c->wet.cols,
                         c->wet.pitch, host, fmt, st);
+    } else if (plane == PAINTY_PLANE_VL) {
+      void* p[1] = {static_cast<char*>(c->wet.V) + pg::v_bytes(c->wet.storage)};
+      pg::upload_planes(p, 1, pg::v_type(c->wet.storage), c->wet.rows, c->wet.cols,
+                        c->wet.pitch, host, fmt, st, c->wet.estride);
     } else {
       void* p[3] = {nullptr, nullptr, nullptr};
       int nch = 0;
@@ -977,6 +981,10 @@ painty_status painty_canvas_download(const painty_canvas* c, painty_plane plane,
       const void* p[1] = {c->h};
       pg::download_planes(p, 1, pg::v_type(c->wet.storage), c->wet.rows, c->wet.cols,
                           c->wet.pitch, host, fmt, st);
+    } else if (plane == PAINTY_PLANE_VL) {
+      const void* p[1] = {static_cast<const char*>(c->wet.V) + pg::v_bytes(c->wet.storage)};
+      pg::download_planes(p, 1, pg::v_type(c->wet.storage), c->wet.rows, c->wet.cols,
+                          c->wet.pitch, host, fmt, st, c->wet.estride);
     } else {
       void* p[3] = {nullptr, nullptr, nullptr};
       int nch = 0;

@@ -1,0 +1,140 @@
+"""The oracle's restatement of painty's GL canvas path (gl_path.cpp): hand-derived cases of the
+compute shaders, the texture dictionary's lookup and the strip raster + imprint."""
+import numpy as np
+import pytest
+
+
+def _glsl_reflectance_np(K, S, r0, d):
+    """ComposeLayerOnSubstrate.compute.glsl:28-47 in float64 numpy (shader semantics)."""
+    a = 1.0 + K / S
+    b = np.sqrt(np.maximum(a * a - 1.0, 0.0))
+    bSh = b * S * d
+    if np.any(np.abs(bSh) < 1e-5):
+        return r0
+    bc = np.where(bSh > 20.0, 1.0, np.cosh(bSh) / np.sinh(bSh))
+    return (1.0 - r0 * (a - bc)) / (a - r0 + bc)
+
+
+def _px(K, S, V, R0, VL=0.0):
+    K4 = np.array([[[*K, V]]], np.float32)
+    S4 = np.array([[[*S, VL]]], np.float32)
+    R4 = np.array([[[*R0, 1.0]]], np.float32)
+    return K4, S4, R4
+
+
+def test_glsl_compose_pixel(oracle):
+    K, S, R0 = np.array([0.5, 1.2, 2.0]), np.array([0.7, 0.3, 1.1]), np.array([0.9, 0.85, 0.8])
+    for V in (0.05, 0.4, 3.0):
+        out = oracle.glsl_compose(*_px(K, S, V, R0))[0, 0]
+        want = _glsl_reflectance_np(K.astype(np.float32).astype(np.float64),
+                                    S.astype(np.float32).astype(np.float64),
+                                    R0.astype(np.float32).astype(np.float64),
+                                    np.float64(np.float32(V)))
+        np.testing.assert_allclose(out[:3], want, rtol=2e-6, atol=2e-7)
+        assert out[3] == 1.0
+
+
+def test_glsl_compose_thresholds(oracle):
+    R0 = np.array([0.9, 0.8, 0.7])
+    # |d| <= 1e-5 keeps R0
+    out = oracle.glsl_compose(*_px([1, 1, 1], [1, 1, 1], 1e-6, R0))[0, 0]
+    np.testing.assert_array_equal(out[:3], R0.astype(np.float32))
+    # K = 0 in one channel: b = 0 there, so |bSh| < 1e-5 and the shader keeps R0 (the CPU
+    # path gives NaN)
+    out = oracle.glsl_compose(*_px([0, 1, 1], [1, 1, 1], 0.5, R0))[0, 0]
+    np.testing.assert_array_equal(out[:3], R0.astype(np.float32))
+
+
+def test_glsl_dry_step(oracle):
+    K, S, R0 = np.array([0.5, 1.2, 2.0]), np.array([0.7, 0.3, 1.1]), np.array([0.9, 0.85, 0.8])
+    K4, S4, R4 = _px(K, S, 0.25, R0)
+    k1, r1 = oracle.glsl_dry_step(K4, S4, R4, 0.1)
+    assert k1[0, 0, 3] == np.float32(np.float32(0.25) - np.float32(0.1))
+    np.testing.assert_array_equal(k1[0, 0, :3], K4[0, 0, :3])
+    want = oracle.glsl_compose(*_px(K, S, np.float32(0.25) - k1[0, 0, 3], R0))[0, 0]
+    np.testing.assert_array_equal(r1[0, 0], want)
+    # less paint than the portion: all of it dries
+    k2, r2 = oracle.glsl_dry_step(k1, S4, r1, 1.0)
+    assert k2[0, 0, 3] == 0.0
+
+
+def _dictionary(oracle, seed=3):
+    rng = np.random.default_rng(seed)
+    d = oracle.texture_dictionary(seed)
+    idx = {}
+    for rc, rows in ((4, 10), (16, 34)):
+        for lc, cols in ((50, 60), (200, 220)):
+            for k in range(3):
+                idx[(rc, lc, k)] = d.add(rc, lc, rng.random((rows, cols)))
+    return d, idx
+
+
+def test_dictionary_lookup_classes(oracle):
+    d, idx = _dictionary(oracle)
+    short = np.array([[0.0, 0.0], [50.0, 0.0]])
+    long_ = np.array([[0.0, 0.0], [100.0, 0.0], [200.0, 10.0]])
+    # brush size 10 -> size class of 10-row textures; short path -> 60-col class
+    for _ in range(5):
+        assert d.lookup(short, 10.0) in {idx[(4, 50, k)] for k in range(3)}
+        assert d.lookup(long_, 33.0) in {idx[(16, 200, k)] for k in range(3)}
+    # the seeded pick repeats
+    a = [oracle.texture_dictionary(9) for _ in range(2)]
+    rng = np.random.default_rng(0)
+    for x in a:
+        for k in range(4):
+            x.add(8, 40, rng.random((12, 40)) + k)
+    assert [a[0].lookup(short, 12.0) for _ in range(8)] == [a[1].lookup(short, 12.0) for _ in range(8)]
+
+
+def test_gpu_texture_brush_straight_stroke(oracle):
+    """Texture rows ramp 0..1 down the image: the strip's right side (t = 0, GL's bottom row =
+    the image's last row) carries the high end; V and the lighting volume follow the texture."""
+    d = oracle.texture_dictionary(1)
+    rows_t, cols_t = 16, 64
+    ramp = np.repeat(np.linspace(0.0, 1.0, rows_t)[:, None], cols_t, axis=1)
+    d.add(5, 60, ramp)
+    b = oracle.gpu_texture_brush()
+    b.set_radius(8.0)
+    b.dip(np.array([1.0, 2.0, 3.0]), np.array([0.5, 0.6, 0.7]))
+    H, W = 64, 96
+    K4 = np.zeros((H, W, 4), np.float32)
+    S4 = np.zeros((H, W, 4), np.float32)
+    path = np.array([[10.0, 32.0], [50.0, 32.0], [86.0, 32.0]])
+    assert b.paint_stroke(d, K4, S4, path) == 0
+    V = K4[..., 3]
+    # heading +x: d = (-t.y, t.x) = (0, 1), so the right side (c + r d) is at y = 40
+    assert V[39, 48] > V[25, 48] > 0.0
+    assert V[39, 48] > 0.8 and V[25, 48] < 0.2
+    assert V[5, 48] == 0.0 and V[60, 48] == 0.0
+    painted = V > 0
+    np.testing.assert_allclose(K4[painted][:, :3],
+                               np.broadcast_to(np.float32([1.0, 2.0, 3.0]), (painted.sum(), 3)),
+                               rtol=1e-6)
+    np.testing.assert_array_equal(S4[..., 3], V)  # empty canvas: lighting volume = Vtex = V
+    assert not oracle_warped_any(b, H, W)
+
+
+def oracle_warped_any(b, H, W):
+    import ctypes as C
+    ptr = b._warped(b.h)
+    a = np.ctypeslib.as_array(C.cast(ptr, C.POINTER(C.c_float)), (H * W,))
+    return bool(a.any())
+
+
+def test_gpu_texture_brush_rounds_the_dispatch_up(oracle):
+    """The imprint covers the stroke bounds' 16 x 16 tiles: there, existing paint with no new
+    paint gets its lighting volume set to its volume."""
+    d = oracle.texture_dictionary(1)
+    d.add(5, 60, np.random.default_rng(2).random((16, 64)))
+    b = oracle.gpu_texture_brush()
+    b.set_radius(3.0)
+    H, W = 64, 64
+    K4 = np.zeros((H, W, 4), np.float32)
+    S4 = np.zeros((H, W, 4), np.float32)
+    K4[..., 3] = 0.5  # existing paint everywhere, lighting volume 0
+    K4[..., :3] = 1.0
+    path = np.array([[10.0, 10.0], [14.0, 10.0]])
+    b.paint_stroke(d, K4, S4, path)
+    # bounds x 7..17 (width 11 -> one tile: x 7..22), y 7..13 (one tile: y 7..22)
+    assert S4[20, 21, 3] == 0.5 and S4[20, 23, 3] == 0.0 and S4[23, 20, 3] == 0.0
+    assert S4[6, 10, 3] == 0.0
