@@ -143,6 +143,10 @@ painty_status painty_canvas_info(const painty_canvas* canvas, int32_t* rows, int
                                  painty_storage* storage);
 /* replaces Renderer<vec>::compose(canvas) (painty/renderer/Renderer.hxx:26-53) */
 painty_status painty_canvas_compose(const painty_canvas* canvas, painty_image* out, void* stream);
+/* replaces Renderer::render(canvas) (painty/renderer/Renderer.hxx:60-156): the composite lit
+ * by painty's point light (Cook-Torrance with its Beckmann and geometric terms; normals from
+ * the wet layer's volume), clamped to [0, 1]. out: F64 for F64 canvases, F32 otherwise. */
+painty_status painty_canvas_render(const painty_canvas* canvas, painty_image* out, void* stream);
 /* replaces Canvas::dryCanvas (Canvas.hxx:105-121): h += V, R0 = KM(K,S,R0,V), wet = 0 */
 painty_status painty_canvas_dry(painty_canvas* canvas, void* stream);
 

@@ -68,6 +68,7 @@ class Oracle:
         self._cp = L.f("canvas_plane", _P, _I32, res=_P)
         self._cdry = L.f("canvas_dry", _P)
         self._ccomp = L.f("canvas_compose", _P, _P)
+        self._crender = L.f("canvas_render", _P, _P)
         self._bc = L.f("brush_create", _D, _P, _I32, _I32, res=_P)
         self._bd = L.f("brush_destroy", _P)
         self._bsr = L.f("brush_set_radius", _P, _D)
@@ -346,6 +347,12 @@ class OCanvas:
         self.o._ccomp(self.h, _p(out))
         return out
 
+    def render(self) -> np.ndarray:
+        """Renderer::render: the lit canvas (rows, cols, 3)."""
+        out = np.zeros((self.rows, self.cols, 3))
+        self.o._crender(self.h, _p(out))
+        return out
+
 
 class OBrush:
     def __init__(self, o: Oracle, radius: float, footprint: np.ndarray):
@@ -421,6 +428,7 @@ class Reference:
         self._cset = L.f("canvas_set", _P, _I32, _P)
         self._cdry = L.f("canvas_dry", _P)
         self._ccomp = L.f("canvas_compose", _P, _P)
+        self._crender = L.f("canvas_render", _P, _P)
         self._bc = L.f("brush_create", _D, _P, _I32, _I32, res=_P)
         self._bd = L.f("brush_destroy", _P)
         self._bsr = L.f("brush_set_radius", _P, _D)
@@ -511,6 +519,11 @@ class RCanvas:
     def compose(self):
         out = np.zeros((self.rows, self.cols, 3))
         self.r._ccomp(self.h, _p(out))
+        return out
+
+    def render(self):
+        out = np.zeros((self.rows, self.cols, 3))
+        self.r._crender(self.h, _p(out))
         return out
 
 

@@ -603,6 +603,76 @@ void orc_canvas_compose(const orc_canvas* c, double* out_rgb) {
                     &out_rgb[i * 3]);
 }
 
+// Renderer::render (Renderer.hxx:60-156): the composed canvas lit by a point light with a
+// Beckmann / Cook-Torrance specular term; normals from the wet layer's volume (central
+// differences through Interpolate). Vector arithmetic per coefficient as Eigen's: squared norm
+// and dot products summed left to right, normalized() divides by sqrt(squaredNorm).
+void orc_canvas_render(const orc_canvas* c, double* out_rgb) {
+  const int H = c->wet.rows, W = c->wet.cols;
+  std::vector<double> comp(static_cast<size_t>(H) * W * 3);
+  orc_canvas_compose(c, comp.data());
+  constexpr double Pi = 3.141592653589793238462643383279502884197169399375105820974;
+  struct V3 {
+    double x, y, z;
+  };
+  auto sub = [](V3 a, V3 b) { return V3{a.x - b.x, a.y - b.y, a.z - b.z}; };
+  auto dot = [](V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; };
+  auto nrm = [&](V3 a) {
+    const double n = dot(a, a);
+    if (n > 0.0) {
+      const double r = std::sqrt(n);
+      return V3{a.x / r, a.y / r, a.z / r};
+    }
+    return a;
+  };
+  const double m = 0.5, s = 0.2;
+  const V3 lightPos = {-200, -1500, -2000.};
+  const V3 eyePos = {W / 2.0, H / 2.0, -100.};
+  const std::vector<double>& hm = c->wet.V;
+  for (int i = 0; i < H; ++i)
+    for (int j = 0; j < W; ++j) {
+      const double s11 = hm[static_cast<size_t>(i) * W + j];
+      const double s01 = interpolate(hm.data(), H, W, static_cast<double>(j) - 1.0, i);
+      const double s21 = interpolate(hm.data(), H, W, static_cast<double>(j) + 1.0, i);
+      const double s10 = interpolate(hm.data(), H, W, j, static_cast<double>(i) - 1.0);
+      const double s12 = interpolate(hm.data(), H, W, j, static_cast<double>(i) + 1.0);
+      const V3 va = nrm({2.0, 0.0, s21 - s01});
+      const V3 vb = nrm({0.0, 2.0, s12 - s10});
+      V3 n = nrm({va.y * vb.z - va.z * vb.y, va.z * vb.x - va.x * vb.z, va.x * vb.y - va.y * vb.x});
+      n.z *= -1.;
+      const V3 pixPos = {static_cast<double>(j), static_cast<double>(i), s11};
+      const V3 lightDirection = nrm(sub(lightPos, pixPos));
+      const V3 l = nrm(lightDirection);
+      const V3 v = nrm(sub(eyePos, pixPos));
+      const V3 h = nrm({v.x + l.x, v.y + l.y, v.z + l.z});
+      const double* Kd = &comp[(static_cast<size_t>(i) * W + j) * 3];
+      const double NdotH = std::max(0.0, dot(n, h));
+      const double VdotH = std::max(0.0, dot(v, h));
+      const double NdotV = std::max(0.0, dot(n, v));
+      const double NdotL = std::max(0.0, dot(n, l));
+      double spec[3] = {0.0, 0.0, 0.0};
+      if (NdotL > 0.0 && NdotV > 0.0) {
+        const double A = 1.0 / (std::pow(m, 2.0) + std::pow(NdotH, 4.0) * Pi);
+        const double B = std::exp(-std::pow(std::tan(std::acos(NdotH)), 2.0) / std::pow(m, 2.0));
+        const double G1 = 2.0 * NdotH * NdotV / VdotH;
+        const double G2 = 2.0 * NdotH * NdotL / VdotH;
+        const double G = std::min(1.0, std::min(G1, G2));
+        const double f5 = std::pow(1.0 - VdotH, 5.0);
+        const double bg = A * B * G;
+        for (int k = 0; k < 3; k++) {
+          const double RF = 1.0 + (1.0 - 1.0) * f5;  // Ks = 1
+          spec[k] = bg * RF / (NdotL * NdotV);
+        }
+      }
+      const double beta = 15.0 * (1.0 / (4.0 * Pi * std::pow(std::sqrt(dot(lightDirection, lightDirection)), 2.0)));
+      for (int k = 0; k < 3; k++) {
+        const double ambient = Kd[k] * 0.2;
+        const double r = (beta * NdotL) * ((1.0 - s) * Kd[k] + s * spec[k]) + ambient * Kd[k];
+        out_rgb[(static_cast<size_t>(i) * W + j) * 3 + k] = std::min(std::max(r, 0.0), 1.0);
+      }
+    }
+}
+
 orc_brush* orc_brush_create(double radius, const double* footprint_full, int32_t fh,
                             int32_t fw) {
   auto* b = new orc_brush();

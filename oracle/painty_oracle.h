@@ -14,9 +14,11 @@
  *   painty/renderer/Canvas.hxx:26-121      Canvas (ctor, setBackground, dryCanvas)
  *   painty/renderer/FootprintBrush.hxx:46-431  setRadius, imprint, dip/clean, paintStroke,
  *                                          updateSnapshot, blend, pickupPaint, depositPaint
- *   painty/renderer/Renderer.hxx:26-53     Renderer::compose
+ *   painty/renderer/Renderer.hxx:26-156    Renderer::compose, Renderer::render (lit)
+ *   painty/renderer/TextureBrush.hxx:20-237, Smudge.hxx:16-229  the texture brush
  *   painty/mixer/src/PaintMixer.cxx:327-355, 536-548  mixSinglePaint, mixed
  *   painty/core/Color.hxx:186-198, 248-252, 658-763   rgb2xyz, xyz2lab, CIEDE2000
+ * and, in float (gl_path.cpp), the GL canvas path's shaders (CanvasGpu, TextureBrushGpu),
  * plus an FP64 Kubelka-Munk oracle (reflectance R and transmittance T) that uses the series
  * form of x*coth(x) near x -> 0 and is finite where the reference returns NaN (K = 0).
  *
@@ -111,6 +113,9 @@ double orc_ciede2000(const double lab1[3], const double lab2[3]);
 /* per-pixel CIEDE2000 between two linear-RGB images (npix*3); returns max, writes mean */
 double orc_delta_e_images(int64_t npix, const double* rgb_a, const double* rgb_b,
                           double* mean_out, int32_t nthreads);
+
+/* Renderer::render (Renderer.hxx:60-156): lit rendering of the canvas, out npix*3 */
+void orc_canvas_render(const orc_canvas* c, double* out_rgb);
 
 /* TextureBrush<vec3> (TextureBrush.hxx) with its Smudge; the texture is the thickness map. */
 typedef struct orc_tbrush orc_tbrush;

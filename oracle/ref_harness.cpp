@@ -164,6 +164,13 @@ void ref_canvas_compose(ref_canvas* c, double* out) {
     for (int ch = 0; ch < 3; ch++) out[i * 3 + ch] = R(static_cast<int>(i))[ch];
 }
 
+void ref_canvas_render(ref_canvas* c, double* out) {
+  painty::Renderer<vec3> r;
+  const auto R = r.render(c->c);
+  for (size_t i = 0; i < R.total(); i++)
+    for (int ch = 0; ch < 3; ch++) out[i * 3 + ch] = R(static_cast<int>(i))[ch];
+}
+
 ref_brush* ref_brush_create(double radius, const double* fp, int32_t fh, int32_t fw) {
   g_footprint_full = painty::Mat<double>(fh, fw);
   for (int i = 0; i < fh * fw; i++) g_footprint_full(i) = fp[i];

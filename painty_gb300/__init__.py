@@ -101,6 +101,7 @@ _sig("painty_texture_brush_set_thickness_scale", _P, _D)
 _sig("painty_texture_brush_paint_stroke", _P, _P, _P, _I32, C.POINTER(_I64), _P)
 _sig("painty_texture_brush_smudge_map", _P, C.c_int, _P, C.POINTER(_I32), _P)
 _sig("painty_canvas_compose_glsl", _P, _P, _P)
+_sig("painty_canvas_render", _P, _P, _P)
 _sig("painty_canvas_dry_step", _P, C.c_float, _P)
 _sig("painty_texture_dictionary_create", C.c_uint32, C.POINTER(_P))
 _sig("painty_texture_dictionary_destroy", _P)
@@ -353,6 +354,13 @@ class Renderer:
         if out is None:
             out = Image(canvas.rows, canvas.cols, "f64" if canvas.storage == "f64" else "f32")
         _check(_lib.painty_canvas_compose(canvas._h, out._h, _stream(stream)))
+        return out
+
+    def render(self, canvas: Canvas, out: Image | None = None, stream=None) -> Image:
+        """Renderer::render (Renderer.hxx:60-156): the composite lit by a point light."""
+        if out is None:
+            out = Image(canvas.rows, canvas.cols, "f64" if canvas.storage == "f64" else "f32")
+        _check(_lib.painty_canvas_render(canvas._h, out._h, _stream(stream)))
         return out
 
 

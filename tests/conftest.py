@@ -34,7 +34,8 @@ def golden():
     kat = json.loads((ROOT / "tests/golden/kat.json").read_text())
     stamps = dict(np.load(ROOT / "tests/golden/stamps_ref.npz"))
     texture = dict(np.load(ROOT / "tests/golden/texture_ref.npz"))
-    return {"kat": kat, "stamps": stamps, "texture": texture}
+    render = dict(np.load(ROOT / "tests/golden/render_ref.npz"))
+    return {"kat": kat, "stamps": stamps, "texture": texture, "render": render}
 
 
 @pytest.fixture(scope="session")

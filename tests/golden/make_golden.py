@@ -11,6 +11,8 @@ stamps_ref.npz canvas and pickup-map planes after imprint sequences run by paint
                checkout, so the fixtures travel with the tests.
 texture_ref.npz canvas planes after texture-brush stroke sessions (TextureBrush + Smudge) run
                by painty's own TextureBrush.hxx through the same harness.
+render_ref.npz  Renderer::render (the lit canvas) of random canvases and of a painted one, by
+               painty's own Renderer.hxx through the same harness.
 """
 from __future__ import annotations
 
@@ -189,13 +191,41 @@ def texture_fixture() -> dict:
     return arrays
 
 
+def render_fixture() -> dict:
+    ref = Reference()
+    rng = np.random.default_rng(404)
+    arrays = {}
+    for name, (rows, cols) in (("random_a", (24, 40)), ("random_b", (37, 29))):
+        c = ref.canvas(rows, cols)
+        planes = {"R0": rng.uniform(0.8, 0.95, (rows, cols, 3)),
+                  "K": rng.uniform(0.01, 5, (rows, cols, 3)),
+                  "S": rng.uniform(0.05, 3, (rows, cols, 3)),
+                  "V": rng.uniform(0, 1, (rows, cols)) * (rng.random((rows, cols)) < 0.6)}
+        for p, a in planes.items():
+            c.set(p, a)
+            arrays[f"{name}/{p}"] = a
+        arrays[f"{name}/out"] = c.render()
+    # a canvas painted by the imprint brush (smooth volume: the normals see brush ridges)
+    c = ref.canvas(40, 60)
+    c.set("R0", np.full((40, 60, 3), 0.9))
+    b = ref.brush(6.0, workloads.footprint_image(seed=7))
+    b.set_rates(0.05, 0.1)
+    b.dip(np.array([0.3, 1.2, 2.0]), np.array([0.5, 0.4, 0.9]))
+    b.paint_stroke(c, np.array([[5.0, 5.0], [30.0, 12.5], [52.0, 30.0], [20.0, 33.0]]))
+    for p in ("R0", "K", "S", "V"):
+        arrays[f"painted/{p}"] = c.get(p)
+    arrays["painted/out"] = c.render()
+    return arrays
+
+
 def main() -> None:
     if not Reference.available():
         raise SystemExit("reference checkout / oracle/_ref build not available")
     (HERE / "kat.json").write_text(json.dumps(kat(), indent=1) + "\n")
     np.savez_compressed(HERE / "stamps_ref.npz", **stamps_fixture())
     np.savez_compressed(HERE / "texture_ref.npz", **texture_fixture())
-    print("wrote kat.json, stamps_ref.npz, texture_ref.npz")
+    np.savez_compressed(HERE / "render_ref.npz", **render_fixture())
+    print("wrote kat.json, stamps_ref.npz, texture_ref.npz, render_ref.npz")
 
 
 if __name__ == "__main__":
