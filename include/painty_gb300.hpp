@@ -18,6 +18,11 @@
  *   set/get Pickup / Deposition rate, UseSnapshotBuffer, getPickupMap, getFootprint,
  *   updateSnapshot                    :168-204, 477-495  the same
  *   Renderer::compose(canvas | layer, R0)  Renderer.hxx:26-53  Renderer::compose
+ *   Renderer::render(canvas)          Renderer.hxx:60-156  Renderer::render
+ *   TextureBrush<vec3>(sampleDir)     TextureBrush.hxx:25-237  TextureBrush(texture, rows, cols)
+ *   CanvasGpu::getComposed / dryStep  CanvasGpu.cxx:91-128  Canvas::getComposedGlsl / dryStep
+ *   TextureBrushDictionary / TextureBrushGpu  TextureBrushGpu.cxx:17-250  the same
+ *   LoadPalette / SavePalette         mixer/src/Serialization.cxx:38-53  the same
  *
  * Host images are row-major, pixel-interleaved doubles (cv::Mat_<vec3>'s layout): rows*cols*3
  * values for three channels, rows*cols for one. Errors are painty's exception types:
@@ -28,8 +33,15 @@
 #define PAINTY_GB300_HPP
 
 #include <array>
+#include <cctype>
+#include <cstring>
 #include <cstdint>
+#include <cstdlib>
+#include <istream>
+#include <iterator>
 #include <new>
+#include <ostream>
+#include <sstream>
 #include <stdexcept>
 #include <string>
 #include <utility>
@@ -207,6 +219,13 @@ class Canvas {
     return Image(i, rows_, cols_);
   }
   void dryCanvas() { check(painty_canvas_dry(own_.get(), nullptr)); }
+  // the GL canvas path (CanvasGpu.cxx:91-128): its composite and its partial drying step
+  Image getComposedGlsl() const {
+    Image out(rows_, cols_, Storage::F32);
+    check(painty_canvas_compose_glsl(own_.get(), out.handle(), nullptr));
+    return out;
+  }
+  void dryStep(float step = 0.01F) { check(painty_canvas_dry_step(own_.get(), step, nullptr)); }
   painty_canvas* handle() const { return own_.get(); }
 
  private:
@@ -317,7 +336,280 @@ class Renderer {
     check(painty_compose_layers(L, 1, R0.handle(), out.handle(), nullptr));
     return out;
   }
+  // Renderer::render (Renderer.hxx:60-156): the composite lit by painty's point light;
+  // storage F64 for F64 canvases, F32 otherwise
+  Image render(const Canvas& canvas, Storage storage = Storage::F32) const {
+    Image out(canvas.rows(), canvas.cols(), storage);
+    check(painty_canvas_render(canvas.handle(), out.handle(), nullptr));
+    return out;
+  }
 };
+
+namespace detail {
+inline std::vector<double> flatten(const std::vector<vec2>& path) {
+  std::vector<double> xy;
+  xy.reserve(path.size() * 2);
+  for (const auto& p : path) {
+    xy.push_back(p.x);
+    xy.push_back(p.y);
+  }
+  return xy;
+}
+}  // namespace detail
+
+// painty::TextureBrush<vec3> (TextureBrush.hxx:20-237) with its Smudge. `texture` is the
+// brush-stroke sample's thickness map (rows x cols), which painty reads from a sample folder.
+class TextureBrush {
+ public:
+  TextureBrush(const std::vector<double>& texture, int32_t rows, int32_t cols) {
+    if (texture.size() != size_t(rows) * size_t(cols)) throw std::invalid_argument("texture size");
+    painty_texture_brush* h = nullptr;
+    check(painty_texture_brush_create(texture.data(), rows, cols, &h));
+    own_ = Owner(h);
+  }
+  void setRadius(double radius) { check(painty_texture_brush_set_radius(own_.get(), radius)); }
+  void dip(const std::array<vec3, 2>& paint) {
+    check(painty_texture_brush_dip(own_.get(), paint[0].data(), paint[1].data()));
+  }
+  void enableSmudge(bool enable) { check(painty_texture_brush_set_smudge(own_.get(), enable ? 1 : 0)); }
+  void setThicknessScale(double s) { check(painty_texture_brush_set_thickness_scale(own_.get(), s)); }
+  // TextureBrush::paintStroke (TextureBrush.hxx:52-205); returns the pixels painted
+  int64_t paintStroke(const std::vector<vec2>& path, Canvas& canvas) {
+    const auto xy = detail::flatten(path);
+    int64_t n = 0;
+    check(painty_texture_brush_paint_stroke(canvas.handle(), own_.get(), xy.data(),
+                                            static_cast<int32_t>(path.size()), &n, nullptr));
+    return n;
+  }
+
+ private:
+  using Owner = detail::Handle<painty_texture_brush, painty_texture_brush_destroy>;
+  Owner own_;
+};
+
+// painty::TextureBrushDictionary (TextureBrushDictionary.hxx:17-39): brush textures in
+// (radius, length) classes; the random pick is seeded.
+class TextureBrushDictionary {
+ public:
+  explicit TextureBrushDictionary(uint32_t seed = 0) {
+    painty_texture_dictionary* h = nullptr;
+    check(painty_texture_dictionary_create(seed, &h));
+    own_ = Owner(h);
+  }
+  int32_t add(uint32_t radiusClass, uint32_t lengthClass, const std::vector<double>& height,
+              int32_t rows, int32_t cols) {
+    if (height.size() != size_t(rows) * size_t(cols)) throw std::invalid_argument("texture size");
+    int32_t i = -1;
+    check(painty_texture_dictionary_add(own_.get(), radiusClass, lengthClass, height.data(),
+                                        rows, cols, &i));
+    return i;
+  }
+  // lookup(path, brushSize) (TextureBrushDictionary.cxx:66-110): the chosen texture's index
+  int32_t lookup(const std::vector<vec2>& path, double brushSize) {
+    const auto xy = detail::flatten(path);
+    int32_t i = -1;
+    check(painty_texture_dictionary_lookup(own_.get(), xy.data(),
+                                           static_cast<int32_t>(path.size()), brushSize, &i));
+    return i;
+  }
+  painty_texture_dictionary* handle() const { return own_.get(); }
+
+ private:
+  using Owner = detail::Handle<painty_texture_dictionary, painty_texture_dictionary_destroy>;
+  Owner own_;
+};
+
+// painty::TextureBrushGpu (TextureBrushGpu.hxx:21-64) on the GL canvas path; the dictionary
+// must outlive the brush.
+class TextureBrushGpu {
+ public:
+  explicit TextureBrushGpu(TextureBrushDictionary& dict) {
+    painty_gpu_texture_brush* h = nullptr;
+    check(painty_gpu_texture_brush_create(dict.handle(), &h));
+    own_ = Owner(h);
+  }
+  void setRadius(double radius) { check(painty_gpu_texture_brush_set_radius(own_.get(), radius)); }
+  void dip(const std::array<vec3, 2>& paint) {
+    check(painty_gpu_texture_brush_dip(own_.get(), paint[0].data(), paint[1].data()));
+  }
+  void setThicknessScale(double s) {
+    check(painty_gpu_texture_brush_set_thickness_scale(own_.get(), s));
+  }
+  void enableSmudge(bool enable) { check(painty_gpu_texture_brush_set_smudge(own_.get(), enable ? 1 : 0)); }
+  // paintStroke(path, CanvasGpu&) (TextureBrushGpu.cxx:74-167)
+  void paintStroke(const std::vector<vec2>& path, Canvas& canvas) {
+    const auto xy = detail::flatten(path);
+    check(painty_gpu_texture_brush_paint_stroke(canvas.handle(), own_.get(), xy.data(),
+                                                static_cast<int32_t>(path.size()), nullptr));
+  }
+
+ private:
+  using Owner = detail::Handle<painty_gpu_texture_brush, painty_gpu_texture_brush_destroy>;
+  Owner own_;
+};
+
+// painty::PaintCoeff (mixer/PaintCoeff.hxx) and its palette JSON files.
+struct PaintCoeff {
+  vec3 K{}, S{};
+};
+using Palette = std::vector<PaintCoeff>;
+
+namespace detail {
+// The palette JSON grammar: an array of objects whose "K" and "S" members are arrays of three
+// numbers (other members are skipped). Throws std::invalid_argument on malformed input.
+class PaletteParser {
+ public:
+  explicit PaletteParser(std::string text) : t_(std::move(text)) {}
+  Palette parse() {
+    Palette out;
+    expect('[');
+    if (peek() == ']') {
+      ++i_;
+      return out;
+    }
+    for (;;) {
+      out.push_back(entry());
+      const char c = next();
+      if (c == ']') break;
+      if (c != ',') fail("',' or ']'");
+    }
+    return out;
+  }
+
+ private:
+  PaintCoeff entry() {
+    PaintCoeff p;
+    bool hasK = false, hasS = false;
+    expect('{');
+    if (peek() == '}') fail("K and S");
+    for (;;) {
+      const std::string key = str();
+      expect(':');
+      if (key == "K" || key == "S") {
+        vec3 v{};
+        expect('[');
+        for (int c = 0; c < 3; c++) {
+          if (c) expect(',');
+          v[static_cast<size_t>(c)] = num();
+        }
+        if (peek() == ',') fail("three coefficients");
+        expect(']');
+        (key == "K" ? p.K : p.S) = v;
+        (key == "K" ? hasK : hasS) = true;
+      } else {
+        skip();
+      }
+      const char c = next();
+      if (c == '}') break;
+      if (c != ',') fail("',' or '}'");
+    }
+    if (!hasK || !hasS) fail("K and S");
+    return p;
+  }
+  void skip() {  // any JSON value
+    const char c = peek();
+    if (c == '"') {
+      str();
+    } else if (c == '[' || c == '{') {
+      const char close = c == '[' ? ']' : '}';
+      ++i_;
+      if (peek() == close) {
+        ++i_;
+        return;
+      }
+      for (;;) {
+        if (c == '{') {
+          str();
+          expect(':');
+        }
+        skip();
+        const char d = next();
+        if (d == close) break;
+        if (d != ',') fail("separator");
+      }
+    } else {
+      size_t j = i_;
+      while (j < t_.size() && !std::strchr(",]} \t\r\n", t_[j])) ++j;
+      if (j == i_) fail("value");
+      i_ = j;
+    }
+  }
+  double num() {
+    ws();
+    const char* b = t_.c_str() + i_;
+    char* e = nullptr;
+    const double v = std::strtod(b, &e);
+    if (e == b) fail("number");
+    i_ += static_cast<size_t>(e - b);
+    return v;
+  }
+  std::string str() {
+    expect('"');
+    std::string s;
+    while (i_ < t_.size() && t_[i_] != '"') {
+      if (t_[i_] == '\\' && i_ + 1 < t_.size()) ++i_;
+      s.push_back(t_[i_++]);
+    }
+    if (i_ >= t_.size()) fail("closing quote");
+    ++i_;
+    return s;
+  }
+  void ws() {
+    while (i_ < t_.size() && std::isspace(static_cast<unsigned char>(t_[i_]))) ++i_;
+  }
+  char peek() {
+    ws();
+    return i_ < t_.size() ? t_[i_] : '\0';
+  }
+  char next() {
+    const char c = peek();
+    if (i_ < t_.size()) ++i_;
+    return c;
+  }
+  void expect(char c) {
+    if (next() != c) fail(std::string("'") + c + "'");
+  }
+  [[noreturn]] void fail(const std::string& what) {
+    throw std::invalid_argument("palette JSON: expected " + what + " at offset " +
+                                std::to_string(i_));
+  }
+  std::string t_;
+  size_t i_ = 0;
+};
+}  // namespace detail
+
+// LoadPalette (mixer/src/Serialization.cxx:38-44): appends the stream's paints
+inline void LoadPalette(std::istream& stream, Palette& palette) {
+  const std::string text((std::istreambuf_iterator<char>(stream)), std::istreambuf_iterator<char>());
+  const Palette p = detail::PaletteParser(text).parse();
+  palette.insert(palette.end(), p.begin(), p.end());
+}
+
+// SavePalette (mixer/src/Serialization.cxx:46-53): compact JSON with sorted keys, numbers in
+// the shortest form that reads back to the same double
+inline void SavePalette(std::ostream& stream, const Palette& palette) {
+  auto number = [](double v) {
+    for (int prec = 1; prec <= 17; prec++) {
+      std::ostringstream o;
+      o.precision(prec);
+      o << v;
+      if (std::strtod(o.str().c_str(), nullptr) == v) {
+        std::string s = o.str();
+        if (s.find_first_of(".eEn") == std::string::npos) s += ".0";
+        return s;
+      }
+    }
+    return std::to_string(v);
+  };
+  stream << '[';
+  for (size_t i = 0; i < palette.size(); i++) {
+    if (i) stream << ',';
+    stream << "{\"K\":[" << number(palette[i].K[0]) << ',' << number(palette[i].K[1]) << ','
+           << number(palette[i].K[2]) << "],\"S\":[" << number(palette[i].S[0]) << ','
+           << number(palette[i].S[1]) << ',' << number(palette[i].S[2]) << "]}";
+  }
+  stream << ']';
+}
 
 // PaintMixer::mixSinglePaint (mixer/src/PaintMixer.cxx:327-355) over a palette of n paints
 inline std::array<vec3, 2> mixSinglePaint(const std::vector<double>& weights,

@@ -1,6 +1,7 @@
 // Exercises include/painty_gb300.hpp the way painty's own code uses its classes.
 //   facade_demo errors            argument errors surface as std::invalid_argument (no GPU)
 //   facade_demo paint IN OUT      paints the stroke described in IN, writes the canvas to OUT
+//   facade_demo palette IN OUT    LoadPalette(IN) then SavePalette(OUT) (no GPU)
 // IN (doubles): rows, cols, fh, fw, footprint[fh*fw], npts, path[2*npts], radius, spacing,
 //               pickup, deposition, K[3], S[3], R0[rows*cols*3]
 // OUT (doubles): stamps, K[rows*cols*3], S[rows*cols*3], V[rows*cols], composite[rows*cols*3]
@@ -8,6 +9,7 @@
 #include <cstring>
 #include <fstream>
 #include <iostream>
+#include <sstream>
 #include <stdexcept>
 #include <vector>
 
@@ -28,8 +30,27 @@ static int errors() {
   } catch (const std::invalid_argument&) {
     ok++;
   }
-  std::printf("%s\n", ok == 2 ? "errors ok" : "errors FAILED");
-  return ok == 2 ? 0 : 1;
+  for (const char* bad : {"[{\"K\":[1,2,3]}]", "[{\"K\":[1,2],\"S\":[1,2,3]}]", "{", "[1]"}) {
+    try {
+      std::istringstream in(bad);
+      pg::Palette p;
+      pg::LoadPalette(in, p);
+    } catch (const std::invalid_argument&) {
+      ok++;
+    }
+  }
+  std::printf("%s\n", ok == 6 ? "errors ok" : "errors FAILED");
+  return ok == 6 ? 0 : 1;
+}
+
+static int palette(const char* in, const char* out) {
+  std::ifstream f(in);
+  pg::Palette p;
+  pg::LoadPalette(f, p);
+  std::ofstream o(out);
+  pg::SavePalette(o, p);
+  std::printf("palette of %zu paints\n", p.size());
+  return 0;
 }
 
 static int paint(const char* in, const char* out) {
@@ -78,6 +99,7 @@ static int paint(const char* in, const char* out) {
 int main(int argc, char** argv) {
   if (argc >= 2 && std::strcmp(argv[1], "errors") == 0) return errors();
   if (argc >= 4 && std::strcmp(argv[1], "paint") == 0) return paint(argv[2], argv[3]);
+  if (argc >= 4 && std::strcmp(argv[1], "palette") == 0) return palette(argv[2], argv[3]);
   std::fprintf(stderr, "usage: facade_demo errors | paint IN OUT\n");
   return 2;
 }

@@ -40,6 +40,27 @@ def test_facade_translates_argument_errors(demo):
     assert "errors ok" in r.stdout
 
 
+def test_facade_palette_round_trip(demo, tmp_path):
+    """LoadPalette / SavePalette in C++ read painty's palette format and write what the Python
+    side writes (nlohmann's compact form)."""
+    from painty_gb300 import palette as P
+    rng = np.random.default_rng(3)
+    pal = [(rng.uniform(0, 5, 3), rng.uniform(0, 3, 3)) for _ in range(6)]
+    pal.append((np.array([0.0, 0.5, 1.0]), np.array([1e-05, 0.003, 123.25])))
+    src = tmp_path / "in.json"
+    # painty's files are indented; the reader must not care
+    import json
+    src.write_text(json.dumps([{"K": list(K), "S": list(S)} for K, S in pal], indent=2))
+    dst = tmp_path / "out.json"
+    r = subprocess.run([str(demo), "palette", str(src), str(dst)], capture_output=True, text=True,
+                       timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert dst.read_text() == P.dumps_palette(pal)
+    back = P.load_palette(dst)
+    for (K, S), (K2, S2) in zip(pal, back):
+        assert np.array_equal(K, K2) and np.array_equal(S, S2)
+
+
 @pytest.mark.gpu
 def test_facade_paints_like_python_binding(demo, pg, tmp_path):
     rows, cols = 70, 90
