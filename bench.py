@@ -208,6 +208,153 @@ def run_stamps_only(args):
     print(json.dumps(run_stamps_config0(pg, torch, args.strokes)), flush=True)
 
 
+def _event_ms(torch, fn, reps: int, warm: int = 3) -> float:
+    """Average device time of fn() over `reps` calls (CUDA events on the current stream)."""
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(reps):
+        fn()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def run_texture_paths(pg, torch, cpu: bool = True):
+    """The next rows beside the hot path: the texture brush (TextureBrush + Smudge), the GL
+    canvas path (TextureBrushGpu strip raster + imprint, GLSL compose and drying step) and
+    the lit render (Renderer::render), each with the oracle's CPU time on a sample."""
+    from oracle.oracle import Oracle
+    from painty_gb300 import workloads
+
+    peak, peak_kind = _peaks()
+    rows, cols = 768, 1024
+    tex = workloads.stroke_texture(seed=13)
+    strokes = workloads.strokes(cols, rows, 40, seed=3)
+    out = {}
+    o = Oracle() if cpu else None
+    # -- TextureBrush: host-synchronous per stroke (the smudge needs the thickness maximum)
+    for storage, smudge in (("f32", True), ("f32", False), ("f64", True)):
+        c = pg.Canvas(rows, cols, storage)
+        b = pg.TextureBrush(tex)
+        b.enableSmudge(smudge)
+        todo = strokes if storage == "f32" else strokes[:8]
+        for s in todo[:2]:
+            b.setRadius(s.radius)
+            b.dip((s.K, s.S))
+            b.paintStroke(s.path, c)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        px = 0
+        for s in todo:
+            b.setRadius(s.radius)
+            b.dip((s.K, s.S))
+            px += b.paintStroke(s.path, c)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t
+        key = f"texture_brush_{storage}{'_smudge' if smudge else ''}"
+        out[key] = {"metric": "strokes/s", "value": round(len(todo) / dt, 2),
+                    "painted_mpix_per_s": round(px / dt / 1e6, 3),
+                    "ms_per_stroke": round(dt * 1e3 / len(todo), 3)}
+    if o is not None:
+        oc = o.canvas(rows, cols)
+        ob = o.texture_brush(tex)
+        t = time.perf_counter()
+        px = 0
+        for s in strokes[:4]:
+            ob.set_radius(s.radius)
+            ob.dip(s.K, s.S)
+            px += ob.paint_stroke(oc, s.path)
+        dt = time.perf_counter() - t
+        out["texture_brush_f32_smudge"]["cpu_baseline"] = {
+            "value": round(4 / dt, 3), "unit": "strokes/s", "cores": 1, "kind": "port",
+            "sample": "the first 4 strokes, painty's TextureBrush + Smudge restated (double)"}
+    # -- TextureBrushGpu on the GL canvas path
+    gd = pg.TextureBrushDictionary(1)
+    rng = np.random.default_rng(0)
+    for rc, nr in ((8, 24), (32, 64)):
+        for lc, nc in ((400, 400), (1600, 1600)):
+            for k in range(3):
+                gd.add(rc, lc, rng.random((nr, nc)))
+    gstrokes = workloads.strokes(cols, rows, 200, seed=3)
+    c = pg.Canvas(rows, cols, "f32")
+    gb = pg.TextureBrushGpu(gd)
+
+    def gl_all():
+        for s in gstrokes:
+            gb.setRadius(s.radius)
+            gb.dip((s.K, s.S))
+            gb.paintStroke(s.path, c)
+
+    ms = _event_ms(torch, gl_all, 3, warm=1)
+    out["gl_texture_brush_f32"] = {"metric": "strokes/s", "value": round(len(gstrokes) / ms * 1e3, 1),
+                                   "ms_per_stroke": round(ms / len(gstrokes), 4)}
+    if o is not None:
+        od = o.texture_dictionary(1)
+        rng = np.random.default_rng(0)
+        for rc, nr in ((8, 24), (32, 64)):
+            for lc, nc in ((400, 400), (1600, 1600)):
+                for k in range(3):
+                    od.add(rc, lc, rng.random((nr, nc)))
+        ogb = o.gpu_texture_brush()
+        K4 = np.zeros((rows, cols, 4), np.float32)
+        S4 = np.zeros((rows, cols, 4), np.float32)
+        t = time.perf_counter()
+        for s in gstrokes[:10]:
+            ogb.set_radius(s.radius)
+            ogb.dip(s.K, s.S)
+            ogb.paint_stroke(od, K4, S4, s.path)
+        dt = time.perf_counter() - t
+        out["gl_texture_brush_f32"]["cpu_baseline"] = {
+            "value": round(10 / dt, 2), "unit": "strokes/s", "cores": 1, "kind": "port",
+            "sample": "the first 10 strokes, the GL path's shaders restated in float"}
+    # -- lit render and the GLSL passes at 4096^2 (inputs above L2)
+    n = 4096
+    big = pg.Canvas(n, n, "f32")
+    g = np.random.default_rng(1)
+    big.upload("K", g.uniform(0.01, 5.0, (n, n, 3)).astype(np.float32))
+    big.upload("S", g.uniform(0.05, 3.0, (n, n, 3)).astype(np.float32))
+    big.upload("V", g.uniform(0, 1, (n, n)).astype(np.float32))
+    img = pg.Image(n, n, "f32")
+    r = pg.Renderer()
+    for key, fn, nbytes in (
+            ("render_f32", lambda: r.render(big, img), 32 + 12 + 12),
+            ("glsl_compose_f32", lambda: big.getComposedGlsl(img), 32 + 12 + 12),
+            ("dry_step_f32", lambda: big.dryStep(0.0), 32 + 12 + 12 + 32)):
+        ms = _event_ms(torch, fn, 20)
+        gbs = n * n * nbytes / (ms * 1e-3) / 1e9
+        out[key] = {"metric": "Mpix/s", "value": round(n * n / ms / 1e3, 1),
+                    "ms_per_launch": round(ms, 4),
+                    "roofline": {"bound": "hbm", "achieved": round(gbs, 1), "peak": peak,
+                                 "unit": "GB/s", "frac": round(gbs / peak, 3),
+                                 "bytes_per_px": nbytes, "peak_kind": peak_kind}}
+    if o is not None:
+        sr = 64
+        oc = o.canvas(sr, n)
+        g = np.random.default_rng(2)
+        oc.set("K", g.uniform(0.01, 5.0, (sr, n, 3)))
+        oc.set("S", g.uniform(0.05, 3.0, (sr, n, 3)))
+        oc.set("V", g.uniform(0, 1, (sr, n)))
+        t = time.perf_counter()
+        oc.render()
+        dt = time.perf_counter() - t
+        out["render_f32"]["cpu_baseline"] = {
+            "value": round(sr * n / dt / 1e6, 3), "unit": "Mpix/s", "cores": 1, "kind": "port",
+            "sample": f"{sr} rows x {n} cols, painty's Renderer::render restated (double)"}
+    return out
+
+
+def run_texture_only(args):
+    import torch
+
+    import painty_gb300 as pg
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    print(json.dumps(run_texture_paths(pg, torch, cpu=not args.no_cpu)), flush=True)
+
+
 def run_ours(args):
     import torch
 
@@ -740,6 +887,8 @@ def main():
     ap.add_argument("--serve-only", action="store_true", help="only the serving case")
     ap.add_argument("--precision-only", action="store_true", help="only the precision case")
     ap.add_argument("--batch-only", action="store_true", help="only the batched stamping case")
+    ap.add_argument("--texture-only", action="store_true",
+                    help="only the texture brushes, GL canvas path and lit render")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="serving arrivals per second")
     ap.add_argument("--serve-seconds", type=float, default=5.0, help="serving arrival window")
     args = ap.parse_args()
@@ -756,6 +905,8 @@ def main():
         run_precision_only(args)
     elif args.batch_only:
         run_batch_only(args)
+    elif args.texture_only:
+        run_texture_only(args)
     else:
         run_ours(args)
 
