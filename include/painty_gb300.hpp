@@ -23,6 +23,7 @@
  *   CanvasGpu::getComposed / dryStep  CanvasGpu.cxx:91-128  Canvas::getComposedGlsl / dryStep
  *   TextureBrushDictionary / TextureBrushGpu  TextureBrushGpu.cxx:17-250  the same
  *   LoadPalette / SavePalette         mixer/src/Serialization.cxx:38-53  the same
+ *   SbrRenderThread                   SbrRenderThread.hxx:19-116  the same (no window)
  *
  * Host images are row-major, pixel-interleaved doubles (cv::Mat_<vec3>'s layout): rows*cols*3
  * values for three channels, rows*cols for one. Errors are painty's exception types:
@@ -34,6 +35,14 @@
 
 #include <array>
 #include <cctype>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <functional>
+#include <future>
+#include <memory>
+#include <mutex>
+#include <thread>
 #include <cstring>
 #include <cstdint>
 #include <cstdlib>
@@ -446,6 +455,142 @@ class TextureBrushGpu {
  private:
   using Owner = detail::Handle<painty_gpu_texture_brush, painty_gpu_texture_brush_destroy>;
   Owner own_;
+};
+
+// painty::SbrRenderThread (renderer/SbrRenderThread.hxx:19-116, src/SbrRenderThread.cxx):
+// one worker thread owns a canvas and a TextureBrushGpu (the GL canvas path) and runs the
+// requests in submission order; calls return futures. Like painty's, the worker dries the
+// canvas by CanvasGpu::dryStep() every `dryInterval` (250 ms in painty; zero turns it off,
+// which makes results independent of timing). painty's window refresh has no counterpart.
+// The dictionary must outlive the object.
+class SbrRenderThread {
+ public:
+  SbrRenderThread(int32_t rows, int32_t cols, TextureBrushDictionary& dict,
+                  const std::vector<double>& background = {},
+                  std::chrono::milliseconds dryInterval = std::chrono::milliseconds(250))
+      : rows_(rows), cols_(cols), dryInterval_(dryInterval) {
+    // painty creates the brush and canvas on its GL thread; here the worker does too
+    auto ready = post([this, &dict, background] {
+      brush_ = std::make_unique<TextureBrushGpu>(dict);
+      canvas_ = std::make_unique<Canvas>(rows_, cols_, Storage::F32);
+      if (!background.empty()) canvas_->setBackground(background);
+    });
+    worker_ = std::thread([this] { loop(); });
+    try {
+      ready.get();
+    } catch (...) {
+      shutdown();
+      throw;
+    }
+  }
+  SbrRenderThread(const SbrRenderThread&) = delete;
+  SbrRenderThread& operator=(const SbrRenderThread&) = delete;
+  ~SbrRenderThread() { shutdown(); }
+  std::pair<int32_t, int32_t> getSize() const { return {rows_, cols_}; }
+  double getBrushThicknessScale() const { return thicknessScale_; }
+  // render(path, radius, ks) (SbrRenderThread.cxx:70-78): dip, setRadius, paintStroke
+  std::future<void> render(const std::vector<vec2>& path, double radius,
+                           const std::array<vec3, 2>& ks) {
+    return post([this, path, radius, ks] {
+      brush_->dip(ks);
+      brush_->setRadius(radius);
+      brush_->paintStroke(path, *canvas_);
+    });
+  }
+  // getLinearRgbImage (:80-85): CanvasGpu::getCompositionLinearRgb, rows*cols*3 doubles
+  std::future<std::vector<double>> getLinearRgbImage() {
+    return post([this] { return canvas_->getComposedGlsl().download(); });
+  }
+  void setBrushThicknessScale(double scale) {
+    thicknessScale_ = scale;
+    post([this, scale] { brush_->setThicknessScale(scale); });
+  }
+  // enableSmudge (:94-98): the GL smudge pass is not provided (see TextureBrushGpu)
+  void enableSmudge(bool enable) {
+    if (enable)
+      throw std::runtime_error("unsupported: the GL smudge pass is not provided");
+  }
+  // dryCanvas (:100-104): dryStep(1.0)
+  std::future<void> dryCanvas() {
+    return post([this] { canvas_->dryStep(1.0F); });
+  }
+
+ private:
+  template <class F>
+  auto post(F&& f) -> std::future<decltype(f())> {
+    using R = decltype(f());
+    auto task = std::make_shared<std::packaged_task<R()>>(std::forward<F>(f));
+    std::future<R> fut = task->get_future();
+    {
+      std::lock_guard<std::mutex> g(m_);
+      q_.emplace_back([task] { (*task)(); });
+    }
+    cv_.notify_one();
+    return fut;
+  }
+  // drains the queue (the last job releases the brush and canvas on the worker), then joins
+  void shutdown() {
+    if (!worker_.joinable()) return;
+    post([this] {
+      brush_.reset();
+      canvas_.reset();
+    });
+    {
+      std::lock_guard<std::mutex> g(m_);
+      stop_ = true;
+    }
+    cv_.notify_one();
+    worker_.join();
+  }
+  void loop() {
+    using clock = std::chrono::steady_clock;
+    const bool timer = dryInterval_.count() > 0;
+    auto nextDry = clock::now() + dryInterval_;
+    for (;;) {
+      std::function<void()> job;
+      bool dry = false;
+      {
+        std::unique_lock<std::mutex> lk(m_);
+        for (;;) {
+          if (timer && clock::now() >= nextDry) {
+            dry = true;
+            break;
+          }
+          if (!q_.empty()) {
+            job = std::move(q_.front());
+            q_.pop_front();
+            break;
+          }
+          if (stop_) return;
+          if (timer)
+            cv_.wait_until(lk, nextDry);
+          else
+            cv_.wait(lk);
+        }
+      }
+      if (dry) {  // the drying timer (SbrRenderThread.cxx:37-41): dryStep() every interval
+        nextDry = clock::now() + dryInterval_;
+        if (canvas_) {
+          try {
+            canvas_->dryStep();
+          } catch (...) {
+          }
+        }
+        continue;
+      }
+      job();
+    }
+  }
+  int32_t rows_, cols_;
+  std::chrono::milliseconds dryInterval_;
+  double thicknessScale_ = 1.0;
+  std::unique_ptr<TextureBrushGpu> brush_;
+  std::unique_ptr<Canvas> canvas_;
+  std::mutex m_;
+  std::condition_variable cv_;
+  std::deque<std::function<void()>> q_;
+  bool stop_ = false;
+  std::thread worker_;
 };
 
 // painty::PaintCoeff (mixer/PaintCoeff.hxx) and its palette JSON files.

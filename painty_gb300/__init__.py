@@ -573,6 +573,97 @@ class TextureBrushGpu:
                                                           p.shape[0], _stream(stream)))
 
 
+class SbrRenderThread:
+    """painty::SbrRenderThread (SbrRenderThread.hxx:19-116): one worker thread owns a canvas
+    and a TextureBrushGpu (the GL canvas path) and runs requests in order; calls return
+    concurrent.futures futures. The worker dries the canvas by Canvas.dryStep() every
+    `dry_interval` seconds (0.25 in painty; 0 turns it off). No window is shown."""
+
+    def __init__(self, rows: int, cols: int, dictionary: TextureBrushDictionary,
+                 background: np.ndarray | None = None, dry_interval: float = 0.25):
+        import concurrent.futures as cf
+        import threading
+
+        self._rows, self._cols = rows, cols
+        self._dict = dictionary
+        self._scale = 1.0
+        self._pool = cf.ThreadPoolExecutor(max_workers=1)
+
+        def make():
+            self._brush = TextureBrushGpu(dictionary)
+            self._canvas = Canvas(rows, cols, "f32")
+            if background is not None:
+                self._canvas.setBackground(background)
+
+        self._pool.submit(make).result()
+        self._stop = threading.Event()
+        self._timer = None
+        if dry_interval > 0:
+            def tick():
+                while not self._stop.wait(dry_interval):
+                    try:
+                        self._pool.submit(self._canvas.dryStep)
+                    except RuntimeError:  # the pool has shut down
+                        return
+            self._timer = threading.Thread(target=tick, daemon=True)
+            self._timer.start()
+
+    def close(self) -> None:
+        if self._pool is None:
+            return
+        self._stop.set()
+        if self._timer is not None:
+            self._timer.join()
+
+        def release():
+            self._brush = None
+            self._canvas = None
+
+        self._pool.submit(release).result()
+        self._pool.shutdown(wait=True)
+        self._pool = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def getSize(self):
+        return self._rows, self._cols
+
+    def getBrushThicknessScale(self) -> float:
+        return self._scale
+
+    def render(self, path: np.ndarray, radius: float, ks):
+        """dip, setRadius, paintStroke on the worker (SbrRenderThread.cxx:70-78)."""
+        path = np.array(path, dtype=np.float64)
+        ks = (np.array(ks[0], dtype=np.float64), np.array(ks[1], dtype=np.float64))
+
+        def job():
+            self._brush.dip(ks)
+            self._brush.setRadius(radius)
+            self._brush.paintStroke(path, self._canvas)
+
+        return self._pool.submit(job)
+
+    def getLinearRgbImage(self):
+        """CanvasGpu::getCompositionLinearRgb: a (rows, cols, 3) float64 image."""
+        return self._pool.submit(lambda: self._canvas.getComposedGlsl().download())
+
+    def setBrushThicknessScale(self, scale: float) -> None:
+        self._scale = float(scale)
+        self._pool.submit(self._brush.setThicknessScale, float(scale))
+
+    def enableSmudge(self, enable: bool) -> None:
+        if enable:
+            raise PaintyError(4, "unsupported: the GL smudge pass is not provided")
+
+    def dryCanvas(self):
+        """dryStep(1.0) (SbrRenderThread.cxx:100-104)."""
+        return self._pool.submit(self._canvas.dryStep, 1.0)
+
+
 def mix_single_paint(weights: np.ndarray, palette_K: np.ndarray, palette_S: np.ndarray):
     """PaintMixer::mixSinglePaint (PaintMixer.cxx:327-355): (K, S) of the weighted mix."""
     w = np.ascontiguousarray(weights, dtype=np.float64)

@@ -665,7 +665,8 @@ int64_t paint_texture_stroke(painty_canvas* c, painty_texture_brush* b, const do
       sa.maxbits = maxbits;
       sa.pickupRate = static_cast<M>(0.1);      // Smudge.hxx:156
       sa.depositionRate = static_cast<M>(0.1);  // Smudge.hxx:158
-      sa.seed = static_cast<uint32_t>(c->id * 0x9e3779b97f4a7c15ull + c->version);
+      // from the canvas's write count: the same painting session gives the same bits
+      sa.seed = static_cast<uint32_t>(c->version * 0x9e3779b97f4a7c15ull >> 32);
       if (!steps.empty() && cells > 0) {
         // both maps in shared memory when they fit (side <= 64 in FP32, <= 45 in FP64)
         const size_t smem = 2 * cells * 7 * sizeof(M);

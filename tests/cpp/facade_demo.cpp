@@ -2,6 +2,8 @@
 //   facade_demo errors            argument errors surface as std::invalid_argument (no GPU)
 //   facade_demo paint IN OUT      paints the stroke described in IN, writes the canvas to OUT
 //   facade_demo palette IN OUT    LoadPalette(IN) then SavePalette(OUT) (no GPU)
+//   facade_demo sbr               strokes through SbrRenderThread equal the same strokes
+//                                 painted directly with TextureBrushGpu (GPU)
 // IN (doubles): rows, cols, fh, fw, footprint[fh*fw], npts, path[2*npts], radius, spacing,
 //               pickup, deposition, K[3], S[3], R0[rows*cols*3]
 // OUT (doubles): stamps, K[rows*cols*3], S[rows*cols*3], V[rows*cols], composite[rows*cols*3]
@@ -96,7 +98,78 @@ static int paint(const char* in, const char* out) {
   return 0;
 }
 
+// deterministic values in [0, 1) (a 64-bit LCG; the demo needs no particular generator)
+static double unit(uint64_t& s) {
+  s = s * 6364136223846793005ULL + 1442695040888963407ULL;
+  return static_cast<double>(s >> 11) * (1.0 / 9007199254740992.0);
+}
+
+static void fill_dictionary(pg::TextureBrushDictionary& d) {
+  uint64_t s = 99;
+  for (int rc = 0; rc < 2; rc++)
+    for (int lc = 0; lc < 2; lc++)
+      for (int k = 0; k < 2; k++) {
+        const int rows = rc ? 34 : 10, cols = lc ? 220 : 60;
+        std::vector<double> h(size_t(rows) * cols);
+        for (auto& x : h) x = unit(s);
+        d.add(rc ? 16 : 4, lc ? 200 : 50, h, rows, cols);
+      }
+}
+
+static int sbr() {
+  const int rows = 96, cols = 128;
+  std::vector<double> bg(size_t(rows) * cols * 3, 0.9);
+  struct Stroke {
+    std::vector<pg::vec2> path;
+    double radius;
+    std::array<pg::vec3, 2> ks;
+  };
+  std::vector<Stroke> strokes;
+  uint64_t s = 7;
+  for (int i = 0; i < 12; i++) {
+    Stroke st;
+    const int n = 2 + static_cast<int>(unit(s) * 5);
+    for (int p = 0; p < n; p++) st.path.push_back({unit(s) * cols, unit(s) * rows});
+    st.radius = 2.0 + 18.0 * unit(s);
+    st.ks = {pg::vec3{unit(s) * 5, unit(s) * 5, unit(s) * 5},
+             pg::vec3{0.05 + unit(s) * 3, 0.05 + unit(s) * 3, 0.05 + unit(s) * 3}};
+    strokes.push_back(st);
+  }
+  std::vector<double> a, b;
+  {
+    pg::TextureBrushDictionary dict(5);
+    fill_dictionary(dict);
+    pg::SbrRenderThread sbr(rows, cols, dict, bg, std::chrono::milliseconds(0));
+    std::vector<std::future<void>> done;
+    for (const auto& st : strokes) done.push_back(sbr.render(st.path, st.radius, st.ks));
+    a = sbr.getLinearRgbImage().get();
+    for (auto& f : done) f.get();
+    sbr.dryCanvas().get();
+    const auto dried = sbr.getLinearRgbImage().get();
+    if (dried.size() != a.size()) return 1;
+  }
+  {
+    pg::TextureBrushDictionary dict(5);
+    fill_dictionary(dict);
+    pg::TextureBrushGpu brush(dict);
+    pg::Canvas canvas(rows, cols, pg::Storage::F32);
+    canvas.setBackground(bg);
+    for (const auto& st : strokes) {
+      brush.dip(st.ks);
+      brush.setRadius(st.radius);
+      brush.paintStroke(st.path, canvas);
+    }
+    b = canvas.getComposedGlsl().download();
+  }
+  const bool same = a.size() == b.size() && std::memcmp(a.data(), b.data(), a.size() * 8) == 0;
+  bool painted = false;
+  for (size_t i = 0; i < a.size(); i++) painted = painted || a[i] != 0.9f;
+  std::printf("%s\n", same && painted ? "sbr ok" : "sbr FAILED");
+  return same && painted ? 0 : 1;
+}
+
 int main(int argc, char** argv) {
+  if (argc >= 2 && std::strcmp(argv[1], "sbr") == 0) return sbr();
   if (argc >= 2 && std::strcmp(argv[1], "errors") == 0) return errors();
   if (argc >= 4 && std::strcmp(argv[1], "paint") == 0) return paint(argv[2], argv[3]);
   if (argc >= 4 && std::strcmp(argv[1], "palette") == 0) return palette(argv[2], argv[3]);

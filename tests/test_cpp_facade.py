@@ -27,7 +27,7 @@ def demo(tmp_path_factory, pg):
     if shutil.which("g++") is None:
         pytest.skip("no C++ compiler")
     exe = tmp_path_factory.mktemp("cpp") / "facade_demo"
-    cmd = ["g++", "-std=c++17", "-O1", "-Wall", "-Werror", f"-I{ROOT / 'include'}",
+    cmd = ["g++", "-std=c++17", "-O1", "-pthread", "-Wall", "-Werror", f"-I{ROOT / 'include'}",
            str(ROOT / "tests" / "cpp" / "facade_demo.cpp"), "-o", str(exe), f"-L{LIB}",
            "-lpainty_gb300", f"-Wl,-rpath,{LIB}", f"-Wl,-rpath,{_cuda_lib()}"]
     subprocess.run(cmd, check=True, capture_output=True)
@@ -59,6 +59,14 @@ def test_facade_palette_round_trip(demo, tmp_path):
     back = P.load_palette(dst)
     for (K, S), (K2, S2) in zip(pal, back):
         assert np.array_equal(K, K2) and np.array_equal(S, S2)
+
+
+@pytest.mark.gpu
+def test_facade_sbr_render_thread(demo):
+    """SbrRenderThread's futures, on its worker thread, paint what direct calls paint."""
+    r = subprocess.run([str(demo), "sbr"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "sbr ok" in r.stdout
 
 
 @pytest.mark.gpu

@@ -152,3 +152,36 @@ def test_gl_path_errors(pg):
     with pytest.raises(pg.PaintyError):
         pg.Canvas(16, 16, "f64").dryStep(0.1)
     gb.paintStroke(np.array([[1.0, 1.0]]), pg.Canvas(16, 16, "f32"))  # one point: nothing
+
+
+def test_sbr_render_thread_matches_direct_calls(pg):
+    """SbrRenderThread's worker paints what direct TextureBrushGpu calls paint (drying off)."""
+    rows, cols = 80, 100
+    rng = np.random.default_rng(6)
+    textures = [((4, 50), rng.random((10, 60))), ((4, 200), rng.random((10, 220))),
+                ((16, 50), rng.random((34, 60))), ((16, 200), rng.random((34, 220)))]
+    strokes = _stroke_session(np.random.default_rng(2), rows, cols, 8)
+    bg = np.full((rows, cols, 3), 0.85)
+    d1, d2 = pg.TextureBrushDictionary(4), pg.TextureBrushDictionary(4)
+    for (rc, lc), t in textures:
+        d1.add(rc, lc, t)
+        d2.add(rc, lc, t)
+    sbr = pg.SbrRenderThread(rows, cols, d1, background=bg, dry_interval=0.0)
+    futs = [sbr.render(p, r, (K, S)) for p, r, K, S, _ in strokes]
+    img = sbr.getLinearRgbImage().result()
+    assert all(f.done() for f in futs)
+    sbr.dryCanvas().result()
+    dried = sbr.getLinearRgbImage().result()
+    sbr.close()
+    c = pg.Canvas(rows, cols, "f32")
+    c.setBackground(bg)
+    b = pg.TextureBrushGpu(d2)
+    for p, r, K, S, _ in strokes:
+        b.dip((K, S))
+        b.setRadius(r)
+        b.paintStroke(p, c)
+    np.testing.assert_array_equal(img, c.getComposedGlsl().download())
+    c.dryStep(1.0)
+    np.testing.assert_array_equal(dried, c.getComposedGlsl().download())
+    with pytest.raises(pg.PaintyError):
+        pg.SbrRenderThread(8, 8, d1, dry_interval=0.0).enableSmudge(True)
