@@ -339,22 +339,45 @@ __device__ __forceinline__ bool covers(const StripArgs& a, const Tri& t, long lo
 }
 
 // Raster pass 1: each strip triangle marks the centres it covers with its index (the last
-// triangle wins, as GL draws the strip in order without blending). One CTA per triangle.
+// triangle wins, as GL draws the strip in order without blending). A triangle's pixel box is
+// cut into 16 x 16 tiles shared out over the CTAs of its grid row; a tile whose four corner
+// regions all lie outside one edge is skipped whole (the strip's triangles are long and thin,
+// so most of a box is empty), otherwise each thread tests one pixel centre.
+constexpr int kCoverSplit = 16;  // CTAs per triangle
 __global__ void __launch_bounds__(256) strip_cover_kernel(const StripArgs a) {
   const int k = blockIdx.x;
   const Tri t = strip_tri(a, k);
   if (t.area == 0) return;
-  const long long xmin = min(a.X[t.ia], min(a.X[t.ib], a.X[t.ic]));
-  const long long xmax = max(a.X[t.ia], max(a.X[t.ib], a.X[t.ic]));
-  const long long ymin = min(a.Y[t.ia], min(a.Y[t.ib], a.Y[t.ic]));
-  const long long ymax = max(a.Y[t.ia], max(a.Y[t.ib], a.Y[t.ic]));
+  const long long xa = a.X[t.ia], ya = a.Y[t.ia], xb = a.X[t.ib], yb = a.Y[t.ib];
+  const long long xc = a.X[t.ic], yc = a.Y[t.ic];
+  const long long xmin = min(xa, min(xb, xc)), xmax = max(xa, max(xb, xc));
+  const long long ymin = min(ya, min(yb, yc)), ymax = max(ya, max(yb, yc));
   // pixel centres 256 x + 128 inside [xmin, xmax]
-  const long long x0 = max(0LL, floordiv256(xmin - 128 + 255)), x1 = min(static_cast<long long>(a.cols - 1), floordiv256(xmax - 128));
-  const long long y0 = max(0LL, floordiv256(ymin - 128 + 255)), y1 = min(static_cast<long long>(a.rows - 1), floordiv256(ymax - 128));
+  const long long x0 = max(0LL, floordiv256(xmin - 128 + 255));
+  const long long x1 = min(static_cast<long long>(a.cols - 1), floordiv256(xmax - 128));
+  const long long y0 = max(0LL, floordiv256(ymin - 128 + 255));
+  const long long y1 = min(static_cast<long long>(a.rows - 1), floordiv256(ymax - 128));
   if (x0 > x1 || y0 > y1) return;
-  const long long nx = x1 - x0 + 1, n = nx * (y1 - y0 + 1);
-  for (long long i = threadIdx.x; i < n; i += blockDim.x) {
-    const long long wy = y0 + i / nx, x = x0 + i % nx;
+  const long long tx = (x1 - x0) / 16 + 1, ty = (y1 - y0) / 16 + 1;
+  const int lx = threadIdx.x & 15, ly = threadIdx.x >> 4;
+  for (long long tile = blockIdx.y; tile < tx * ty; tile += gridDim.y) {
+    const long long bx = x0 + (tile % tx) * 16, by = y0 + (tile / tx) * 16;
+    // the tile's centre box [bx, bx + 15] x [by, by + 15] in 1/256 units
+    const long long cx0 = 256 * bx + 128, cx1 = cx0 + 256 * 15;
+    const long long cy0 = 256 * by + 128, cy1 = cy0 + 256 * 15;
+    bool outside = false;
+    const long long ex[3][4] = {{xb, yb, xc, yc}, {xc, yc, xa, ya}, {xa, ya, xb, yb}};
+#pragma unroll
+    for (int e = 0; e < 3; e++) {
+      // an edge function is affine: its maximum over the box is at a corner
+      const long long dx = ex[e][2] - ex[e][0], dy = ex[e][3] - ex[e][1];
+      const long long px = dy > 0 ? cx0 : cx1;  // maximises -dy * px
+      const long long py = dx > 0 ? cy1 : cy0;  // maximises dx * py
+      if (edge_fn(ex[e][0], ex[e][1], ex[e][2], ex[e][3], px, py) < 0) outside = true;
+    }
+    if (outside) continue;  // uniform over the CTA
+    const long long x = bx + lx, wy = by + ly;
+    if (x > x1 || wy > y1) continue;
     long long w[3];
     if (!covers(a, t, 256 * x + 128, 256 * wy + 128, w)) continue;
     const long long y = a.rows - 1 - wy;  // canvas row of window row wy
@@ -539,7 +562,7 @@ void gl_paint_stroke(painty_canvas* c, painty_gpu_texture_brush* b, const double
     sa.wy0 = static_cast<int>(wy0);
     sa.wnx = static_cast<int>(px1 - px0 + 1);
     sa.wny = static_cast<int>(wy1 - wy0 + 1);
-    strip_cover_kernel<<<nv - 2, 256, 0, st>>>(sa);
+    strip_cover_kernel<<<dim3(nv - 2, kCoverSplit), 256, 0, st>>>(sa);
     count_launch();
     PG_CUDA(cudaGetLastError());
     strip_sample_kernel<<<grid_for_px(static_cast<int64_t>(sa.wnx) * sa.wny), 256, 0, st>>>(sa);

@@ -77,7 +77,8 @@ __global__ void __launch_bounds__(256) render_lit_kernel(const void* canvas, con
   const M fj = static_cast<M>(j), fi = static_cast<M>(i);
   const V3<M> lightDirection = nrm3<M>({M(-200) - fj, M(-1500) - fi, M(-2000.) - s11});
   const V3<M> l = nrm3(lightDirection);
-  const V3<M> v = nrm3<M>({static_cast<M>(cols / 2.0) - fj, static_cast<M>(rows / 2.0) - fi,
+  // eyePos = (width / 2.0, height / 2.0, -100): exact in float too (sizes below 2^24)
+  const V3<M> v = nrm3<M>({static_cast<M>(cols) * M(0.5) - fj, static_cast<M>(rows) * M(0.5) - fi,
                            M(-100.) - s11});
   const V3<M> h = nrm3<M>({v.x + l.x, v.y + l.y, v.z + l.z});
   const M NdotH = fmax(M(0), dot3(n, h));

@@ -284,7 +284,7 @@ struct SmudgeArgs {
 };
 
 // Cells a thread exchanges per batch (its canvas loads are in flight together).
-template <class M> constexpr int kSmudgeBatch = sizeof(M) == 8 ? 2 : 4;
+template <class M> constexpr int kSmudgeBatch = 2;
 
 // Launch 2: Smudge::smudge (Smudge.hxx:38-145) with updateOrientation (:160-199), one CTA
 // walking the steps in order. Per step the map is rotated from one buffer into the other
@@ -316,50 +316,38 @@ __global__ void __launch_bounds__(kSmudgeThreads, 1) tb_smudge_kernel(const __gr
   // 1 / maxD: FP32 multiplies by it; FP64 divides as painty does
   const M rmaxD = M(1) / maxD;
   const M c0 = a.ctr, radius = a.radius, fside = static_cast<M>(side);
+  const float rside = 1.0f / static_cast<float>(side);
   SmudgeStep<M> st = a.steps[0];
   for (int64_t k = 0; k < a.nsteps; k++) {
     // the next step's parameters load while this one runs
     const SmudgeStep<M> st_next = a.steps[k + 1 < a.nsteps ? k + 1 : k];
-    // updateOrientation: nxt = cur rotated about the map centre
     const M cs = st.c, sn = st.s;
-    for (int i = tid; i < cells; i += T) {
-      const int y = i / side, x = i - y * side;
-      const M px = static_cast<M>(x) - c0, py = static_cast<M>(y) - c0;
-      const M qx = px * cs - py * sn + c0;
-      const M qy = px * sn + py * cs + c0;
-      if (qx < M(0) || qy < M(0) || qx >= fside || qy >= fside) {
-#pragma unroll
-        for (int q = 0; q < 7; q++) nxt[q * cells + i] = cur[q * cells + i];
-      } else {
-        // 0 <= q < side: the BORDER_REFLECT neighbours are q's cell and the next one, which
-        // reflects back onto the last cell at the border
-        const int fx = static_cast<int>(floor(qx)), fy = static_cast<int>(floor(qy));
-        const int x0 = fx, x1 = min(fx + 1, side - 1);
-        const int y0 = fy, y1 = min(fy + 1, side - 1);
-        const M wa = qx - static_cast<M>(fx), wc = qy - static_cast<M>(fy);
-        const int o00 = y0 * side + x0, o01 = y0 * side + x1;
-        const int o10 = y1 * side + x0, o11 = y1 * side + x1;
-#pragma unroll
-        for (int q = 0; q < 7; q++) {
-          const M* s = cur + q * cells;
-          nxt[q * cells + i] = (s[o00] * (M(1) - wa) + s[o01] * wa) * (M(1) - wc) +
-                               (s[o10] * (M(1) - wa) + s[o11] * wa) * wc;
-        }
-      }
-    }
-    __syncthreads();
-    // paint exchange between the pickup map and the canvas under it; a cell and its canvas
-    // pixel are touched by no other cell of the step
+    // One pass per step: a cell's rotated value (updateOrientation: nxt = cur rotated about
+    // the map centre) depends only on the previous map, and its exchange with the canvas only
+    // on that value and its own canvas pixel, so each thread rotates and exchanges its cells
+    // without waiting for the others; one barrier ends the step.
     for (int base = 0; base < cells; base += J * T) {
-      int cid[J], pix[J];
+      int cxy[J], pix[J];  // cell (y << 16 | x), or -1; canvas record, or -1
       M D[J];
+      PixRec<TK, TV> cr[J];
 #pragma unroll
       for (int j = 0; j < J; j++) {
         const int i = base + j * T + tid;
-        cid[j] = -1;
+        cxy[j] = -1;
+        pix[j] = -1;
         D[j] = M(0);
         if (i >= cells) continue;
-        const int y = i / side, x = i - y * side;
+        // (x, y) of cell i: a float quotient corrected by one step is exact
+        int y = static_cast<int>((static_cast<float>(i) + 0.5f) * rside);
+        int x = i - y * side;
+        if (x < 0) {
+          y--;
+          x += side;
+        } else if (x >= side) {
+          y++;
+          x -= side;
+        }
+        cxy[j] = y << 16 | x;
         const int cpx = x + st.roi_x, cpy = y + st.roi_y;
         if (cpx < 0 || cpy < 0 || cpx >= a.cols || cpy >= a.rows) continue;
         const int mx = cpx - a.bx0, my = cpy - a.by0;
@@ -369,62 +357,88 @@ __global__ void __launch_bounds__(kSmudgeThreads, 1) tb_smudge_kernel(const __gr
         const M dx = st.cx - static_cast<M>(cpx);
         const M dy = st.cy - static_cast<M>(cpy);
         if (sqrt(dx * dx + dy * dy) > radius) continue;
+        // the thickness and the canvas record load together, before the rotation
         D[j] = __ldg(a.tmap + static_cast<int64_t>(tpy) * a.tcols + tpx);
-        cid[j] = i;
         pix[j] = static_cast<int>(static_cast<int64_t>(cpy) * a.pitch + cpx);
+        cr[j] = load_rec<false, TK, TV>(a.canvas, pix[j]);
       }
-      PixRec<TK, TV> cr[J];
-#pragma unroll
-      for (int j = 0; j < J; j++)
-        if (cid[j] >= 0 && D[j] > M(0)) cr[j] = load_rec<false, TK, TV>(a.canvas, pix[j]);
 #pragma unroll
       for (int j = 0; j < J; j++) {
-        if (cid[j] < 0 || !(D[j] > M(0))) continue;
-        const int i = cid[j];
-        const M cV = ld_elem<M>(&cr[j].v[6]), pV = nxt[6 * cells + i];
-        M cVl, pVl;
-        if constexpr (sizeof(M) == 8) {
-          cVl = cV * a.depositionRate * D[j] / maxD;
-          pVl = pV * a.pickupRate * D[j] / maxD;
+        if (cxy[j] < 0) continue;
+        const int y = cxy[j] >> 16, x = cxy[j] & 0xffff;
+        const int i = y * side + x;
+        M val[7];
+        const M px = static_cast<M>(x) - c0, py = static_cast<M>(y) - c0;
+        const M qx = px * cs - py * sn + c0;
+        const M qy = px * sn + py * cs + c0;
+        if (qx < M(0) || qy < M(0) || qx >= fside || qy >= fside) {
+#pragma unroll
+          for (int q = 0; q < 7; q++) val[q] = cur[q * cells + i];
         } else {
-          cVl = cV * a.depositionRate * D[j] * rmaxD;
-          pVl = pV * a.pickupRate * D[j] * rmaxD;
-        }
-        const M cVr = cV - cVl;
-        const M pVr = pV - pVl;
-        M cK[6], pK[6];
+          // 0 <= q < side: the BORDER_REFLECT neighbours are q's cell and the next one, which
+          // reflects back onto the last cell at the border
+          const int fx = static_cast<int>(floor(qx)), fy = static_cast<int>(floor(qy));
+          const int x1 = min(fx + 1, side - 1), y1 = min(fy + 1, side - 1);
+          const M wa = qx - static_cast<M>(fx), wc = qy - static_cast<M>(fy);
+          const int o00 = fy * side + fx, o01 = fy * side + x1;
+          const int o10 = y1 * side + fx, o11 = y1 * side + x1;
 #pragma unroll
-        for (int q = 0; q < 6; q++) {
-          cK[q] = ld_elem<M>(&cr[j].k[q]);
-          pK[q] = nxt[q * cells + i];
-        }
-        constexpr double MinVolume = 0.001;
-        const M pVnew = pVr + cVl;
-        if (pVnew > M(MinVolume)) {
-          const M inv = M(1) / pVnew;
-#pragma unroll
-          for (int q = 0; q < 6; q++) nxt[q * cells + i] = inv * (pVr * pK[q] + cVl * cK[q]);
-          nxt[6 * cells + i] = pVnew > M(0) ? pVnew : M(0);
-        }
-        const M cVnew = cVr + pVl;
-        if (cVnew > M(MinVolume)) {
-          // 16-bit storage rounds stochastically: a step moves a pixel by a small fraction of
-          // the difference, which round-to-nearest would drop (bits from stroke, step, pixel)
-          uint32_t h[4] = {0u, 0u, 0u, 0u};
-          if constexpr (sizeof(TK) == 2) {
-            h[0] = hash32(hash32(a.seed + static_cast<uint32_t>(k)) ^
-                          (static_cast<uint32_t>(pix[j]) * 0x9e3779b1u));
-#pragma unroll
-            for (int q = 1; q < 4; q++) h[q] = hash32(h[q - 1] + 0x632be5abu);
+          for (int q = 0; q < 7; q++) {
+            const M* sp = cur + q * cells;
+            val[q] = (sp[o00] * (M(1) - wa) + sp[o01] * wa) * (M(1) - wc) +
+                     (sp[o10] * (M(1) - wa) + sp[o11] * wa) * wc;
           }
-          const M inv = M(1) / cVnew;
-#pragma unroll
-          for (int q = 0; q < 6; q++)
-            st_elem_sr<M>(&cr[j].k[q], inv * (cVr * cK[q] + pVl * pK[q]),
-                          (q & 1) ? h[q >> 1] >> 16 : h[q >> 1]);
-          st_elem_sr<M>(&cr[j].v[6], cVnew > M(0) ? cVnew : M(0), h[3]);
-          store_rec<TK, TV>(a.canvas, pix[j], cr[j]);
         }
+        // the exchange (Smudge.hxx:60-142) where the cell covers painted canvas
+        if (pix[j] >= 0 && D[j] > M(0)) {
+          const M cV = ld_elem<M>(&cr[j].v[6]), pV = val[6];
+          M cVl, pVl;
+          if constexpr (sizeof(M) == 8) {
+            cVl = cV * a.depositionRate * D[j] / maxD;
+            pVl = pV * a.pickupRate * D[j] / maxD;
+          } else {
+            cVl = cV * a.depositionRate * D[j] * rmaxD;
+            pVl = pV * a.pickupRate * D[j] * rmaxD;
+          }
+          const M cVr = cV - cVl;
+          const M pVr = pV - pVl;
+          M cK[6], pK[6];
+#pragma unroll
+          for (int q = 0; q < 6; q++) {
+            cK[q] = ld_elem<M>(&cr[j].k[q]);
+            pK[q] = val[q];
+          }
+          constexpr double MinVolume = 0.001;
+          const M pVnew = pVr + cVl;
+          if (pVnew > M(MinVolume)) {
+            const M inv = M(1) / pVnew;
+#pragma unroll
+            for (int q = 0; q < 6; q++) val[q] = inv * (pVr * pK[q] + cVl * cK[q]);
+            val[6] = pVnew > M(0) ? pVnew : M(0);
+          }
+          const M cVnew = cVr + pVl;
+          if (cVnew > M(MinVolume)) {
+            // 16-bit storage rounds stochastically: a step moves a pixel by a small fraction
+            // of the difference, which round-to-nearest would drop (bits from stroke, step,
+            // pixel)
+            uint32_t h[4] = {0u, 0u, 0u, 0u};
+            if constexpr (sizeof(TK) == 2) {
+              h[0] = hash32(hash32(a.seed + static_cast<uint32_t>(k)) ^
+                            (static_cast<uint32_t>(pix[j]) * 0x9e3779b1u));
+#pragma unroll
+              for (int q = 1; q < 4; q++) h[q] = hash32(h[q - 1] + 0x632be5abu);
+            }
+            const M inv = M(1) / cVnew;
+#pragma unroll
+            for (int q = 0; q < 6; q++)
+              st_elem_sr<M>(&cr[j].k[q], inv * (cVr * cK[q] + pVl * pK[q]),
+                            (q & 1) ? h[q >> 1] >> 16 : h[q >> 1]);
+            st_elem_sr<M>(&cr[j].v[6], cVnew > M(0) ? cVnew : M(0), h[3]);
+            store_rec<TK, TV>(a.canvas, pix[j], cr[j]);
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < 7; q++) nxt[q * cells + i] = val[q];
       }
     }
     __syncthreads();
@@ -529,6 +543,7 @@ int64_t paint_texture_stroke(painty_canvas* c, painty_texture_brush* b, const do
   // the smudge steps u by 1 / length: about length + 1 steps
   PG_REQUIRE(!b->useSmudge || length < static_cast<double>(1 << 26),
              "stroke too long for the smudge");
+  PG_REQUIRE(!b->useSmudge || b->side <= 4096, "smudge map wider than 4096 (radius above 2048)");
   // outline: the right side reversed, then the left side; uv (u, 1) then (u, 0)
   std::vector<double2> up, down, upUv, downUv;
   for (size_t i = 0; i < v.size(); ++i) {
