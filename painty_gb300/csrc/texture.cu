@@ -14,6 +14,7 @@
 // storage reproduces painty bit for bit). Outline geometry and texture sampling are double in
 // every storage mode; the smudge and the deposit run in the storage's math type.
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <type_traits>
@@ -286,6 +287,76 @@ struct SmudgeArgs {
 // Cells a thread exchanges per batch (its canvas loads are in flight together).
 template <class M> constexpr int kSmudgeBatch = 2;
 
+// The paint exchange of one smudge cell (values `val`: K r,g,b, S r,g,b, V) with its canvas
+// pixel (record `cr` at `pix`) under thickness D (Smudge.hxx:60-142).
+template <class TK, class TV, class M>
+__device__ __forceinline__ void smudge_exchange(const SmudgeArgs<M>& a, M (&val)[7],
+                                                PixRec<TK, TV>& cr, M D, int pix, int64_t k,
+                                                M maxD, M rmaxD) {
+  const M cV = ld_elem<M>(&cr.v[6]), pV = val[6];
+  M cVl, pVl;
+  if constexpr (sizeof(M) == 8) {  // painty divides by maxD
+    cVl = cV * a.depositionRate * D / maxD;
+    pVl = pV * a.pickupRate * D / maxD;
+  } else {
+    cVl = cV * a.depositionRate * D * rmaxD;
+    pVl = pV * a.pickupRate * D * rmaxD;
+  }
+  const M cVr = cV - cVl;
+  const M pVr = pV - pVl;
+  M cK[6], pK[6];
+#pragma unroll
+  for (int q = 0; q < 6; q++) {
+    cK[q] = ld_elem<M>(&cr.k[q]);
+    pK[q] = val[q];
+  }
+  constexpr double MinVolume = 0.001;
+  const M pVnew = pVr + cVl;
+  if (pVnew > M(MinVolume)) {
+    const M inv = M(1) / pVnew;
+#pragma unroll
+    for (int q = 0; q < 6; q++) val[q] = inv * (pVr * pK[q] + cVl * cK[q]);
+    val[6] = pVnew > M(0) ? pVnew : M(0);
+  }
+  const M cVnew = cVr + pVl;
+  if (cVnew > M(MinVolume)) {
+    // 16-bit storage rounds stochastically: a step moves a pixel by a small fraction of the
+    // difference, which round-to-nearest would drop (bits from stroke, step, pixel)
+    uint32_t h[4] = {0u, 0u, 0u, 0u};
+    if constexpr (sizeof(TK) == 2) {
+      h[0] = hash32(hash32(a.seed + static_cast<uint32_t>(k)) ^
+                    (static_cast<uint32_t>(pix) * 0x9e3779b1u));
+#pragma unroll
+      for (int q = 1; q < 4; q++) h[q] = hash32(h[q - 1] + 0x632be5abu);
+    }
+    const M inv = M(1) / cVnew;
+#pragma unroll
+    for (int q = 0; q < 6; q++)
+      st_elem_sr<M>(&cr.k[q], inv * (cVr * cK[q] + pVl * pK[q]),
+                    (q & 1) ? h[q >> 1] >> 16 : h[q >> 1]);
+    st_elem_sr<M>(&cr.v[6], cVnew > M(0) ? cVnew : M(0), h[3]);
+    store_rec<TK, TV>(a.canvas, pix, cr);
+  }
+}
+
+// Geometry of one smudge cell (x, y) at a step: its canvas record, or -1 when the cell is off
+// the canvas, outside the thickness map or beyond the smudge radius; D its thickness.
+template <class M>
+__device__ __forceinline__ int smudge_cell_pixel(const SmudgeArgs<M>& a, const SmudgeStep<M>& st,
+                                                 int x, int y, M* D) {
+  const int cpx = x + st.roi_x, cpy = y + st.roi_y;
+  if (cpx < 0 || cpy < 0 || cpx >= a.cols || cpy >= a.rows) return -1;
+  const int mx = cpx - a.bx0, my = cpy - a.by0;
+  const int tpx = (a.bxf && mx >= 1) ? mx - 1 : mx;
+  const int tpy = (a.byf && my >= 1) ? my - 1 : my;
+  if (tpx < 0 || tpy < 0 || tpx >= a.tcols || tpy >= a.trows) return -1;
+  const M dx = st.cx - static_cast<M>(cpx);
+  const M dy = st.cy - static_cast<M>(cpy);
+  if (sqrt(dx * dx + dy * dy) > a.radius) return -1;
+  *D = __ldg(a.tmap + static_cast<int64_t>(tpy) * a.tcols + tpx);
+  return static_cast<int>(static_cast<int64_t>(cpy) * a.pitch + cpx);
+}
+
 // Launch 2: Smudge::smudge (Smudge.hxx:38-145) with updateOrientation (:160-199), one CTA
 // walking the steps in order. Per step the map is rotated from one buffer into the other
 // (painty copies dst to src, then rotates src into dst: cells that rotate in from outside keep
@@ -315,7 +386,7 @@ __global__ void __launch_bounds__(kSmudgeThreads, 1) tb_smudge_kernel(const __gr
     maxD = __uint_as_float(static_cast<unsigned>(*a.maxbits));
   // 1 / maxD: FP32 multiplies by it; FP64 divides as painty does
   const M rmaxD = M(1) / maxD;
-  const M c0 = a.ctr, radius = a.radius, fside = static_cast<M>(side);
+  const M c0 = a.ctr, fside = static_cast<M>(side);
   const float rside = 1.0f / static_cast<float>(side);
   SmudgeStep<M> st = a.steps[0];
   for (int64_t k = 0; k < a.nsteps; k++) {
@@ -348,19 +419,9 @@ __global__ void __launch_bounds__(kSmudgeThreads, 1) tb_smudge_kernel(const __gr
           x -= side;
         }
         cxy[j] = y << 16 | x;
-        const int cpx = x + st.roi_x, cpy = y + st.roi_y;
-        if (cpx < 0 || cpy < 0 || cpx >= a.cols || cpy >= a.rows) continue;
-        const int mx = cpx - a.bx0, my = cpy - a.by0;
-        const int tpx = (a.bxf && mx >= 1) ? mx - 1 : mx;
-        const int tpy = (a.byf && my >= 1) ? my - 1 : my;
-        if (tpx < 0 || tpy < 0 || tpx >= a.tcols || tpy >= a.trows) continue;
-        const M dx = st.cx - static_cast<M>(cpx);
-        const M dy = st.cy - static_cast<M>(cpy);
-        if (sqrt(dx * dx + dy * dy) > radius) continue;
         // the thickness and the canvas record load together, before the rotation
-        D[j] = __ldg(a.tmap + static_cast<int64_t>(tpy) * a.tcols + tpx);
-        pix[j] = static_cast<int>(static_cast<int64_t>(cpy) * a.pitch + cpx);
-        cr[j] = load_rec<false, TK, TV>(a.canvas, pix[j]);
+        pix[j] = smudge_cell_pixel(a, st, x, y, &D[j]);
+        if (pix[j] >= 0) cr[j] = load_rec<false, TK, TV>(a.canvas, pix[j]);
       }
 #pragma unroll
       for (int j = 0; j < J; j++) {
@@ -390,53 +451,8 @@ __global__ void __launch_bounds__(kSmudgeThreads, 1) tb_smudge_kernel(const __gr
           }
         }
         // the exchange (Smudge.hxx:60-142) where the cell covers painted canvas
-        if (pix[j] >= 0 && D[j] > M(0)) {
-          const M cV = ld_elem<M>(&cr[j].v[6]), pV = val[6];
-          M cVl, pVl;
-          if constexpr (sizeof(M) == 8) {
-            cVl = cV * a.depositionRate * D[j] / maxD;
-            pVl = pV * a.pickupRate * D[j] / maxD;
-          } else {
-            cVl = cV * a.depositionRate * D[j] * rmaxD;
-            pVl = pV * a.pickupRate * D[j] * rmaxD;
-          }
-          const M cVr = cV - cVl;
-          const M pVr = pV - pVl;
-          M cK[6], pK[6];
-#pragma unroll
-          for (int q = 0; q < 6; q++) {
-            cK[q] = ld_elem<M>(&cr[j].k[q]);
-            pK[q] = val[q];
-          }
-          constexpr double MinVolume = 0.001;
-          const M pVnew = pVr + cVl;
-          if (pVnew > M(MinVolume)) {
-            const M inv = M(1) / pVnew;
-#pragma unroll
-            for (int q = 0; q < 6; q++) val[q] = inv * (pVr * pK[q] + cVl * cK[q]);
-            val[6] = pVnew > M(0) ? pVnew : M(0);
-          }
-          const M cVnew = cVr + pVl;
-          if (cVnew > M(MinVolume)) {
-            // 16-bit storage rounds stochastically: a step moves a pixel by a small fraction
-            // of the difference, which round-to-nearest would drop (bits from stroke, step,
-            // pixel)
-            uint32_t h[4] = {0u, 0u, 0u, 0u};
-            if constexpr (sizeof(TK) == 2) {
-              h[0] = hash32(hash32(a.seed + static_cast<uint32_t>(k)) ^
-                            (static_cast<uint32_t>(pix[j]) * 0x9e3779b1u));
-#pragma unroll
-              for (int q = 1; q < 4; q++) h[q] = hash32(h[q - 1] + 0x632be5abu);
-            }
-            const M inv = M(1) / cVnew;
-#pragma unroll
-            for (int q = 0; q < 6; q++)
-              st_elem_sr<M>(&cr[j].k[q], inv * (cVr * cK[q] + pVl * pK[q]),
-                            (q & 1) ? h[q >> 1] >> 16 : h[q >> 1]);
-            st_elem_sr<M>(&cr[j].v[6], cVnew > M(0) ? cVnew : M(0), h[3]);
-            store_rec<TK, TV>(a.canvas, pix[j], cr[j]);
-          }
-        }
+        if (pix[j] >= 0 && D[j] > M(0))
+          smudge_exchange<TK, TV, M>(a, val, cr[j], D[j], pix[j], k, maxD, rmaxD);
 #pragma unroll
         for (int q = 0; q < 7; q++) nxt[q * cells + i] = val[q];
       }
@@ -450,6 +466,137 @@ __global__ void __launch_bounds__(kSmudgeThreads, 1) tb_smudge_kernel(const __gr
   // the state map: write the current map back to the first global map
   if (SM || cur != a.maps)
     for (int i = tid; i < 7 * cells; i += T) a.maps[i] = cur[i];
+}
+
+// Distributed shared memory: the shared::cluster address of `local` (a shared address of this
+// CTA) in CTA `rank` of the cluster, and loads from such addresses.
+__device__ __forceinline__ unsigned dsmem_map(unsigned local, unsigned rank) {
+  unsigned r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(local), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ float dsmem_ld(unsigned addr, float) {
+  float v;
+  asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(addr) : "memory");
+  return v;
+}
+__device__ __forceinline__ double dsmem_ld(unsigned addr, double) {
+  double v;
+  asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(addr) : "memory");
+  return v;
+}
+
+constexpr int kSmudgeClusterThreads = 256;
+
+// Launch 2 on a thread-block cluster: the same steps with the map's rows split into bands, one
+// per CTA (band b: rows [b B, b B + B), B = ceil(side / CTAs)), each band's two buffers in its
+// CTA's shared memory. A cell's rotation reads its four neighbours wherever they live through
+// distributed shared memory; its exchange touches only its own band and canvas pixel. One
+// cluster barrier per step orders the maps and the canvas writes (canvas reads bypass L1:
+// another CTA may have written the pixel in an earlier step). The FP64 rotation's work spreads
+// over the cluster's SMs.
+template <class TK, class TV, class M>
+__global__ void __launch_bounds__(kSmudgeClusterThreads, 1)
+    tb_smudge_cluster_kernel(const __grid_constant__ SmudgeArgs<M> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int J = kSmudgeBatch<M>;
+  const int tid = threadIdx.x, T = blockDim.x;
+  const int side = a.side, cells = side * side;
+  const int rank = static_cast<int>(cluster_rank()), C = static_cast<int>(cluster_size());
+  const int B = (side + C - 1) / C;            // band rows
+  const int P = B * side;                      // band cells (plane stride in shared memory)
+  const int ry0 = rank * B, ry1 = min(side, ry0 + B);
+  const int nloc = ry1 > ry0 ? (ry1 - ry0) * side : 0;
+  M* cur = reinterpret_cast<M*>(smem_raw);
+  M* nxt = cur + 7 * P;
+  for (int i = tid; i < nloc; i += T)
+#pragma unroll
+    for (int q = 0; q < 7; q++) cur[q * P + i] = a.maps[q * cells + ry0 * side + i];
+  cluster_barrier();  // every band loaded before any remote read
+  M maxD;
+  if constexpr (sizeof(M) == 8)
+    maxD = __longlong_as_double(static_cast<long long>(*a.maxbits));
+  else
+    maxD = __uint_as_float(static_cast<unsigned>(*a.maxbits));
+  const M rmaxD = M(1) / maxD;
+  const M c0 = a.ctr, fside = static_cast<M>(side);
+  const float rside = 1.0f / static_cast<float>(side);
+  constexpr unsigned ES = sizeof(M);
+  SmudgeStep<M> st = a.steps[0];
+  for (int64_t k = 0; k < a.nsteps; k++) {
+    const SmudgeStep<M> st_next = a.steps[k + 1 < a.nsteps ? k + 1 : k];
+    const M cs = st.c, sn = st.s;
+    const unsigned cur_s = static_cast<unsigned>(__cvta_generic_to_shared(cur));
+    for (int base = 0; base < nloc; base += J * T) {
+      int cxy[J], pix[J];
+      M D[J];
+      PixRec<TK, TV> cr[J];
+#pragma unroll
+      for (int j = 0; j < J; j++) {
+        const int li = base + j * T + tid;
+        cxy[j] = -1;
+        pix[j] = -1;
+        D[j] = M(0);
+        if (li >= nloc) continue;
+        int yl = static_cast<int>((static_cast<float>(li) + 0.5f) * rside);
+        int x = li - yl * side;
+        if (x < 0) {
+          yl--;
+          x += side;
+        } else if (x >= side) {
+          yl++;
+          x -= side;
+        }
+        const int y = ry0 + yl;
+        cxy[j] = y << 16 | x;
+        pix[j] = smudge_cell_pixel(a, st, x, y, &D[j]);
+        if (pix[j] >= 0) cr[j] = load_rec<true, TK, TV>(a.canvas, pix[j]);
+      }
+#pragma unroll
+      for (int j = 0; j < J; j++) {
+        if (cxy[j] < 0) continue;
+        const int y = cxy[j] >> 16, x = cxy[j] & 0xffff;
+        const int li = (y - ry0) * side + x;
+        M val[7];
+        const M px = static_cast<M>(x) - c0, py = static_cast<M>(y) - c0;
+        const M qx = px * cs - py * sn + c0;
+        const M qy = px * sn + py * cs + c0;
+        if (qx < M(0) || qy < M(0) || qx >= fside || qy >= fside) {
+#pragma unroll
+          for (int q = 0; q < 7; q++) val[q] = cur[q * P + li];
+        } else {
+          const int fx = static_cast<int>(floor(qx)), fy = static_cast<int>(floor(qy));
+          const int x1 = min(fx + 1, side - 1), y1 = min(fy + 1, side - 1);
+          const M wa = qx - static_cast<M>(fx), wc = qy - static_cast<M>(fy);
+          // the two neighbour rows, in their bands' CTAs
+          const int o0 = fy / B, o1 = y1 / B;
+          const unsigned r0 = dsmem_map(cur_s + ES * static_cast<unsigned>((fy - o0 * B) * side), o0);
+          const unsigned r1 = dsmem_map(cur_s + ES * static_cast<unsigned>((y1 - o1 * B) * side), o1);
+          const unsigned ax0 = ES * static_cast<unsigned>(fx), ax1 = ES * static_cast<unsigned>(x1);
+#pragma unroll
+          for (int q = 0; q < 7; q++) {
+            const unsigned pq = ES * static_cast<unsigned>(q * P);
+            const M s00 = dsmem_ld(r0 + pq + ax0, M(0)), s01 = dsmem_ld(r0 + pq + ax1, M(0));
+            const M s10 = dsmem_ld(r1 + pq + ax0, M(0)), s11 = dsmem_ld(r1 + pq + ax1, M(0));
+            val[q] = (s00 * (M(1) - wa) + s01 * wa) * (M(1) - wc) +
+                     (s10 * (M(1) - wa) + s11 * wa) * wc;
+          }
+        }
+        if (pix[j] >= 0 && D[j] > M(0))
+          smudge_exchange<TK, TV, M>(a, val, cr[j], D[j], pix[j], k, maxD, rmaxD);
+#pragma unroll
+        for (int q = 0; q < 7; q++) nxt[q * P + li] = val[q];
+      }
+    }
+    cluster_barrier();  // the step's maps and canvas writes before the next step's reads
+    M* t = cur;
+    cur = nxt;
+    nxt = t;
+    st = st_next;
+  }
+  for (int i = tid; i < nloc; i += T)
+#pragma unroll
+    for (int q = 0; q < 7; q++) a.maps[q * cells + ry0 * side + i] = cur[q * P + i];
 }
 
 template <class M>
@@ -503,6 +650,71 @@ int max_dyn_smem() {
 
 int grid_of(int64_t n, int block) {
   return static_cast<int>(std::max<int64_t>(1, std::min<int64_t>((n + block - 1) / block, 152 * 16)));
+}
+
+size_t smudge_cluster_smem(int side, int cl, size_t es) {
+  const size_t B = static_cast<size_t>((side + cl - 1) / cl);
+  return 2 * 7 * B * static_cast<size_t>(side) * es;
+}
+
+// CTAs of the smudge cluster for a map of `side`: PAINTY_SMUDGE_CLUSTER (1, 2, 4, 8, 16) when
+// set, else 16 (FP64: its rotation is bound by the FP64 rate) or 8 (FP32) when the device can
+// co-schedule such a cluster with the band buffers in shared memory; 1 means one CTA.
+template <class TK, class TV, class M>
+int smudge_cluster(int side) {
+  int want = sizeof(M) == 8 ? 16 : 8;
+  if (const char* v = std::getenv("PAINTY_SMUDGE_CLUSTER")) {
+    const int n = std::atoi(v);
+    if (n == 1 || n == 2 || n == 4 || n == 8 || n == 16) want = n;
+  }
+  while (want > 1 && want > side) want /= 2;  // at least one map row per CTA
+  auto kern = tb_smudge_cluster_kernel<TK, TV, M>;
+  for (; want > 1; want /= 2) {
+    const size_t smem = smudge_cluster_smem(side, want, sizeof(M));
+    if (smem > static_cast<size_t>(max_dyn_smem())) continue;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(smem)) != cudaSuccess ||
+        (want > 8 &&
+         cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+           cudaSuccess)) {
+      cudaGetLastError();
+      continue;
+    }
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(static_cast<unsigned>(want));
+    cfg.blockDim = dim3(kSmudgeClusterThreads);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = static_cast<unsigned>(want);
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, kern, &cfg) == cudaSuccess && n >= 1) return want;
+    cudaGetLastError();
+  }
+  return 1;
+}
+
+template <class TK, class TV, class M>
+void launch_smudge_cluster(const SmudgeArgs<M>& sa, int cl, cudaStream_t st) {
+  auto kern = tb_smudge_cluster_kernel<TK, TV, M>;
+  const size_t smem = smudge_cluster_smem(sa.side, cl, sizeof(M));
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(static_cast<unsigned>(cl));
+  cfg.blockDim = dim3(kSmudgeClusterThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = static_cast<unsigned>(cl);
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  PG_CUDA(cudaLaunchKernelEx(&cfg, kern, sa));
 }
 
 // TextureBrush::paintStroke (TextureBrush.hxx:52-205); returns the pixels painted.
@@ -683,9 +895,14 @@ int64_t paint_texture_stroke(painty_canvas* c, painty_texture_brush* b, const do
       // from the canvas's write count: the same painting session gives the same bits
       sa.seed = static_cast<uint32_t>(c->version * 0x9e3779b97f4a7c15ull >> 32);
       if (!steps.empty() && cells > 0) {
-        // both maps in shared memory when they fit (side <= 64 in FP32, <= 45 in FP64)
+        // a cluster of CTAs shares the map by bands when the device has one free; otherwise
+        // one CTA holds both maps in shared memory when they fit (side <= 64 in FP32, <= 45
+        // in FP64), else in global memory
         const size_t smem = 2 * cells * 7 * sizeof(M);
-        if (smem <= static_cast<size_t>(max_dyn_smem())) {
+        const int cl = smudge_cluster<TK, TV, M>(b->side);
+        if (cl > 1) {
+          launch_smudge_cluster<TK, TV, M>(sa, cl, st);
+        } else if (smem <= static_cast<size_t>(max_dyn_smem())) {
           auto kern = tb_smudge_kernel<TK, TV, M, true>;
           PG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(smem)));

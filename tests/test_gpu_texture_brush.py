@@ -43,10 +43,14 @@ def test_f64_bitexact_vs_reference_fixture(pg, golden, name):
         assert np.array_equal(c.download(p), fx[f"{name}/out_{p}"]), p
 
 
-# radii up to 20: the smudge maps fit in shared memory; 36-44: they stay in global memory
-@pytest.mark.parametrize("smudge,rmin,rmax", [(True, 2.0, 20.0), (False, 2.0, 20.0),
-                                              (True, 36.0, 44.0)])
-def test_f64_bitexact_vs_oracle_random(pg, oracle, smudge, rmin, rmax):
+# cluster "": the default launch (a 16-CTA cluster in FP64); "1": one CTA, with both smudge maps
+# in shared memory for radii up to 20 and in global memory for 36-44; "2": a 2-CTA cluster
+@pytest.mark.parametrize("smudge,rmin,rmax,cluster", [
+    (True, 2.0, 20.0, ""), (False, 2.0, 20.0, ""), (True, 36.0, 44.0, ""),
+    (True, 2.0, 20.0, "1"), (True, 36.0, 44.0, "1"), (True, 2.0, 20.0, "2")])
+def test_f64_bitexact_vs_oracle_random(pg, oracle, monkeypatch, smudge, rmin, rmax, cluster):
+    if cluster:
+        monkeypatch.setenv("PAINTY_SMUDGE_CLUSTER", cluster)
     rng = np.random.default_rng(101 + smudge)
     rows, cols = 72, 96
     tex = workloads.stroke_texture(seed=13)
