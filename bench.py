@@ -475,7 +475,7 @@ def run_ours(args):
         batch = {s_: run_batch(pg, torch, s_, args.batch_canvases, args.batch_max_strokes,
                                rank, ws) for s_ in ("f32", "f16")}
     if rank == 0 and not args.no_stamps:
-        stamps = run_stamps_config0(pg, torch)
+        stamps = run_stamps_config0(pg, torch, cpu=not args.no_cpu)
         serve = run_serve(pg, torch, args.serve_rate, args.serve_seconds)
         prec = run_precision(pg, torch)
     if rank == 0 and not args.no_cpu:
@@ -520,7 +520,7 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def run_stamps_config0(pg, torch, nstrokes: int = 200):
+def run_stamps_config0(pg, torch, nstrokes: int = 200, cpu: bool = False):
     """1024x768 FP32 canvas, 200 strokes, r ~ U[8,32], spacing 0.25 r, through the C ABI."""
     from painty_gb300 import workloads
 
@@ -546,11 +546,35 @@ def run_stamps_config0(pg, torch, nstrokes: int = 200):
     n = step()
     torch.cuda.synchronize()
     dt = time.perf_counter() - t
-    return {"metric": "stamps/s", "value": round(n / dt, 1), "unit": "stamps/s",
-            "stamps_per_step": n, "ms_per_step": round(dt * 1e3, 2),
-            "config": "1024x768 FP32, 200 strokes, r U[8,32], spacing 0.25 r, snapshot on, "
-                      "deposit 0.1, pickup 0.05, final composite; through the C ABI",
-            "gpu_launches": pg.kernel_launch_count() - l0}
+    out = {"metric": "stamps/s", "value": round(n / dt, 1), "unit": "stamps/s",
+           "stamps_per_step": n, "ms_per_step": round(dt * 1e3, 2),
+           "config": "1024x768 FP32, 200 strokes, r U[8,32], spacing 0.25 r, snapshot on, "
+                     "deposit 0.1, pickup 0.05, final composite; through the C ABI",
+           "gpu_launches": pg.kernel_launch_count() - l0}
+    if cpu:
+        # painty's imprint loop restated (double, one core) on the first strokes
+        from oracle.oracle import Oracle
+        o = Oracle()
+        oc = o.canvas(rows, cols)
+        oc.set("R0", r0)
+        ob = o.brush(strokes[0].radius, fp)
+        ob.set_rates(0.05, 0.1)
+        t = time.perf_counter()
+        ns = 0
+        used = 0
+        for s in strokes:
+            ob.set_radius(s.radius)
+            ob.dip(s.K, s.S)
+            ns += ob.paint_stroke(oc, s.path, s.spacing)
+            used += 1
+            if time.perf_counter() - t > 10.0:
+                break
+        cdt = time.perf_counter() - t
+        out["cpu_baseline"] = {"value": round(ns / cdt, 1), "unit": "stamps/s", "cores": 1,
+                               "kind": "port",
+                               "sample": f"the first {used} strokes ({ns} stamps), painty's "
+                                         "FootprintBrush imprint loop restated (double)"}
+    return out
 
 
 def run_batch(pg, torch, storage: str, ncanvas: int, max_strokes, rank: int = 0,
