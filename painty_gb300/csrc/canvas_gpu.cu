@@ -59,9 +59,11 @@ namespace {
 
 constexpr float kGlEps = 10e-6f;  // the shaders' Eps
 
-__device__ __forceinline__ float glsl_coth(float x) {  // ComposeLayerOnSubstrate.compute.glsl:13-22
+// coth (ComposeLayerOnSubstrate.compute.glsl:13-22): 1 above 20, cosh(x) / sinh(x) for x != 0,
+// else infinity. cosh / sinh = 1 + 2 / (e^2x - 1), with expm1 accurate near 0.
+__device__ __forceinline__ float glsl_coth(float x) {
   if (x > 20.0f) return 1.0f;
-  if (fabsf(x) > 0.0f) return coshf(x) / sinhf(x);
+  if (fabsf(x) > 0.0f) return 1.0f + 2.0f / expm1f(2.0f * x);
   return __int_as_float(0x7f800000);
 }
 

@@ -107,71 +107,50 @@ double normalize_angle_h(double a) {  // Smudge.hxx:201-211
 }
 
 // ---------------------------------------------------------------------- device code
+// r, A, D of painty's generalized barycentric coordinates for outline vertex i at (px, py):
+// s_i = poly[i] - p, r = |s_i|, A = det(s_i, s_i+1) / 2, D = s_i . s_i+1 (Math.hxx:82-95).
+struct BaryTerms {
+  double r, A, D;
+};
+__device__ __forceinline__ BaryTerms bary_terms(const double2* poly, int n, int i, double px,
+                                                double py) {
+  const double2 pi = poly[i], pj = poly[i + 1 < n ? i + 1 : 0];
+  const double sx = pi.x - px, sy = pi.y - py;
+  const double tx = pj.x - px, ty = pj.y - py;
+  return {sqrt(sx * sx + sy * sy), (sx * ty - tx * sy) / 2.0, sx * tx + sy * ty};
+}
+
 // generalizedBarycentricCoordinatesInterpolate (Math.hxx:72-147) of the outline `poly` at
-// (px, py) with texture coordinates `uv` (n > 1 vertices, global memory).
+// (px, py) with texture coordinates `uv` (n > 1 vertices, global memory). painty makes two
+// passes (r, A, D and the early returns, then the weights); here one pass evaluates each
+// vertex's terms once: vertex i's early returns are taken at step i, in painty's order, before
+// its weight joins the sums, so the result is painty's to the bit.
 __device__ D2 barycentric_uv(const double2* poly, const double2* uv, int n, double px,
                              double py) {
   constexpr double Eps = 2.220446049250313080847e-16 * 100.0;
-  // pass 1: r, A, D and the early returns (on a vertex, or on an edge)
-  double rprev = 0.0, Aprev = 0.0, Dprev = 0.0;  // of vertex n-1 (filled at i = n-1)
-  double r0 = 0.0, A0 = 0.0, D0 = 0.0;
-  for (int i = 0; i < n; i++) {
-    const double2 pi = poly[i], pj = poly[i + 1 < n ? i + 1 : 0];
-    const double sx = pi.x - px, sy = pi.y - py;
-    const double tx = pj.x - px, ty = pj.y - py;
-    const double r = sqrt(sx * sx + sy * sy);
-    if (fabs(r - 0.0) < Eps) return {uv[i].x, uv[i].y};
-    const double det = sx * ty - tx * sy;
-    const double A = det / 2.0;
-    const double D = sx * tx + sy * ty;
-    if (fabs(A - 0.0) < Eps && D < 0.0) {
-      const double ri1 = sqrt(tx * tx + ty * ty);
-      const double2 fi1 = uv[i + 1 < n ? i + 1 : 0];
-      const double k = 1.0 / (r + ri1);
-      return {(ri1 * uv[i].x + r * fi1.x) * k, (ri1 * uv[i].y + r * fi1.y) * k};
-    }
-    if (i == 0) {
-      r0 = r;
-      A0 = A;
-      D0 = D;
-    }
-    if (i == n - 1) {
-      rprev = r;
-      Aprev = A;
-      Dprev = D;
-    }
-  }
-  // pass 2: weights, in painty's order
+  const BaryTerms last = bary_terms(poly, n, n - 1, px, py);
+  const BaryTerms first = bary_terms(poly, n, 0, px, py);
   double fx = 0.0, fy = 0.0, W = 0.0;
-  double r_1 = rprev, A_1 = Aprev, D_1 = Dprev;  // of vertex i-1
-  double ri = r0, Ai = A0, Di = D0;
+  BaryTerms prv = last, cur = first;  // vertices i-1 and i
   for (int i = 0; i < n; i++) {
-    // r, A, D of vertex i+1 (recomputed rather than stored)
-    double rn, An, Dn;
-    if (i + 1 < n) {
-      const double2 pi = poly[i + 1], pj = poly[i + 2 < n ? i + 2 : 0];
-      const double sx = pi.x - px, sy = pi.y - py;
-      const double tx = pj.x - px, ty = pj.y - py;
-      rn = sqrt(sx * sx + sy * sy);
-      An = (sx * ty - tx * sy) / 2.0;
-      Dn = sx * tx + sy * ty;
-    } else {
-      rn = r0;
-      An = A0;
-      Dn = D0;
+    const BaryTerms nxt = i + 1 == n ? first : (i + 1 == n - 1 ? last : bary_terms(poly, n, i + 1, px, py));
+    // early returns (painty's first pass): on vertex i, or on its edge to vertex i+1, whose
+    // |s_i+1| is nxt.r
+    if (fabs(cur.r - 0.0) < Eps) return {uv[i].x, uv[i].y};
+    if (fabs(cur.A - 0.0) < Eps && cur.D < 0.0) {
+      const double2 fi1 = uv[i + 1 < n ? i + 1 : 0];
+      const double k = 1.0 / (cur.r + nxt.r);
+      return {(nxt.r * uv[i].x + cur.r * fi1.x) * k, (nxt.r * uv[i].y + cur.r * fi1.y) * k};
     }
+    // the weight (painty's second pass)
     double w = 0.0;
-    if (A_1 != 0.0) w = w + (r_1 - D_1 / ri) / A_1;
-    if (Ai != 0.0) w = w + (rn - Di / ri) / Ai;
+    if (prv.A != 0.0) w = w + (prv.r - prv.D / cur.r) / prv.A;
+    if (cur.A != 0.0) w = w + (nxt.r - cur.D / cur.r) / cur.A;
     fx = fx + w * uv[i].x;
     fy = fy + w * uv[i].y;
     W = W + w;
-    r_1 = ri;
-    A_1 = Ai;
-    D_1 = Di;
-    ri = rn;
-    Ai = An;
-    Di = Dn;
+    prv = cur;
+    cur = nxt;
   }
   if (!(fabs(W - 0.0) < Eps)) {
     const double k = 1.0 / W;
