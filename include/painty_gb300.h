@@ -245,9 +245,10 @@ painty_status painty_texture_brush_set_smudge(painty_texture_brush* brush, int32
 painty_status painty_texture_brush_set_thickness_scale(painty_texture_brush* brush,
                                                        double scale);
 /* replaces paintStroke(verts, canvas) (:52-205): path_xy = n (x, y) pairs (host, n >= 2 to
- * paint). painted_out (may be null) receives the pixels the stroke deposited on. A stroke
- * whose bounds lie off the canvas paints nothing (painty fails on it). Synchronises the
- * stream. */
+ * paint; at most 4096 points). painted_out (may be null) receives the pixels the stroke
+ * deposited on. A stroke whose bounds lie off the canvas paints nothing (painty fails on it).
+ * With the smudge on, the smudge map is at most 4096 wide (radius below 2048). Synchronises
+ * the stream. */
 painty_status painty_texture_brush_paint_stroke(painty_canvas* canvas,
                                                 painty_texture_brush* brush,
                                                 const double* path_xy, int32_t n,

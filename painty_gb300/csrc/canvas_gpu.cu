@@ -716,7 +716,8 @@ painty_status painty_gpu_texture_brush_destroy(painty_gpu_texture_brush* b) {
 painty_status painty_gpu_texture_brush_set_radius(painty_gpu_texture_brush* b, double radius) {
   return guard([&] {
     PG_REQUIRE(b != nullptr, "brush is null");
-    PG_REQUIRE(std::isfinite(radius) && radius >= 0.0, "radius must be finite and >= 0");
+    PG_REQUIRE(std::isfinite(radius) && radius >= 0.0 && radius <= 1e6,
+               "radius must be in [0, 1e6]");
     if (!(std::fabs(b->radius - radius) < 0.5)) b->radius = radius;  // TextureBrushGpu.cxx:48-61
   });
 }

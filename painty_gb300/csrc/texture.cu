@@ -955,7 +955,8 @@ painty_status painty_texture_brush_destroy(painty_texture_brush* b) {
 painty_status painty_texture_brush_set_radius(painty_texture_brush* b, double radius) {
   return guard([&] {
     PG_REQUIRE(b != nullptr, "brush is null");
-    PG_REQUIRE(std::isfinite(radius) && radius >= 0.0, "radius must be finite and >= 0");
+    PG_REQUIRE(std::isfinite(radius) && radius >= 0.0 && radius <= 1e6,
+               "radius must be in [0, 1e6]");
     if (!(std::fabs(b->radius - radius) < 0.5)) {  // TextureBrush.hxx:33-41
       b->radius = radius;
       if (b->useSmudge) b->make_smudge(static_cast<int32_t>(2.0 * radius));
@@ -995,8 +996,11 @@ painty_status painty_texture_brush_paint_stroke(painty_canvas* c, painty_texture
   return guard([&] {
     PG_REQUIRE(c && b, "null handle");
     PG_REQUIRE(n >= 0 && (n == 0 || path_xy), "path is null");
+    // every pixel of the stroke's bounds walks the 2 (n + 2)-vertex outline
+    PG_REQUIRE(n <= 4096, "path longer than 4096 points");
     for (int64_t i = 0; i < 2 * static_cast<int64_t>(n); i++)
-      PG_REQUIRE(std::isfinite(path_xy[i]), "path coordinates must be finite");
+      PG_REQUIRE(std::isfinite(path_xy[i]) && std::fabs(path_xy[i]) < 1e9,
+                 "path coordinates must be finite and within 1e9");
     PG_REQUIRE(static_cast<int64_t>(c->wet.rows) * c->wet.pitch < (int64_t(1) << 31),
                "canvas too large for the texture brush");
     const bool f64 = c->wet.storage == PAINTY_STORAGE_F64;

@@ -50,3 +50,51 @@ def test_mix_paint_matches_reference_formula(pg, oracle):
     k1, s1 = pg.mix_single_paint(w, K, S)
     k2, s2 = oracle.mix_single_paint(w, K, S)
     assert np.array_equal(k1, k2) and np.array_equal(s1, s2)
+
+
+def test_texture_and_gl_brush_arguments_rejected_without_gpu(pg):
+    import numpy as np
+    import pytest
+    tex = np.random.default_rng(0).random((8, 16))
+    with pytest.raises(ValueError):
+        pg.TextureBrush(np.zeros((0, 4)))
+    b = pg.TextureBrush(tex)
+    for bad in (float("nan"), -1.0, 2e6):
+        with pytest.raises(ValueError):
+            b.setRadius(bad)
+    with pytest.raises(ValueError):
+        b.setThicknessScale(float("inf"))
+    d = pg.TextureBrushDictionary(1)
+    with pytest.raises(ValueError):
+        d.add(1, 1, np.zeros((0, 3)))
+    with pytest.raises(ValueError):
+        d.add(1, 1, np.array([[1.0, float("nan")]]))
+    with pytest.raises(ValueError):  # empty dictionary
+        d.lookup(np.array([[0.0, 0.0], [5.0, 0.0]]), 4.0)
+    d.add(4, 10, tex)
+    assert d.lookup(np.array([[0.0, 0.0], [5.0, 0.0]]), 8.0) == 0
+    g = pg.TextureBrushGpu(d)
+    with pytest.raises(ValueError):
+        g.setRadius(-3.0)
+    with pytest.raises(pg.PaintyError):
+        g.enableSmudge(True)
+    assert g.lastTexture() == -1
+
+
+def test_texture_dictionary_lookup_matches_oracle(pg, oracle):
+    """The class choice of TextureBrushDictionary::lookup, including painty's initial length
+    class 1 and its first-size-class distance, agrees with the oracle's restatement."""
+    import numpy as np
+    rng = np.random.default_rng(5)
+    d, o = pg.TextureBrushDictionary(9), oracle.texture_dictionary(9)
+    for rc, rows in ((3, 6), (9, 18), (27, 54)):
+        for lc, cols in ((20, 30), (90, 100), (300, 320)):
+            for k in range(2):
+                t = rng.random((rows, cols))
+                d.add(rc, lc, t)
+                o.add(rc, lc, t)
+    for trial in range(60):
+        n = int(rng.integers(2, 6))
+        path = rng.uniform(0, 400, (n, 2))
+        size = float(rng.uniform(1, 80))
+        assert d.lookup(path, size) == o.lookup(path, size)
