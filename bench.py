@@ -550,7 +550,9 @@ def run_stamps_config0(pg, torch, nstrokes: int = 200, cpu: bool = False):
            "stamps_per_step": n, "ms_per_step": round(dt * 1e3, 2),
            "config": "1024x768 FP32, 200 strokes, r U[8,32], spacing 0.25 r, snapshot on, "
                      "deposit 0.1, pickup 0.05, final composite; through the C ABI",
-           "gpu_launches": pg.kernel_launch_count() - l0}
+           "gpu_launches": pg.kernel_launch_count() - l0,
+           "roofline": stamp_roofline([(s.radius, pg_stroke_stamps(s.path, s.spacing))
+                                       for s in strokes], n, dt, "f32")}
     if cpu:
         # painty's imprint loop restated (double, one core) on the first strokes
         from oracle.oracle import Oracle
@@ -622,8 +624,14 @@ def run_batch(pg, torch, storage: str, ncanvas: int, max_strokes, rank: int = 0,
         dt, n = float(t_.item()), int(n_.item())
     px = sum(r * c for r, c, _ in specs)
     cl, nclusters = pg.batch_last_shape()
+    roof = stamp_roofline([(s[2], pg_stroke_stamps(np.asarray(s[1]), s[3])) for s in strokes],
+                          n, dt, storage)
+    if roof:
+        roof["note"] = ("canvases run concurrently, each canvas's stamps in order; the "
+                        "heaviest canvas's chain of stamps bounds the launch")
     return {"metric": "stamps/s", "value": round(n / dt, 1), "unit": "stamps/s", "stamps": n,
             "s": round(dt, 3), "storage": storage, "gpu_launches": pg.kernel_launch_count() - l0,
+            "roofline": roof,
             "ctas_per_canvas": cl, "clusters": nclusters,
             "config": f"{ncanvas} canvases (side logU[256,2048], aspect U[0.5,2], "
                       f"{pg_canvas_px(px)}), {len(strokes)} strokes (logU[50,2000] per canvas"
@@ -714,6 +722,27 @@ def run_serve(pg, torch, rate: float, seconds: float, seed: int = 4, budget_gb: 
 def pg_stroke_stamps(path, spacing):
     d = np.linalg.norm(np.diff(path, axis=0), axis=1)
     return int(np.sum(np.floor(d / spacing)))
+
+
+def stamp_roofline(pairs, n_stamps: int, seconds: float, storage: str):
+    """Algorithmic bytes of stamping against HBM: a stamp of footprint side s touches s^2
+    canvas pixels, reading and writing their K, S, V and the snapshot's and pickup map's
+    (56 B per pixel in FP32, 28 B in 16-bit storage). `pairs` = (radius, approximate stamp
+    count) per stroke, to weight the mean footprint; n_stamps is the exact total."""
+    import math
+    w = sum(c for _, c in pairs)
+    if w <= 0 or seconds <= 0:
+        return None
+    mean_px = sum(c * math.ceil(math.sqrt(2.0) * (2 * math.ceil(r) + 1)) ** 2
+                  for r, c in pairs) / w
+    per_px = 28 if storage in ("f16", "bf16") else 56
+    gbs = n_stamps * mean_px * per_px / seconds / 1e9
+    peak, kind = _peaks()
+    return {"bound": "latency", "achieved": round(gbs, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(gbs / peak, 4), "bytes_per_stamp": round(mean_px * per_px),
+            "peak_kind": kind,
+            "note": "stamps of a canvas run strictly in order on one CTA cluster; the canvas "
+                    "and snapshot stay in L2, so the per-stamp chain, not HBM, bounds it"}
 
 
 def pg_canvas_px(px):
