@@ -725,10 +725,11 @@ def pg_stroke_stamps(path, spacing):
 
 
 def stamp_roofline(pairs, n_stamps: int, seconds: float, storage: str):
-    """Algorithmic bytes of stamping against HBM: a stamp of footprint side s touches s^2
-    canvas pixels, reading and writing their K, S, V and the snapshot's and pickup map's
-    (56 B per pixel in FP32, 28 B in 16-bit storage). `pairs` = (radius, approximate stamp
-    count) per stroke, to weight the mean footprint; n_stamps is the exact total."""
+    """Algorithmic bytes of stamping against HBM: a stamp of footprint side s reads and
+    writes the K, S, V of s^2 canvas pixels (7 values each way: 56 B per pixel in FP32, 28 B
+    in 16-bit storage; the snapshot and pickup map add traffic that stays on chip).
+    `pairs` = (radius, approximate stamp count) per stroke, to weight the mean footprint;
+    n_stamps is the exact total."""
     import math
     w = sum(c for _, c in pairs)
     if w <= 0 or seconds <= 0:
