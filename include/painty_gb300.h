@@ -95,6 +95,12 @@ painty_status painty_layer_upload(painty_layer* layer, painty_plane plane, const
                                   painty_host_format fmt, void* stream);
 painty_status painty_layer_download(const painty_layer* layer, painty_plane plane, void* host,
                                     painty_host_format fmt, void* stream);
+/* replaces PaintLayer::set(i, j, k, s, v) (PaintLayer.hxx:122-127) for n cells in order:
+ * rows_cols = n (row, col) pairs, K and S = n triples, V = n values (host). Later cells win
+ * where cells repeat. At most 2^24 cells per call. */
+painty_status painty_layer_set_cells(painty_layer* layer, int64_t n, const int32_t* rows_cols,
+                                     const double* K, const double* S, const double* V,
+                                     void* stream);
 /* replaces PaintLayer::copyTo (PaintLayer.hxx:103-111); same size and storage */
 painty_status painty_layer_copy(const painty_layer* src, painty_layer* dst, void* stream);
 painty_status painty_layer_info(const painty_layer* layer, int32_t* rows, int32_t* cols,

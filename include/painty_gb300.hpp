@@ -165,6 +165,11 @@ class PaintLayer {
     check(painty_layer_upload(h_, PAINTY_PLANE_S, S.data(), PAINTY_HOST_F64_INTERLEAVED, nullptr));
     check(painty_layer_upload(h_, PAINTY_PLANE_V, V.data(), PAINTY_HOST_F64_INTERLEAVED, nullptr));
   }
+  // PaintLayer::set(i, j, k, s, v) (PaintLayer.hxx:122-127)
+  void set(int32_t i, int32_t j, const vec3& k, const vec3& s, double v) {
+    const int32_t rc[2] = {i, j};
+    check(painty_layer_set_cells(h_, 1, rc, k.data(), s.data(), &v, nullptr));
+  }
   std::vector<double> getK_buffer() const { return plane(PAINTY_PLANE_K, 3); }
   std::vector<double> getS_buffer() const { return plane(PAINTY_PLANE_S, 3); }
   std::vector<double> getV_buffer() const { return plane(PAINTY_PLANE_V, 1); }

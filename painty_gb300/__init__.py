@@ -57,6 +57,7 @@ _sig("painty_layer_clear", _P, _P)
 _sig("painty_layer_upload", _P, C.c_int, _P, C.c_int, _P)
 _sig("painty_layer_download", _P, C.c_int, _P, C.c_int, _P)
 _sig("painty_layer_copy", _P, _P, _P)
+_sig("painty_layer_set_cells", _P, _I64, _P, _P, _P, _P, _P)
 _sig("painty_layer_info", _P, C.POINTER(_I32), C.POINTER(_I32), C.POINTER(C.c_int))
 _sig("painty_image_create", _I32, _I32, C.c_int, C.POINTER(_P))
 _sig("painty_image_destroy", _P)
@@ -222,6 +223,22 @@ class PaintLayer:
         self.upload("K", K, stream=stream)
         self.upload("S", S, stream=stream)
         self.upload("V", V, stream=stream)
+
+    def setCells(self, rows_cols, K, S, V, stream=None) -> None:
+        """PaintLayer::set(i, j, k, s, v) (PaintLayer.hxx:122-127) for many cells, in order."""
+        rc = np.ascontiguousarray(rows_cols, dtype=np.int32).reshape(-1, 2)
+        K = np.ascontiguousarray(K, dtype=np.float64).reshape(-1, 3)
+        S = np.ascontiguousarray(S, dtype=np.float64).reshape(-1, 3)
+        V = np.ascontiguousarray(V, dtype=np.float64).reshape(-1)
+        n = rc.shape[0]
+        if not (K.shape[0] == S.shape[0] == V.shape[0] == n):
+            raise ValueError("rows_cols, K, S and V describe different numbers of cells")
+        _check(_lib.painty_layer_set_cells(self._h, n, _ptr(rc), _ptr(K), _ptr(S), _ptr(V),
+                                           _stream(stream)))
+
+    def setCell(self, i: int, j: int, k, s, v: float) -> None:
+        """PaintLayer::set(i, j, k, s, v)."""
+        self.setCells([[i, j]], [k], [s], [v])
 
     def getK_buffer(self):
         return self.download("K")

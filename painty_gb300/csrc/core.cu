@@ -221,6 +221,26 @@ __global__ void fill_kernel(PlanePtrs dst, int nch, int64_t elems, double v0, do
   }
 }
 
+// PaintLayer::set(i, j, k, s, v) for n cells in order: cell m writes its 7 values (K, S as
+// triples, V) at (rows[m], cols[m]). Later cells win where cells repeat, as successive set()
+// calls do.
+template <class TK, class TV>
+__global__ void set_cells_kernel(LayerPtrs dst, int64_t pitch, int64_t es, const int32_t* rc,
+                                 const double* vals, int64_t n) {
+  for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < n;
+       m += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t at = (static_cast<int64_t>(rc[2 * m]) * pitch + rc[2 * m + 1]) * es;
+    // a later cell at the same position takes precedence
+    bool later = false;
+    for (int64_t q = m + 1; q < n && !later; q++)
+      later = rc[2 * q] == rc[2 * m] && rc[2 * q + 1] == rc[2 * m + 1];
+    if (later) continue;
+#pragma unroll
+    for (int c = 0; c < 6; c++) static_cast<TK*>(dst.p[c])[at] = convert<TK, double>(vals[7 * m + c]);
+    static_cast<TV*>(dst.p[6])[at] = convert<TV, double>(vals[7 * m + 6]);
+  }
+}
+
 // Layer copy between any layouts: the 7 values of each pixel, src element stride -> dst.
 template <class TK, class TV>
 __global__ void copy_layer_kernel(LayerPtrs src, LayerPtrs dst, int64_t elems, int64_t ses,
@@ -789,6 +809,67 @@ painty_status painty_layer_copy(const painty_layer* src, painty_layer* dst, void
     PG_REQUIRE(src && dst, "layer is null");
     pg::copy_layer(*src, *dst, pg::as_stream(stream));
     dst->touch();
+  });
+}
+
+painty_status painty_layer_set_cells(painty_layer* layer, int64_t n, const int32_t* rows_cols,
+                                     const double* K, const double* S, const double* V,
+                                     void* stream) {
+  return guard([&] {
+    PG_REQUIRE(layer != nullptr, "layer is null");
+    PG_REQUIRE(n >= 0 && n <= (int64_t(1) << 24), "n must be in [0, 2^24]");
+    if (n == 0) return;
+    PG_REQUIRE(rows_cols && K && S && V, "null argument");
+    std::vector<double> vals(static_cast<size_t>(n) * 7);
+    for (int64_t m = 0; m < n; m++) {
+      const int32_t r = rows_cols[2 * m], c = rows_cols[2 * m + 1];
+      PG_REQUIRE(r >= 0 && r < layer->rows && c >= 0 && c < layer->cols,
+                 "cell outside the layer");
+      for (int q = 0; q < 3; q++) {
+        vals[7 * m + q] = K[3 * m + q];
+        vals[7 * m + 3 + q] = S[3 * m + q];
+      }
+      vals[7 * m + 6] = V[m];
+    }
+    const cudaStream_t st = pg::as_stream(stream);
+    char* d = nullptr;
+    const size_t brc = static_cast<size_t>(n) * 2 * sizeof(int32_t);
+    const size_t bv = vals.size() * sizeof(double);
+    PG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&d), brc + bv + 16, st));
+    char* dv = d + (brc + 15) / 16 * 16;
+    PG_CUDA(cudaMemcpyAsync(d, rows_cols, brc, cudaMemcpyHostToDevice, st));
+    PG_CUDA(cudaMemcpyAsync(dv, vals.data(), bv, cudaMemcpyHostToDevice, st));
+    pg::LayerPtrs lp{};
+    for (int c = 0; c < 3; c++) {
+      lp.p[c] = layer->K[c];
+      lp.p[3 + c] = layer->S[c];
+    }
+    lp.p[6] = layer->V;
+    for (int64_t b0 = 0; b0 < n; b0 += 4096) {
+      const int64_t nb = std::min<int64_t>(4096, n - b0);
+      const auto* rc = reinterpret_cast<const int32_t*>(d) + 2 * b0;
+      const auto* v = reinterpret_cast<const double*>(dv) + 7 * b0;
+      const int g = static_cast<int>((nb + 255) / 256);
+      switch (layer->storage) {
+        case PAINTY_STORAGE_F32:
+          pg::set_cells_kernel<float, float><<<g, 256, 0, st>>>(lp, layer->pitch, layer->estride, rc, v, nb);
+          break;
+        case PAINTY_STORAGE_F16:
+          pg::set_cells_kernel<__half, __half><<<g, 256, 0, st>>>(lp, layer->pitch, layer->estride, rc, v, nb);
+          break;
+        case PAINTY_STORAGE_BF16:
+          pg::set_cells_kernel<__nv_bfloat16, __half><<<g, 256, 0, st>>>(lp, layer->pitch, layer->estride, rc, v, nb);
+          break;
+        case PAINTY_STORAGE_F64:
+          pg::set_cells_kernel<double, double><<<g, 256, 0, st>>>(lp, layer->pitch, layer->estride, rc, v, nb);
+          break;
+      }
+      pg::count_launch();
+      PG_CUDA(cudaGetLastError());
+    }
+    PG_CUDA(cudaFreeAsync(d, st));
+    PG_CUDA(cudaStreamSynchronize(st));
+    layer->touch();
   });
 }
 

@@ -120,3 +120,28 @@ def test_upload_download_roundtrip(pg):
         planar = np.ascontiguousarray(np.moveaxis(a, -1, 0))
         ly.upload("K", planar, planar=True)
         assert np.abs(ly.download("K") - a).max() <= tol
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("storage", ["f32", "f64", "f16"])
+def test_layer_set_cells(pg, storage):
+    """PaintLayer::set(i, j, k, s, v) on planar layers and a canvas's packed wet layer; the
+    last of repeated cells wins."""
+    rng = np.random.default_rng(8)
+    for layer in (pg.PaintLayer(20, 30, storage), pg.Canvas(20, 30, storage).getPaintLayer()):
+        rc = np.array([[0, 0], [5, 7], [19, 29], [5, 7], [10, 3]])
+        K, S, V = rng.uniform(0, 5, (5, 3)), rng.uniform(0, 3, (5, 3)), rng.uniform(0, 1, 5)
+        layer.setCells(rc, K, S, V)
+        layer.setCell(10, 3, K[0], S[0], 0.25)
+        gk, gs, gv = layer.download("K"), layer.download("S"), layer.download("V")
+        want = {(0, 0): 0, (5, 7): 3, (19, 29): 2}
+        tol = 0 if storage != "f16" else 2e-3
+        for (r, c), m in want.items():
+            np.testing.assert_allclose(gk[r, c], K[m], rtol=tol)
+            np.testing.assert_allclose(gs[r, c], S[m], rtol=tol)
+            np.testing.assert_allclose(gv[r, c], V[m], rtol=tol)
+        np.testing.assert_allclose(gk[10, 3], K[0], rtol=tol)
+        assert gv[10, 3] == 0.25
+        assert gv.sum() == pytest.approx(sum(V[m] for m in want.values()) + 0.25, rel=1e-3)
+    with pytest.raises(pg.PaintyValueError):
+        pg.PaintLayer(4, 4, storage).setCell(4, 0, [1, 1, 1], [1, 1, 1], 1.0)
