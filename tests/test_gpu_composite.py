@@ -135,13 +135,13 @@ def test_layer_set_cells(pg, storage):
         layer.setCell(10, 3, K[0], S[0], 0.25)
         gk, gs, gv = layer.download("K"), layer.download("S"), layer.download("V")
         want = {(0, 0): 0, (5, 7): 3, (19, 29): 2}
-        tol = 0 if storage != "f16" else 2e-3
+        tol = {"f64": 0.0, "f32": 1e-7, "f16": 2e-3}[storage]  # the storage's rounding
         for (r, c), m in want.items():
             np.testing.assert_allclose(gk[r, c], K[m], rtol=tol)
             np.testing.assert_allclose(gs[r, c], S[m], rtol=tol)
             np.testing.assert_allclose(gv[r, c], V[m], rtol=tol)
         np.testing.assert_allclose(gk[10, 3], K[0], rtol=tol)
-        assert gv[10, 3] == 0.25
+        assert gv[10, 3] == 0.25  # exact in every storage
         assert gv.sum() == pytest.approx(sum(V[m] for m in want.values()) + 0.25, rel=1e-3)
     with pytest.raises(pg.PaintyValueError):
         pg.PaintLayer(4, 4, storage).setCell(4, 0, [1, 1, 1], [1, 1, 1], 1.0)
