@@ -451,7 +451,7 @@ def run_ours(args):
 
     e2e_step()
     barrier()
-    e_steps = max(1, min(args.steps, 5))
+    e_steps = max(1, min(args.steps, 10))
     tw = time.perf_counter()
     for _ in range(e_steps):
         e2e_step()
