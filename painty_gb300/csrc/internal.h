@@ -139,6 +139,8 @@ struct painty_brush {
   bool pickup_clear = true;
   void* d_owner = nullptr;
   size_t d_owner_bytes = 0;
+  void* d_cellmap = nullptr;  // cell maps of large stamps (2 F*F ints per CTA)
+  size_t d_cellmap_bytes = 0;
   // snapshot (FootprintBrush.hxx:471): canvas-sized layer, allocated at first use
   painty_layer snapshot;
   bool has_snapshot = false;

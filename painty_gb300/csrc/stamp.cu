@@ -126,6 +126,9 @@ struct StampArgs {
   int32_t pickup_smem;    // stage the pickup map in shared memory for the launch
   int32_t footprint_smem; // stage the footprint in shared memory
   int* owner_global;      // S*S ints when the owner table does not fit in shared memory
+  // 2 F*F ints per CTA of the cluster when the cell maps do not fit in shared memory beside
+  // the support-disc list (large stamps); NULL: in shared memory
+  int* cellmap_global;
   unsigned* status;
 };
 
@@ -440,7 +443,7 @@ struct StampSmem {
 template <class M>
 __host__ __device__ inline StampSmem stamp_smem_layout(int F, int S, int ndisc, bool fp_smem,
                                                        bool pick_smem, bool own_smem,
-                                                       int pick_vals = 8) {
+                                                       int pick_vals = 8, bool cm_smem = true) {
   StampSmem L{};
   size_t o = 0;
   L.fp = o;
@@ -460,7 +463,7 @@ __host__ __device__ inline StampSmem stamp_smem_layout(int F, int S, int ndisc, 
   L.disc = o;
   if (ndisc > 0) o = align_up(o + size_t(ndisc) * sizeof(uint32_t), 16);
   L.cellmap = o;
-  if (ndisc > 0) o = align_up(o + size_t(2) * F * F * sizeof(int), 16);
+  if (ndisc > 0 && cm_smem) o = align_up(o + size_t(2) * F * F * sizeof(int), 16);
   L.total = o;
   return L;
 }
@@ -855,7 +858,8 @@ __device__ __forceinline__ void run_stroke(const StampArgs<TK, TV>& a, const Src
   const int F = a.F, S = a.S;
   const int npix = F * F;
   const int cells = S * S;
-  const StampSmem L = stamp_smem_layout<M>(F, S, a.ndisc, !BIG, PS, !BIG, PK ? 8 : 7);
+  const StampSmem L = stamp_smem_layout<M>(F, S, a.ndisc, !BIG, PS, !BIG, PK ? 8 : 7,
+                                           a.cellmap_global == nullptr);
   const M* fps = !BIG ? reinterpret_cast<M*>(smem_raw + L.fp) : a.footprint;
   M* pbase = PS ? reinterpret_cast<M*>(smem_raw + L.pick) : nullptr;
   int* own = BIG ? a.owner_global : reinterpret_cast<int*>(smem_raw + L.own);
@@ -864,9 +868,11 @@ __device__ __forceinline__ void run_stroke(const StampArgs<TK, TV>& a, const Src
   uint16_t* dc_b = reinterpret_cast<uint16_t*>(smem_raw + L.done_c);
   uint16_t* dr_b = reinterpret_cast<uint16_t*>(smem_raw + L.done_r);
   uint32_t* disc = reinterpret_cast<uint32_t*>(smem_raw + L.disc);
-  int* cm_b = reinterpret_cast<int*>(smem_raw + L.cellmap);
   const int ndisc = a.ndisc;
   const int crank = static_cast<int>(cluster_rank()), csize = static_cast<int>(cluster_size());
+  // each CTA keeps its own pair of cell maps, as in shared memory
+  int* cm_b = a.cellmap_global ? a.cellmap_global + static_cast<int64_t>(crank) * 2 * npix
+                               : reinterpret_cast<int*>(smem_raw + L.cellmap);
   auto csync = [csize]() {
     if (csize > 1)
       cluster_barrier();
@@ -1236,6 +1242,7 @@ __global__ void __launch_bounds__(kStampThreads, 1) batch_kernel(const __grid_co
         sa.owner_global = (st.plan & 2)
                             ? b.scratch_owner + static_cast<int64_t>(cid) * b.owner_stride
                             : nullptr;
+        sa.cellmap_global = nullptr;  // the batch plans keep cell maps in shared memory
         sa.status = b.status;
       }
       const double* pts = b.points + 2 * st.first_point;
@@ -1378,22 +1385,30 @@ int max_dyn_smem() {
 // in shared memory (BIG = false); maps too large for that keep both in global memory. The
 // pickup map (7 planes) is staged in shared memory when it fits beside them.
 // The support-disc list and cell map (ndisc > 0) are kept when some variant fits with them.
+// cm_global: the cell maps live in global memory (allow_cm_global; the support-disc list stays
+// in shared memory), which keeps the disc painting for stamps too large for both.
 struct SmemPlan {
   bool big, pick;
   int ndisc;
   StampSmem layout;
+  bool cm_global = false;
 };
 template <class M>
 SmemPlan plan_smem_limit(int F, int S, int ndisc, size_t limit, bool allow_small = true,
-                         bool allow_pick = true) {
+                         bool allow_pick = true, bool allow_cm_global = false) {
   const bool cand[4][2] = {{false, true}, {false, false}, {true, true}, {true, false}};
-  for (int nd : {ndisc, 0}) {
+  for (int pass = 0; pass < 3; pass++) {
+    // pass 0: the disc list and cell maps in shared memory; 1: the cell maps in global
+    // memory; 2: no disc list (every stamp paints in waves)
+    const int nd = pass == 2 ? 0 : ndisc;
+    const bool cm_smem = pass != 1;
+    if (pass == 1 && (!allow_cm_global || ndisc == 0)) continue;
     for (const auto& c : cand) {
       const bool big = c[0], pick = c[1];
       if (!big && !allow_small) continue;
       if (pick && !allow_pick) continue;
-      const StampSmem L = stamp_smem_layout<M>(F, S, nd, !big, pick, !big);
-      if (L.total <= limit) return SmemPlan{big, pick, nd, L};
+      const StampSmem L = stamp_smem_layout<M>(F, S, nd, !big, pick, !big, 8, cm_smem);
+      if (L.total <= limit) return SmemPlan{big, pick, nd, L, !cm_smem};
     }
     if (ndisc == 0) break;
   }
@@ -1401,10 +1416,11 @@ SmemPlan plan_smem_limit(int F, int S, int ndisc, size_t limit, bool allow_small
 }
 
 template <class M>
-SmemPlan plan_smem(int F, int S, int ndisc, bool allow_small, bool allow_pick = true) {
+SmemPlan plan_smem(int F, int S, int ndisc, bool allow_small, bool allow_pick = true,
+                   bool allow_cm_global = false) {
   const size_t limit = static_cast<size_t>(max_dyn_smem()) - sizeof(StampParams) * kParamRing -
                        sizeof(StampShared) - 512;
-  return plan_smem_limit<M>(F, S, ndisc, limit, allow_small, allow_pick);
+  return plan_smem_limit<M>(F, S, ndisc, limit, allow_small, allow_pick, allow_cm_global);
 }
 
 // Launch of a stamp-path kernel with `cluster` CTAs per thread-block cluster (1: a plain
@@ -1513,15 +1529,18 @@ void launch_stamps(painty_canvas* c, painty_brush* b, const StampRec* d_stamps, 
   a.pickup_zero = pickup_zero ? 1 : 0;
   a.status = b->d_status;
   a.support2 = b->support2;
-  // one canvas: a cluster of CTAs shares each stamp when the stamp is large enough to split
-  // (the pickup map is then in global memory); a lone CTA stages it in shared memory
+  // one canvas: a cluster of 8 CTAs shares each stamp when the stamp is large enough to split
+  // (the pickup map is then in global memory); a lone CTA stages it in shared memory. Measured
+  // on GB300 (3,000 stamps per radius, FP32): one CTA is fastest up to F = 35 (194k vs 176k
+  // stamps/s at cluster 8), cluster 8 from F = 47 (172k vs 161k) up (134k vs 54k at F = 91);
+  // clusters of 2 or 4 are never the fastest.
   const int nd = disc_count(b->F, b->support2);
   int cl = env_cluster("PAINTY_STAMP_CLUSTER");
-  if (cl == 0) cl = nd >= 4096 ? 4 : nd >= 1536 ? 2 : 1;
+  if (cl == 0) cl = nd >= 1400 ? 8 : 1;
   SmemPlan plan{};
   void (*kern)(StampArgs<TK, TV>) = nullptr;
   for (;;) {
-    plan = plan_smem<M>(b->F, b->sizeMap, nd, true, cl == 1);
+    plan = plan_smem<M>(b->F, b->sizeMap, nd, true, cl == 1, true);
     if (cl > 1)
       kern = plan.big ? stamp_kernel<false, true, true, true, TK, TV>
                       : stamp_kernel<false, false, true, true, TK, TV>;
@@ -1539,6 +1558,12 @@ void launch_stamps(painty_canvas* c, painty_brush* b, const StampRec* d_stamps, 
   if (plan.big) {
     ensure(&b->d_owner, &b->d_owner_bytes, cells * sizeof(int));
     a.owner_global = static_cast<int*>(b->d_owner);
+  }
+  a.cellmap_global = nullptr;
+  if (plan.cm_global) {
+    ensure(&b->d_cellmap, &b->d_cellmap_bytes,
+           static_cast<size_t>(cl) * 2 * static_cast<size_t>(b->F) * b->F * sizeof(int));
+    a.cellmap_global = static_cast<int*>(b->d_cellmap);
   }
   a.footprint_smem = plan.big ? 0 : 1;
   a.pickup_smem = plan.pick ? 1 : 0;
@@ -2074,6 +2099,7 @@ painty_status painty_brush_destroy(painty_brush* b) {
     pg::device_free(b->d_footprint);
     pg::device_free(b->d_pickup);
     pg::device_free(b->d_owner);
+    pg::device_free(b->d_cellmap);
     pg::device_free(b->d_stamps);
     pg::device_free(b->d_status);
     if (b->has_snapshot) pg::device_free(b->snapshot.base);
