@@ -1470,11 +1470,11 @@ int max_clusters(void (*kern)(Arg), int cluster, size_t smem) {
 }
 
 // Cluster size from the environment (PAINTY_STAMP_CLUSTER / PAINTY_BATCH_CLUSTER), 0 if unset.
-int env_cluster(const char* name) {
+int env_cluster(const char* name, int max_cluster = 8) {
   const char* v = std::getenv(name);
   if (!v || !*v) return 0;
   const int n = std::atoi(v);
-  return (n == 1 || n == 2 || n == 4 || n == 8) ? n : 0;
+  return (n == 1 || n == 2 || n == 4 || n == 8 || n == 16) && n <= max_cluster ? n : 0;
 }
 
 // Box pixels (F x F, centre wr) with dc^2 + dr^2 <= support2: the kernel's support-disc list.
@@ -1529,14 +1529,15 @@ void launch_stamps(painty_canvas* c, painty_brush* b, const StampRec* d_stamps, 
   a.pickup_zero = pickup_zero ? 1 : 0;
   a.status = b->d_status;
   a.support2 = b->support2;
-  // one canvas: a cluster of 8 CTAs shares each stamp when the stamp is large enough to split
+  // one canvas: a cluster of CTAs shares each stamp when the stamp is large enough to split
   // (the pickup map is then in global memory); a lone CTA stages it in shared memory. Measured
-  // on GB300 (3,000 stamps per radius, FP32): one CTA is fastest up to F = 35 (194k vs 176k
-  // stamps/s at cluster 8), cluster 8 from F = 47 (172k vs 161k) up (134k vs 54k at F = 91);
-  // clusters of 2 or 4 are never the fastest.
+  // on GB300 (3,000 stamps per radius, FP32, stamps/s): one CTA is fastest up to F = 35 (196k;
+  // 174k at cluster 8), cluster 8 and 16 tie at F = 47 (170k; one CTA 162k), cluster 16 leads
+  // from F = 57 (165k vs 160k) and more so for larger stamps (98k vs 82k at F = 137); clusters
+  // of 2 or 4 are never the fastest. 16 needs a non-portable cluster, else 8 is used.
   const int nd = disc_count(b->F, b->support2);
-  int cl = env_cluster("PAINTY_STAMP_CLUSTER");
-  if (cl == 0) cl = nd >= 1400 ? 8 : 1;
+  int cl = env_cluster("PAINTY_STAMP_CLUSTER", 16);
+  if (cl == 0) cl = nd >= 2400 ? 16 : nd >= 1400 ? 8 : 1;
   SmemPlan plan{};
   void (*kern)(StampArgs<TK, TV>) = nullptr;
   for (;;) {
@@ -1551,6 +1552,13 @@ void launch_stamps(painty_canvas* c, painty_brush* b, const StampRec* d_stamps, 
                                    : stamp_kernel<false, false, false, true, TK, TV>);
     PG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(plan.layout.total)));
+    if (cl > 8 &&
+        cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+          cudaSuccess) {
+      cudaGetLastError();
+      cl = 8;
+      continue;
+    }
     if (cl == 1 || max_clusters(kern, cl, plan.layout.total) >= 1) break;
     cl /= 2;
   }
