@@ -1137,7 +1137,8 @@ struct BatchStroke {
   int32_t npoints;
   int32_t F, S, wr, support2;
   int32_t ndisc;  // support-disc list length (0: waves only)
-  int32_t plan;  // bit 0: pickup map in shared memory; bit 1: footprint and owners global
+  int32_t plan;  // bit 0: pickup map in shared memory; bit 1: footprint and owners global;
+                 // bit 2: cell maps global
   int64_t fp_offset;
   double radius, spacing;
   double K[3], Sc[3];
@@ -1156,7 +1157,8 @@ struct BatchArgs {
   int* claims;        // per cluster: the canvas it claimed last
   M* scratch_pickup;  // per cluster: Smax^2 cell records
   int* scratch_owner; // per cluster: Smax^2
-  int64_t pickup_stride, owner_stride;
+  int* scratch_cellmap;  // per cluster: CTAs x 2 Fmax^2 (strokes whose cell maps are global)
+  int64_t pickup_stride, owner_stride, cellmap_stride;
   unsigned* status;
 };
 
@@ -1242,7 +1244,8 @@ __global__ void __launch_bounds__(kStampThreads, 1) batch_kernel(const __grid_co
         sa.owner_global = (st.plan & 2)
                             ? b.scratch_owner + static_cast<int64_t>(cid) * b.owner_stride
                             : nullptr;
-        sa.cellmap_global = nullptr;  // the batch plans keep cell maps in shared memory
+        sa.cellmap_global = (st.plan & 4) ? b.scratch_cellmap + static_cast<int64_t>(cid) * b.cellmap_stride
+                                          : nullptr;
         sa.status = b.status;
       }
       const double* pts = b.points + 2 * st.first_point;
@@ -1840,12 +1843,16 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   // cluster size (autotuned by the cost model unless PAINTY_BATCH_CLUSTER sets it) and the
   // strokes' shared-memory plans (clusters keep the pickup map in global memory)
   auto kern = batch_kernel<TK, TV>;
+  int fmax_cm = 0;  // largest footprint whose cell maps live in global memory
   auto plan_all = [&](int cl) {
     dyn = 0;
+    fmax_cm = 0;
     for (size_t i = 0; i < bs.size(); i++) {
-      const SmemPlan plan = plan_smem_limit<M>(bs[i].F, bs[i].S, disc_of[i], limit, true, cl == 1);
+      const SmemPlan plan =
+        plan_smem_limit<M>(bs[i].F, bs[i].S, disc_of[i], limit, true, cl == 1, true);
       bs[i].ndisc = plan.ndisc;
-      bs[i].plan = (plan.pick ? 1 : 0) | (plan.big ? 2 : 0);
+      bs[i].plan = (plan.pick ? 1 : 0) | (plan.big ? 2 : 0) | (plan.cm_global ? 4 : 0);
+      if (plan.cm_global) fmax_cm = std::max(fmax_cm, bs[i].F);
       dyn = std::max(dyn, plan.layout.total);
     }
     PG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1890,6 +1897,9 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   void* d_counter = nullptr;
   PG_CUDA(cudaMallocAsync(&d_scratch_p, slots * pstride * msz, st));
   PG_CUDA(cudaMallocAsync(&d_scratch_o, slots * ostride * sizeof(int), st));
+  const int64_t cmstride = static_cast<int64_t>(cl) * 2 * fmax_cm * fmax_cm;
+  void* d_scratch_cm = nullptr;
+  PG_CUDA(cudaMallocAsync(&d_scratch_cm, std::max<int64_t>(slots * cmstride, 4) * sizeof(int), st));
   PG_CUDA(cudaMallocAsync(&d_counter, sizeof(int) * (2 + slots), st));
   PG_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(int) * (2 + slots), st));
   BatchArgs<TK, TV> a{};
@@ -1904,6 +1914,8 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   a.claims = static_cast<int*>(d_counter) + 2;
   a.scratch_pickup = static_cast<M*>(d_scratch_p);
   a.scratch_owner = static_cast<int*>(d_scratch_o);
+  a.scratch_cellmap = static_cast<int*>(d_scratch_cm);
+  a.cellmap_stride = cmstride;
   a.pickup_stride = pstride;
   a.owner_stride = ostride;
   launch_clustered(kern, grid, cl, std::max<size_t>(dyn, 16), st, a);
@@ -1911,7 +1923,8 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   PG_CUDA(cudaGetLastError());
   unsigned status = 0;
   PG_CUDA(cudaMemcpyAsync(&status, a.status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
-  for (void* d : {d_canvas, d_strokes, d_points, d_fp, d_order, d_scratch_p, d_scratch_o, d_counter})
+  for (void* d : {d_canvas, d_strokes, d_points, d_fp, d_order, d_scratch_p, d_scratch_o,
+                  d_scratch_cm, d_counter})
     PG_CUDA(cudaFreeAsync(d, st));
   PG_CUDA(cudaStreamSynchronize(st));
   for (int32_t c = 0; c < nc; c++) {

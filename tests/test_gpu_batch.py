@@ -55,11 +55,18 @@ def _setup(pg, sizes, storage, rng_seed=7, snap=True):
     return cs, bs, r0s
 
 
-@pytest.mark.parametrize("snap", [True, False])
-def test_batch_f64_equals_sequential_and_oracle(pg, oracle, snap):
+# radii up to 20; and 40-75, whose cell maps do not fit in shared memory beside the
+# support-disc list (global cell maps)
+@pytest.mark.parametrize("snap,rmin,rmax", [(True, 1.5, 20.0), (False, 1.5, 20.0),
+                                            (True, 40.0, 75.0)])
+def test_batch_f64_equals_sequential_and_oracle(pg, oracle, snap, rmin, rmax):
     rng = np.random.default_rng(11 + snap)
-    sizes = _canvases(rng, 7)
-    strokes = _session(rng, sizes)
+    if rmax > 30:
+        sizes = _canvases(rng, 3, smin=120, smax=220)
+        strokes = _session(rng, sizes, strokes_per=(2, 4), rmin=rmin, rmax=rmax)
+    else:
+        sizes = _canvases(rng, 7)
+        strokes = _session(rng, sizes)
     cs, bs, r0s = _setup(pg, sizes, "f64", snap=snap)
     n = pg.paint_batch(cs, bs, strokes)
     # sequential painty calls through the single-canvas entry points
