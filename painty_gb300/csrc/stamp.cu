@@ -1861,7 +1861,7 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   const int forced = env_cluster("PAINTY_BATCH_CLUSTER");
   int cl = 1, slots = 0;
   double best = 1e300;
-  for (int c2 : {1, 2, 4}) {
+  for (int c2 : {1, 2, 4, 8}) {
     if (forced && c2 != forced) continue;
     plan_all(c2);
     const int fits = max_clusters(kern, c2, std::max<size_t>(dyn, 16));
