@@ -2,6 +2,9 @@
 //   facade_demo errors            argument errors surface as std::invalid_argument (no GPU)
 //   facade_demo paint IN OUT      paints the stroke described in IN, writes the canvas to OUT
 //   facade_demo palette IN OUT    LoadPalette(IN) then SavePalette(OUT) (no GPU)
+//   facade_demo texture IN OUT    TextureBrush stroke + Renderer::render (F64), canvas to OUT
+//                                 IN: rows, cols, th, tw, tex[th*tw], npts, path[2*npts],
+//                                 radius, K[3], S[3]; OUT: painted, K, S, V, lit[rows*cols*3]
 //   facade_demo sbr               strokes through SbrRenderThread equal the same strokes
 //                                 painted directly with TextureBrushGpu (GPU)
 // IN (doubles): rows, cols, fh, fw, footprint[fh*fw], npts, path[2*npts], radius, spacing,
@@ -168,7 +171,48 @@ static int sbr() {
   return same && painted ? 0 : 1;
 }
 
+static int texture(const char* in, const char* out) {
+  std::ifstream f(in, std::ios::binary | std::ios::ate);
+  const std::streamsize bytes = f.tellg();
+  f.seekg(0);
+  std::vector<double> v(static_cast<size_t>(bytes) / sizeof(double));
+  f.read(reinterpret_cast<char*>(v.data()), static_cast<std::streamsize>(v.size() * sizeof(double)));
+  size_t i = 0;
+  auto take = [&](size_t n) {
+    std::vector<double> r(v.begin() + i, v.begin() + i + n);
+    i += n;
+    return r;
+  };
+  const int rows = static_cast<int>(v[i++]), cols = static_cast<int>(v[i++]);
+  const int th = static_cast<int>(v[i++]), tw = static_cast<int>(v[i++]);
+  const auto tex = take(size_t(th) * tw);
+  const int npts = static_cast<int>(v[i++]);
+  const auto xy = take(size_t(npts) * 2);
+  const double radius = v[i++];
+  const auto K = take(3), S = take(3);
+  pg::Canvas canvas(rows, cols, pg::Storage::F64);
+  canvas.setBackground(std::vector<double>(size_t(rows) * cols * 3, 0.9));
+  pg::TextureBrush brush(tex, th, tw);
+  brush.setRadius(radius);
+  brush.dip({pg::vec3{K[0], K[1], K[2]}, pg::vec3{S[0], S[1], S[2]}});
+  std::vector<pg::vec2> path;
+  for (int p = 0; p < npts; p++) path.push_back({xy[2 * p], xy[2 * p + 1]});
+  const int64_t painted = brush.paintStroke(path, canvas);
+  auto layer = canvas.getPaintLayer();
+  const auto k = layer.getK_buffer(), s = layer.getS_buffer(), vol = layer.getV_buffer();
+  const auto lit = pg::Renderer().render(canvas, pg::Storage::F64).download();
+  std::ofstream o(out, std::ios::binary);
+  const double nd = static_cast<double>(painted);
+  o.write(reinterpret_cast<const char*>(&nd), sizeof(double));
+  for (const auto* vec : {&k, &s, &vol, &lit})
+    o.write(reinterpret_cast<const char*>(vec->data()),
+            static_cast<std::streamsize>(vec->size() * sizeof(double)));
+  std::printf("painted %lld pixels\n", static_cast<long long>(painted));
+  return 0;
+}
+
 int main(int argc, char** argv) {
+  if (argc >= 4 && std::strcmp(argv[1], "texture") == 0) return texture(argv[2], argv[3]);
   if (argc >= 2 && std::strcmp(argv[1], "sbr") == 0) return sbr();
   if (argc >= 2 && std::strcmp(argv[1], "errors") == 0) return errors();
   if (argc >= 4 && std::strcmp(argv[1], "paint") == 0) return paint(argv[2], argv[3]);

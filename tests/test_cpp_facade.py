@@ -93,3 +93,34 @@ def test_facade_paints_like_python_binding(demo, pg, tmp_path):
     want = [np.array([n], dtype=np.float64), c.download("K").ravel(), c.download("S").ravel(),
             c.download("V").ravel(), pg.Renderer().compose(c).download().ravel()]
     assert np.array_equal(got, np.concatenate(want))
+
+
+@pytest.mark.gpu
+def test_facade_texture_brush_and_render(demo, pg, tmp_path):
+    """TextureBrush and Renderer::render through the C++ facade equal the Python binding."""
+    rows, cols = 60, 80
+    tex = workloads.stroke_texture(seed=13)
+    path = np.array([[5.0, 10.0], [40.0, 30.0], [75.0, 22.0]])
+    K, S = np.array([0.4, 1.1, 2.2]), np.array([0.6, 0.3, 0.2])
+    buf = np.concatenate([[rows, cols, tex.shape[0], tex.shape[1]], tex.ravel(), [len(path)],
+                          path.ravel(), [9.0], K, S])
+    inp, out = tmp_path / "tin.bin", tmp_path / "tout.bin"
+    buf.astype(np.float64).tofile(inp)
+    r = subprocess.run([str(demo), "texture", str(inp), str(out)], capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    got = np.fromfile(out, dtype=np.float64)
+    c = pg.Canvas(rows, cols, "f64")
+    c.setBackground(np.full((rows, cols, 3), 0.9))
+    b = pg.TextureBrush(tex)
+    b.setRadius(9.0)
+    b.dip((K, S))
+    n = b.paintStroke(path, c)
+    npx = rows * cols
+    assert got[0] == n and n > 0
+    o = 1
+    for p, nch in (("K", 3), ("S", 3), ("V", 1)):
+        want = c.download(p).ravel()
+        assert np.array_equal(got[o:o + npx * nch], want), p
+        o += npx * nch
+    assert np.array_equal(got[o:o + npx * 3], pg.Renderer().render(c).download().ravel())
