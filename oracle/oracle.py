@@ -1,7 +1,7 @@
 """Python binding of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
 
-Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this module, as the
-checker. It loads oracle/_build/liboracle.so (the double-precision restatement of painty's
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this module, to check
+results. It loads oracle/_build/liboracle.so (the double-precision restatement of painty's
 paint path, oracle/painty_oracle.cpp) and, where it was built, oracle/_ref/libpainty_ref.so
 (painty's own headers compiled against the repository's Eigen/OpenCV stand-ins).
 """

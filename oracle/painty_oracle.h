@@ -1,8 +1,8 @@
 /*
  * painty_oracle.h -- CPU oracle for the Kubelka-Munk paint path of lindemeier/painty.
  *
- * TEST INFRASTRUCTURE ONLY. This library is the checker: only tests/, the smoke check in
- * __graft_entry__.py and bench.py's CPU-baseline leg may load it. The product library
+ * TEST INFRASTRUCTURE ONLY. This library checks the GPU results: only tests/, the smoke check
+ * in __graft_entry__.py and bench.py's CPU-baseline leg may load it. The product library
  * (painty_gb300) never links or calls it.
  *
  * It restates, in double precision and with the reference's own loop order and branches:
