@@ -132,6 +132,27 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows), "window": where}
 
 
+def _workloads_module():
+    """painty_gb300/workloads.py loaded by path: the reference arm must not import the package
+    (its __init__ maps the CUDA library)."""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("painty_workloads_standalone",
+                                                  ROOT / "painty_gb300" / "workloads.py")
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[spec.name] = mod  # dataclasses look their module up while being defined
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def _headline_config(ws: int) -> dict:
+    """The `config` of the headline line, shared by both arms."""
+    return {"workload": f"KM composite {ROWS}x{COLS}, {LAYERS} stacked FP32 layers -> RGB",
+            "rows": ROWS, "cols": COLS, "layers": LAYERS, "storage": "f32",
+            "l2": "inputs 4.2 GB per step > 129 MB L2 (no flush needed)",
+            "parallelism": f"replicas{ws}"}
+
+
 def _dist():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -486,10 +507,7 @@ def run_ours(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded, generated on the device)",
-            "config": {"workload": f"KM composite {ROWS}x{COLS}, {LAYERS} stacked FP32 layers -> RGB",
-                       "rows": ROWS, "cols": COLS, "layers": LAYERS, "storage": "f32",
-                       "l2": "inputs 4.2 GB per step > 129 MB L2 (no flush needed)",
-                       "parallelism": f"replicas{ws}"},
+            "config": _headline_config(ws),
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                          "unit": "GB/s", "frac": round(achieved / peak, 4),
                          "peak_kind": peak_kind, "traffic": _traffic_from_profile(),
@@ -893,8 +911,8 @@ def run_reference(args):
     if rank != 0:
         return
     from oracle.oracle import Oracle
-    from painty_gb300 import workloads
 
+    workloads = _workloads_module()
     o = Oracle()
     cores = os.cpu_count() or 1
     rows = 256  # per step: 256 rows x 4096 cols through all 8 layers
@@ -913,8 +931,7 @@ def run_reference(args):
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-        "config": {"workload": f"KM composite {ROWS}x{COLS}, {LAYERS} stacked FP32 layers -> RGB",
-                   "rows": ROWS, "cols": COLS, "layers": LAYERS},
+        "config": _headline_config(ws),
         "cpu_baseline": {"value": round(value, 3), "unit": "Mpix/s", "cores": cores,
                          "kind": "port", "sample": sample},
         "e2e": {"value": round(value, 3), "unit": "Mpix/s", "h2d_bytes_per_step": 0,

@@ -8,6 +8,7 @@ paint path, oracle/painty_oracle.cpp) and, where it was built, oracle/_ref/libpa
 from __future__ import annotations
 
 import ctypes as C
+import os
 import subprocess
 from pathlib import Path
 
@@ -16,7 +17,8 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liboracle.so"
 REF_LIB = HERE / "_ref" / "libpainty_ref.so"
-REFERENCE_ROOT = Path("/root/reference")
+# the reference checkout (only the reference-header build reads it)
+REFERENCE_ROOT = Path(os.environ.get("PAINTY_REFERENCE_ROOT", "/root/reference"))
 
 _P, _I32, _I64, _D = C.c_void_p, C.c_int32, C.c_int64, C.c_double
 

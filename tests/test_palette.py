@@ -1,6 +1,7 @@
 """Palette JSON I/O (LoadPalette / SavePalette, Serialization.cxx:38-53) and the swatch image
 (VisualizePalette, :64-135)."""
 import io
+import os
 from pathlib import Path
 
 import numpy as np
@@ -36,7 +37,7 @@ def test_load_rejects_incomplete_entries():
 
 def test_load_reference_palettes():
     """painty's own palette files, where the checkout is present (14-pigment measured set)."""
-    root = Path("/root/reference/data/paint_palettes")
+    root = Path(os.environ.get("PAINTY_REFERENCE_ROOT", "/root/reference")) / "data" / "paint_palettes"
     if not root.is_dir():
         pytest.skip("reference checkout not present")
     pal = P.load_palette(root / "lindemeier-measured.json")
