@@ -196,7 +196,9 @@ def run_precision_only(args):
     import painty_gb300 as pg
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    print(json.dumps(run_precision(pg, torch)), flush=True)
+    host = generate_stack_device(torch, seed=1)
+    Kh, Sh, Vh, R0h = (host[k].numpy() for k in ("K", "S", "V", "R0"))
+    print(json.dumps(run_precision(pg, torch, (Kh, Sh, Vh, R0h))), flush=True)
 
 
 def run_batch_only(args):
@@ -498,7 +500,7 @@ def run_ours(args):
     if rank == 0 and not args.no_stamps:
         stamps = run_stamps_config0(pg, torch, cpu=not args.no_cpu)
         serve = run_serve(pg, torch, args.serve_rate, args.serve_seconds)
-        prec = run_precision(pg, torch)
+        prec = run_precision(pg, torch, (Kh, Sh, Vh, R0h))
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(Kh, Sh, Vh, R0h)
     if rank == 0:
@@ -604,7 +606,10 @@ def run_batch(pg, torch, storage: str, ncanvas: int, max_strokes, rank: int = 0,
     by estimated work), and the job's rate is all stamps over the slowest rank's time."""
     from painty_gb300 import sharding, workloads
 
-    specs, strokes = workloads.batch_canvases(ncanvas, seed=2, max_strokes=max_strokes)
+    if ncanvas == 512 and max_strokes is None:
+        specs, strokes = config2_workload()
+    else:
+        specs, strokes = workloads.batch_canvases(ncanvas, seed=2, max_strokes=max_strokes)
     if world > 1:
         work = np.zeros(len(specs))
         for c, path, r, sp, _, _ in strokes:
@@ -642,8 +647,11 @@ def run_batch(pg, torch, storage: str, ncanvas: int, max_strokes, rank: int = 0,
         dt, n = float(t_.item()), int(n_.item())
     px = sum(r * c for r, c, _ in specs)
     cl, nclusters = pg.batch_last_shape()
-    roof = stamp_roofline([(s[2], pg_stroke_stamps(np.asarray(s[1]), s[3])) for s in strokes],
-                          n, dt, storage)
+    per_stroke = [pg_stroke_stamps(np.asarray(s[1]), s[3]) for s in strokes]
+    per_canvas = np.zeros(len(specs))
+    for s_, k_ in zip(strokes, per_stroke):
+        per_canvas[s_[0]] += k_
+    roof = stamp_roofline([(s[2], k_) for s, k_ in zip(strokes, per_stroke)], n, dt, storage)
     if roof:
         roof["note"] = ("canvases run concurrently, each canvas's stamps in order; the "
                         "heaviest canvas's chain of stamps bounds the launch")
@@ -651,6 +659,10 @@ def run_batch(pg, torch, storage: str, ncanvas: int, max_strokes, rank: int = 0,
             "s": round(dt, 3), "storage": storage, "gpu_launches": pg.kernel_launch_count() - l0,
             "roofline": roof,
             "ctas_per_canvas": cl, "clusters": nclusters,
+            "makespan_s": round(dt, 3),
+            "heaviest_canvas_stamps": int(per_canvas.max()) if len(per_canvas) else 0,
+            "heaviest_canvas_stamps_per_s": round(float(per_canvas.max()) / dt, 1) if n else 0.0,
+            "mean_canvas_stamps": round(float(per_canvas.mean()), 1) if len(per_canvas) else 0.0,
             "config": f"{ncanvas} canvases (side logU[256,2048], aspect U[0.5,2], "
                       f"{pg_canvas_px(px)}), {len(strokes)} strokes (logU[50,2000] per canvas"
                       f"{'' if max_strokes is None else f', at most {max_strokes}'}), "
@@ -805,75 +817,186 @@ def composite_precision(pg, torch, Kh, Sh, Vh, R0h, steps: int):
     return out
 
 
-def run_precision(pg, torch):
-    """Reduced-precision storage against the F64 path (painty's double arithmetic, bit-exact
-    with its CPU code; tested): CIEDE2000 max / mean and max |dR| of the composed reflectance.
-    composite: the composite-stress distributions on 1024 x 1024 x 8 layers; stamps: the plain
-    case's first 40 strokes; batched: 6 canvases of the batching workload, at most 30 strokes
-    each, in one paint_batch per storage."""
-    from painty_gb300 import color, workloads
+_CONFIG2 = {}
+
+
+def config2_workload():
+    """The batching workload at its stated size (512 canvases, seed 2), generated once."""
+    if "w" not in _CONFIG2:
+        from painty_gb300 import workloads
+        _CONFIG2["w"] = workloads.batch_canvases(512, seed=2)
+    return _CONFIG2["w"]
+
+
+def _precision_canvases(n: int = 8):
+    """The n canvases of the batching workload with at least 1500 strokes and the fewest
+    stamps (long stroke chains, radii up to 64), in that order."""
+    specs, strokes = config2_workload()
+    ns = np.zeros(len(specs), int)
+    st = np.zeros(len(specs))
+    for c, path, r, sp, _, _ in strokes:
+        ns[c] += 1
+        st[c] += pg_stroke_stamps(np.asarray(path), sp)
+    cand = [c for c in np.argsort(st, kind="stable") if ns[c] >= 1500][:n]
+    return [int(c) for c in cand], ns, st
+
+
+def run_precision(pg, torch, host=None):
+    """Reduced-precision storage against the double oracle (painty's CPU path restated, pinned
+    bit for bit to painty's own code): CIEDE2000 max / mean and max |dR| of the composed
+    reflectance, per storage (FP32, FP16, BF16; all arithmetic FP32).
+
+    composite: the composite-stress workload at its full 4096 x 4096 x 8, against the oracle's
+               double composite of the same FP32 inputs (all host threads).
+    stamps:    the plain workload in full (1024 x 768, 200 strokes) against the oracle.
+    batched:   8 canvases of the batching workload (512-canvas generator) with 1500+ strokes,
+               the 8 with the fewest stamps, radii up to 64, one paint_batch per storage; against
+               the GPU's F64 mode for all 8 (painty's double arithmetic, bit-exact with the
+               oracle in the tests) and against the oracle itself for the 2 smallest -- where the
+               F64 mode's equality with the oracle is checked too."""
+    import concurrent.futures as cf
+
+    from oracle.oracle import Oracle
+    from painty_gb300 import workloads
+
+    o = Oracle()
+    cores = os.cpu_count() or 1
 
     def stats(ref, got):
-        de = color.delta_e(ref, got)
-        return {"de_max": round(float(de.max()), 4), "de_mean": round(float(de.mean()), 5),
+        de_max, de_mean = o.delta_e(got, ref, threads=cores)
+        return {"de_max": round(float(de_max), 4), "de_mean": round(float(de_mean), 5),
                 "dr_max": float(f"{np.abs(got - ref).max():.3g}")}
 
-    out = {"reference": "F64 storage (painty's double arithmetic)"}
-    # composite
-    n = 1024
-    K, S, V, R0 = workloads.composite_stack(n, n, LAYERS, seed=1, dtype=np.float64)
-    imgs = {}
-    for st in ("f64", "f32", "f16", "bf16"):
-        rs = "f64" if st == "f64" else "f32"
-        layers = []
-        for l in range(LAYERS):
-            ly = pg.PaintLayer(n, n, st)
-            ly.upload("K", K[l], planar=True)
-            ly.upload("S", S[l], planar=True)
-            ly.upload("V", V[l], planar=True)
-            layers.append(ly)
-        r0 = pg.Image(n, n, rs)
-        r0.upload(R0, planar=True)
-        img = pg.Image(n, n, rs)
-        pg.compose_layers(layers, r0, img)
-        imgs[st] = img.download()
-    out["composite"] = {st: stats(imgs["f64"], imgs[st]) for st in ("f32", "f16", "bf16")}
-    # plain painting
-    rows, cols = 768, 1024
-    strokes = workloads.strokes(cols, rows, 40, seed=3)
+    out = {"reference": "the double oracle (painty's CPU path restated; pinned to painty's own "
+                        "code bit for bit)", "target": "max dE2000 < 0.5 (16-bit storage)"}
     fp = workloads.footprint_image(seed=7)
-    r0h = workloads.substrate(rows, cols, seed=5)
-    imgs = {}
-    for st in ("f64", "f32", "f16", "bf16"):
-        cv = pg.Canvas(rows, cols, st)
+    pool = cf.ThreadPoolExecutor(max_workers=4)
+
+    # -- oracle work on host threads, beside the GPU runs below
+    rows0, cols0 = 768, 1024
+    strokes0 = workloads.strokes(cols0, rows0, 200, seed=3)
+    r0h = workloads.substrate(rows0, cols0, seed=5)
+
+    def oracle_config0():
+        oc = o.canvas(rows0, cols0)
+        oc.set("R0", r0h)
+        ob = o.brush(strokes0[0].radius, fp)
+        ob.set_rates(0.05, 0.1)
+        for s_ in strokes0:
+            ob.set_radius(s_.radius)
+            ob.dip(s_.K, s_.S)
+            ob.paint_stroke(oc, s_.path, s_.spacing)
+        return oc.compose(), {p_: oc.get(p_) for p_ in ("K", "S", "V")}
+
+    specs, strokes = config2_workload()
+    pick, ns, st = _precision_canvases(8)
+    sub_specs = [specs[c] for c in pick]
+    index = {c: i for i, c in enumerate(pick)}
+    sub_strokes = [(index[x[0]],) + tuple(x[1:]) for x in strokes if x[0] in index]
+
+    def oracle_canvas(i):
+        rows, cols, r0 = sub_specs[i]
+        oc = o.canvas(rows, cols)
+        oc.set("R0", r0.astype(np.float64))
+        ob = o.brush(8.0, fp)
+        ob.set_rates(0.05, 0.1)
+        for ci, path, r, sp, K, S in sub_strokes:
+            if ci == i:
+                ob.set_radius(r)
+                ob.dip(K, S)
+                ob.paint_stroke(oc, path, sp)
+        return oc.compose(), {p_: oc.get(p_) for p_ in ("K", "S", "V")}
+
+    t_or = time.perf_counter()
+    fut0 = pool.submit(oracle_config0)
+    fut_c = [pool.submit(oracle_canvas, i) for i in (0, 1)]
+
+    # -- plain painting, full config 0, on the GPU
+    imgs0 = {}
+    for stg in ("f32", "f16", "bf16"):
+        cv = pg.Canvas(rows0, cols0, stg)
         cv.setBackground(r0h)
-        br = pg.FootprintBrush(strokes[0].radius, fp)
+        br = pg.FootprintBrush(strokes0[0].radius, fp)
         br.setPickupRate(0.05)
         br.setDepositionRate(0.1)
-        workloads.paint_config0(cv, br, strokes)
-        imgs[st] = pg.Renderer().compose(cv).download()
-    out["stamps"] = {st: stats(imgs["f64"], imgs[st]) for st in ("f32", "f16", "bf16")}
-    # batched painting
-    specs, bstrokes = workloads.batch_canvases(6, seed=2, max_strokes=30)
+        workloads.paint_config0(cv, br, strokes0)
+        imgs0[stg] = (pg.Renderer().compose(cv).download(),
+                      {p_: cv.download(p_) for p_ in ("K", "S", "V")})
+        del cv, br
+
+    # -- batched painting of the 8 canvases, every storage
     res = {}
-    for st in ("f64", "f16", "bf16"):
+    for stg in ("f64", "f32", "f16", "bf16"):
         cvs, brs = [], []
-        for rr, cc, r0 in specs:
-            cv = pg.Canvas(rr, cc, st)
+        for rr, cc, r0 in sub_specs:
+            cv = pg.Canvas(rr, cc, stg)
             cv.upload("R0", r0)
             b = pg.FootprintBrush(8.0, fp)
             b.setPickupRate(0.05)
             b.setDepositionRate(0.1)
             cvs.append(cv)
             brs.append(b)
-        pg.paint_batch(cvs, brs, bstrokes)
-        res[st] = [pg.Renderer().compose(cv).download() for cv in cvs]
-    out["batched"] = {}
-    for st in ("f16", "bf16"):
-        per = [stats(a, b) for a, b in zip(res["f64"], res[st])]
-        out["batched"][st] = {"de_max": max(p["de_max"] for p in per),
-                              "de_mean": round(float(np.mean([p["de_mean"] for p in per])), 5),
-                              "dr_max": max(p["dr_max"] for p in per)}
+        t = time.perf_counter()
+        pg.paint_batch(cvs, brs, sub_strokes)
+        torch.cuda.synchronize()
+        res[stg] = ([pg.Renderer().compose(cv).download() for cv in cvs],
+                    [{p_: cv.download(p_) for p_ in ("K", "S", "V")} for cv in (cvs[:2] if stg == "f64" else [])],
+                    time.perf_counter() - t)
+        del cvs, brs
+
+    # -- composite: full composite-stress workload, GPU storages vs the oracle
+    comp = {}
+    if host is not None:
+        Kh, Sh, Vh, R0h = host
+        R, Cc = R0h.shape[1:]
+        ref = o.compose_layers_f32_planar_f64(Kh, Sh, Vh, R0h, threads=cores)
+        for stg in ("f32", "f16", "bf16"):
+            layers = []
+            for l in range(Vh.shape[0]):
+                ly = pg.PaintLayer(R, Cc, stg)
+                ly.upload("K", Kh[l], planar=True)
+                ly.upload("S", Sh[l], planar=True)
+                ly.upload("V", Vh[l], planar=True)
+                layers.append(ly)
+            r0 = pg.Image(R, Cc)
+            r0.upload(R0h, planar=True)
+            img = pg.Image(R, Cc)
+            pg.compose_layers(layers, r0, img)
+            comp[stg] = stats(ref, img.download())
+            del layers, r0, img
+        del ref
+        comp["workload"] = (f"{R}x{Cc}, {Vh.shape[0]} layers (composite-stress distributions); "
+                            "oracle: painty's ComputeReflectance loop in double, every pixel")
+    out["composite"] = comp
+
+    ref0, planes0 = fut0.result()
+    out["stamps"] = {stg: stats(ref0, imgs0[stg][0]) for stg in ("f32", "f16", "bf16")}
+    rel = max(float((np.abs(imgs0["f32"][1][p_] - planes0[p_]) /
+                     np.maximum(np.abs(planes0[p_]), 1.0)).max()) for p_ in ("K", "S", "V"))
+    out["stamps"]["f32"]["rel_max_KSV"] = float(f"{rel:.3g}")
+    out["stamps"]["workload"] = "1024x768, 200 strokes r U[8,32] (the plain workload, full); oracle: the whole canvas"
+    ocs = [f.result() for f in fut_c]
+    oracle_s = time.perf_counter() - t_or
+    bat = {"canvases": pick, "strokes": [int(ns[c]) for c in pick],
+           "stamps": [int(st[c]) for c in pick], "rmax": 64}
+    bat["vs_gpu_f64"] = {}
+    for stg in ("f32", "f16", "bf16"):
+        per = [stats(a, b) for a, b in zip(res["f64"][0], res[stg][0])]
+        bat["vs_gpu_f64"][stg] = {"de_max": max(q["de_max"] for q in per),
+                                  "de_mean": round(float(np.mean([q["de_mean"] for q in per])), 5),
+                                  "dr_max": max(q["dr_max"] for q in per)}
+    bat["vs_oracle"] = {"canvases": pick[:2]}
+    for stg in ("f32", "f16", "bf16"):
+        per = [stats(ocs[i][0], res[stg][0][i]) for i in range(2)]
+        bat["vs_oracle"][stg] = {"de_max": max(q["de_max"] for q in per),
+                                 "de_mean": round(float(np.mean([q["de_mean"] for q in per])), 5),
+                                 "dr_max": max(q["dr_max"] for q in per)}
+    bat["vs_oracle"]["gpu_f64_equals_oracle"] = bool(all(
+        np.array_equal(res["f64"][1][i][p_], ocs[i][1][p_]) for i in range(2) for p_ in ("K", "S", "V")))
+    bat["gpu_s"] = {stg: round(res[stg][2], 2) for stg in res}
+    bat["oracle_s"] = round(oracle_s, 1)
+    out["batched"] = bat
+    pool.shutdown()
     torch.cuda.synchronize()
     return out
 
@@ -949,10 +1072,10 @@ def main():
     ap.add_argument("--cols", type=int, default=COLS, help="composite cols (profiling cases)")
     ap.add_argument("--no-stamps", action="store_true")
     ap.add_argument("--stamps-only", action="store_true", help="only the stamping case")
-    ap.add_argument("--batch-canvases", type=int, default=152,
-                    help="canvases in the batched stamping case")
-    ap.add_argument("--batch-max-strokes", type=int, default=200,
-                    help="cap on strokes per canvas in the batched stamping case")
+    ap.add_argument("--batch-canvases", type=int, default=512,
+                    help="canvases in the batched stamping case (the stated workload: 512)")
+    ap.add_argument("--batch-max-strokes", type=int, default=None,
+                    help="cap on strokes per canvas in the batched stamping case (none: as stated)")
     ap.add_argument("--strokes", type=int, default=200, help="strokes in the stamping case")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--serve-only", action="store_true", help="only the serving case")

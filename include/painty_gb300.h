@@ -391,20 +391,25 @@ painty_status painty_mix_paint(const double* weights, int32_t n, const double* p
  * callers that cannot allocate device memory).
  *
  * Some callers cannot call cudaMalloc: a plugin whose host application owns every byte of
- * device memory and hands out fixed buffers, a real-time paint loop that must not pay the
- * device-wide synchronisation an allocation can cause, or code that runs while another
- * thread captures a CUDA graph. painty_stamps allocates on first use (snapshot, pickup map,
- * scratch); this entry point allocates nothing. The caller passes every input and output as
- * its own device memory, and the only scratch -- an owner table of map_side^2 ints and a
- * status word -- is a fixed array inside the library (about 258 KB, held on every GPU that
- * loads the library until the process exits).
+ * device memory and hands out fixed buffers, or a real-time paint loop that must not pay the
+ * device-wide synchronisation an allocation can cause. painty_stamps allocates on first use
+ * (snapshot, pickup map, scratch); this entry point allocates nothing. The caller passes every
+ * input and output as its own device memory, and the only scratch -- an owner table of
+ * map_side^2 ints and a status word -- is a fixed array inside the library (about 256 KB,
+ * held on every GPU that loads the library until the process exits).
  *
  * Semantics are painty_stamps' on an F32 canvas: stamps applied in order, each one
- * FootprintBrush::imprint. Limits: map_side <= PAINTY_NOALLOC_MAX_MAP_SIDE (radius about 90);
- * larger sizes return PAINTY_ERR_INVALID_ARGUMENT. The first call on a device looks up the
- * scratch address; make it before any stream capture. Calls share the scratch: calls that
- * overlap on the GPU (other streams, other threads) race, so serialise them. The call returns
- * after the stamps ran (it reads the kernel's status word).
+ * FootprintBrush::imprint. Limits: map_side <= PAINTY_NOALLOC_MAX_MAP_SIDE (256; with the
+ * footprint side at most 255 this is radius 90); larger sizes return
+ * PAINTY_ERR_INVALID_ARGUMENT, as do a negative or non-finite radius and non-finite rates,
+ * capacity or paint. The stamp records are device data and are not checked: they must be
+ * finite, with |cx|, |cy| < 1e9 (painty_stamps' bound).
+ *
+ * The first call on a device -- and the first after that device's context was re-created,
+ * e.g. by cudaDeviceReset -- looks up the scratch array's device address; make that call
+ * before any stream capture. Calls share the scratch: calls that overlap on the GPU (other
+ * streams, other threads) race, so serialise them. The call waits for its stream: it
+ * returns after the stamps ran (it reads the kernel's status word back to the host).
  *
  * Buffers (device memory, FP32):
  *   canvas_*:   the wet layer, rows x pitch elements per plane (pitch >= cols)
@@ -416,7 +421,7 @@ painty_status painty_mix_paint(const double* weights, int32_t n, const double* p
  *   stamps:     n records of 4 doubles: cx, cy, cos(-theta), sin(-theta)
  * Brush values: radius (the brush's current radius), rates, capacity (painty uses 1.0) and the
  * dipped paint. */
-#define PAINTY_NOALLOC_MAX_MAP_SIDE 257
+#define PAINTY_NOALLOC_MAX_MAP_SIDE 256
 typedef struct painty_stamp_buffers_f32 {
   float* canvas_K[3];
   float* canvas_S[3];

@@ -65,6 +65,7 @@ class Oracle:
         self._interp = L.f("interpolate", _P, _I32, _I32, _D, _D, res=_D)
         self._compose = L.f("compose_layers", _I64, _I32, _P, _P, _P, _P, _P, _I32, _I32)
         self._compose32 = L.f("compose_layers_f32_soa", _I64, _I32, _P, _P, _P, _P, _P, _I32)
+        self._compose32d = L.f("compose_layers_f32_soa_f64", _I64, _I32, _P, _P, _P, _P, _P, _I32)
         self._cc = L.f("canvas_create", _I32, _I32, res=_P)
         self._cd = L.f("canvas_destroy", _P)
         self._cp = L.f("canvas_plane", _P, _I32, res=_P)
@@ -85,6 +86,7 @@ class Oracle:
         self._binfo = L.f("brush_info", _P, C.POINTER(_I32), C.POINTER(_I32), res=_D)
         self._bfp = L.f("brush_footprint", _P, res=_P)
         self._bpick = L.f("brush_pickup", _P, _I32, res=_P)
+        self._bsnapget = L.f("brush_snapshot", _P, _I32, C.POINTER(_I32), C.POINTER(_I32), res=_P)
         self._mix = L.f("mix_single_paint", _P, _I32, _P, _P, _P, _P)
         self._lab = L.f("rgb2lab", _P, _P)
         self._de = L.f("ciede2000", _P, _P, res=_D)
@@ -134,6 +136,16 @@ class Oracle:
         npix = V[0].size
         out = np.empty((3,) + V.shape[1:], dtype=np.float32)
         self._compose32(npix, L, _p(K), _p(S), _p(V), _p(R0), _p(out), threads)
+        return out
+
+    def compose_layers_f32_planar_f64(self, K, S, V, R0, threads: int = 1):
+        """The reference composite over float32 planar stacks K, S (L, 3, rows, cols),
+        V (L, rows, cols), R0 (3, rows, cols), kept in double: (rows, cols, 3)."""
+        K, S, V, R0 = (np.ascontiguousarray(x, dtype=np.float32) for x in (K, S, V, R0))
+        L = V.shape[0]
+        npix = V[0].size
+        out = np.empty(V.shape[1:] + (3,), dtype=np.float64)
+        self._compose32d(npix, L, _p(K), _p(S), _p(V), _p(R0), _p(out), threads)
         return out
 
     def mix_single_paint(self, w, K, S):
@@ -409,6 +421,19 @@ class OBrush:
         n = S * S * (1 if which == "V" else 3)
         a = np.ctypeslib.as_array(C.cast(self.o._bpick(self.h, idx), C.POINTER(_D)), (n,))
         return a.reshape((S, S) if which == "V" else (S, S, 3)).copy()
+
+    def snapshot(self, which: str):
+        """The brush's snapshot buffer (FootprintBrush::_snapshotBuffer) plane K, S or V;
+        None before the brush's first snapshot."""
+        idx = {"K": 0, "S": 1, "V": 2}[which]
+        rows, cols = _I32(0), _I32(0)
+        ptr = self.o._bsnapget(self.h, idx, C.byref(rows), C.byref(cols))
+        if not ptr or rows.value * cols.value == 0:
+            return None
+        n = rows.value * cols.value * (1 if which == "V" else 3)
+        a = np.ctypeslib.as_array(C.cast(ptr, C.POINTER(_D)), (n,))
+        shape = (rows.value, cols.value) if which == "V" else (rows.value, cols.value, 3)
+        return a.reshape(shape).copy()
 
 
 class Reference:

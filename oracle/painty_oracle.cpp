@@ -533,6 +533,44 @@ void orc_compose_layers(int64_t npix, int32_t L, const double* K, const double* 
   });
 }
 
+extern "C++" {
+namespace {
+// Renderer::compose over float32 planar stacks in double (PaintLayer.hxx:81-96 per layer),
+// written through `put(p, r)`.
+template <class Put>
+void compose_f32_soa(int64_t npix, int32_t L, const float* K, const float* S, const float* V,
+                     const float* R0, int32_t nthreads, Put put) {
+  parallel_for(npix, nthreads, [&](int64_t lo, int64_t hi, int) {
+    for (int64_t p = lo; p < hi; p++) {
+      double r[3] = {R0[p], R0[npix + p], R0[2 * npix + p]};
+      for (int l = 0; l < L; l++) {
+        double k[3], s[3], nr[3];
+        for (int ch = 0; ch < 3; ch++) {
+          k[ch] = K[(static_cast<int64_t>(l) * 3 + ch) * npix + p];
+          s[ch] = S[(static_cast<int64_t>(l) * 3 + ch) * npix + p];
+        }
+        reflectance_ref(k, s, r, V[static_cast<int64_t>(l) * npix + p], nr);
+        r[0] = nr[0];
+        r[1] = nr[1];
+        r[2] = nr[2];
+      }
+      put(p, r);
+    }
+  });
+}
+}  // namespace
+}  // extern "C++"
+
+// The same composite with the double result kept, interleaved (npix, 3): the reference values
+// that reduced-precision results are measured against.
+void orc_compose_layers_f32_soa_f64(int64_t npix, int32_t L, const float* K, const float* S,
+                                    const float* V, const float* R0, double* out,
+                                    int32_t nthreads) {
+  compose_f32_soa(npix, L, K, S, V, R0, nthreads, [&](int64_t p, const double* r) {
+    for (int ch = 0; ch < 3; ch++) out[3 * p + ch] = r[ch];
+  });
+}
+
 void orc_compose_layers_f32_soa(int64_t npix, int32_t L, const float* K, const float* S,
                                 const float* V, const float* R0, float* out,
                                 int32_t nthreads) {

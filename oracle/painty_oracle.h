@@ -59,6 +59,9 @@ void orc_compose_layers(int64_t npix, int32_t L, const double* K, const double* 
                         const double* V, const double* R0, double* out, int32_t mode,
                         int32_t nthreads);
 /* Same with float inputs (timed CPU baseline over the GPU's own fp32 planes, SoA). */
+void orc_compose_layers_f32_soa_f64(int64_t npix, int32_t L, const float* K, const float* S,
+                                    const float* V, const float* R0, double* out,
+                                    int32_t nthreads);
 void orc_compose_layers_f32_soa(int64_t npix, int32_t L, const float* K, const float* S,
                                 const float* V, const float* R0, float* out,
                                 int32_t nthreads);

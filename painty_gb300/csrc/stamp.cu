@@ -1398,7 +1398,8 @@ struct SmemPlan {
 };
 template <class M>
 SmemPlan plan_smem_limit(int F, int S, int ndisc, size_t limit, bool allow_small = true,
-                         bool allow_pick = true, bool allow_cm_global = false) {
+                         bool allow_pick = true, bool allow_cm_global = false,
+                         int pick_vals = 8) {
   const bool cand[4][2] = {{false, true}, {false, false}, {true, true}, {true, false}};
   for (int pass = 0; pass < 3; pass++) {
     // pass 0: the disc list and cell maps in shared memory; 1: the cell maps in global
@@ -1410,7 +1411,7 @@ SmemPlan plan_smem_limit(int F, int S, int ndisc, size_t limit, bool allow_small
       const bool big = c[0], pick = c[1];
       if (!big && !allow_small) continue;
       if (pick && !allow_pick) continue;
-      const StampSmem L = stamp_smem_layout<M>(F, S, nd, !big, pick, !big, 8, cm_smem);
+      const StampSmem L = stamp_smem_layout<M>(F, S, nd, !big, pick, !big, pick_vals, cm_smem);
       if (L.total <= limit) return SmemPlan{big, pick, nd, L, !cm_smem};
     }
     if (ndisc == 0) break;
@@ -1418,12 +1419,15 @@ SmemPlan plan_smem_limit(int F, int S, int ndisc, size_t limit, bool allow_small
   fail(PAINTY_ERR_UNSUPPORTED, "stamp kernel shared memory plan failed");
 }
 
+// pick_vals: values per staged pickup cell -- 8 for the packed kernels' cell records, 7 for
+// the planar kernel's planes.
 template <class M>
 SmemPlan plan_smem(int F, int S, int ndisc, bool allow_small, bool allow_pick = true,
-                   bool allow_cm_global = false) {
+                   bool allow_cm_global = false, int pick_vals = 8) {
   const size_t limit = static_cast<size_t>(max_dyn_smem()) - sizeof(StampParams) * kParamRing -
                        sizeof(StampShared) - 512;
-  return plan_smem_limit<M>(F, S, ndisc, limit, allow_small, allow_pick, allow_cm_global);
+  return plan_smem_limit<M>(F, S, ndisc, limit, allow_small, allow_pick, allow_cm_global,
+                            pick_vals);
 }
 
 // Launch of a stamp-path kernel with `cluster` CTAs per thread-block cluster (1: a plain
@@ -2061,9 +2065,10 @@ void expand_stroke(const double* path, int32_t n, double spacing, std::vector<St
 
 // ====================================================================== allocation-free stamping
 // Scratch of painty_stamps_f32_noalloc: the per-stamp owner table (map_side^2 ints, up to
-// 257^2) followed by one status word. Every GPU that loads this library holds it (about
-// 258 KB) until the process exits. All calls share it; calls that overlap on the GPU race.
-constexpr int kNoAllocMaxMapSide = 257;
+// 256^2) followed by one status word. Every GPU that loads this library holds it (about
+// 256 KB) until the process exits. All calls share it; calls that overlap on the GPU race.
+// The footprint bound (side^2 <= 64 x 1024, side odd: at most 255) caps the map side at 256.
+constexpr int kNoAllocMaxMapSide = 256;
 constexpr int kNoAllocOwnerCells = kNoAllocMaxMapSide * kNoAllocMaxMapSide;
 static __device__ __align__(256) int g_noalloc_scratch[kNoAllocOwnerCells + 64];
 
@@ -2072,15 +2077,48 @@ namespace {
 constexpr int kNoAllocMaxDevices = 64;
 std::mutex g_noalloc_mu;
 void* g_noalloc_addr[kNoAllocMaxDevices] = {};
+unsigned long long g_noalloc_ctx[kNoAllocMaxDevices] = {};
+
+// Identity of the calling thread's current CUDA context (cuCtxGetId: unique for the life of
+// the process), through the runtime's driver entry points so the library needs no libcuda
+// link; 0 when unavailable or when no context is current yet. Called under g_noalloc_mu.
+unsigned long long current_context_id() {
+  using GetCurrent = int (*)(void**);                     // cuCtxGetCurrent(CUcontext*)
+  using GetId = int (*)(void*, unsigned long long*);      // cuCtxGetId(CUcontext, id*)
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static bool resolved = false;
+  if (!resolved) {
+    resolved = true;
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+          cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrent>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+          cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetId>(f);
+    cudaGetLastError();
+  }
+  if (!get_current || !get_id) return 0;
+  void* ctx = nullptr;
+  if (get_current(&ctx) != 0 || ctx == nullptr) return 0;
+  unsigned long long id = 0;
+  return get_id(ctx, &id) == 0 ? id : 0;
+}
 
 // Device address of the scratch array on the current device. The host-side symbol is only a
-// stand-in, so the address is looked up once per device, with that device current.
+// stand-in, so the address is looked up with that device current: once per device, and again
+// when the device's context was re-created since (cudaDeviceReset reloads the module, and the
+// array may move).
 int* noalloc_scratch() {
   int dev = 0;
   PG_CUDA(cudaGetDevice(&dev));
   PG_REQUIRE(dev >= 0 && dev < kNoAllocMaxDevices, "device ordinal out of range");
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_addr[dev]) {
+  const unsigned long long ctx = current_context_id();
+  if (!g_noalloc_addr[dev] || (ctx != 0 && ctx != g_noalloc_ctx[dev])) {
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || p == nullptr) {
@@ -2089,6 +2127,7 @@ int* noalloc_scratch() {
                               cudaGetErrorString(e));
     }
     g_noalloc_addr[dev] = p;
+    g_noalloc_ctx[dev] = current_context_id();  // the lookup made the context current
   }
   return static_cast<int*>(g_noalloc_addr[dev]);
 }
@@ -2277,8 +2316,9 @@ painty_status painty_stroke(painty_canvas* c, painty_brush* b, const double* pat
 }
 
 // Runs the stamp kernel on caller-owned buffers without allocating: the owner table and the
-// status word live in g_noalloc_scratch. The first call on a device looks up the scratch
-// address (make it before any stream capture). Synchronous: returns after the stamps ran.
+// status word live in g_noalloc_scratch. The first call on a device (and the first after its
+// context was re-created) looks up the scratch address; make it before any stream capture.
+// Synchronous: returns after the stamps ran.
 painty_status painty_stamps_f32_noalloc(const painty_stamp_buffers_f32* b, void* stream) {
   return guard([&] {
     PG_REQUIRE(b != nullptr, "buffers is null");
@@ -2286,15 +2326,23 @@ painty_status painty_stamps_f32_noalloc(const painty_stamp_buffers_f32* b, void*
     PG_REQUIRE(b->rows > 0 && b->cols > 0 && b->pitch >= b->cols, "bad canvas geometry");
     PG_REQUIRE(static_cast<int64_t>(b->rows) * b->pitch < (int64_t(1) << 31),
                "canvas too large for stamping (a plane holds 2^31 elements or more)");
+    PG_REQUIRE(b->map_side > 0 && b->map_side <= kNoAllocMaxMapSide,
+               "pickup map side above the allocation-free maximum of 256 (radius about 90)");
     PG_REQUIRE(b->footprint_side > 0 && (b->footprint_side & 1) == 1,
                "footprint side must be odd and positive");
     PG_REQUIRE(b->map_side >= b->footprint_side && b->map_side <= b->footprint_side + 1,
                "map side must be the footprint side or one more");
-    PG_REQUIRE(b->map_side <= kNoAllocMaxMapSide,
-               "pickup map side above the allocation-free maximum of 257 (radius about 90)");
     PG_REQUIRE(static_cast<int64_t>(b->footprint_side) * b->footprint_side <=
                  int64_t(pg::kMaxPixelsPerThread) * pg::kStampThreads,
-               "footprint side above 256");
+               "footprint side above 255");
+    // the brush values painty_brush_create / set_rates / dip accept
+    PG_REQUIRE(std::isfinite(b->radius) && b->radius >= 0.0, "radius must be finite and >= 0");
+    PG_REQUIRE(std::isfinite(b->pickup_rate) && std::isfinite(b->deposition_rate) &&
+                 std::isfinite(b->capacity),
+               "rates and capacity must be finite");
+    for (int i = 0; i < 3; i++)
+      PG_REQUIRE(std::isfinite(b->paint_K[i]) && std::isfinite(b->paint_S[i]),
+                 "paint K and S must be finite");
     for (int i = 0; i < 3; i++)
       PG_REQUIRE(b->canvas_K[i] && b->canvas_S[i] && b->pickup_K[i] && b->pickup_S[i],
                  "null plane");
@@ -2344,8 +2392,10 @@ painty_status painty_stamps_f32_noalloc(const painty_stamp_buffers_f32* b, void*
     a.owner_global = scratch;
     a.status = status;
     a.support2 = 2 * b->footprint_side * b->footprint_side;  // no cull: every box pixel
+    // planar pickup map: 7 values per staged cell
     const pg::SmemPlan plan = pg::plan_smem<float>(
-        b->footprint_side, b->map_side, pg::disc_count(b->footprint_side, a.support2), false);
+        b->footprint_side, b->map_side, pg::disc_count(b->footprint_side, a.support2), false,
+        true, false, 7);
     a.ndisc = plan.ndisc;
     a.pickup_smem = plan.pick ? 1 : 0;
     a.footprint_smem = 0;
@@ -2353,7 +2403,7 @@ painty_status painty_stamps_f32_noalloc(const painty_stamp_buffers_f32* b, void*
     auto kern = a.pickup_smem ? pg::stamp_kernel<true, true, false, false, float, float>
                               : pg::stamp_kernel<false, true, false, false, float, float>;
     const pg::StampSmem Lk = pg::stamp_smem_layout<float>(b->footprint_side, b->map_side, a.ndisc,
-                                                          false, a.pickup_smem != 0, false);
+                                                          false, a.pickup_smem != 0, false, 7);
     PG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(Lk.total)));
     kern<<<1, pg::kStampThreads, Lk.total, st>>>(a);

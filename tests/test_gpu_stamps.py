@@ -10,13 +10,13 @@ from painty_gb300 import workloads
 
 pytestmark = pytest.mark.gpu
 
-F32_REL_TOL = 2e-3   # per-value relative error of K, S, V after a stroke sequence (FP32)
-F32_DELTA_E = 0.05   # CIEDE2000 of the composed canvas, FP32 storage vs the double oracle
-F16_DELTA_E = 0.5    # CIEDE2000 of the composed canvas, FP16 storage vs the double oracle
-# BF16 keeps 8 significant bits; a pixel re-blended by every stamp over it drifts. With the
-# stochastic rounding of 16-bit stores this case measures 1.50 max, 0.31 mean (round-to-nearest:
-# 1.04 here, but twice the stochastic error on long painting sessions): the bound documents it.
-BF16_DELTA_E = 2.0
+# FP32 storage vs the double oracle after a stroke sequence: per-value error of K, S, V
+# relative to max(|value|, 1), and CIEDE2000 of the composed canvas
+F32_REL_TOL = 1e-4
+F32_DELTA_E = 0.05
+# 16-bit storage (FP32 arithmetic) vs the double oracle: CIEDE2000 of the composed canvas
+F16_DELTA_E = 0.5
+BF16_DELTA_E = 0.5
 
 
 def _gpu_replay(pg, fx, name, storage="f64"):
@@ -144,7 +144,14 @@ def test_hand_single_stamp_empty_canvas(pg):
     assert V.sum() == b.getFootprint().sum()
 
 
-@pytest.mark.parametrize("storage", ["f32", "f16", "bf16"])
+# BF16 keeps 8 significant bits; a pixel re-blended by every stamp over it drifts. With the
+# stochastic rounding of 16-bit stores this case measures about 1.5 max, 0.3 mean: above the
+# 0.5 target, recorded as an expected failure.
+BF16_XFAIL = pytest.mark.xfail(strict=True, reason="BF16 storage misses dE < 0.5 on painting "
+                                                   "(measured about 1.5 max)")
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16", pytest.param("bf16", marks=BF16_XFAIL)])
 def test_reduced_precision_vs_oracle(pg, oracle, storage):
     rng = np.random.default_rng(41)
     session = _random_session(rng, 80, 100, 8, 3.0, 20.0, 40)
@@ -229,3 +236,35 @@ def test_host_setup_matches_oracle(pg, oracle):
         ob = oracle.brush(r, fp)
         assert b.info() == ob.info()
         assert np.array_equal(b.getFootprint(), ob.footprint()), r
+
+
+def test_f32_config0_full_vs_oracle(pg, oracle):
+    """The plain workload in full -- 1024 x 768 FP32 canvas, 200 Catmull-Rom strokes, r U[8,32],
+    spacing 0.25 r, rates 0.1 / 0.05, snapshot on -- against the double oracle: K, S, V within
+    F32_REL_TOL and the composite within F32_DELTA_E."""
+    rows, cols = 768, 1024
+    strokes = workloads.strokes(cols, rows, 200, seed=3)
+    fp = workloads.footprint_image(seed=7)
+    r0 = workloads.substrate(rows, cols, seed=5)
+    c = pg.Canvas(rows, cols, "f32")
+    c.setBackground(r0)
+    b = pg.FootprintBrush(strokes[0].radius, fp)
+    b.setPickupRate(0.05)
+    b.setDepositionRate(0.1)
+    n = workloads.paint_config0(c, b, strokes)
+    oc = oracle.canvas(rows, cols)
+    oc.set("R0", r0)
+    ob = oracle.brush(strokes[0].radius, fp)
+    ob.set_rates(0.05, 0.1)
+    no = 0
+    for s in strokes:
+        ob.set_radius(s.radius)
+        ob.dip(s.K, s.S)
+        no += ob.paint_stroke(oc, s.path, s.spacing)
+    assert n == no and n > 100000
+    errs = {}
+    for p in ("K", "S", "V"):
+        g, w = c.download(p), oc.get(p)
+        errs[p] = float((np.abs(g - w) / np.maximum(np.abs(w), 1.0)).max())
+    de_max, de_mean = oracle.delta_e(pg.Renderer().compose(c).download(), oc.compose())
+    assert max(errs.values()) <= F32_REL_TOL and de_max <= F32_DELTA_E, (errs, de_max, de_mean)

@@ -15,10 +15,12 @@ pytestmark = pytest.mark.gpu
 F32_REL_TOL = 1e-3   # per-value relative error of K, S, V after a stroke session (FP32)
 F32_DELTA_E = 0.05   # CIEDE2000 of the composed canvas, FP32 storage vs the double oracle
 F16_DELTA_E = 0.5    # the same, FP16 storage
+BF16_DELTA_E = 0.5   # the same, BF16 storage: missed (below)
 # BF16 keeps 8 significant bits of K and S, and the smudge re-blends a pixel at every step that
 # covers it (about 2r steps per stroke); with stochastic rounding this session measures
-# 1.5-2.2 max (mean 0.13) depending on the rounding bits: the bound documents it
-BF16_DELTA_E = 3.0
+# 1.5-2.2 max (mean 0.13) depending on the rounding bits: an expected failure
+BF16_XFAIL = pytest.mark.xfail(strict=True, reason="BF16 storage misses dE < 0.5 under the "
+                                                   "smudge (measured 1.5-2.2 max)")
 
 
 def _gpu_run(pg, storage, rows, cols, tex, session, smudge=True, scale=1.0, r0=0.9):
@@ -113,7 +115,7 @@ def test_radius_change_resets_smudge(pg, oracle):
     assert m.shape == (60, 60) and not m.any()
 
 
-@pytest.mark.parametrize("storage", ["f32", "f16", "bf16"])
+@pytest.mark.parametrize("storage", ["f32", "f16", pytest.param("bf16", marks=BF16_XFAIL)])
 def test_reduced_precision_vs_oracle(pg, oracle, storage):
     rng = np.random.default_rng(55)
     rows, cols = 80, 100

@@ -167,3 +167,16 @@ def test_ciede2000_sanity(oracle):
     # published CIEDE2000 test pair (Sharma, Wu, Dalal 2005, pair 1): 2.0425
     d = oracle.ciede2000(np.array([50.0, 2.6772, -79.7751]), np.array([50.0, 0.0, -82.7485]))
     assert abs(d - 2.0425) < 1e-4
+
+
+def test_planar_f32_composite_in_double_equals_interleaved(oracle):
+    """The planar float32 composite kept in double (the reference the precision figures are
+    measured against) equals the interleaved double composite of the same values."""
+    from painty_gb300 import workloads
+    K, S, V, R0 = workloads.composite_stack(23, 31, layers=5, seed=3)
+    got = oracle.compose_layers_f32_planar_f64(K, S, V, R0, threads=3)
+    il = lambda a: np.ascontiguousarray(np.moveaxis(a, 0, -1).reshape(-1, 3), dtype=np.float64)
+    want = oracle.compose_layers(np.stack([il(K[l]) for l in range(5)]),
+                                 np.stack([il(S[l]) for l in range(5)]),
+                                 V.reshape(5, -1).astype(np.float64), il(R0))
+    assert np.array_equal(got.reshape(-1, 3), want)

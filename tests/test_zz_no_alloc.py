@@ -1,11 +1,12 @@
 """painty_stamps_f32_noalloc: stamping for callers that cannot allocate device memory (GPU).
 
 Some callers cannot call cudaMalloc -- a plugin whose host application hands out fixed
-device buffers, a real-time loop that must not stall on an allocation, code running while a
-CUDA graph is being captured. This entry point takes every buffer from the caller and keeps
-its only scratch in a fixed array inside the library. This test calls it through the C ABI
-on buffers the test allocates itself, twice in a row, and checks the canvas and pickup map
-against the allocating entry point (painty_stamps) on the same inputs.
+device buffers, or a real-time loop that must not stall on an allocation. This entry point
+takes every buffer from the caller and keeps its only scratch in a fixed array inside the
+library. This test calls it through the C ABI on buffers the test allocates itself, twice in a
+row, and checks every plane it writes: the canvas and the pickup map against the allocating
+entry point (painty_stamps) on the same inputs, and the caller's snapshot planes against the
+double oracle's snapshot buffer.
 
 Kept in its own file, collected last, so a run that stops at its first failure has already
 run every other test.
@@ -17,10 +18,9 @@ import numpy as np
 import pytest
 
 from painty_gb300 import workloads
+from test_gpu_stamps import F32_REL_TOL
 
 pytestmark = pytest.mark.gpu
-
-F32_REL_TOL = 2e-3  # the stamp tests' FP32 tolerance (relative, floor 1.0)
 
 _FP = C.POINTER(C.c_float)
 
@@ -47,18 +47,25 @@ def _records(torch, st):
     return torch.from_numpy(rec).cuda()
 
 
-def _close(got, want):
-    rel = np.abs(got.astype(np.float64) - want) / np.maximum(np.abs(want), 1.0)
-    return rel.max() <= F32_REL_TOL
+def _rel(got, want):
+    """Largest error relative to max(|want|, 1), the stamp tests' FP32 measure."""
+    return float((np.abs(got.astype(np.float64) - want) / np.maximum(np.abs(want), 1.0)).max())
 
 
-@pytest.mark.parametrize("radius", [12.0, 85.0])
-def test_noalloc_matches_allocating_entry(pg, radius):
-    torch = pytest.importorskip("torch")
-    lib = pg._lib
-    fn = lib.painty_stamps_f32_noalloc
+def _fn(pg):
+    fn = pg._lib.painty_stamps_f32_noalloc
     fn.argtypes = [C.POINTER(StampBuffers), C.c_void_p]
     fn.restype = C.c_int
+    return fn
+
+
+# radius 12: a small stamp; radius 90: footprint side 255 and map side 256, the largest the
+# fixed scratch array accepts
+@pytest.mark.parametrize("radius", [12.0, 90.0])
+def test_noalloc_matches_allocating_entry(pg, oracle, radius):
+    torch = pytest.importorskip("torch")
+    lib = pg._lib
+    fn = _fn(pg)
 
     rows, cols, pitch = 150, 190, 200
     rng = np.random.default_rng(int(radius))
@@ -77,6 +84,15 @@ def test_noalloc_matches_allocating_entry(pg, radius):
     brush.setDepositionRate(0.1)
     brush.dip(paint)
     r_eff, F, S = brush.info()
+    if radius == 90.0:
+        assert (F, S) == (255, 256)
+    # the double oracle on the same values, for the snapshot buffer
+    oc = oracle.canvas(rows, cols)
+    for k, v in wet.items():
+        oc.set(k, v.astype(np.float64))
+    ob = oracle.brush(radius, fp_img)
+    ob.set_rates(0.05, 0.1)
+    ob.dip(*paint)
 
     # caller-owned device buffers for the allocation-free entry point
     def planes(n, h, w):
@@ -105,34 +121,49 @@ def test_noalloc_matches_allocating_entry(pg, radius):
     buf.footprint_side, buf.map_side = F, S
     buf.radius, buf.pickup_rate, buf.deposition_rate, buf.capacity = r_eff, 0.05, 0.1, 1.0
 
+    def host(ts, h, w):
+        return np.stack([t[:h, :w].cpu().numpy() for t in ts], axis=-1)
+
     for call in range(2):  # two calls in a row; state carries over as with painty's brush
         st = np.stack([rng.uniform(-10, cols + 10, 12), rng.uniform(-10, rows + 10, 12),
                        rng.uniform(-3.2, 3.2, 12)], axis=1)
         st[0, :2] = [0.5, 0.25]
         brush.stamps(st, canvas)
+        ob.stamps(oc, st)
         rec = _records(torch, st)
         buf.stamps = C.cast(C.c_void_p(rec.data_ptr()), C.POINTER(C.c_double))
         buf.n = len(st)
         status = fn(C.byref(buf), None)
         assert status == 0, lib.painty_last_error().decode()
         torch.cuda.synchronize()
-        got_K = np.stack([t[:, :cols].cpu().numpy() for t in cK], axis=-1)
-        got_S = np.stack([t[:, :cols].cpu().numpy() for t in cS], axis=-1)
-        got_V = cV[:, :cols].cpu().numpy()
-        assert _close(got_K, canvas.download("K")), call
-        assert _close(got_S, canvas.download("S")), call
-        assert _close(got_V, canvas.download("V")), call
-        pick_V = pV.cpu().numpy()
-        assert _close(pick_V, brush.getPickupMap("V")), call
+        errs = {
+            "canvas K": _rel(host(cK, rows, cols), canvas.download("K")),
+            "canvas S": _rel(host(cS, rows, cols), canvas.download("S")),
+            "canvas V": _rel(cV[:, :cols].cpu().numpy(), canvas.download("V")),
+            "pickup K": _rel(host(pK, S, S), brush.getPickupMap("K")),
+            "pickup S": _rel(host(pS, S, S), brush.getPickupMap("S")),
+            "pickup V": _rel(pV.cpu().numpy(), brush.getPickupMap("V")),
+            "snapshot K": _rel(host(sK, rows, cols), ob.snapshot("K")),
+            "snapshot S": _rel(host(sS, rows, cols), ob.snapshot("S")),
+            "snapshot V": _rel(sV[:, :cols].cpu().numpy(), ob.snapshot("V")),
+        }
+        assert max(errs.values()) <= F32_REL_TOL, (call, errs)
 
 
-def test_noalloc_rejects_oversized_map(pg):
+def test_noalloc_rejects_bad_sizes_and_values(pg):
     lib = pg._lib
-    fn = lib.painty_stamps_f32_noalloc
-    fn.argtypes = [C.POINTER(StampBuffers), C.c_void_p]
-    fn.restype = C.c_int
-    buf = StampBuffers()
-    buf.rows, buf.cols, buf.pitch = 10, 10, 10
-    buf.footprint_side, buf.map_side = 257, 258
-    assert fn(C.byref(buf), None) == 1  # PAINTY_ERR_INVALID_ARGUMENT
-    assert "257" in lib.painty_last_error().decode()
+    fn = _fn(pg)
+
+    def call(F, S, radius=10.0, rate=0.05):
+        buf = StampBuffers()
+        buf.rows, buf.cols, buf.pitch = 10, 10, 10
+        buf.footprint_side, buf.map_side = F, S
+        buf.radius, buf.pickup_rate, buf.deposition_rate, buf.capacity = radius, rate, 0.1, 1.0
+        return fn(C.byref(buf), None), lib.painty_last_error().decode()
+
+    status, msg = call(257, 257)  # the first map side beyond the scratch array
+    assert status == 1 and "256" in msg, msg  # PAINTY_ERR_INVALID_ARGUMENT
+    assert call(255, 257)[0] == 1
+    assert call(31, 32, radius=float("nan"))[0] == 1
+    assert call(31, 32, radius=-1.0)[0] == 1
+    assert call(31, 32, rate=float("inf"))[0] == 1
