@@ -337,6 +337,13 @@ void upload_planes(void* const* planes, int nch, DevType dt, int32_t rows, int32
 void download_planes(const void* const* planes, int nch, DevType dt, int32_t rows,
                      int32_t cols, int64_t pitch, void* host, painty_host_format fmt,
                      cudaStream_t st, int64_t estride) {
+  download_planes_async(planes, nch, dt, rows, cols, pitch, host, fmt, st, estride);
+  PG_CUDA(cudaStreamSynchronize(st));
+}
+
+void download_planes_async(const void* const* planes, int nch, DevType dt, int32_t rows,
+                           int32_t cols, int64_t pitch, void* host, painty_host_format fmt,
+                           cudaStream_t st, int64_t estride) {
   PG_REQUIRE(host != nullptr, "host buffer is null");
   PG_REQUIRE(fmt >= PAINTY_HOST_F64_INTERLEAVED && fmt <= PAINTY_HOST_F32_PLANAR,
              "unknown host format");
@@ -349,7 +356,6 @@ void download_planes(const void* const* planes, int nch, DevType dt, int32_t row
         PG_CUDA(cudaMemcpy2DAsync(static_cast<char*>(host) + c * n * hes, cols * hes,
                                   planes[c], pitch * hes, cols * hes, rows,
                                   cudaMemcpyDeviceToHost, st));
-      PG_CUDA(cudaStreamSynchronize(st));
       return;
     }
   }
@@ -366,7 +372,6 @@ void download_planes(const void* const* planes, int nch, DevType dt, int32_t row
                          estride, st);
   PG_CUDA(cudaMemcpyAsync(host, staging, n * nch * hes, cudaMemcpyDeviceToHost, st));
   PG_CUDA(cudaFreeAsync(staging, st));
-  PG_CUDA(cudaStreamSynchronize(st));
 }
 
 void fill_planes(void* const* planes, int nch, DevType dt, int64_t elems, const double* v,

@@ -181,6 +181,11 @@ void upload_planes(void* const* planes, int nch, DevType dt, int32_t rows, int32
 void download_planes(const void* const* planes, int nch, DevType dt, int32_t rows,
                      int32_t cols, int64_t pitch, void* host, painty_host_format fmt,
                      cudaStream_t st, int64_t estride = 1);
+// The same without waiting: the copy is ordered on `st` (the host buffer is written once the
+// stream passes it; pinned host memory keeps the call from blocking).
+void download_planes_async(const void* const* planes, int nch, DevType dt, int32_t rows,
+                           int32_t cols, int64_t pitch, void* host, painty_host_format fmt,
+                           cudaStream_t st, int64_t estride = 1);
 void fill_planes(void* const* planes, int nch, DevType dt, int64_t elems, const double* values,
                  cudaStream_t st, int64_t estride = 1);
 // Copies a layer's 7 planes into another of the same size and storage (any layouts).
@@ -189,9 +194,19 @@ void copy_planes_async(void* const* dst, const void* const* src, int nch, size_t
                        cudaStream_t st);
 
 // Batched painting (stamp.cu): painty_paint_batch after argument checks.
+// BatchOptions (NULL: the defaults): max_cluster caps the CTAs per canvas the cost model may
+// choose (1, 2, 4 or 8). With status_host set (pinned host memory) the call returns right
+// after the launch: the kernel's status word is copied there in stream order, temporaries
+// are freed in stream order, and the caller checks the word once the stream has passed the
+// launch (nonzero: the kernel reported an internal error).
+struct BatchOptions {
+  int max_cluster = 8;
+  unsigned* status_host = nullptr;
+};
 void paint_batch(painty_canvas* const* canvases, painty_brush* const* brushes, int32_t nc,
                  const painty_stroke_desc* strokes, int64_t ns, const double* points,
-                 int64_t npoints, int64_t* stamps_out, cudaStream_t st);
+                 int64_t npoints, int64_t* stamps_out, cudaStream_t st,
+                 const BatchOptions* opt = nullptr);
 // Stamps painty's paintStroke puts on a path at the given chord spacing (host count).
 int64_t stroke_stamp_count(const double* path, int32_t n, double spacing);
 

@@ -559,25 +559,26 @@ __device__ __forceinline__ void build_refresh(const StampParams& sp, const int* 
   if (lane == 0) rl->pre[0] = 0;
 }
 
-// All threads of a CTA: copy its share (of `csize`) of the listed ring pixels canvas ->
-// snapshot (7 planes), two pixels per thread in flight. `skip` (may be NULL): the current
-// stamp's cell map, its box starting at canvas (x0, y0); pixels it paints (cell >= 0) are
-// copied by their painter instead, and the rest of the list is not touched by the stamp, so
-// the copy runs beside its painting.
+// All threads of a CTA: copy its share (of the cluster's 2^lg_csize CTAs) of the listed ring
+// pixels canvas -> snapshot (7 planes), two pixels per thread in flight. `rt` is the thread's
+// index counted from the CTA's last thread: the copy falls on the high warps, painting on the
+// low ones. `skip` (may be NULL): the current stamp's cell map, its box starting at canvas
+// (x0, y0); pixels it paints (cell >= 0) are copied by their painter instead, and the rest of
+// the list is not touched by the stamp, so the copy runs beside its painting.
 template <bool CG, bool PK, class TK, class TV>
 __device__ __forceinline__ void refresh_ring(const StampArgs<TK, TV>& a, const RefreshList& rl,
-                                             int tid, int T, int crank, int csize,
+                                             int rt, int T, int crank, int lg_csize,
                                              const int* skip, int x0, int y0) {
-  const int all = rl.pre[kRefreshRects];
-  const int first = static_cast<int>(static_cast<int64_t>(all) * crank / csize);
-  const int total = static_cast<int>(static_cast<int64_t>(all) * (crank + 1) / csize);
+  const int all = rl.pre[kRefreshRects];  // < 2^22 pixels: the products below fit 32 bits
+  const int first = (all * crank) >> lg_csize;
+  const int total = (all * (crank + 1)) >> lg_csize;
   const int F = a.F;
   constexpr int U = 2;
   for (int base = first; base < total; base += U * T) {
     int64_t off[U];
 #pragma unroll
     for (int u = 0; u < U; u++) {
-      const int idx = base + u * T + tid;
+      const int idx = base + u * T + rt;
       off[u] = -1;
       if (idx < total) {
         int r = 0;  // the rectangle holding idx: pre[r] <= idx < pre[r + 1] (binary search)
@@ -667,9 +668,9 @@ template <class TK, class TV, class M>
 __device__ __forceinline__ void classify_disc(const StampArgs<TK, TV>& a, const StampParams& sp,
                                               const int* xs, const int* ys, const M* fps,
                                               const uint32_t* disc, int ndisc, int* cellmap,
-                                              int tid, int T) {
+                                              int rt, int T) {
   const int F = a.F;
-  for (int i = tid; i < ndisc; i += T) {
+  for (int i = rt; i < ndisc; i += T) {  // rt: counted from the last thread (high warps)
     const uint32_t e = disc[i];
     const int row = static_cast<int>(e >> 16), col = static_cast<int>(e & 0xffffu);
     M fp;
@@ -684,15 +685,15 @@ __device__ __forceinline__ void classify_disc(const StampArgs<TK, TV>& a, const 
 // these values).
 template <bool PS, bool CG, bool PK, class TK, class TV, class M>
 __device__ __forceinline__ void paint_disc(const StampArgs<TK, TV>& a, const int* xs, const int* ys,
-                                        const M* fps, M* pbase, const uint32_t* disc, int ndisc,
-                                        const int* cellmap, uint32_t seed, int tid, int T,
-                                        int crank, int csize, const StampParams* nxt) {
+                                        const M* fps, M* pbase, const uint32_t* disc, int first,
+                                        int last, const int* cellmap, uint32_t seed, int tid,
+                                        int T, const StampParams* nxt) {
   const int F = a.F, S = a.S;
   const int cells = S * S;
   const int pitch32 = static_cast<int>(a.pitch);  // planes hold fewer than 2^31 elements
-  const int first = ndisc * crank / csize, last = ndisc * (crank + 1) / csize;
   const bool snapping = nxt != nullptr && a.use_snapshot;
   // canvas pixel (x, y) lies in the next stamp's ring: its grown box minus the box's interior
+  // (this CTA paints disc entries [first, last))
   auto in_ring = [&](int x, int y) -> bool {
     if (!snapping) return false;
     const bool g = x >= nxt->tla[0] && x <= nxt->bra[0] && y >= nxt->tla[1] && y <= nxt->bra[1];
@@ -813,13 +814,14 @@ __device__ __noinline__ int paint_waves(const StampArgs<TK, TV>& a, const StampP
 // Per-stamp setup of a stamp: canvas columns / rows of the box (double, as the reference),
 // duplicate flags reset, the ring rectangles (warp 0) given the previous stamp's box and
 // grown box `prev`. Returns whether this thread saw an edge duplicate.
-template <class TK, class TV>
+template <class TK, class TV, class Prev>
 __device__ __forceinline__ int setup_stamp(const StampArgs<TK, TV>& a, const StampParams& sp,
-                                           const int* prev, int* xs, int* ys, uint16_t* done_c,
-                                           uint16_t* done_r, RefreshList* rl, int tid, int T) {
+                                           const Prev& prev_of, int* xs, int* ys,
+                                           uint16_t* done_c, uint16_t* done_r, RefreshList* rl,
+                                           int rt, int T) {
   const int F = a.F;
   int dup = 0;
-  for (int i = tid; i < F; i += T) {
+  for (int i = rt; i < F; i += T) {  // rt: counted from the last thread (high warps)
     const int x = static_cast<int>(__dadd_rn(static_cast<double>(i - a.wr), sp.cx));
     const int y = static_cast<int>(__dadd_rn(static_cast<double>(i - a.wr), sp.cy));
     xs[i] = x;
@@ -832,7 +834,11 @@ __device__ __forceinline__ int setup_stamp(const StampArgs<TK, TV>& a, const Sta
       dup |= (x == x1) | (y == y1);
     }
   }
-  if (a.use_snapshot && (tid >> 5) == 0) build_refresh(sp, prev, tid & 31, rl);
+  if (a.use_snapshot && (rt >> 5) == 0) {  // the last warp
+    int prev[8];
+    prev_of(prev);
+    build_refresh(sp, prev, 31 - (rt & 31), rl);
+  }
   return dup;
 }
 
@@ -880,30 +886,41 @@ __device__ __forceinline__ void run_stroke(const StampArgs<TK, TV>& a, const Src
       __syncthreads();
   };
   if (tid == 0 && (PS || !CG) && csize > 1) atomicOr(a.status, kStatusWaveCap);  // host bug
-  auto par = [&](int64_t k) -> StampParams& { return sparams[static_cast<int>(k % kParamRing)]; };
-  auto xs_of = [&](int64_t k) { return xs_b + static_cast<int>(k % kStampBufs) * F; };
-  auto ys_of = [&](int64_t k) { return ys_b + static_cast<int>(k % kStampBufs) * F; };
-  auto dc_of = [&](int64_t k) { return dc_b + static_cast<int>(k % kStampBufs) * F; };
-  auto dr_of = [&](int64_t k) { return dr_b + static_cast<int>(k % kStampBufs) * F; };
-  auto cm_of = [&](int64_t k) { return cm_b + static_cast<int>(k & 1) * npix; };
-  auto rl_of = [&](int64_t k) { return &sh->rl[k & 1]; };
+  // Work split inside the CTA: painting takes disc entries from the first thread up; the ring
+  // copy, classification and per-stamp setup count threads from the last one (rt), so they
+  // fall on the warps that paint least.
+  const int rt = T - 1 - tid;
+  const int lg_csize = 31 - __clz(csize);  // cluster sizes are powers of two
+  const int ns = static_cast<int>(nstamps);  // < 2^31 stamps per launch (checked by the host)
+  const int dfirst = (ndisc * crank) >> lg_csize, dlast = (ndisc * (crank + 1)) >> lg_csize;
+  static_assert((kParamRing & (kParamRing - 1)) == 0, "parameter ring size is a power of two");
+  auto par = [&](int k) -> StampParams& { return sparams[k & (kParamRing - 1)]; };
+  // stamp k's per-stamp arrays sit in slot k mod 3 (columns, rows, duplicate flags) and its
+  // cell map and ring list in slot k mod 2
+  auto xs_at = [&](int slot) { return xs_b + slot * F; };
+  auto ys_at = [&](int slot) { return ys_b + slot * F; };
+  auto dc_at = [&](int slot) { return dc_b + slot * F; };
+  auto dr_at = [&](int slot) { return dr_b + slot * F; };
+  auto cm_of = [&](int k) { return cm_b + (k & 1) * npix; };
+  auto rl_of = [&](int k) { return &sh->rl[k & 1]; };
+  auto next_slot = [](int slot) { return slot == kStampBufs - 1 ? 0 : slot + 1; };
   // rectangles of stamp k - 1 (the brush's ring state before the first stamp)
-  auto prev_of = [&](int64_t k, int* out) {
+  auto prev_of = [&](int k, int* out) {
     if (k == 0)
       for (int i = 0; i < 8; i++) out[i] = sh->prev[i];
     else
       stamp_rects(par(k - 1), out);
   };
-  auto derive_chunk = [&](int64_t k0) {  // parameters of stamps k0 .. k0 + 31 (threads < 32)
-    const int64_t j = k0 + tid;
-    if (tid < kParamChunk && j < nstamps)
+  // parameters of stamps k0 .. k0 + 31 (one warp in the middle of the CTA)
+  const int dtid = tid - (T >> 1);
+  auto derive_chunk = [&](int k0) {
+    const int j = k0 + dtid;
+    if (dtid >= 0 && dtid < kParamChunk && j < ns)
       par(j) = derive_params(src.get(j), a.wr, a.radius, a.rows, a.cols);
   };
-  auto setup = [&](int64_t k) -> int {
-    int prev[8];
-    prev_of(k, prev);
-    return setup_stamp(a, par(k), prev, xs_of(k), ys_of(k), dc_of(k), dr_of(k), rl_of(k), tid,
-                       T);
+  auto setup = [&](int k, int slot) -> int {
+    return setup_stamp(a, par(k), [&](int* out) { prev_of(k, out); }, xs_at(slot), ys_at(slot),
+                       dc_at(slot), dr_at(slot), rl_of(k), rt, T);
   };
 
   // launch prologue: footprint and pickup map staged, owner table reset, ring state
@@ -977,52 +994,54 @@ __device__ __forceinline__ void run_stroke(const StampArgs<TK, TV>& a, const Src
   csync();  // parameters, disc list; a cleared pickup map is visible to the whole cluster
   // stamps 0 and 1 set up, stamp 0's ring refreshed and its disc classified
   int dup0 = 0, dup1 = 0;
-  if (nstamps > 0) dup0 = __syncthreads_or(setup(0));
-  if (nstamps > 1) dup1 = __syncthreads_or(setup(1));
-  if (nstamps > 0) {
+  int s0 = 0;  // slot of the stamp being painted (k mod 3)
+  if (ns > 0) dup0 = __syncthreads_or(setup(0, 0));
+  if (ns > 1) dup1 = __syncthreads_or(setup(1, 1));
+  if (ns > 0) {
     if (a.use_snapshot)
-      refresh_ring<CG, PK>(a, *rl_of(0), tid, T, crank, csize, nullptr, 0, 0);
+      refresh_ring<CG, PK>(a, *rl_of(0), rt, T, crank, lg_csize, nullptr, 0, 0);
     if (!dup0 && ndisc > 0)
-      classify_disc(a, par(0), xs_of(0), ys_of(0), fps, disc, ndisc, cm_of(0), tid, T);
+      classify_disc(a, par(0), xs_at(0), ys_at(0), fps, disc, ndisc, cm_of(0), rt, T);
   }
   csync();
   int epoch = 0;
-  for (int64_t k = 0; k < nstamps; k++) {
+  for (int k = 0; k < ns; k++) {
     const StampParams& sp = par(k);
-    const bool has_next = k + 1 < nstamps;
+    const bool has_next = k + 1 < ns;
+    const int s1 = next_slot(s0), s2 = next_slot(s1);
     const uint32_t seed = hash32(sh->seed0 + static_cast<uint32_t>(k));
     if (!dup0 && ndisc > 0) {
-      paint_disc<PS, CG, PK, TK, TV, M>(a, xs_of(k), ys_of(k), fps, pbase, disc, ndisc, cm_of(k),
-                                        seed, tid, T, crank, csize,
+      paint_disc<PS, CG, PK, TK, TV, M>(a, xs_at(s0), ys_at(s0), fps, pbase, disc, dfirst, dlast,
+                                        cm_of(k), seed, tid, T,
                                         has_next ? &par(k + 1) : nullptr);
       if (has_next && a.use_snapshot)
-        refresh_ring<CG, PK>(a, *rl_of(k + 1), tid, T, crank, csize, cm_of(k), xs_of(k)[0],
-                             ys_of(k)[0]);
+        refresh_ring<CG, PK>(a, *rl_of(k + 1), rt, T, crank, lg_csize, cm_of(k), xs_at(s0)[0],
+                             ys_at(s0)[0]);
     } else {
       if (crank == 0)  // edge duplicates: the first CTA alone, in waves
-        epoch = paint_waves<PS, CG, PK, TK, TV, M>(a, sp, xs_of(k), ys_of(k), dc_of(k), dr_of(k),
-                                                   fps, pbase, own, epoch, seed);
+        epoch = paint_waves<PS, CG, PK, TK, TV, M>(a, sp, xs_at(s0), ys_at(s0), dc_at(s0),
+                                                   dr_at(s0), fps, pbase, own, epoch, seed);
       csync();
       if (has_next && a.use_snapshot)
-        refresh_ring<CG, PK>(a, *rl_of(k + 1), tid, T, crank, csize, nullptr, 0, 0);
+        refresh_ring<CG, PK>(a, *rl_of(k + 1), rt, T, crank, lg_csize, nullptr, 0, 0);
     }
     if (has_next && !dup1 && ndisc > 0)
-      classify_disc(a, par(k + 1), xs_of(k + 1), ys_of(k + 1), fps, disc, ndisc, cm_of(k + 1),
-                    tid, T);
-    if ((k + 3) % kParamChunk == 0) derive_chunk(k + 3);  // read from phase k + 1 on
+      classify_disc(a, par(k + 1), xs_at(s1), ys_at(s1), fps, disc, ndisc, cm_of(k + 1), rt, T);
+    if (((k + 3) & (kParamChunk - 1)) == 0) derive_chunk(k + 3);  // read from phase k + 1 on
     int nd = 0;
-    if (k + 2 < nstamps) nd = setup(k + 2);
+    if (k + 2 < ns) nd = setup(k + 2, s2);
     nd = __syncthreads_or(nd);
     if (csize > 1) cluster_barrier();  // this phase's writes before the next phase's reads
     dup0 = dup1;
     dup1 = nd;
+    s0 = s1;
   }
   // epilogue: the brush keeps its pickup map and the ring state
   if (tid == 0 && crank == 0 && a.stamp_count)
-    *a.stamp_count = sh->seed0 + static_cast<unsigned>(nstamps);
+    *a.stamp_count = sh->seed0 + static_cast<unsigned>(ns);
   if (tid == 0 && crank == 0 && a.ring && a.use_snapshot) {
-    if (nstamps > 0)
-      stamp_rects(par(nstamps - 1), a.ring);
+    if (ns > 0)
+      stamp_rects(par(ns - 1), a.ring);
     else
       for (int i = 0; i < 8; i++) a.ring[i] = sh->prev[i];
   }
@@ -1627,6 +1646,7 @@ void run_stamps(painty_canvas* c, painty_brush* b, const std::vector<StampRec>& 
                 cudaStream_t st) {
   PG_REQUIRE(c && b, "null handle");
   if (recs.empty()) return;
+  PG_REQUIRE(recs.size() < static_cast<size_t>(INT_MAX), "at most 2^31 - 1 stamps per call");
   PG_REQUIRE(b->sizeMap > 0 && b->F > 0, "brush radius gives an empty footprint");
   PG_REQUIRE(static_cast<int64_t>(b->F) * b->F <= int64_t(kMaxPixelsPerThread) * kStampThreads,
              "brush radius above the supported maximum (footprint side 256)");
@@ -1729,7 +1749,8 @@ double batch_makespan(const std::vector<double>& N, const std::vector<double>& P
 template <class TK, class TV>
 void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushes, int32_t nc,
                      const painty_stroke_desc* strokes, int64_t ns, const double* points,
-                     int64_t npoints, int64_t* stamps_out, cudaStream_t st) {
+                     int64_t npoints, int64_t* stamps_out, cudaStream_t st,
+                     const BatchOptions& opt) {
   using M = typename MathOf<TK>::type;
   const bool f64 = std::is_same<M, double>::value;
   const size_t msz = sizeof(M);
@@ -1788,6 +1809,7 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
       smax = std::max(smax, b->sizeMap);
       // stamp count (paintStroke's loop bounds) and the load estimates
       const int64_t n = stroke_stamp_count(points + 2 * sk.first_point, sk.npoints, sk.spacing);
+      PG_REQUIRE(n < INT_MAX, "at most 2^31 - 1 stamps per stroke");
       total_stamps += n;
       loadN[c] += static_cast<double>(n);
       loadP[c] += static_cast<double>(n) * di->second;
@@ -1866,7 +1888,7 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   int cl = 1, slots = 0;
   double best = 1e300;
   for (int c2 : {1, 2, 4, 8}) {
-    if (forced && c2 != forced) continue;
+    if (forced ? c2 != forced : c2 > opt.max_cluster) continue;
     plan_all(c2);
     const int fits = max_clusters(kern, c2, std::max<size_t>(dyn, 16));
     const int sl = std::min(fits, nc);
@@ -1926,11 +1948,12 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   count_launch();
   PG_CUDA(cudaGetLastError());
   unsigned status = 0;
-  PG_CUDA(cudaMemcpyAsync(&status, a.status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+  PG_CUDA(cudaMemcpyAsync(opt.status_host ? opt.status_host : &status, a.status,
+                          sizeof(unsigned), cudaMemcpyDeviceToHost, st));
   for (void* d : {d_canvas, d_strokes, d_points, d_fp, d_order, d_scratch_p, d_scratch_o,
                   d_scratch_cm, d_counter})
     PG_CUDA(cudaFreeAsync(d, st));
-  PG_CUDA(cudaStreamSynchronize(st));
+  if (!opt.status_host) PG_CUDA(cudaStreamSynchronize(st));
   for (int32_t c = 0; c < nc; c++) {
     if (per[c].empty()) continue;
     painty_brush* b = brushes[c];
@@ -1957,7 +1980,12 @@ int64_t stroke_stamp_count(const double* p, int32_t npts, double spacing) {
 
 void paint_batch(painty_canvas* const* canvases, painty_brush* const* brushes, int32_t ncanvas,
                  const painty_stroke_desc* strokes, int64_t nstrokes, const double* points,
-                 int64_t npoints, int64_t* stamps_out, cudaStream_t st) {
+                 int64_t npoints, int64_t* stamps_out, cudaStream_t st,
+                 const BatchOptions* options) {
+  const BatchOptions opt = options ? *options : BatchOptions{};
+  PG_REQUIRE(opt.max_cluster == 1 || opt.max_cluster == 2 || opt.max_cluster == 4 ||
+               opt.max_cluster == 8,
+             "max_cluster must be 1, 2, 4 or 8");
   PG_REQUIRE(ncanvas > 0 && canvases && brushes, "no canvases");
   PG_REQUIRE(nstrokes >= 0 && (nstrokes == 0 || strokes), "strokes is null");
   PG_REQUIRE(npoints >= 0 && (npoints == 0 || points), "points is null");
@@ -1990,16 +2018,20 @@ void paint_batch(painty_canvas* const* canvases, painty_brush* const* brushes, i
   }
   switch (storage) {
     case PAINTY_STORAGE_F32:
-      run_batch_typed<float, float>(canvases, brushes, ncanvas, strokes, nstrokes, points, npoints, stamps_out, st);
+      run_batch_typed<float, float>(canvases, brushes, ncanvas, strokes, nstrokes, points,
+                                       npoints, stamps_out, st, opt);
       break;
     case PAINTY_STORAGE_F16:
-      run_batch_typed<__half, __half>(canvases, brushes, ncanvas, strokes, nstrokes, points, npoints, stamps_out, st);
+      run_batch_typed<__half, __half>(canvases, brushes, ncanvas, strokes, nstrokes, points,
+                                       npoints, stamps_out, st, opt);
       break;
     case PAINTY_STORAGE_BF16:
-      run_batch_typed<__nv_bfloat16, __half>(canvases, brushes, ncanvas, strokes, nstrokes, points, npoints, stamps_out, st);
+      run_batch_typed<__nv_bfloat16, __half>(canvases, brushes, ncanvas, strokes, nstrokes, points,
+                                       npoints, stamps_out, st, opt);
       break;
     case PAINTY_STORAGE_F64:
-      run_batch_typed<double, double>(canvases, brushes, ncanvas, strokes, nstrokes, points, npoints, stamps_out, st);
+      run_batch_typed<double, double>(canvases, brushes, ncanvas, strokes, nstrokes, points,
+                                       npoints, stamps_out, st, opt);
       break;
   }
 }
@@ -2322,7 +2354,7 @@ painty_status painty_stroke(painty_canvas* c, painty_brush* b, const double* pat
 painty_status painty_stamps_f32_noalloc(const painty_stamp_buffers_f32* b, void* stream) {
   return guard([&] {
     PG_REQUIRE(b != nullptr, "buffers is null");
-    PG_REQUIRE(b->n >= 0, "negative stamp count");
+    PG_REQUIRE(b->n >= 0 && b->n < INT_MAX, "stamp count must lie in [0, 2^31 - 1)");
     PG_REQUIRE(b->rows > 0 && b->cols > 0 && b->pitch >= b->cols, "bad canvas geometry");
     PG_REQUIRE(static_cast<int64_t>(b->rows) * b->pitch < (int64_t(1) << 31),
                "canvas too large for stamping (a plane holds 2^31 elements or more)");
