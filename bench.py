@@ -218,7 +218,11 @@ def run_serve_only(args):
     import painty_gb300 as pg
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    print(json.dumps(run_serve(pg, torch, args.serve_rate, args.serve_seconds)), flush=True)
+    if args.serve_sweep:
+        print(json.dumps(run_serving(pg, torch, full_rate=args.serve_rate,
+                                     full_s=args.serve_seconds)), flush=True)
+    else:
+        print(json.dumps(run_serve(pg, torch, args.serve_rate, args.serve_seconds)), flush=True)
 
 
 def run_stamps_only(args):
@@ -499,7 +503,7 @@ def run_ours(args):
                                rank, ws) for s_ in ("f32", "f16")}
     if rank == 0 and not args.no_stamps:
         stamps = run_stamps_config0(pg, torch, cpu=not args.no_cpu)
-        serve = run_serve(pg, torch, args.serve_rate, args.serve_seconds)
+        serve = run_serving(pg, torch, full_rate=args.serve_rate, full_s=args.serve_seconds)
         prec = run_precision(pg, torch, (Kh, Sh, Vh, R0h))
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(Kh, Sh, Vh, R0h)
@@ -669,22 +673,19 @@ def run_batch(pg, torch, storage: str, ncanvas: int, max_strokes, rank: int = 0,
                       "r logU[4,64], spacing 0.25 r; one persistent launch"}
 
 
-def run_serve(pg, torch, rate: float, seconds: float, seed: int = 4, budget_gb: float = 120.0,
-              storage: str = "f16"):
-    """Serving: Poisson arrivals at `rate` req/s for `seconds`; each request a canvas of side
-    log-uniform in [512, 4096] (aspect 1) with 1-500 strokes (geometric, mean 60) from the
-    plain case's generators; 30% continue an earlier canvas; FP16 state under the budget."""
-    import threading
-
+def serve_plan(rate: float, seconds: float, seed: int = 4):
+    """The serving workload: Poisson arrivals at `rate` req/s for `seconds`; each request a
+    canvas of side log-uniform in [512, 4096] (aspect 1) with 1-500 strokes (geometric, mean 60)
+    from the plain case's generators (r U[8,32], spacing 0.25 r, Dirichlet(0.3) paints); 30%
+    continue a canvas an earlier request created. Returns [(t, continue_index or -1, rows,
+    cols, strokes)]."""
     from painty_gb300 import workloads
 
     rng = np.random.default_rng(seed)
     PK, PS = workloads.pigments()
-    fp = workloads.footprint_image(seed=7)
-    substrate = rng.uniform(0.8, 0.95, (4096, 4096, 3)).astype(np.float32)
     n = max(1, int(rng.poisson(rate * seconds)))
     arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
-    plan = []  # (t, continue_index or -1, rows, cols, strokes)
+    plan = []
     for i in range(n):
         cont = -1
         if i > 0 and rng.random() < 0.30:
@@ -695,58 +696,155 @@ def run_serve(pg, torch, rate: float, seconds: float, seed: int = 4, budget_gb: 
         else:
             rows = cols = int(np.exp(rng.uniform(np.log(512), np.log(4096))))
         ns = min(500, int(rng.geometric(1.0 / 60.0)))
-        strokes = []
-        for _ in range(ns):
-            path = np.stack([rng.uniform(0, cols, 8), rng.uniform(0, rows, 8)], axis=1)
-            r = float(rng.uniform(8, 32))
-            w = rng.dirichlet(np.full(len(PK), 0.3))
-            k = (w / w.sum()) @ PK
-            s_ = (w / w.sum()) @ PS
-            strokes.append((path, r, 0.25 * r, k, s_))
+        paths = np.stack([rng.uniform(0, cols, (ns, 8)), rng.uniform(0, rows, (ns, 8))], axis=2)
+        radii = rng.uniform(8, 32, ns)
+        w = rng.dirichlet(np.full(len(PK), 0.3), ns)
+        K, S = w @ PK, w @ PS
+        strokes = [(paths[j], float(radii[j]), 0.25 * float(radii[j]), K[j], S[j])
+                   for j in range(ns)]
         plan.append((float(arrivals[i]), cont, rows, cols, strokes))
+    return plan
+
+
+class _PinnedPool:
+    """Pinned host buffers for request results, reused by size class, at most `cap` bytes
+    (beyond it a request gets pageable memory)."""
+
+    def __init__(self, torch, cap: int):
+        self.torch, self.cap, self.total = torch, cap, 0
+        self.free = {}
+        import threading
+        self.lock = threading.Lock()
+
+    def take(self, rows: int, cols: int):
+        n = rows * cols * 3
+        cls = 1 << max(20, (n - 1).bit_length())  # floats, power-of-two classes
+        with self.lock:
+            lst = self.free.get(cls)
+            if lst:
+                t = lst.pop()
+            elif self.total + 4 * cls <= self.cap:
+                t = self.torch.empty(cls, dtype=self.torch.float32, pin_memory=True)
+                self.total += 4 * cls
+            else:
+                return None, np.empty((rows, cols, 3), dtype=np.float32)
+        return (cls, t), t[:n].numpy().reshape(rows, cols, 3)
+
+    def give(self, key):
+        if key is not None:
+            with self.lock:
+                self.free.setdefault(key[0], []).append(key[1])
+
+
+def run_serve(pg, torch, rate: float, seconds: float, seed: int = 4, budget_gb: float = 120.0,
+              storage: str = "f16", drain_s: float = 60.0, plan=None, pool=None):
+    """Serving at `rate` req/s for `seconds` (serve_plan): a client thread submits each
+    request at its arrival time into a result buffer (pinned, from a bounded pool) and releases
+    each canvas after its last request; a consumer thread waits for the requests in order and
+    returns their buffers. Requests still unfinished `drain_s` after the last arrival are
+    cancelled and counted as unfinished. Latency = submit to result in the caller's buffer."""
+    import threading
+
+    from painty_gb300 import workloads
+
+    plan = plan if plan is not None else serve_plan(rate, seconds, seed)
+    n = len(plan)
+    last = {}
+    for i, (_, cont, *_r) in enumerate(plan):
+        last[cont if cont >= 0 else i] = i
+    fp = workloads.footprint_image(seed=7)
+    substrate = np.random.default_rng(seed).uniform(0.8, 0.95, (4096, 4096, 3)).astype(np.float32)
+    pool = pool if pool is not None else _PinnedPool(torch, 24 << 30)
     srv = pg.Server(int(budget_gb * (1 << 30)), fp, storage=storage, step_stamps=16384)
     rids = [None] * n
     cids = [None] * n
+    keys = [None] * n
+    submitted = threading.Semaphore(0)
+    lat = np.full(n, np.nan)
+    stamps_done = [0]
     t0 = time.perf_counter()
+    deadline = t0 + seconds + drain_s
 
     def client():
         for i, (t, cont, rows, cols, strokes) in enumerate(plan):
             dt = t - (time.perf_counter() - t0)
             if dt > 0:
                 time.sleep(dt)
+            keys[i], out = pool.take(rows, cols)
+            root = cont if cont >= 0 else i
             if cont >= 0:
-                while cids[cont] is None:
-                    time.sleep(0.0005)
-                rids[i], cids[i] = srv.submit(strokes, canvas_id=cids[cont])
+                rids[i], cids[i] = srv.submit(strokes, canvas_id=cids[cont], out=out)
             else:
                 r0 = np.ascontiguousarray(substrate[:rows, :cols])
-                rids[i], cids[i] = srv.submit(strokes, rows=rows, cols=cols, r0=r0)
+                rids[i], cids[i] = srv.submit(strokes, rows=rows, cols=cols, r0=r0, out=out)
+            if last[root] == i:
+                srv.release(cids[i])
+            submitted.release()
+
+    def consumer():
+        for i in range(n):
+            submitted.acquire()
+            left = max(0.0, deadline - time.perf_counter())
+            try:
+                _, l, st = srv.wait(rids[i], left)
+                lat[i] = l
+                stamps_done[0] += st
+                pool.give(keys[i])
+            except pg.PaintyError as e:
+                if e.status != 6:  # over (failed or cancelled); a timed-out one may still write
+                    pool.give(keys[i])
 
     th = threading.Thread(target=client)
+    tc = threading.Thread(target=consumer)
     th.start()
+    tc.start()
     th.join()
-    lat, stamps = [], 0
-    for i in range(n):
-        _, l, st = srv.wait(rids[i], -1)
-        lat.append(l)
-        stamps += st
+    tc.join()
     wall = time.perf_counter() - t0
+    unfinished = int(np.isnan(lat).sum())
+    for i in range(n):
+        if np.isnan(lat[i]):
+            srv.cancel(rids[i])
     stats = srv.stats()
     srv.close()
-    lat = np.array(lat)
+    done = lat[~np.isnan(lat)]
     offered = sum(
         int(sum(pg_stroke_stamps(p, sp) for p, _, sp, _, _ in strokes)) for *_, strokes in plan)
-    return {"metric": "request latency", "p50_s": round(float(np.percentile(lat, 50)), 4),
-            "p99_s": round(float(np.percentile(lat, 99)), 4),
-            "throughput_req_s": round(n / wall, 2), "stamps_per_s": round(stamps / wall, 1),
-            "requests": n, "arrival_rate": rate, "arrival_window_s": seconds,
-            "offered_stamps_per_s": round(offered / seconds, 1),
-            "wall_s": round(wall, 2), "storage": storage, "budget_gb": budget_gb,
-            "evictions": stats["evictions"], "restores": stats["restores"],
-            "steps": stats["steps"], "peak_resident_gb": round(stats["peak_resident_bytes"] / 2**30, 2),
-            "config": "Poisson arrivals; canvas side logU[512,4096]; 1-500 strokes (geometric, "
-                      "mean 60), r U[8,32], spacing 0.25 r; 30% continue an earlier canvas; "
-                      "composite returned per request"}
+    out = {"metric": "request latency", "arrival_rate": rate, "arrival_window_s": seconds,
+           "requests": n, "completed": int(done.size), "unfinished": unfinished,
+           "p50_s": round(float(np.percentile(done, 50)), 4) if done.size else None,
+           "p99_s": round(float(np.percentile(done, 99)), 4) if done.size else None,
+           "throughput_req_s": round(done.size / wall, 2),
+           "stamps_per_s": round(stamps_done[0] / wall, 1),
+           "offered_stamps_per_s": round(offered / seconds, 1),
+           "wall_s": round(wall, 2), "storage": storage, "budget_gb": budget_gb,
+           "evictions": stats["evictions"], "restores": stats["restores"],
+           "launches": stats["steps"],
+           "peak_resident_gb": round(stats["peak_resident_bytes"] / 2**30, 2),
+           "config": "Poisson arrivals; canvas side logU[512,4096]; 1-500 strokes (geometric, "
+                     "mean 60), r U[8,32], spacing 0.25 r; 30% continue an earlier canvas; "
+                     "composite returned per request into a pinned buffer; canvases released "
+                     "after their last request"}
+    # sustained: nothing left unfinished and completions kept pace with arrivals
+    out["sustained"] = bool(unfinished == 0 and done.size and
+                            out["p99_s"] is not None and out["p99_s"] < 10.0)
+    return out
+
+
+def run_serving(pg, torch, rates=(20.0, 50.0, 100.0), sweep_s: float = 10.0,
+                full_rate: float = 200.0, full_s: float = 60.0):
+    """The stated serving run (full_rate req/s for full_s) and a sweep of lower rates over
+    shorter windows; reports the highest sustained rate."""
+    pool = _PinnedPool(torch, 24 << 30)
+    sweep = [run_serve(pg, torch, r, sweep_s, pool=pool, drain_s=30.0) for r in rates]
+    full = run_serve(pg, torch, full_rate, full_s, pool=pool)
+    ok = [x["arrival_rate"] for x in sweep + [full] if x["sustained"]]
+    full["sweep"] = [{k: x[k] for k in ("arrival_rate", "arrival_window_s", "requests",
+                                        "completed", "unfinished", "p50_s", "p99_s",
+                                        "throughput_req_s", "stamps_per_s", "sustained")}
+                     for x in sweep]
+    full["highest_sustained_rate"] = max(ok) if ok else None
+    return full
 
 
 def pg_stroke_stamps(path, spacing):
@@ -1083,8 +1181,10 @@ def main():
     ap.add_argument("--batch-only", action="store_true", help="only the batched stamping case")
     ap.add_argument("--texture-only", action="store_true",
                     help="only the texture brushes, GL canvas path and lit render")
-    ap.add_argument("--serve-rate", type=float, default=20.0, help="serving arrivals per second")
-    ap.add_argument("--serve-seconds", type=float, default=5.0, help="serving arrival window")
+    ap.add_argument("--serve-rate", type=float, default=200.0, help="serving arrivals per second")
+    ap.add_argument("--serve-seconds", type=float, default=60.0, help="serving arrival window")
+    ap.add_argument("--serve-sweep", action="store_true",
+                    help="with --serve-only: the rate sweep before the stated run")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

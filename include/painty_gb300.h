@@ -342,8 +342,8 @@ typedef struct painty_server painty_server;
 typedef struct painty_server_options {
   uint64_t budget_bytes;   /* device memory for resident canvases (state, snapshot, maps) */
   painty_storage storage;  /* canvas storage format */
-  int32_t max_active;      /* requests painted at once (<= 0: 256) */
-  int64_t step_stamps;     /* stamps per request per step (<= 0: 16384) */
+  int32_t max_active;      /* requests painted at once: one stream each (<= 0: 256; at most 1024) */
+  int64_t step_stamps;     /* stamps per launch of a request (whole strokes; <= 0: 16384) */
   double pickup_rate, deposition_rate;
   const double* footprint; /* brush footprint image (copied) */
   int32_t footprint_rows, footprint_cols;
@@ -374,9 +374,13 @@ painty_status painty_server_submit(painty_server* server, const painty_request* 
  * PAINTY_ERR_TIMEOUT when it has not finished in time. */
 painty_status painty_server_wait(painty_server* server, uint64_t request_id, double timeout_s,
                                  double* latency_s, int64_t* stamps);
-/* Cancels a request: before it runs it is dropped; while it runs it stops at the next step
- * (its canvas keeps the strokes painted so far). */
+/* Cancels a request: before it runs it is dropped; while it runs it stops after its current
+ * chunk of strokes (its canvas keeps the strokes painted so far). */
 painty_status painty_server_cancel(painty_server* server, uint64_t request_id);
+/* Drops a canvas: once the requests already queued on it have finished, its device memory,
+ * brush and any host copy are freed; later submits to it fail. No counterpart in painty (its
+ * canvases are freed by their owner); a serving host calls it after a canvas's last request. */
+painty_status painty_server_release(painty_server* server, uint64_t canvas_id);
 painty_status painty_server_stats(painty_server* server, painty_server_counters* out);
 /* Stops the worker after its current step; unfinished requests end as cancelled. */
 painty_status painty_server_destroy(painty_server* server);

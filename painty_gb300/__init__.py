@@ -750,6 +750,7 @@ _sig("painty_server_create", C.POINTER(_ServerOptions), C.POINTER(_P))
 _sig("painty_server_submit", _P, C.POINTER(_Request), C.POINTER(C.c_uint64), C.POINTER(C.c_uint64))
 _sig("painty_server_wait", _P, C.c_uint64, _D, C.POINTER(_D), C.POINTER(_I64))
 _sig("painty_server_cancel", _P, C.c_uint64)
+_sig("painty_server_release", _P, C.c_uint64)
 _sig("painty_server_stats", _P, C.POINTER(_Counters))
 _sig("painty_server_destroy", _P)
 
@@ -784,13 +785,20 @@ class Server:
         self._live = {}  # request id -> buffers that must outlive the request
 
     def submit(self, strokes, canvas_id: int = 0, rows: int = 0, cols: int = 0, r0=None,
-               want_result: bool = True):
-        """strokes: [(path, radius, spacing, K, S)]; returns (request_id, canvas_id)."""
+               want_result: bool = True, out=None):
+        """strokes: [(path, radius, spacing, K, S)]; returns (request_id, canvas_id).
+        out: the caller's (rows, cols, 3) float32 buffer for the result (pinned host memory
+        keeps the server's worker from blocking on the copy); by default a new array."""
         desc, pts = _strokes_to_desc(strokes)
         if canvas_id:
             rows, cols = self._dims.get(canvas_id, (0, 0))
         r0a = None if r0 is None else np.ascontiguousarray(r0, dtype=np.float32)
-        out = np.empty((rows, cols, 3), dtype=np.float32) if want_result else None
+        if out is not None:
+            if (out.dtype != np.float32 or out.shape != (rows, cols, 3)
+                    or not out.flags["C_CONTIGUOUS"]):
+                raise ValueError("out must be a C-contiguous float32 array of (rows, cols, 3)")
+        elif want_result:
+            out = np.empty((rows, cols, 3), dtype=np.float32)
         req = _Request(canvas_id, rows, cols, None if r0a is None else r0a.ctypes.data,
                        desc.ctypes.data, len(desc), pts.ctypes.data, pts.shape[0],
                        None if out is None else out.ctypes.data)
@@ -813,6 +821,10 @@ class Server:
 
     def cancel(self, request_id: int) -> None:
         _check(_lib.painty_server_cancel(self._h, request_id))
+
+    def release(self, canvas_id: int) -> None:
+        """Drops a canvas once the requests queued on it have finished."""
+        _check(_lib.painty_server_release(self._h, canvas_id))
 
     def stats(self) -> dict:
         c = _Counters()

@@ -78,6 +78,20 @@ void* device_alloc(size_t bytes) {
 void device_free(void* p) {
   if (p) cudaFree(p);
 }
+void* device_alloc_on(size_t bytes, cudaMemPool_t pool, cudaStream_t st) {
+  void* p = nullptr;
+  if (bytes == 0) return nullptr;
+  const cudaError_t e = cudaMallocFromPoolAsync(&p, bytes, pool, st);
+  if (e == cudaErrorMemoryAllocation) {
+    cudaGetLastError();
+    fail(PAINTY_ERR_OUT_OF_MEMORY, "device memory exhausted (pool allocation)");
+  }
+  PG_CUDA(e);
+  return p;
+}
+void device_free_on(void* p, cudaStream_t st) {
+  if (p) cudaFreeAsync(p, st);
+}
 
 // Planar: 7 planes, each 256-byte aligned. Packed: one record of 8 elements per pixel (K and
 // S, V of the same size in every storage format).
@@ -142,6 +156,41 @@ void canvas_relayout(painty_canvas* c, void* base) {
   image_layout(c->r0, rows, cols, rs, static_cast<char*>(base) + lb);
   c->r0.owned = false;
   c->h = static_cast<char*>(base) + lb + ib;
+}
+
+painty_canvas* canvas_create_on(int32_t rows, int32_t cols, painty_storage storage,
+                                cudaMemPool_t pool, cudaStream_t st) {
+  PG_REQUIRE(rows > 0 && cols > 0, "rows and cols must be positive");
+  PG_REQUIRE(valid_storage(storage), "unknown storage format");
+  auto* c = new painty_canvas();
+  const painty_storage rs = storage == PAINTY_STORAGE_F64 ? PAINTY_STORAGE_F64 : PAINTY_STORAGE_F32;
+  const size_t lb = layer_bytes(rows, cols, storage, true);
+  const size_t ib = image_bytes(rows, cols, rs);
+  const size_t hb = static_cast<size_t>(rows) * pitch_for(cols) * v_bytes(storage);
+  try {
+    c->wet.rows = rows;
+    c->wet.cols = cols;
+    c->wet.storage = storage;
+    c->r0.storage = rs;
+    c->bytes = lb + ib + align256(hb);
+    canvas_relayout(c, device_alloc_on(c->bytes, pool, st));
+    c->id = g_canvas_ids.fetch_add(1);
+    PG_CUDA(cudaMemsetAsync(c->base, 0, c->bytes, st));
+    const double one[3] = {1.0, 1.0, 1.0};  // Canvas.hxx:33 background
+    fill_planes(c->r0.R, 3, r_type(rs), c->r0.plane_elems(), one, st);
+    PG_CUDA(cudaStreamSynchronize(st));
+  } catch (...) {
+    if (c->base) device_free_on(c->base, st);
+    delete c;
+    throw;
+  }
+  return c;
+}
+
+void canvas_destroy_on(painty_canvas* c, cudaStream_t st) {
+  if (!c) return;
+  device_free_on(c->base, st);
+  delete c;
 }
 
 // ------------------------------------------------------------------ transfer kernels

@@ -63,6 +63,11 @@ inline int64_t pitch_for(int32_t cols) { return (static_cast<int64_t>(cols) + 63
 
 void* device_alloc(size_t bytes);
 void device_free(void* p);
+// Stream-ordered device memory from `pool` (a pool with a retained release threshold): the
+// allocation and the release are ordered on `st` and never synchronise the device. For
+// objects a long-running owner (the server) creates and drops while kernels run.
+void* device_alloc_on(size_t bytes, cudaMemPool_t pool, cudaStream_t st);
+void device_free_on(void* p, cudaStream_t st);
 
 }  // namespace pg
 
@@ -152,6 +157,10 @@ struct painty_brush {
   int ring_pending = -1;
   void* d_stamps = nullptr;
   size_t d_stamps_bytes = 0;
+  // device memory from a pool, ordered on pool_stream (set by an owner that runs the brush's
+  // kernels on that stream), instead of cudaMalloc / cudaFree
+  cudaMemPool_t pool = nullptr;
+  cudaStream_t pool_stream = nullptr;
   unsigned* d_status = nullptr;  // 16 words: [0] kernel status, [2] stamps applied (rounding
                                  // seed), [8..15] the ring state
   int* d_ring() const { return reinterpret_cast<int*>(d_status) + 8; }
@@ -167,6 +176,11 @@ size_t image_bytes(int32_t rows, int32_t cols, painty_storage s);
 // Points a canvas's plane views into a new device allocation of the canvas layout (nullptr:
 // no allocation, as for a canvas whose state was moved to host memory).
 void canvas_relayout(painty_canvas* c, void* base);
+// A canvas (as painty_canvas_create) in pool memory ordered on `st`; returns after `st` has
+// finished initialising it. Free with canvas_destroy_on.
+painty_canvas* canvas_create_on(int32_t rows, int32_t cols, painty_storage storage,
+                                cudaMemPool_t pool, cudaStream_t st);
+void canvas_destroy_on(painty_canvas* c, cudaStream_t st);
 
 // Plane transfer between a host buffer and `nch` device planes of element type `dev_type`
 // (0 f32, 1 f16, 2 bf16, 3 f64) with the given pitch and element stride (1 planar, 8 packed).

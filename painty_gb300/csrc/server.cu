@@ -1,23 +1,31 @@
 // server.cu -- continuous-batching stroke-render server.
 //
 // Requests (paint these strokes on a new canvas, or continue a canvas an earlier request
-// created) arrive at any time. A worker thread runs short steps: each step paints the next
-// slice of every admitted request's strokes -- up to `step_stamps` stamps per request -- in
-// one batched launch (the painty_paint_batch kernel), so requests that arrive while others
-// are on the GPU join at the next step instead of waiting for them to finish. Canvases stay
-// resident on the device between requests; admission keeps their bytes under a device-memory
-// budget by evicting idle canvases (least recently used first) to pinned host memory and
-// restoring them when a later request continues them. A canvas's requests run one after
-// another, in submission order; different canvases are independent, so a request's result
-// does not depend on what else is in flight.
+// created) arrive at any time. A worker thread admits each one as soon as a slot (a stream
+// with its event and status word) and device memory allow, and runs it as a chain of
+// stamp-kernel launches on its slot's stream: each launch paints the request's next
+// `step_stamps` stamps (whole strokes) with the batched stamp kernel. Launches of different
+// requests run concurrently on the device -- nothing waits for a step of the whole server --
+// so a request that arrives while others are painting starts as soon as it is admitted. The
+// worker polls the slots' events: a finished chunk is followed by the next one, a finished
+// request by the KM composite of its canvas (Renderer::compose,
+// painty/renderer/Renderer.hxx:26-53) and its download into the caller's buffer, all in the
+// slot's stream order.
 //
-// Each request completes with the KM composite of its canvas (Renderer::compose,
-// painty/renderer/Renderer.hxx:26-53) downloaded into the caller's buffer.
+// Canvases stay resident on the device between requests. Their memory (canvas, composite
+// image, brush buffers) comes from a stream-ordered pool, so creating and dropping canvases
+// never synchronises the device. Admission keeps the resident bytes under a budget by
+// evicting idle canvases (least recently used first) to pinned host memory and restoring them
+// when a later request continues them. A canvas's requests run one after another, in
+// submission order; different canvases are independent, so a request's result does not
+// depend on what else is in flight. painty_server_release drops a canvas once its queued
+// requests are done.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -35,21 +43,11 @@ double now_s() {
 }
 
 enum ReqState { REQ_PENDING = 0, REQ_ACTIVE = 1, REQ_DONE = 2 };
+enum Phase { PH_PAINT = 0, PH_FINISH = 1 };
 
-struct HostBlob {  // pinned host copy of a device allocation
+struct HostBlob {  // pinned host memory holding an evicted device allocation
   void* p = nullptr;
   size_t bytes = 0;
-  void ensure(size_t n) {
-    if (p && bytes >= n) return;
-    if (p) cudaFreeHost(p);
-    p = nullptr;
-    bytes = 0;
-    PG_CUDA(cudaMallocHost(&p, n));
-    bytes = n;
-  }
-  ~HostBlob() {
-    if (p) cudaFreeHost(p);
-  }
 };
 
 struct ServerCanvas {
@@ -57,8 +55,11 @@ struct ServerCanvas {
   int32_t rows = 0, cols = 0;
   painty_canvas* cv = nullptr;  // created by the canvas's first request
   painty_brush* brush = nullptr;
+  painty_image img{};           // the composite of the canvas (resident with it)
   bool resident = false;
-  bool busy = false;  // one of its requests is active
+  bool busy = false;     // one of its requests is admitted
+  bool release = false;  // drop the canvas once its queued requests are done
+  bool dropped = false;  // released and freed
   uint64_t last_used = 0;
   size_t bytes = 0;  // device bytes when resident
   std::vector<float> r0;  // substrate until the canvas is created
@@ -74,11 +75,20 @@ struct ServerRequest {
   float* out_rgb = nullptr;
   size_t next = 0;  // next stroke to paint
   int state = REQ_PENDING;
+  int phase = PH_PAINT;
+  int slot = -1;
   bool cancel = false;
   painty_status status = PAINTY_OK;
   std::string error;
   int64_t stamps = 0;
   double t_submit = 0, t_done = 0;
+};
+
+struct Slot {
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev = nullptr;
+  unsigned* status = nullptr;  // pinned: the last launch's kernel status word
+  bool busy = false;
 };
 
 }  // namespace
@@ -87,94 +97,165 @@ struct painty_server {
   painty_server_options opt{};
   std::vector<double> footprint;
   int device = 0;
-  cudaStream_t stream = nullptr;
+  int sms = 0;
+  cudaStream_t stream = nullptr;  // creation, eviction and restore
+  cudaMemPool_t pool = nullptr;
+  std::vector<Slot> slots;
+  unsigned* status_words = nullptr;
+  std::multimap<size_t, void*> pinned_free;  // pinned blobs of released canvases, by size
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<uint64_t> pending;
   std::vector<uint64_t> active;
   std::unordered_map<uint64_t, std::unique_ptr<ServerRequest>> reqs;
   std::unordered_map<uint64_t, std::unique_ptr<ServerCanvas>> canvases;
+  std::vector<ServerCanvas*> to_drop;  // released canvases waiting for the worker to free them
   size_t resident = 0, peak = 0;
-  uint64_t next_req = 1, next_canvas = 1, step = 0;
+  uint64_t next_req = 1, next_canvas = 1, tick = 0;
   painty_server_counters stats{};
   bool stop = false;
-  uint64_t gen = 0;  // bumped by submit, cancel and finish: the idle worker waits for a change
-  std::string worker_error;
+  uint64_t gen = 0;  // bumped by submit, cancel, release and finish
   std::thread worker;
 };
 
 namespace {
 
+painty_storage image_storage(const painty_server* s) {
+  return s->opt.storage == PAINTY_STORAGE_F64 ? PAINTY_STORAGE_F64 : PAINTY_STORAGE_F32;
+}
+
 size_t canvas_device_bytes(const painty_server* s, int32_t rows, int32_t cols) {
   const painty_storage st = s->opt.storage;
-  const painty_storage rs = st == PAINTY_STORAGE_F64 ? PAINTY_STORAGE_F64 : PAINTY_STORAGE_F32;
+  const painty_storage rs = image_storage(s);
   const size_t pe = static_cast<size_t>(rows) * pg::pitch_for(cols);
-  return pg::layer_bytes(rows, cols, st, true) + pg::image_bytes(rows, cols, rs) +
+  return pg::layer_bytes(rows, cols, st, true) + 2 * pg::image_bytes(rows, cols, rs) +
          pe * pg::v_bytes(st) + pg::layer_bytes(rows, cols, st, true) /* snapshot */ +
          (4u << 20) /* pickup map, footprint, scratch */;
 }
 
-// Moves a canvas's device state (canvas planes and the brush's snapshot) to
-// pinned host memory and frees it on the device.
+// Pinned host memory for an eviction: a released canvas's blob of at least that size, or a
+// new one.
+void* pinned_take(painty_server* s, size_t bytes, size_t* got) {
+  auto it = s->pinned_free.lower_bound(bytes);
+  if (it != s->pinned_free.end() && it->first <= 2 * bytes) {
+    void* p = it->second;
+    *got = it->first;
+    s->pinned_free.erase(it);
+    return p;
+  }
+  void* p = nullptr;
+  PG_CUDA(cudaMallocHost(&p, bytes));
+  *got = bytes;
+  return p;
+}
+
+void blob_save(painty_server* s, HostBlob& b, const void* dev, size_t bytes) {
+  if (!b.p || b.bytes < bytes) {
+    if (b.p) s->pinned_free.emplace(b.bytes, b.p);
+    b.p = pinned_take(s, bytes, &b.bytes);
+  }
+  PG_CUDA(cudaMemcpyAsync(b.p, dev, bytes, cudaMemcpyDeviceToHost, s->stream));
+}
+
+void image_alloc(painty_server* s, ServerCanvas* c) {
+  const painty_storage rs = image_storage(s);
+  void* base = pg::device_alloc_on(pg::image_bytes(c->rows, c->cols, rs), s->pool, s->stream);
+  pg::image_layout(c->img, c->rows, c->cols, rs, base);
+  c->img.owned = false;
+}
+
+void image_free(painty_server* s, ServerCanvas* c) {
+  pg::device_free_on(c->img.base, s->stream);
+  c->img.base = nullptr;
+}
+
+// Moves a canvas's device state (canvas planes and the brush's snapshot) to pinned host
+// memory and frees it on the device. Called by the worker for idle canvases only.
 void evict(painty_server* s, ServerCanvas* c) {
   painty_canvas* cv = c->cv;
   painty_brush* b = c->brush;
-  c->save_canvas.ensure(cv->bytes);
-  PG_CUDA(cudaMemcpyAsync(c->save_canvas.p, cv->base, cv->bytes, cudaMemcpyDeviceToHost,
-                          s->stream));
-  if (b->has_snapshot) {
-    c->save_snapshot.ensure(b->snapshot.bytes);
-    PG_CUDA(cudaMemcpyAsync(c->save_snapshot.p, b->snapshot.base, b->snapshot.bytes,
-                            cudaMemcpyDeviceToHost, s->stream));
-  }
+  b->pool_stream = s->stream;
+  blob_save(s, c->save_canvas, cv->base, cv->bytes);
+  if (b->has_snapshot) blob_save(s, c->save_snapshot, b->snapshot.base, b->snapshot.bytes);
   PG_CUDA(cudaStreamSynchronize(s->stream));
-  pg::device_free(cv->base);
+  pg::device_free_on(cv->base, s->stream);
   pg::canvas_relayout(cv, nullptr);
   if (b->has_snapshot) {
-    pg::device_free(b->snapshot.base);
+    pg::device_free_on(b->snapshot.base, s->stream);
     b->snapshot.base = nullptr;
   }
+  image_free(s, c);
   c->resident = false;
 }
 
 void restore(painty_server* s, ServerCanvas* c) {
   painty_canvas* cv = c->cv;
   painty_brush* b = c->brush;
-  void* base = pg::device_alloc(cv->bytes);
+  b->pool_stream = s->stream;
+  void* base = pg::device_alloc_on(cv->bytes, s->pool, s->stream);
   PG_CUDA(cudaMemcpyAsync(base, c->save_canvas.p, cv->bytes, cudaMemcpyHostToDevice, s->stream));
   pg::canvas_relayout(cv, base);
   if (b->has_snapshot) {
-    void* sb = pg::device_alloc(b->snapshot.bytes);
+    void* sb = pg::device_alloc_on(b->snapshot.bytes, s->pool, s->stream);
     PG_CUDA(cudaMemcpyAsync(sb, c->save_snapshot.p, b->snapshot.bytes, cudaMemcpyHostToDevice,
                             s->stream));
     pg::layer_layout(b->snapshot, b->snapshot.rows, b->snapshot.cols, b->snapshot.storage, sb,
                      true);
   }
+  image_alloc(s, c);
   PG_CUDA(cudaStreamSynchronize(s->stream));
   c->resident = true;
 }
 
 void create(painty_server* s, ServerCanvas* c) {
-  painty_canvas* cv = nullptr;
-  painty_status st = painty_canvas_create(c->rows, c->cols, s->opt.storage, &cv);
-  if (st != PAINTY_OK) pg::fail(st, painty_last_error());
-  if (!c->r0.empty())
-    pg::upload_planes(cv->r0.R, 3, pg::r_type(cv->r0.storage), c->rows, c->cols, cv->wet.pitch,
-                      c->r0.data(), PAINTY_HOST_F32_INTERLEAVED, s->stream);
-  cv->version++;
-  painty_brush* b = nullptr;
-  st = painty_brush_create(8.0, s->footprint.data(), s->opt.footprint_rows,
-                           s->opt.footprint_cols, &b);
-  if (st != PAINTY_OK) {
-    painty_canvas_destroy(cv);
-    pg::fail(st, painty_last_error());
+  painty_canvas* cv = pg::canvas_create_on(c->rows, c->cols, s->opt.storage, s->pool, s->stream);
+  try {
+    if (!c->r0.empty())
+      pg::upload_planes(cv->r0.R, 3, pg::r_type(cv->r0.storage), c->rows, c->cols,
+                        cv->wet.pitch, c->r0.data(), PAINTY_HOST_F32_INTERLEAVED, s->stream);
+    cv->version++;
+    painty_brush* b = nullptr;
+    const painty_status st = painty_brush_create(8.0, s->footprint.data(),
+                                                 s->opt.footprint_rows, s->opt.footprint_cols, &b);
+    if (st != PAINTY_OK) pg::fail(st, painty_last_error());
+    b->pickupRate = s->opt.pickup_rate;
+    b->depositionRate = s->opt.deposition_rate;
+    b->pool = s->pool;
+    b->pool_stream = s->stream;
+    c->brush = b;
+  } catch (...) {
+    pg::canvas_destroy_on(cv, s->stream);
+    throw;
   }
-  b->pickupRate = s->opt.pickup_rate;
-  b->depositionRate = s->opt.deposition_rate;
   c->cv = cv;
-  c->brush = b;
+  image_alloc(s, c);
+  PG_CUDA(cudaStreamSynchronize(s->stream));
   c->resident = true;
   std::vector<float>().swap(c->r0);
+}
+
+// Frees a released canvas (worker thread; nothing of it is in flight).
+void drop(painty_server* s, ServerCanvas* c) {
+  if (c->brush) {
+    c->brush->pool_stream = s->stream;
+    painty_brush_destroy(c->brush);
+  }
+  if (c->cv) {
+    if (c->resident) {
+      image_free(s, c);
+      pg::canvas_destroy_on(c->cv, s->stream);
+    } else {
+      delete c->cv;  // evicted: no device memory left to free
+    }
+  }
+  for (HostBlob* b : {&c->save_canvas, &c->save_snapshot}) {
+    if (b->p) s->pinned_free.emplace(b->bytes, b->p);
+    *b = HostBlob{};
+  }
+  c->brush = nullptr;
+  c->cv = nullptr;
+  c->resident = false;
+  c->dropped = true;
 }
 
 // Marks a request finished (lock held).
@@ -192,17 +273,90 @@ void finish(painty_server* s, ServerRequest* r, painty_status st, const std::str
   ServerCanvas* c = s->canvases[r->canvas_id].get();
   if (!c->waiting.empty() && c->waiting.front() == r->id) c->waiting.pop_front();
   c->busy = false;
-  c->last_used = s->step;
+  c->last_used = s->tick;
+  if (r->slot >= 0) s->slots[r->slot].busy = false;
+  r->slot = -1;
+  if (c->release && c->waiting.empty() && !c->busy) {
+    if (c->resident) s->resident -= c->bytes;
+    s->to_drop.push_back(c);
+  }
   s->gen++;  // requests queued behind this one may be admitted now
 }
 
-// One scheduling round: admit what fits, paint one step of every active request, complete
-// the requests whose strokes are all painted. Called with the lock held.
-void worker_round(painty_server* s, std::unique_lock<std::mutex>& lk) {
-  // ---- admission: pending requests in arrival order
-  std::vector<ServerCanvas*> prep, evictions;
-  for (auto it = s->pending.begin(); it != s->pending.end();) {
-    if (static_cast<int32_t>(s->active.size()) >= s->opt.max_active) break;
+// Cluster cap for a launch: larger clusters shorten one canvas's chain of stamps, single CTAs
+// paint the most canvases at once, so the cap shrinks as more requests are in flight.
+int cluster_cap(const painty_server* s) {
+  const int inflight = static_cast<int>(s->active.size());
+  for (int c : {8, 4, 2})
+    if (inflight * c <= s->sms) return c;
+  return 1;
+}
+
+// Launches the next chunk of a request's strokes (worker thread, lock not held).
+void launch_chunk(painty_server* s, ServerRequest* r, ServerCanvas* c, int cap) {
+  Slot& sl = s->slots[r->slot];
+  size_t k = r->next;
+  int64_t budget = 0;
+  while (k < r->strokes.size() &&
+         (k == r->next || budget + r->stroke_stamps[k] <= s->opt.step_stamps)) {
+    budget += r->stroke_stamps[k];
+    k++;
+  }
+  std::vector<painty_stroke_desc> descs;
+  std::vector<double> pts;
+  for (size_t j = r->next; j < k; j++) {
+    painty_stroke_desc d = r->strokes[j];
+    const double* p = r->points.data() + 2 * d.first_point;
+    d.canvas = 0;
+    d.first_point = static_cast<int64_t>(pts.size() / 2);
+    pts.insert(pts.end(), p, p + 2 * d.npoints);
+    descs.push_back(d);
+  }
+  *sl.status = 0;
+  pg::BatchOptions opt;
+  opt.max_cluster = cap;
+  opt.status_host = sl.status;
+  c->brush->pool_stream = sl.st;  // its buffers are (re)allocated in this stream's order
+  int64_t n = 0;
+  painty_canvas* cvs[1] = {c->cv};
+  painty_brush* brs[1] = {c->brush};
+  pg::paint_batch(cvs, brs, 1, descs.data(), static_cast<int64_t>(descs.size()), pts.data(),
+                  static_cast<int64_t>(pts.size() / 2), &n, sl.st, &opt);
+  PG_CUDA(cudaEventRecord(sl.ev, sl.st));
+  r->stamps += budget;
+  r->next = k;
+}
+
+// The composite of a finished request's canvas, downloaded into the caller's buffer in the
+// slot's stream order (worker thread).
+void launch_finish(painty_server* s, ServerRequest* r, ServerCanvas* c) {
+  Slot& sl = s->slots[r->slot];
+  const painty_layer* L[1] = {&c->cv->wet};
+  pg::launch_compose(L, 1, &c->cv->r0, &c->img, sl.st);
+  const void* p[3] = {c->img.R[0], c->img.R[1], c->img.R[2]};
+  // out_rgb is float RGB whatever the storage (F64 results are rounded to float)
+  pg::download_planes_async(p, 3, pg::r_type(c->img.storage), c->rows, c->cols, c->img.pitch,
+                            r->out_rgb, PAINTY_HOST_F32_INTERLEAVED, sl.st);
+  PG_CUDA(cudaEventRecord(sl.ev, sl.st));
+}
+
+struct Admitted {
+  ServerRequest* r;
+  ServerCanvas* c;
+  bool prep;  // create or restore the canvas first
+};
+
+// One round of the worker: admit what fits, start admitted requests, advance every request
+// whose slot's work has finished. Called with the lock held; returns whether anything moved.
+bool worker_round(painty_server* s, std::unique_lock<std::mutex>& lk) {
+  // ---- drops and admission (lock held): pending requests in arrival order
+  std::vector<ServerCanvas*> drops;
+  drops.swap(s->to_drop);
+  std::vector<ServerCanvas*> evictions;
+  std::vector<Admitted> admitted;
+  int free_slots = 0;
+  for (const Slot& sl : s->slots) free_slots += sl.busy ? 0 : 1;
+  for (auto it = s->pending.begin(); it != s->pending.end() && free_slots > 0;) {
     ServerRequest* r = s->reqs[*it].get();
     ServerCanvas* c = s->canvases[r->canvas_id].get();
     if (c->busy || c->waiting.empty() || c->waiting.front() != r->id) {
@@ -224,7 +378,7 @@ void worker_round(painty_server* s, std::unique_lock<std::mutex>& lk) {
       ServerCanvas* lru = nullptr;
       for (auto& kv : s->canvases) {
         ServerCanvas* x = kv.second.get();
-        if (x->resident && !x->busy &&
+        if (x->resident && !x->busy && !x->release &&
             std::find(evictions.begin(), evictions.end(), x) == evictions.end() &&
             (!lru || x->last_used < lru->last_used))
           lru = x;
@@ -238,111 +392,120 @@ void worker_round(painty_server* s, std::unique_lock<std::mutex>& lk) {
     s->peak = std::max(s->peak, s->resident);
     c->busy = true;
     r->state = REQ_ACTIVE;
-    if (!c->resident) prep.push_back(c);
+    r->phase = PH_PAINT;
+    for (int i = 0; i < static_cast<int>(s->slots.size()); i++)
+      if (!s->slots[i].busy) {
+        s->slots[i].busy = true;
+        r->slot = i;
+        break;
+      }
+    free_slots--;
+    admitted.push_back({r, c, !c->resident});
     s->active.push_back(r->id);
     it = s->pending.erase(it);
   }
-  std::vector<ServerRequest*> act;
-  for (uint64_t id : s->active) act.push_back(s->reqs[id].get());
-  s->step++;
+  // requests in flight and their cancel flags, as of now
+  struct Running {
+    ServerRequest* r;
+    ServerCanvas* c;
+    bool cancel;
+  };
+  std::vector<Running> running;
+  for (uint64_t id : s->active) {
+    ServerRequest* r = s->reqs[id].get();
+    bool fresh = false;
+    for (const Admitted& a : admitted) fresh = fresh || a.r == r;
+    if (!fresh) running.push_back({r, s->canvases[r->canvas_id].get(), r->cancel});
+  }
+  const int cap = cluster_cap(s);
+  s->tick++;
   lk.unlock();
 
   // ---- device work (only this thread touches device state)
   std::vector<std::pair<ServerRequest*, std::string>> failures;
   std::vector<ServerRequest*> done;
-  int64_t step_stamps = 0;
+  bool moved = !admitted.empty() || !drops.empty();
+  int64_t chunks = 0;
+  for (ServerCanvas* c : drops) drop(s, c);
   try {
     for (ServerCanvas* c : evictions) evict(s, c);
-    for (ServerCanvas* c : prep) {
-      if (!c->cv) {
-        create(s, c);
-      } else {
-        restore(s, c);
-        s->stats.restores++;
-      }
-    }
-    s->stats.evictions += static_cast<int64_t>(evictions.size());
-    // the next slice of every active request, one batched launch
-    std::vector<painty_canvas*> cvs;
-    std::vector<painty_brush*> brs;
-    std::vector<painty_stroke_desc> descs;
-    std::vector<double> pts;
-    std::vector<std::pair<ServerRequest*, size_t>> slice;  // request, strokes taken
-    for (ServerRequest* r : act) {
-      ServerCanvas* c = s->canvases[r->canvas_id].get();
-      size_t k = r->next;
-      int64_t budget = 0;
-      while (k < r->strokes.size() && (k == r->next || budget + r->stroke_stamps[k] <= s->opt.step_stamps)) {
-        budget += r->stroke_stamps[k];
-        k++;
-      }
-      const int32_t ci = static_cast<int32_t>(cvs.size());
-      if (k > r->next) {
-        cvs.push_back(c->cv);
-        brs.push_back(c->brush);
-        for (size_t j = r->next; j < k; j++) {
-          painty_stroke_desc d = r->strokes[j];
-          const double* p = r->points.data() + 2 * d.first_point;
-          d.canvas = ci;
-          d.first_point = static_cast<int64_t>(pts.size() / 2);
-          pts.insert(pts.end(), p, p + 2 * d.npoints);
-          descs.push_back(d);
+  } catch (const std::exception& e) {  // the canvases stay resident; their bytes count again
+    lk.lock();
+    for (ServerCanvas* c : evictions)
+      if (c->resident) s->resident += c->bytes;
+    lk.unlock();
+    for (const Admitted& a : admitted) failures.emplace_back(a.r, e.what());
+    admitted.clear();
+  }
+  for (const Admitted& a : admitted) {
+    try {
+      if (a.prep) {
+        if (!a.c->cv) {
+          create(s, a.c);
+        } else {
+          restore(s, a.c);
+          s->stats.restores++;
         }
       }
-      slice.emplace_back(r, k - r->next);
-    }
-    if (!cvs.empty()) {
-      pg::paint_batch(cvs.data(), brs.data(), static_cast<int32_t>(cvs.size()), descs.data(),
-                      static_cast<int64_t>(descs.size()), pts.data(),
-                      static_cast<int64_t>(pts.size() / 2), &step_stamps, s->stream);
-    }
-    for (auto& sl : slice) {
-      ServerRequest* r = sl.first;
-      for (size_t j = r->next; j < r->next + sl.second; j++) r->stamps += r->stroke_stamps[j];
-      r->next += sl.second;
-      if (r->next == r->strokes.size() || r->cancel) done.push_back(r);
-    }
-    for (ServerRequest* r : done) {  // composite into the caller's buffer
-      if (r->cancel || !r->out_rgb) continue;
-      ServerCanvas* c = s->canvases[r->canvas_id].get();
-      painty_image* img = nullptr;
-      const painty_storage rs =
-        s->opt.storage == PAINTY_STORAGE_F64 ? PAINTY_STORAGE_F64 : PAINTY_STORAGE_F32;
-      if (painty_image_create(c->rows, c->cols, rs, &img) != PAINTY_OK)
-        pg::fail(PAINTY_ERR_OUT_OF_MEMORY, painty_last_error());
-      const painty_layer* L[1] = {&c->cv->wet};
-      try {
-        pg::launch_compose(L, 1, &c->cv->r0, img, s->stream);
-        const void* p[3] = {img->R[0], img->R[1], img->R[2]};
-        // out_rgb is float RGB whatever the storage (F64 results are rounded to float)
-        pg::download_planes(p, 3, pg::r_type(rs), c->rows, c->cols, img->pitch, r->out_rgb,
-                            PAINTY_HOST_F32_INTERLEAVED, s->stream);
-      } catch (...) {
-        painty_image_destroy(img);
-        throw;
+      if (a.r->strokes.empty()) {
+        a.r->phase = PH_FINISH;
+        if (a.r->out_rgb)
+          launch_finish(s, a.r, a.c);
+        else
+          PG_CUDA(cudaEventRecord(s->slots[a.r->slot].ev, s->slots[a.r->slot].st));
+      } else {
+        launch_chunk(s, a.r, a.c, cap);
+        chunks++;
       }
-      painty_image_destroy(img);
+    } catch (const std::exception& e) {
+      failures.emplace_back(a.r, e.what());
     }
-  } catch (const std::exception& e) {
-    for (ServerRequest* r : act) failures.emplace_back(r, e.what());
+  }
+  s->stats.evictions += static_cast<int64_t>(evictions.size());
+  for (const Running& x : running) {
+    ServerRequest* r = x.r;
+    const cudaError_t q = cudaEventQuery(s->slots[r->slot].ev);
+    if (q == cudaErrorNotReady) continue;
+    moved = true;
+    try {
+      PG_CUDA(q);
+      if (r->phase == PH_FINISH) {
+        done.push_back(r);
+        continue;
+      }
+      if (*s->slots[r->slot].status != 0)
+        pg::fail(PAINTY_ERR_CUDA, "batched stamp kernel reported an internal error");
+      if (r->next < r->strokes.size() && !x.cancel) {
+        launch_chunk(s, r, x.c, cap);
+        chunks++;
+      } else if (r->out_rgb && !x.cancel) {
+        r->phase = PH_FINISH;
+        launch_finish(s, r, x.c);
+      } else {
+        done.push_back(r);
+      }
+    } catch (const std::exception& e) {
+      failures.emplace_back(r, e.what());
+    }
   }
 
   lk.lock();
-  s->stats.steps++;
-  s->stats.stamps += step_stamps;
-  if (!failures.empty()) {
-    for (auto& f : failures) {
-      finish(s, f.first, PAINTY_ERR_CUDA, f.second);
-      s->active.erase(std::find(s->active.begin(), s->active.end(), f.first->id));
-    }
-  } else {
-    for (ServerRequest* r : done) {
-      finish(s, r, r->cancel ? PAINTY_ERR_CANCELLED : PAINTY_OK,
-             r->cancel ? "cancelled while painting" : "");
-      s->active.erase(std::find(s->active.begin(), s->active.end(), r->id));
-    }
+  s->stats.steps += chunks;
+  for (auto& f : failures) {
+    // a failed request's slot is not reused before its stream has drained
+    if (f.first->slot >= 0) cudaStreamSynchronize(s->slots[f.first->slot].st);
+    finish(s, f.first, PAINTY_ERR_CUDA, f.second);
+    s->active.erase(std::find(s->active.begin(), s->active.end(), f.first->id));
   }
-  s->cv_done.notify_all();
+  for (ServerRequest* r : done) {
+    s->stats.stamps += r->stamps;
+    const bool cancelled = r->cancel && (r->next < r->strokes.size() || r->out_rgb);
+    finish(s, r, cancelled ? PAINTY_ERR_CANCELLED : PAINTY_OK,
+           cancelled ? "cancelled while painting" : "");
+    s->active.erase(std::find(s->active.begin(), s->active.end(), r->id));
+  }
+  if (!failures.empty() || !done.empty()) s->cv_done.notify_all();
+  return moved;
 }
 
 void worker_main(painty_server* s) {
@@ -351,17 +514,28 @@ void worker_main(painty_server* s) {
   uint64_t idle_gen = ~0ull;
   while (true) {
     s->cv_work.wait(lk, [&] {
-      return s->stop || !s->active.empty() || (!s->pending.empty() && s->gen != idle_gen);
+      return s->stop || !s->active.empty() || !s->to_drop.empty() ||
+             (!s->pending.empty() && s->gen != idle_gen);
     });
     if (s->stop) break;
     const uint64_t g = s->gen;
-    worker_round(s, lk);
-    // nothing admitted and nothing painting: sleep until a submit or cancel changes things
-    idle_gen = s->active.empty() ? g : ~0ull;
+    const bool moved = worker_round(s, lk);
+    if (s->active.empty()) {
+      // nothing in flight and nothing admitted: sleep until a submit, cancel or release
+      idle_gen = g;
+    } else {
+      idle_gen = ~0ull;
+      // kernels are running: poll their events again shortly, or sooner on a new request
+      if (!moved) s->cv_work.wait_for(lk, std::chrono::microseconds(200));
+    }
   }
-  // shutting down: every unfinished request is cancelled
+  // shutting down: every request still queued is cancelled; launched work drains first
+  std::vector<uint64_t> act = s->active;
+  lk.unlock();
+  for (const Slot& sl : s->slots) cudaStreamSynchronize(sl.st);
+  lk.lock();
   for (uint64_t id : s->pending) finish(s, s->reqs[id].get(), PAINTY_ERR_CANCELLED, "server shut down");
-  for (uint64_t id : s->active) finish(s, s->reqs[id].get(), PAINTY_ERR_CANCELLED, "server shut down");
+  for (uint64_t id : act) finish(s, s->reqs[id].get(), PAINTY_ERR_CANCELLED, "server shut down");
   s->pending.clear();
   s->active.clear();
   s->cv_done.notify_all();
@@ -383,12 +557,31 @@ painty_status painty_server_create(const painty_server_options* opt, painty_serv
     auto s = std::make_unique<painty_server>();
     s->opt = *opt;
     if (s->opt.max_active <= 0) s->opt.max_active = 256;
+    s->opt.max_active = std::min(s->opt.max_active, 1024);
     if (s->opt.step_stamps <= 0) s->opt.step_stamps = 16384;
     s->footprint.assign(opt->footprint,
                         opt->footprint + static_cast<size_t>(opt->footprint_rows) * opt->footprint_cols);
     s->opt.footprint = nullptr;
     PG_CUDA(cudaGetDevice(&s->device));
+    PG_CUDA(cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->device));
     PG_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    // a pool of its own that keeps freed memory for reuse (no release at synchronisation)
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = s->device;
+    PG_CUDA(cudaMemPoolCreate(&s->pool, &props));
+    uint64_t keep = ~0ull;
+    PG_CUDA(cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    PG_CUDA(cudaMallocHost(&s->status_words, sizeof(unsigned) * s->opt.max_active));
+    s->slots.resize(static_cast<size_t>(s->opt.max_active));
+    for (int i = 0; i < s->opt.max_active; i++) {
+      Slot& sl = s->slots[i];
+      PG_CUDA(cudaStreamCreateWithFlags(&sl.st, cudaStreamNonBlocking));
+      PG_CUDA(cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming));
+      sl.status = s->status_words + i;
+      *sl.status = 0;
+    }
     painty_server* raw = s.get();
     s->worker = std::thread(worker_main, raw);
     *out = s.release();
@@ -434,6 +627,7 @@ painty_status painty_server_submit(painty_server* s, const painty_request* req,
       auto it = s->canvases.find(req->canvas_id);
       PG_REQUIRE(it != s->canvases.end(), "unknown canvas id");
       c = it->second.get();
+      PG_REQUIRE(!c->release, "the canvas was released");
     }
     r->id = s->next_req++;
     r->canvas_id = c->id;
@@ -444,6 +638,24 @@ painty_status painty_server_submit(painty_server* s, const painty_request* req,
     if (request_id) *request_id = r->id;
     if (canvas_id) *canvas_id = c->id;
     s->reqs.emplace(r->id, std::move(r));
+    s->cv_work.notify_one();
+  });
+}
+
+painty_status painty_server_release(painty_server* s, uint64_t canvas_id) {
+  return guard([&] {
+    PG_REQUIRE(s != nullptr, "server is null");
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->canvases.find(canvas_id);
+    PG_REQUIRE(it != s->canvases.end(), "unknown canvas id");
+    ServerCanvas* c = it->second.get();
+    if (c->release) return;
+    c->release = true;
+    if (c->waiting.empty() && !c->busy) {
+      if (c->resident) s->resident -= c->bytes;
+      s->to_drop.push_back(c);
+    }
+    s->gen++;
     s->cv_work.notify_one();
   });
 }
@@ -496,7 +708,9 @@ painty_status painty_server_stats(painty_server* s, painty_server_counters* out)
     out->peak_resident_bytes = s->peak;
     out->active = static_cast<int64_t>(s->active.size());
     out->pending = static_cast<int64_t>(s->pending.size());
-    out->canvases = static_cast<int64_t>(s->canvases.size());
+    int64_t live = 0;
+    for (auto& kv : s->canvases) live += kv.second->release ? 0 : 1;
+    out->canvases = live;
   });
 }
 
@@ -509,14 +723,16 @@ painty_status painty_server_destroy(painty_server* s) {
     }
     s->cv_work.notify_all();
     if (s->worker.joinable()) s->worker.join();
-    for (auto& kv : s->canvases) {
-      ServerCanvas* c = kv.second.get();
-      if (c->brush) painty_brush_destroy(c->brush);
-      if (c->cv) {
-        if (c->resident) painty_canvas_destroy(c->cv);
-        else delete c->cv;  // evicted: no device memory left to free
-      }
+    for (auto& kv : s->canvases)
+      if (!kv.second->dropped) drop(s, kv.second.get());
+    cudaStreamSynchronize(s->stream);
+    for (auto& kv : s->pinned_free) cudaFreeHost(kv.second);
+    for (Slot& sl : s->slots) {
+      cudaEventDestroy(sl.ev);
+      cudaStreamDestroy(sl.st);
     }
+    cudaFreeHost(s->status_words);
+    cudaMemPoolDestroy(s->pool);
     cudaStreamDestroy(s->stream);
     delete s;
   });

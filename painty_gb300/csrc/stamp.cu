@@ -1383,12 +1383,23 @@ void set_radius(painty_brush* b, double radius) {
   b->pickup_clear = true;
 }
 
-void ensure(void** p, size_t* cap, size_t bytes) {
+// Device memory of a brush: cudaMalloc / cudaFree, or stream-ordered from the brush's pool.
+void* brush_alloc(const painty_brush* b, size_t bytes) {
+  return b->pool ? device_alloc_on(bytes, b->pool, b->pool_stream) : device_alloc(bytes);
+}
+void brush_free(const painty_brush* b, void* p) {
+  if (b->pool)
+    device_free_on(p, b->pool_stream);
+  else
+    device_free(p);
+}
+
+void ensure(const painty_brush* b, void** p, size_t* cap, size_t bytes) {
   if (*cap >= bytes && *p) return;
-  if (*p) device_free(*p);
+  if (*p) brush_free(b, *p);
   *p = nullptr;
   *cap = 0;
-  *p = device_alloc(bytes);
+  *p = brush_alloc(b, bytes);
   *cap = bytes;
 }
 
@@ -1590,12 +1601,12 @@ void launch_stamps(painty_canvas* c, painty_brush* b, const StampRec* d_stamps, 
   }
   a.ndisc = plan.ndisc;
   if (plan.big) {
-    ensure(&b->d_owner, &b->d_owner_bytes, cells * sizeof(int));
+    ensure(b, &b->d_owner, &b->d_owner_bytes, cells * sizeof(int));
     a.owner_global = static_cast<int*>(b->d_owner);
   }
   a.cellmap_global = nullptr;
   if (plan.cm_global) {
-    ensure(&b->d_cellmap, &b->d_cellmap_bytes,
+    ensure(b, &b->d_cellmap, &b->d_cellmap_bytes,
            static_cast<size_t>(cl) * 2 * static_cast<size_t>(b->F) * b->F * sizeof(int));
     a.cellmap_global = static_cast<int*>(b->d_cellmap);
   }
@@ -1616,9 +1627,9 @@ int prepare_snapshot(painty_canvas* c, painty_brush* b, cudaStream_t st) {
   int mode = kRingKeep;
   if (!b->has_snapshot || b->snapshot.rows != c->wet.rows || b->snapshot.cols != c->wet.cols ||
       b->snapshot.storage != c->wet.storage) {
-    if (b->has_snapshot) device_free(b->snapshot.base);
+    if (b->has_snapshot) brush_free(b, b->snapshot.base);
     b->has_snapshot = false;
-    void* base = device_alloc(layer_bytes(c->wet.rows, c->wet.cols, c->wet.storage, true));
+    void* base = brush_alloc(b, layer_bytes(c->wet.rows, c->wet.cols, c->wet.storage, true));
     layer_layout(b->snapshot, c->wet.rows, c->wet.cols, c->wet.storage, base, true);
     b->has_snapshot = true;
     PG_CUDA(cudaMemcpyAsync(b->snapshot.base, c->wet.base, c->wet.bytes,
@@ -1636,7 +1647,7 @@ int prepare_snapshot(painty_canvas* c, painty_brush* b, cudaStream_t st) {
 // Device status word and ring state of a brush.
 void ensure_status(painty_brush* b, cudaStream_t st) {
   if (b->d_status) return;
-  b->d_status = static_cast<unsigned*>(device_alloc(16 * sizeof(unsigned)));
+  b->d_status = static_cast<unsigned*>(brush_alloc(b, 16 * sizeof(unsigned)));
   PG_CUDA(cudaMemsetAsync(b->d_status, 0, 16 * sizeof(unsigned), st));
   b->ring_canvas = 0;  // the ring state holds nothing yet
 }
@@ -1661,7 +1672,7 @@ void run_stamps(painty_canvas* c, painty_brush* b, const std::vector<StampRec>& 
   // footprint
   const size_t fp_bytes = static_cast<size_t>(b->F) * b->F * msz;
   if (b->footprint_stale || b->d_footprint_bytes < fp_bytes) {
-    ensure(&b->d_footprint, &b->d_footprint_bytes, fp_bytes);
+    ensure(b, &b->d_footprint, &b->d_footprint_bytes, fp_bytes);
     if (f64) {
       PG_CUDA(cudaMemcpyAsync(b->d_footprint, b->footprint.data(), fp_bytes,
                               cudaMemcpyHostToDevice, st));
@@ -1675,7 +1686,7 @@ void run_stamps(painty_canvas* c, painty_brush* b, const std::vector<StampRec>& 
   // pickup map: cleared by the kernel itself when a dip / new radius is pending
   const size_t pk_bytes = static_cast<size_t>(b->sizeMap) * b->sizeMap * 8 * msz;
   if (b->d_pickup_bytes < pk_bytes) {
-    ensure(&b->d_pickup, &b->d_pickup_bytes, pk_bytes);
+    ensure(b, &b->d_pickup, &b->d_pickup_bytes, pk_bytes);
     b->pickup_clear = true;
   }
   const bool pickup_zero = b->pickup_clear;
@@ -1684,7 +1695,7 @@ void run_stamps(painty_canvas* c, painty_brush* b, const std::vector<StampRec>& 
   const int ring_reset = prepare_snapshot(c, b, st);
   // stamps
   const size_t sbytes = recs.size() * sizeof(StampRec);
-  ensure(&b->d_stamps, &b->d_stamps_bytes, sbytes);
+  ensure(b, &b->d_stamps, &b->d_stamps_bytes, sbytes);
   PG_CUDA(cudaMemcpyAsync(b->d_stamps, recs.data(), sbytes, cudaMemcpyHostToDevice, st));
   const auto* ds = static_cast<const StampRec*>(b->d_stamps);
   const int64_t n = static_cast<int64_t>(recs.size());
@@ -1833,7 +1844,7 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
                "a brush paints either F64 canvases or F32/F16/BF16 canvases, not both");
     ensure_status(b, st);
     const size_t pk_bytes = static_cast<size_t>(b->sizeMap) * b->sizeMap * 8 * msz;
-    ensure(&b->d_pickup, &b->d_pickup_bytes, pk_bytes);
+    ensure(b, &b->d_pickup, &b->d_pickup_bytes, pk_bytes);
     const int ring_reset = per[c].empty() ? kRingKeep : prepare_snapshot(cv, b, st);
     BatchCanvas<TK, TV>& x = bc[c];
     for (int i = 0; i < 3; i++) {
@@ -2188,13 +2199,10 @@ painty_status painty_brush_create(double radius, const double* footprint, int32_
 painty_status painty_brush_destroy(painty_brush* b) {
   return guard([&] {
     if (!b) return;
-    pg::device_free(b->d_footprint);
-    pg::device_free(b->d_pickup);
-    pg::device_free(b->d_owner);
-    pg::device_free(b->d_cellmap);
-    pg::device_free(b->d_stamps);
-    pg::device_free(b->d_status);
-    if (b->has_snapshot) pg::device_free(b->snapshot.base);
+    for (void* d : {b->d_footprint, b->d_pickup, b->d_owner, b->d_cellmap, b->d_stamps,
+                    static_cast<void*>(b->d_status)})
+      pg::brush_free(b, d);
+    if (b->has_snapshot) pg::brush_free(b, b->snapshot.base);
     delete b;
   });
 }
@@ -2251,9 +2259,9 @@ painty_status painty_brush_update_snapshot(painty_brush* b, const painty_canvas*
     const cudaStream_t st = pg::as_stream(stream);
     if (!b->has_snapshot || b->snapshot.rows != c->wet.rows || b->snapshot.cols != c->wet.cols ||
         b->snapshot.storage != c->wet.storage) {
-      if (b->has_snapshot) pg::device_free(b->snapshot.base);
+      if (b->has_snapshot) pg::brush_free(b, b->snapshot.base);
       b->has_snapshot = false;
-      void* base = pg::device_alloc(pg::layer_bytes(c->wet.rows, c->wet.cols, c->wet.storage, true));
+      void* base = pg::brush_alloc(b, pg::layer_bytes(c->wet.rows, c->wet.cols, c->wet.storage, true));
       pg::layer_layout(b->snapshot, c->wet.rows, c->wet.cols, c->wet.storage, base, true);
       b->has_snapshot = true;
     }

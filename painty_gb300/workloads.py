@@ -78,6 +78,18 @@ def mix_single_paint_np(weights: np.ndarray, K: np.ndarray, S: np.ndarray):
     return k, s
 
 
+def mix_paints_np(weights: np.ndarray, K: np.ndarray, S: np.ndarray):
+    """mix_single_paint_np for many weight rows at once (weights (n, pigments)), with the same
+    accumulation order per row: equal to it bit for bit."""
+    W = np.asarray(weights, dtype=np.float64)
+    wsum = np.cumsum(W, axis=1)[:, -1]
+    norm = np.where(np.abs(wsum - 1.0) < 10e-6, 1.0, 1.0 / wsum)
+    nw = norm[:, None] * W
+    k = np.cumsum(nw[:, :, None] * K[None, :, :], axis=1)[:, -1, :]
+    s = np.cumsum(nw[:, :, None] * S[None, :, :], axis=1)[:, -1, :]
+    return k, s
+
+
 @dataclass
 class Stroke:
     path: np.ndarray  # (n, 2) control points, x then y
@@ -153,23 +165,27 @@ def batch_canvases(n: int, seed: int = 2, smin: float = 256, smax: float = 2048,
     """The batching workload: n canvases with side log-uniform in [smin, smax] and aspect
     U[0.5, 2]; strokes per canvas log-uniform in [strokes_min, strokes_max] (optionally capped
     at max_strokes); radius log-uniform in [rmin, rmax]; 8 uniform control points; spacing
-    0.25 r; Dirichlet(0.3) paints. Returns [(rows, cols, R0 (rows, cols, 3))] and strokes as
+    0.25 r; Dirichlet(0.3) paints; substrate R0 ~ U[0.80, 0.95]. Canvas c is drawn from its
+    own generator (seeded with (seed, c)), so canvases are independent of one another.
+    Returns [(rows, cols, R0 (rows, cols, 3) float32)] and strokes as
     (canvas, path, radius, spacing, K, S)."""
-    rng = np.random.default_rng(seed)
     PK, PS = pigments(pigment_seed)
     canvases, strokes_out = [], []
     for c in range(n):
+        rng = np.random.default_rng([seed, c])
         side = float(np.exp(rng.uniform(np.log(smin), np.log(smax))))
         asp = rng.uniform(0.5, 2.0)
         cols, rows = int(side * np.sqrt(asp)), int(side / np.sqrt(asp))
         ns = int(np.exp(rng.uniform(np.log(strokes_min), np.log(strokes_max))))
         if max_strokes is not None:
             ns = min(ns, max_strokes)
-        canvases.append((rows, cols, rng.uniform(0.80, 0.95, (rows, cols, 3)).astype(np.float32)))
-        for _ in range(ns):
-            path = np.stack([rng.uniform(0, cols, 8), rng.uniform(0, rows, 8)], axis=1)
-            r = float(np.exp(rng.uniform(np.log(rmin), np.log(rmax))))
-            w = rng.dirichlet(np.full(len(PK), 0.3))
-            k, s = mix_single_paint_np(w, PK, PS)
-            strokes_out.append((c, path, r, 0.25 * r, k, s))
+        r0 = (0.80 + 0.15 * rng.random((rows, cols, 3), dtype=np.float32)).astype(np.float32)
+        canvases.append((rows, cols, r0))
+        u = rng.random((ns, 8, 2))
+        paths = u * np.array([cols, rows], dtype=np.float64)
+        radii = np.exp(rng.uniform(np.log(rmin), np.log(rmax), ns))
+        K, S = mix_paints_np(rng.dirichlet(np.full(len(PK), 0.3), ns), PK, PS)
+        for j in range(ns):
+            r = float(radii[j])
+            strokes_out.append((c, np.ascontiguousarray(paths[j]), r, 0.25 * r, K[j], S[j]))
     return canvases, strokes_out
