@@ -8,8 +8,10 @@ substrate R0 ~ U[0.8,0.95], output RGB reflectance. Metric: Mpixel-composites/s,
 counted once it has gone through all 8 layers. One step = one fused composite launch over
 resident inputs (4.2 GB per step, above the 129 MB L2, so no L2 flush is needed).
 
-`e2e` is the same metric through the C ABI with host buffers: each step uploads the 8
-layers and R0 from pinned host memory, composites, and downloads the RGB result.
+`e2e` is the same metric through the C ABI with host buffers: each step is one
+painty_compose_layers_host call that uploads the 8 layers and R0 from pinned host memory,
+composites and downloads the RGB result, its transfers pipelined in row bands; the line also
+carries this box's measured host-link bandwidth and the step's fraction of that bound.
 
 Secondary (the `stamps` object): the plain imprint-brush case -- a 1024 x 768 FP32 canvas,
 200 Catmull-Rom strokes of radius U[8,32] at 0.25 r spacing through the C ABI -- as
@@ -464,17 +466,12 @@ def run_ours(args):
     torch.cuda.synchronize()
     unfused_value = npix * args.steps / (u0.elapsed_time(u1) / 1e3) / 1e6
 
-    # ---- end to end through the C ABI with host buffers
+    # ---- end to end through the C ABI with host buffers: painty_compose_layers_host
+    # (pinned host stacks in, pinned host image out, transfers pipelined in row bands)
     out_host = torch.empty((3, ROWS, COLS), dtype=torch.float32, pin_memory=True).numpy()
 
     def e2e_step():
-        for l in range(LAYERS):
-            layers[l].upload("K", Kh[l], planar=True)
-            layers[l].upload("S", Sh[l], planar=True)
-            layers[l].upload("V", Vh[l], planar=True)
-        r0.upload(R0h, planar=True)
-        pg.compose_layers(layers, r0, out)
-        out.download(out=out_host, planar=True)
+        pg.compose_layers_host(Kh, Sh, Vh, R0h, out=out_host)
 
     e2e_step()
     barrier()
@@ -484,6 +481,7 @@ def run_ours(args):
         e2e_step()
     barrier()
     e2e_s = (time.perf_counter() - tw) / e_steps
+    link = host_link(torch)
     if ws > 1:
         import torch.distributed as dist
         t = torch.tensor([e2e_s], device="cuda")
@@ -522,7 +520,11 @@ def run_ours(args):
                          "kernel_ms": round(kern_ms, 4)},
             "e2e": {"value": round(ws * npix / e2e_s / 1e6, 2), "unit": "Mpix/s",
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "ms_per_step": round(e2e_s * 1e3, 2)},
+                    "ms_per_step": round(e2e_s * 1e3, 2),
+                    "call": "painty_compose_layers_host (pinned host buffers)",
+                    "host_link": link,
+                    "link_bound_ms": round(h2d / (link["h2d_gbs"] * 1e9) * 1e3, 2),
+                    "frac_of_link_bound": round(h2d / (link["h2d_gbs"] * 1e9) / e2e_s, 3)},
             "gpu_launches": launches,
             "unfused_value": round(unfused_value, 2),
             "clocks": clocks.summary(),
@@ -542,6 +544,26 @@ def run_ours(args):
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def host_link(torch, nbytes: int = 1 << 30, reps: int = 5):
+    """Measured host <-> device copy bandwidth of this machine: one pinned 1 GiB buffer copied
+    each way, best of `reps` (GB/s)."""
+    h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    out = {}
+    for name, fn in (("h2d_gbs", lambda: d.copy_(h, non_blocking=True)),
+                     ("d2h_gbs", lambda: h.copy_(d, non_blocking=True))):
+        best = 1e30
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            best = min(best, time.perf_counter() - t)
+        out[name] = round(nbytes / best / 1e9, 1)
+    del h, d
+    return out
 
 
 def run_stamps_config0(pg, torch, nstrokes: int = 200, cpu: bool = False):

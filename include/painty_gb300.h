@@ -78,6 +78,12 @@ typedef struct painty_brush painty_brush;   /* FootprintBrush<vec3> */
 
 /* ------------------------------------------------------------------ library */
 int32_t painty_abi_version(void);
+/* Build properties of the loaded library: PAINTY_BUILD_BOUNDS_CHECK is set in the
+ * bounds-checked build (libpainty_gb300_checked.so), whose stamp kernels test every computed
+ * index against its buffer and return PAINTY_ERR_CUDA naming the access instead of faulting.
+ * No counterpart in painty. */
+#define PAINTY_BUILD_BOUNDS_CHECK 1
+int32_t painty_build_flags(void);
 const char* painty_status_string(painty_status s);
 const char* painty_last_error(void);
 /* Number of this library's kernel launches so far in this process (all devices). */
@@ -128,6 +134,16 @@ painty_status painty_compose_layers(const painty_layer* const* layers, int32_t L
 painty_status painty_compose_layers_unfused(const painty_layer* const* layers, int32_t L,
                                             const painty_image* r0, painty_image* out,
                                             void* stream);
+/* Renderer::compose of layer stacks held in host memory into a host image
+ * (painty/renderer/Renderer.hxx:26-53, returning a host Mat; per layer PaintLayer.hxx:81-96):
+ * the composite of painty_compose_layers with the transfers pipelined in row bands on three
+ * internal streams, so the upload of one band, the composite of another and the download of a
+ * third overlap. Host layout, FP32 planar, rows x cols per plane, contiguous: K and S
+ * [L][3][rows][cols], V [L][rows][cols], R0 and out [3][rows][cols]. Pinned host buffers give
+ * full host-link speed. Returns once `out` holds the result; `stream` is waited on first. */
+painty_status painty_compose_layers_host(const float* K, const float* S, const float* V,
+                                         int32_t L, const float* R0, float* out, int32_t rows,
+                                         int32_t cols, void* stream);
 
 /* ------------------------------------------------------------------ canvas
  * replaces Canvas<vec>::Canvas(rows, cols) (painty/renderer/Canvas.hxx:26-35): wet layer

@@ -24,7 +24,11 @@ from pathlib import Path
 import numpy as np
 
 _HERE = Path(__file__).resolve().parent
-LIB_PATH = _HERE / "_lib" / "libpainty_gb300.so"
+# PAINTY_BOUNDS_CHECK=1 loads the bounds-checked build of the library (the stamp kernels test
+# every computed index before the access and raise instead of faulting)
+BOUNDS_CHECKED = os.environ.get("PAINTY_BOUNDS_CHECK", "") not in ("", "0")
+LIB_PATH = _HERE / "_lib" / ("libpainty_gb300_checked.so" if BOUNDS_CHECKED
+                             else "libpainty_gb300.so")
 
 if not LIB_PATH.exists():
     raise ImportError(
@@ -48,6 +52,7 @@ def _sig(name, *args, res=C.c_int):
 
 
 _sig("painty_abi_version", res=_I32)
+_sig("painty_build_flags", res=_I32)
 _sig("painty_status_string", C.c_int, res=C.c_char_p)
 _sig("painty_last_error", res=C.c_char_p)
 _sig("painty_kernel_launch_count", res=_I64)
@@ -66,6 +71,7 @@ _sig("painty_image_upload", _P, _P, C.c_int, _P)
 _sig("painty_image_download", _P, _P, C.c_int, _P)
 _sig("painty_compose_layers", _P, _I32, _P, _P, _P)
 _sig("painty_compose_layers_unfused", _P, _I32, _P, _P, _P)
+_sig("painty_compose_layers_host", _P, _P, _P, _I32, _P, _P, _I32, _I32, _P)
 _sig("painty_canvas_create", _I32, _I32, C.c_int, C.POINTER(_P))
 _sig("painty_canvas_destroy", _P)
 _sig("painty_canvas_clear", _P, _P)
@@ -144,6 +150,11 @@ def _check(status: int) -> None:
     if status == 2:
         raise MemoryError(msg)
     raise PaintyError(status, msg)
+
+
+def bounds_checked() -> bool:
+    """Whether the loaded library is the bounds-checked build."""
+    return bool(_lib.painty_build_flags() & 1)
 
 
 def kernel_launch_count() -> int:
@@ -295,6 +306,29 @@ def compose_layers(layers, r0: Image, out: Image, fused: bool = True, stream=Non
     arr = (_P * max(1, len(layers)))(*[l._h for l in layers])
     fn = _lib.painty_compose_layers if fused else _lib.painty_compose_layers_unfused
     _check(fn(arr, len(layers), r0._h, out._h, _stream(stream)))
+
+
+def compose_layers_host(K: np.ndarray, S: np.ndarray, V: np.ndarray, R0: np.ndarray,
+                        out: np.ndarray | None = None, stream=None) -> np.ndarray:
+    """Renderer::compose of host layer stacks into a host image in one call, the transfers
+    pipelined in row bands: K, S float32 (L, 3, rows, cols), V (L, rows, cols), R0 and the
+    result (3, rows, cols). Pinned host arrays give full host-link speed."""
+    R0 = np.ascontiguousarray(R0, dtype=np.float32)
+    if R0.ndim != 3 or R0.shape[0] != 3:
+        raise ValueError("R0 must be (3, rows, cols)")
+    rows, cols = R0.shape[1:]
+    L = V.shape[0]
+    arrs = [np.ascontiguousarray(a, dtype=np.float32) for a in (K, S, V)]
+    if arrs[0].shape != (L, 3, rows, cols) or arrs[1].shape != (L, 3, rows, cols) or \
+            arrs[2].shape != (L, rows, cols):
+        raise ValueError("K, S must be (L, 3, rows, cols) and V (L, rows, cols)")
+    if out is None:
+        out = np.empty((3, rows, cols), dtype=np.float32)
+    elif out.shape != (3, rows, cols) or out.dtype != np.float32 or not out.flags["C_CONTIGUOUS"]:
+        raise ValueError("out must be a C-contiguous float32 array of (3, rows, cols)")
+    _check(_lib.painty_compose_layers_host(_ptr(arrs[0]), _ptr(arrs[1]), _ptr(arrs[2]), L,
+                                           _ptr(R0), _ptr(out), rows, cols, _stream(stream)))
+    return out
 
 
 class Canvas:

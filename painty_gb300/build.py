@@ -21,6 +21,10 @@ ROOT = HERE.parent
 CSRC = HERE / "csrc"
 OUT_DIR = HERE / "_lib"
 LIB = OUT_DIR / "libpainty_gb300.so"
+# The bounds-checked build of the same library (PAINTY_BOUNDS_CHECK): the stamp kernels test
+# every computed index against its buffer before the access and report instead of faulting.
+LIB_CHECKED = OUT_DIR / "libpainty_gb300_checked.so"
+CHECKED_SOURCES = {"stamp.cu"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -46,10 +50,10 @@ def sources() -> list[Path]:
 NO_FMAD = {"texture.cu", "canvas_gpu.cu"}
 
 
-def _compile(src: Path, obj: Path) -> None:
+def _compile(src: Path, obj: Path, defines=()) -> None:
     cmd = [nvcc(), *ARCH, "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-Wall", "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr", "-I", str(ROOT / "include"),
-           "-I", str(CSRC), "-c", str(src), "-o", str(obj)]
+           "-I", str(CSRC), *[f"-D{d}" for d in defines], "-c", str(src), "-o", str(obj)]
     if src.name in NO_FMAD:
         cmd.insert(1, "--fmad=false")
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -57,29 +61,43 @@ def _compile(src: Path, obj: Path) -> None:
         raise RuntimeError(f"nvcc failed for {src.name}:\n{r.stdout}\n{r.stderr}")
 
 
-def build(verbose: bool = False) -> Path:
-    OUT_DIR.mkdir(exist_ok=True)
-    objs = []
-    jobs = []
-    with cf.ThreadPoolExecutor(max_workers=max(1, min(len(sources()), os.cpu_count() or 4))) as ex:
-        for src in sources():
-            obj = OUT_DIR / (src.stem + ".o")
-            objs.append(obj)
-            jobs.append(ex.submit(_compile, src, obj))
-        for j in jobs:
-            j.result()
+def _link(objs, lib: Path) -> None:
     libdir = cuda_lib_dir()
-    tmp = LIB.with_suffix(".so.tmp")
+    tmp = lib.with_suffix(".so.tmp")
     cmd = [nvcc(), *ARCH, "-shared", "-cudart", "shared", "-o", str(tmp), *map(str, objs),
            "-Xlinker", f"-rpath={libdir}", "-L", libdir]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
-    for o in objs:
+    os.replace(tmp, lib)
+
+
+def build(verbose: bool = False, checked: bool = True) -> Path:
+    """Builds the library and, with `checked`, its bounds-checked twin (the translation units
+    in CHECKED_SOURCES compiled again with PAINTY_BOUNDS_CHECK, the rest shared)."""
+    OUT_DIR.mkdir(exist_ok=True)
+    objs, checked_objs, jobs = [], [], []
+    srcs = sources()
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(len(srcs) + 1, os.cpu_count() or 4))) as ex:
+        for src in srcs:
+            obj = OUT_DIR / (src.stem + ".o")
+            objs.append(obj)
+            jobs.append(ex.submit(_compile, src, obj))
+            if checked and src.name in CHECKED_SOURCES:
+                cobj = OUT_DIR / (src.stem + "_checked.o")
+                checked_objs.append(cobj)
+                jobs.append(ex.submit(_compile, src, cobj, ("PAINTY_BOUNDS_CHECK=1",)))
+            else:
+                checked_objs.append(obj)
+        for j in jobs:
+            j.result()
+    _link(objs, LIB)
+    if checked:
+        _link(checked_objs, LIB_CHECKED)
+    for o in set(objs) | set(checked_objs):
         o.unlink(missing_ok=True)
     if verbose:
-        print(f"built {LIB}")
+        print(f"built {LIB}" + (f" and {LIB_CHECKED}" if checked else ""))
     return LIB
 
 

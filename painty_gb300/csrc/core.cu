@@ -541,6 +541,78 @@ __global__ void __launch_bounds__(256) km_composite_kernel(
 
 // Composite over layers of any layout (a canvas's packed wet layer, or mixed stacks): one
 // thread per pixel, each layer's values read with its element stride.
+// 16-bit layer storage (FP16 / BF16 K and S, FP16 V): 4 pixels per thread, each plane read
+// as one 8-byte vector, and the next layer's 7 vectors loaded before this layer is computed,
+// so a thread keeps a layer's loads in flight while its KM arithmetic runs (FP32 math, R0 and
+// the result in FP32).
+template <class TK, class TV>
+struct Compose16Args {
+  const TK* K[kMaxLayersPerLaunch][3];
+  const TK* S[kMaxLayersPerLaunch][3];
+  const TV* V[kMaxLayersPerLaunch];
+  const float* r0[3];
+  float* out[3];
+  int32_t L;
+  int64_t groups;  // plane elements / 4
+};
+struct Layer16 {  // one layer's 4 pixels: K r,g,b, S r,g,b, V as packed 16-bit pairs
+  uint2 k[3], s[3], v;
+};
+template <class T>
+__device__ __forceinline__ float elem16(const uint2& w, int i) {
+  const uint32_t word = i < 2 ? w.x : w.y;
+  const unsigned short h = static_cast<unsigned short>((i & 1) ? word >> 16 : word & 0xffffu);
+  T t;
+  memcpy(&t, &h, 2);
+  return to_f(t);
+}
+template <class TK, class TV>
+__device__ __forceinline__ void load_layer16(const Compose16Args<TK, TV>& a, int l, int64_t e,
+                                             Layer16& o) {
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    o.k[c] = ld_stream_u2(a.K[l][c] + e);
+    o.s[c] = ld_stream_u2(a.S[l][c] + e);
+  }
+  o.v = ld_stream_u2(a.V[l] + e);
+}
+template <class TK, class TV>
+__global__ void __launch_bounds__(256) km_composite16_kernel(
+  const __grid_constant__ Compose16Args<TK, TV> a) {
+  const int64_t groups = a.groups;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t g = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; g < groups;
+       g += stride) {
+    const int64_t e = g * 4;
+    float r[3][4];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      const uint4 t = ld_stream_u4(a.r0[c] + e);
+      r[c][0] = __uint_as_float(t.x);
+      r[c][1] = __uint_as_float(t.y);
+      r[c][2] = __uint_as_float(t.z);
+      r[c][3] = __uint_as_float(t.w);
+    }
+    Layer16 cur, nxt;
+    load_layer16(a, 0, e, cur);
+    for (int l = 0; l < a.L; l++) {
+      if (l + 1 < a.L) load_layer16(a, l + 1, e, nxt);
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        const float d = elem16<TV>(cur.v, i);
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+          r[c][i] = km_reflectance(elem16<TK>(cur.k[c], i), elem16<TK>(cur.s[c], i), r[c][i], d);
+      }
+      cur = nxt;
+    }
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+      st_stream_u4(a.out[c] + e, make_uint4(__float_as_uint(r[c][0]), __float_as_uint(r[c][1]),
+                                            __float_as_uint(r[c][2]), __float_as_uint(r[c][3])));
+  }
+}
+
 template <class TK, class TV, class TR>
 struct ComposeStridedArgs {
   const TK* K[kMaxLayersPerLaunch][3];
@@ -619,6 +691,38 @@ void compose_strided(const painty_layer* const* layers, int32_t L, const painty_
   }
 }
 
+template <class TK, class TV>
+void compose16(const painty_layer* const* layers, int32_t L, const painty_image* r0,
+               painty_image* out, cudaStream_t st) {
+  const int64_t elems = r0->plane_elems();  // a multiple of 64 elements
+  auto kern = km_composite16_kernel<TK, TV>;
+  const int wave = resident_grid(kern, 256);
+  for (int32_t l0 = 0; l0 < L; l0 += kMaxLayersPerLaunch) {
+    Compose16Args<TK, TV> a{};
+    const int32_t n = std::min<int32_t>(kMaxLayersPerLaunch, L - l0);
+    for (int32_t i = 0; i < n; i++) {
+      const painty_layer* ly = layers[l0 + i];
+      for (int c = 0; c < 3; c++) {
+        a.K[i][c] = static_cast<const TK*>(ly->K[c]);
+        a.S[i][c] = static_cast<const TK*>(ly->S[c]);
+      }
+      a.V[i] = static_cast<const TV*>(ly->V);
+    }
+    const painty_image* src = l0 == 0 ? r0 : out;
+    for (int c = 0; c < 3; c++) {
+      a.r0[c] = static_cast<const float*>(src->R[c]);
+      a.out[c] = static_cast<float*>(out->R[c]);
+    }
+    a.L = n;
+    a.groups = elems / 4;
+    const int64_t blocks_needed = (a.groups + 255) / 256;
+    const int grid = static_cast<int>(std::min<int64_t>(blocks_needed, wave));
+    kern<<<std::max(grid, 1), 256, 0, st>>>(a);
+    count_launch();
+    PG_CUDA(cudaGetLastError());
+  }
+}
+
 template <class TK, class TV, class TR>
 void compose_typed(const painty_layer* const* layers, int32_t L, const painty_image* r0,
                    painty_image* out, cudaStream_t st) {
@@ -627,6 +731,9 @@ void compose_typed(const painty_layer* const* layers, int32_t L, const painty_im
       compose_strided<TK, TV, TR>(layers, L, r0, out, st);
       return;
     }
+  if constexpr (sizeof(TK) == 2) {
+    compose16<TK, TV>(layers, L, r0, out, st);
+  } else {
   constexpr int PIX = 16 / sizeof(TK);
   const int64_t elems = r0->plane_elems();  // a multiple of 64 elements
   auto kern = km_composite_kernel<TK, TV, TR>;
@@ -654,6 +761,7 @@ void compose_typed(const painty_layer* const* layers, int32_t L, const painty_im
     kern<<<std::max(grid, 1), 256, 0, st>>>(a);
     count_launch();
     PG_CUDA(cudaGetLastError());
+  }
   }
 }
 
@@ -1016,6 +1124,113 @@ painty_status painty_compose_layers_unfused(const painty_layer* const* layers, i
     }
     pg::launch_compose(layers, 1, r0, out, pg::as_stream(stream));
     for (int32_t l = 1; l < L; l++) pg::launch_compose(layers + l, 1, out, out, pg::as_stream(stream));
+  });
+}
+
+painty_status painty_compose_layers_host(const float* K, const float* S, const float* V,
+                                         int32_t L, const float* R0, float* out, int32_t rows,
+                                         int32_t cols, void* stream) {
+  return guard([&] {
+    PG_REQUIRE(rows > 0 && cols > 0, "rows and cols must be positive");
+    PG_REQUIRE(L >= 0 && (L == 0 || (K && S && V)), "layer planes are null");
+    PG_REQUIRE(R0 && out, "R0 or out is null");
+    constexpr int kStreams = 3;
+    const int64_t pitch = pg::pitch_for(cols);
+    // bands of about 16 MB of layer data each
+    const int64_t row_bytes = static_cast<int64_t>(7 * L + 6) * pitch * 4;
+    const int32_t band = static_cast<int32_t>(
+      std::max<int64_t>(1, std::min<int64_t>(rows, (int64_t(16) << 20) / row_bytes)));
+    const int64_t plane = static_cast<int64_t>(band) * pitch;  // device plane of one band
+    const int64_t nplanes = 7 * static_cast<int64_t>(L) + 6;   // K, S, V, R0, out
+    PG_CUDA(cudaStreamSynchronize(pg::as_stream(stream)));
+    cudaStream_t st[kStreams] = {};
+    void* buf[kStreams] = {};
+    auto cleanup = [&] {
+      for (int i = 0; i < kStreams; i++) {
+        if (buf[i]) cudaFreeAsync(buf[i], st[i]);
+        if (st[i]) {
+          cudaStreamSynchronize(st[i]);
+          cudaStreamDestroy(st[i]);
+        }
+      }
+    };
+    try {
+      for (int i = 0; i < kStreams; i++) {
+        PG_CUDA(cudaStreamCreateWithFlags(&st[i], cudaStreamNonBlocking));
+        PG_CUDA(cudaMallocAsync(&buf[i], static_cast<size_t>(nplanes * plane) * 4, st[i]));
+        // the pitch padding is computed on but never copied out: start it at zero
+        PG_CUDA(cudaMemsetAsync(buf[i], 0, static_cast<size_t>(nplanes * plane) * 4, st[i]));
+      }
+      // host planes [n][rows][cols] <-> device planes [n][band][pitch], rows r0 .. r0 + h
+      auto copy3d = [&](const float* hbase, float* dbase, int n, int32_t r0, int32_t h,
+                        bool up, cudaStream_t s) {
+        cudaMemcpy3DParms m{};
+        cudaPitchedPtr hp = make_cudaPitchedPtr(const_cast<float*>(hbase), cols * 4, cols, rows);
+        cudaPitchedPtr dp = make_cudaPitchedPtr(dbase, pitch * 4, pitch, band);
+        m.extent = make_cudaExtent(static_cast<size_t>(cols) * 4, h, n);
+        if (up) {
+          m.srcPtr = hp;
+          m.srcPos = make_cudaPos(0, r0, 0);
+          m.dstPtr = dp;
+          m.kind = cudaMemcpyHostToDevice;
+        } else {
+          m.srcPtr = dp;
+          m.dstPtr = hp;
+          m.dstPos = make_cudaPos(0, r0, 0);
+          m.kind = cudaMemcpyDeviceToHost;
+        }
+        PG_CUDA(cudaMemcpy3DAsync(&m, s));
+      };
+      std::vector<painty_layer> views(static_cast<size_t>(L));
+      std::vector<const painty_layer*> lp(static_cast<size_t>(L));
+      int b = 0;
+      for (int32_t r0 = 0; r0 < rows; r0 += band, b++) {
+        const int32_t h = std::min(band, rows - r0);
+        cudaStream_t s = st[b % kStreams];
+        float* d = static_cast<float*>(buf[b % kStreams]);
+        float* dK = d;
+        float* dS = dK + 3 * static_cast<int64_t>(L) * plane;
+        float* dV = dS + 3 * static_cast<int64_t>(L) * plane;
+        float* dR = dV + static_cast<int64_t>(L) * plane;
+        float* dO = dR + 3 * plane;
+        if (L > 0) {
+          copy3d(K, dK, 3 * L, r0, h, true, s);
+          copy3d(S, dS, 3 * L, r0, h, true, s);
+          copy3d(V, dV, L, r0, h, true, s);
+        }
+        copy3d(R0, dR, 3, r0, h, true, s);
+        for (int32_t l = 0; l < L; l++) {
+          painty_layer& ly = views[l];
+          ly.rows = h;
+          ly.cols = cols;
+          ly.pitch = pitch;
+          ly.storage = PAINTY_STORAGE_F32;
+          for (int c = 0; c < 3; c++) {
+            ly.K[c] = dK + (3 * static_cast<int64_t>(l) + c) * plane;
+            ly.S[c] = dS + (3 * static_cast<int64_t>(l) + c) * plane;
+          }
+          ly.V = dV + static_cast<int64_t>(l) * plane;
+          ly.owned = false;
+          lp[l] = &ly;
+        }
+        painty_image ir{}, io{};
+        ir.rows = io.rows = h;
+        ir.cols = io.cols = cols;
+        ir.pitch = io.pitch = pitch;
+        ir.storage = io.storage = PAINTY_STORAGE_F32;
+        ir.owned = io.owned = false;
+        for (int c = 0; c < 3; c++) {
+          ir.R[c] = dR + c * plane;
+          io.R[c] = dO + c * plane;
+        }
+        pg::launch_compose(lp.data(), L, &ir, &io, s);
+        copy3d(out, dO, 3, r0, h, false, s);
+      }
+    } catch (...) {
+      cleanup();
+      throw;
+    }
+    cleanup();
   });
 }
 

@@ -80,6 +80,39 @@ __device__ __forceinline__ void st_elem_sr(T* p, M v, uint32_t r) {
   *p = to_store_sr<T>(v, r);
 }
 
+// ------------------------------------------------------------------ bounds-checked builds
+// A library built with PAINTY_BOUNDS_CHECK (libpainty_gb300_checked.so) tests the computed
+// indices of the stamp kernels against their buffers' extents before each access. An index
+// outside is recorded -- bit kStatusBounds in status word 0, the first such access's kind in
+// word 4 and its index in word 5 -- and the access is skipped instead of faulting. The host
+// turns a recorded access into an error naming them.
+#ifdef PAINTY_BOUNDS_CHECK
+constexpr bool kBoundsCheck = true;
+#else
+constexpr bool kBoundsCheck = false;
+#endif
+constexpr unsigned kStatusBounds = 4u;
+enum BoundsKind : unsigned {
+  kBoundsCanvas = 1,    // canvas / snapshot pixel record
+  kBoundsCell = 2,      // pickup-map cell
+  kBoundsFootprint = 3, // footprint height
+  kBoundsCellMap = 4,   // per-stamp cell map
+  kBoundsOwner = 5,     // owner table
+};
+__device__ __forceinline__ bool in_bounds(unsigned* status, unsigned kind, int64_t idx,
+                                          int64_t n) {
+  if constexpr (!kBoundsCheck) {
+    return true;
+  } else {
+    if (idx >= 0 && idx < n) return true;
+    if (status) {
+      atomicOr(status, kStatusBounds);
+      if (atomicCAS(status + 4, 0u, kind) == 0u) atomicExch(status + 5, static_cast<unsigned>(idx));
+    }
+    return false;
+  }
+}
+
 // ------------------------------------------------------------------ thread-block clusters
 // Rank of this CTA in its cluster and the cluster's size (1 and 0 without a cluster launch).
 __device__ __forceinline__ unsigned cluster_rank() {
@@ -148,6 +181,13 @@ __device__ __forceinline__ uint4 ld_stream_u4(const void* p) {
   uint4 r;
   asm volatile("ld.global.nc.L1::no_allocate.v4.u32 {%0,%1,%2,%3}, [%4];"
                : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+               : "l"(p));
+  return r;
+}
+__device__ __forceinline__ uint2 ld_stream_u2(const void* p) {
+  uint2 r;
+  asm volatile("ld.global.nc.L1::no_allocate.v2.u32 {%0,%1}, [%2];"
+               : "=r"(r.x), "=r"(r.y)
                : "l"(p));
   return r;
 }

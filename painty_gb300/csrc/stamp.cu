@@ -202,6 +202,9 @@ template <bool PS, bool CG, bool PK, class TK, class TV, class M>
 __device__ __forceinline__ void process_pixel(const StampArgs<TK, TV>& a, M* pbase, int cells,
                                               M fp, int c, int m, uint32_t seed, bool snap) {
   using A = Arith<M>;
+  if (!in_bounds(a.status, kBoundsCanvas, c, static_cast<int64_t>(a.rows) * a.pitch) ||
+      !in_bounds(a.status, kBoundsCell, m, static_cast<int64_t>(a.S) * a.S))
+    return;
   // 16-bit storage rounds its stores stochastically (bits from the canvas's stamp count and
   // the pixel; independent of how stamps are grouped into launches)
   constexpr bool kSR = sizeof(TK) == 2;
@@ -376,7 +379,9 @@ __device__ __forceinline__ PixelInfo pixel_info(const StampArgs<TK, TV>& a, cons
   const bool inside = p.yc >= 0 && p.xc >= 0 && p.xc < a.cols && p.yc < a.rows && p.my >= 0 &&
                       p.mx >= 0 && p.mx < a.S && p.my < a.S;
   M fp = M(0);
-  if (inside && p.mx < a.F && p.my < a.F) fp = fps[p.my * a.F + p.mx];
+  if (inside && p.mx < a.F && p.my < a.F &&
+      in_bounds(a.status, kBoundsFootprint, p.my * a.F + p.mx, static_cast<int64_t>(a.F) * a.F))
+    fp = fps[p.my * a.F + p.mx];
   *fp_out = fp;
   p.live = inside && fp > M(0);
   return p;
@@ -598,7 +603,9 @@ __device__ __forceinline__ void refresh_ring(const StampArgs<TK, TV>& a, const R
           const int bx = x - x0, by = y - y0;
           take = !(bx >= 0 && by >= 0 && bx < F && by < F && skip[by * F + bx] >= 0);
         }
-        if (take) off[u] = static_cast<int64_t>(y) * a.pitch + x;
+        if (take && in_bounds(a.status, kBoundsCanvas, static_cast<int64_t>(y) * a.pitch + x,
+                              static_cast<int64_t>(a.rows) * a.pitch))
+          off[u] = static_cast<int64_t>(y) * a.pitch + x;
       }
     }
     if constexpr (PK) {  // whole pixel records
@@ -675,7 +682,8 @@ __device__ __forceinline__ void classify_disc(const StampArgs<TK, TV>& a, const 
     const int row = static_cast<int>(e >> 16), col = static_cast<int>(e & 0xffffu);
     M fp;
     const PixelInfo p = pixel_info(a, sp, xs, ys, fps, row, col, &fp);
-    cellmap[row * F + col] = p.live ? ((p.my << 16) | p.mx) : -1;
+    if (in_bounds(a.status, kBoundsCellMap, row * F + col, static_cast<int64_t>(F) * F))
+      cellmap[row * F + col] = p.live ? ((p.my << 16) | p.mx) : -1;
   }
 }
 
@@ -703,6 +711,8 @@ __device__ __forceinline__ void paint_disc(const StampArgs<TK, TV>& a, const int
   for (int i = first + tid; i < last; i += T) {
     const uint32_t e = disc[i];
     const int row = static_cast<int>(e >> 16), col = static_cast<int>(e & 0xffffu);
+    if (!in_bounds(a.status, kBoundsCellMap, row * F + col, static_cast<int64_t>(F) * F))
+      continue;
     const int* cm = cellmap + row * F + col;
     const int m = cm[0];
     if (m < 0) continue;
@@ -717,6 +727,7 @@ __device__ __forceinline__ void paint_disc(const StampArgs<TK, TV>& a, const int
     if (d && cm[F] == m) follow |= 4u;
     if (d && r && cm[F + 1] == m) follow |= 8u;
     const int mx = m & 0xffff, my = m >> 16;
+    if (!in_bounds(a.status, kBoundsFootprint, my * F + mx, static_cast<int64_t>(F) * F)) continue;
     const M fp = fps[my * F + mx];
     const int cell = my * S + mx;
     process_pixel<PS, CG, PK, TK, TV, M>(a, pbase, cells, fp, ys[row] * pitch32 + xs[col], cell,
@@ -763,7 +774,7 @@ __device__ __noinline__ int paint_waves(const StampArgs<TK, TV>& a, const StampP
       if (dc * dc + dr * dr <= a.support2) {
         M fp;
         const PixelInfo p = pixel_info(a, sp, xs, ys, fps, row, col, &fp);
-        if (p.live) {
+        if (p.live && in_bounds(a.status, kBoundsOwner, p.my * S + p.mx, cells)) {
           lv = true;
           atomicMin(&own[p.my * S + p.mx], key_hi | (row * F + col));
         }
@@ -1644,6 +1655,17 @@ int prepare_snapshot(painty_canvas* c, painty_brush* b, cudaStream_t st) {
   return mode;
 }
 
+// A stamp launch's status words (0: status bits, 4 and 5: the first out-of-range access of a
+// bounds-checked build) as an error.
+void check_stamp_status(const unsigned* w, const char* what) {
+  if (w[0] == 0) return;
+  if (w[0] & kStatusBounds)
+    fail(PAINTY_ERR_CUDA, std::string(what) + ": bounds check: access kind " +
+                            std::to_string(w[4]) + " at index " +
+                            std::to_string(static_cast<int32_t>(w[5])) + " out of range");
+  fail(PAINTY_ERR_CUDA, std::string(what) + " reported an internal error");
+}
+
 // Device status word and ring state of a brush.
 void ensure_status(painty_brush* b, cudaStream_t st) {
   if (b->d_status) return;
@@ -1721,10 +1743,10 @@ void run_stamps(painty_canvas* c, painty_brush* b, const std::vector<StampRec>& 
     b->ring_version = c->version;
   }
   // the stamp records live in a reused buffer: finish before returning
-  unsigned status = 0;
-  PG_CUDA(cudaMemcpyAsync(&status, b->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+  unsigned status[6] = {};
+  PG_CUDA(cudaMemcpyAsync(status, b->d_status, sizeof(status), cudaMemcpyDeviceToHost, st));
   PG_CUDA(cudaStreamSynchronize(st));
-  if (status != 0) fail(PAINTY_ERR_CUDA, "stamp kernel reported an internal error");
+  check_stamp_status(status, "stamp kernel");
 }
 
 
@@ -1937,8 +1959,9 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   const int64_t cmstride = static_cast<int64_t>(cl) * 2 * fmax_cm * fmax_cm;
   void* d_scratch_cm = nullptr;
   PG_CUDA(cudaMallocAsync(&d_scratch_cm, std::max<int64_t>(slots * cmstride, 4) * sizeof(int), st));
-  PG_CUDA(cudaMallocAsync(&d_counter, sizeof(int) * (2 + slots), st));
-  PG_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(int) * (2 + slots), st));
+  // counter, status words 1..7 (bounds-check records at status + 4, + 5), claims
+  PG_CUDA(cudaMallocAsync(&d_counter, sizeof(int) * (8 + slots), st));
+  PG_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(int) * (8 + slots), st));
   BatchArgs<TK, TV> a{};
   a.canvases = static_cast<const BatchCanvas<TK, TV>*>(d_canvas);
   a.strokes = static_cast<const BatchStroke*>(d_strokes);
@@ -1948,7 +1971,7 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   a.ncanvas = nc;
   a.counter = static_cast<int*>(d_counter);
   a.status = reinterpret_cast<unsigned*>(static_cast<int*>(d_counter) + 1);
-  a.claims = static_cast<int*>(d_counter) + 2;
+  a.claims = static_cast<int*>(d_counter) + 8;
   a.scratch_pickup = static_cast<M*>(d_scratch_p);
   a.scratch_owner = static_cast<int*>(d_scratch_o);
   a.scratch_cellmap = static_cast<int*>(d_scratch_cm);
@@ -1958,9 +1981,10 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   launch_clustered(kern, grid, cl, std::max<size_t>(dyn, 16), st, a);
   count_launch();
   PG_CUDA(cudaGetLastError());
-  unsigned status = 0;
-  PG_CUDA(cudaMemcpyAsync(opt.status_host ? opt.status_host : &status, a.status,
-                          sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+  unsigned status[6] = {};
+  PG_CUDA(cudaMemcpyAsync(opt.status_host ? opt.status_host : status, a.status,
+                          opt.status_host ? sizeof(unsigned) : sizeof(status),
+                          cudaMemcpyDeviceToHost, st));
   for (void* d : {d_canvas, d_strokes, d_points, d_fp, d_order, d_scratch_p, d_scratch_o,
                   d_scratch_cm, d_counter})
     PG_CUDA(cudaFreeAsync(d, st));
@@ -1975,7 +1999,7 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
     }
     b->pickup_clear = false;  // the last stroke's pickup map is in the brush's buffer
   }
-  if (status != 0) fail(PAINTY_ERR_CUDA, "batched stamp kernel reported an internal error");
+  check_stamp_status(status, "batched stamp kernel");
 }
 
 }  // namespace
@@ -2396,7 +2420,7 @@ painty_status painty_stamps_f32_noalloc(const painty_stamp_buffers_f32* b, void*
     const cudaStream_t st = pg::as_stream(stream);
     int* scratch = pg::noalloc_scratch();
     unsigned* status = reinterpret_cast<unsigned*>(scratch + kNoAllocOwnerCells);
-    PG_CUDA(cudaMemsetAsync(status, 0, sizeof(unsigned), st));
+    PG_CUDA(cudaMemsetAsync(status, 0, 8 * sizeof(unsigned), st));
     pg::StampArgs<float, float> a{};
     for (int i = 0; i < 3; i++) {
       a.cK[i] = b->canvas_K[i];
@@ -2449,12 +2473,14 @@ painty_status painty_stamps_f32_noalloc(const painty_stamp_buffers_f32* b, void*
     kern<<<1, pg::kStampThreads, Lk.total, st>>>(a);
     pg::count_launch();
     PG_CUDA(cudaGetLastError());
-    unsigned hs = 0;
-    PG_CUDA(cudaMemcpyAsync(&hs, status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    unsigned hs[6] = {};
+    PG_CUDA(cudaMemcpyAsync(hs, status, sizeof(hs), cudaMemcpyDeviceToHost, st));
     PG_CUDA(cudaStreamSynchronize(st));
-    if (hs != 0) pg::fail(PAINTY_ERR_CUDA, "stamp kernel reported an internal error");
+    pg::check_stamp_status(hs, "stamp kernel");
   });
 }
+
+int32_t painty_build_flags(void) { return pg::kBoundsCheck ? PAINTY_BUILD_BOUNDS_CHECK : 0; }
 
 painty_status painty_batch_last_shape(int32_t* cluster, int32_t* clusters) {
   return guard([&] {

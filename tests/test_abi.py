@@ -98,3 +98,15 @@ def test_texture_dictionary_lookup_matches_oracle(pg, oracle):
         path = rng.uniform(0, 400, (n, 2))
         size = float(rng.uniform(1, 80))
         assert d.lookup(path, size) == o.lookup(path, size)
+
+
+def test_bounds_checked_build_exports_and_reports_itself(pg):
+    """The bounds-checked twin library loads without a GPU, exports every declared entry and
+    reports its build flag; the default library does not set it."""
+    checked = pg.LIB_PATH.parent / "libpainty_gb300_checked.so"
+    lib = ctypes.CDLL(str(checked))
+    missing = [n for n in declared_symbols() if not hasattr(lib, n)]
+    assert not missing, missing
+    lib.painty_build_flags.restype = ctypes.c_int32
+    assert lib.painty_build_flags() & 1
+    assert pg.bounds_checked() == pg.BOUNDS_CHECKED

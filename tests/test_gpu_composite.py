@@ -145,3 +145,15 @@ def test_layer_set_cells(pg, storage):
         assert gv.sum() == pytest.approx(sum(V[m] for m in want.values()) + 0.25, rel=1e-3)
     with pytest.raises(pg.PaintyValueError):
         pg.PaintLayer(4, 4, storage).setCell(4, 0, [1, 1, 1], [1, 1, 1], 1.0)
+
+
+@pytest.mark.parametrize("rows,cols,L", [(37, 101, 3), (300, 130, 8), (9, 64, 17), (20, 20, 0)])
+def test_host_composite_equals_device_composite(pg, rows, cols, L):
+    """painty_compose_layers_host (host stacks in, host image out, transfers pipelined in row
+    bands) equals painty_compose_layers on device layers bit for bit; 17 layers take two
+    passes of the fused kernel, 0 layers return R0."""
+    K, S, V, R0 = workloads.composite_stack(rows, cols, layers=max(L, 1), seed=rows + L)
+    K, S, V = K[:L], S[:L], V[:L]
+    got = pg.compose_layers_host(K, S, V, R0)
+    want = gpu_compose(pg, K, S, V, R0) if L else R0.astype(np.float64)
+    assert np.array_equal(got.astype(np.float64), want)
