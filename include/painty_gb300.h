@@ -377,9 +377,10 @@ typedef struct painty_request {
 } painty_request;
 typedef struct painty_server_counters {
   int64_t submitted, completed, failed, cancelled;
-  int64_t steps, stamps, evictions, restores;
+  int64_t steps, stamps, evictions, restores;  /* steps: stamp-kernel launches */
   uint64_t resident_bytes, peak_resident_bytes;
   int64_t active, pending, canvases;
+  int64_t worker_busy_us;  /* time the worker thread spent issuing device work */
 } painty_server_counters;
 painty_status painty_server_create(const painty_server_options* options, painty_server** out);
 /* Non-blocking. Returns the request id and its canvas id (new canvases get one here). */
@@ -390,6 +391,11 @@ painty_status painty_server_submit(painty_server* server, const painty_request* 
  * PAINTY_ERR_TIMEOUT when it has not finished in time. */
 painty_status painty_server_wait(painty_server* server, uint64_t request_id, double timeout_s,
                                  double* latency_s, int64_t* stamps);
+/* Blocks until a request has finished that no earlier poll returned (timeout_s < 0: no
+ * limit) and returns its id in completion order; PAINTY_ERR_TIMEOUT when none finished in
+ * time. Every request appears once, whether or not it was also waited for. Its result and
+ * status then come from painty_server_wait with a zero timeout. */
+painty_status painty_server_poll(painty_server* server, double timeout_s, uint64_t* request_id);
 /* Cancels a request: before it runs it is dropped; while it runs it stops after its current
  * chunk of strokes (its canvas keeps the strokes painted so far). */
 painty_status painty_server_cancel(painty_server* server, uint64_t request_id);

@@ -777,7 +777,7 @@ class _Counters(C.Structure):
     _fields_ = [(n, C.c_int64) for n in ("submitted", "completed", "failed", "cancelled", "steps",
                                           "stamps", "evictions", "restores")] + \
                [("resident_bytes", C.c_uint64), ("peak_resident_bytes", C.c_uint64)] + \
-               [(n, C.c_int64) for n in ("active", "pending", "canvases")]
+               [(n, C.c_int64) for n in ("active", "pending", "canvases", "worker_busy_us")]
 
 
 _sig("painty_server_create", C.POINTER(_ServerOptions), C.POINTER(_P))
@@ -785,6 +785,7 @@ _sig("painty_server_submit", _P, C.POINTER(_Request), C.POINTER(C.c_uint64), C.P
 _sig("painty_server_wait", _P, C.c_uint64, _D, C.POINTER(_D), C.POINTER(_I64))
 _sig("painty_server_cancel", _P, C.c_uint64)
 _sig("painty_server_release", _P, C.c_uint64)
+_sig("painty_server_poll", _P, _D, C.POINTER(C.c_uint64))
 _sig("painty_server_stats", _P, C.POINTER(_Counters))
 _sig("painty_server_destroy", _P)
 
@@ -852,6 +853,15 @@ class Server:
             self._live.pop(request_id, None)
         _check(status)
         return out, lat.value, st.value
+
+    def poll(self, timeout: float = -1.0):
+        """The id of the next request to finish (completion order), or None on timeout."""
+        rid = C.c_uint64()
+        status = _lib.painty_server_poll(self._h, timeout, C.byref(rid))
+        if status == 6:
+            return None
+        _check(status)
+        return rid.value
 
     def cancel(self, request_id: int) -> None:
         _check(_lib.painty_server_cancel(self._h, request_id))

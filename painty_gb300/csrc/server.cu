@@ -106,6 +106,7 @@ struct painty_server {
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<uint64_t> pending;
+  std::deque<uint64_t> finished;  // completion order, for painty_server_poll
   std::vector<uint64_t> active;
   std::unordered_map<uint64_t, std::unique_ptr<ServerRequest>> reqs;
   std::unordered_map<uint64_t, std::unique_ptr<ServerCanvas>> canvases;
@@ -264,6 +265,7 @@ void finish(painty_server* s, ServerRequest* r, painty_status st, const std::str
   r->error = err;
   r->state = REQ_DONE;
   r->t_done = now_s();
+  s->finished.push_back(r->id);
   if (st == PAINTY_OK)
     s->stats.completed++;
   else if (st == PAINTY_ERR_CANCELLED)
@@ -422,6 +424,7 @@ bool worker_round(painty_server* s, std::unique_lock<std::mutex>& lk) {
   lk.unlock();
 
   // ---- device work (only this thread touches device state)
+  const double t_work = now_s();
   std::vector<std::pair<ServerRequest*, std::string>> failures;
   std::vector<ServerRequest*> done;
   bool moved = !admitted.empty() || !drops.empty();
@@ -489,8 +492,10 @@ bool worker_round(painty_server* s, std::unique_lock<std::mutex>& lk) {
     }
   }
 
+  const double busy = now_s() - t_work;
   lk.lock();
   s->stats.steps += chunks;
+  s->stats.worker_busy_us += static_cast<int64_t>(busy * 1e6);
   for (auto& f : failures) {
     // a failed request's slot is not reused before its stream has drained
     if (f.first->slot >= 0) cudaStreamSynchronize(s->slots[f.first->slot].st);
@@ -681,6 +686,25 @@ painty_status painty_server_wait(painty_server* s, uint64_t request_id, double t
     if (stamps) *stamps = r->stamps;
     result = r->status;
     if (r->status != PAINTY_OK) pg::set_last_error(r->error);
+  });
+  return st != PAINTY_OK ? st : result;
+}
+
+painty_status painty_server_poll(painty_server* s, double timeout_s, uint64_t* request_id) {
+  painty_status result = PAINTY_OK;
+  const painty_status st = guard([&] {
+    PG_REQUIRE(s && request_id, "null argument");
+    std::unique_lock<std::mutex> lk(s->mu);
+    const auto pred = [&] { return !s->finished.empty(); };
+    if (timeout_s < 0)
+      s->cv_done.wait(lk, pred);
+    else if (!s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), pred)) {
+      result = PAINTY_ERR_TIMEOUT;
+      pg::set_last_error("no request finished within the timeout");
+      return;
+    }
+    *request_id = s->finished.front();
+    s->finished.pop_front();
   });
   return st != PAINTY_OK ? st : result;
 }

@@ -1779,6 +1779,45 @@ double batch_makespan(const std::vector<double>& N, const std::vector<double>& P
   return span;
 }
 
+// Per-process facts about a batch kernel instance, looked up once: its static shared memory,
+// the dynamic shared memory it is allowed (raised as launches need more), and how many
+// clusters of each size fit on the device for a given dynamic size.
+struct BatchKernelInfo {
+  std::mutex mu;
+  size_t static_smem = 0;
+  size_t allowed = 0;
+  std::map<std::pair<int, size_t>, int> fit;
+  template <class K>
+  void allow_smem(K kern, size_t bytes) {
+    std::lock_guard<std::mutex> lk(mu);
+    if (bytes <= allowed) return;
+    PG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(bytes)));
+    allowed = bytes;
+  }
+  template <class K>
+  int fits(K kern, int cluster, size_t bytes) {
+    std::lock_guard<std::mutex> lk(mu);
+    const auto key = std::make_pair(cluster, bytes);
+    auto it = fit.find(key);
+    if (it != fit.end()) return it->second;
+    const int n = max_clusters(kern, cluster, key.second);
+    fit.emplace(key, n);
+    return n;
+  }
+};
+template <class TK, class TV>
+BatchKernelInfo& batch_kernel_info() {
+  static BatchKernelInfo* info = [] {
+    auto* i = new BatchKernelInfo();
+    cudaFuncAttributes fa{};
+    PG_CUDA(cudaFuncGetAttributes(&fa, batch_kernel<TK, TV>));
+    i->static_smem = fa.sharedSizeBytes;
+    return i;
+  }();
+  return *info;
+}
+
 template <class TK, class TV>
 void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushes, int32_t nc,
                      const painty_stroke_desc* strokes, int64_t ns, const double* points,
@@ -1791,9 +1830,8 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   std::vector<std::vector<int64_t>> per(nc);
   for (int64_t i = 0; i < ns; i++) per[strokes[i].canvas].push_back(i);
   // launch shared-memory budget: the opt-in maximum minus the kernel's static shared memory
-  cudaFuncAttributes fa{};
-  PG_CUDA(cudaFuncGetAttributes(&fa, batch_kernel<TK, TV>));
-  const size_t limit = static_cast<size_t>(max_dyn_smem()) - fa.sharedSizeBytes - 256;
+  BatchKernelInfo& info = batch_kernel_info<TK, TV>();
+  const size_t limit = static_cast<size_t>(max_dyn_smem()) - info.static_smem - 256;
   std::vector<BatchStroke> bs;
   bs.reserve(static_cast<size_t>(ns));
   std::vector<M> fptable;
@@ -1914,16 +1952,19 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
       if (plan.cm_global) fmax_cm = std::max(fmax_cm, bs[i].F);
       dyn = std::max(dyn, plan.layout.total);
     }
-    PG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(std::max<size_t>(dyn, 16))));
+    // in whole KB (fewer distinct occupancy queries), within the budget the plans respect
+    dyn = std::min((std::max<size_t>(dyn, 16) + 1023) / 1024 * 1024, std::max<size_t>(dyn, limit));
+    info.allow_smem(kern, dyn);
   };
   const int forced = env_cluster("PAINTY_BATCH_CLUSTER");
   int cl = 1, slots = 0;
   double best = 1e300;
+  int last_planned = 0;
   for (int c2 : {1, 2, 4, 8}) {
     if (forced ? c2 != forced : c2 > opt.max_cluster) continue;
     plan_all(c2);
-    const int fits = max_clusters(kern, c2, std::max<size_t>(dyn, 16));
+    last_planned = c2;
+    const int fits = info.fits(kern, c2, std::max<size_t>(dyn, 16));
     const int sl = std::min(fits, nc);
     const double span = batch_makespan(loadN, loadP, order, sl, c2);
     if (sl >= 1 && span < best) {
@@ -1935,33 +1976,49 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   PG_REQUIRE(slots >= 1, "no stamp cluster fits on the device");
   g_last_batch_shape[0] = cl;
   g_last_batch_shape[1] = slots;
-  plan_all(cl);
+  if (cl != last_planned) plan_all(cl);
   const int grid = slots * cl;
-  // device copies of the descriptors (stream-ordered, freed after the launch)
-  auto upload = [&](const void* h, size_t bytes) -> void* {
-    void* d = nullptr;
-    PG_CUDA(cudaMallocAsync(&d, std::max<size_t>(bytes, 16), st));
-    if (bytes) PG_CUDA(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, st));
-    return d;
+  // the descriptors in one device buffer (one allocation, one copy) and the scratch in
+  // another, both stream-ordered and freed after the launch; pieces 256-byte aligned
+  std::vector<unsigned char> hdesc;
+  auto piece = [&](const void* h, size_t bytes) -> size_t {
+    const size_t off = align_up(hdesc.size(), 256);
+    hdesc.resize(off + std::max<size_t>(bytes, 16));
+    if (bytes) std::memcpy(hdesc.data() + off, h, bytes);
+    return off;
   };
-  void* d_canvas = upload(bc.data(), bc.size() * sizeof(bc[0]));
-  void* d_strokes = upload(bs.data(), bs.size() * sizeof(BatchStroke));
-  void* d_points = upload(points, static_cast<size_t>(npoints) * 2 * sizeof(double));
-  void* d_fp = upload(fptable.data(), fptable.size() * sizeof(M));
-  void* d_order = upload(order.data(), order.size() * sizeof(int32_t));
+  const size_t o_canvas = piece(bc.data(), bc.size() * sizeof(bc[0]));
+  const size_t o_strokes = piece(bs.data(), bs.size() * sizeof(BatchStroke));
+  const size_t o_points = piece(points, static_cast<size_t>(npoints) * 2 * sizeof(double));
+  const size_t o_fp = piece(fptable.data(), fptable.size() * sizeof(M));
+  const size_t o_order = piece(order.data(), order.size() * sizeof(int32_t));
+  void* d_desc = nullptr;
+  PG_CUDA(cudaMallocAsync(&d_desc, hdesc.size(), st));
+  PG_CUDA(cudaMemcpyAsync(d_desc, hdesc.data(), hdesc.size(), cudaMemcpyHostToDevice, st));
+  auto at = [&](size_t off) { return static_cast<void*>(static_cast<char*>(d_desc) + off); };
+  void* d_canvas = at(o_canvas);
+  void* d_strokes = at(o_strokes);
+  void* d_points = at(o_points);
+  void* d_fp = at(o_fp);
+  void* d_order = at(o_order);
   const int64_t pstride = static_cast<int64_t>(8) * smax * smax;
   const int64_t ostride = static_cast<int64_t>(smax) * smax;
-  void* d_scratch_p = nullptr;
-  void* d_scratch_o = nullptr;
-  void* d_counter = nullptr;
-  PG_CUDA(cudaMallocAsync(&d_scratch_p, slots * pstride * msz, st));
-  PG_CUDA(cudaMallocAsync(&d_scratch_o, slots * ostride * sizeof(int), st));
   const int64_t cmstride = static_cast<int64_t>(cl) * 2 * fmax_cm * fmax_cm;
-  void* d_scratch_cm = nullptr;
-  PG_CUDA(cudaMallocAsync(&d_scratch_cm, std::max<int64_t>(slots * cmstride, 4) * sizeof(int), st));
-  // counter, status words 1..7 (bounds-check records at status + 4, + 5), claims
-  PG_CUDA(cudaMallocAsync(&d_counter, sizeof(int) * (8 + slots), st));
-  PG_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(int) * (8 + slots), st));
+  // counter, status words 1..7 (bounds-check records at status + 4, + 5), claims; then the
+  // per-cluster pickup maps, owner tables and cell maps
+  const size_t s_counter = 0;
+  const size_t s_pick = align_up(sizeof(int) * (8 + slots), 256);
+  const size_t s_own = align_up(s_pick + slots * pstride * msz, 256);
+  const size_t s_cm = align_up(s_own + slots * ostride * sizeof(int), 256);
+  const size_t s_end = align_up(s_cm + std::max<int64_t>(slots * cmstride, 4) * sizeof(int), 256);
+  void* d_scratch = nullptr;
+  PG_CUDA(cudaMallocAsync(&d_scratch, s_end, st));
+  PG_CUDA(cudaMemsetAsync(d_scratch, 0, sizeof(int) * (8 + slots), st));
+  auto sat = [&](size_t off) { return static_cast<void*>(static_cast<char*>(d_scratch) + off); };
+  void* d_counter = sat(s_counter);
+  void* d_scratch_p = sat(s_pick);
+  void* d_scratch_o = sat(s_own);
+  void* d_scratch_cm = sat(s_cm);
   BatchArgs<TK, TV> a{};
   a.canvases = static_cast<const BatchCanvas<TK, TV>*>(d_canvas);
   a.strokes = static_cast<const BatchStroke*>(d_strokes);
@@ -1985,9 +2042,8 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   PG_CUDA(cudaMemcpyAsync(opt.status_host ? opt.status_host : status, a.status,
                           opt.status_host ? sizeof(unsigned) : sizeof(status),
                           cudaMemcpyDeviceToHost, st));
-  for (void* d : {d_canvas, d_strokes, d_points, d_fp, d_order, d_scratch_p, d_scratch_o,
-                  d_scratch_cm, d_counter})
-    PG_CUDA(cudaFreeAsync(d, st));
+  PG_CUDA(cudaFreeAsync(d_desc, st));
+  PG_CUDA(cudaFreeAsync(d_scratch, st));
   if (!opt.status_host) PG_CUDA(cudaStreamSynchronize(st));
   for (int32_t c = 0; c < nc; c++) {
     if (per[c].empty()) continue;

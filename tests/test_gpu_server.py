@@ -172,3 +172,16 @@ def test_release_frees_canvases_and_pinned_results(pg):
         img, _, _ = ref.wait(ref.submit(st, rows=rows, cols=cols, r0=r0)[0], 60)
         assert np.array_equal(img, out)
     ref.close()
+
+
+def test_poll_returns_each_request_once_in_completion_order(pg):
+    fp = workloads.footprint_image(seed=7)
+    reqs = _request_set(31, 6)
+    srv = pg.Server(8 << 30, fp, storage="f32", step_stamps=5000)
+    ids = [srv.submit(st, rows=rr, cols=cc, r0=r0)[0] for rr, cc, r0, st in reqs]
+    seen = [srv.poll(60.0) for _ in ids]
+    assert sorted(seen) == sorted(ids)
+    assert srv.poll(0.05) is None
+    for rid in ids:  # finished: waiting returns at once
+        srv.wait(rid, 0.0)
+    srv.close()
