@@ -678,6 +678,8 @@ def run_batch(pg, torch, storage: str, ncanvas: int, max_strokes, rank: int = 0,
     for s_, k_ in zip(strokes, per_stroke):
         per_canvas[s_[0]] += k_
     roof = stamp_roofline([(s[2], k_) for s, k_ in zip(strokes, per_stroke)], n, dt, storage)
+    heavy = int(np.argmax(per_canvas)) if len(per_canvas) else -1
+    bound = _dependency_bound(specs, strokes, heavy) if heavy >= 0 else None
     if roof:
         roof["note"] = ("canvases run concurrently, each canvas's stamps in order; the "
                         "heaviest canvas's chain of stamps bounds the launch")
@@ -689,6 +691,7 @@ def run_batch(pg, torch, storage: str, ncanvas: int, max_strokes, rank: int = 0,
             "heaviest_canvas_stamps": int(per_canvas.max()) if len(per_canvas) else 0,
             "heaviest_canvas_stamps_per_s": round(float(per_canvas.max()) / dt, 1) if n else 0.0,
             "mean_canvas_stamps": round(float(per_canvas.mean()), 1) if len(per_canvas) else 0.0,
+            "heaviest_canvas_dependency_bound": bound,
             "config": f"{ncanvas} canvases (side logU[256,2048], aspect U[0.5,2], "
                       f"{pg_canvas_px(px)}), {len(strokes)} strokes (logU[50,2000] per canvas"
                       f"{'' if max_strokes is None else f', at most {max_strokes}'}), "
@@ -777,6 +780,23 @@ class _PinnedPool:
         if key is not None:
             with self.lock:
                 self.free.setdefault(key[0], []).append(key[1])
+
+
+_BOUND = {}
+
+
+def _dependency_bound(specs, strokes, c: int):
+    """The heaviest canvas's serial work over its critical path when strokes may overlap in
+    time wherever their grown boxes share no 32-pixel tile (painty_gb300.schedule): the most a
+    stroke-level scheduler could shorten that canvas's chain."""
+    from painty_gb300 import schedule
+    key = (id(strokes), c)
+    if key not in _BOUND:
+        mine = [(x[1], x[2], x[3]) for x in strokes if x[0] == c]
+        n, W, C = schedule.canvas_dependency_bound(specs[c][0], specs[c][1], mine, tile=32)
+        _BOUND[key] = {"canvas": c, "stamps": n, "tile": 32,
+                       "serial_work_over_critical_path": round(W / C, 3) if C else None}
+    return _BOUND[key]
 
 
 def run_serve(pg, torch, rate: float, seconds: float, seed: int = 4, budget_gb: float = 120.0,
