@@ -824,6 +824,7 @@ def run_serve(pg, torch, rate: float, seconds: float, seed: int = 4, budget_gb: 
     rids = [None] * n
     cids = [None] * n
     keys = [None] * n
+    r0_keys = [None] * n
     lat = np.full(n, np.nan)
     stamps_done = [0]
     t0 = time.perf_counter()
@@ -838,8 +839,9 @@ def run_serve(pg, torch, rate: float, seconds: float, seed: int = 4, budget_gb: 
             root = cont if cont >= 0 else i
             if cont >= 0:
                 rids[i], cids[i] = srv.submit(strokes, canvas_id=cids[cont], out=out)
-            else:
-                r0 = np.ascontiguousarray(substrate[:rows, :cols])
+            else:  # the substrate in a pinned buffer too: the server reads it in place
+                r0_keys[i], r0 = pool.take(rows, cols)
+                np.copyto(r0, substrate[:rows, :cols])
                 rids[i], cids[i] = srv.submit(strokes, rows=rows, cols=cols, r0=r0, out=out)
             index[rids[i]] = i
             if last[root] == i:
@@ -863,6 +865,7 @@ def run_serve(pg, torch, rate: float, seconds: float, seed: int = 4, budget_gb: 
             except pg.PaintyError:
                 pass
             pool.give(keys[i])
+            pool.give(r0_keys[i])
 
     th = threading.Thread(target=client)
     tc = threading.Thread(target=consumer)

@@ -367,7 +367,9 @@ typedef struct painty_server_options {
 typedef struct painty_request {
   uint64_t canvas_id;      /* 0: a new canvas of rows x cols; else continue that canvas */
   int32_t rows, cols;
-  const float* r0;         /* new canvas substrate, rows*cols*3 interleaved (NULL: 1.0) */
+  const float* r0;         /* new canvas substrate, rows*cols*3 interleaved (NULL: 1.0); pinned
+                              host memory is read in place when the canvas is created (keep it
+                              valid until the request finishes), other memory is copied */
   const painty_stroke_desc* strokes; /* `canvas` ignored; copied at submit */
   int64_t nstrokes;
   const double* points;    /* copied at submit */

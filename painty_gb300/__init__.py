@@ -840,7 +840,7 @@ class Server:
         rid, cid = C.c_uint64(), C.c_uint64()
         _check(_lib.painty_server_submit(self._h, C.byref(req), C.byref(rid), C.byref(cid)))
         self._dims.setdefault(cid.value, (rows, cols))
-        self._live[rid.value] = out
+        self._live[rid.value] = (out, r0a)  # a pinned substrate is read when the canvas is made
         return rid.value, cid.value
 
     def wait(self, request_id: int, timeout: float = -1.0):
@@ -848,7 +848,7 @@ class Server:
         stamps). Raises on a failed, cancelled or unfinished request."""
         lat, st = _D(), _I64()
         status = _lib.painty_server_wait(self._h, request_id, timeout, C.byref(lat), C.byref(st))
-        out = self._live.get(request_id)
+        out = self._live.get(request_id, (None, None))[0]
         if status != 6:  # not a timeout: the request is over
             self._live.pop(request_id, None)
         _check(status)

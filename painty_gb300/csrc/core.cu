@@ -159,7 +159,7 @@ void canvas_relayout(painty_canvas* c, void* base) {
 }
 
 painty_canvas* canvas_create_on(int32_t rows, int32_t cols, painty_storage storage,
-                                cudaMemPool_t pool, cudaStream_t st) {
+                                cudaMemPool_t pool, cudaStream_t st, bool sync) {
   PG_REQUIRE(rows > 0 && cols > 0, "rows and cols must be positive");
   PG_REQUIRE(valid_storage(storage), "unknown storage format");
   auto* c = new painty_canvas();
@@ -178,7 +178,7 @@ painty_canvas* canvas_create_on(int32_t rows, int32_t cols, painty_storage stora
     PG_CUDA(cudaMemsetAsync(c->base, 0, c->bytes, st));
     const double one[3] = {1.0, 1.0, 1.0};  // Canvas.hxx:33 background
     fill_planes(c->r0.R, 3, r_type(rs), c->r0.plane_elems(), one, st);
-    PG_CUDA(cudaStreamSynchronize(st));
+    if (sync) PG_CUDA(cudaStreamSynchronize(st));
   } catch (...) {
     if (c->base) device_free_on(c->base, st);
     delete c;
@@ -350,6 +350,13 @@ void launch_gather(DevType dt, PlanePtrs src, TD* dst, int nch, int il, int32_t 
 void upload_planes(void* const* planes, int nch, DevType dt, int32_t rows, int32_t cols,
                    int64_t pitch, const void* host, painty_host_format fmt, cudaStream_t st,
                    int64_t estride) {
+  upload_planes_async(planes, nch, dt, rows, cols, pitch, host, fmt, st, estride);
+  PG_CUDA(cudaStreamSynchronize(st));
+}
+
+void upload_planes_async(void* const* planes, int nch, DevType dt, int32_t rows, int32_t cols,
+                         int64_t pitch, const void* host, painty_host_format fmt,
+                         cudaStream_t st, int64_t estride) {
   PG_REQUIRE(host != nullptr, "host buffer is null");
   PG_REQUIRE(fmt >= PAINTY_HOST_F64_INTERLEAVED && fmt <= PAINTY_HOST_F32_PLANAR,
              "unknown host format");
@@ -364,7 +371,6 @@ void upload_planes(void* const* planes, int nch, DevType dt, int32_t rows, int32
         PG_CUDA(cudaMemcpy2DAsync(planes[c], pitch * hes,
                                   static_cast<const char*>(host) + c * n * hes, cols * hes,
                                   cols * hes, rows, cudaMemcpyHostToDevice, st));
-      PG_CUDA(cudaStreamSynchronize(st));
       return;
     }
   }
@@ -380,7 +386,6 @@ void upload_planes(void* const* planes, int nch, DevType dt, int32_t rows, int32
     launch_scatter<float>(dt, static_cast<const float*>(staging), pp, nch, il, rows, cols,
                           pitch, estride, st);
   PG_CUDA(cudaFreeAsync(staging, st));
-  PG_CUDA(cudaStreamSynchronize(st));
 }
 
 void download_planes(const void* const* planes, int nch, DevType dt, int32_t rows,
@@ -598,11 +603,16 @@ __global__ void __launch_bounds__(256) km_composite16_kernel(
     for (int l = 0; l < a.L; l++) {
       if (l + 1 < a.L) load_layer16(a, l + 1, e, nxt);
 #pragma unroll
-      for (int i = 0; i < 4; i++) {
-        const float d = elem16<TV>(cur.v, i);
+      for (int i = 0; i < 4; i += 2) {  // pixel pairs on the packed FP32 pipe
+        const float2 d = f2(elem16<TV>(cur.v, i), elem16<TV>(cur.v, i + 1));
 #pragma unroll
-        for (int c = 0; c < 3; c++)
-          r[c][i] = km_reflectance(elem16<TK>(cur.k[c], i), elem16<TK>(cur.s[c], i), r[c][i], d);
+        for (int c = 0; c < 3; c++) {
+          const float2 o = km_reflectance2(
+            f2(elem16<TK>(cur.k[c], i), elem16<TK>(cur.k[c], i + 1)),
+            f2(elem16<TK>(cur.s[c], i), elem16<TK>(cur.s[c], i + 1)), f2(r[c][i], r[c][i + 1]), d);
+          r[c][i] = o.x;
+          r[c][i + 1] = o.y;
+        }
       }
       cur = nxt;
     }
@@ -1136,10 +1146,10 @@ painty_status painty_compose_layers_host(const float* K, const float* S, const f
     PG_REQUIRE(R0 && out, "R0 or out is null");
     constexpr int kStreams = 3;
     const int64_t pitch = pg::pitch_for(cols);
-    // bands of about 16 MB of layer data each
+    // bands of about 96 MB of layer data each (large copies keep the copy engines at speed)
     const int64_t row_bytes = static_cast<int64_t>(7 * L + 6) * pitch * 4;
     const int32_t band = static_cast<int32_t>(
-      std::max<int64_t>(1, std::min<int64_t>(rows, (int64_t(16) << 20) / row_bytes)));
+      std::max<int64_t>(1, std::min<int64_t>(rows, (int64_t(96) << 20) / row_bytes)));
     const int64_t plane = static_cast<int64_t>(band) * pitch;  // device plane of one band
     const int64_t nplanes = 7 * static_cast<int64_t>(L) + 6;   // K, S, V, R0, out
     PG_CUDA(cudaStreamSynchronize(pg::as_stream(stream)));
@@ -1164,6 +1174,17 @@ painty_status painty_compose_layers_host(const float* K, const float* S, const f
       // host planes [n][rows][cols] <-> device planes [n][band][pitch], rows r0 .. r0 + h
       auto copy3d = [&](const float* hbase, float* dbase, int n, int32_t r0, int32_t h,
                         bool up, cudaStream_t s) {
+        if (pitch == cols) {  // each plane's band is one contiguous run on both sides
+          const size_t run = static_cast<size_t>(h) * cols * 4;
+          const size_t hstep = static_cast<size_t>(rows) * cols * 4, dstep = plane * 4;
+          char* hp = reinterpret_cast<char*>(const_cast<float*>(hbase)) +
+                     static_cast<size_t>(r0) * cols * 4;
+          if (up)
+            PG_CUDA(cudaMemcpy2DAsync(dbase, dstep, hp, hstep, run, n, cudaMemcpyHostToDevice, s));
+          else
+            PG_CUDA(cudaMemcpy2DAsync(hp, hstep, dbase, dstep, run, n, cudaMemcpyDeviceToHost, s));
+          return;
+        }
         cudaMemcpy3DParms m{};
         cudaPitchedPtr hp = make_cudaPitchedPtr(const_cast<float*>(hbase), cols * 4, cols, rows);
         cudaPitchedPtr dp = make_cudaPitchedPtr(dbase, pitch * 4, pitch, band);

@@ -273,6 +273,40 @@ __device__ __forceinline__ float km_reflectance(float K, float S, float R0, floa
   return fabsf(d) < kEps ? R0 : r;
 }
 
+// km_reflectance for two pixels at once on Blackwell's packed FP32 pipe (FFMA2 / FMUL2 /
+// FADD2 each do two lanes of the scalar operation with the same rounding): the same formula,
+// with every multiply-add written as an explicit fma, in about half the issued instructions.
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 km_reflectance2(float2 K, float2 S, float2 R0, float2 d) {
+  constexpr float kEps = 2.220446049250313e-12f;  // 1e4 * DBL_EPSILON
+  S.x = fabsf(S.x) > kEps ? S.x : 1e-11f;
+  S.y = fabsf(S.y) > kEps ? S.y : 1e-11f;
+  const float2 one = f2(1.0f, 1.0f);
+  float2 q = __fmul2_rn(K, __ffma2_rn(f2(2.0f, 2.0f), S, K));  // K (2S + K)
+  q.x = fmaxf(q.x, 1e-30f);
+  q.y = fmaxf(q.y, 1e-30f);
+  const float2 beta = __fmul2_rn(q, f2(rsqrt_approx(q.x), rsqrt_approx(q.y)));
+  const float2 x = __fmul2_rn(beta, d);
+  const float2 nR0 = f2(-R0.x, -R0.y);
+  const float2 omr = __fadd2_rn(one, nR0);
+  const float2 A = __ffma2_rn(S, omr, __fmul2_rn(nR0, K));
+  const float2 B = __ffma2_rn(S, omr, K);
+  const float2 t = __fmul2_rn(f2(-2.8853900817779268f, -2.8853900817779268f), x);
+  const float2 e = f2(ex2_approx(t.x), ex2_approx(t.y));  // exp(-2x)
+  const float2 x2 = __fmul2_rn(x, x);
+  const float2 g = __ffma2_rn(x2, __ffma2_rn(x2, f2(-1.0f / 45.0f, -1.0f / 45.0f),
+                                              f2(1.0f / 3.0f, 1.0f / 3.0f)), one);
+  const float2 ome = __fadd2_rn(one, f2(-e.x, -e.y));
+  const float2 bope = __fmul2_rn(beta, __fadd2_rn(one, e));
+  const bool sx = x.x < 0.05f, sy = x.y < 0.05f;
+  const float2 u = f2(sx ? d.x : ome.x, sy ? d.y : ome.y);
+  const float2 w = f2(sx ? g.x : bope.x, sy ? g.y : bope.y);
+  const float2 num = __ffma2_rn(A, u, __fmul2_rn(R0, w));
+  const float2 den = __ffma2_rn(B, u, w);
+  const float2 r = __fmul2_rn(num, f2(rcp_approx(den.x), rcp_approx(den.y)));
+  return f2(fabsf(d.x) < kEps ? R0.x : r.x, fabsf(d.y) < kEps ? R0.y : r.y);
+}
+
 // painty's coth (painty/core/Math.hxx:157-169) and ComputeReflectance in double, in the
 // reference's own operation order; for the F64 parity storage mode.
 __device__ __forceinline__ double coth_ref(double x) {

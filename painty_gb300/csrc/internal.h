@@ -6,6 +6,7 @@
 #include <atomic>
 #include <cstdint>
 #include <map>
+#include <memory>
 #include <utility>
 #include <vector>
 #include <stdexcept>
@@ -123,8 +124,9 @@ struct painty_brush {
   int32_t F = 0;
   int32_t support2 = 0;  // squared stamp-pixel radius beyond which the footprint is zero
   int32_t width = 0;     // footprint width before padding (2 ceil(r) + 1)
-  // footprints already built from `full`, by width: (padded footprint, support2)
-  std::map<int32_t, std::pair<std::vector<double>, int32_t>> fp_cache;
+  // footprints built from `full`, by width, shared by every brush of the same footprint image
+  // (the process-wide cache of stamp.cu)
+  std::shared_ptr<struct FootprintFamily> fp_family;
   std::vector<double> full;
   int32_t fh = 0, fw = 0;
   std::vector<double> footprint;  // F*F
@@ -176,10 +178,10 @@ size_t image_bytes(int32_t rows, int32_t cols, painty_storage s);
 // Points a canvas's plane views into a new device allocation of the canvas layout (nullptr:
 // no allocation, as for a canvas whose state was moved to host memory).
 void canvas_relayout(painty_canvas* c, void* base);
-// A canvas (as painty_canvas_create) in pool memory ordered on `st`; returns after `st` has
-// finished initialising it. Free with canvas_destroy_on.
+// A canvas (as painty_canvas_create) in pool memory, initialised in `st`'s order (with
+// `sync`, returns after `st` has finished that). Free with canvas_destroy_on.
 painty_canvas* canvas_create_on(int32_t rows, int32_t cols, painty_storage storage,
-                                cudaMemPool_t pool, cudaStream_t st);
+                                cudaMemPool_t pool, cudaStream_t st, bool sync = true);
 void canvas_destroy_on(painty_canvas* c, cudaStream_t st);
 
 // Plane transfer between a host buffer and `nch` device planes of element type `dev_type`
@@ -192,6 +194,11 @@ DevType r_type(painty_storage s);
 void upload_planes(void* const* planes, int nch, DevType dt, int32_t rows, int32_t cols,
                    int64_t pitch, const void* host, painty_host_format fmt, cudaStream_t st,
                    int64_t estride = 1);
+// The same ordered on `st` without waiting (a pinned host buffer must stay valid until the
+// stream passes the copy; pageable memory is copied out before the call returns).
+void upload_planes_async(void* const* planes, int nch, DevType dt, int32_t rows, int32_t cols,
+                         int64_t pitch, const void* host, painty_host_format fmt,
+                         cudaStream_t st, int64_t estride = 1);
 void download_planes(const void* const* planes, int nch, DevType dt, int32_t rows,
                      int32_t cols, int64_t pitch, void* host, painty_host_format fmt,
                      cudaStream_t st, int64_t estride = 1);

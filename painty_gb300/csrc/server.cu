@@ -62,7 +62,8 @@ struct ServerCanvas {
   bool dropped = false;  // released and freed
   uint64_t last_used = 0;
   size_t bytes = 0;  // device bytes when resident
-  std::vector<float> r0;  // substrate until the canvas is created
+  std::vector<float> r0;  // substrate until the canvas is created (a copy of pageable memory)
+  const float* r0_pinned = nullptr;  // or the caller's pinned substrate
   std::deque<uint64_t> waiting;  // its unfinished requests, in submission order
   HostBlob save_canvas, save_snapshot;
 };
@@ -158,9 +159,9 @@ void blob_save(painty_server* s, HostBlob& b, const void* dev, size_t bytes) {
   PG_CUDA(cudaMemcpyAsync(b.p, dev, bytes, cudaMemcpyDeviceToHost, s->stream));
 }
 
-void image_alloc(painty_server* s, ServerCanvas* c) {
+void image_alloc(painty_server* s, ServerCanvas* c, cudaStream_t st) {
   const painty_storage rs = image_storage(s);
-  void* base = pg::device_alloc_on(pg::image_bytes(c->rows, c->cols, rs), s->pool, s->stream);
+  void* base = pg::device_alloc_on(pg::image_bytes(c->rows, c->cols, rs), s->pool, st);
   pg::image_layout(c->img, c->rows, c->cols, rs, base);
   c->img.owned = false;
 }
@@ -203,36 +204,38 @@ void restore(painty_server* s, ServerCanvas* c) {
     pg::layer_layout(b->snapshot, b->snapshot.rows, b->snapshot.cols, b->snapshot.storage, sb,
                      true);
   }
-  image_alloc(s, c);
+  image_alloc(s, c, s->stream);
   PG_CUDA(cudaStreamSynchronize(s->stream));
   c->resident = true;
 }
 
-void create(painty_server* s, ServerCanvas* c) {
-  painty_canvas* cv = pg::canvas_create_on(c->rows, c->cols, s->opt.storage, s->pool, s->stream);
+// A new canvas, its substrate and its brush, all in the order of `st` (the stream of the
+// request that creates it; nothing waits).
+void create(painty_server* s, ServerCanvas* c, cudaStream_t st) {
+  painty_canvas* cv = pg::canvas_create_on(c->rows, c->cols, s->opt.storage, s->pool, st, false);
   try {
-    if (!c->r0.empty())
-      pg::upload_planes(cv->r0.R, 3, pg::r_type(cv->r0.storage), c->rows, c->cols,
-                        cv->wet.pitch, c->r0.data(), PAINTY_HOST_F32_INTERLEAVED, s->stream);
+    const float* r0 = c->r0_pinned ? c->r0_pinned : (c->r0.empty() ? nullptr : c->r0.data());
+    if (r0)
+      pg::upload_planes_async(cv->r0.R, 3, pg::r_type(cv->r0.storage), c->rows, c->cols,
+                              cv->wet.pitch, r0, PAINTY_HOST_F32_INTERLEAVED, st);
     cv->version++;
     painty_brush* b = nullptr;
-    const painty_status st = painty_brush_create(8.0, s->footprint.data(),
-                                                 s->opt.footprint_rows, s->opt.footprint_cols, &b);
-    if (st != PAINTY_OK) pg::fail(st, painty_last_error());
+    const painty_status bst = painty_brush_create(8.0, s->footprint.data(),
+                                                  s->opt.footprint_rows, s->opt.footprint_cols, &b);
+    if (bst != PAINTY_OK) pg::fail(bst, painty_last_error());
     b->pickupRate = s->opt.pickup_rate;
     b->depositionRate = s->opt.deposition_rate;
     b->pool = s->pool;
-    b->pool_stream = s->stream;
+    b->pool_stream = st;
     c->brush = b;
   } catch (...) {
-    pg::canvas_destroy_on(cv, s->stream);
+    pg::canvas_destroy_on(cv, st);
     throw;
   }
   c->cv = cv;
-  image_alloc(s, c);
-  PG_CUDA(cudaStreamSynchronize(s->stream));
+  image_alloc(s, c, st);
   c->resident = true;
-  std::vector<float>().swap(c->r0);
+  std::vector<float>().swap(c->r0);  // a pageable source was copied out during the call
 }
 
 // Frees a released canvas (worker thread; nothing of it is in flight).
@@ -444,7 +447,7 @@ bool worker_round(painty_server* s, std::unique_lock<std::mutex>& lk) {
     try {
       if (a.prep) {
         if (!a.c->cv) {
-          create(s, a.c);
+          create(s, a.c, s->slots[a.r->slot].st);
         } else {
           restore(s, a.c);
           s->stats.restores++;
@@ -494,6 +497,7 @@ bool worker_round(painty_server* s, std::unique_lock<std::mutex>& lk) {
 
   const double busy = now_s() - t_work;
   lk.lock();
+  for (ServerCanvas* c : drops) s->canvases.erase(c->id);  // its requests are all finished
   s->stats.steps += chunks;
   s->stats.worker_busy_us += static_cast<int64_t>(busy * 1e6);
   for (auto& f : failures) {
@@ -624,8 +628,16 @@ painty_status painty_server_submit(painty_server* s, const painty_request* req,
       nc->rows = req->rows;
       nc->cols = req->cols;
       nc->bytes = canvas_device_bytes(s, req->rows, req->cols);
-      if (req->r0)
-        nc->r0.assign(req->r0, req->r0 + static_cast<size_t>(req->rows) * req->cols * 3);
+      if (req->r0) {
+        // pinned substrates are read in place when the canvas is created; others are copied
+        cudaPointerAttributes pa{};
+        if (cudaPointerGetAttributes(&pa, req->r0) == cudaSuccess &&
+            pa.type == cudaMemoryTypeHost)
+          nc->r0_pinned = req->r0;
+        else
+          nc->r0.assign(req->r0, req->r0 + static_cast<size_t>(req->rows) * req->cols * 3);
+        cudaGetLastError();
+      }
       c = nc.get();
       s->canvases.emplace(nc->id, std::move(nc));
     } else {

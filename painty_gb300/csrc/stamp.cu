@@ -1358,13 +1358,65 @@ int32_t support_radius2(const double* fp, int F) {
   return static_cast<int32_t>(std::floor(b * b)) + 1;
 }
 
+}  // namespace
+}  // namespace pg
+
+// The padded footprints of one footprint image, by brush width: (footprint, support2). Brushes
+// made from equal images share one family, so a new brush (a server's new canvas) finds the
+// resampled footprints already built.
+struct FootprintFamily {
+  std::mutex mu;
+  std::vector<double> image;
+  int32_t fh = 0, fw = 0;
+  std::map<int32_t, std::pair<std::vector<double>, int32_t>> by_width;
+};
+
+namespace pg {
+namespace {
+
+std::mutex g_family_mu;
+std::map<uint64_t, std::vector<std::weak_ptr<FootprintFamily>>> g_families;
+
+// The family of a footprint image (FNV-1a of its bytes, then compared value for value).
+std::shared_ptr<FootprintFamily> footprint_family(const std::vector<double>& img, int32_t fh,
+                                                  int32_t fw) {
+  uint64_t h = 1469598103934665603ull;
+  auto mix = [&h](const void* p, size_t n) {
+    const unsigned char* c = static_cast<const unsigned char*>(p);
+    for (size_t i = 0; i < n; i++) h = (h ^ c[i]) * 1099511628211ull;
+  };
+  mix(&fh, sizeof(fh));
+  mix(&fw, sizeof(fw));
+  mix(img.data(), img.size() * sizeof(double));
+  std::lock_guard<std::mutex> lk(g_family_mu);
+  auto& list = g_families[h];
+  for (auto it = list.begin(); it != list.end();) {
+    std::shared_ptr<FootprintFamily> f = it->lock();
+    if (!f) {
+      it = list.erase(it);
+      continue;
+    }
+    if (f->fh == fh && f->fw == fw && f->image == img) return f;
+    ++it;
+  }
+  auto f = std::make_shared<FootprintFamily>();
+  f->image = img;
+  f->fh = fh;
+  f->fw = fw;
+  list.push_back(f);
+  return f;
+}
+
 // FootprintBrush::setRadius (FootprintBrush.hxx:46-63). The footprint image is resampled to
 // width x width by a pixel-centre aligned bilinear resample (in place of OpenCV's
 // Lanczos-4 resize) and zero-padded by (sizeMap - width) / 2 on each side.
 // The padded footprint of a brush width (cached per width: the resample depends on it only).
 const std::pair<std::vector<double>, int32_t>& footprint_for(painty_brush* b, int width) {
-  auto it = b->fp_cache.find(width);
-  if (it != b->fp_cache.end()) return it->second;
+  if (!b->fp_family) b->fp_family = footprint_family(b->full, b->fh, b->fw);
+  FootprintFamily& fam = *b->fp_family;
+  std::lock_guard<std::mutex> lk(fam.mu);  // entries are never erased: references stay valid
+  auto it = fam.by_width.find(width);
+  if (it != fam.by_width.end()) return it->second;
   const int sizeMap = static_cast<int>(std::ceil(std::sqrt(2.0) * width));
   const int pad = (sizeMap - width) / 2;
   const int F = width + 2 * pad;
@@ -1376,7 +1428,7 @@ const std::pair<std::vector<double>, int32_t>& footprint_for(painty_brush* b, in
         interpolate(b->full.data(), b->fh, b->fw, (static_cast<double>(j) + 0.5) * sx - 0.5,
                     (static_cast<double>(i) + 0.5) * sy - 0.5);
   const int32_t s2 = support_radius2(fp.data(), F);
-  return b->fp_cache.emplace(width, std::make_pair(std::move(fp), s2)).first->second;
+  return fam.by_width.emplace(width, std::make_pair(std::move(fp), s2)).first->second;
 }
 
 void set_radius(painty_brush* b, double radius) {
