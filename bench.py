@@ -743,7 +743,8 @@ class _PinnedPool:
 
     @staticmethod
     def size_class(rows: int, cols: int) -> int:
-        return 1 << max(20, (rows * cols * 3 - 1).bit_length())  # floats, powers of two
+        step = 1 << 22  # floats: classes of 16 MB
+        return (rows * cols * 3 + step - 1) // step * step
 
     def prewarm(self, plan, rate: float, seconds: float = 2.0):
         """Allocates, before the timed run, the buffers `seconds` of arrivals would hold."""
@@ -776,6 +777,15 @@ class _PinnedPool:
                 return None, np.empty((rows, cols, 3), dtype=np.float32)
         return (cls, t), t[:n].numpy().reshape(rows, cols, 3)
 
+    def substrate(self, seed: int):
+        """One pinned buffer of 4096 x 4096 x 3 substrate values U[0.8, 0.95]."""
+        if getattr(self, "_sub", None) is None:
+            g = np.random.default_rng(seed)
+            t = self.torch.empty(4096 * 4096 * 3, dtype=self.torch.float32, pin_memory=True)
+            t.numpy()[:] = g.uniform(0.8, 0.95, 4096 * 4096 * 3).astype(np.float32)
+            self._sub = t
+        return self._sub.numpy()
+
     def give(self, key):
         if key is not None:
             with self.lock:
@@ -800,12 +810,16 @@ def _dependency_bound(specs, strokes, c: int):
 
 
 def run_serve(pg, torch, rate: float, seconds: float, seed: int = 4, budget_gb: float = 120.0,
-              storage: str = "f16", drain_s: float = 60.0, plan=None, pool=None):
+              storage: str = "f16", drain_s: float = 60.0, plan=None, pool=None,
+              max_outstanding: int = 512):
     """Serving at `rate` req/s for `seconds` (serve_plan): a client thread submits each
     request at its arrival time into a result buffer (pinned, from a bounded pool) and releases
-    each canvas after its last request; a consumer thread waits for the requests in order and
-    returns their buffers. Requests still unfinished `drain_s` after the last arrival are
-    cancelled and counted as unfinished. Latency = submit to result in the caller's buffer."""
+    each canvas after its last request; a consumer thread takes results in completion order and
+    returns their buffers. A request arriving while `max_outstanding` are unfinished is shed
+    (not submitted; counted), which bounds the host memory of an overloaded run. Requests still
+    unfinished `drain_s` after the last arrival are cancelled and counted as unfinished.
+    Latency = submit to result in the caller's buffer. New canvases take their substrate from
+    one pinned U[0.8, 0.95] buffer (a contiguous prefix per canvas), read in place."""
     import threading
 
     from painty_gb300 import workloads
@@ -817,31 +831,40 @@ def run_serve(pg, torch, rate: float, seconds: float, seed: int = 4, budget_gb: 
     for i, (_, cont, *_r) in enumerate(plan):
         last[cont if cont >= 0 else i] = i
     fp = workloads.footprint_image(seed=7)
-    substrate = np.random.default_rng(seed).uniform(0.8, 0.95, (4096, 4096, 3)).astype(np.float32)
-    pool = pool if pool is not None else _PinnedPool(torch, 24 << 30)
+    pool = pool if pool is not None else _PinnedPool(torch, 32 << 30)
+    substrate = pool.substrate(seed)
     pool.prewarm(plan, rate)
     srv = pg.Server(int(budget_gb * (1 << 30)), fp, storage=storage, step_stamps=65536)
     rids = [None] * n
     cids = [None] * n
     keys = [None] * n
-    r0_keys = [None] * n
     lat = np.full(n, np.nan)
     stamps_done = [0]
     t0 = time.perf_counter()
     deadline = t0 + seconds + drain_s
+
+    outstanding = [0]
+    shed = [0]
+    lock = threading.Lock()
 
     def client():
         for i, (t, cont, rows, cols, strokes) in enumerate(plan):
             dt = t - (time.perf_counter() - t0)
             if dt > 0:
                 time.sleep(dt)
-            keys[i], out = pool.take(rows, cols)
             root = cont if cont >= 0 else i
+            if (outstanding[0] >= max_outstanding or (cont >= 0 and cids[cont] is None)):
+                shed[0] += 1  # over the limit (or its canvas's first request was shed)
+                if last[root] == i and cids[root] is not None:
+                    srv.release(cids[root])
+                continue
+            keys[i], out = pool.take(rows, cols)
+            with lock:
+                outstanding[0] += 1
             if cont >= 0:
                 rids[i], cids[i] = srv.submit(strokes, canvas_id=cids[cont], out=out)
-            else:  # the substrate in a pinned buffer too: the server reads it in place
-                r0_keys[i], r0 = pool.take(rows, cols)
-                np.copyto(r0, substrate[:rows, :cols])
+            else:
+                r0 = substrate[:rows * cols * 3].reshape(rows, cols, 3)
                 rids[i], cids[i] = srv.submit(strokes, rows=rows, cols=cols, r0=r0, out=out)
             index[rids[i]] = i
             if last[root] == i:
@@ -849,7 +872,7 @@ def run_serve(pg, torch, rate: float, seconds: float, seed: int = 4, budget_gb: 
 
     def consumer():  # results in completion order: buffers go back as soon as they are filled
         got = 0
-        while got < n:
+        while got < n - shed[0] or th.is_alive():
             left = deadline - time.perf_counter()
             rid = srv.poll(max(0.0, left)) if left > 0 else None
             if rid is None:
@@ -865,7 +888,8 @@ def run_serve(pg, torch, rate: float, seconds: float, seed: int = 4, budget_gb: 
             except pg.PaintyError:
                 pass
             pool.give(keys[i])
-            pool.give(r0_keys[i])
+            with lock:
+                outstanding[0] -= 1
 
     th = threading.Thread(target=client)
     tc = threading.Thread(target=consumer)
@@ -874,9 +898,9 @@ def run_serve(pg, torch, rate: float, seconds: float, seed: int = 4, budget_gb: 
     th.join()
     tc.join()
     wall = time.perf_counter() - t0
-    unfinished = int(np.isnan(lat).sum())
+    unfinished = int(sum(1 for i in range(n) if rids[i] is not None and np.isnan(lat[i])))
     for i in range(n):
-        if np.isnan(lat[i]):
+        if rids[i] is not None and np.isnan(lat[i]):
             srv.cancel(rids[i])
     stats = srv.stats()
     srv.close()
@@ -885,6 +909,7 @@ def run_serve(pg, torch, rate: float, seconds: float, seed: int = 4, budget_gb: 
         int(sum(pg_stroke_stamps(p, sp) for p, _, sp, _, _ in strokes)) for *_, strokes in plan)
     out = {"metric": "request latency", "arrival_rate": rate, "arrival_window_s": seconds,
            "requests": n, "completed": int(done.size), "unfinished": unfinished,
+           "shed": shed[0], "max_outstanding": max_outstanding,
            "p50_s": round(float(np.percentile(done, 50)), 4) if done.size else None,
            "p99_s": round(float(np.percentile(done, 99)), 4) if done.size else None,
            "throughput_req_s": round(done.size / wall, 2),
@@ -900,7 +925,7 @@ def run_serve(pg, torch, rate: float, seconds: float, seed: int = 4, budget_gb: 
                      "composite returned per request into a pinned buffer; canvases released "
                      "after their last request"}
     # sustained: nothing left unfinished and completions kept pace with arrivals
-    out["sustained"] = bool(unfinished == 0 and done.size and
+    out["sustained"] = bool(unfinished == 0 and shed[0] == 0 and done.size and
                             out["p99_s"] is not None and out["p99_s"] < 10.0)
     return out
 
@@ -909,12 +934,12 @@ def run_serving(pg, torch, rates=(20.0, 50.0, 100.0), sweep_s: float = 10.0,
                 full_rate: float = 200.0, full_s: float = 60.0):
     """The stated serving run (full_rate req/s for full_s) and a sweep of lower rates over
     shorter windows; reports the highest sustained rate."""
-    pool = _PinnedPool(torch, 24 << 30)
+    pool = _PinnedPool(torch, 32 << 30)
     sweep = [run_serve(pg, torch, r, sweep_s, pool=pool, drain_s=30.0) for r in rates]
     full = run_serve(pg, torch, full_rate, full_s, pool=pool)
     ok = [x["arrival_rate"] for x in sweep + [full] if x["sustained"]]
     full["sweep"] = [{k: x[k] for k in ("arrival_rate", "arrival_window_s", "requests",
-                                        "completed", "unfinished", "p50_s", "p99_s",
+                                        "completed", "unfinished", "shed", "p50_s", "p99_s",
                                         "throughput_req_s", "stamps_per_s", "sustained")}
                      for x in sweep]
     full["highest_sustained_rate"] = max(ok) if ok else None

@@ -582,7 +582,7 @@ __device__ __forceinline__ void load_layer16(const Compose16Args<TK, TV>& a, int
   o.v = ld_stream_u2(a.V[l] + e);
 }
 template <class TK, class TV>
-__global__ void __launch_bounds__(256) km_composite16_kernel(
+__global__ void __launch_bounds__(256, 4) km_composite16_kernel(
   const __grid_constant__ Compose16Args<TK, TV> a) {
   const int64_t groups = a.groups;
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
@@ -605,13 +605,18 @@ __global__ void __launch_bounds__(256) km_composite16_kernel(
 #pragma unroll
       for (int i = 0; i < 4; i += 2) {  // pixel pairs on the packed FP32 pipe
         const float2 d = f2(elem16<TV>(cur.v, i), elem16<TV>(cur.v, i + 1));
+        float2 K[3], S[3], R[3];
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-          const float2 o = km_reflectance2(
-            f2(elem16<TK>(cur.k[c], i), elem16<TK>(cur.k[c], i + 1)),
-            f2(elem16<TK>(cur.s[c], i), elem16<TK>(cur.s[c], i + 1)), f2(r[c][i], r[c][i + 1]), d);
-          r[c][i] = o.x;
-          r[c][i + 1] = o.y;
+          K[c] = f2(elem16<TK>(cur.k[c], i), elem16<TK>(cur.k[c], i + 1));
+          S[c] = f2(elem16<TK>(cur.s[c], i), elem16<TK>(cur.s[c], i + 1));
+          R[c] = f2(r[c][i], r[c][i + 1]);
+        }
+        km_reflectance2x3(K, S, R, d);
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          r[c][i] = R[c].x;
+          r[c][i + 1] = R[c].y;
         }
       }
       cur = nxt;

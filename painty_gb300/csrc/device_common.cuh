@@ -307,6 +307,55 @@ __device__ __forceinline__ float2 km_reflectance2(float2 K, float2 S, float2 R0,
   return f2(fabsf(d.x) < kEps ? R0.x : r.x, fabsf(d.y) < kEps ? R0.y : r.y);
 }
 
+// The three colour channels of two pixels, with one reciprocal per pixel instead of one per
+// channel: R_c = N_c / D_c = N_c * (product of the other two D) / (D_r D_g D_b). D lies
+// between about 0.03 and 30, so the product stays far inside FP32's range; the extra products
+// cost a few roundings (well below FP16 storage's).
+__device__ __forceinline__ void km_reflectance2x3(const float2 (&K)[3], const float2 (&S)[3],
+                                                  float2 (&R)[3], float2 d) {
+  constexpr float kEps = 2.220446049250313e-12f;  // 1e4 * DBL_EPSILON
+  const float2 one = f2(1.0f, 1.0f);
+  float2 num[3], den[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    float2 s = S[c];
+    s.x = fabsf(s.x) > kEps ? s.x : 1e-11f;
+    s.y = fabsf(s.y) > kEps ? s.y : 1e-11f;
+    float2 q = __fmul2_rn(K[c], __ffma2_rn(f2(2.0f, 2.0f), s, K[c]));
+    q.x = fmaxf(q.x, 1e-30f);
+    q.y = fmaxf(q.y, 1e-30f);
+    const float2 beta = __fmul2_rn(q, f2(rsqrt_approx(q.x), rsqrt_approx(q.y)));
+    const float2 x = __fmul2_rn(beta, d);
+    const float2 nR0 = f2(-R[c].x, -R[c].y);
+    const float2 omr = __fadd2_rn(one, nR0);
+    const float2 A = __ffma2_rn(s, omr, __fmul2_rn(nR0, K[c]));
+    const float2 B = __ffma2_rn(s, omr, K[c]);
+    const float2 t = __fmul2_rn(f2(-2.8853900817779268f, -2.8853900817779268f), x);
+    const float2 e = f2(ex2_approx(t.x), ex2_approx(t.y));  // exp(-2x)
+    const float2 x2 = __fmul2_rn(x, x);
+    const float2 g = __ffma2_rn(x2, __ffma2_rn(x2, f2(-1.0f / 45.0f, -1.0f / 45.0f),
+                                                f2(1.0f / 3.0f, 1.0f / 3.0f)), one);
+    const float2 ome = __fadd2_rn(one, f2(-e.x, -e.y));
+    const float2 bope = __fmul2_rn(beta, __fadd2_rn(one, e));
+    const bool sx = x.x < 0.05f, sy = x.y < 0.05f;
+    const float2 u = f2(sx ? d.x : ome.x, sy ? d.y : ome.y);
+    const float2 w = f2(sx ? g.x : bope.x, sy ? g.y : bope.y);
+    num[c] = __ffma2_rn(A, u, __fmul2_rn(R[c], w));
+    den[c] = __ffma2_rn(B, u, w);
+  }
+  const float2 d01 = __fmul2_rn(den[0], den[1]);
+  const float2 d12 = __fmul2_rn(den[1], den[2]);
+  const float2 d02 = __fmul2_rn(den[0], den[2]);
+  const float2 all = __fmul2_rn(d01, den[2]);
+  const float2 inv = f2(rcp_approx(all.x), rcp_approx(all.y));
+  const float2 o[3] = {__fmul2_rn(__fmul2_rn(num[0], d12), inv),
+                       __fmul2_rn(__fmul2_rn(num[1], d02), inv),
+                       __fmul2_rn(__fmul2_rn(num[2], d01), inv)};
+  const bool keep_x = fabsf(d.x) < kEps, keep_y = fabsf(d.y) < kEps;
+#pragma unroll
+  for (int c = 0; c < 3; c++) R[c] = f2(keep_x ? R[c].x : o[c].x, keep_y ? R[c].y : o[c].y);
+}
+
 // painty's coth (painty/core/Math.hxx:157-169) and ComputeReflectance in double, in the
 // reference's own operation order; for the F64 parity storage mode.
 __device__ __forceinline__ double coth_ref(double x) {
