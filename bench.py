@@ -65,7 +65,8 @@ class ClockSampler:
 
     Q = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,"
+         "utilization.gpu")
 
     def __init__(self, index: int = 0):
         self.index = index
@@ -112,7 +113,8 @@ class ClockSampler:
                 continue
             try:
                 ts = datetime.datetime.strptime(f[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
-                rows.append((ts, float(f[1]), float(f[2]), f[5], f[6], f[7], f[8]))
+                util = float(f[9]) if len(f) > 9 else float("nan")
+                rows.append((ts, float(f[1]), float(f[2]), f[5], f[6], f[7], f[8], util))
             except ValueError:
                 continue
         os.unlink(self.file.name)
@@ -130,8 +132,10 @@ class ClockSampler:
         sm = sorted(r[0] for r in rows)
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[i] for r in rows for i in range(4) if r[2 + i] == "Active"})
+        util = [r[6] for r in rows if r[6] == r[6]]
         return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": max(r[1] for r in rows),
-                "reasons": reasons, "samples": len(rows), "window": where}
+                "reasons": reasons, "samples": len(rows), "window": where,
+                "gpu_util_pct_mean": round(float(np.mean(util)), 1) if util else None}
 
 
 def _workloads_module():
@@ -893,11 +897,16 @@ def run_serve(pg, torch, rate: float, seconds: float, seed: int = 4, budget_gb: 
 
     th = threading.Thread(target=client)
     tc = threading.Thread(target=consumer)
+    sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))).__enter__()
+    w0 = time.time()
     th.start()
     tc.start()
     th.join()
     tc.join()
     wall = time.perf_counter() - t0
+    sampler.window = (w0, time.time())
+    sampler.__exit__(None, None, None)
+    device = sampler.summary()
     unfinished = int(sum(1 for i in range(n) if rids[i] is not None and np.isnan(lat[i])))
     for i in range(n):
         if rids[i] is not None and np.isnan(lat[i]):
@@ -919,6 +928,8 @@ def run_serve(pg, torch, rate: float, seconds: float, seed: int = 4, budget_gb: 
            "evictions": stats["evictions"], "restores": stats["restores"],
            "launches": stats["steps"],
            "server_worker_busy_frac": round(stats["worker_busy_us"] / 1e6 / wall, 3),
+           "gpu_util_pct_mean": device.get("gpu_util_pct_mean"),
+           "clocks": {k: device.get(k) for k in ("sm_mhz", "sm_max_mhz", "reasons")},
            "peak_resident_gb": round(stats["peak_resident_bytes"] / 2**30, 2),
            "config": "Poisson arrivals; canvas side logU[512,4096]; 1-500 strokes (geometric, "
                      "mean 60), r U[8,32], spacing 0.25 r; 30% continue an earlier canvas; "

@@ -540,7 +540,7 @@ void gl_paint_stroke(painty_canvas* c, painty_gpu_texture_brush* b, const double
   std::memcpy(host.data() + 2 * bx, tu.data(), bf);
   std::memcpy(host.data() + 2 * bx + bf, tv.data(), bf);
   char* dv = nullptr;
-  PG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&dv), host.size(), st));
+  dv = static_cast<decltype(dv)>(temp_alloc(host.size(), st));
   PG_CUDA(cudaMemcpyAsync(dv, host.data(), host.size(), cudaMemcpyHostToDevice, st));
   StripArgs sa{};
   sa.X = reinterpret_cast<const long long*>(dv);

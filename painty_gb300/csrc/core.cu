@@ -7,6 +7,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -91,6 +92,32 @@ void* device_alloc_on(size_t bytes, cudaMemPool_t pool, cudaStream_t st) {
 }
 void device_free_on(void* p, cudaStream_t st) {
   if (p) cudaFreeAsync(p, st);
+}
+
+// The library's pool for launch temporaries, one per device, keeping freed memory for reuse:
+// the default pool returns memory at every synchronisation, and mapping it again on the next
+// allocation costs more than the launches it serves.
+void* temp_alloc(size_t bytes, cudaStream_t st) {
+  static std::mutex mu;
+  static cudaMemPool_t pools[64] = {};
+  int dev = 0;
+  PG_CUDA(cudaGetDevice(&dev));
+  PG_REQUIRE(dev >= 0 && dev < 64, "device ordinal out of range");
+  cudaMemPool_t pool = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (!pools[dev]) {
+      cudaMemPoolProps props{};
+      props.allocType = cudaMemAllocationTypePinned;
+      props.location.type = cudaMemLocationTypeDevice;
+      props.location.id = dev;
+      PG_CUDA(cudaMemPoolCreate(&pools[dev], &props));
+      uint64_t keep = ~0ull;
+      PG_CUDA(cudaMemPoolSetAttribute(pools[dev], cudaMemPoolAttrReleaseThreshold, &keep));
+    }
+    pool = pools[dev];
+  }
+  return device_alloc_on(std::max<size_t>(bytes, 16), pool, st);
 }
 
 // Planar: 7 planes, each 256-byte aligned. Packed: one record of 8 elements per pixel (K and
@@ -375,7 +402,7 @@ void upload_planes_async(void* const* planes, int nch, DevType dt, int32_t rows,
     }
   }
   void* staging = nullptr;
-  PG_CUDA(cudaMallocAsync(&staging, n * nch * hes, st));
+  staging = temp_alloc(n * nch * hes, st);
   PG_CUDA(cudaMemcpyAsync(staging, host, n * nch * hes, cudaMemcpyHostToDevice, st));
   PlanePtrs pp{{planes[0], nch > 1 ? planes[1] : nullptr, nch > 2 ? planes[2] : nullptr}};
   const int il = host_is_interleaved(fmt) ? 1 : 0;
@@ -414,7 +441,7 @@ void download_planes_async(const void* const* planes, int nch, DevType dt, int32
     }
   }
   void* staging = nullptr;
-  PG_CUDA(cudaMallocAsync(&staging, n * nch * hes, st));
+  staging = temp_alloc(n * nch * hes, st);
   PlanePtrs pp{{const_cast<void*>(planes[0]), nch > 1 ? const_cast<void*>(planes[1]) : nullptr,
                 nch > 2 ? const_cast<void*>(planes[2]) : nullptr}};
   const int il = host_is_interleaved(fmt) ? 1 : 0;
@@ -1012,7 +1039,7 @@ painty_status painty_layer_set_cells(painty_layer* layer, int64_t n, const int32
     char* d = nullptr;
     const size_t brc = static_cast<size_t>(n) * 2 * sizeof(int32_t);
     const size_t bv = vals.size() * sizeof(double);
-    PG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&d), brc + bv + 16, st));
+    d = static_cast<decltype(d)>(pg::temp_alloc(brc + bv + 16, st));
     char* dv = d + (brc + 15) / 16 * 16;
     PG_CUDA(cudaMemcpyAsync(d, rows_cols, brc, cudaMemcpyHostToDevice, st));
     PG_CUDA(cudaMemcpyAsync(dv, vals.data(), bv, cudaMemcpyHostToDevice, st));
@@ -1151,10 +1178,10 @@ painty_status painty_compose_layers_host(const float* K, const float* S, const f
     PG_REQUIRE(R0 && out, "R0 or out is null");
     constexpr int kStreams = 3;
     const int64_t pitch = pg::pitch_for(cols);
-    // bands of about 96 MB of layer data each (large copies keep the copy engines at speed)
+    // bands of about 16 MB of layer data each
     const int64_t row_bytes = static_cast<int64_t>(7 * L + 6) * pitch * 4;
     const int32_t band = static_cast<int32_t>(
-      std::max<int64_t>(1, std::min<int64_t>(rows, (int64_t(96) << 20) / row_bytes)));
+      std::max<int64_t>(1, std::min<int64_t>(rows, (int64_t(16) << 20) / row_bytes)));
     const int64_t plane = static_cast<int64_t>(band) * pitch;  // device plane of one band
     const int64_t nplanes = 7 * static_cast<int64_t>(L) + 6;   // K, S, V, R0, out
     PG_CUDA(cudaStreamSynchronize(pg::as_stream(stream)));
@@ -1172,24 +1199,13 @@ painty_status painty_compose_layers_host(const float* K, const float* S, const f
     try {
       for (int i = 0; i < kStreams; i++) {
         PG_CUDA(cudaStreamCreateWithFlags(&st[i], cudaStreamNonBlocking));
-        PG_CUDA(cudaMallocAsync(&buf[i], static_cast<size_t>(nplanes * plane) * 4, st[i]));
+        buf[i] = pg::temp_alloc(static_cast<size_t>(nplanes * plane) * 4, st[i]);
         // the pitch padding is computed on but never copied out: start it at zero
         PG_CUDA(cudaMemsetAsync(buf[i], 0, static_cast<size_t>(nplanes * plane) * 4, st[i]));
       }
       // host planes [n][rows][cols] <-> device planes [n][band][pitch], rows r0 .. r0 + h
       auto copy3d = [&](const float* hbase, float* dbase, int n, int32_t r0, int32_t h,
                         bool up, cudaStream_t s) {
-        if (pitch == cols) {  // each plane's band is one contiguous run on both sides
-          const size_t run = static_cast<size_t>(h) * cols * 4;
-          const size_t hstep = static_cast<size_t>(rows) * cols * 4, dstep = plane * 4;
-          char* hp = reinterpret_cast<char*>(const_cast<float*>(hbase)) +
-                     static_cast<size_t>(r0) * cols * 4;
-          if (up)
-            PG_CUDA(cudaMemcpy2DAsync(dbase, dstep, hp, hstep, run, n, cudaMemcpyHostToDevice, s));
-          else
-            PG_CUDA(cudaMemcpy2DAsync(hp, hstep, dbase, dstep, run, n, cudaMemcpyDeviceToHost, s));
-          return;
-        }
         cudaMemcpy3DParms m{};
         cudaPitchedPtr hp = make_cudaPitchedPtr(const_cast<float*>(hbase), cols * 4, cols, rows);
         cudaPitchedPtr dp = make_cudaPitchedPtr(dbase, pitch * 4, pitch, band);

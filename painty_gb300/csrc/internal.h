@@ -69,6 +69,9 @@ void device_free(void* p);
 // objects a long-running owner (the server) creates and drops while kernels run.
 void* device_alloc_on(size_t bytes, cudaMemPool_t pool, cudaStream_t st);
 void device_free_on(void* p, cudaStream_t st);
+// A launch temporary, ordered on `st` (free with cudaFreeAsync on a stream ordered after its
+// last use), from the library's own pool that keeps freed memory for reuse.
+void* temp_alloc(size_t bytes, cudaStream_t st);
 
 }  // namespace pg
 

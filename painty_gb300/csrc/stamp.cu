@@ -2045,7 +2045,7 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   const size_t o_fp = piece(fptable.data(), fptable.size() * sizeof(M));
   const size_t o_order = piece(order.data(), order.size() * sizeof(int32_t));
   void* d_desc = nullptr;
-  PG_CUDA(cudaMallocAsync(&d_desc, hdesc.size(), st));
+  d_desc = temp_alloc(hdesc.size(), st);
   PG_CUDA(cudaMemcpyAsync(d_desc, hdesc.data(), hdesc.size(), cudaMemcpyHostToDevice, st));
   auto at = [&](size_t off) { return static_cast<void*>(static_cast<char*>(d_desc) + off); };
   void* d_canvas = at(o_canvas);
@@ -2064,7 +2064,7 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   const size_t s_cm = align_up(s_own + slots * ostride * sizeof(int), 256);
   const size_t s_end = align_up(s_cm + std::max<int64_t>(slots * cmstride, 4) * sizeof(int), 256);
   void* d_scratch = nullptr;
-  PG_CUDA(cudaMallocAsync(&d_scratch, s_end, st));
+  d_scratch = temp_alloc(s_end, st);
   PG_CUDA(cudaMemsetAsync(d_scratch, 0, sizeof(int) * (8 + slots), st));
   auto sat = [&](size_t off) { return static_cast<void*>(static_cast<char*>(d_scratch) + off); };
   void* d_counter = sat(s_counter);

@@ -764,7 +764,7 @@ int64_t paint_texture_stroke(painty_canvas* c, painty_texture_brush* b, const do
   const size_t off_poly = 0, off_uv = align256(np * sizeof(double2)),
                off_max = off_uv + align256(np * sizeof(double2)),
                off_tmap = off_max + 256, total = off_tmap + align256(tmap_bytes);
-  PG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&d), total, st));
+  d = static_cast<decltype(d)>(temp_alloc(total, st));
   PG_CUDA(cudaMemcpyAsync(d + off_poly, up.data(), np * sizeof(double2), cudaMemcpyHostToDevice, st));
   PG_CUDA(cudaMemcpyAsync(d + off_uv, upUv.data(), np * sizeof(double2), cudaMemcpyHostToDevice, st));
   PG_CUDA(cudaMemsetAsync(d + off_max, 0, 256 + align256(tmap_bytes), st));
@@ -845,8 +845,8 @@ int64_t paint_texture_stroke(painty_canvas* c, painty_texture_brush* b, const do
         b->maps_zero = false;
       }
       SmudgeStep<M>* dsteps = nullptr;
-      PG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&dsteps),
-                              std::max<size_t>(steps.size(), 1) * sizeof(SmudgeStep<M>), st));
+      dsteps = static_cast<SmudgeStep<M>*>(
+        temp_alloc(std::max<size_t>(steps.size(), 1) * sizeof(SmudgeStep<M>), st));
       if (!steps.empty())
         PG_CUDA(cudaMemcpyAsync(dsteps, steps.data(), steps.size() * sizeof(SmudgeStep<M>),
                                 cudaMemcpyHostToDevice, st));
