@@ -98,6 +98,7 @@ enum BoundsKind : unsigned {
   kBoundsFootprint = 3, // footprint height
   kBoundsCellMap = 4,   // per-stamp cell map
   kBoundsOwner = 5,     // owner table
+  kBoundsDescriptor = 6,  // batch descriptors (canvas, stroke, path points, footprint, slot)
 };
 __device__ __forceinline__ bool in_bounds(unsigned* status, unsigned kind, int64_t idx,
                                           int64_t n) {

@@ -1190,6 +1190,9 @@ struct BatchArgs {
   int* scratch_cellmap;  // per cluster: CTAs x 2 Fmax^2 (strokes whose cell maps are global)
   int64_t pickup_stride, owner_stride, cellmap_stride;
   unsigned* status;
+  // extents of the descriptor arrays and the scratch, for the bounds-checked build
+  int64_t nstrokes, npoints, nfootprint;
+  int32_t nslots;
 };
 
 // Persistent batched painting: each CTA claims canvases (heaviest first) and applies their
@@ -1221,11 +1224,23 @@ __global__ void __launch_bounds__(kStampThreads, 1) batch_kernel(const __grid_co
       __syncthreads();
     const int ci = s_item;
     if (ci < 0) return;
+    if (!in_bounds(b.status, kBoundsDescriptor, ci, b.ncanvas) ||
+        !in_bounds(b.status, kBoundsDescriptor, cid, b.nslots))
+      return;
     const BatchCanvas<TK, TV>& cv = b.canvases[ci];
+    if (!in_bounds(b.status, kBoundsDescriptor, cv.first_stroke + cv.nstrokes - 1,
+                   b.nstrokes + (cv.nstrokes == 0 ? 1 : 0)))
+      continue;
     bool ran = false;  // a stroke with stamps has run on this canvas (uniform over the CTA)
     for (int32_t k = 0; k < cv.nstrokes; k++) {
       const BatchStroke& st = b.strokes[cv.first_stroke + k];
       const int nseg = st.npoints - 1;
+      if (!in_bounds(b.status, kBoundsDescriptor, st.first_point + st.npoints - 1,
+                     b.npoints + (st.npoints == 0 ? 1 : 0)) ||
+          !in_bounds(b.status, kBoundsDescriptor, st.fp_offset + int64_t(st.F) * st.F - 1,
+                     b.nfootprint) ||
+          !in_bounds(b.status, kBoundsDescriptor, nseg, kMaxPathPoints))
+        continue;
       __syncthreads();
       if (tid == 0) {
         const bool last = k + 1 == cv.nstrokes;
@@ -1304,7 +1319,7 @@ __global__ void __launch_bounds__(kStampThreads, 1) batch_kernel(const __grid_co
         else
           run_stroke<false, false, true, true>(sa, src, smem_raw, sparams, &sh);
       } else {
-        switch (st.plan) {
+        switch (st.plan & 3) {  // bit 2 (global cell maps) travels in sa.cellmap_global
           case 0: run_stroke<false, false, false, true>(sa, src, smem_raw, sparams, &sh); break;
           case 1: run_stroke<true, false, false, true>(sa, src, smem_raw, sparams, &sh); break;
           case 2: run_stroke<false, true, false, true>(sa, src, smem_raw, sparams, &sh); break;
@@ -2087,6 +2102,10 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   a.cellmap_stride = cmstride;
   a.pickup_stride = pstride;
   a.owner_stride = ostride;
+  a.nstrokes = static_cast<int64_t>(bs.size());
+  a.npoints = npoints;
+  a.nfootprint = static_cast<int64_t>(fptable.size());
+  a.nslots = slots;
   launch_clustered(kern, grid, cl, std::max<size_t>(dyn, 16), st, a);
   count_launch();
   PG_CUDA(cudaGetLastError());

@@ -99,6 +99,33 @@ def test_batch_f64_equals_sequential_and_oracle(pg, oracle, snap, rmin, rmax):
         assert bs[ci].info() == bs2[ci].info()
 
 
+@pytest.mark.parametrize("cluster", ["1", "2"])
+def test_batch_forced_cluster_large_radii_f64(pg, oracle, monkeypatch, cluster):
+    """One CTA per canvas (and a 2-CTA cluster) with radii 40-75, whose cell maps live in
+    global memory beside the pickup map and owner table in shared or global memory: F64
+    bit-exact against the oracle."""
+    monkeypatch.setenv("PAINTY_BATCH_CLUSTER", cluster)
+    rng = np.random.default_rng(21)
+    sizes = _canvases(rng, 4, smin=120, smax=220)
+    strokes = _session(rng, sizes, strokes_per=(2, 4), rmin=40.0, rmax=75.0)
+    cs, bs, r0s = _setup(pg, sizes, "f64")
+    pg.paint_batch(cs, bs, strokes)
+    assert pg.batch_last_shape()[0] == int(cluster)
+    fp = workloads.footprint_image(seed=7)
+    for ci, (rows, cols) in enumerate(sizes):
+        oc = oracle.canvas(rows, cols)
+        oc.set("R0", r0s[ci])
+        ob = oracle.brush(3.0, fp)
+        ob.set_rates(0.05, 0.1)
+        for cj, path, r, spacing, K, S in strokes:
+            if cj == ci:
+                ob.set_radius(r)
+                ob.dip(K, S)
+                ob.paint_stroke(oc, path, spacing)
+        for p in ("K", "S", "V"):
+            assert np.array_equal(cs[ci].download(p), oc.get(p)), (ci, p)
+
+
 def test_batch_f32_close_to_sequential(pg):
     rng = np.random.default_rng(5)
     sizes = _canvases(rng, 12, 64, 300)
