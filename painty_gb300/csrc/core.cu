@@ -94,6 +94,16 @@ void device_free_on(void* p, cudaStream_t st) {
   if (p) cudaFreeAsync(p, st);
 }
 
+// Settings of the library's stream-ordered pools: freed memory is kept for reuse, and memory
+// freed on one stream is not handed to another by making the second wait for the first (that
+// reuse would chain independent streams, e.g. a server's requests, into one).
+void configure_pool(cudaMemPool_t pool) {
+  uint64_t keep = ~0ull;
+  PG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+  int no = 0;
+  PG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolReuseAllowInternalDependencies, &no));
+}
+
 // The library's pool for launch temporaries, one per device, keeping freed memory for reuse:
 // the default pool returns memory at every synchronisation, and mapping it again on the next
 // allocation costs more than the launches it serves.
@@ -112,8 +122,7 @@ void* temp_alloc(size_t bytes, cudaStream_t st) {
       props.location.type = cudaMemLocationTypeDevice;
       props.location.id = dev;
       PG_CUDA(cudaMemPoolCreate(&pools[dev], &props));
-      uint64_t keep = ~0ull;
-      PG_CUDA(cudaMemPoolSetAttribute(pools[dev], cudaMemPoolAttrReleaseThreshold, &keep));
+      configure_pool(pools[dev]);
     }
     pool = pools[dev];
   }

@@ -72,6 +72,8 @@ void device_free_on(void* p, cudaStream_t st);
 // A launch temporary, ordered on `st` (free with cudaFreeAsync on a stream ordered after its
 // last use), from the library's own pool that keeps freed memory for reuse.
 void* temp_alloc(size_t bytes, cudaStream_t st);
+// Pool settings shared by the library's pools (retained memory, no cross-stream reuse waits).
+void configure_pool(cudaMemPool_t pool);
 
 }  // namespace pg
 

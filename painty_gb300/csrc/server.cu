@@ -90,6 +90,8 @@ struct Slot {
   cudaEvent_t ev = nullptr;
   unsigned* status = nullptr;  // pinned: the last launch's kernel status word
   bool busy = false;
+  painty_server* owner = nullptr;
+  int index = 0;
 };
 
 }  // namespace
@@ -112,6 +114,7 @@ struct painty_server {
   std::unordered_map<uint64_t, std::unique_ptr<ServerRequest>> reqs;
   std::unordered_map<uint64_t, std::unique_ptr<ServerCanvas>> canvases;
   std::vector<ServerCanvas*> to_drop;  // released canvases waiting for the worker to free them
+  std::vector<int> passed;  // slots whose stream reached the end of their last launch
   size_t resident = 0, peak = 0;
   uint64_t next_req = 1, next_canvas = 1, tick = 0;
   painty_server_counters stats{};
@@ -157,6 +160,23 @@ void blob_save(painty_server* s, HostBlob& b, const void* dev, size_t bytes) {
     b.p = pinned_take(s, bytes, &b.bytes);
   }
   PG_CUDA(cudaMemcpyAsync(b.p, dev, bytes, cudaMemcpyDeviceToHost, s->stream));
+}
+
+// Host callback at the end of a slot's launched work: the worker learns of it without polling.
+void CUDART_CB slot_passed(void* p) {
+  Slot* sl = static_cast<Slot*>(p);
+  painty_server* s = sl->owner;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->passed.push_back(sl->index);
+  }
+  s->cv_work.notify_one();
+}
+
+// Marks the end of the work just queued on a slot: its event and the callback after it.
+void mark_slot(Slot& sl) {
+  PG_CUDA(cudaEventRecord(sl.ev, sl.st));
+  PG_CUDA(cudaLaunchHostFunc(sl.st, slot_passed, &sl));
 }
 
 void image_alloc(painty_server* s, ServerCanvas* c, cudaStream_t st) {
@@ -327,7 +347,7 @@ void launch_chunk(painty_server* s, ServerRequest* r, ServerCanvas* c, int cap) 
   painty_brush* brs[1] = {c->brush};
   pg::paint_batch(cvs, brs, 1, descs.data(), static_cast<int64_t>(descs.size()), pts.data(),
                   static_cast<int64_t>(pts.size() / 2), &n, sl.st, &opt);
-  PG_CUDA(cudaEventRecord(sl.ev, sl.st));
+  mark_slot(sl);
   r->stamps += budget;
   r->next = k;
 }
@@ -342,7 +362,7 @@ void launch_finish(painty_server* s, ServerRequest* r, ServerCanvas* c) {
   // out_rgb is float RGB whatever the storage (F64 results are rounded to float)
   pg::download_planes_async(p, 3, pg::r_type(c->img.storage), c->rows, c->cols, c->img.pitch,
                             r->out_rgb, PAINTY_HOST_F32_INTERLEAVED, sl.st);
-  PG_CUDA(cudaEventRecord(sl.ev, sl.st));
+  mark_slot(sl);
 }
 
 struct Admitted {
@@ -416,11 +436,20 @@ bool worker_round(painty_server* s, std::unique_lock<std::mutex>& lk) {
     bool cancel;
   };
   std::vector<Running> running;
-  for (uint64_t id : s->active) {
-    ServerRequest* r = s->reqs[id].get();
-    bool fresh = false;
-    for (const Admitted& a : admitted) fresh = fresh || a.r == r;
-    if (!fresh) running.push_back({r, s->canvases[r->canvas_id].get(), r->cancel});
+  std::vector<int> passed;
+  passed.swap(s->passed);
+  if (!passed.empty()) {
+    std::vector<ServerRequest*> by_slot(s->slots.size(), nullptr);
+    for (uint64_t id : s->active) {
+      ServerRequest* r = s->reqs[id].get();
+      if (r->slot >= 0) by_slot[r->slot] = r;
+    }
+    for (int slot : passed) {
+      ServerRequest* r = by_slot[slot];
+      bool fresh = false;
+      for (const Admitted& a : admitted) fresh = fresh || a.r == r;
+      if (r && !fresh) running.push_back({r, s->canvases[r->canvas_id].get(), r->cancel});
+    }
   }
   const int cap = cluster_cap(s);
   s->tick++;
@@ -458,7 +487,7 @@ bool worker_round(painty_server* s, std::unique_lock<std::mutex>& lk) {
         if (a.r->out_rgb)
           launch_finish(s, a.r, a.c);
         else
-          PG_CUDA(cudaEventRecord(s->slots[a.r->slot].ev, s->slots[a.r->slot].st));
+          mark_slot(s->slots[a.r->slot]);
       } else {
         launch_chunk(s, a.r, a.c, cap);
         chunks++;
@@ -495,14 +524,16 @@ bool worker_round(painty_server* s, std::unique_lock<std::mutex>& lk) {
     }
   }
 
+  // a failed request's slot is not reused before its stream has drained (its callback takes
+  // the lock, so the wait happens here, unlocked)
+  for (auto& f : failures)
+    if (f.first->slot >= 0) cudaStreamSynchronize(s->slots[f.first->slot].st);
   const double busy = now_s() - t_work;
   lk.lock();
   for (ServerCanvas* c : drops) s->canvases.erase(c->id);  // its requests are all finished
   s->stats.steps += chunks;
   s->stats.worker_busy_us += static_cast<int64_t>(busy * 1e6);
   for (auto& f : failures) {
-    // a failed request's slot is not reused before its stream has drained
-    if (f.first->slot >= 0) cudaStreamSynchronize(s->slots[f.first->slot].st);
     finish(s, f.first, PAINTY_ERR_CUDA, f.second);
     s->active.erase(std::find(s->active.begin(), s->active.end(), f.first->id));
   }
@@ -522,21 +553,15 @@ void worker_main(painty_server* s) {
   std::unique_lock<std::mutex> lk(s->mu);
   uint64_t idle_gen = ~0ull;
   while (true) {
-    s->cv_work.wait(lk, [&] {
-      return s->stop || !s->active.empty() || !s->to_drop.empty() ||
+    // wake on a finished launch, a drop, or a change to what could be admitted
+    s->cv_work.wait_for(lk, std::chrono::milliseconds(50), [&] {
+      return s->stop || !s->passed.empty() || !s->to_drop.empty() ||
              (!s->pending.empty() && s->gen != idle_gen);
     });
     if (s->stop) break;
     const uint64_t g = s->gen;
-    const bool moved = worker_round(s, lk);
-    if (s->active.empty()) {
-      // nothing in flight and nothing admitted: sleep until a submit, cancel or release
-      idle_gen = g;
-    } else {
-      idle_gen = ~0ull;
-      // kernels are running: poll their events again shortly, or sooner on a new request
-      if (!moved) s->cv_work.wait_for(lk, std::chrono::microseconds(200));
-    }
+    worker_round(s, lk);
+    idle_gen = g;  // admit again only after a submit, cancel, release or finish
   }
   // shutting down: every request still queued is cancelled; launched work drains first
   std::vector<uint64_t> act = s->active;
@@ -580,8 +605,7 @@ painty_status painty_server_create(const painty_server_options* opt, painty_serv
     props.location.type = cudaMemLocationTypeDevice;
     props.location.id = s->device;
     PG_CUDA(cudaMemPoolCreate(&s->pool, &props));
-    uint64_t keep = ~0ull;
-    PG_CUDA(cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    pg::configure_pool(s->pool);
     PG_CUDA(cudaMallocHost(&s->status_words, sizeof(unsigned) * s->opt.max_active));
     s->slots.resize(static_cast<size_t>(s->opt.max_active));
     for (int i = 0; i < s->opt.max_active; i++) {
@@ -590,6 +614,8 @@ painty_status painty_server_create(const painty_server_options* opt, painty_serv
       PG_CUDA(cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming));
       sl.status = s->status_words + i;
       *sl.status = 0;
+      sl.owner = s.get();
+      sl.index = i;
     }
     painty_server* raw = s.get();
     s->worker = std::thread(worker_main, raw);
