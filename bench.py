@@ -928,6 +928,10 @@ def run_serve(pg, torch, rate: float, seconds: float, seed: int = 4, budget_gb: 
            "evictions": stats["evictions"], "restores": stats["restores"],
            "launches": stats["steps"],
            "server_worker_busy_frac": round(stats["worker_busy_us"] / 1e6 / wall, 3),
+           "server_worker_ms_per": {
+               "new_canvas": round(stats["worker_create_us"] / 1e3 / max(1, stats["submitted"]), 3),
+               "stamp_launch": round(stats["worker_launch_us"] / 1e3 / max(1, stats["steps"]), 3),
+               "finish_launch": round(stats["worker_finish_us"] / 1e3 / max(1, stats["completed"]), 3)},
            "gpu_util_pct_mean": device.get("gpu_util_pct_mean"),
            "clocks": {k: device.get(k) for k in ("sm_mhz", "sm_max_mhz", "reasons")},
            "peak_resident_gb": round(stats["peak_resident_bytes"] / 2**30, 2),

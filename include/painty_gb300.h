@@ -382,7 +382,9 @@ typedef struct painty_server_counters {
   int64_t steps, stamps, evictions, restores;  /* steps: stamp-kernel launches */
   uint64_t resident_bytes, peak_resident_bytes;
   int64_t active, pending, canvases;
-  int64_t worker_busy_us;  /* time the worker thread spent issuing device work */
+  int64_t worker_busy_us;  /* time the worker thread spent issuing device work, of which: */
+  int64_t worker_create_us, worker_launch_us, worker_finish_us; /* new canvases, stamp
+                              launches, composite + download launches */
 } painty_server_counters;
 painty_status painty_server_create(const painty_server_options* options, painty_server** out);
 /* Non-blocking. Returns the request id and its canvas id (new canvases get one here). */

@@ -777,7 +777,9 @@ class _Counters(C.Structure):
     _fields_ = [(n, C.c_int64) for n in ("submitted", "completed", "failed", "cancelled", "steps",
                                           "stamps", "evictions", "restores")] + \
                [("resident_bytes", C.c_uint64), ("peak_resident_bytes", C.c_uint64)] + \
-               [(n, C.c_int64) for n in ("active", "pending", "canvases", "worker_busy_us")]
+               [(n, C.c_int64) for n in ("active", "pending", "canvases", "worker_busy_us",
+                                          "worker_create_us", "worker_launch_us",
+                                          "worker_finish_us")]
 
 
 _sig("painty_server_create", C.POINTER(_ServerOptions), C.POINTER(_P))

@@ -319,6 +319,7 @@ int cluster_cap(const painty_server* s) {
 
 // Launches the next chunk of a request's strokes (worker thread, lock not held).
 void launch_chunk(painty_server* s, ServerRequest* r, ServerCanvas* c, int cap) {
+  const double t0 = now_s();
   Slot& sl = s->slots[r->slot];
   size_t k = r->next;
   int64_t budget = 0;
@@ -350,11 +351,13 @@ void launch_chunk(painty_server* s, ServerRequest* r, ServerCanvas* c, int cap) 
   mark_slot(sl);
   r->stamps += budget;
   r->next = k;
+  s->stats.worker_launch_us += static_cast<int64_t>((now_s() - t0) * 1e6);
 }
 
 // The composite of a finished request's canvas, downloaded into the caller's buffer in the
 // slot's stream order (worker thread).
 void launch_finish(painty_server* s, ServerRequest* r, ServerCanvas* c) {
+  const double t0 = now_s();
   Slot& sl = s->slots[r->slot];
   const painty_layer* L[1] = {&c->cv->wet};
   pg::launch_compose(L, 1, &c->cv->r0, &c->img, sl.st);
@@ -363,6 +366,7 @@ void launch_finish(painty_server* s, ServerRequest* r, ServerCanvas* c) {
   pg::download_planes_async(p, 3, pg::r_type(c->img.storage), c->rows, c->cols, c->img.pitch,
                             r->out_rgb, PAINTY_HOST_F32_INTERLEAVED, sl.st);
   mark_slot(sl);
+  s->stats.worker_finish_us += static_cast<int64_t>((now_s() - t0) * 1e6);
 }
 
 struct Admitted {
@@ -476,7 +480,9 @@ bool worker_round(painty_server* s, std::unique_lock<std::mutex>& lk) {
     try {
       if (a.prep) {
         if (!a.c->cv) {
+          const double t = now_s();
           create(s, a.c, s->slots[a.r->slot].st);
+          s->stats.worker_create_us += static_cast<int64_t>((now_s() - t) * 1e6);
         } else {
           restore(s, a.c);
           s->stats.restores++;
@@ -606,6 +612,17 @@ painty_status painty_server_create(const painty_server_options* opt, painty_serv
     props.location.id = s->device;
     PG_CUDA(cudaMemPoolCreate(&s->pool, &props));
     pg::configure_pool(s->pool);
+    // map the budget into the pool once: canvases are then carved from it without the pool
+    // growing (mapping fresh memory) under load
+    {
+      void* r = nullptr;
+      if (cudaMallocFromPoolAsync(&r, s->opt.budget_bytes, s->pool, s->stream) == cudaSuccess) {
+        cudaFreeAsync(r, s->stream);
+        PG_CUDA(cudaStreamSynchronize(s->stream));
+      } else {
+        cudaGetLastError();  // the budget is more than is free now: the pool grows as needed
+      }
+    }
     PG_CUDA(cudaMallocHost(&s->status_words, sizeof(unsigned) * s->opt.max_active));
     s->slots.resize(static_cast<size_t>(s->opt.max_active));
     for (int i = 0; i < s->opt.max_active; i++) {
