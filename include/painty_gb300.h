@@ -135,12 +135,13 @@ painty_status painty_compose_layers_unfused(const painty_layer* const* layers, i
                                             const painty_image* r0, painty_image* out,
                                             void* stream);
 /* Renderer::compose of layer stacks held in host memory into a host image
- * (painty/renderer/Renderer.hxx:26-53, returning a host Mat; per layer PaintLayer.hxx:81-96):
- * the composite of painty_compose_layers with the transfers pipelined in row bands on three
- * internal streams, so the upload of one band, the composite of another and the download of a
- * third overlap. Host layout, FP32 planar, rows x cols per plane, contiguous: K and S
- * [L][3][rows][cols], V [L][rows][cols], R0 and out [3][rows][cols]. Pinned host buffers give
- * full host-link speed. Returns once `out` holds the result; `stream` is waited on first. */
+ * (painty/renderer/Renderer.hxx:26-53, returning a host Mat; per layer PaintLayer.hxx:81-96).
+ * Host layout, FP32 planar, rows x cols per plane, contiguous: K and S [L][3][rows][cols],
+ * V [L][rows][cols], R0 and out [3][rows][cols]. When every buffer is pinned (mapped into the
+ * device's address space; rows * cols a multiple of 4, planes 16-byte aligned) the fused
+ * composite reads and writes them in place over the host link; otherwise the transfers run
+ * in row bands on three internal streams, the upload of one band, the composite of another and
+ * the download of a third overlapping. Returns once `out` holds the result. */
 painty_status painty_compose_layers_host(const float* K, const float* S, const float* V,
                                          int32_t L, const float* R0, float* out, int32_t rows,
                                          int32_t cols, void* stream);

@@ -1185,6 +1185,59 @@ painty_status painty_compose_layers_host(const float* K, const float* S, const f
     PG_REQUIRE(rows > 0 && cols > 0, "rows and cols must be positive");
     PG_REQUIRE(L >= 0 && (L == 0 || (K && S && V)), "layer planes are null");
     PG_REQUIRE(R0 && out, "R0 or out is null");
+    const int64_t npix = static_cast<int64_t>(rows) * cols;
+    // Pinned host buffers are mapped into the device's address space (and on Grace-Blackwell
+    // read coherently over NVLink-C2C): the fused composite then reads the layer stacks and
+    // writes the image where they lie, streaming at the host link's rate with no staging.
+    // Planes must start on 16 bytes and hold a multiple of 4 pixels for its vector accesses.
+    {
+      const float* hp[5] = {K, S, V, R0, out};
+      const float* dp[5] = {};
+      bool mapped = npix % 4 == 0;
+      for (int i = 0; i < 5 && mapped; i++) {
+        if (!hp[i]) continue;  // no layers
+        cudaPointerAttributes pa{};
+        if (cudaPointerGetAttributes(&pa, hp[i]) != cudaSuccess || pa.type != cudaMemoryTypeHost ||
+            !pa.devicePointer || (reinterpret_cast<uintptr_t>(pa.devicePointer) & 15) != 0) {
+          cudaGetLastError();
+          mapped = false;
+          break;
+        }
+        dp[i] = static_cast<const float*>(pa.devicePointer);
+      }
+      if (mapped) {
+        const cudaStream_t st = pg::as_stream(stream);
+        std::vector<painty_layer> views(static_cast<size_t>(L));
+        std::vector<const painty_layer*> lp(static_cast<size_t>(L));
+        for (int32_t l = 0; l < L; l++) {
+          painty_layer& ly = views[l];
+          ly.rows = rows;
+          ly.cols = cols;
+          ly.pitch = cols;  // npix, a multiple of 4, is the plane's extent
+          ly.storage = PAINTY_STORAGE_F32;
+          for (int c = 0; c < 3; c++) {
+            ly.K[c] = const_cast<float*>(dp[0]) + (3 * static_cast<int64_t>(l) + c) * npix;
+            ly.S[c] = const_cast<float*>(dp[1]) + (3 * static_cast<int64_t>(l) + c) * npix;
+          }
+          ly.V = const_cast<float*>(dp[2]) + static_cast<int64_t>(l) * npix;
+          ly.owned = false;
+          lp[l] = &ly;
+        }
+        painty_image ir{}, io{};
+        ir.rows = io.rows = rows;
+        ir.cols = io.cols = cols;
+        ir.pitch = io.pitch = cols;
+        ir.storage = io.storage = PAINTY_STORAGE_F32;
+        ir.owned = io.owned = false;
+        for (int c = 0; c < 3; c++) {
+          ir.R[c] = const_cast<float*>(dp[3]) + c * npix;
+          io.R[c] = const_cast<float*>(dp[4]) + c * npix;
+        }
+        pg::launch_compose(lp.data(), L, &ir, &io, st);
+        PG_CUDA(cudaStreamSynchronize(st));
+        return;
+      }
+    }
     constexpr int kStreams = 3;
     const int64_t pitch = pg::pitch_for(cols);
     // bands of about 16 MB of layer data each

@@ -157,3 +157,23 @@ def test_host_composite_equals_device_composite(pg, rows, cols, L):
     got = pg.compose_layers_host(K, S, V, R0)
     want = gpu_compose(pg, K, S, V, R0) if L else R0.astype(np.float64)
     assert np.array_equal(got.astype(np.float64), want)
+
+
+@pytest.mark.parametrize("rows,cols,L", [(64, 100, 8), (33, 37, 3), (16, 16, 18)])
+def test_host_composite_pinned_in_place(pg, rows, cols, L):
+    """With pinned host buffers the composite reads the stacks and writes the image in place
+    (33 x 37 pixels, not a multiple of 4, take the banded copies instead): both equal the
+    device composite bit for bit."""
+    torch = pytest.importorskip("torch")
+    K, S, V, R0 = workloads.composite_stack(rows, cols, layers=L, seed=rows * cols + L)
+
+    def pinned(a):
+        t = torch.empty(a.shape, dtype=torch.float32, pin_memory=True).numpy()
+        t[...] = a
+        return t
+
+    out = pinned(np.zeros((3, rows, cols), np.float32))
+    got = pg.compose_layers_host(pinned(K), pinned(S), pinned(V), pinned(R0), out=out)
+    assert got is out
+    want = gpu_compose(pg, K, S, V, R0)
+    assert np.array_equal(out.astype(np.float64), want)
