@@ -88,6 +88,11 @@ const char* painty_status_string(painty_status s);
 const char* painty_last_error(void);
 /* Number of this library's kernel launches so far in this process (all devices). */
 int64_t painty_kernel_launch_count(void);
+/* Reads and clears the current device's pipeline-fault word: nonzero when a kernel's
+ * shared-memory copy pipeline stalled beyond its one-second wait limit since the last call
+ * (that kernel wrote NaN where it stopped instead of hanging). Synchronises the device.
+ * No counterpart in painty. */
+painty_status painty_take_device_faults(uint32_t* faults);
 
 /* ------------------------------------------------------------------ layers
  * replaces PaintLayer<vec>::PaintLayer(rows, cols) + clear()  (painty/renderer/PaintLayer.hxx:27-30, 68-74) */

@@ -56,6 +56,7 @@ _sig("painty_build_flags", res=_I32)
 _sig("painty_status_string", C.c_int, res=C.c_char_p)
 _sig("painty_last_error", res=C.c_char_p)
 _sig("painty_kernel_launch_count", res=_I64)
+_sig("painty_take_device_faults", C.POINTER(C.c_uint32))
 _sig("painty_layer_create", _I32, _I32, C.c_int, C.POINTER(_P))
 _sig("painty_layer_destroy", _P)
 _sig("painty_layer_clear", _P, _P)
@@ -160,6 +161,14 @@ def bounds_checked() -> bool:
 def kernel_launch_count() -> int:
     """Kernel launches this library has issued in this process."""
     return int(_lib.painty_kernel_launch_count())
+
+
+def take_device_faults() -> int:
+    """Reads and clears the device's pipeline-fault word (nonzero: a kernel's copy pipeline
+    stalled past its wait limit and wrote NaN instead of hanging)."""
+    v = C.c_uint32()
+    _check(_lib.painty_take_device_faults(C.byref(v)))
+    return int(v.value)
 
 
 def _ptr(a: np.ndarray) -> int:

@@ -16,6 +16,11 @@
 
 namespace pg {
 
+// Set by a kernel whose shared-memory pipeline stalled beyond its wait limit (the kernel
+// then writes NaN where it stopped and returns); read and cleared by
+// painty_take_device_faults.
+__device__ unsigned int g_pipeline_fault = 0;
+
 namespace {
 thread_local std::string g_last_error;
 std::atomic<int64_t> g_launches{0};
@@ -664,6 +669,228 @@ __global__ void __launch_bounds__(256, 4) km_composite16_kernel(
   }
 }
 
+// ---- bulk-copy pipeline primitives (mbarrier + cp.async.bulk, PTX ISA 8.0+)
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(b)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(b)) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(b)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+    "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+    "selp.u32 %0, 1, 0, p;\n\t}"
+    : "=r"(ok)
+    : "r"(smem_addr(b)), "r"(parity)
+    : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Waits for the completion of the barrier's phase of `parity`. Gives up -- recording the
+// fault in g_pipeline_fault and raising the block's abort flag -- after one second, or at
+// once when another thread of the block has given up already (abort flag set).
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity,
+                                          volatile int* abort_flag) {
+  if (mbar_try_wait(b, parity)) return true;
+  const uint64_t t0 = global_ns();
+  for (;;) {
+    if (mbar_try_wait(b, parity)) return true;
+    if (abort_flag && *abort_flag) return false;
+    if (global_ns() - t0 > 1000000000ull) {
+      atomicExch(&g_pipeline_fault, 1u);
+      if (abort_flag) *abort_flag = 1;
+      return false;
+    }
+  }
+}
+// Global -> shared bulk copy completing on `bar` (16-byte aligned addresses, size a multiple
+// of 16).
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
+                                         uint64_t* bar) {
+  asm volatile(
+    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+    ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar))
+    : "memory");
+}
+
+// 16-bit composite fed by bulk copies. The register-fed kernel above keeps only two layers'
+// loads in flight per thread and its occupancy is limited by the KM arithmetic's registers,
+// so HBM waits on latency. Here one thread per block streams the planes into shared memory
+// with cp.async.bulk (a 5-deep ring of stages, one stage = one layer's 7 planes of a tile of
+// 1024 pixels, plus the tile's R0 planes with its first layer), and eight warps compute
+// from shared memory: ~70 KB in flight per block, two blocks per SM, whatever the registers.
+// Each consumer thread owns 4 consecutive pixels of the tile and carries R through the
+// layers in registers; the result is stored straight from registers.
+constexpr int kBulkTile = 1024;     // pixels per tile
+constexpr int kBulkStages = 5;      // ring depth
+constexpr int kBulkConsumers = 8;   // consumer warps (4 pixels per thread)
+constexpr size_t kBulkStageBytes = size_t(7) * kBulkTile * 2;
+constexpr size_t kBulkR0Bytes = size_t(3) * kBulkTile * 4;
+constexpr size_t kBulkSmem = kBulkStages * kBulkStageBytes + 2 * kBulkR0Bytes + 256;
+
+template <class TK, class TV>
+__global__ void __launch_bounds__(32 * (kBulkConsumers + 1), 2) km_composite16_bulk_kernel(
+  const __grid_constant__ Compose16Args<TK, TV> a) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint16_t* stages = reinterpret_cast<uint16_t*>(smem);
+  float* r0buf = reinterpret_cast<float*>(smem + kBulkStages * kBulkStageBytes);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kBulkStages * kBulkStageBytes +
+                                               2 * kBulkR0Bytes);
+  uint64_t* full = bars;                      // [kBulkStages], one arrival + the bytes
+  uint64_t* empty = bars + kBulkStages;       // [kBulkStages], one arrival per consumer warp
+  uint64_t* r0free = bars + 2 * kBulkStages;  // [2], one arrival per consumer warp
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(bars + 2 * kBulkStages + 2);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kBulkStages; i++) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], kBulkConsumers);
+    }
+    mbar_init(&r0free[0], kBulkConsumers);
+    mbar_init(&r0free[1], kBulkConsumers);
+    *abort_flag = 0;
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  const int64_t elems = a.groups * 4;
+  const int64_t ntiles = (elems + kBulkTile - 1) / kBulkTile;
+  const int L = a.L;
+
+  if (warp == kBulkConsumers) {  // producer
+    if (lane != 0) return;
+    uint32_t q = 0, slot = 0, use = 0, tl = 0;
+    bool ok = true;
+    for (int64_t tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x, tl++) {
+      const int64_t base = tile * kBulkTile;
+      const int64_t rest = elems - base;
+      const uint32_t n = static_cast<uint32_t>(rest < kBulkTile ? rest : kBulkTile);
+      for (int l = 0; l < L; l++) {
+        if (use > 0 && !mbar_wait(&empty[slot], (use - 1) & 1, abort_flag)) {
+          ok = false;
+          break;
+        }
+        if (l == 0 && tl >= 2 && !mbar_wait(&r0free[tl & 1], ((tl >> 1) - 1) & 1, abort_flag)) {
+          ok = false;
+          break;
+        }
+        const uint32_t pb = n * 2;
+        mbar_arrive_expect_tx(&full[slot], 7 * pb + (l == 0 ? 3 * n * 4 : 0));
+        uint16_t* sb = stages + slot * (7 * kBulkTile);
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          bulk_g2s(sb + c * kBulkTile, a.K[l][c] + base, pb, &full[slot]);
+          bulk_g2s(sb + (3 + c) * kBulkTile, a.S[l][c] + base, pb, &full[slot]);
+        }
+        bulk_g2s(sb + 6 * kBulkTile, a.V[l] + base, pb, &full[slot]);
+        if (l == 0) {
+          float* rb = r0buf + (tl & 1) * (3 * kBulkTile);
+#pragma unroll
+          for (int c = 0; c < 3; c++) bulk_g2s(rb + c * kBulkTile, a.r0[c] + base, n * 4, &full[slot]);
+        }
+        q++;
+        if (++slot == kBulkStages) {
+          slot = 0;
+          use++;
+        }
+      }
+    }
+    if (!ok) {  // the consumers gave up: let the copies in flight land before the block exits
+      for (uint32_t k = q > kBulkStages ? q - kBulkStages : 0; k < q; k++)
+        mbar_wait(&full[k % kBulkStages], (k / kBulkStages) & 1, nullptr);
+    }
+    return;
+  }
+
+  // consumers
+  const int p0 = threadIdx.x * 4;
+  uint32_t slot = 0, use = 0, tl = 0;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, tl++) {
+    const int64_t base = tile * kBulkTile;
+    const bool act = base + p0 < elems;
+    float r[3][4];
+    for (int l = 0; l < L; l++) {
+      if (!mbar_wait(&full[slot], use & 1, abort_flag)) {
+        if (act) {  // a stalled pipeline leaves NaN, never a plausible image
+#pragma unroll
+          for (int c = 0; c < 3; c++)
+            st_stream_u4(a.out[c] + base + p0, make_uint4(0x7fc00000u, 0x7fc00000u,
+                                                           0x7fc00000u, 0x7fc00000u));
+        }
+        return;
+      }
+      if (l == 0) {
+        const float* rb = r0buf + (tl & 1) * (3 * kBulkTile);
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          const float4 t = *reinterpret_cast<const float4*>(rb + c * kBulkTile + p0);
+          r[c][0] = t.x;
+          r[c][1] = t.y;
+          r[c][2] = t.z;
+          r[c][3] = t.w;
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&r0free[tl & 1]);
+      }
+      const uint16_t* sb = stages + slot * (7 * kBulkTile) + p0;
+      Layer16 cur;
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        cur.k[c] = *reinterpret_cast<const uint2*>(sb + c * kBulkTile);
+        cur.s[c] = *reinterpret_cast<const uint2*>(sb + (3 + c) * kBulkTile);
+      }
+      cur.v = *reinterpret_cast<const uint2*>(sb + 6 * kBulkTile);
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[slot]);
+      if (++slot == kBulkStages) {
+        slot = 0;
+        use++;
+      }
+#pragma unroll
+      for (int i = 0; i < 4; i += 2) {
+        const float2 d = f2(elem16<TV>(cur.v, i), elem16<TV>(cur.v, i + 1));
+        float2 K[3], S[3], R[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          K[c] = f2(elem16<TK>(cur.k[c], i), elem16<TK>(cur.k[c], i + 1));
+          S[c] = f2(elem16<TK>(cur.s[c], i), elem16<TK>(cur.s[c], i + 1));
+          R[c] = f2(r[c][i], r[c][i + 1]);
+        }
+        km_reflectance2x3(K, S, R, d);
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          r[c][i] = R[c].x;
+          r[c][i + 1] = R[c].y;
+        }
+      }
+    }
+    if (act) {
+#pragma unroll
+      for (int c = 0; c < 3; c++)
+        st_stream_u4(a.out[c] + base + p0,
+                     make_uint4(__float_as_uint(r[c][0]), __float_as_uint(r[c][1]),
+                                __float_as_uint(r[c][2]), __float_as_uint(r[c][3])));
+    }
+  }
+}
+
 template <class TK, class TV, class TR>
 struct ComposeStridedArgs {
   const TK* K[kMaxLayersPerLaunch][3];
@@ -743,11 +970,40 @@ void compose_strided(const painty_layer* const* layers, int32_t L, const painty_
 }
 
 template <class TK, class TV>
+int bulk_grid() {
+  static int cached[64] = {0};
+  int dev = 0;
+  PG_CUDA(cudaGetDevice(&dev));
+  if (dev < 64 && cached[dev] > 0) return cached[dev];
+  auto kern = km_composite16_bulk_kernel<TK, TV>;
+  PG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               static_cast<int>(kBulkSmem)));
+  int sms = 0, per_sm = 0;
+  PG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  PG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * (kBulkConsumers + 1),
+                                                        kBulkSmem));
+  const int g = std::max(1, sms * std::max(1, per_sm));
+  if (dev < 64) cached[dev] = g;
+  return g;
+}
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
+template <class TK, class TV>
 void compose16(const painty_layer* const* layers, int32_t L, const painty_image* r0,
                painty_image* out, cudaStream_t st) {
   const int64_t elems = r0->plane_elems();  // a multiple of 64 elements
-  auto kern = km_composite16_kernel<TK, TV>;
-  const int wave = resident_grid(kern, 256);
+  bool bulk = true;  // every plane 16-byte aligned: the bulk-copy kernel
+  for (int32_t l = 0; l < L; l++) {
+    for (int c = 0; c < 3; c++)
+      bulk = bulk && aligned16(layers[l]->K[c]) && aligned16(layers[l]->S[c]);
+    bulk = bulk && aligned16(layers[l]->V);
+  }
+  for (int c = 0; c < 3; c++) bulk = bulk && aligned16(r0->R[c]) && aligned16(out->R[c]);
+  auto kern = bulk ? km_composite16_bulk_kernel<TK, TV> : km_composite16_kernel<TK, TV>;
+  const int block = bulk ? 32 * (kBulkConsumers + 1) : 256;
+  const size_t smem = bulk ? kBulkSmem : 0;
+  const int wave = bulk ? bulk_grid<TK, TV>() : resident_grid(kern, 256);
   for (int32_t l0 = 0; l0 < L; l0 += kMaxLayersPerLaunch) {
     Compose16Args<TK, TV> a{};
     const int32_t n = std::min<int32_t>(kMaxLayersPerLaunch, L - l0);
@@ -766,9 +1022,10 @@ void compose16(const painty_layer* const* layers, int32_t L, const painty_image*
     }
     a.L = n;
     a.groups = elems / 4;
-    const int64_t blocks_needed = (a.groups + 255) / 256;
+    const int64_t blocks_needed =
+      bulk ? (elems + kBulkTile - 1) / kBulkTile : (a.groups + 255) / 256;
     const int grid = static_cast<int>(std::min<int64_t>(blocks_needed, wave));
-    kern<<<std::max(grid, 1), 256, 0, st>>>(a);
+    kern<<<std::max(grid, 1), block, smem, st>>>(a);
     count_launch();
     PG_CUDA(cudaGetLastError());
   }
@@ -928,6 +1185,17 @@ const char* painty_status_string(painty_status s) {
 const char* painty_last_error(void) { return pg::g_last_error.c_str(); }
 
 int64_t painty_kernel_launch_count(void) { return pg::g_launches.load(); }
+
+painty_status painty_take_device_faults(uint32_t* faults) {
+  return guard([&] {
+    PG_REQUIRE(faults != nullptr, "faults is null");
+    unsigned int v = 0, zero = 0;
+    PG_CUDA(cudaDeviceSynchronize());
+    PG_CUDA(cudaMemcpyFromSymbol(&v, pg::g_pipeline_fault, sizeof(v)));
+    PG_CUDA(cudaMemcpyToSymbol(pg::g_pipeline_fault, &zero, sizeof(zero)));
+    *faults = v;
+  });
+}
 
 // ---------------------------------------------------------------- layers
 painty_status painty_layer_create(int32_t rows, int32_t cols, painty_storage storage,

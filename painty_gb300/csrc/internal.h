@@ -228,6 +228,10 @@ void copy_planes_async(void* const* dst, const void* const* src, int nch, size_t
 struct BatchOptions {
   int max_cluster = 8;
   unsigned* status_host = nullptr;
+  // pinned host memory the launch's descriptors are staged in when they fit (the caller
+  // guarantees no earlier copy from it is still pending); otherwise a pageable copy
+  void* host_staging = nullptr;
+  size_t host_staging_bytes = 0;
 };
 void paint_batch(painty_canvas* const* canvases, painty_brush* const* brushes, int32_t nc,
                  const painty_stroke_desc* strokes, int64_t ns, const double* points,

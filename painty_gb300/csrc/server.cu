@@ -85,10 +85,15 @@ struct ServerRequest {
   double t_submit = 0, t_done = 0;
 };
 
+// Pinned staging per slot for a launch's descriptors (a chunk of strokes: their descriptors
+// and path points); larger chunks are copied from pageable memory.
+constexpr size_t kStagingBytes = 128 << 10;
+
 struct Slot {
   cudaStream_t st = nullptr;
   cudaEvent_t ev = nullptr;
   unsigned* status = nullptr;  // pinned: the last launch's kernel status word
+  void* staging = nullptr;     // pinned: the last launch's descriptors (kStagingBytes)
   bool busy = false;
   painty_server* owner = nullptr;
   int index = 0;
@@ -105,6 +110,7 @@ struct painty_server {
   cudaMemPool_t pool = nullptr;
   std::vector<Slot> slots;
   unsigned* status_words = nullptr;
+  unsigned char* staging = nullptr;  // pinned, kStagingBytes per slot
   std::multimap<size_t, void*> pinned_free;  // pinned blobs of released canvases, by size
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
@@ -342,6 +348,8 @@ void launch_chunk(painty_server* s, ServerRequest* r, ServerCanvas* c, int cap) 
   pg::BatchOptions opt;
   opt.max_cluster = cap;
   opt.status_host = sl.status;
+  opt.host_staging = sl.staging;  // the slot's previous copy finished before this launch
+  opt.host_staging_bytes = kStagingBytes;
   c->brush->pool_stream = sl.st;  // its buffers are (re)allocated in this stream's order
   int64_t n = 0;
   painty_canvas* cvs[1] = {c->cv};
@@ -624,12 +632,14 @@ painty_status painty_server_create(const painty_server_options* opt, painty_serv
       }
     }
     PG_CUDA(cudaMallocHost(&s->status_words, sizeof(unsigned) * s->opt.max_active));
+    PG_CUDA(cudaMallocHost(&s->staging, kStagingBytes * s->opt.max_active));
     s->slots.resize(static_cast<size_t>(s->opt.max_active));
     for (int i = 0; i < s->opt.max_active; i++) {
       Slot& sl = s->slots[i];
       PG_CUDA(cudaStreamCreateWithFlags(&sl.st, cudaStreamNonBlocking));
       PG_CUDA(cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming));
       sl.status = s->status_words + i;
+      sl.staging = s->staging + kStagingBytes * i;
       *sl.status = 0;
       sl.owner = s.get();
       sl.index = i;
@@ -811,6 +821,7 @@ painty_status painty_server_destroy(painty_server* s) {
       cudaStreamDestroy(sl.st);
     }
     cudaFreeHost(s->status_words);
+    cudaFreeHost(s->staging);
     cudaMemPoolDestroy(s->pool);
     cudaStreamDestroy(s->stream);
     delete s;

@@ -42,6 +42,7 @@
 #include <cstring>
 #include <cstdlib>
 #include <map>
+#include <tuple>
 #include <queue>
 #include <type_traits>
 #include <mutex>
@@ -1169,7 +1170,8 @@ struct BatchStroke {
   int32_t ndisc;  // support-disc list length (0: waves only)
   int32_t plan;  // bit 0: pickup map in shared memory; bit 1: footprint and owners global;
                  // bit 2: cell maps global
-  int64_t fp_offset;
+  int32_t fp_len;         // elements of the footprint array (F^2)
+  const void* footprint;  // the width's padded footprint in the math type, device-resident
   double radius, spacing;
   double K[3], Sc[3];
 };
@@ -1180,7 +1182,6 @@ struct BatchArgs {
   const BatchCanvas<TK, TV>* canvases;
   const BatchStroke* strokes;
   const double* points;
-  const M* footprints;
   const int32_t* order;  // canvases, heaviest first
   int32_t ncanvas;
   int* counter;
@@ -1191,7 +1192,7 @@ struct BatchArgs {
   int64_t pickup_stride, owner_stride, cellmap_stride;
   unsigned* status;
   // extents of the descriptor arrays and the scratch, for the bounds-checked build
-  int64_t nstrokes, npoints, nfootprint;
+  int64_t nstrokes, npoints;
   int32_t nslots;
 };
 
@@ -1237,8 +1238,8 @@ __global__ void __launch_bounds__(kStampThreads, 1) batch_kernel(const __grid_co
       const int nseg = st.npoints - 1;
       if (!in_bounds(b.status, kBoundsDescriptor, st.first_point + st.npoints - 1,
                      b.npoints + (st.npoints == 0 ? 1 : 0)) ||
-          !in_bounds(b.status, kBoundsDescriptor, st.fp_offset + int64_t(st.F) * st.F - 1,
-                     b.nfootprint) ||
+          !in_bounds(b.status, kBoundsDescriptor, int64_t(st.F) * st.F - 1,
+                     st.footprint ? st.fp_len : 0) ||
           !in_bounds(b.status, kBoundsDescriptor, nseg, kMaxPathPoints))
         continue;
       __syncthreads();
@@ -1264,7 +1265,7 @@ __global__ void __launch_bounds__(kStampThreads, 1) batch_kernel(const __grid_co
         sa.pV = nullptr;
         sa.prec = pk;
         (void)cells;
-        sa.footprint = b.footprints + st.fp_offset;
+        sa.footprint = static_cast<const M*>(st.footprint);
         sa.stamps = nullptr;
         sa.n = 0;
         sa.rows = cv.rows;
@@ -1384,13 +1385,19 @@ struct FootprintFamily {
   std::vector<double> image;
   int32_t fh = 0, fw = 0;
   std::map<int32_t, std::pair<std::vector<double>, int32_t>> by_width;
+  // device copies of the padded footprints by (device, width, element bytes): uploaded once,
+  // then shared by every launch that paints with the width
+  std::map<std::tuple<int, int32_t, int>, void*> on_device;
 };
 
 namespace pg {
 namespace {
 
 std::mutex g_family_mu;
-std::map<uint64_t, std::vector<std::weak_ptr<FootprintFamily>>> g_families;
+// every family ever made, for the life of the process: a family's device footprints may be
+// read by launches still in flight when its last brush is destroyed, and the next brush of
+// the same image finds them ready
+std::map<uint64_t, std::vector<std::shared_ptr<FootprintFamily>>> g_families;
 
 // The family of a footprint image (FNV-1a of its bytes, then compared value for value).
 std::shared_ptr<FootprintFamily> footprint_family(const std::vector<double>& img, int32_t fh,
@@ -1405,15 +1412,8 @@ std::shared_ptr<FootprintFamily> footprint_family(const std::vector<double>& img
   mix(img.data(), img.size() * sizeof(double));
   std::lock_guard<std::mutex> lk(g_family_mu);
   auto& list = g_families[h];
-  for (auto it = list.begin(); it != list.end();) {
-    std::shared_ptr<FootprintFamily> f = it->lock();
-    if (!f) {
-      it = list.erase(it);
-      continue;
-    }
+  for (const auto& f : list)
     if (f->fh == fh && f->fw == fw && f->image == img) return f;
-    ++it;
-  }
   auto f = std::make_shared<FootprintFamily>();
   f->image = img;
   f->fh = fh;
@@ -1444,6 +1444,35 @@ const std::pair<std::vector<double>, int32_t>& footprint_for(painty_brush* b, in
                     (static_cast<double>(i) + 0.5) * sy - 0.5);
   const int32_t s2 = support_radius2(fp.data(), F);
   return fam.by_width.emplace(width, std::make_pair(std::move(fp), s2)).first->second;
+}
+
+// The device copy of a width's padded footprint in the math type M, uploaded on first use
+// (synchronously, on a stream of its own) and reused by every later launch on the device.
+template <class M>
+const M* device_footprint(painty_brush* b, int width) {
+  const std::vector<double>& fp = footprint_for(b, width).first;
+  FootprintFamily& fam = *b->fp_family;
+  int dev = 0;
+  PG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(fam.mu);
+  const auto key = std::make_tuple(dev, static_cast<int32_t>(width), static_cast<int>(sizeof(M)));
+  auto it = fam.on_device.find(key);
+  if (it != fam.on_device.end()) return static_cast<const M*>(it->second);
+  const std::vector<M> h(fp.begin(), fp.end());
+  void* d = nullptr;
+  PG_CUDA(cudaMalloc(&d, h.size() * sizeof(M)));
+  cudaStream_t s = nullptr;
+  PG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  const cudaError_t e1 = cudaMemcpyAsync(d, h.data(), h.size() * sizeof(M),
+                                         cudaMemcpyHostToDevice, s);
+  const cudaError_t e2 = cudaStreamSynchronize(s);
+  cudaStreamDestroy(s);
+  if (e1 != cudaSuccess || e2 != cudaSuccess) {
+    cudaFree(d);
+    PG_CUDA(e1 != cudaSuccess ? e1 : e2);
+  }
+  fam.on_device.emplace(key, d);
+  return static_cast<const M*>(d);
 }
 
 void set_radius(painty_brush* b, double radius) {
@@ -1901,8 +1930,6 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   const size_t limit = static_cast<size_t>(max_dyn_smem()) - info.static_smem - 256;
   std::vector<BatchStroke> bs;
   bs.reserve(static_cast<size_t>(ns));
-  std::vector<M> fptable;
-  std::map<std::pair<const painty_brush*, int32_t>, int64_t> fp_off;
   std::vector<double> work(nc, 0.0), loadN(nc, 0.0), loadP(nc, 0.0);
   std::vector<int32_t> disc_of;  // per stroke: support-disc pixels
   disc_of.reserve(static_cast<size_t>(ns));
@@ -1920,12 +1947,6 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
       PG_REQUIRE(b->sizeMap > 0 && b->F > 0, "brush radius gives an empty footprint");
       PG_REQUIRE(static_cast<int64_t>(b->F) * b->F <= int64_t(kMaxPixelsPerThread) * kStampThreads,
                  "brush radius above the supported maximum (footprint side 256)");
-      const auto key = std::make_pair(static_cast<const painty_brush*>(b), b->width);
-      auto it = fp_off.find(key);
-      if (it == fp_off.end()) {
-        it = fp_off.emplace(key, static_cast<int64_t>(fptable.size())).first;
-        for (double v : b->footprint) fptable.push_back(static_cast<M>(v));
-      }
       BatchStroke x{};
       x.first_point = sk.first_point;
       x.npoints = sk.npoints;
@@ -1933,7 +1954,8 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
       x.S = b->sizeMap;
       x.wr = (b->F - 1) / 2;
       x.support2 = b->support2;
-      x.fp_offset = it->second;
+      x.footprint = device_footprint<M>(b, b->width);
+      x.fp_len = b->F * b->F;
       x.radius = b->radius;
       x.spacing = sk.spacing;
       for (int i = 0; i < 3; i++) {
@@ -2057,16 +2079,19 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   const size_t o_canvas = piece(bc.data(), bc.size() * sizeof(bc[0]));
   const size_t o_strokes = piece(bs.data(), bs.size() * sizeof(BatchStroke));
   const size_t o_points = piece(points, static_cast<size_t>(npoints) * 2 * sizeof(double));
-  const size_t o_fp = piece(fptable.data(), fptable.size() * sizeof(M));
   const size_t o_order = piece(order.data(), order.size() * sizeof(int32_t));
   void* d_desc = nullptr;
   d_desc = temp_alloc(hdesc.size(), st);
-  PG_CUDA(cudaMemcpyAsync(d_desc, hdesc.data(), hdesc.size(), cudaMemcpyHostToDevice, st));
+  const void* hsrc = hdesc.data();
+  if (opt.host_staging && hdesc.size() <= opt.host_staging_bytes) {
+    std::memcpy(opt.host_staging, hdesc.data(), hdesc.size());
+    hsrc = opt.host_staging;
+  }
+  PG_CUDA(cudaMemcpyAsync(d_desc, hsrc, hdesc.size(), cudaMemcpyHostToDevice, st));
   auto at = [&](size_t off) { return static_cast<void*>(static_cast<char*>(d_desc) + off); };
   void* d_canvas = at(o_canvas);
   void* d_strokes = at(o_strokes);
   void* d_points = at(o_points);
-  void* d_fp = at(o_fp);
   void* d_order = at(o_order);
   const int64_t pstride = static_cast<int64_t>(8) * smax * smax;
   const int64_t ostride = static_cast<int64_t>(smax) * smax;
@@ -2090,7 +2115,6 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   a.canvases = static_cast<const BatchCanvas<TK, TV>*>(d_canvas);
   a.strokes = static_cast<const BatchStroke*>(d_strokes);
   a.points = static_cast<const double*>(d_points);
-  a.footprints = static_cast<const M*>(d_fp);
   a.order = static_cast<const int32_t*>(d_order);
   a.ncanvas = nc;
   a.counter = static_cast<int*>(d_counter);
@@ -2104,7 +2128,6 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   a.owner_stride = ostride;
   a.nstrokes = static_cast<int64_t>(bs.size());
   a.npoints = npoints;
-  a.nfootprint = static_cast<int64_t>(fptable.size());
   a.nslots = slots;
   launch_clustered(kern, grid, cl, std::max<size_t>(dyn, 16), st, a);
   count_launch();

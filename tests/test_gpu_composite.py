@@ -52,6 +52,39 @@ def test_half_storage_delta_e(pg, oracle, storage):
     assert de_max < HALF_DELTA_E, (de_max, de_mean)
 
 
+# FP16/BF16 storage with FP32 arithmetic vs the double oracle on the values the layers
+# actually hold (downloaded back): only the arithmetic differs. The sizes give the bulk-copy
+# kernel one partial tile, many tiles per block (1100 x 1100: 1182 tiles of 1024 pixels), and
+# two launches of 16 + 2 layers; afterwards no copy pipeline may have stalled.
+HALF_F32_MATH_ABS_TOL = 2e-5
+
+
+@pytest.mark.parametrize("storage", ["f16", "bf16"])
+@pytest.mark.parametrize("rows,cols,L", [(48, 160, 8), (1100, 1100, 8), (300, 517, 18)])
+def test_half_storage_fp32_math(pg, oracle, storage, rows, cols, L):
+    K, S, V, R0 = workloads.composite_stack(rows, cols, layers=L, seed=rows + L, dtype=np.float64)
+    layers = []
+    Ks, Ss, Vs = np.empty_like(K), np.empty_like(S), np.empty_like(V)
+    for l in range(L):
+        ly = pg.PaintLayer(rows, cols, storage)
+        ly.upload("K", K[l], planar=True)
+        ly.upload("S", S[l], planar=True)
+        ly.upload("V", V[l], planar=True)
+        Ks[l], Ss[l], Vs[l] = (ly.download("K", planar=True), ly.download("S", planar=True),
+                               ly.download("V"))
+        layers.append(ly)
+    r0 = pg.Image(rows, cols, "f32")
+    r0.upload(R0, planar=True)
+    out = pg.Image(rows, cols, "f32")
+    pg.compose_layers(layers, r0, out)
+    got = out.download(dtype=np.float64, planar=True)
+    R0s = R0.astype(np.float32).astype(np.float64)
+    want = oracle_compose(oracle, Ks, Ss, Vs, R0s, mode=0)
+    err = np.abs(got - want).max()
+    assert err <= HALF_F32_MATH_ABS_TOL, err
+    assert pg.take_device_faults() == 0
+
+
 def test_fused_equals_unfused_bitwise(pg):
     K, S, V, R0 = workloads.composite_stack(33, 130, layers=8, seed=5)
     a = gpu_compose(pg, K, S, V, R0, "f32", fused=True)
