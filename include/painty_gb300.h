@@ -391,6 +391,8 @@ typedef struct painty_server_counters {
   int64_t worker_busy_us;  /* time the worker thread spent issuing device work, of which: */
   int64_t worker_create_us, worker_launch_us, worker_finish_us; /* new canvases, stamp
                               launches, composite + download launches */
+  uint64_t heap_bytes;     /* the device reservation canvases are carved from */
+  int64_t heap_fallbacks;  /* allocations it could not hold (stream-ordered instead) */
 } painty_server_counters;
 painty_status painty_server_create(const painty_server_options* options, painty_server** out);
 /* Non-blocking. Returns the request id and its canvas id (new canvases get one here). */

@@ -788,7 +788,8 @@ class _Counters(C.Structure):
                [("resident_bytes", C.c_uint64), ("peak_resident_bytes", C.c_uint64)] + \
                [(n, C.c_int64) for n in ("active", "pending", "canvases", "worker_busy_us",
                                           "worker_create_us", "worker_launch_us",
-                                          "worker_finish_us")]
+                                          "worker_finish_us")] + \
+               [("heap_bytes", C.c_uint64), ("heap_fallbacks", C.c_int64)]
 
 
 _sig("painty_server_create", C.POINTER(_ServerOptions), C.POINTER(_P))

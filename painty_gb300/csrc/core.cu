@@ -200,9 +200,10 @@ void canvas_relayout(painty_canvas* c, void* base) {
 }
 
 painty_canvas* canvas_create_on(int32_t rows, int32_t cols, painty_storage storage,
-                                cudaMemPool_t pool, cudaStream_t st, bool sync) {
+                                DeviceHeap* heap, cudaStream_t st, bool sync) {
   PG_REQUIRE(rows > 0 && cols > 0, "rows and cols must be positive");
   PG_REQUIRE(valid_storage(storage), "unknown storage format");
+  PG_REQUIRE(heap != nullptr, "no heap");
   auto* c = new painty_canvas();
   const painty_storage rs = storage == PAINTY_STORAGE_F64 ? PAINTY_STORAGE_F64 : PAINTY_STORAGE_F32;
   const size_t lb = layer_bytes(rows, cols, storage, true);
@@ -214,24 +215,127 @@ painty_canvas* canvas_create_on(int32_t rows, int32_t cols, painty_storage stora
     c->wet.storage = storage;
     c->r0.storage = rs;
     c->bytes = lb + ib + align256(hb);
-    canvas_relayout(c, device_alloc_on(c->bytes, pool, st));
+    canvas_relayout(c, heap->alloc(c->bytes, st));
     c->id = g_canvas_ids.fetch_add(1);
     PG_CUDA(cudaMemsetAsync(c->base, 0, c->bytes, st));
     const double one[3] = {1.0, 1.0, 1.0};  // Canvas.hxx:33 background
     fill_planes(c->r0.R, 3, r_type(rs), c->r0.plane_elems(), one, st);
     if (sync) PG_CUDA(cudaStreamSynchronize(st));
   } catch (...) {
-    if (c->base) device_free_on(c->base, st);
+    if (c->base) {
+      cudaStreamSynchronize(st);  // the memory is reused at once: let queued work finish
+      heap->free(c->base, st);
+    }
     delete c;
     throw;
   }
   return c;
 }
 
-void canvas_destroy_on(painty_canvas* c, cudaStream_t st) {
+void canvas_destroy_on(painty_canvas* c, DeviceHeap* heap, cudaStream_t st) {
   if (!c) return;
-  device_free_on(c->base, st);
+  heap->free(c->base, st);
   delete c;
+}
+
+// ------------------------------------------------------------------ device heap
+DeviceHeap::DeviceHeap(size_t bytes) {
+  bytes = (bytes + 255) / 256 * 256;
+  void* p = nullptr;
+  if (bytes > 0 && cudaMalloc(&p, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    size_t free_b = 0, total_b = 0;
+    p = nullptr;
+    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && free_b > (size_t(1) << 30)) {
+      bytes = (free_b - (size_t(1) << 30)) / 256 * 256;  // leave 1 GB to everything else
+      if (cudaMalloc(&p, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        p = nullptr;
+      }
+    }
+    if (!p) bytes = 0;
+  }
+  base_ = static_cast<char*>(p);
+  size_ = p ? bytes : 0;
+  if (size_) insert_free(0, size_);
+}
+
+DeviceHeap::~DeviceHeap() {
+  if (base_) cudaFree(base_);
+  for (void* p : outside_) cudaFree(p);
+}
+
+void DeviceHeap::insert_free(size_t off, size_t len) {
+  free_by_off_.emplace(off, len);
+  free_by_len_.emplace(len, off);
+}
+
+void DeviceHeap::erase_free(size_t off, size_t len) {
+  free_by_off_.erase(off);
+  auto r = free_by_len_.equal_range(len);
+  for (auto it = r.first; it != r.second; ++it)
+    if (it->second == off) {
+      free_by_len_.erase(it);
+      break;
+    }
+}
+
+void* DeviceHeap::alloc(size_t bytes, cudaStream_t st) {
+  const size_t len = (std::max<size_t>(bytes, 1) + 255) / 256 * 256;
+  {
+    std::lock_guard<std::mutex> lk(mu_);
+    auto it = free_by_len_.lower_bound(len);  // best fit
+    if (it != free_by_len_.end()) {
+      const size_t flen = it->first, off = it->second;
+      erase_free(off, flen);
+      if (flen > len) insert_free(off + len, flen - len);
+      used_.emplace(off, len);
+      return base_ + off;
+    }
+    fallbacks_++;
+  }
+  void* p = nullptr;
+  const cudaError_t e = cudaMallocAsync(&p, len, st);
+  if (e == cudaErrorMemoryAllocation) {
+    cudaGetLastError();
+    fail(PAINTY_ERR_OUT_OF_MEMORY, "device memory exhausted (heap fallback)");
+  }
+  PG_CUDA(e);
+  std::lock_guard<std::mutex> lk(mu_);
+  outside_.insert(p);
+  return p;
+}
+
+void DeviceHeap::free(void* p, cudaStream_t st) {
+  if (!p) return;
+  std::lock_guard<std::mutex> lk(mu_);
+  char* c = static_cast<char*>(p);
+  if (base_ && c >= base_ && c < base_ + size_) {
+    size_t off = static_cast<size_t>(c - base_);
+    auto u = used_.find(off);
+    if (u == used_.end()) return;  // not an allocation of this heap
+    size_t len = u->second;
+    used_.erase(u);
+    auto next = free_by_off_.lower_bound(off);
+    if (next != free_by_off_.end() && next->first == off + len) {  // merge the following gap
+      const size_t nl = next->second;
+      erase_free(next->first, nl);
+      len += nl;
+    }
+    auto prev = free_by_off_.lower_bound(off);
+    if (prev != free_by_off_.begin()) {  // merge the preceding gap
+      --prev;
+      if (prev->first + prev->second == off) {
+        const size_t po = prev->first, pl = prev->second;
+        erase_free(po, pl);
+        off = po;
+        len += pl;
+      }
+    }
+    insert_free(off, len);
+    return;
+  }
+  if (outside_.erase(p)) cudaFreeAsync(p, st);
 }
 
 // ------------------------------------------------------------------ transfer kernels

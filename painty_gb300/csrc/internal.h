@@ -7,10 +7,13 @@
 #include <cstdint>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <utility>
 #include <vector>
 #include <stdexcept>
 #include <string>
+#include <unordered_map>
+#include <unordered_set>
 
 #include "painty_gb300.h"
 
@@ -74,6 +77,35 @@ void device_free_on(void* p, cudaStream_t st);
 void* temp_alloc(size_t bytes, cudaStream_t st);
 // Pool settings shared by the library's pools (retained memory, no cross-stream reuse waits).
 void configure_pool(cudaMemPool_t pool);
+
+// One device reservation carved up on the host: allocation and release are host bookkeeping
+// (best fit, neighbours merged on release, 256-byte granules), so neither calls the driver.
+// For an owner that releases memory only once the GPU has finished with it (the server: a
+// canvas's memory after its last request completed). A request the reservation cannot hold
+// falls back to stream-ordered cudaMallocAsync on the given stream.
+class DeviceHeap {
+ public:
+  explicit DeviceHeap(size_t bytes);  // reserves `bytes`, or what the device has free
+  ~DeviceHeap();
+  DeviceHeap(const DeviceHeap&) = delete;
+  DeviceHeap& operator=(const DeviceHeap&) = delete;
+  void* alloc(size_t bytes, cudaStream_t st);
+  void free(void* p, cudaStream_t st);
+  size_t reserved() const { return size_; }
+  int64_t fallbacks() const { return fallbacks_; }
+
+ private:
+  std::mutex mu_;
+  char* base_ = nullptr;
+  size_t size_ = 0;
+  std::map<size_t, size_t> free_by_off_;       // offset -> length
+  std::multimap<size_t, size_t> free_by_len_;  // length -> offset
+  std::unordered_map<size_t, size_t> used_;    // offset -> length
+  std::unordered_set<void*> outside_;          // fallback allocations
+  int64_t fallbacks_ = 0;
+  void insert_free(size_t off, size_t len);
+  void erase_free(size_t off, size_t len);
+};
 
 }  // namespace pg
 
@@ -164,10 +196,10 @@ struct painty_brush {
   int ring_pending = -1;
   void* d_stamps = nullptr;
   size_t d_stamps_bytes = 0;
-  // device memory from a pool, ordered on pool_stream (set by an owner that runs the brush's
-  // kernels on that stream), instead of cudaMalloc / cudaFree
-  cudaMemPool_t pool = nullptr;
-  cudaStream_t pool_stream = nullptr;
+  // device memory from an owner's heap (released only after the brush's work finished; the
+  // heap's fallback is ordered on heap_stream), instead of cudaMalloc / cudaFree
+  pg::DeviceHeap* heap = nullptr;
+  cudaStream_t heap_stream = nullptr;
   unsigned* d_status = nullptr;  // 16 words: [0] kernel status, [2] stamps applied (rounding
                                  // seed), [8..15] the ring state
   int* d_ring() const { return reinterpret_cast<int*>(d_status) + 8; }
@@ -183,11 +215,12 @@ size_t image_bytes(int32_t rows, int32_t cols, painty_storage s);
 // Points a canvas's plane views into a new device allocation of the canvas layout (nullptr:
 // no allocation, as for a canvas whose state was moved to host memory).
 void canvas_relayout(painty_canvas* c, void* base);
-// A canvas (as painty_canvas_create) in pool memory, initialised in `st`'s order (with
-// `sync`, returns after `st` has finished that). Free with canvas_destroy_on.
+// A canvas (as painty_canvas_create) in heap memory, initialised in `st`'s order (with
+// `sync`, returns after `st` has finished that). Free with canvas_destroy_on once the GPU
+// has finished with it.
 painty_canvas* canvas_create_on(int32_t rows, int32_t cols, painty_storage storage,
-                                cudaMemPool_t pool, cudaStream_t st, bool sync = true);
-void canvas_destroy_on(painty_canvas* c, cudaStream_t st);
+                                DeviceHeap* heap, cudaStream_t st, bool sync = true);
+void canvas_destroy_on(painty_canvas* c, DeviceHeap* heap, cudaStream_t st);
 
 // Plane transfer between a host buffer and `nch` device planes of element type `dev_type`
 // (0 f32, 1 f16, 2 bf16, 3 f64) with the given pitch and element stride (1 planar, 8 packed).
@@ -232,6 +265,15 @@ struct BatchOptions {
   // guarantees no earlier copy from it is still pending); otherwise a pageable copy
   void* host_staging = nullptr;
   size_t host_staging_bytes = 0;
+  // device buffers for the launch's descriptors and scratch, used when large enough (the
+  // caller guarantees no earlier launch still uses them); otherwise launch temporaries.
+  // *_needed (when set) receive the sizes this launch wanted.
+  void* device_desc = nullptr;
+  size_t device_desc_bytes = 0;
+  void* device_scratch = nullptr;
+  size_t device_scratch_bytes = 0;
+  size_t* desc_needed = nullptr;
+  size_t* scratch_needed = nullptr;
 };
 void paint_batch(painty_canvas* const* canvases, painty_brush* const* brushes, int32_t nc,
                  const painty_stroke_desc* strokes, int64_t ns, const double* points,

@@ -13,10 +13,11 @@
 // slot's stream order.
 //
 // Canvases stay resident on the device between requests. Their memory (canvas, composite
-// image, brush buffers) comes from a stream-ordered pool, so creating and dropping canvases
-// never synchronises the device. Admission keeps the resident bytes under a budget by
-// evicting idle canvases (least recently used first) to pinned host memory and restoring them
-// when a later request continues them. A canvas's requests run one after another, in
+// image, brush buffers) is carved on the host from one device reservation made when the
+// server starts, so creating and dropping canvases calls no allocator of the driver; memory
+// is returned only when the GPU has finished with it (a canvas after its last request).
+// Admission keeps the resident bytes under a budget by evicting idle canvases (least recently
+// used first) to pinned host memory and restoring them when a later request continues them. A canvas's requests run one after another, in
 // submission order; different canvases are independent, so a request's result does not
 // depend on what else is in flight. painty_server_release drops a canvas once its queued
 // requests are done.
@@ -94,6 +95,9 @@ struct Slot {
   cudaEvent_t ev = nullptr;
   unsigned* status = nullptr;  // pinned: the last launch's kernel status word
   void* staging = nullptr;     // pinned: the last launch's descriptors (kStagingBytes)
+  void* d_desc = nullptr;      // device: the launch's descriptors (kStagingBytes)
+  void* d_scratch = nullptr;   // device: the launch's scratch, grown to what launches need
+  size_t d_scratch_bytes = 0;
   bool busy = false;
   painty_server* owner = nullptr;
   int index = 0;
@@ -107,7 +111,7 @@ struct painty_server {
   int device = 0;
   int sms = 0;
   cudaStream_t stream = nullptr;  // creation, eviction and restore
-  cudaMemPool_t pool = nullptr;
+  std::unique_ptr<pg::DeviceHeap> heap;  // canvases, images, brush buffers, slot buffers
   std::vector<Slot> slots;
   unsigned* status_words = nullptr;
   unsigned char* staging = nullptr;  // pinned, kStagingBytes per slot
@@ -187,13 +191,13 @@ void mark_slot(Slot& sl) {
 
 void image_alloc(painty_server* s, ServerCanvas* c, cudaStream_t st) {
   const painty_storage rs = image_storage(s);
-  void* base = pg::device_alloc_on(pg::image_bytes(c->rows, c->cols, rs), s->pool, st);
+  void* base = s->heap->alloc(pg::image_bytes(c->rows, c->cols, rs), st);
   pg::image_layout(c->img, c->rows, c->cols, rs, base);
   c->img.owned = false;
 }
 
 void image_free(painty_server* s, ServerCanvas* c) {
-  pg::device_free_on(c->img.base, s->stream);
+  s->heap->free(c->img.base, s->stream);
   c->img.base = nullptr;
 }
 
@@ -202,14 +206,14 @@ void image_free(painty_server* s, ServerCanvas* c) {
 void evict(painty_server* s, ServerCanvas* c) {
   painty_canvas* cv = c->cv;
   painty_brush* b = c->brush;
-  b->pool_stream = s->stream;
+  b->heap_stream = s->stream;
   blob_save(s, c->save_canvas, cv->base, cv->bytes);
   if (b->has_snapshot) blob_save(s, c->save_snapshot, b->snapshot.base, b->snapshot.bytes);
   PG_CUDA(cudaStreamSynchronize(s->stream));
-  pg::device_free_on(cv->base, s->stream);
+  s->heap->free(cv->base, s->stream);
   pg::canvas_relayout(cv, nullptr);
   if (b->has_snapshot) {
-    pg::device_free_on(b->snapshot.base, s->stream);
+    s->heap->free(b->snapshot.base, s->stream);
     b->snapshot.base = nullptr;
   }
   image_free(s, c);
@@ -219,12 +223,12 @@ void evict(painty_server* s, ServerCanvas* c) {
 void restore(painty_server* s, ServerCanvas* c) {
   painty_canvas* cv = c->cv;
   painty_brush* b = c->brush;
-  b->pool_stream = s->stream;
-  void* base = pg::device_alloc_on(cv->bytes, s->pool, s->stream);
+  b->heap_stream = s->stream;
+  void* base = s->heap->alloc(cv->bytes, s->stream);
   PG_CUDA(cudaMemcpyAsync(base, c->save_canvas.p, cv->bytes, cudaMemcpyHostToDevice, s->stream));
   pg::canvas_relayout(cv, base);
   if (b->has_snapshot) {
-    void* sb = pg::device_alloc_on(b->snapshot.bytes, s->pool, s->stream);
+    void* sb = s->heap->alloc(b->snapshot.bytes, s->stream);
     PG_CUDA(cudaMemcpyAsync(sb, c->save_snapshot.p, b->snapshot.bytes, cudaMemcpyHostToDevice,
                             s->stream));
     pg::layer_layout(b->snapshot, b->snapshot.rows, b->snapshot.cols, b->snapshot.storage, sb,
@@ -238,7 +242,8 @@ void restore(painty_server* s, ServerCanvas* c) {
 // A new canvas, its substrate and its brush, all in the order of `st` (the stream of the
 // request that creates it; nothing waits).
 void create(painty_server* s, ServerCanvas* c, cudaStream_t st) {
-  painty_canvas* cv = pg::canvas_create_on(c->rows, c->cols, s->opt.storage, s->pool, st, false);
+  painty_canvas* cv = pg::canvas_create_on(c->rows, c->cols, s->opt.storage, s->heap.get(), st,
+                                           false);
   try {
     const float* r0 = c->r0_pinned ? c->r0_pinned : (c->r0.empty() ? nullptr : c->r0.data());
     if (r0)
@@ -251,11 +256,12 @@ void create(painty_server* s, ServerCanvas* c, cudaStream_t st) {
     if (bst != PAINTY_OK) pg::fail(bst, painty_last_error());
     b->pickupRate = s->opt.pickup_rate;
     b->depositionRate = s->opt.deposition_rate;
-    b->pool = s->pool;
-    b->pool_stream = st;
+    b->heap = s->heap.get();
+    b->heap_stream = st;
     c->brush = b;
   } catch (...) {
-    pg::canvas_destroy_on(cv, st);
+    cudaStreamSynchronize(st);  // its memory is reused at once: let queued work finish
+    pg::canvas_destroy_on(cv, s->heap.get(), st);
     throw;
   }
   c->cv = cv;
@@ -267,13 +273,13 @@ void create(painty_server* s, ServerCanvas* c, cudaStream_t st) {
 // Frees a released canvas (worker thread; nothing of it is in flight).
 void drop(painty_server* s, ServerCanvas* c) {
   if (c->brush) {
-    c->brush->pool_stream = s->stream;
+    c->brush->heap_stream = s->stream;
     painty_brush_destroy(c->brush);
   }
   if (c->cv) {
     if (c->resident) {
       image_free(s, c);
-      pg::canvas_destroy_on(c->cv, s->stream);
+      pg::canvas_destroy_on(c->cv, s->heap.get(), s->stream);
     } else {
       delete c->cv;  // evicted: no device memory left to free
     }
@@ -348,14 +354,28 @@ void launch_chunk(painty_server* s, ServerRequest* r, ServerCanvas* c, int cap) 
   pg::BatchOptions opt;
   opt.max_cluster = cap;
   opt.status_host = sl.status;
-  opt.host_staging = sl.staging;  // the slot's previous copy finished before this launch
+  opt.host_staging = sl.staging;  // the slot's previous launch finished before this one
   opt.host_staging_bytes = kStagingBytes;
-  c->brush->pool_stream = sl.st;  // its buffers are (re)allocated in this stream's order
+  if (!sl.d_desc) sl.d_desc = s->heap->alloc(kStagingBytes, sl.st);
+  opt.device_desc = sl.d_desc;
+  opt.device_desc_bytes = kStagingBytes;
+  opt.device_scratch = sl.d_scratch;
+  opt.device_scratch_bytes = sl.d_scratch_bytes;
+  size_t scratch_needed = 0;
+  opt.scratch_needed = &scratch_needed;
+  c->brush->heap_stream = sl.st;
   int64_t n = 0;
   painty_canvas* cvs[1] = {c->cv};
   painty_brush* brs[1] = {c->brush};
   pg::paint_batch(cvs, brs, 1, descs.data(), static_cast<int64_t>(descs.size()), pts.data(),
                   static_cast<int64_t>(pts.size() / 2), &n, sl.st, &opt);
+  if (scratch_needed > sl.d_scratch_bytes) {
+    // this launch used a temporary; the slot's buffer (last used by a finished launch) grows
+    // for the next one
+    s->heap->free(sl.d_scratch, sl.st);
+    sl.d_scratch_bytes = (scratch_needed + (64 << 10) - 1) / (64 << 10) * (64 << 10);
+    sl.d_scratch = s->heap->alloc(sl.d_scratch_bytes, sl.st);
+  }
   mark_slot(sl);
   r->stamps += budget;
   r->next = k;
@@ -613,24 +633,11 @@ painty_status painty_server_create(const painty_server_options* opt, painty_serv
     PG_CUDA(cudaGetDevice(&s->device));
     PG_CUDA(cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->device));
     PG_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
-    // a pool of its own that keeps freed memory for reuse (no release at synchronisation)
-    cudaMemPoolProps props{};
-    props.allocType = cudaMemAllocationTypePinned;
-    props.location.type = cudaMemLocationTypeDevice;
-    props.location.id = s->device;
-    PG_CUDA(cudaMemPoolCreate(&s->pool, &props));
-    pg::configure_pool(s->pool);
-    // map the budget into the pool once: canvases are then carved from it without the pool
-    // growing (mapping fresh memory) under load
-    {
-      void* r = nullptr;
-      if (cudaMallocFromPoolAsync(&r, s->opt.budget_bytes, s->pool, s->stream) == cudaSuccess) {
-        cudaFreeAsync(r, s->stream);
-        PG_CUDA(cudaStreamSynchronize(s->stream));
-      } else {
-        cudaGetLastError();  // the budget is more than is free now: the pool grows as needed
-      }
-    }
+    // one reservation for everything the server keeps on the device, carved on the host: the
+    // budget's canvases plus the slots' launch buffers
+    s->heap = std::make_unique<pg::DeviceHeap>(
+      s->opt.budget_bytes + static_cast<size_t>(s->opt.max_active) * (kStagingBytes + (1u << 20)) +
+      (size_t(256) << 20));
     PG_CUDA(cudaMallocHost(&s->status_words, sizeof(unsigned) * s->opt.max_active));
     PG_CUDA(cudaMallocHost(&s->staging, kStagingBytes * s->opt.max_active));
     s->slots.resize(static_cast<size_t>(s->opt.max_active));
@@ -800,6 +807,8 @@ painty_status painty_server_stats(painty_server* s, painty_server_counters* out)
     int64_t live = 0;
     for (auto& kv : s->canvases) live += kv.second->release ? 0 : 1;
     out->canvases = live;
+    out->heap_bytes = s->heap->reserved();
+    out->heap_fallbacks = s->heap->fallbacks();
   });
 }
 
@@ -822,7 +831,11 @@ painty_status painty_server_destroy(painty_server* s) {
     }
     cudaFreeHost(s->status_words);
     cudaFreeHost(s->staging);
-    cudaMemPoolDestroy(s->pool);
+    for (Slot& sl : s->slots) {
+      s->heap->free(sl.d_desc, s->stream);
+      s->heap->free(sl.d_scratch, s->stream);
+    }
+    s->heap.reset();
     cudaStreamDestroy(s->stream);
     delete s;
   });

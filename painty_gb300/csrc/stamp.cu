@@ -1490,13 +1490,13 @@ void set_radius(painty_brush* b, double radius) {
   b->pickup_clear = true;
 }
 
-// Device memory of a brush: cudaMalloc / cudaFree, or stream-ordered from the brush's pool.
+// Device memory of a brush: cudaMalloc / cudaFree, or from its owner's heap.
 void* brush_alloc(const painty_brush* b, size_t bytes) {
-  return b->pool ? device_alloc_on(bytes, b->pool, b->pool_stream) : device_alloc(bytes);
+  return b->heap ? b->heap->alloc(bytes, b->heap_stream) : device_alloc(bytes);
 }
 void brush_free(const painty_brush* b, void* p) {
-  if (b->pool)
-    device_free_on(p, b->pool_stream);
+  if (b->heap)
+    b->heap->free(p, b->heap_stream);
   else
     device_free(p);
 }
@@ -2081,7 +2081,9 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   const size_t o_points = piece(points, static_cast<size_t>(npoints) * 2 * sizeof(double));
   const size_t o_order = piece(order.data(), order.size() * sizeof(int32_t));
   void* d_desc = nullptr;
-  d_desc = temp_alloc(hdesc.size(), st);
+  const bool own_desc = !(opt.device_desc && hdesc.size() <= opt.device_desc_bytes);
+  d_desc = own_desc ? temp_alloc(hdesc.size(), st) : opt.device_desc;
+  if (opt.desc_needed) *opt.desc_needed = hdesc.size();
   const void* hsrc = hdesc.data();
   if (opt.host_staging && hdesc.size() <= opt.host_staging_bytes) {
     std::memcpy(opt.host_staging, hdesc.data(), hdesc.size());
@@ -2104,7 +2106,9 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   const size_t s_cm = align_up(s_own + slots * ostride * sizeof(int), 256);
   const size_t s_end = align_up(s_cm + std::max<int64_t>(slots * cmstride, 4) * sizeof(int), 256);
   void* d_scratch = nullptr;
-  d_scratch = temp_alloc(s_end, st);
+  const bool own_scratch = !(opt.device_scratch && s_end <= opt.device_scratch_bytes);
+  d_scratch = own_scratch ? temp_alloc(s_end, st) : opt.device_scratch;
+  if (opt.scratch_needed) *opt.scratch_needed = s_end;
   PG_CUDA(cudaMemsetAsync(d_scratch, 0, sizeof(int) * (8 + slots), st));
   auto sat = [&](size_t off) { return static_cast<void*>(static_cast<char*>(d_scratch) + off); };
   void* d_counter = sat(s_counter);
@@ -2136,8 +2140,8 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   PG_CUDA(cudaMemcpyAsync(opt.status_host ? opt.status_host : status, a.status,
                           opt.status_host ? sizeof(unsigned) : sizeof(status),
                           cudaMemcpyDeviceToHost, st));
-  PG_CUDA(cudaFreeAsync(d_desc, st));
-  PG_CUDA(cudaFreeAsync(d_scratch, st));
+  if (own_desc) PG_CUDA(cudaFreeAsync(d_desc, st));
+  if (own_scratch) PG_CUDA(cudaFreeAsync(d_scratch, st));
   if (!opt.status_host) PG_CUDA(cudaStreamSynchronize(st));
   for (int32_t c = 0; c < nc; c++) {
     if (per[c].empty()) continue;

@@ -60,6 +60,34 @@ def test_result_same_alone_and_in_the_mix(pg, storage):
     assert np.array_equal(a_img, m_img)
     assert s["completed"] == 24 and s["failed"] == 0
     assert s["steps"] >= 24  # every request launched at least one chunk of strokes
+    # everything came from the server's device reservation
+    assert s["heap_bytes"] >= 8 << 30 and s["heap_fallbacks"] == 0
+
+
+def test_heap_reuses_released_memory(pg):
+    """Canvases of mixed sizes created and released one after another, many times over a
+    small budget: the reservation's freed ranges are merged and reused, never exceeded, and
+    each result equals the same request on a fresh server."""
+    fp = workloads.footprint_image(seed=7)
+    rng = np.random.default_rng(11)
+    srv = pg.Server(96 << 20, fp, storage="f16", step_stamps=4000)
+    first = None
+    for i in range(40):
+        side = int(rng.choice([96, 160, 300, 480]))
+        st = _strokes(np.random.default_rng(100 + i), side, side, 2)
+        rid, cid = srv.submit(st, rows=side, cols=side)
+        img, _, _ = srv.wait(rid, 60)
+        srv.release(cid)
+        if i == 0:
+            first = (side, st, img)
+    s = srv.stats()
+    srv.close()
+    assert s["completed"] == 40 and s["failed"] == 0 and s["heap_fallbacks"] == 0
+    side, st, img = first
+    fresh = pg.Server(96 << 20, fp, storage="f16", step_stamps=4000)
+    again, _, _ = fresh.wait(fresh.submit(st, rows=side, cols=side)[0], 60)
+    fresh.close()
+    assert np.array_equal(img, again)
 
 
 def test_continuation_matches_batch_painting(pg):
