@@ -676,7 +676,8 @@ def run_batch(pg, torch, storage: str, ncanvas: int, max_strokes, rank: int = 0,
         dist.all_reduce(n_, op=dist.ReduceOp.SUM)
         dt, n = float(t_.item()), int(n_.item())
     px = sum(r * c for r, c, _ in specs)
-    cl, nclusters = pg.batch_last_shape()
+    cl, nclusters, cta_threads = pg.batch_last_shape()
+    split_cl, split_canvases = pg.batch_last_split()
     per_stroke = [pg_stroke_stamps(np.asarray(s[1]), s[3]) for s in strokes]
     per_canvas = np.zeros(len(specs))
     for s_, k_ in zip(strokes, per_stroke):
@@ -690,7 +691,8 @@ def run_batch(pg, torch, storage: str, ncanvas: int, max_strokes, rank: int = 0,
     return {"metric": "stamps/s", "value": round(n / dt, 1), "unit": "stamps/s", "stamps": n,
             "s": round(dt, 3), "storage": storage, "gpu_launches": pg.kernel_launch_count() - l0,
             "roofline": roof,
-            "ctas_per_canvas": cl, "clusters": nclusters,
+            "ctas_per_canvas": cl, "clusters": nclusters, "cta_threads": cta_threads,
+            "heaviest_canvases_launch": {"ctas_per_canvas": split_cl, "canvases": split_canvases},
             "makespan_s": round(dt, 3),
             "heaviest_canvas_stamps": int(per_canvas.max()) if len(per_canvas) else 0,
             "heaviest_canvas_stamps_per_s": round(float(per_canvas.max()) / dt, 1) if n else 0.0,

@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define PAINTY_GB300_ABI_VERSION 1
+#define PAINTY_GB300_ABI_VERSION 2
 
 typedef enum painty_status {
   PAINTY_OK = 0,
@@ -245,10 +245,17 @@ painty_status painty_paint_batch(painty_canvas* const* canvases, painty_brush* c
                                  void* stream);
 
 /* The launch shape the last painty_paint_batch on this thread chose: CTAs per canvas (a
- * thread-block cluster sharing each stamp; picked by a makespan model of the batch unless the
- * environment variable PAINTY_BATCH_CLUSTER sets it) and the number of clusters launched.
- * No counterpart in painty. */
-painty_status painty_batch_last_shape(int32_t* cluster, int32_t* clusters);
+ * thread-block cluster sharing each stamp), the number of clusters launched, and threads per
+ * CTA (1024: one CTA per SM; 512: two per SM, twice the canvases in flight). Picked by a
+ * makespan model of the batch unless the environment variables PAINTY_BATCH_CLUSTER /
+ * PAINTY_BATCH_THREADS set them. Any pointer may be NULL. No counterpart in painty. */
+painty_status painty_batch_last_shape(int32_t* cluster, int32_t* clusters, int32_t* threads);
+/* Whether the last painty_paint_batch on this thread gave its heaviest canvases a launch of
+ * their own, next to the rest, on clusters of `cluster` CTAs (0: no such launch), and how
+ * many canvases that launch painted. The shape above is then that of the rest. A canvas's
+ * stamps run in order, so the heaviest canvas bounds a batch unless more CTAs share its
+ * stamps. No counterpart in painty. */
+painty_status painty_batch_last_split(int32_t* cluster, int32_t* canvases);
 
 /* ------------------------------------------------------------------ texture brush
  * TextureBrush<vec3> (painty/renderer/TextureBrush.hxx:20-237) with its Smudge<vec3>

@@ -99,7 +99,8 @@ _sig("painty_stamps", _P, _P, _P, _I64, _P)
 _sig("painty_stroke", _P, _P, _P, _I32, _D, C.POINTER(_I64), _P)
 _sig("painty_mix_paint", _P, _I32, _P, _P, _P, _P)
 _sig("painty_paint_batch", _P, _P, _I32, _P, _I64, _P, _I64, C.POINTER(_I64), _P)
-_sig("painty_batch_last_shape", C.POINTER(_I32), C.POINTER(_I32))
+_sig("painty_batch_last_shape", C.POINTER(_I32), C.POINTER(_I32), C.POINTER(_I32))
+_sig("painty_batch_last_split", C.POINTER(_I32), C.POINTER(_I32))
 _sig("painty_texture_brush_create", _P, _I32, _I32, C.POINTER(_P))
 _sig("painty_texture_brush_destroy", _P)
 _sig("painty_texture_brush_set_radius", _P, _D)
@@ -763,9 +764,17 @@ def paint_batch(canvases, brushes, strokes, stream=None) -> int:
 
 
 def batch_last_shape():
-    """(CTAs per canvas, clusters) of the last paint_batch on this thread."""
+    """(CTAs per canvas, clusters, threads per CTA) of the last paint_batch on this thread."""
+    cl, n, t = _I32(), _I32(), _I32()
+    _check(_lib.painty_batch_last_shape(C.byref(cl), C.byref(n), C.byref(t)))
+    return cl.value, n.value, t.value
+
+
+def batch_last_split():
+    """(cluster size, canvases) of the last paint_batch's launch for its heaviest canvases on
+    this thread ((0, 0): none)."""
     cl, n = _I32(), _I32()
-    _check(_lib.painty_batch_last_shape(C.byref(cl), C.byref(n)))
+    _check(_lib.painty_batch_last_split(C.byref(cl), C.byref(n)))
     return cl.value, n.value
 
 

@@ -499,6 +499,17 @@ void upload_planes(void* const* planes, int nch, DevType dt, int32_t rows, int32
   PG_CUDA(cudaStreamSynchronize(st));
 }
 
+// The device address of pinned (page-locked, mapped) host memory, or nullptr for pageable
+// memory. Kernels read and write such memory in place over the host link.
+const void* mapped_host(const void* host) {
+  cudaPointerAttributes pa{};
+  if (cudaPointerGetAttributes(&pa, host) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return pa.type == cudaMemoryTypeHost ? pa.devicePointer : nullptr;
+}
+
 void upload_planes_async(void* const* planes, int nch, DevType dt, int32_t rows, int32_t cols,
                          int64_t pitch, const void* host, painty_host_format fmt,
                          cudaStream_t st, int64_t estride) {
@@ -519,18 +530,24 @@ void upload_planes_async(void* const* planes, int nch, DevType dt, int32_t rows,
       return;
     }
   }
+  // pinned host memory is read in place by the scatter kernel; pageable memory goes through
+  // a device staging copy
+  const void* mapped = mapped_host(host);
   void* staging = nullptr;
-  staging = temp_alloc(n * nch * hes, st);
-  PG_CUDA(cudaMemcpyAsync(staging, host, n * nch * hes, cudaMemcpyHostToDevice, st));
+  if (!mapped) {
+    staging = temp_alloc(n * nch * hes, st);
+    PG_CUDA(cudaMemcpyAsync(staging, host, n * nch * hes, cudaMemcpyHostToDevice, st));
+  }
+  const void* src = mapped ? mapped : staging;
   PlanePtrs pp{{planes[0], nch > 1 ? planes[1] : nullptr, nch > 2 ? planes[2] : nullptr}};
   const int il = host_is_interleaved(fmt) ? 1 : 0;
   if (f64)
-    launch_scatter<double>(dt, static_cast<const double*>(staging), pp, nch, il, rows, cols,
-                           pitch, estride, st);
+    launch_scatter<double>(dt, static_cast<const double*>(src), pp, nch, il, rows, cols, pitch,
+                           estride, st);
   else
-    launch_scatter<float>(dt, static_cast<const float*>(staging), pp, nch, il, rows, cols,
-                          pitch, estride, st);
-  PG_CUDA(cudaFreeAsync(staging, st));
+    launch_scatter<float>(dt, static_cast<const float*>(src), pp, nch, il, rows, cols, pitch,
+                          estride, st);
+  if (staging) PG_CUDA(cudaFreeAsync(staging, st));
 }
 
 void download_planes(const void* const* planes, int nch, DevType dt, int32_t rows,
@@ -558,19 +575,24 @@ void download_planes_async(const void* const* planes, int nch, DevType dt, int32
       return;
     }
   }
-  void* staging = nullptr;
-  staging = temp_alloc(n * nch * hes, st);
+  // pinned host memory is written in place by the gather kernel; pageable memory through a
+  // device staging copy
+  void* mapped = const_cast<void*>(mapped_host(host));
+  void* staging = mapped ? nullptr : temp_alloc(n * nch * hes, st);
+  void* dst = mapped ? mapped : staging;
   PlanePtrs pp{{const_cast<void*>(planes[0]), nch > 1 ? const_cast<void*>(planes[1]) : nullptr,
                 nch > 2 ? const_cast<void*>(planes[2]) : nullptr}};
   const int il = host_is_interleaved(fmt) ? 1 : 0;
   if (f64)
-    launch_gather<double>(dt, pp, static_cast<double*>(staging), nch, il, rows, cols, pitch,
+    launch_gather<double>(dt, pp, static_cast<double*>(dst), nch, il, rows, cols, pitch,
                           estride, st);
   else
-    launch_gather<float>(dt, pp, static_cast<float*>(staging), nch, il, rows, cols, pitch,
-                         estride, st);
-  PG_CUDA(cudaMemcpyAsync(host, staging, n * nch * hes, cudaMemcpyDeviceToHost, st));
-  PG_CUDA(cudaFreeAsync(staging, st));
+    launch_gather<float>(dt, pp, static_cast<float*>(dst), nch, il, rows, cols, pitch, estride,
+                         st);
+  if (staging) {
+    PG_CUDA(cudaMemcpyAsync(host, staging, n * nch * hes, cudaMemcpyDeviceToHost, st));
+    PG_CUDA(cudaFreeAsync(staging, st));
+  }
 }
 
 void fill_planes(void* const* planes, int nch, DevType dt, int64_t elems, const double* v,
@@ -977,7 +999,7 @@ __global__ void __launch_bounds__(32 * (kBulkConsumers + 1), 2) km_composite16_b
           S[c] = f2(elem16<TK>(cur.s[c], i), elem16<TK>(cur.s[c], i + 1));
           R[c] = f2(r[c][i], r[c][i + 1]);
         }
-        km_reflectance2x3(K, S, R, d);
+        km_reflectance2x3<false>(K, S, R, d);  // 16-bit layers: no guards needed
 #pragma unroll
         for (int c = 0; c < 3; c++) {
           r[c][i] = R[c].x;

@@ -312,6 +312,13 @@ __device__ __forceinline__ float2 km_reflectance2(float2 K, float2 S, float2 R0,
 // channel: R_c = N_c / D_c = N_c * (product of the other two D) / (D_r D_g D_b). D lies
 // between about 0.03 and 30, so the product stays far inside FP32's range; the extra products
 // cost a few roundings (well below FP16 storage's).
+// kGuards: painty's two guards -- S replaced by 1e-11 where |S| <= 1e4 DBL_EPSILON (it
+// divides by S), and R kept where |d| < 1e4 DBL_EPSILON. 16-bit layers skip both. This form
+// never divides by S, so the substitution moves R by about 1e-11 relative, below FP32's
+// resolution. Thickness stored as FP16 is either 0 or at least 2^-24, and at d = +-0 the
+// formula itself returns R exactly (x = 0 takes the series: u = d = 0, w = g = 1, so every
+// numerator is R, every denominator 1 and the reciprocal of their product 1).
+template <bool kGuards = true>
 __device__ __forceinline__ void km_reflectance2x3(const float2 (&K)[3], const float2 (&S)[3],
                                                   float2 (&R)[3], float2 d) {
   constexpr float kEps = 2.220446049250313e-12f;  // 1e4 * DBL_EPSILON
@@ -320,8 +327,10 @@ __device__ __forceinline__ void km_reflectance2x3(const float2 (&K)[3], const fl
 #pragma unroll
   for (int c = 0; c < 3; c++) {
     float2 s = S[c];
-    s.x = fabsf(s.x) > kEps ? s.x : 1e-11f;
-    s.y = fabsf(s.y) > kEps ? s.y : 1e-11f;
+    if constexpr (kGuards) {
+      s.x = fabsf(s.x) > kEps ? s.x : 1e-11f;
+      s.y = fabsf(s.y) > kEps ? s.y : 1e-11f;
+    }
     float2 q = __fmul2_rn(K[c], __ffma2_rn(f2(2.0f, 2.0f), s, K[c]));
     q.x = fmaxf(q.x, 1e-30f);
     q.y = fmaxf(q.y, 1e-30f);
@@ -352,9 +361,14 @@ __device__ __forceinline__ void km_reflectance2x3(const float2 (&K)[3], const fl
   const float2 o[3] = {__fmul2_rn(__fmul2_rn(num[0], d12), inv),
                        __fmul2_rn(__fmul2_rn(num[1], d02), inv),
                        __fmul2_rn(__fmul2_rn(num[2], d01), inv)};
-  const bool keep_x = fabsf(d.x) < kEps, keep_y = fabsf(d.y) < kEps;
+  if constexpr (kGuards) {
+    const bool keep_x = fabsf(d.x) < kEps, keep_y = fabsf(d.y) < kEps;
 #pragma unroll
-  for (int c = 0; c < 3; c++) R[c] = f2(keep_x ? R[c].x : o[c].x, keep_y ? R[c].y : o[c].y);
+    for (int c = 0; c < 3; c++) R[c] = f2(keep_x ? R[c].x : o[c].x, keep_y ? R[c].y : o[c].y);
+  } else {
+#pragma unroll
+    for (int c = 0; c < 3; c++) R[c] = o[c];
+  }
 }
 
 // painty's coth (painty/core/Math.hxx:157-169) and ComputeReflectance in double, in the

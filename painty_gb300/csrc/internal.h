@@ -77,6 +77,9 @@ void device_free_on(void* p, cudaStream_t st);
 void* temp_alloc(size_t bytes, cudaStream_t st);
 // Pool settings shared by the library's pools (retained memory, no cross-stream reuse waits).
 void configure_pool(cudaMemPool_t pool);
+// The device address of pinned (page-locked, mapped) host memory, or nullptr for pageable
+// memory: kernels read and write such memory in place over the host link.
+const void* mapped_host(const void* host);
 
 // One device reservation carved up on the host: allocation and release are host bookkeeping
 // (best fit, neighbours merged on release, 256-byte granules), so neither calls the driver.
@@ -260,6 +263,7 @@ void copy_planes_async(void* const* dst, const void* const* src, int nch, size_t
 // launch (nonzero: the kernel reported an internal error).
 struct BatchOptions {
   int max_cluster = 8;
+  int threads = 0;  // CTA size: 512 or 1024, 0 = chosen by the cost model
   unsigned* status_host = nullptr;
   // pinned host memory the launch's descriptors are staged in when they fit (the caller
   // guarantees no earlier copy from it is still pending); otherwise a pageable copy
@@ -274,6 +278,10 @@ struct BatchOptions {
   size_t device_scratch_bytes = 0;
   size_t* desc_needed = nullptr;
   size_t* scratch_needed = nullptr;
+  // pinned host word the kernel sets to done_value once the launch's results (and the status
+  // word) are visible to the host; such a launch is never split
+  unsigned* done_host = nullptr;
+  unsigned done_value = 0;
 };
 void paint_batch(painty_canvas* const* canvases, painty_brush* const* brushes, int32_t nc,
                  const painty_stroke_desc* strokes, int64_t ns, const double* points,

@@ -21,7 +21,11 @@
 // submission order; different canvases are independent, so a request's result does not
 // depend on what else is in flight. painty_server_release drops a canvas once its queued
 // requests are done.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -34,6 +38,7 @@
 #include <unordered_map>
 #include <vector>
 
+#include "device_common.cuh"
 #include "internal.h"
 
 namespace {
@@ -94,6 +99,14 @@ struct Slot {
   cudaStream_t st = nullptr;
   cudaEvent_t ev = nullptr;
   unsigned* status = nullptr;  // pinned: the last launch's kernel status word
+  // pinned completion word: the slot's self-signalling kernels store `seq` into it when their
+  // results are visible, and the worker polls it (nothing is queued behind those kernels: an
+  // item waiting on a long kernel holds back other streams' work in the device's queues)
+  unsigned* done = nullptr;
+  unsigned* done_dev = nullptr;  // its device address
+  unsigned seq = 0;
+  double armed_at = 0.0;
+  unsigned* d_counter = nullptr;  // device: finish kernel's count of finished blocks
   void* staging = nullptr;     // pinned: the last launch's descriptors (kStagingBytes)
   void* d_desc = nullptr;      // device: the launch's descriptors (kStagingBytes)
   void* d_scratch = nullptr;   // device: the launch's scratch, grown to what launches need
@@ -114,7 +127,9 @@ struct painty_server {
   std::unique_ptr<pg::DeviceHeap> heap;  // canvases, images, brush buffers, slot buffers
   std::vector<Slot> slots;
   unsigned* status_words = nullptr;
+  unsigned* done_words = nullptr;
   unsigned char* staging = nullptr;  // pinned, kStagingBytes per slot
+  std::vector<int> watch;  // slots whose self-signalling launch is in flight (worker only)
   std::multimap<size_t, void*> pinned_free;  // pinned blobs of released canvases, by size
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
@@ -187,6 +202,77 @@ void CUDART_CB slot_passed(void* p) {
 void mark_slot(Slot& sl) {
   PG_CUDA(cudaEventRecord(sl.ev, sl.st));
   PG_CUDA(cudaLaunchHostFunc(sl.st, slot_passed, &sl));
+}
+
+// The next completion value of a slot whose launch signals by itself (worker thread).
+unsigned arm_slot(painty_server* s, Slot& sl) {
+  sl.seq++;
+  sl.armed_at = now_s();
+  s->watch.push_back(sl.index);
+  return sl.seq;
+}
+
+// Slots whose completion word caught up with their launch (worker thread, lock held).
+void poll_watched(painty_server* s) {
+  for (size_t i = 0; i < s->watch.size();) {
+    Slot& sl = s->slots[s->watch[i]];
+    bool passed = *reinterpret_cast<volatile unsigned*>(sl.done) == sl.seq;
+    if (!passed && now_s() - sl.armed_at > 2.0) {
+      // a long launch: make sure the stream has not failed (a failed stream never signals)
+      const cudaError_t q = cudaStreamQuery(sl.st);
+      if (q != cudaErrorNotReady) {
+        if (q != cudaSuccess) *sl.status = 1u << 31;  // reported as an internal error
+        passed = true;
+      }
+      sl.armed_at = now_s();
+    }
+    if (passed) {
+      std::atomic_thread_fence(std::memory_order_acquire);  // then its status and results
+      s->passed.push_back(sl.index);
+      s->watch[i] = s->watch.back();
+      s->watch.pop_back();
+    } else {
+      i++;
+    }
+  }
+}
+
+template <class TK, class TV>
+struct LayerView {
+  const TK* K[3];
+  const TK* S[3];
+  const TV* V;
+  int64_t es;  // element stride (8: packed pixel records)
+};
+
+// The composite of a canvas (its wet layer over R0, Renderer::compose of one layer,
+// painty/renderer/Renderer.hxx:26-53) written as float RGB straight into pinned host memory,
+// one grid-stride pass; the last block to finish stores `value` into the completion word.
+template <class TK, class TV, class M>
+__global__ void finish_kernel(LayerView<TK, TV> w, const M* __restrict__ r0r,
+                              const M* __restrict__ r0g, const M* __restrict__ r0b, int32_t rows,
+                              int32_t cols, int64_t wpitch, int64_t rpitch,
+                              float* __restrict__ out, unsigned* counter, unsigned* done,
+                              unsigned value) {
+  const int64_t n = static_cast<int64_t>(rows) * cols;
+  for (int64_t p = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; p < n;
+       p += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int64_t r = p / cols, c = p - r * cols;
+    const int64_t j = (r * wpitch + c) * w.es, e = r * rpitch + c;
+    const M d = pg::ld_elem<M>(w.V + j);
+    const M R[3] = {r0r[e], r0g[e], r0b[e]};
+#pragma unroll
+    for (int ch = 0; ch < 3; ch++)
+      out[p * 3 + ch] = static_cast<float>(
+        pg::km_reflectance(pg::ld_elem<M>(w.K[ch] + j), pg::ld_elem<M>(w.S[ch] + j), R[ch], d));
+  }
+  __threadfence_system();  // this thread's results before the block's count
+  __syncthreads();
+  if (threadIdx.x == 0 && atomicAdd(counter, 1u) == gridDim.x - 1) {
+    __threadfence_system();
+    *reinterpret_cast<volatile unsigned*>(done) = value;
+    __threadfence_system();
+  }
 }
 
 void image_alloc(painty_server* s, ServerCanvas* c, cudaStream_t st) {
@@ -363,6 +449,8 @@ void launch_chunk(painty_server* s, ServerRequest* r, ServerCanvas* c, int cap) 
   opt.device_scratch_bytes = sl.d_scratch_bytes;
   size_t scratch_needed = 0;
   opt.scratch_needed = &scratch_needed;
+  opt.done_host = sl.done;  // the kernel signals its own completion
+  opt.done_value = arm_slot(s, sl);
   c->brush->heap_stream = sl.st;
   int64_t n = 0;
   painty_canvas* cvs[1] = {c->cv};
@@ -376,24 +464,61 @@ void launch_chunk(painty_server* s, ServerRequest* r, ServerCanvas* c, int cap) 
     sl.d_scratch_bytes = (scratch_needed + (64 << 10) - 1) / (64 << 10) * (64 << 10);
     sl.d_scratch = s->heap->alloc(sl.d_scratch_bytes, sl.st);
   }
-  mark_slot(sl);
   r->stamps += budget;
   r->next = k;
   s->stats.worker_launch_us += static_cast<int64_t>((now_s() - t0) * 1e6);
 }
 
-// The composite of a finished request's canvas, downloaded into the caller's buffer in the
-// slot's stream order (worker thread).
+template <class TK, class TV, class M>
+void launch_finish_kernel(painty_server* s, Slot& sl, ServerCanvas* c, float* out_dev,
+                          unsigned value) {
+  const painty_layer& wet = c->cv->wet;
+  const painty_image& r0 = c->cv->r0;
+  LayerView<TK, TV> w{};
+  for (int i = 0; i < 3; i++) {
+    w.K[i] = static_cast<const TK*>(wet.K[i]);
+    w.S[i] = static_cast<const TK*>(wet.S[i]);
+  }
+  w.V = static_cast<const TV*>(wet.V);
+  w.es = wet.estride;
+  PG_CUDA(cudaMemsetAsync(sl.d_counter, 0, sizeof(unsigned), sl.st));
+  const int64_t n = static_cast<int64_t>(c->rows) * c->cols;
+  const int grid = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256,
+                                                                          int64_t(s->sms) * 8)));
+  finish_kernel<TK, TV, M><<<grid, 256, 0, sl.st>>>(
+    w, static_cast<const M*>(r0.R[0]), static_cast<const M*>(r0.R[1]),
+    static_cast<const M*>(r0.R[2]), c->rows, c->cols, wet.pitch, r0.pitch, out_dev,
+    sl.d_counter, sl.done_dev, value);
+  pg::count_launch();
+  PG_CUDA(cudaGetLastError());
+}
+
+// The composite of a finished request's canvas into the caller's buffer, in the slot's
+// stream order (worker thread): computed straight into a pinned buffer by one kernel that
+// signals its completion word, or composed on the device and downloaded (pageable buffers).
 void launch_finish(painty_server* s, ServerRequest* r, ServerCanvas* c) {
   const double t0 = now_s();
   Slot& sl = s->slots[r->slot];
-  const painty_layer* L[1] = {&c->cv->wet};
-  pg::launch_compose(L, 1, &c->cv->r0, &c->img, sl.st);
-  const void* p[3] = {c->img.R[0], c->img.R[1], c->img.R[2]};
   // out_rgb is float RGB whatever the storage (F64 results are rounded to float)
-  pg::download_planes_async(p, 3, pg::r_type(c->img.storage), c->rows, c->cols, c->img.pitch,
-                            r->out_rgb, PAINTY_HOST_F32_INTERLEAVED, sl.st);
-  mark_slot(sl);
+  float* out_dev = static_cast<float*>(const_cast<void*>(pg::mapped_host(r->out_rgb)));
+  if (out_dev) {
+    const unsigned v = arm_slot(s, sl);
+    switch (s->opt.storage) {
+      case PAINTY_STORAGE_F16: launch_finish_kernel<__half, __half, float>(s, sl, c, out_dev, v); break;
+      case PAINTY_STORAGE_BF16:
+        launch_finish_kernel<__nv_bfloat16, __half, float>(s, sl, c, out_dev, v);
+        break;
+      case PAINTY_STORAGE_F64: launch_finish_kernel<double, double, double>(s, sl, c, out_dev, v); break;
+      default: launch_finish_kernel<float, float, float>(s, sl, c, out_dev, v); break;
+    }
+  } else {
+    const painty_layer* L[1] = {&c->cv->wet};
+    pg::launch_compose(L, 1, &c->cv->r0, &c->img, sl.st);
+    const void* p[3] = {c->img.R[0], c->img.R[1], c->img.R[2]};
+    pg::download_planes_async(p, 3, pg::r_type(c->img.storage), c->rows, c->cols, c->img.pitch,
+                              r->out_rgb, PAINTY_HOST_F32_INTERLEAVED, sl.st);
+    mark_slot(sl);
+  }
   s->stats.worker_finish_us += static_cast<int64_t>((now_s() - t0) * 1e6);
 }
 
@@ -469,6 +594,7 @@ bool worker_round(painty_server* s, std::unique_lock<std::mutex>& lk) {
   };
   std::vector<Running> running;
   std::vector<int> passed;
+  poll_watched(s);
   passed.swap(s->passed);
   if (!passed.empty()) {
     std::vector<ServerRequest*> by_slot(s->slots.size(), nullptr);
@@ -561,7 +687,14 @@ bool worker_round(painty_server* s, std::unique_lock<std::mutex>& lk) {
   // a failed request's slot is not reused before its stream has drained (its callback takes
   // the lock, so the wait happens here, unlocked)
   for (auto& f : failures)
-    if (f.first->slot >= 0) cudaStreamSynchronize(s->slots[f.first->slot].st);
+    if (f.first->slot >= 0) {
+      Slot& sl = s->slots[f.first->slot];
+      cudaStreamSynchronize(sl.st);
+      // any completion value its launches wrote is stale now: the next one starts above it
+      s->watch.erase(std::remove(s->watch.begin(), s->watch.end(), sl.index), s->watch.end());
+      const unsigned seen = *reinterpret_cast<volatile unsigned*>(sl.done);
+      sl.seq = std::max(sl.seq, seen);
+    }
   const double busy = now_s() - t_work;
   lk.lock();
   for (ServerCanvas* c : drops) s->canvases.erase(c->id);  // its requests are all finished
@@ -588,10 +721,14 @@ void worker_main(painty_server* s) {
   uint64_t idle_gen = ~0ull;
   while (true) {
     // wake on a finished launch, a drop, or a change to what could be admitted
-    s->cv_work.wait_for(lk, std::chrono::milliseconds(50), [&] {
+    // launches that signal through their completion words are polled every 50 us
+    const auto wait = s->watch.empty() ? std::chrono::microseconds(50000)
+                                       : std::chrono::microseconds(50);
+    s->cv_work.wait_for(lk, wait, [&] {
       return s->stop || !s->passed.empty() || !s->to_drop.empty() ||
              (!s->pending.empty() && s->gen != idle_gen);
     });
+    poll_watched(s);
     if (s->stop) break;
     const uint64_t g = s->gen;
     worker_round(s, lk);
@@ -639,6 +776,9 @@ painty_status painty_server_create(const painty_server_options* opt, painty_serv
       s->opt.budget_bytes + static_cast<size_t>(s->opt.max_active) * (kStagingBytes + (1u << 20)) +
       (size_t(256) << 20));
     PG_CUDA(cudaMallocHost(&s->status_words, sizeof(unsigned) * s->opt.max_active));
+    // completion words a cache line apart (the GPU writes them, the worker polls them)
+    PG_CUDA(cudaMallocHost(&s->done_words, 64 * static_cast<size_t>(s->opt.max_active)));
+    std::memset(s->done_words, 0, 64 * static_cast<size_t>(s->opt.max_active));
     PG_CUDA(cudaMallocHost(&s->staging, kStagingBytes * s->opt.max_active));
     s->slots.resize(static_cast<size_t>(s->opt.max_active));
     for (int i = 0; i < s->opt.max_active; i++) {
@@ -646,6 +786,10 @@ painty_status painty_server_create(const painty_server_options* opt, painty_serv
       PG_CUDA(cudaStreamCreateWithFlags(&sl.st, cudaStreamNonBlocking));
       PG_CUDA(cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming));
       sl.status = s->status_words + i;
+      sl.done = s->done_words + 16 * i;
+      sl.done_dev = static_cast<unsigned*>(const_cast<void*>(pg::mapped_host(sl.done)));
+      PG_REQUIRE(sl.done_dev != nullptr, "pinned completion words are not mapped");
+      sl.d_counter = static_cast<unsigned*>(s->heap->alloc(256, s->stream));
       sl.staging = s->staging + kStagingBytes * i;
       *sl.status = 0;
       sl.owner = s.get();
@@ -830,10 +974,12 @@ painty_status painty_server_destroy(painty_server* s) {
       cudaStreamDestroy(sl.st);
     }
     cudaFreeHost(s->status_words);
+    cudaFreeHost(s->done_words);
     cudaFreeHost(s->staging);
     for (Slot& sl : s->slots) {
       s->heap->free(sl.d_desc, s->stream);
       s->heap->free(sl.d_scratch, s->stream);
+      s->heap->free(sl.d_counter, s->stream);
     }
     s->heap.reset();
     cudaStreamDestroy(s->stream);

@@ -41,6 +41,7 @@
 #include <cmath>
 #include <cstring>
 #include <cstdlib>
+#include <cstdio>
 #include <map>
 #include <tuple>
 #include <queue>
@@ -475,7 +476,11 @@ __host__ __device__ inline StampSmem stamp_smem_layout(int F, int S, int ndisc, 
 }
 
 constexpr int kEpochMax = 32767;  // owner keys: ((kEpochMax - epoch) << 16) | pixel index
-constexpr int kWarps = kStampThreads / 32;
+// Whether paint_waves' per-thread pixel mask (64 bits: rows per warp x 32-column groups)
+// covers an F x F box with `threads` threads.
+__host__ __device__ constexpr bool waves_fit(int F, int threads) {
+  return ((F + threads / 32 - 1) / (threads / 32)) * ((F + 31) / 32) <= 64;
+}
 
 // ---------------------------------------------------------------------- snapshot ring
 // painty refreshes the snapshot from the canvas over a ring around every stamp: the box grown
@@ -758,6 +763,7 @@ __device__ __noinline__ int paint_waves(const StampArgs<TK, TV>& a, const StampP
   const int F = a.F, S = a.S;
   const int cells = S * S;
   const int NC = (F + 31) / 32;
+  const int kWarps = static_cast<int>(blockDim.x) >> 5;
   if (epoch > kEpochMax - 2 * kMaxWaves) {  // owner keys about to wrap: reset the table
     for (int i = tid; i < cells; i += blockDim.x) own[i] = INT_MAX;
     epoch = 0;
@@ -1182,8 +1188,9 @@ struct BatchArgs {
   const BatchCanvas<TK, TV>* canvases;
   const BatchStroke* strokes;
   const double* points;
-  const int32_t* order;  // canvases, heaviest first
-  int32_t ncanvas;
+  const int32_t* order;  // this launch's queue of canvases, heaviest first
+  int32_t norder;        // its length
+  int32_t ncanvas;       // canvases of the batch (indices in the queue are below it)
   int* counter;
   int* claims;        // per cluster: the canvas it claimed last
   M* scratch_pickup;  // per cluster: Smax^2 cell records
@@ -1194,12 +1201,17 @@ struct BatchArgs {
   // extents of the descriptor arrays and the scratch, for the bounds-checked build
   int64_t nstrokes, npoints;
   int32_t nslots;
+  unsigned* status_host;  // device address of pinned host memory for the final status, or null
+  unsigned* done_host;    // device address of a pinned completion word, or null
+  unsigned done_value;    // written there once everything above is visible to the host
 };
 
 // Persistent batched painting: each CTA claims canvases (heaviest first) and applies their
-// strokes in order, each as setRadius + dip + paintStroke on the canvas's brush.
-template <class TK, class TV>
-__global__ void __launch_bounds__(kStampThreads, 1) batch_kernel(const __grid_constant__ BatchArgs<TK, TV> b) {
+// strokes in order, each as setRadius + dip + paintStroke on the canvas's brush. NT threads
+// per CTA: 1024 (one CTA per SM) or 512 (two per SM, twice the canvases in flight, each
+// painted by half the threads), with the same register budget.
+template <class TK, class TV, int NT>
+__global__ void __launch_bounds__(NT, 1024 / NT) batch_kernel(const __grid_constant__ BatchArgs<TK, TV> b) {
   using M = typename MathOf<TK>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ StampParams sparams[kParamRing];
@@ -1215,7 +1227,7 @@ __global__ void __launch_bounds__(kStampThreads, 1) batch_kernel(const __grid_co
     __syncthreads();
     if (tid == 0 && crank == 0) {
       const int i = atomicAdd(b.counter, 1);
-      b.claims[cid] = i < b.ncanvas ? b.order[i] : -1;
+      b.claims[cid] = i < b.norder ? b.order[i] : -1;
     }
     if (csize > 1) cluster_barrier();
     if (tid == 0) s_item = __ldcg(b.claims + cid);
@@ -1224,10 +1236,10 @@ __global__ void __launch_bounds__(kStampThreads, 1) batch_kernel(const __grid_co
     else
       __syncthreads();
     const int ci = s_item;
-    if (ci < 0) return;
+    if (ci < 0) break;
     if (!in_bounds(b.status, kBoundsDescriptor, ci, b.ncanvas) ||
         !in_bounds(b.status, kBoundsDescriptor, cid, b.nslots))
-      return;
+      break;
     const BatchCanvas<TK, TV>& cv = b.canvases[ci];
     if (!in_bounds(b.status, kBoundsDescriptor, cv.first_stroke + cv.nstrokes - 1,
                    b.nstrokes + (cv.nstrokes == 0 ? 1 : 0)))
@@ -1328,6 +1340,21 @@ __global__ void __launch_bounds__(kStampThreads, 1) batch_kernel(const __grid_co
         }
       }
       ran = true;
+    }
+  }
+  // the last CTA to finish stores the launch's status word into the caller's pinned memory
+  // (status_host: its device address), so no copy has to follow the kernel on the stream
+  // and then the completion word: a host thread polling it learns the launch is over without
+  // anything queued behind the kernel
+  if ((b.status_host || b.done_host) && tid == 0) {
+    __threadfence_system();  // this CTA's canvas and brush writes
+    if (atomicAdd(b.counter + 7, 1) == static_cast<int>(gridDim.x) - 1) {
+      __threadfence_system();
+      if (b.status_host)
+        *reinterpret_cast<volatile unsigned*>(b.status_host) = atomicOr(b.status, 0u);
+      __threadfence_system();
+      if (b.done_host) *reinterpret_cast<volatile unsigned*>(b.done_host) = b.done_value;
+      __threadfence_system();
     }
   }
 }
@@ -1571,14 +1598,14 @@ SmemPlan plan_smem(int F, int S, int ndisc, bool allow_small, bool allow_pick = 
 // launch).
 template <class Arg>
 void launch_clustered(void (*kern)(Arg), int grid, int cluster, size_t smem, cudaStream_t st,
-                      const Arg& arg) {
+                      const Arg& arg, int threads = kStampThreads) {
   if (cluster <= 1) {
-    kern<<<grid, kStampThreads, smem, st>>>(arg);
+    kern<<<grid, threads, smem, st>>>(arg);
     return;
   }
   cudaLaunchConfig_t cfg{};
   cfg.gridDim = dim3(static_cast<unsigned>(grid));
-  cfg.blockDim = dim3(kStampThreads);
+  cfg.blockDim = dim3(static_cast<unsigned>(threads));
   cfg.dynamicSmemBytes = smem;
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
@@ -1593,10 +1620,10 @@ void launch_clustered(void (*kern)(Arg), int grid, int cluster, size_t smem, cud
 
 // Clusters of `cluster` stamp CTAs (smem bytes each) that fit on the device at once.
 template <class Arg>
-int max_clusters(void (*kern)(Arg), int cluster, size_t smem) {
+int max_clusters(void (*kern)(Arg), int cluster, size_t smem, int threads = kStampThreads) {
   cudaLaunchConfig_t cfg{};
   cfg.gridDim = dim3(static_cast<unsigned>(cluster));
-  cfg.blockDim = dim3(kStampThreads);
+  cfg.blockDim = dim3(static_cast<unsigned>(threads));
   cfg.dynamicSmemBytes = smem;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -1853,20 +1880,46 @@ void run_stamps(painty_canvas* c, painty_brush* b, const std::vector<StampRec>& 
 constexpr double kStampFixed = 7000.0;
 constexpr double kStampPerPixel = 12.0;
 constexpr double kClusterSync = 1500.0;
+// 512-thread CTAs (two per SM): the fixed part and the per-pixel part relative to 1024
+constexpr double kHalfFixed = 1.2;
+constexpr double kHalfPerPixel = 2.4;
 
-thread_local int32_t g_last_batch_shape[2] = {0, 0};  // cluster size, clusters
+// cluster size, clusters, threads of the batch's main launch; cluster size and clusters of its
+// launch for the heaviest canvases (0: none)
+thread_local int32_t g_last_batch_shape[5] = {0, 0, 0, 0, 0};
+
+// A side stream of the calling thread (per device) with fork and join events, for a batch's
+// second launch.
+struct SideStream {
+  cudaStream_t st = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+};
+SideStream& side_stream() {
+  thread_local std::map<int, SideStream> by_dev;
+  int dev = 0;
+  PG_CUDA(cudaGetDevice(&dev));
+  SideStream& s = by_dev[dev];
+  if (!s.st) {
+    PG_CUDA(cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking));
+    PG_CUDA(cudaEventCreateWithFlags(&s.fork, cudaEventDisableTiming));
+    PG_CUDA(cudaEventCreateWithFlags(&s.join, cudaEventDisableTiming));
+  }
+  return s;
+}
 
 // Makespan of painting canvases with loads (stamps N, stamp-pixels P) on `slots` clusters of
 // `cl` CTAs, heaviest canvas first onto the least-loaded cluster (the kernel's claim order).
 double batch_makespan(const std::vector<double>& N, const std::vector<double>& P,
-                      const std::vector<int32_t>& order, int slots, int cl) {
+                      const std::vector<int32_t>& order, int slots, int cl, int threads) {
   if (slots < 1) return 1e300;
   std::priority_queue<double, std::vector<double>, std::greater<double>> q;
   for (int i = 0; i < slots; i++) q.push(0.0);
   double span = 0.0;
+  // 512-thread CTAs: half the threads per stamp pixel, and an SM shared by two CTAs
+  const double fixed = threads == 512 ? kStampFixed * kHalfFixed : kStampFixed;
+  const double per_pixel = threads == 512 ? kStampPerPixel * kHalfPerPixel : kStampPerPixel;
   for (int32_t c : order) {
-    const double t = N[c] * (kStampFixed + (cl > 1 ? kClusterSync : 0.0)) +
-                     kStampPerPixel * P[c] / cl;
+    const double t = N[c] * (fixed + (cl > 1 ? kClusterSync : 0.0)) + per_pixel * P[c] / cl;
     const double end = q.top() + t;
     q.pop();
     q.push(end);
@@ -1880,6 +1933,7 @@ double batch_makespan(const std::vector<double>& N, const std::vector<double>& P
 // clusters of each size fit on the device for a given dynamic size.
 struct BatchKernelInfo {
   std::mutex mu;
+  int threads = kStampThreads;
   size_t static_smem = 0;
   size_t allowed = 0;
   std::map<std::pair<int, size_t>, int> fit;
@@ -1897,21 +1951,41 @@ struct BatchKernelInfo {
     const auto key = std::make_pair(cluster, bytes);
     auto it = fit.find(key);
     if (it != fit.end()) return it->second;
-    const int n = max_clusters(kern, cluster, key.second);
+    const int n = max_clusters(kern, cluster, key.second, threads);
     fit.emplace(key, n);
     return n;
   }
 };
-template <class TK, class TV>
+template <class TK, class TV, int NT>
 BatchKernelInfo& batch_kernel_info() {
   static BatchKernelInfo* info = [] {
     auto* i = new BatchKernelInfo();
     cudaFuncAttributes fa{};
-    PG_CUDA(cudaFuncGetAttributes(&fa, batch_kernel<TK, TV>));
+    PG_CUDA(cudaFuncGetAttributes(&fa, batch_kernel<TK, TV, NT>));
     i->static_smem = fa.sharedSizeBytes;
+    i->threads = NT;
     return i;
   }();
   return *info;
+}
+
+int smem_per_sm() {
+  static int cached[64] = {0};
+  int dev = 0;
+  PG_CUDA(cudaGetDevice(&dev));
+  if (dev < 64 && cached[dev] > 0) return cached[dev];
+  int v = 0;
+  PG_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
+  if (dev < 64) cached[dev] = v;
+  return v;
+}
+
+// Thread count from the environment (PAINTY_BATCH_THREADS: 512 or 1024), 0 if unset.
+int env_threads(const char* name) {
+  const char* v = std::getenv(name);
+  if (!v || !*v) return 0;
+  const int n = std::atoi(v);
+  return n == 512 || n == 1024 ? n : 0;
 }
 
 template <class TK, class TV>
@@ -1926,8 +2000,22 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   std::vector<std::vector<int64_t>> per(nc);
   for (int64_t i = 0; i < ns; i++) per[strokes[i].canvas].push_back(i);
   // launch shared-memory budget: the opt-in maximum minus the kernel's static shared memory
-  BatchKernelInfo& info = batch_kernel_info<TK, TV>();
-  const size_t limit = static_cast<size_t>(max_dyn_smem()) - info.static_smem - 256;
+  BatchKernelInfo& info1k = batch_kernel_info<TK, TV, 1024>();
+  BatchKernelInfo& info512 = batch_kernel_info<TK, TV, 512>();
+  // shared-memory budgets: a 1024-thread CTA may take the opt-in maximum; two 512-thread CTAs
+  // share one SM's shared memory (each CTA also reserves a little for the system)
+  int reserved = 0;
+  {
+    int dev = 0;
+    PG_CUDA(cudaGetDevice(&dev));
+    PG_CUDA(cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev));
+  }
+  const size_t limit1k = static_cast<size_t>(max_dyn_smem()) - info1k.static_smem - 256;
+  const size_t half = static_cast<size_t>(smem_per_sm()) / 2;
+  const size_t limit512 =
+    std::min(static_cast<size_t>(max_dyn_smem()) - info512.static_smem - 256,
+             half > info512.static_smem + reserved + 256
+               ? half - info512.static_smem - reserved - 256 : size_t(0));
   std::vector<BatchStroke> bs;
   bs.reserve(static_cast<size_t>(ns));
   std::vector<double> work(nc, 0.0), loadN(nc, 0.0), loadP(nc, 0.0);
@@ -1935,7 +2023,6 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   disc_of.reserve(static_cast<size_t>(ns));
   std::map<std::pair<int32_t, int32_t>, int32_t> disc_cache;
   int32_t smax = 1;
-  size_t dyn = 0;
   int64_t total_stamps = 0;
   std::vector<int64_t> first(nc, 0);
   for (int32_t c = 0; c < nc; c++) {
@@ -2026,49 +2113,179 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   for (int32_t c = 0; c < nc; c++) order[c] = c;
   std::stable_sort(order.begin(), order.end(),
                    [&](int32_t a, int32_t b2) { return work[a] > work[b2]; });
-  // cluster size (autotuned by the cost model unless PAINTY_BATCH_CLUSTER sets it) and the
-  // strokes' shared-memory plans (clusters keep the pickup map in global memory)
-  auto kern = batch_kernel<TK, TV>;
-  int fmax_cm = 0;  // largest footprint whose cell maps live in global memory
-  auto plan_all = [&](int cl) {
-    dyn = 0;
-    fmax_cm = 0;
-    for (size_t i = 0; i < bs.size(); i++) {
-      const SmemPlan plan =
-        plan_smem_limit<M>(bs[i].F, bs[i].S, disc_of[i], limit, true, cl == 1, true);
-      bs[i].ndisc = plan.ndisc;
-      bs[i].plan = (plan.pick ? 1 : 0) | (plan.big ? 2 : 0) | (plan.cm_global ? 4 : 0);
-      if (plan.cm_global) fmax_cm = std::max(fmax_cm, bs[i].F);
-      dyn = std::max(dyn, plan.layout.total);
+  auto kern1k = batch_kernel<TK, TV, 1024>;
+  auto kern512 = batch_kernel<TK, TV, 512>;
+  // distinct stroke shapes (footprint side, map side, support-disc pixels): shared-memory
+  // plans are made per shape, and per canvas the shapes it paints
+  std::map<std::tuple<int, int, int>, int32_t> shape_id;
+  std::vector<std::tuple<int, int, int>> shapes;
+  std::vector<int32_t> shape_of(bs.size());
+  std::vector<std::vector<int32_t>> canvas_shapes(nc);
+  for (int32_t c = 0; c < nc; c++)
+    for (size_t k = 0; k < per[c].size(); k++) {
+      const size_t i = static_cast<size_t>(first[c]) + k;
+      const auto key = std::make_tuple(bs[i].F, bs[i].S, disc_of[i]);
+      auto it = shape_id.find(key);
+      if (it == shape_id.end()) {
+        it = shape_id.emplace(key, static_cast<int32_t>(shapes.size())).first;
+        shapes.push_back(key);
+      }
+      shape_of[i] = it->second;
+      auto& cs = canvas_shapes[c];
+      if (std::find(cs.begin(), cs.end(), it->second) == cs.end()) cs.push_back(it->second);
     }
-    // in whole KB (fewer distinct occupancy queries), within the budget the plans respect
-    dyn = std::min((std::max<size_t>(dyn, 16) + 1023) / 1024 * 1024, std::max<size_t>(dyn, limit));
-    info.allow_smem(kern, dyn);
+  // a shape's plan for a launch of nt-thread CTAs in clusters of cl (nullptr: the shape does
+  // not fit 512-thread CTAs); clusters keep the pickup map in global memory
+  std::map<std::tuple<int32_t, int, bool>, std::unique_ptr<SmemPlan>> plans;
+  auto shape_plan = [&](int32_t sid, int nt, int cl) -> const SmemPlan* {
+    const auto key = std::make_tuple(sid, nt, cl == 1);
+    auto it = plans.find(key);
+    if (it != plans.end()) return it->second.get();
+    std::unique_ptr<SmemPlan> pl;
+    const int F = std::get<0>(shapes[sid]), S = std::get<1>(shapes[sid]);
+    const int nd = std::get<2>(shapes[sid]);
+    if (nt == 1024) {
+      pl = std::make_unique<SmemPlan>(plan_smem_limit<M>(F, S, nd, limit1k, true, cl == 1, true));
+    } else if (waves_fit(F, 512) && limit512 > 0) {
+      try {
+        pl = std::make_unique<SmemPlan>(plan_smem_limit<M>(F, S, nd, limit512, true, cl == 1, true));
+      } catch (const Error&) {
+      }
+    }
+    return plans.emplace(key, std::move(pl)).first->second.get();
   };
+  // a candidate launch: one persistent kernel over the canvases order[begin, end)
+  struct Launch {
+    int begin = 0, end = 0, nt = 1024, cl = 1, slots = 0;
+    size_t dyn = 0;
+    int fmax_cm = 0;  // largest footprint whose cell maps live in global memory
+    double span = 1e300;
+  };
+  auto evaluate = [&](int begin, int end, int nt, int cl, int max_slots) {
+    Launch L;
+    L.begin = begin;
+    L.end = end;
+    L.nt = nt;
+    L.cl = cl;
+    std::vector<char> seen(shapes.size(), 0);
+    for (int k = begin; k < end; k++)
+      for (int32_t sid : canvas_shapes[order[k]]) {
+        if (seen[sid]) continue;
+        seen[sid] = 1;
+        const SmemPlan* pl = shape_plan(sid, nt, cl);
+        if (!pl) return Launch{};
+        L.dyn = std::max(L.dyn, pl->layout.total);
+        if (pl->cm_global) L.fmax_cm = std::max(L.fmax_cm, std::get<0>(shapes[sid]));
+      }
+    // in whole KB (fewer distinct occupancy queries), within the budget the plans respect
+    const size_t limit = nt == 512 ? limit512 : limit1k;
+    L.dyn = std::min((std::max<size_t>(L.dyn, 16) + 1023) / 1024 * 1024,
+                     std::max<size_t>(L.dyn, limit));
+    int fits = 0;
+    if (nt == 512) {
+      info512.allow_smem(kern512, L.dyn);
+      fits = info512.fits(kern512, cl, L.dyn);
+    } else {
+      info1k.allow_smem(kern1k, L.dyn);
+      fits = info1k.fits(kern1k, cl, L.dyn);
+    }
+    L.slots = std::min({fits, max_slots, end - begin});
+    if (L.slots < 1) return Launch{};
+    const std::vector<int32_t> sub(order.begin() + begin, order.begin() + end);
+    L.span = batch_makespan(loadN, loadP, sub, L.slots, cl, nt);
+    return L;
+  };
+  // thread count and cluster size: autotuned by the cost model unless PAINTY_BATCH_THREADS /
+  // PAINTY_BATCH_CLUSTER (or the caller's options) set them
   const int forced = env_cluster("PAINTY_BATCH_CLUSTER");
-  int cl = 1, slots = 0;
-  double best = 1e300;
-  int last_planned = 0;
-  for (int c2 : {1, 2, 4, 8}) {
-    if (forced ? c2 != forced : c2 > opt.max_cluster) continue;
-    plan_all(c2);
-    last_planned = c2;
-    const int fits = info.fits(kern, c2, std::max<size_t>(dyn, 16));
-    const int sl = std::min(fits, nc);
-    const double span = batch_makespan(loadN, loadP, order, sl, c2);
-    if (sl >= 1 && span < best) {
-      best = span;
-      cl = c2;
-      slots = sl;
+  const int want_nt = env_threads("PAINTY_BATCH_THREADS") ? env_threads("PAINTY_BATCH_THREADS")
+                                                          : opt.threads;
+  auto best_launch = [&](int begin, int end, int max_slots_1k, int max_slots_512) {
+    Launch best;
+    // a requested thread count first; any other only when no launch of it fits
+    for (int pass = 0; pass < 2 && best.slots < 1; pass++)
+      for (int n2 : {1024, 512}) {
+        if (pass == 0 && want_nt && n2 != want_nt) continue;
+        for (int c2 : {1, 2, 4, 8}) {
+          if (forced ? c2 != forced : c2 > opt.max_cluster) continue;
+          const int ms = n2 == 512 ? max_slots_512 : max_slots_1k;
+          const Launch L = evaluate(begin, end, n2, c2, ms == INT_MAX ? ms : ms / c2);
+          if (L.slots >= 1 && L.span < best.span) best = L;
+        }
+      }
+    return best;
+  };
+  const Launch single = best_launch(0, nc, INT_MAX, INT_MAX);
+  PG_REQUIRE(single.slots >= 1, "no stamp cluster fits on the device");
+  // the heaviest canvases on large clusters (a launch of their own, next to the rest): a
+  // canvas's stamps run in order, so the heaviest canvas bounds the batch unless more CTAs
+  // share its stamps
+  Launch heavy, rest;
+  // PAINTY_BATCH_SPLIT="<cluster>:<canvases>" forces the split (tests)
+  int force_ch = 0, force_h = 0;
+  if (const char* v = std::getenv("PAINTY_BATCH_SPLIT")) {
+    if (std::sscanf(v, "%d:%d", &force_ch, &force_h) != 2 ||
+        !(force_ch == 2 || force_ch == 4 || force_ch == 8) || force_h < 1 || force_h >= nc)
+      force_ch = force_h = 0;
+  }
+  if (opt.done_host) force_ch = 0;  // one launch signals completion: no split
+  if (force_ch) {
+    heavy = evaluate(0, force_h, 1024, force_ch, force_h);
+    int dev = 0, sms = 0;
+    PG_CUDA(cudaGetDevice(&dev));
+    PG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int left = std::max(1, sms - force_h * force_ch);
+    rest = best_launch(force_h, nc, left, 2 * left);
+    PG_REQUIRE(heavy.slots == force_h && rest.slots >= 1, "PAINTY_BATCH_SPLIT does not fit");
+  } else if (!forced && !want_nt && !opt.done_host && nc >= 2 && opt.max_cluster >= 4) {
+    int dev = 0, sms = 0;
+    PG_CUDA(cudaGetDevice(&dev));
+    PG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    double best = single.span * 0.97;  // a split must clearly pay for its second launch
+    for (int ch : {8, 4}) {
+      if (ch > opt.max_cluster) continue;
+      for (int h = 1; h < nc && 2 * h * ch <= sms; h++) {
+        const Launch A = evaluate(0, h, 1024, ch, h);
+        if (A.slots < h || A.span >= best) break;
+        const int left = sms - h * ch;  // SMs the heavy launch leaves (one 1024-thread CTA each)
+        const Launch B = best_launch(h, nc, left, 2 * left);
+        if (B.slots < 1) continue;
+        const double span = std::max(A.span, B.span);
+        if (span < best) {
+          best = span;
+          heavy = A;
+          rest = B;
+        }
+      }
     }
   }
-  PG_REQUIRE(slots >= 1, "no stamp cluster fits on the device");
-  g_last_batch_shape[0] = cl;
-  g_last_batch_shape[1] = slots;
-  if (cl != last_planned) plan_all(cl);
-  const int grid = slots * cl;
-  // the descriptors in one device buffer (one allocation, one copy) and the scratch in
-  // another, both stream-ordered and freed after the launch; pieces 256-byte aligned
+  const bool split = heavy.slots >= 1;
+  const Launch& main_l = split ? rest : single;
+  g_last_batch_shape[0] = main_l.cl;
+  g_last_batch_shape[1] = main_l.slots;
+  g_last_batch_shape[2] = main_l.nt;
+  g_last_batch_shape[3] = split ? heavy.cl : 0;
+  g_last_batch_shape[4] = split ? heavy.slots : 0;
+  // the strokes' plans for the launch that paints their canvas
+  auto apply = [&](const Launch& L) {
+    for (int k = L.begin; k < L.end; k++) {
+      const int32_t c = order[k];
+      for (size_t j = 0; j < per[c].size(); j++) {
+        const size_t i = static_cast<size_t>(first[c]) + j;
+        const SmemPlan* pl = shape_plan(shape_of[i], L.nt, L.cl);
+        bs[i].ndisc = pl->ndisc;
+        bs[i].plan = (pl->pick ? 1 : 0) | (pl->big ? 2 : 0) | (pl->cm_global ? 4 : 0);
+      }
+    }
+  };
+  if (split) {
+    apply(heavy);
+    apply(rest);
+  } else {
+    apply(single);
+  }
+  // the descriptors in one device buffer (one allocation, one copy) and the scratch of each
+  // launch in another, all stream-ordered and freed after the launches; pieces 256-byte aligned
   std::vector<unsigned char> hdesc;
   auto piece = [&](const void* h, size_t bytes) -> size_t {
     const size_t off = align_up(hdesc.size(), 256);
@@ -2091,57 +2308,102 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   }
   PG_CUDA(cudaMemcpyAsync(d_desc, hsrc, hdesc.size(), cudaMemcpyHostToDevice, st));
   auto at = [&](size_t off) { return static_cast<void*>(static_cast<char*>(d_desc) + off); };
-  void* d_canvas = at(o_canvas);
-  void* d_strokes = at(o_strokes);
-  void* d_points = at(o_points);
-  void* d_order = at(o_order);
   const int64_t pstride = static_cast<int64_t>(8) * smax * smax;
   const int64_t ostride = static_cast<int64_t>(smax) * smax;
-  const int64_t cmstride = static_cast<int64_t>(cl) * 2 * fmax_cm * fmax_cm;
-  // counter, status words 1..7 (bounds-check records at status + 4, + 5), claims; then the
-  // per-cluster pickup maps, owner tables and cell maps
-  const size_t s_counter = 0;
-  const size_t s_pick = align_up(sizeof(int) * (8 + slots), 256);
-  const size_t s_own = align_up(s_pick + slots * pstride * msz, 256);
-  const size_t s_cm = align_up(s_own + slots * ostride * sizeof(int), 256);
-  const size_t s_end = align_up(s_cm + std::max<int64_t>(slots * cmstride, 4) * sizeof(int), 256);
-  void* d_scratch = nullptr;
-  const bool own_scratch = !(opt.device_scratch && s_end <= opt.device_scratch_bytes);
-  d_scratch = own_scratch ? temp_alloc(s_end, st) : opt.device_scratch;
-  if (opt.scratch_needed) *opt.scratch_needed = s_end;
-  PG_CUDA(cudaMemsetAsync(d_scratch, 0, sizeof(int) * (8 + slots), st));
-  auto sat = [&](size_t off) { return static_cast<void*>(static_cast<char*>(d_scratch) + off); };
-  void* d_counter = sat(s_counter);
-  void* d_scratch_p = sat(s_pick);
-  void* d_scratch_o = sat(s_own);
-  void* d_scratch_cm = sat(s_cm);
-  BatchArgs<TK, TV> a{};
-  a.canvases = static_cast<const BatchCanvas<TK, TV>*>(d_canvas);
-  a.strokes = static_cast<const BatchStroke*>(d_strokes);
-  a.points = static_cast<const double*>(d_points);
-  a.order = static_cast<const int32_t*>(d_order);
-  a.ncanvas = nc;
-  a.counter = static_cast<int*>(d_counter);
-  a.status = reinterpret_cast<unsigned*>(static_cast<int*>(d_counter) + 1);
-  a.claims = static_cast<int*>(d_counter) + 8;
-  a.scratch_pickup = static_cast<M*>(d_scratch_p);
-  a.scratch_owner = static_cast<int*>(d_scratch_o);
-  a.scratch_cellmap = static_cast<int*>(d_scratch_cm);
-  a.cellmap_stride = cmstride;
-  a.pickup_stride = pstride;
-  a.owner_stride = ostride;
-  a.nstrokes = static_cast<int64_t>(bs.size());
-  a.npoints = npoints;
-  a.nslots = slots;
-  launch_clustered(kern, grid, cl, std::max<size_t>(dyn, 16), st, a);
-  count_launch();
-  PG_CUDA(cudaGetLastError());
+  // a launch's scratch: counter, status words 1..7 (bounds-check records at status + 4, + 5),
+  // claims; then the per-cluster pickup maps, owner tables and cell maps
+  struct ScratchLayout {
+    size_t pick, own, cm, end;
+    int64_t cmstride;
+  };
+  auto layout_of = [&](const Launch& L) {
+    ScratchLayout S{};
+    S.cmstride = static_cast<int64_t>(L.cl) * 2 * L.fmax_cm * L.fmax_cm;
+    S.pick = align_up(sizeof(int) * (8 + L.slots), 256);
+    S.own = align_up(S.pick + L.slots * pstride * msz, 256);
+    S.cm = align_up(S.own + L.slots * ostride * sizeof(int), 256);
+    S.end = align_up(S.cm + std::max<int64_t>(L.slots * S.cmstride, 4) * sizeof(int), 256);
+    return S;
+  };
+  const Launch& first_l = split ? heavy : single;
+  const ScratchLayout S1 = layout_of(first_l);
+  const bool own_scratch = !(opt.device_scratch && S1.end <= opt.device_scratch_bytes);
+  void* d_scratch = own_scratch ? temp_alloc(S1.end, st) : opt.device_scratch;
+  if (opt.scratch_needed) *opt.scratch_needed = S1.end;
+  PG_CUDA(cudaMemsetAsync(d_scratch, 0, sizeof(int) * (8 + first_l.slots), st));
+  unsigned* d_status = reinterpret_cast<unsigned*>(static_cast<int*>(d_scratch) + 1);
+  ScratchLayout S2{};
+  void* d_scratch2 = nullptr;
+  if (split) {
+    S2 = layout_of(rest);
+    d_scratch2 = temp_alloc(S2.end, st);
+    PG_CUDA(cudaMemsetAsync(d_scratch2, 0, sizeof(int) * (8 + rest.slots), st));
+  }
+  auto args_for = [&](const Launch& L, void* scratch, const ScratchLayout& SL) {
+    auto sat = [&](size_t off) { return static_cast<void*>(static_cast<char*>(scratch) + off); };
+    BatchArgs<TK, TV> a{};
+    a.canvases = static_cast<const BatchCanvas<TK, TV>*>(at(o_canvas));
+    a.strokes = static_cast<const BatchStroke*>(at(o_strokes));
+    a.points = static_cast<const double*>(at(o_points));
+    a.order = static_cast<const int32_t*>(at(o_order)) + L.begin;
+    a.norder = L.end - L.begin;
+    a.ncanvas = nc;
+    a.counter = static_cast<int*>(scratch);
+    a.status = d_status;  // one status word for every launch of the batch
+    a.claims = static_cast<int*>(scratch) + 8;
+    a.scratch_pickup = static_cast<M*>(sat(SL.pick));
+    a.scratch_owner = static_cast<int*>(sat(SL.own));
+    a.scratch_cellmap = static_cast<int*>(sat(SL.cm));
+    a.cellmap_stride = SL.cmstride;
+    a.pickup_stride = pstride;
+    a.owner_stride = ostride;
+    a.nstrokes = static_cast<int64_t>(bs.size());
+    a.npoints = npoints;
+    a.nslots = L.slots;
+    return a;
+  };
+  auto launch = [&](const Launch& L, const BatchArgs<TK, TV>& a, cudaStream_t s) {
+    if (L.nt == 512)
+      launch_clustered(kern512, L.slots * L.cl, L.cl, std::max<size_t>(L.dyn, 16), s, a, 512);
+    else
+      launch_clustered(kern1k, L.slots * L.cl, L.cl, std::max<size_t>(L.dyn, 16), s, a, 1024);
+    count_launch();
+    PG_CUDA(cudaGetLastError());
+  };
+  // a lone launch stores its final status into the caller's pinned memory itself: a copy
+  // queued behind the kernel would hold back other streams' work
+  unsigned* mapped_status =
+    opt.status_host && !split
+      ? static_cast<unsigned*>(const_cast<void*>(mapped_host(opt.status_host)))
+      : nullptr;
+  const bool status_in_kernel = mapped_status != nullptr;
+  if (split) {  // the rest on a side stream forked from and joined back into `st`
+    SideStream& side = side_stream();
+    PG_CUDA(cudaEventRecord(side.fork, st));
+    PG_CUDA(cudaStreamWaitEvent(side.st, side.fork, 0));
+    launch(heavy, args_for(heavy, d_scratch, S1), st);
+    launch(rest, args_for(rest, d_scratch2, S2), side.st);
+    PG_CUDA(cudaEventRecord(side.join, side.st));
+    PG_CUDA(cudaStreamWaitEvent(st, side.join, 0));
+  } else {
+    BatchArgs<TK, TV> a = args_for(single, d_scratch, S1);
+    a.status_host = mapped_status;
+    if (opt.done_host) {
+      a.done_host = static_cast<unsigned*>(const_cast<void*>(mapped_host(opt.done_host)));
+      PG_REQUIRE(a.done_host != nullptr, "the completion word must be pinned host memory");
+      a.done_value = opt.done_value;
+    }
+    launch(single, a, st);
+  }
   unsigned status[6] = {};
-  PG_CUDA(cudaMemcpyAsync(opt.status_host ? opt.status_host : status, a.status,
-                          opt.status_host ? sizeof(unsigned) : sizeof(status),
-                          cudaMemcpyDeviceToHost, st));
+  if (!status_in_kernel) {
+    PG_CUDA(cudaMemcpyAsync(opt.status_host ? opt.status_host : status, d_status,
+                            opt.status_host ? sizeof(unsigned) : sizeof(status),
+                            cudaMemcpyDeviceToHost, st));
+  }
   if (own_desc) PG_CUDA(cudaFreeAsync(d_desc, st));
   if (own_scratch) PG_CUDA(cudaFreeAsync(d_scratch, st));
+  if (d_scratch2) PG_CUDA(cudaFreeAsync(d_scratch2, st));
   if (!opt.status_host) PG_CUDA(cudaStreamSynchronize(st));
   for (int32_t c = 0; c < nc; c++) {
     if (per[c].empty()) continue;
@@ -2636,10 +2898,18 @@ painty_status painty_stamps_f32_noalloc(const painty_stamp_buffers_f32* b, void*
 
 int32_t painty_build_flags(void) { return pg::kBoundsCheck ? PAINTY_BUILD_BOUNDS_CHECK : 0; }
 
-painty_status painty_batch_last_shape(int32_t* cluster, int32_t* clusters) {
+painty_status painty_batch_last_split(int32_t* cluster, int32_t* canvases) {
+  return guard([&] {
+    if (cluster) *cluster = pg::g_last_batch_shape[3];
+    if (canvases) *canvases = pg::g_last_batch_shape[4];
+  });
+}
+
+painty_status painty_batch_last_shape(int32_t* cluster, int32_t* clusters, int32_t* threads) {
   return guard([&] {
     if (cluster) *cluster = pg::g_last_batch_shape[0];
     if (clusters) *clusters = pg::g_last_batch_shape[1];
+    if (threads) *threads = pg::g_last_batch_shape[2];
   });
 }
 

@@ -25,7 +25,7 @@ def test_library_exports_all_declared(pg):
 
 
 def test_abi_version_and_status_strings(pg):
-    assert pg.ABI_VERSION == 1
+    assert pg.ABI_VERSION == 2
     lib = pg._lib
     for s in range(0, 9):
         assert lib.painty_status_string(s)

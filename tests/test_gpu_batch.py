@@ -126,6 +126,73 @@ def test_batch_forced_cluster_large_radii_f64(pg, oracle, monkeypatch, cluster):
             assert np.array_equal(cs[ci].download(p), oc.get(p)), (ci, p)
 
 
+# 512-thread CTAs (two per SM): radii up to 20 with and without the snapshot, and 35-50
+# (footprint sides up to 143, global cell maps), alone and as 2-CTA clusters
+@pytest.mark.parametrize("snap,rmin,rmax,cluster", [(True, 1.5, 20.0, "1"), (False, 1.5, 20.0, "1"),
+                                                    (True, 35.0, 50.0, "1"), (True, 1.5, 20.0, "2")])
+def test_batch_512_threads_f64(pg, oracle, monkeypatch, snap, rmin, rmax, cluster):
+    monkeypatch.setenv("PAINTY_BATCH_THREADS", "512")
+    monkeypatch.setenv("PAINTY_BATCH_CLUSTER", cluster)
+    rng = np.random.default_rng(31 + snap)
+    sizes = _canvases(rng, 5, smin=90, smax=200)
+    strokes = _session(rng, sizes, strokes_per=(2, 5), rmin=rmin, rmax=rmax)
+    cs, bs, r0s = _setup(pg, sizes, "f64", snap=snap)
+    pg.paint_batch(cs, bs, strokes)
+    assert pg.batch_last_shape()[0] == int(cluster) and pg.batch_last_shape()[2] == 512
+    fp = workloads.footprint_image(seed=7)
+    for ci, (rows, cols) in enumerate(sizes):
+        oc = oracle.canvas(rows, cols)
+        oc.set("R0", r0s[ci])
+        ob = oracle.brush(3.0, fp)
+        ob.set_rates(0.05, 0.1)
+        ob.set_snapshot(snap)
+        for cj, path, r, spacing, K, S in strokes:
+            if cj == ci:
+                ob.set_radius(r)
+                ob.dip(K, S)
+                ob.paint_stroke(oc, path, spacing)
+        for p in ("K", "S", "V"):
+            assert np.array_equal(cs[ci].download(p), oc.get(p)), (ci, p)
+
+
+@pytest.mark.parametrize("split", ["8:1", "4:2", "2:1"])
+def test_batch_split_launch_f64(pg, oracle, monkeypatch, split):
+    """The heaviest canvases on a launch of their own (clusters of 8, 4 or 2), the rest next to
+    it on a side stream: F64 bit-exact against the oracle, and reported."""
+    monkeypatch.setenv("PAINTY_BATCH_SPLIT", split)
+    rng = np.random.default_rng(51)
+    sizes = _canvases(rng, 6, smin=80, smax=180)
+    strokes = _session(rng, sizes, strokes_per=(2, 5), rmin=2.0, rmax=18.0)
+    cs, bs, r0s = _setup(pg, sizes, "f64")
+    pg.paint_batch(cs, bs, strokes)
+    ch, h = (int(x) for x in split.split(":"))
+    assert pg.batch_last_split() == (ch, h)
+    fp = workloads.footprint_image(seed=7)
+    for ci, (rows, cols) in enumerate(sizes):
+        oc = oracle.canvas(rows, cols)
+        oc.set("R0", r0s[ci])
+        ob = oracle.brush(3.0, fp)
+        ob.set_rates(0.05, 0.1)
+        for cj, path, r, spacing, K, S in strokes:
+            if cj == ci:
+                ob.set_radius(r)
+                ob.dip(K, S)
+                ob.paint_stroke(oc, path, spacing)
+        for p in ("K", "S", "V"):
+            assert np.array_equal(cs[ci].download(p), oc.get(p)), (ci, p)
+
+
+def test_batch_512_threads_falls_back_for_large_boxes(pg, monkeypatch):
+    """Boxes wider than 512-thread CTAs cover (radius 70: side 199) run on 1024 threads."""
+    monkeypatch.setenv("PAINTY_BATCH_THREADS", "512")
+    rng = np.random.default_rng(41)
+    sizes = _canvases(rng, 2, smin=150, smax=200)
+    strokes = _session(rng, sizes, strokes_per=(1, 2), rmin=70.0, rmax=70.0)
+    cs, bs, _ = _setup(pg, sizes, "f32")
+    pg.paint_batch(cs, bs, strokes)
+    assert pg.batch_last_shape()[2] == 1024
+
+
 def test_batch_f32_close_to_sequential(pg):
     rng = np.random.default_rng(5)
     sizes = _canvases(rng, 12, 64, 300)

@@ -63,6 +63,7 @@ HALF_F32_MATH_ABS_TOL = 2e-5
 @pytest.mark.parametrize("rows,cols,L", [(48, 160, 8), (1100, 1100, 8), (300, 517, 18)])
 def test_half_storage_fp32_math(pg, oracle, storage, rows, cols, L):
     K, S, V, R0 = workloads.composite_stack(rows, cols, layers=L, seed=rows + L, dtype=np.float64)
+    V[:, :, :16] = 0.0  # pixels no layer covers: exactly R0
     layers = []
     Ks, Ss, Vs = np.empty_like(K), np.empty_like(S), np.empty_like(V)
     for l in range(L):
@@ -82,6 +83,7 @@ def test_half_storage_fp32_math(pg, oracle, storage, rows, cols, L):
     want = oracle_compose(oracle, Ks, Ss, Vs, R0s, mode=0)
     err = np.abs(got - want).max()
     assert err <= HALF_F32_MATH_ABS_TOL, err
+    assert np.array_equal(got[:, :, :16], R0s[:, :, :16])
     assert pg.take_device_faults() == 0
 
 
