@@ -238,7 +238,12 @@ def run_stamps_only(args):
     import painty_gb300 as pg
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    print(json.dumps(run_stamps_config0(pg, torch, args.strokes)), flush=True)
+    out = run_stamps_config0(pg, torch, args.strokes)
+    if pg.PHASE_TIMERS:  # PAINTY_PHASE_TIMERS=1: where a stamp's cycles go, per warp
+        out["phases"] = pg.take_phase_cycles()
+        out["phases"]["note"] = ("phase-timing build: clock cycles per stamp per warp, averaged "
+                                 "over warps and over the timed and untimed steps")
+    print(json.dumps(out), flush=True)
 
 
 def _event_ms(torch, fn, reps: int, warm: int = 3) -> float:
@@ -947,7 +952,7 @@ def run_serve(pg, torch, rate: float, seconds: float, seed: int = 4, budget_gb: 
     return out
 
 
-def run_serving(pg, torch, rates=(20.0, 50.0, 100.0), sweep_s: float = 10.0,
+def run_serving(pg, torch, rates=(20.0, 50.0, 100.0, 150.0), sweep_s: float = 10.0,
                 full_rate: float = 200.0, full_s: float = 60.0):
     """The stated serving run (full_rate req/s for full_s) and a sweep of lower rates over
     shorter windows; reports the highest sustained rate."""

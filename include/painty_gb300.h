@@ -83,7 +83,18 @@ int32_t painty_abi_version(void);
  * index against its buffer and return PAINTY_ERR_CUDA naming the access instead of faulting.
  * No counterpart in painty. */
 #define PAINTY_BUILD_BOUNDS_CHECK 1
+/* PAINTY_BUILD_PHASE_TIMERS is set in the phase-timing build (libpainty_gb300_phases.so), whose
+ * stamp loop adds each warp's clock cycles per phase into device counters read with
+ * painty_take_phase_cycles. */
+#define PAINTY_BUILD_PHASE_TIMERS 2
 int32_t painty_build_flags(void);
+/* Phase-timing build only: reads and clears the stamp loop's counters (synchronises the
+ * device). out[0..7]: warp cycles summed over warps and stamps in painting, the snapshot ring
+ * refresh, classification, parameter derivation, per-stamp setup, the CTA barrier, the
+ * cluster barrier, and edge-duplicate (wave) painting with its refresh; out[8]: stamps summed
+ * over CTAs; out[9]: warp-stamps (stamps times warps per CTA, summed over CTAs); out[10..15]:
+ * 0. PAINTY_ERR_UNSUPPORTED in other builds. No counterpart in painty. */
+painty_status painty_take_phase_cycles(uint64_t out[16]);
 const char* painty_status_string(painty_status s);
 const char* painty_last_error(void);
 /* Number of this library's kernel launches so far in this process (all devices). */

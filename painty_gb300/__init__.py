@@ -27,7 +27,11 @@ _HERE = Path(__file__).resolve().parent
 # PAINTY_BOUNDS_CHECK=1 loads the bounds-checked build of the library (the stamp kernels test
 # every computed index before the access and raise instead of faulting)
 BOUNDS_CHECKED = os.environ.get("PAINTY_BOUNDS_CHECK", "") not in ("", "0")
+# PAINTY_PHASE_TIMERS=1 loads the phase-timing build (per-phase clock counters of the stamp
+# loop, read with take_phase_cycles)
+PHASE_TIMERS = os.environ.get("PAINTY_PHASE_TIMERS", "") not in ("", "0")
 LIB_PATH = _HERE / "_lib" / ("libpainty_gb300_checked.so" if BOUNDS_CHECKED
+                             else "libpainty_gb300_phases.so" if PHASE_TIMERS
                              else "libpainty_gb300.so")
 
 if not LIB_PATH.exists():
@@ -57,6 +61,7 @@ _sig("painty_status_string", C.c_int, res=C.c_char_p)
 _sig("painty_last_error", res=C.c_char_p)
 _sig("painty_kernel_launch_count", res=_I64)
 _sig("painty_take_device_faults", C.POINTER(C.c_uint32))
+_sig("painty_take_phase_cycles", C.POINTER(C.c_uint64))
 _sig("painty_layer_create", _I32, _I32, C.c_int, C.POINTER(_P))
 _sig("painty_layer_destroy", _P)
 _sig("painty_layer_clear", _P, _P)
@@ -162,6 +167,20 @@ def bounds_checked() -> bool:
 def kernel_launch_count() -> int:
     """Kernel launches this library has issued in this process."""
     return int(_lib.painty_kernel_launch_count())
+
+
+PHASES = ("paint", "refresh", "classify", "derive", "setup", "cta_barrier", "cluster_barrier",
+          "waves")
+
+
+def take_phase_cycles() -> dict:
+    """Phase-timing build: reads and clears the stamp loop's counters. Returns the stamps
+    (summed over CTAs) and, per phase, the clock cycles a warp spent in it per stamp."""
+    v = (C.c_uint64 * 16)()
+    _check(_lib.painty_take_phase_cycles(v))
+    ws = max(int(v[9]), 1)  # warp-stamps: lane 0 of each warp records its warp
+    return {"stamps": int(v[8]),
+            "cycles_per_stamp": {p: round(v[i] / ws, 1) for i, p in enumerate(PHASES)}}
 
 
 def take_device_faults() -> int:

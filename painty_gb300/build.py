@@ -25,6 +25,9 @@ LIB = OUT_DIR / "libpainty_gb300.so"
 # every computed index against its buffer before the access and report instead of faulting.
 LIB_CHECKED = OUT_DIR / "libpainty_gb300_checked.so"
 CHECKED_SOURCES = {"stamp.cu"}
+# The phase-timing build (PAINTY_PHASE_TIMERS): the stamp loop adds each warp's clock cycles per
+# phase into device counters (painty_take_phase_cycles), for profiling.
+LIB_PHASES = OUT_DIR / "libpainty_gb300_phases.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -73,10 +76,11 @@ def _link(objs, lib: Path) -> None:
 
 
 def build(verbose: bool = False, checked: bool = True) -> Path:
-    """Builds the library and, with `checked`, its bounds-checked twin (the translation units
-    in CHECKED_SOURCES compiled again with PAINTY_BOUNDS_CHECK, the rest shared)."""
+    """Builds the library and, with `checked`, its bounds-checked and phase-timing twins (the
+    translation units in CHECKED_SOURCES compiled again with PAINTY_BOUNDS_CHECK or
+    PAINTY_PHASE_TIMERS, the rest shared)."""
     OUT_DIR.mkdir(exist_ok=True)
-    objs, checked_objs, jobs = [], [], []
+    objs, checked_objs, phase_objs, jobs = [], [], [], []
     srcs = sources()
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(srcs) + 1, os.cpu_count() or 4))) as ex:
         for src in srcs:
@@ -87,17 +91,22 @@ def build(verbose: bool = False, checked: bool = True) -> Path:
                 cobj = OUT_DIR / (src.stem + "_checked.o")
                 checked_objs.append(cobj)
                 jobs.append(ex.submit(_compile, src, cobj, ("PAINTY_BOUNDS_CHECK=1",)))
+                pobj = OUT_DIR / (src.stem + "_phases.o")
+                phase_objs.append(pobj)
+                jobs.append(ex.submit(_compile, src, pobj, ("PAINTY_PHASE_TIMERS=1",)))
             else:
                 checked_objs.append(obj)
+                phase_objs.append(obj)
         for j in jobs:
             j.result()
     _link(objs, LIB)
     if checked:
         _link(checked_objs, LIB_CHECKED)
-    for o in set(objs) | set(checked_objs):
+        _link(phase_objs, LIB_PHASES)
+    for o in set(objs) | set(checked_objs) | set(phase_objs):
         o.unlink(missing_ok=True)
     if verbose:
-        print(f"built {LIB}" + (f" and {LIB_CHECKED}" if checked else ""))
+        print(f"built {LIB}" + (f", {LIB_CHECKED} and {LIB_PHASES}" if checked else ""))
     return LIB
 
 

@@ -59,6 +59,14 @@ struct StampRec {
   double cx, cy, c, s;  // centre, cos(-theta), sin(-theta)
 };
 
+#ifdef PAINTY_PHASE_TIMERS
+constexpr bool kPhaseTimers = true;
+#else
+constexpr bool kPhaseTimers = false;
+#endif
+// per phase of the stamp loop: warp cycles summed over warps and stamps (phase-timing build)
+__device__ unsigned long long g_phase_cycles[16];
+
 namespace {
 
 constexpr int kStampThreads = 1024;
@@ -677,19 +685,47 @@ struct RecordSource {
 //
 // Pass 1: cell of every support-disc pixel (packed my << 16 | mx; -1 when the pixel changes
 // nothing: outside the canvas or the map, or a zero footprint).
+//
+// In a cluster each CTA classifies its own share of the disc [first, last) and stores each
+// entry into every CTA's map: `peers` holds the other CTAs' maps for this stamp (shared::cluster
+// addresses of maps in shared memory, or global pointers), `npeers` of them. The cluster
+// barrier that ends the phase makes the stores visible; the maps written here were last read
+// in the phase before it.
+struct PeerMaps {
+  unsigned smem[16];  // shared::cluster addresses (maps in shared memory)
+  int* glob[16];      // global maps
+};
+__device__ __forceinline__ unsigned dsmem_map_u32(unsigned local, unsigned rank) {
+  unsigned r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(local), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void dsmem_st(unsigned addr, int v) {
+  asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
+}
 template <class TK, class TV, class M>
 __device__ __forceinline__ void classify_disc(const StampArgs<TK, TV>& a, const StampParams& sp,
                                               const int* xs, const int* ys, const M* fps,
-                                              const uint32_t* disc, int ndisc, int* cellmap,
-                                              int rt, int T) {
+                                              const uint32_t* disc, int first, int last,
+                                              int* cellmap, int rt, int T,
+                                              const PeerMaps* peers, int npeers, bool peer_smem) {
   const int F = a.F;
-  for (int i = rt; i < ndisc; i += T) {  // rt: counted from the last thread (high warps)
+  for (int i = first + rt; i < last; i += T) {  // rt: counted from the last thread (high warps)
     const uint32_t e = disc[i];
     const int row = static_cast<int>(e >> 16), col = static_cast<int>(e & 0xffffu);
     M fp;
     const PixelInfo p = pixel_info(a, sp, xs, ys, fps, row, col, &fp);
-    if (in_bounds(a.status, kBoundsCellMap, row * F + col, static_cast<int64_t>(F) * F))
-      cellmap[row * F + col] = p.live ? ((p.my << 16) | p.mx) : -1;
+    if (in_bounds(a.status, kBoundsCellMap, row * F + col, static_cast<int64_t>(F) * F)) {
+      const int v = p.live ? ((p.my << 16) | p.mx) : -1;
+      const int idx = row * F + col;
+      cellmap[idx] = v;
+      for (int q = 0; q < npeers; q++) {
+        if (peer_smem)
+          dsmem_st(peers->smem[q] + 4u * static_cast<unsigned>(idx), v);
+        else
+          peers->glob[q][idx] = v;
+      }
+    }
   }
 }
 
@@ -920,6 +956,11 @@ __device__ __forceinline__ void run_stroke(const StampArgs<TK, TV>& a, const Src
   auto dc_at = [&](int slot) { return dc_b + slot * F; };
   auto dr_at = [&](int slot) { return dr_b + slot * F; };
   auto cm_of = [&](int k) { return cm_b + (k & 1) * npix; };
+  // classification in a cluster: each CTA its share of the disc, stored into every CTA's map
+  __shared__ PeerMaps peer_maps[2];
+  const int npeers = csize > 1 ? csize - 1 : 0;
+  const bool peer_smem = a.cellmap_global == nullptr;
+  const int cfirst = csize > 1 ? dfirst : 0, clast = csize > 1 ? dlast : ndisc;
   auto rl_of = [&](int k) { return &sh->rl[k & 1]; };
   auto next_slot = [](int slot) { return slot == kStampBufs - 1 ? 0 : slot + 1; };
   // rectangles of stamp k - 1 (the brush's ring state before the first stamp)
@@ -964,6 +1005,17 @@ __device__ __forceinline__ void run_stroke(const StampArgs<TK, TV>& a, const Src
   }
   if (!BIG || crank == 0)
     for (int i = tid; i < cells; i += T) own[i] = INT_MAX;
+  if (tid < 2 * npeers) {  // the other CTAs' maps, per stamp parity
+    const int par_k = tid / npeers, q = tid - par_k * npeers;
+    const int rank = q < crank ? q : q + 1;
+    if (peer_smem) {
+      const unsigned local = static_cast<unsigned>(__cvta_generic_to_shared(cm_b + par_k * npix));
+      peer_maps[par_k].smem[q] = dsmem_map_u32(local, static_cast<unsigned>(rank));
+    } else {
+      peer_maps[par_k].glob[q] = a.cellmap_global + static_cast<int64_t>(rank) * 2 * npix +
+                                 static_cast<int64_t>(par_k) * npix;
+    }
+  }
   if (tid == 0) {  // the stamp before the first: from the brush's ring state or the reset mode
     const int big = 1 << 30;
     const int unknown[8] = {0, 0, -1, -1, 0, 0, -1, -1};
@@ -1019,10 +1071,21 @@ __device__ __forceinline__ void run_stroke(const StampArgs<TK, TV>& a, const Src
     if (a.use_snapshot)
       refresh_ring<CG, PK>(a, *rl_of(0), rt, T, crank, lg_csize, nullptr, 0, 0);
     if (!dup0 && ndisc > 0)
-      classify_disc(a, par(0), xs_at(0), ys_at(0), fps, disc, ndisc, cm_of(0), rt, T);
+      classify_disc(a, par(0), xs_at(0), ys_at(0), fps, disc, cfirst, clast, cm_of(0), rt, T,
+                    &peer_maps[0], npeers, peer_smem);
   }
   csync();
   int epoch = 0;
+  // phase timers (phase-timing build): each thread's clock between the loop's phase marks
+  unsigned long long acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  long long t_mark = kPhaseTimers ? clock64() : 0;
+  auto lap = [&](int i) {
+    if constexpr (kPhaseTimers) {
+      const long long t = clock64();
+      acc[i] += static_cast<unsigned long long>(t - t_mark);
+      t_mark = t;
+    }
+  };
   for (int k = 0; k < ns; k++) {
     const StampParams& sp = par(k);
     const bool has_next = k + 1 < ns;
@@ -1032,9 +1095,11 @@ __device__ __forceinline__ void run_stroke(const StampArgs<TK, TV>& a, const Src
       paint_disc<PS, CG, PK, TK, TV, M>(a, xs_at(s0), ys_at(s0), fps, pbase, disc, dfirst, dlast,
                                         cm_of(k), seed, tid, T,
                                         has_next ? &par(k + 1) : nullptr);
+      lap(0);
       if (has_next && a.use_snapshot)
         refresh_ring<CG, PK>(a, *rl_of(k + 1), rt, T, crank, lg_csize, cm_of(k), xs_at(s0)[0],
                              ys_at(s0)[0]);
+      lap(1);
     } else {
       if (crank == 0)  // edge duplicates: the first CTA alone, in waves
         epoch = paint_waves<PS, CG, PK, TK, TV, M>(a, sp, xs_at(s0), ys_at(s0), dc_at(s0),
@@ -1042,17 +1107,33 @@ __device__ __forceinline__ void run_stroke(const StampArgs<TK, TV>& a, const Src
       csync();
       if (has_next && a.use_snapshot)
         refresh_ring<CG, PK>(a, *rl_of(k + 1), rt, T, crank, lg_csize, nullptr, 0, 0);
+      lap(7);
     }
     if (has_next && !dup1 && ndisc > 0)
-      classify_disc(a, par(k + 1), xs_at(s1), ys_at(s1), fps, disc, ndisc, cm_of(k + 1), rt, T);
+      classify_disc(a, par(k + 1), xs_at(s1), ys_at(s1), fps, disc, cfirst, clast, cm_of(k + 1),
+                    rt, T, &peer_maps[(k + 1) & 1], npeers, peer_smem);
+    lap(2);
     if (((k + 3) & (kParamChunk - 1)) == 0) derive_chunk(k + 3);  // read from phase k + 1 on
+    lap(3);
     int nd = 0;
     if (k + 2 < ns) nd = setup(k + 2, s2);
+    lap(4);
     nd = __syncthreads_or(nd);
+    lap(5);
     if (csize > 1) cluster_barrier();  // this phase's writes before the next phase's reads
+    lap(6);
     dup0 = dup1;
     dup1 = nd;
     s0 = s1;
+  }
+  if constexpr (kPhaseTimers) {
+    if ((tid & 31) == 0) {  // lane 0 stands for its warp
+      for (int i = 0; i < 8; i++) atomicAdd(&g_phase_cycles[i], acc[i]);
+      if (tid == 0) {
+        atomicAdd(&g_phase_cycles[8], static_cast<unsigned long long>(ns));
+        atomicAdd(&g_phase_cycles[9], static_cast<unsigned long long>(ns) * (T >> 5));
+      }
+    }
   }
   // epilogue: the brush keeps its pickup map and the ring state
   if (tid == 0 && crank == 0 && a.stamp_count)
@@ -2896,7 +2977,23 @@ painty_status painty_stamps_f32_noalloc(const painty_stamp_buffers_f32* b, void*
   });
 }
 
-int32_t painty_build_flags(void) { return pg::kBoundsCheck ? PAINTY_BUILD_BOUNDS_CHECK : 0; }
+int32_t painty_build_flags(void) {
+  return (pg::kBoundsCheck ? PAINTY_BUILD_BOUNDS_CHECK : 0) |
+         (pg::kPhaseTimers ? PAINTY_BUILD_PHASE_TIMERS : 0);
+}
+
+painty_status painty_take_phase_cycles(uint64_t out[16]) {
+  return guard([&] {
+    PG_REQUIRE(out != nullptr, "out is null");
+    if (!pg::kPhaseTimers)
+      pg::fail(PAINTY_ERR_UNSUPPORTED, "not the phase-timing build (PAINTY_PHASE_TIMERS=1)");
+    unsigned long long v[16] = {}, zero[16] = {};
+    PG_CUDA(cudaDeviceSynchronize());
+    PG_CUDA(cudaMemcpyFromSymbol(v, pg::g_phase_cycles, sizeof(v)));
+    PG_CUDA(cudaMemcpyToSymbol(pg::g_phase_cycles, zero, sizeof(zero)));
+    for (int i = 0; i < 16; i++) out[i] = v[i];
+  });
+}
 
 painty_status painty_batch_last_split(int32_t* cluster, int32_t* canvases) {
   return guard([&] {

@@ -110,3 +110,17 @@ def test_bounds_checked_build_exports_and_reports_itself(pg):
     lib.painty_build_flags.restype = ctypes.c_int32
     assert lib.painty_build_flags() & 1
     assert pg.bounds_checked() == pg.BOUNDS_CHECKED
+
+
+def test_phase_timing_build_exports_and_reports_itself(pg):
+    """The phase-timing twin library loads without a GPU, exports every declared entry and
+    reports its build flag; in the default build the phase counters are unsupported."""
+    phases = pg.LIB_PATH.parent / "libpainty_gb300_phases.so"
+    lib = ctypes.CDLL(str(phases))
+    missing = [n for n in declared_symbols() if not hasattr(lib, n)]
+    assert not missing, missing
+    lib.painty_build_flags.restype = ctypes.c_int32
+    assert lib.painty_build_flags() & 2 and not lib.painty_build_flags() & 1
+    if not pg.PHASE_TIMERS:
+        out = (ctypes.c_uint64 * 16)()
+        assert pg._lib.painty_take_phase_cycles(out) == 4  # PAINTY_ERR_UNSUPPORTED

@@ -12,7 +12,7 @@ from test_gpu_stamps import _gpu_replay
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("cl", [2, 4])
+@pytest.mark.parametrize("cl", [2, 4, 8, 16])
 @pytest.mark.parametrize("name", ["snap_small", "nosnap_small", "snap_default_rates"])
 def test_single_canvas_cluster_bitexact_vs_reference(pg, golden, monkeypatch, cl, name):
     monkeypatch.setenv("PAINTY_STAMP_CLUSTER", str(cl))
@@ -23,12 +23,14 @@ def test_single_canvas_cluster_bitexact_vs_reference(pg, golden, monkeypatch, cl
         assert np.array_equal(b.getPickupMap(p), fx[f"{name}/pickup_{p}"]), "pickup " + p
 
 
-@pytest.mark.parametrize("storage", ["f32", "f16"])
-def test_single_canvas_cluster_sizes_agree(pg, monkeypatch, storage):
+# radii 10-40, and 50-64 (cell maps in global memory beside the support-disc list); every CTA
+# of a cluster classifies its share of the disc into every CTA's map
+@pytest.mark.parametrize("storage,rmin,rmax", [("f32", 10, 40), ("f16", 10, 40), ("f32", 50, 64)])
+def test_single_canvas_cluster_sizes_agree(pg, monkeypatch, storage, rmin, rmax):
     fp = workloads.footprint_image(seed=7)
-    strokes = workloads.strokes(300, 220, 6, seed=19, rmin=10, rmax=40)
+    strokes = workloads.strokes(300, 220, 6, seed=19, rmin=rmin, rmax=rmax)
     out = {}
-    for cl in (1, 2, 4):
+    for cl in (1, 2, 4, 8, 16):
         monkeypatch.setenv("PAINTY_STAMP_CLUSTER", str(cl))
         c = pg.Canvas(220, 300, storage)
         c.upload("R0", np.full((220, 300, 3), 0.85))
@@ -37,7 +39,7 @@ def test_single_canvas_cluster_sizes_agree(pg, monkeypatch, storage):
         b.setDepositionRate(0.1)
         workloads.paint_config0(c, b, strokes)
         out[cl] = [c.download(p) for p in ("K", "S", "V")]
-    for cl in (2, 4):
+    for cl in (2, 4, 8, 16):
         for a, b in zip(out[1], out[cl]):
             assert np.array_equal(a, b), cl
 
