@@ -9,6 +9,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "device_common.cuh"
@@ -733,10 +734,15 @@ struct Layer16 {  // one layer's 4 pixels: K r,g,b, S r,g,b, V as packed 16-bit 
 template <class T>
 __device__ __forceinline__ float elem16(const uint2& w, int i) {
   const uint32_t word = i < 2 ? w.x : w.y;
-  const unsigned short h = static_cast<unsigned short>((i & 1) ? word >> 16 : word & 0xffffu);
-  T t;
-  memcpy(&t, &h, 2);
-  return to_f(t);
+  if constexpr (std::is_same<T, __nv_bfloat16>::value) {
+    // BF16 is the top half of an FP32: place the half in the high bits (bit operations only)
+    return __uint_as_float((i & 1) ? (word & 0xffff0000u) : (word << 16));
+  } else {
+    const unsigned short h = static_cast<unsigned short>((i & 1) ? word >> 16 : word & 0xffffu);
+    T t;
+    memcpy(&t, &h, 2);
+    return to_f(t);
+  }
 }
 template <class TK, class TV>
 __device__ __forceinline__ void load_layer16(const Compose16Args<TK, TV>& a, int l, int64_t e,

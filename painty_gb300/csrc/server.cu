@@ -88,8 +88,13 @@ struct ServerRequest {
   painty_status status = PAINTY_OK;
   std::string error;
   int64_t stamps = 0;
+  int64_t total_stamps = 0;  // of all its strokes
   double t_submit = 0, t_done = 0;
+  int64_t remaining() const { return total_stamps - stamps; }
 };
+
+// A request with more stamps than this left is "long": its serial chain sets the tail latency.
+constexpr int64_t kLongRequest = 200000;
 
 // Pinned staging per slot for a launch's descriptors (a chunk of strokes: their descriptors
 // and path points); larger chunks are copied from pageable memory.
@@ -545,6 +550,10 @@ bool worker_round(painty_server* s, std::unique_lock<std::mutex>& lk) {
       ++it;  // its canvas is painting an earlier request
       continue;
     }
+    if (std::find(evictions.begin(), evictions.end(), c) != evictions.end()) {
+      ++it;  // chosen for eviction in this round: it is admitted (and restored) in a later one
+      continue;
+    }
     if (r->cancel) {
       finish(s, r, PAINTY_ERR_CANCELLED, "cancelled before it ran");
       it = s->pending.erase(it);
@@ -609,7 +618,10 @@ bool worker_round(painty_server* s, std::unique_lock<std::mutex>& lk) {
       if (r && !fresh) running.push_back({r, s->canvases[r->canvas_id].get(), r->cancel});
     }
   }
-  const int cap = cluster_cap(s);
+  int cap = cluster_cap(s);
+  // no queue: the GPU has room, so a long request's chain may take a large cluster (its
+  // latency, the server's p99, is that chain); under a backlog throughput comes first
+  const int long_cap = s->pending.empty() ? 8 : cap;
   s->tick++;
   lk.unlock();
 
@@ -649,7 +661,7 @@ bool worker_round(painty_server* s, std::unique_lock<std::mutex>& lk) {
         else
           mark_slot(s->slots[a.r->slot]);
       } else {
-        launch_chunk(s, a.r, a.c, cap);
+        launch_chunk(s, a.r, a.c, a.r->remaining() > kLongRequest ? long_cap : cap);
         chunks++;
       }
     } catch (const std::exception& e) {
@@ -671,7 +683,7 @@ bool worker_round(painty_server* s, std::unique_lock<std::mutex>& lk) {
       if (*s->slots[r->slot].status != 0)
         pg::fail(PAINTY_ERR_CUDA, "batched stamp kernel reported an internal error");
       if (r->next < r->strokes.size() && !x.cancel) {
-        launch_chunk(s, r, x.c, cap);
+        launch_chunk(s, r, x.c, r->remaining() > kLongRequest ? long_cap : cap);
         chunks++;
       } else if (r->out_rgb && !x.cancel) {
         r->phase = PH_FINISH;
@@ -818,6 +830,7 @@ painty_status painty_server_submit(painty_server* s, const painty_request* req,
       PG_REQUIRE(std::isfinite(d.spacing) && d.spacing > 0.0, "spacing must be positive");
       r->stroke_stamps.push_back(
         pg::stroke_stamp_count(r->points.data() + 2 * d.first_point, d.npoints, d.spacing));
+      r->total_stamps += r->stroke_stamps.back();
     }
     for (double v : r->points) PG_REQUIRE(std::isfinite(v), "path coordinates must be finite");
     r->out_rgb = req->out_rgb;

@@ -686,14 +686,13 @@ struct RecordSource {
 // Pass 1: cell of every support-disc pixel (packed my << 16 | mx; -1 when the pixel changes
 // nothing: outside the canvas or the map, or a zero footprint).
 //
-// In a cluster each CTA classifies its own share of the disc [first, last) and stores each
-// entry into every CTA's map: `peers` holds the other CTAs' maps for this stamp (shared::cluster
-// addresses of maps in shared memory, or global pointers), `npeers` of them. The cluster
-// barrier that ends the phase makes the stores visible; the maps written here were last read
-// in the phase before it.
+// In a cluster whose maps are in shared memory, each CTA classifies its own share of the disc
+// [first, last) and stores each entry into every CTA's map: `peers` holds the other CTAs' maps
+// for this stamp (shared::cluster addresses), `npeers` of them. The cluster barrier that ends
+// the phase makes the stores visible; the maps written here were last read in the phase
+// before it.
 struct PeerMaps {
-  unsigned smem[16];  // shared::cluster addresses (maps in shared memory)
-  int* glob[16];      // global maps
+  unsigned smem[16];  // shared::cluster addresses of the other CTAs' maps
 };
 __device__ __forceinline__ unsigned dsmem_map_u32(unsigned local, unsigned rank) {
   unsigned r;
@@ -708,7 +707,7 @@ __device__ __forceinline__ void classify_disc(const StampArgs<TK, TV>& a, const 
                                               const int* xs, const int* ys, const M* fps,
                                               const uint32_t* disc, int first, int last,
                                               int* cellmap, int rt, int T,
-                                              const PeerMaps* peers, int npeers, bool peer_smem) {
+                                              const PeerMaps* peers, int npeers) {
   const int F = a.F;
   for (int i = first + rt; i < last; i += T) {  // rt: counted from the last thread (high warps)
     const uint32_t e = disc[i];
@@ -719,12 +718,7 @@ __device__ __forceinline__ void classify_disc(const StampArgs<TK, TV>& a, const 
       const int v = p.live ? ((p.my << 16) | p.mx) : -1;
       const int idx = row * F + col;
       cellmap[idx] = v;
-      for (int q = 0; q < npeers; q++) {
-        if (peer_smem)
-          dsmem_st(peers->smem[q] + 4u * static_cast<unsigned>(idx), v);
-        else
-          peers->glob[q][idx] = v;
-      }
+      for (int q = 0; q < npeers; q++) dsmem_st(peers->smem[q] + 4u * static_cast<unsigned>(idx), v);
     }
   }
 }
@@ -957,10 +951,12 @@ __device__ __forceinline__ void run_stroke(const StampArgs<TK, TV>& a, const Src
   auto dr_at = [&](int slot) { return dr_b + slot * F; };
   auto cm_of = [&](int k) { return cm_b + (k & 1) * npix; };
   // classification in a cluster: each CTA its share of the disc, stored into every CTA's map
+  // through distributed shared memory. Only for maps in shared memory: a map in global memory
+  // is read with L1-cached loads, which could return a line from before a peer's store.
   __shared__ PeerMaps peer_maps[2];
-  const int npeers = csize > 1 ? csize - 1 : 0;
   const bool peer_smem = a.cellmap_global == nullptr;
-  const int cfirst = csize > 1 ? dfirst : 0, clast = csize > 1 ? dlast : ndisc;
+  const int npeers = csize > 1 && peer_smem ? csize - 1 : 0;
+  const int cfirst = npeers > 0 ? dfirst : 0, clast = npeers > 0 ? dlast : ndisc;
   auto rl_of = [&](int k) { return &sh->rl[k & 1]; };
   auto next_slot = [](int slot) { return slot == kStampBufs - 1 ? 0 : slot + 1; };
   // rectangles of stamp k - 1 (the brush's ring state before the first stamp)
@@ -1008,13 +1004,8 @@ __device__ __forceinline__ void run_stroke(const StampArgs<TK, TV>& a, const Src
   if (tid < 2 * npeers) {  // the other CTAs' maps, per stamp parity
     const int par_k = tid / npeers, q = tid - par_k * npeers;
     const int rank = q < crank ? q : q + 1;
-    if (peer_smem) {
-      const unsigned local = static_cast<unsigned>(__cvta_generic_to_shared(cm_b + par_k * npix));
-      peer_maps[par_k].smem[q] = dsmem_map_u32(local, static_cast<unsigned>(rank));
-    } else {
-      peer_maps[par_k].glob[q] = a.cellmap_global + static_cast<int64_t>(rank) * 2 * npix +
-                                 static_cast<int64_t>(par_k) * npix;
-    }
+    const unsigned local = static_cast<unsigned>(__cvta_generic_to_shared(cm_b + par_k * npix));
+    peer_maps[par_k].smem[q] = dsmem_map_u32(local, static_cast<unsigned>(rank));
   }
   if (tid == 0) {  // the stamp before the first: from the brush's ring state or the reset mode
     const int big = 1 << 30;
@@ -1072,7 +1063,7 @@ __device__ __forceinline__ void run_stroke(const StampArgs<TK, TV>& a, const Src
       refresh_ring<CG, PK>(a, *rl_of(0), rt, T, crank, lg_csize, nullptr, 0, 0);
     if (!dup0 && ndisc > 0)
       classify_disc(a, par(0), xs_at(0), ys_at(0), fps, disc, cfirst, clast, cm_of(0), rt, T,
-                    &peer_maps[0], npeers, peer_smem);
+                    &peer_maps[0], npeers);
   }
   csync();
   int epoch = 0;
@@ -1111,7 +1102,7 @@ __device__ __forceinline__ void run_stroke(const StampArgs<TK, TV>& a, const Src
     }
     if (has_next && !dup1 && ndisc > 0)
       classify_disc(a, par(k + 1), xs_at(s1), ys_at(s1), fps, disc, cfirst, clast, cm_of(k + 1),
-                    rt, T, &peer_maps[(k + 1) & 1], npeers, peer_smem);
+                    rt, T, &peer_maps[(k + 1) & 1], npeers);
     lap(2);
     if (((k + 3) & (kParamChunk - 1)) == 0) derive_chunk(k + 3);  // read from phase k + 1 on
     lap(3);

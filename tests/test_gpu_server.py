@@ -113,6 +113,39 @@ def test_continuation_matches_batch_painting(pg):
     assert np.array_equal(imgs[-1], want)
 
 
+def test_eviction_victim_is_not_admitted_in_the_same_round(pg):
+    """Three canvases over a budget that holds two, their continuations queued behind each
+    other: admitting a new canvas evicts an idle one whose next request is also waiting. That
+    request must wait for a later round (and a restore), not paint the canvas being evicted.
+    Results equal those of a server that never evicts."""
+    fp = workloads.footprint_image(seed=7)
+    rng = np.random.default_rng(31)
+    side = 300
+    rounds = [[_strokes(rng, side, side, 3) for _ in range(3)] for _ in range(4)]
+    r0 = rng.uniform(0.8, 0.95, (side, side, 3)).astype(np.float32)
+
+    def run(budget):
+        srv = pg.Server(budget, fp, storage="f16", step_stamps=20000)
+        cids, rids = [None] * 3, []
+        for rnd in rounds:
+            for k in range(3):
+                if cids[k] is None:
+                    rid, cids[k] = srv.submit(rnd[k], rows=side, cols=side, r0=r0)
+                else:
+                    rid, _ = srv.submit(rnd[k], canvas_id=cids[k])
+                rids.append(rid)
+        imgs = [srv.wait(r, 120)[0] for r in rids]
+        st = srv.stats()
+        srv.close()
+        return imgs, st
+
+    tight, st = run(20 << 20)  # two of these canvases fit
+    roomy, _ = run(4 << 30)
+    assert st["evictions"] > 0 and st["restores"] > 0 and st["failed"] == 0, st
+    for a, b in zip(tight, roomy):
+        assert np.array_equal(a, b)
+
+
 def test_eviction_and_restore_keep_results(pg):
     fp = workloads.footprint_image(seed=7)
     reqs = _request_set(11, 10)
