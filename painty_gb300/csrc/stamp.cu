@@ -1151,8 +1151,10 @@ __device__ __forceinline__ void run_stroke(const StampArgs<TK, TV>& a, const Src
 // PS: pickup map staged in shared memory. BIG: footprint and owner table in global memory
 // (maps too large for shared memory); otherwise both are in shared memory. CG: a cluster
 // launch (global loads from L2).
-template <bool PS, bool BIG, bool CG, bool PK, class TK, class TV>
-__global__ void __launch_bounds__(kStampThreads, 1) stamp_kernel(const __grid_constant__ StampArgs<TK, TV> a) {
+// NT threads per CTA: 1024, or 512 for clusters (each CTA then holds 128 registers per thread;
+// measured 188k -> 198k stamps/s on the plain workload).
+template <bool PS, bool BIG, bool CG, bool PK, class TK, class TV, int NT = kStampThreads>
+__global__ void __launch_bounds__(NT, 1) stamp_kernel(const __grid_constant__ StampArgs<TK, TV> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ StampParams sparams[kParamRing];
   __shared__ StampShared sh;
@@ -1778,14 +1780,20 @@ void launch_stamps(painty_canvas* c, painty_brush* b, const StampRec* d_stamps, 
   // 174k at cluster 8), cluster 8 and 16 tie at F = 47 (170k; one CTA 162k), cluster 16 leads
   // from F = 57 (165k vs 160k) and more so for larger stamps (98k vs 82k at F = 137); clusters
   // of 2 or 4 are never the fastest. 16 needs a non-portable cluster, else 8 is used.
+  // Clusters run 512-thread CTAs when the stamp's box fits their edge-duplicate masks.
   const int nd = disc_count(b->F, b->support2);
   int cl = env_cluster("PAINTY_STAMP_CLUSTER", 16);
   if (cl == 0) cl = nd >= 2400 ? 16 : nd >= 1400 ? 8 : 1;
   SmemPlan plan{};
   void (*kern)(StampArgs<TK, TV>) = nullptr;
+  int nt = kStampThreads;
   for (;;) {
     plan = plan_smem<M>(b->F, b->sizeMap, nd, true, cl == 1, true);
-    if (cl > 1)
+    nt = cl > 1 && waves_fit(b->F, 512) ? 512 : kStampThreads;
+    if (cl > 1 && nt == 512)
+      kern = plan.big ? stamp_kernel<false, true, true, true, TK, TV, 512>
+                      : stamp_kernel<false, false, true, true, TK, TV, 512>;
+    else if (cl > 1)
       kern = plan.big ? stamp_kernel<false, true, true, true, TK, TV>
                       : stamp_kernel<false, false, true, true, TK, TV>;
     else
@@ -1802,7 +1810,7 @@ void launch_stamps(painty_canvas* c, painty_brush* b, const StampRec* d_stamps, 
       cl = 8;
       continue;
     }
-    if (cl == 1 || max_clusters(kern, cl, plan.layout.total) >= 1) break;
+    if (cl == 1 || max_clusters(kern, cl, plan.layout.total, nt) >= 1) break;
     cl /= 2;
   }
   a.ndisc = plan.ndisc;
@@ -1819,7 +1827,7 @@ void launch_stamps(painty_canvas* c, painty_brush* b, const StampRec* d_stamps, 
   a.footprint_smem = plan.big ? 0 : 1;
   a.pickup_smem = plan.pick ? 1 : 0;
   const StampSmem Lk = plan.layout;
-  launch_clustered(kern, cl, cl, Lk.total, st, a);
+  launch_clustered(kern, cl, cl, Lk.total, st, a, nt);
   count_launch();
   PG_CUDA(cudaGetLastError());
 }
