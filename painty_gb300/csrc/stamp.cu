@@ -1282,10 +1282,10 @@ struct BatchArgs {
 
 // Persistent batched painting: each CTA claims canvases (heaviest first) and applies their
 // strokes in order, each as setRadius + dip + paintStroke on the canvas's brush. NT threads
-// per CTA: 1024 (one CTA per SM) or 512 (two per SM, twice the canvases in flight, each
-// painted by half the threads), with the same register budget.
+// per CTA, one CTA per SM: 1024 (64 registers per thread), or 512 for clusters (128 registers:
+// the stamps a cluster shares run faster on half-size CTAs).
 template <class TK, class TV, int NT>
-__global__ void __launch_bounds__(NT, 1024 / NT) batch_kernel(const __grid_constant__ BatchArgs<TK, TV> b) {
+__global__ void __launch_bounds__(NT, 1) batch_kernel(const __grid_constant__ BatchArgs<TK, TV> b) {
   using M = typename MathOf<TK>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ StampParams sparams[kParamRing];
@@ -1960,9 +1960,11 @@ void run_stamps(painty_canvas* c, painty_brush* b, const std::vector<StampRec>& 
 constexpr double kStampFixed = 7000.0;
 constexpr double kStampPerPixel = 12.0;
 constexpr double kClusterSync = 1500.0;
-// 512-thread CTAs (two per SM): the fixed part and the per-pixel part relative to 1024
-constexpr double kHalfFixed = 1.2;
-constexpr double kHalfPerPixel = 2.4;
+// 512-thread CTAs in clusters: the stamp time relative to 1024-thread CTAs (measured on the
+// plain workload's clusters: 188k -> 198k stamps/s); a lone 512-thread CTA paints at about the
+// speed of a 1024-thread one (111k vs 114k)
+constexpr double kHalfCluster = 0.95;
+constexpr double kHalfSingle = 1.03;
 
 // cluster size, clusters, threads of the batch's main launch; cluster size and clusters of its
 // launch for the heaviest canvases (0: none)
@@ -1995,11 +1997,10 @@ double batch_makespan(const std::vector<double>& N, const std::vector<double>& P
   std::priority_queue<double, std::vector<double>, std::greater<double>> q;
   for (int i = 0; i < slots; i++) q.push(0.0);
   double span = 0.0;
-  // 512-thread CTAs: half the threads per stamp pixel, and an SM shared by two CTAs
-  const double fixed = threads == 512 ? kStampFixed * kHalfFixed : kStampFixed;
-  const double per_pixel = threads == 512 ? kStampPerPixel * kHalfPerPixel : kStampPerPixel;
+  const double scale = threads == 512 ? (cl > 1 ? kHalfCluster : kHalfSingle) : 1.0;
   for (int32_t c : order) {
-    const double t = N[c] * (fixed + (cl > 1 ? kClusterSync : 0.0)) + per_pixel * P[c] / cl;
+    const double t =
+      scale * (N[c] * (kStampFixed + (cl > 1 ? kClusterSync : 0.0)) + kStampPerPixel * P[c] / cl);
     const double end = q.top() + t;
     q.pop();
     q.push(end);
@@ -2049,16 +2050,6 @@ BatchKernelInfo& batch_kernel_info() {
   return *info;
 }
 
-int smem_per_sm() {
-  static int cached[64] = {0};
-  int dev = 0;
-  PG_CUDA(cudaGetDevice(&dev));
-  if (dev < 64 && cached[dev] > 0) return cached[dev];
-  int v = 0;
-  PG_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev));
-  if (dev < 64) cached[dev] = v;
-  return v;
-}
 
 // Thread count from the environment (PAINTY_BATCH_THREADS: 512 or 1024), 0 if unset.
 int env_threads(const char* name) {
@@ -2082,20 +2073,9 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   // launch shared-memory budget: the opt-in maximum minus the kernel's static shared memory
   BatchKernelInfo& info1k = batch_kernel_info<TK, TV, 1024>();
   BatchKernelInfo& info512 = batch_kernel_info<TK, TV, 512>();
-  // shared-memory budgets: a 1024-thread CTA may take the opt-in maximum; two 512-thread CTAs
-  // share one SM's shared memory (each CTA also reserves a little for the system)
-  int reserved = 0;
-  {
-    int dev = 0;
-    PG_CUDA(cudaGetDevice(&dev));
-    PG_CUDA(cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev));
-  }
+  // shared-memory budgets: the opt-in maximum less the kernel's static shared memory
   const size_t limit1k = static_cast<size_t>(max_dyn_smem()) - info1k.static_smem - 256;
-  const size_t half = static_cast<size_t>(smem_per_sm()) / 2;
-  const size_t limit512 =
-    std::min(static_cast<size_t>(max_dyn_smem()) - info512.static_smem - 256,
-             half > info512.static_smem + reserved + 256
-               ? half - info512.static_smem - reserved - 256 : size_t(0));
+  const size_t limit512 = static_cast<size_t>(max_dyn_smem()) - info512.static_smem - 256;
   std::vector<BatchStroke> bs;
   bs.reserve(static_cast<size_t>(ns));
   std::vector<double> work(nc, 0.0), loadN(nc, 0.0), loadP(nc, 0.0);
@@ -2282,17 +2262,19 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
                                                           : opt.threads;
   auto best_launch = [&](int begin, int end, int max_slots_1k, int max_slots_512) {
     Launch best;
-    // a requested thread count first; any other only when no launch of it fits
-    for (int pass = 0; pass < 2 && best.slots < 1; pass++)
-      for (int n2 : {1024, 512}) {
-        if (pass == 0 && want_nt && n2 != want_nt) continue;
-        for (int c2 : {1, 2, 4, 8}) {
-          if (forced ? c2 != forced : c2 > opt.max_cluster) continue;
-          const int ms = n2 == 512 ? max_slots_512 : max_slots_1k;
-          const Launch L = evaluate(begin, end, n2, c2, ms == INT_MAX ? ms : ms / c2);
-          if (L.slots >= 1 && L.span < best.span) best = L;
-        }
+    for (int c2 : {1, 2, 4, 8}) {
+      if (forced ? c2 != forced : c2 > opt.max_cluster) continue;
+      // a requested thread count, else 512-thread CTAs for clusters and 1024 for lone CTAs;
+      // the other count when the first fits no launch (boxes wider than 512 threads cover)
+      const int first = want_nt ? want_nt : (c2 > 1 ? 512 : 1024);
+      for (int n2 : {first, first == 512 ? 1024 : 512}) {
+        const int ms = n2 == 512 ? max_slots_512 : max_slots_1k;
+        const Launch L = evaluate(begin, end, n2, c2, ms == INT_MAX ? ms : ms / c2);
+        if (L.slots < 1) continue;
+        if (L.span < best.span) best = L;
+        break;
       }
+    }
     return best;
   };
   const Launch single = best_launch(0, nc, INT_MAX, INT_MAX);
@@ -2310,12 +2292,13 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   }
   if (opt.done_host) force_ch = 0;  // one launch signals completion: no split
   if (force_ch) {
-    heavy = evaluate(0, force_h, 1024, force_ch, force_h);
+    heavy = evaluate(0, force_h, 512, force_ch, force_h);
+    if (heavy.slots < force_h) heavy = evaluate(0, force_h, 1024, force_ch, force_h);
     int dev = 0, sms = 0;
     PG_CUDA(cudaGetDevice(&dev));
     PG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const int left = std::max(1, sms - force_h * force_ch);
-    rest = best_launch(force_h, nc, left, 2 * left);
+    rest = best_launch(force_h, nc, left, left);
     PG_REQUIRE(heavy.slots == force_h && rest.slots >= 1, "PAINTY_BATCH_SPLIT does not fit");
   } else if (!forced && !want_nt && !opt.done_host && nc >= 2 && opt.max_cluster >= 4) {
     int dev = 0, sms = 0;
@@ -2325,10 +2308,11 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
     for (int ch : {8, 4}) {
       if (ch > opt.max_cluster) continue;
       for (int h = 1; h < nc && 2 * h * ch <= sms; h++) {
-        const Launch A = evaluate(0, h, 1024, ch, h);
+        Launch A = evaluate(0, h, 512, ch, h);  // clusters: 512-thread CTAs where boxes allow
+        if (A.slots < h) A = evaluate(0, h, 1024, ch, h);
         if (A.slots < h || A.span >= best) break;
         const int left = sms - h * ch;  // SMs the heavy launch leaves (one 1024-thread CTA each)
-        const Launch B = best_launch(h, nc, left, 2 * left);
+        const Launch B = best_launch(h, nc, left, left);
         if (B.slots < 1) continue;
         const double span = std::max(A.span, B.span);
         if (span < best) {
