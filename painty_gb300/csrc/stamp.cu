@@ -484,11 +484,16 @@ __host__ __device__ inline StampSmem stamp_smem_layout(int F, int S, int ndisc, 
 }
 
 constexpr int kEpochMax = 32767;  // owner keys: ((kEpochMax - epoch) << 16) | pixel index
-// Whether paint_waves' per-thread pixel mask (64 bits: rows per warp x 32-column groups)
-// covers an F x F box with `threads` threads.
+// Whether paint_waves' per-thread pixel mask (128 bits: rows per warp x 32-column groups)
+// covers an F x F box with `threads` threads (every box up to side 255 with 512 threads).
 __host__ __device__ constexpr bool waves_fit(int F, int threads) {
-  return ((F + threads / 32 - 1) / (threads / 32)) * ((F + 31) / 32) <= 64;
+  return ((F + threads / 32 - 1) / (threads / 32)) * ((F + 31) / 32) <= 128;
 }
+// Clusters take 512-thread CTAs for boxes up to this side: there a stamp's fixed costs
+// dominate and half-size CTAs win (plain workload, sides 43-91: 188k -> 198k stamps/s);
+// larger boxes are painted faster by 1024 threads (the batch's heaviest canvases, sides up
+// to 183, ran at 80k instead of 135k stamps/s on 512-thread CTAs).
+constexpr int kMax512Side = 127;
 
 // ---------------------------------------------------------------------- snapshot ring
 // painty refreshes the snapshot from the canvas over a ring around every stamp: the box grown
@@ -799,7 +804,7 @@ __device__ __noinline__ int paint_waves(const StampArgs<TK, TV>& a, const StampP
     epoch = 0;
     __syncthreads();
   }
-  uint64_t rem = 0;
+  uint64_t rem[2] = {0, 0};  // this thread's pixels still to paint (bit j: slot j)
   int wave = 1;
   int key_hi = (kEpochMax - epoch) << 16;
   epoch++;
@@ -816,16 +821,18 @@ __device__ __noinline__ int paint_waves(const StampArgs<TK, TV>& a, const StampP
           atomicMin(&own[p.my * S + p.mx], key_hi | (row * F + col));
         }
       }
-      if (lv)
-        rem |= 1ull << (jr * NC + jc);
-      else
+      if (lv) {
+        const int j = jr * NC + jc;
+        rem[j >> 6] |= 1ull << (j & 63);
+      } else
         mark_done(xs, ys, F, done_c, done_r, row, col, 1);  // done "before" wave 1
     }
   }
   __syncthreads();
   for (;;) {
-    for (uint64_t bits = rem; bits; bits &= bits - 1) {
-      const int j = __ffsll(static_cast<long long>(bits)) - 1;
+    for (int wd = 0; wd < 2; wd++)
+    for (uint64_t bits = rem[wd]; bits; bits &= bits - 1) {
+      const int j = 64 * wd + __ffsll(static_cast<long long>(bits)) - 1;
       const int row = warp + kWarps * (j / NC), col = lane + 32 * (j % NC);
       M fp;
       const PixelInfo p = pixel_info(a, sp, xs, ys, fps, row, col, &fp);
@@ -834,11 +841,11 @@ __device__ __noinline__ int paint_waves(const StampArgs<TK, TV>& a, const StampP
         process_pixel<PS, CG, PK, TK, TV, M>(a, pbase, cells, fp,
                                              p.yc * static_cast<int>(a.pitch) + p.xc,
                                              p.my * S + p.mx, seed, false);
-        rem &= ~(1ull << j);
+        rem[wd] &= ~(1ull << (j & 63));
         mark_done(xs, ys, F, done_c, done_r, row, col, static_cast<uint16_t>(wave + 1));
       }
     }
-    const int any = __syncthreads_or(rem != 0);
+    const int any = __syncthreads_or((rem[0] | rem[1]) != 0);
     if (!any) break;
     if (wave >= kMaxWaves) {  // cannot happen: the lowest remaining pixel always runs
       if (tid == 0) atomicOr(a.status, kStatusWaveCap);
@@ -847,8 +854,9 @@ __device__ __noinline__ int paint_waves(const StampArgs<TK, TV>& a, const StampP
     wave++;
     key_hi = (kEpochMax - epoch) << 16;
     epoch++;
-    for (uint64_t bits = rem; bits; bits &= bits - 1) {  // bid for the map cell
-      const int j = __ffsll(static_cast<long long>(bits)) - 1;
+    for (int wd = 0; wd < 2; wd++)
+    for (uint64_t bits = rem[wd]; bits; bits &= bits - 1) {  // bid for the map cell
+      const int j = 64 * wd + __ffsll(static_cast<long long>(bits)) - 1;
       const int row = warp + kWarps * (j / NC), col = lane + 32 * (j % NC);
       M fp;
       const PixelInfo p = pixel_info(a, sp, xs, ys, fps, row, col, &fp);
@@ -1789,7 +1797,7 @@ void launch_stamps(painty_canvas* c, painty_brush* b, const StampRec* d_stamps, 
   int nt = kStampThreads;
   for (;;) {
     plan = plan_smem<M>(b->F, b->sizeMap, nd, true, cl == 1, true);
-    nt = cl > 1 && waves_fit(b->F, 512) ? 512 : kStampThreads;
+    nt = cl > 1 && b->F <= kMax512Side ? 512 : kStampThreads;
     if (cl > 1 && nt == 512)
       kern = plan.big ? stamp_kernel<false, true, true, true, TK, TV, 512>
                       : stamp_kernel<false, false, true, true, TK, TV, 512>;
@@ -2197,6 +2205,8 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   // a shape's plan for a launch of nt-thread CTAs in clusters of cl (nullptr: the shape does
   // not fit 512-thread CTAs); clusters keep the pickup map in global memory
   std::map<std::tuple<int32_t, int, bool>, std::unique_ptr<SmemPlan>> plans;
+  const int want_nt = env_threads("PAINTY_BATCH_THREADS") ? env_threads("PAINTY_BATCH_THREADS")
+                                                          : opt.threads;
   auto shape_plan = [&](int32_t sid, int nt, int cl) -> const SmemPlan* {
     const auto key = std::make_tuple(sid, nt, cl == 1);
     auto it = plans.find(key);
@@ -2206,7 +2216,7 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
     const int nd = std::get<2>(shapes[sid]);
     if (nt == 1024) {
       pl = std::make_unique<SmemPlan>(plan_smem_limit<M>(F, S, nd, limit1k, true, cl == 1, true));
-    } else if (waves_fit(F, 512) && limit512 > 0) {
+    } else if (waves_fit(F, 512) && (want_nt == 512 || F <= kMax512Side) && limit512 > 0) {
       try {
         pl = std::make_unique<SmemPlan>(plan_smem_limit<M>(F, S, nd, limit512, true, cl == 1, true));
       } catch (const Error&) {
@@ -2258,8 +2268,6 @@ void run_batch_typed(painty_canvas* const* canvases, painty_brush* const* brushe
   // thread count and cluster size: autotuned by the cost model unless PAINTY_BATCH_THREADS /
   // PAINTY_BATCH_CLUSTER (or the caller's options) set them
   const int forced = env_cluster("PAINTY_BATCH_CLUSTER");
-  const int want_nt = env_threads("PAINTY_BATCH_THREADS") ? env_threads("PAINTY_BATCH_THREADS")
-                                                          : opt.threads;
   auto best_launch = [&](int begin, int end, int max_slots_1k, int max_slots_512) {
     Launch best;
     for (int c2 : {1, 2, 4, 8}) {

@@ -182,15 +182,22 @@ def test_batch_split_launch_f64(pg, oracle, monkeypatch, split):
             assert np.array_equal(cs[ci].download(p), oc.get(p)), (ci, p)
 
 
-def test_batch_512_threads_falls_back_for_large_boxes(pg, monkeypatch):
-    """Boxes wider than 512-thread CTAs cover (radius 70: side 199) run on 1024 threads."""
-    monkeypatch.setenv("PAINTY_BATCH_THREADS", "512")
+def test_batch_512_threads_large_boxes_equal_1024(pg, monkeypatch):
+    """Boxes up to side 255 fit 512-thread CTAs (radius 70: side 199, its edge duplicates in
+    waves): the same results as 1024-thread CTAs, bit for bit."""
     rng = np.random.default_rng(41)
     sizes = _canvases(rng, 2, smin=150, smax=200)
     strokes = _session(rng, sizes, strokes_per=(1, 2), rmin=70.0, rmax=70.0)
-    cs, bs, _ = _setup(pg, sizes, "f32")
-    pg.paint_batch(cs, bs, strokes)
-    assert pg.batch_last_shape()[2] == 1024
+    out = {}
+    for nt in ("512", "1024"):
+        monkeypatch.setenv("PAINTY_BATCH_THREADS", nt)
+        cs, bs, _ = _setup(pg, sizes, "f32")
+        pg.paint_batch(cs, bs, strokes)
+        assert pg.batch_last_shape()[2] == int(nt)
+        out[nt] = [[c.download(p) for p in ("K", "S", "V")] for c in cs]
+    for a, b in zip(out["512"], out["1024"]):
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y)
 
 
 def test_batch_f32_close_to_sequential(pg):
