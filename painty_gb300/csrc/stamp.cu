@@ -397,6 +397,25 @@ __device__ __forceinline__ PixelInfo pixel_info(const StampArgs<TK, TV>& a, cons
   return p;
 }
 
+// pixel_info of a pixel the first wave pass found live, from its cached map cell (the same
+// canvas pixel, cell and footprint height; recomputed when there is no cache).
+template <class TK, class TV, class M>
+__device__ __forceinline__ PixelInfo cached_pixel(const StampArgs<TK, TV>& a,
+                                                  const StampParams& sp, const int* xs,
+                                                  const int* ys, const M* fps, int row, int col,
+                                                  M* fp_out, const int* cache) {
+  if (!cache) return pixel_info(a, sp, xs, ys, fps, row, col, fp_out);
+  const int code = cache[row * a.F + col];
+  PixelInfo p;
+  p.xc = xs[col];
+  p.yc = ys[row];
+  p.mx = code & 0xffff;
+  p.my = code >> 16;
+  *fp_out = fps[p.my * a.F + p.mx];
+  p.live = true;
+  return p;
+}
+
 // Earlier pixels on the same canvas pixel (left/top edge duplicates) finished in an earlier
 // wave. done_c[row] / done_r[col] hold the 1-based wave in which pixel (c0, row) / (col, r0)
 // finished (c0, r0: the first of the duplicated column / row), 0 while pending.
@@ -789,10 +808,13 @@ __device__ __forceinline__ void paint_disc(const StampArgs<TK, TV>& a, const int
 // whole CTA; returns the next epoch. Out of line: rare, and it keeps the cell path's
 // registers free.
 template <bool PS, bool CG, bool PK, class TK, class TV, class M>
+//
+// `cache` (F*F ints, or null): where the first pass keeps each live pixel's map cell, so the
+// waves after it skip the rotation (the stamp's own cell map, free while it paints in waves).
 __device__ __noinline__ int paint_waves(const StampArgs<TK, TV>& a, const StampParams& sp,
                                         const int* xs, const int* ys, uint16_t* done_c,
                                         uint16_t* done_r, const M* fps, M* pbase, int* own,
-                                        int epoch, uint32_t seed) {
+                                        int epoch, uint32_t seed, int* cache) {
   const int tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
   const int F = a.F, S = a.S;
@@ -819,6 +841,7 @@ __device__ __noinline__ int paint_waves(const StampArgs<TK, TV>& a, const StampP
         if (p.live && in_bounds(a.status, kBoundsOwner, p.my * S + p.mx, cells)) {
           lv = true;
           atomicMin(&own[p.my * S + p.mx], key_hi | (row * F + col));
+          if (cache) cache[row * F + col] = (p.my << 16) | p.mx;
         }
       }
       if (lv) {
@@ -835,7 +858,7 @@ __device__ __noinline__ int paint_waves(const StampArgs<TK, TV>& a, const StampP
       const int j = 64 * wd + __ffsll(static_cast<long long>(bits)) - 1;
       const int row = warp + kWarps * (j / NC), col = lane + 32 * (j % NC);
       M fp;
-      const PixelInfo p = pixel_info(a, sp, xs, ys, fps, row, col, &fp);
+      const PixelInfo p = cached_pixel(a, sp, xs, ys, fps, row, col, &fp, cache);
       if (own[p.my * S + p.mx] == (key_hi | (row * F + col)) &&
           canvas_ready(xs, ys, F, done_c, done_r, row, col, wave)) {
         process_pixel<PS, CG, PK, TK, TV, M>(a, pbase, cells, fp,
@@ -859,7 +882,7 @@ __device__ __noinline__ int paint_waves(const StampArgs<TK, TV>& a, const StampP
       const int j = 64 * wd + __ffsll(static_cast<long long>(bits)) - 1;
       const int row = warp + kWarps * (j / NC), col = lane + 32 * (j % NC);
       M fp;
-      const PixelInfo p = pixel_info(a, sp, xs, ys, fps, row, col, &fp);
+      const PixelInfo p = cached_pixel(a, sp, xs, ys, fps, row, col, &fp, cache);
       atomicMin(&own[p.my * S + p.mx], key_hi | (row * F + col));
     }
     __syncthreads();
@@ -1102,7 +1125,8 @@ __device__ __forceinline__ void run_stroke(const StampArgs<TK, TV>& a, const Src
     } else {
       if (crank == 0)  // edge duplicates: the first CTA alone, in waves
         epoch = paint_waves<PS, CG, PK, TK, TV, M>(a, sp, xs_at(s0), ys_at(s0), dc_at(s0),
-                                                   dr_at(s0), fps, pbase, own, epoch, seed);
+                                                   dr_at(s0), fps, pbase, own, epoch, seed,
+                                                   ndisc > 0 ? cm_of(k) : nullptr);
       csync();
       if (has_next && a.use_snapshot)
         refresh_ring<CG, PK>(a, *rl_of(k + 1), rt, T, crank, lg_csize, nullptr, 0, 0);
