@@ -82,7 +82,7 @@ void configure_pool(cudaMemPool_t pool);
 const void* mapped_host(const void* host);
 
 // One device reservation carved up on the host: allocation and release are host bookkeeping
-// (best fit, neighbours merged on release, 256-byte granules), so neither calls the driver.
+// (best fit, neighbours merged on release, 256-byte granules), so neither calls into CUDA.
 // For an owner that releases memory only once the GPU has finished with it (the server: a
 // canvas's memory after its last request completed). A request the reservation cannot hold
 // falls back to stream-ordered cudaMallocAsync on the given stream.

@@ -14,7 +14,7 @@
 //
 // Canvases stay resident on the device between requests. Their memory (canvas, composite
 // image, brush buffers) is carved on the host from one device reservation made when the
-// server starts, so creating and dropping canvases calls no allocator of the driver; memory
+// server starts, so creating and dropping canvases calls no CUDA allocator; memory
 // is returned only when the GPU has finished with it (a canvas after its last request).
 // Admission keeps the resident bytes under a budget by evicting idle canvases (least recently
 // used first) to pinned host memory and restoring them when a later request continues them. A canvas's requests run one after another, in
@@ -551,7 +551,7 @@ bool worker_round(painty_server* s, std::unique_lock<std::mutex>& lk) {
       continue;
     }
     if (std::find(evictions.begin(), evictions.end(), c) != evictions.end()) {
-      ++it;  // chosen for eviction in this round: it is admitted (and restored) in a later one
+      ++it;  // chosen for eviction in this pass: it is admitted (and restored) in a later one
       continue;
     }
     if (r->cancel) {
