@@ -533,7 +533,7 @@ struct Admitted {
   bool prep;  // create or restore the canvas first
 };
 
-// One round of the worker: admit what fits, start admitted requests, advance every request
+// One pass of the worker: admit what fits, start admitted requests, advance every request
 // whose slot's work has finished. Called with the lock held; returns whether anything moved.
 bool worker_round(painty_server* s, std::unique_lock<std::mutex>& lk) {
   // ---- drops and admission (lock held): pending requests in arrival order
