@@ -257,9 +257,10 @@ painty_status painty_paint_batch(painty_canvas* const* canvases, painty_brush* c
 
 /* The launch shape the last painty_paint_batch on this thread chose: CTAs per canvas (a
  * thread-block cluster sharing each stamp), the number of clusters launched, and threads per
- * CTA (1024: one CTA per SM; 512: two per SM, twice the canvases in flight). Picked by a
- * makespan model of the batch unless the environment variables PAINTY_BATCH_CLUSTER /
- * PAINTY_BATCH_THREADS set them. Any pointer may be NULL. No counterpart in painty. */
+ * CTA (one CTA per SM: 1024 threads, or 512 with twice the registers per thread, used by
+ * clusters for boxes up to side 127). Picked by a makespan model of the batch unless the
+ * environment variables PAINTY_BATCH_CLUSTER / PAINTY_BATCH_THREADS set them. Any pointer may
+ * be NULL. No counterpart in painty. */
 painty_status painty_batch_last_shape(int32_t* cluster, int32_t* clusters, int32_t* threads);
 /* Whether the last painty_paint_batch on this thread gave its heaviest canvases a launch of
  * their own, next to the rest, on clusters of `cluster` CTAs (0: no such launch), and how
