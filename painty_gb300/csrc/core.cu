@@ -258,7 +258,7 @@ DeviceHeap::DeviceHeap(size_t bytes) {
   }
   base_ = static_cast<char*>(p);
   size_ = p ? bytes : 0;
-  if (size_) insert_free(0, size_);
+  ranges_.reset(size_);
 }
 
 DeviceHeap::~DeviceHeap() {
@@ -266,33 +266,12 @@ DeviceHeap::~DeviceHeap() {
   for (void* p : outside_) cudaFree(p);
 }
 
-void DeviceHeap::insert_free(size_t off, size_t len) {
-  free_by_off_.emplace(off, len);
-  free_by_len_.emplace(len, off);
-}
-
-void DeviceHeap::erase_free(size_t off, size_t len) {
-  free_by_off_.erase(off);
-  auto r = free_by_len_.equal_range(len);
-  for (auto it = r.first; it != r.second; ++it)
-    if (it->second == off) {
-      free_by_len_.erase(it);
-      break;
-    }
-}
-
 void* DeviceHeap::alloc(size_t bytes, cudaStream_t st) {
   const size_t len = (std::max<size_t>(bytes, 1) + 255) / 256 * 256;
   {
     std::lock_guard<std::mutex> lk(mu_);
-    auto it = free_by_len_.lower_bound(len);  // best fit
-    if (it != free_by_len_.end()) {
-      const size_t flen = it->first, off = it->second;
-      erase_free(off, flen);
-      if (flen > len) insert_free(off + len, flen - len);
-      used_.emplace(off, len);
-      return base_ + off;
-    }
+    size_t off = 0;
+    if (ranges_.alloc(len, &off)) return base_ + off;  // best fit
     fallbacks_++;
   }
   void* p = nullptr;
@@ -312,28 +291,7 @@ void DeviceHeap::free(void* p, cudaStream_t st) {
   std::lock_guard<std::mutex> lk(mu_);
   char* c = static_cast<char*>(p);
   if (base_ && c >= base_ && c < base_ + size_) {
-    size_t off = static_cast<size_t>(c - base_);
-    auto u = used_.find(off);
-    if (u == used_.end()) return;  // not an allocation of this heap
-    size_t len = u->second;
-    used_.erase(u);
-    auto next = free_by_off_.lower_bound(off);
-    if (next != free_by_off_.end() && next->first == off + len) {  // merge the following gap
-      const size_t nl = next->second;
-      erase_free(next->first, nl);
-      len += nl;
-    }
-    auto prev = free_by_off_.lower_bound(off);
-    if (prev != free_by_off_.begin()) {  // merge the preceding gap
-      --prev;
-      if (prev->first + prev->second == off) {
-        const size_t po = prev->first, pl = prev->second;
-        erase_free(po, pl);
-        off = po;
-        len += pl;
-      }
-    }
-    insert_free(off, len);
+    ranges_.release(static_cast<size_t>(c - base_));  // false: not an allocation of this heap
     return;
   }
   if (outside_.erase(p)) cudaFreeAsync(p, st);

@@ -15,6 +15,7 @@
 #include <unordered_map>
 #include <unordered_set>
 
+#include "offset_alloc.h"
 #include "painty_gb300.h"
 
 namespace pg {
@@ -101,13 +102,9 @@ class DeviceHeap {
   std::mutex mu_;
   char* base_ = nullptr;
   size_t size_ = 0;
-  std::map<size_t, size_t> free_by_off_;       // offset -> length
-  std::multimap<size_t, size_t> free_by_len_;  // length -> offset
-  std::unordered_map<size_t, size_t> used_;    // offset -> length
-  std::unordered_set<void*> outside_;          // fallback allocations
+  OffsetAllocator ranges_;              // the reservation's layout
+  std::unordered_set<void*> outside_;  // fallback allocations
   int64_t fallbacks_ = 0;
-  void insert_free(size_t off, size_t len);
-  void erase_free(size_t off, size_t len);
 };
 
 }  // namespace pg
