@@ -246,6 +246,55 @@ def run_stamps_only(args):
     print(json.dumps(out), flush=True)
 
 
+def run_cluster_sweep(args):
+    """Stamps/s by brush radius and cluster size on one 1024x768 FP32 canvas: 12 strokes of 8
+    control points per point, one untimed pass first, PAINTY_STAMP_CLUSTER set per point (the
+    library reads it at every stroke). One JSON line per radius."""
+    import numpy as np
+    import torch
+
+    import painty_gb300 as pg
+    from painty_gb300 import workloads
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    fp = workloads.footprint_image(seed=7)
+    old = os.environ.get("PAINTY_STAMP_CLUSTER")
+    try:
+        for r in (3.0, 5.0, 7.0, 8.5, 10.0, 13.0, 16.0, 20.0, 24.0, 30.0):
+            row = {"r": r}
+            for cl in (1, 2, 4, 8, 16):
+                os.environ["PAINTY_STAMP_CLUSTER"] = str(cl)
+                rng = np.random.default_rng(3)
+                c = pg.Canvas(768, 1024, "f32")
+                c.upload("R0", np.full((768, 1024, 3), 0.85))
+                b = pg.FootprintBrush(r, fp)
+                b.setPickupRate(0.05)
+                b.setDepositionRate(0.1)
+                paths = [np.stack([rng.uniform(100, 924, 8), rng.uniform(100, 668, 8)], axis=1)
+                         for _ in range(12)]
+
+                def run():
+                    n = 0
+                    for p in paths:
+                        b.dip((rng.uniform(0.01, 5, 3), rng.uniform(0.05, 3, 3)))
+                        n += b.paintStroke(p, c, spacing=0.25 * r)
+                    return n
+
+                run()
+                torch.cuda.synchronize()
+                t = time.perf_counter()
+                n = run()
+                torch.cuda.synchronize()
+                row[str(cl)] = round(n / (time.perf_counter() - t))
+                row["F"] = b.info()[1]
+            print(json.dumps(row), flush=True)
+    finally:
+        if old is None:
+            os.environ.pop("PAINTY_STAMP_CLUSTER", None)
+        else:
+            os.environ["PAINTY_STAMP_CLUSTER"] = old
+
+
 def _event_ms(torch, fn, reps: int, warm: int = 3) -> float:
     """Average device time of fn() over `reps` calls (CUDA events on the current stream)."""
     for _ in range(warm):
@@ -1297,6 +1346,8 @@ def main():
                     help="cap on strokes per canvas in the batched stamping case (none: as stated)")
     ap.add_argument("--strokes", type=int, default=200, help="strokes in the stamping case")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cluster-sweep", action="store_true",
+                    help="stamps/s by brush radius and stamp cluster size")
     ap.add_argument("--serve-only", action="store_true", help="only the serving case")
     ap.add_argument("--precision-only", action="store_true", help="only the precision case")
     ap.add_argument("--batch-only", action="store_true", help="only the batched stamping case")
@@ -1312,6 +1363,8 @@ def main():
     globals()["ROWS"], globals()["COLS"] = args.rows, args.cols
     if args.impl == "reference":
         run_reference(args)
+    elif args.cluster_sweep:
+        run_cluster_sweep(args)
     elif args.stamps_only:
         run_stamps_only(args)
     elif args.serve_only:

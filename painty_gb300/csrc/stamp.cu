@@ -1806,16 +1806,16 @@ void launch_stamps(painty_canvas* c, painty_brush* b, const StampRec* d_stamps, 
   a.pickup_zero = pickup_zero ? 1 : 0;
   a.status = b->d_status;
   a.support2 = b->support2;
-  // one canvas: a cluster of CTAs shares each stamp when the stamp is large enough to split
-  // (the pickup map is then in global memory); a lone CTA stages it in shared memory. Measured
-  // on GB300 (3,000 stamps per radius, FP32, stamps/s): one CTA is fastest up to F = 35 (196k;
-  // 174k at cluster 8), cluster 8 and 16 tie at F = 47 (170k; one CTA 162k), cluster 16 leads
-  // from F = 57 (165k vs 160k) and more so for larger stamps (98k vs 82k at F = 137); clusters
+  // one canvas: a cluster of CTAs shares each stamp (the pickup map is then in global memory);
+  // a lone CTA stages it in shared memory. Measured on GB300 with 512-thread cluster CTAs
+  // (12 strokes across a 1024 x 768 FP32 canvas, stamps/s, clusters 1 / 8 / 16): F = 21
+  // 320k / 305k; F = 27 287k / 296k; F = 29 264k / 293k / 292k; F = 39 197k / 288k / 288k;
+  // F = 47 155k / 278k / 284k; F = 57 109k / 262k / 273k; F = 87 48k / 180k / 242k. Clusters
   // of 2 or 4 are never the fastest. 16 needs a non-portable cluster, else 8 is used.
   // Clusters run 512-thread CTAs when the stamp's box fits their edge-duplicate masks.
   const int nd = disc_count(b->F, b->support2);
   int cl = env_cluster("PAINTY_STAMP_CLUSTER", 16);
-  if (cl == 0) cl = nd >= 2400 ? 16 : nd >= 1400 ? 8 : 1;
+  if (cl == 0) cl = nd >= 1400 ? 16 : nd >= 450 ? 8 : 1;
   SmemPlan plan{};
   void (*kern)(StampArgs<TK, TV>) = nullptr;
   int nt = kStampThreads;
