@@ -83,3 +83,69 @@ def test_stroke_bitexact(oracle, reference):
         assert n1 == n2
         for p in ("K", "S", "V"):
             assert np.array_equal(oc.get(p), rc.get(p))
+
+
+def test_stamps_edge_parameters_bitexact(oracle, reference):
+    """Rates at 0 and 1, radii from below painty's 0.5 setup threshold to a box larger than
+    the canvas, snapshot on and off, stamps on, across and outside a 9 x 13 canvas."""
+    fp = workloads.footprint_image(seed=9)
+    rng = np.random.default_rng(1)
+    K, S = rng.uniform(0.01, 5, 3), rng.uniform(0.05, 3, 3)
+    st = np.stack([rng.uniform(-3, 16, 30), rng.uniform(-3, 12, 30), rng.uniform(-7, 7, 30)],
+                  axis=1)
+    r0 = rng.uniform(0.5, 1, (9, 13, 3))
+    for rad in (0.0, 0.3, 1.0, 2.0, 4.0, 40.0):
+        for rates in ((0.0, 0.0), (1.0, 1.0), (0.0, 1.0), (1.0, 0.0)):
+            for snap in (True, False):
+                oc, rc = oracle.canvas(9, 13), reference.canvas(9, 13)
+                ob, rb = oracle.brush(rad, fp), reference.brush(rad, fp)
+                for b, c in ((ob, oc), (rb, rc)):
+                    c.set("R0", r0)
+                    b.set_rates(*rates)
+                    b.set_snapshot(snap)
+                    b.dip(K, S)
+                    b.stamps(c, st)
+                case = (rad, rates, snap)
+                assert ob.info()[1:] == rb.info(), case
+                for p in ("K", "S", "V"):
+                    assert np.array_equal(oc.get(p), rc.get(p), equal_nan=True), (case, p)
+                    if rb.info()[1] > 0:
+                        assert np.array_equal(ob.pickup(p), rb.pickup(p), equal_nan=True), (case, p)
+
+
+def _tiny_brush_scenario(lib, tiny_stamp: bool):
+    fp = workloads.footprint_image(seed=9)
+    rng = np.random.default_rng(4)
+    c = lib.canvas(15, 21)
+    c.set("R0", rng.uniform(0.6, 0.9, (15, 21, 3)))
+    a, b = lib.brush(0.3, fp), lib.brush(3.0, fp)
+    a.set_snapshot(True)
+    b.set_snapshot(False)
+    a.dip(np.full(3, 2.0), np.full(3, 0.5))
+    b.dip(np.array([4.0, 0.2, 1.0]), np.array([0.3, 2.0, 0.7]))
+    a.stamps(c, np.array([[10.0, 7.0, 0.0]]))  # the snapshot: a copy of the canvas
+    b.stamps(c, np.array([[10.0, 7.0, 0.2], [11.0, 7.5, 0.4]]))  # the canvas changes under it
+    before = [c.get(p) for p in ("K", "S", "V")]
+    if tiny_stamp:
+        a.stamps(c, np.array([[10.3, 7.2, 0.0]]))
+    after = [c.get(p) for p in ("K", "S", "V")]
+    a.set_radius(3.0)
+    a.stamps(c, np.array([[10.0, 7.0, 0.1]]))  # picks up from the snapshot's interior
+    return before, after, [c.get(p) for p in ("K", "S", "V")]
+
+
+def test_brush_below_setup_radius(oracle, reference):
+    """A brush created with radius < 0.5 never sets up its maps (FootprintBrush.hxx:46-63 ignores
+    changes below 0.5, and the radius starts at 0, :437), so its footprint is 0 x 0. Its stamps
+    leave the canvas unchanged, yet with the snapshot on each one still refreshes the snapshot
+    at the stamp's centre pixel (updateSnapshot, :278-319, with half-sizes (0 - 1) / 2 = 0).
+    The oracle does the same, and the refresh changes what a later, larger stamp picks up."""
+    for tiny in (True, False):
+        o, r = _tiny_brush_scenario(oracle, tiny), _tiny_brush_scenario(reference, tiny)
+        for xo, xr in zip(o, r):
+            for u, v in zip(xo, xr):
+                assert np.array_equal(u, v)
+        for u, v in zip(r[0], r[1]):  # the tiny stamp leaves the canvas as it was
+            assert np.array_equal(u, v)
+    with_tiny, without = _tiny_brush_scenario(reference, True), _tiny_brush_scenario(reference, False)
+    assert not all(np.array_equal(u, v) for u, v in zip(with_tiny[2], without[2]))
