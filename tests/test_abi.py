@@ -124,3 +124,21 @@ def test_phase_timing_build_exports_and_reports_itself(pg):
     if not pg.PHASE_TIMERS:
         out = (ctypes.c_uint64 * 16)()
         assert pg._lib.painty_take_phase_cycles(out) == 4  # PAINTY_ERR_UNSUPPORTED
+
+
+def test_brush_host_setup_matches_oracle_without_gpu(pg, oracle):
+    """Brush setup is host code: the radius rule (changes below 0.5 ignored, so a brush created
+    below 0.5 keeps an empty footprint, FootprintBrush.hxx:46-63), the resampled footprint and
+    the map sizes agree with the oracle bit for bit, through a sequence of setRadius calls."""
+    import numpy as np
+    from painty_gb300 import workloads
+    fp = workloads.footprint_image(seed=9)
+    for r0, steps in ((0.0, (0.3, 0.6, 0.9, 1.2)), (0.3, (0.49, 3.0, 3.4, 2.4)),
+                      (12.0, (12.45, 11.6, 64.0, 0.2))):
+        b, ob = pg.FootprintBrush(r0, fp), oracle.brush(r0, fp)
+        for r in (r0,) + steps:
+            b.setRadius(r)
+            ob.set_radius(r)
+            assert b.info() == ob.info(), (r0, r)
+            if b.info()[1]:
+                assert np.array_equal(b.getFootprint(), ob.footprint()), (r0, r)
