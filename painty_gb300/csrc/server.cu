@@ -7,10 +7,11 @@
 // `step_stamps` stamps (whole strokes) with the batched stamp kernel. Launches of different
 // requests run concurrently on the device -- nothing waits for a step of the whole server --
 // so a request that arrives while others are painting starts as soon as it is admitted. The
-// worker polls the slots' events: a finished chunk is followed by the next one, a finished
-// request by the KM composite of its canvas (Renderer::compose,
-// painty/renderer/Renderer.hxx:26-53) and its download into the caller's buffer, all in the
-// slot's stream order.
+// worker polls each slot's completion word, which the slot's last kernel writes into pinned
+// host memory: a finished chunk is followed by the next one, a finished request by the KM
+// composite of its canvas (Renderer::compose, painty/renderer/Renderer.hxx:26-53) written
+// straight into the caller's pinned buffer, or composited and downloaded in the slot's stream
+// order when that buffer is pageable.
 //
 // Canvases stay resident on the device between requests. Their memory (canvas, composite
 // image, brush buffers) is carved on the host from one device reservation made when the
