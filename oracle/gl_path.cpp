@@ -421,24 +421,36 @@ int32_t orc_gtbrush_paint_stroke(orc_gtbrush* b, orc_tdict* dict, int32_t rows, 
     }
   }
 
-  // imprint (PaintTextureFootprintOnCanvas.compute.glsl:17-53) and clear over the AOI's tiles
+  // imprint and clear over the AOI's tiles
   const int32_t aoiW = static_cast<int32_t>(bmax.x - bmin.x) + 1;
   const int32_t aoiH = static_cast<int32_t>(bmax.y - bmin.y) + 1;
   if (aoiW <= 0 || aoiH <= 0) return 0;
   const int32_t x0 = static_cast<int32_t>(bmin.x), y0 = static_cast<int32_t>(bmin.y);
-  const int32_t x1 = x0 + (aoiW + 15) / 16 * 16, y1 = y0 + (aoiH + 15) / 16 * 16;
   const float Kb[3] = {static_cast<float>(b->paint[0][0]), static_cast<float>(b->paint[0][1]),
                        static_cast<float>(b->paint[0][2])};
   const float Sb[3] = {static_cast<float>(b->paint[1][0]), static_cast<float>(b->paint[1][1]),
                        static_cast<float>(b->paint[1][2])};
-  const float scale = static_cast<float>(b->thicknessScale);
+  orc_glsl_imprint(rows, cols, b->warped.data(), K4, S4, x0, y0, aoiW, aoiH, Kb, Sb,
+                   static_cast<float>(b->thicknessScale));
+  orc_glsl_clear(rows, cols, b->warped.data(), x0, y0, aoiW, aoiH);
+  return 0;
+}
+
+// PaintTextureFootprintOnCanvas.compute.glsl:17-53 over the area of interest (aoi_w x aoi_h
+// pixels from (x0, y0), image coordinates), dispatched as whole 16 x 16 tiles: the pixels of
+// those tiles that lie on the canvas mix the warped texture's paint volume into K4 / S4.
+void orc_glsl_imprint(int32_t rows, int32_t cols, const float* warped, float* K4, float* S4,
+                      int32_t x0, int32_t y0, int32_t aoi_w, int32_t aoi_h, const float Kb[3],
+                      const float Sb[3], float scale) {
+  if (aoi_w <= 0 || aoi_h <= 0) return;
+  const int32_t x1 = x0 + (aoi_w + 15) / 16 * 16, y1 = y0 + (aoi_h + 15) / 16 * 16;
   for (int32_t y = std::max(y0, 0); y < std::min(y1, rows); y++)
     for (int32_t x = std::max(x0, 0); x < std::min(x1, cols); x++) {
       const size_t p = static_cast<size_t>(y) * cols + x;
       float* k = K4 + 4 * p;
       float* s = S4 + 4 * p;
       const float vCan = k[3];
-      const float vTex = scale * b->warped[p];
+      const float vTex = scale * warped[p];
       const float vSum = vCan + vTex;
       if (vSum < 10e-6f) continue;
       for (int c = 0; c < 3; c++) {
@@ -448,10 +460,16 @@ int32_t orc_gtbrush_paint_stroke(orc_gtbrush* b, orc_tdict* dict, int32_t rows, 
       k[3] = vSum;
       s[3] = vTex > 0.0f ? vTex : vCan;
     }
+}
+
+// ClearTextureFootprint.compute.glsl over the same tiles.
+void orc_glsl_clear(int32_t rows, int32_t cols, float* warped, int32_t x0, int32_t y0,
+                    int32_t aoi_w, int32_t aoi_h) {
+  if (aoi_w <= 0 || aoi_h <= 0) return;
+  const int32_t x1 = x0 + (aoi_w + 15) / 16 * 16, y1 = y0 + (aoi_h + 15) / 16 * 16;
   for (int32_t y = std::max(y0, 0); y < std::min(y1, rows); y++)
     for (int32_t x = std::max(x0, 0); x < std::min(x1, cols); x++)
-      b->warped[static_cast<size_t>(y) * cols + x] = 0.0f;
-  return 0;
+      warped[static_cast<size_t>(y) * cols + x] = 0.0f;
 }
 
 }  // extern "C"

@@ -2,8 +2,9 @@
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this module, to check
 results. It loads oracle/_build/liboracle.so (the double-precision restatement of painty's
-paint path, oracle/painty_oracle.cpp) and, where it was built, oracle/_ref/libpainty_ref.so
-(painty's own headers compiled against the repository's Eigen/OpenCV stand-ins).
+paint path, oracle/painty_oracle.cpp) and, where they were built, oracle/_ref/libpainty_ref.so
+(painty's own headers compiled against the repository's Eigen/OpenCV stand-ins) and
+oracle/_ref/libglsl_ref.so (painty's GL compute shaders compiled as C++, oracle/glsl_ref.cpp).
 """
 from __future__ import annotations
 
@@ -17,6 +18,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liboracle.so"
 REF_LIB = HERE / "_ref" / "libpainty_ref.so"
+GLSL_LIB = HERE / "_ref" / "libglsl_ref.so"
 # the reference checkout (only the reference-header build reads it)
 REFERENCE_ROOT = Path(os.environ.get("PAINTY_REFERENCE_ROOT", "/root/reference"))
 
@@ -32,7 +34,7 @@ def build(ref: bool = False) -> None:
 
 def _load(path: Path):
     if not path.exists():
-        build(ref=path == REF_LIB)
+        build(ref=path in (REF_LIB, GLSL_LIB))
     return C.CDLL(str(path))
 
 
@@ -202,6 +204,15 @@ class Oracle:
         f = _Lib(self.lib, "orc").f("glsl_dry_step", _I64, _P, _P, _P, C.c_float)
         f(K4.size // 4, _p(K4), _p(S4), _p(R4), float(portion))
         return K4, R4
+
+    def glsl_imprint(self, warped, K4, S4, x0, y0, aoi_w, aoi_h, Kb, Sb, scale):
+        """TextureBrushGpu's imprint pass on copies of K4 / S4; returns (K4, S4)."""
+        return _glsl_imprint(_Lib(self.lib, "orc"), "glsl_imprint", warped, K4, S4, x0, y0,
+                             aoi_w, aoi_h, Kb, Sb, scale)
+
+    def glsl_clear(self, warped, x0, y0, aoi_w, aoi_h):
+        """TextureBrushGpu's clear pass on a copy of the warped texture."""
+        return _glsl_clear(_Lib(self.lib, "orc"), "glsl_clear", warped, x0, y0, aoi_w, aoi_h)
 
     def texture_dictionary(self, seed: int):
         return _TDict(self.lib, seed)
@@ -434,6 +445,71 @@ class OBrush:
         a = np.ctypeslib.as_array(C.cast(ptr, C.POINTER(_D)), (n,))
         shape = (rows.value, cols.value) if which == "V" else (rows.value, cols.value, 3)
         return a.reshape(shape).copy()
+
+
+def _glsl_imprint(L, name, warped, K4, S4, x0, y0, aoi_w, aoi_h, Kb, Sb, scale):
+    warped = np.ascontiguousarray(warped, dtype=np.float32)
+    K4, S4 = (np.array(x, dtype=np.float32, order="C") for x in (K4, S4))
+    Kb, Sb = (np.ascontiguousarray(x, dtype=np.float32) for x in (Kb, Sb))
+    rows, cols = warped.shape
+    f = L.f(name, _I32, _I32, _P, _P, _P, _I32, _I32, _I32, _I32, _P, _P, C.c_float)
+    f(rows, cols, _p(warped), _p(K4), _p(S4), int(x0), int(y0), int(aoi_w), int(aoi_h), _p(Kb),
+      _p(Sb), float(scale))
+    return K4, S4
+
+
+def _glsl_clear(L, name, warped, x0, y0, aoi_w, aoi_h):
+    warped = np.array(warped, dtype=np.float32, order="C")
+    rows, cols = warped.shape
+    f = L.f(name, _I32, _I32, _P, _I32, _I32, _I32, _I32)
+    f(rows, cols, _p(warped), int(x0), int(y0), int(aoi_w), int(aoi_h))
+    return warped
+
+
+class GlslReference:
+    """painty's GL compute shaders compiled as C++ (oracle/glsl_ref.cpp, prefix glref_):
+    the reference the GL-path restatement is pinned to. Arrays are (rows, cols, 4) float32
+    (K4 / S4 / R4) or (rows, cols) float32 (the warped brush texture)."""
+
+    def __init__(self):
+        self.L = _Lib(_load(GLSL_LIB), "glref")
+
+    @staticmethod
+    def available() -> bool:
+        if GLSL_LIB.exists():
+            return True
+        if not (REFERENCE_ROOT / "painty").is_dir():
+            return False
+        try:
+            build(ref=True)
+        except Exception:
+            return False
+        return GLSL_LIB.exists()
+
+    def compose(self, K4, S4, R4):
+        """ComposeLayerOnSubstrate over a copy of R4."""
+        K4, S4 = (np.ascontiguousarray(x, dtype=np.float32) for x in (K4, S4))
+        out = np.array(R4, dtype=np.float32, order="C")
+        rows, cols = out.shape[:2]
+        self.L.f("compose", _I32, _I32, _P, _P, _P)(rows, cols, _p(K4), _p(S4), _p(out))
+        return out
+
+    def dry_step(self, K4, S4, R4, portion):
+        """DryingStep on copies; returns (K4, R4)."""
+        K4, S4, R4 = (np.array(x, dtype=np.float32, order="C") for x in (K4, S4, R4))
+        rows, cols = K4.shape[:2]
+        self.L.f("dry_step", _I32, _I32, _P, _P, _P, C.c_float)(
+            rows, cols, _p(K4), _p(S4), _p(R4), float(portion))
+        return K4, R4
+
+    def imprint(self, warped, K4, S4, x0, y0, aoi_w, aoi_h, Kb, Sb, scale):
+        """PaintTextureFootprintOnCanvas on copies of K4 / S4; returns (K4, S4)."""
+        return _glsl_imprint(self.L, "imprint", warped, K4, S4, x0, y0, aoi_w, aoi_h, Kb, Sb,
+                             scale)
+
+    def clear(self, warped, x0, y0, aoi_w, aoi_h):
+        """ClearTextureFootprint on a copy of the warped texture."""
+        return _glsl_clear(self.L, "clear", warped, x0, y0, aoi_w, aoi_h)
 
 
 class Reference:

@@ -137,6 +137,13 @@ void orc_glsl_compose(int64_t npix, const float* K4, const float* S4, const floa
                       float* out4);
 /* CanvasGpu::dryStep(portion) */
 void orc_glsl_dry_step(int64_t npix, float* K4, const float* S4, float* R4, float portion);
+/* TextureBrushGpu's imprint and clear passes over an area of interest of aoi_w x aoi_h pixels
+ * from (x0, y0), dispatched as whole 16 x 16 tiles; warped: rows*cols floats (R32F) */
+void orc_glsl_imprint(int32_t rows, int32_t cols, const float* warped, float* K4, float* S4,
+                      int32_t x0, int32_t y0, int32_t aoi_w, int32_t aoi_h, const float Kb[3],
+                      const float Sb[3], float scale);
+void orc_glsl_clear(int32_t rows, int32_t cols, float* warped, int32_t x0, int32_t y0,
+                    int32_t aoi_w, int32_t aoi_h);
 /* TextureBrushDictionary with a seeded pick */
 typedef struct orc_tdict orc_tdict;
 orc_tdict* orc_tdict_create(uint32_t seed);

@@ -1,7 +1,82 @@
 """The oracle's restatement of painty's GL canvas path (gl_path.cpp): hand-derived cases of the
-compute shaders, the texture dictionary's lookup and the strip raster + imprint."""
+compute shaders, the texture dictionary's lookup and the strip raster + imprint; and the
+compute passes bit for bit against painty's own shader sources compiled as C++
+(oracle/glsl_ref.cpp), where the reference checkout is present."""
 import numpy as np
 import pytest
+
+
+@pytest.fixture(scope="module")
+def glsl_ref():
+    from oracle.oracle import GlslReference
+    if not GlslReference.available():
+        pytest.skip("reference checkout not present (oracle/_ref cannot be built here)")
+    return GlslReference()
+
+
+def _gl_canvas(rng, rows, cols):
+    """Random K4 / S4 / R4 with the edge cases the shaders branch on: V zero, below and just
+    above the 1e-5 threshold, tiny S (|b S d| < 1e-5), large b S d (coth's > 20 branch)."""
+    K4 = np.empty((rows, cols, 4), np.float32)
+    S4 = np.empty((rows, cols, 4), np.float32)
+    R4 = np.empty((rows, cols, 4), np.float32)
+    K4[..., :3] = rng.uniform(0.0, 5.0, (rows, cols, 3))
+    S4[..., :3] = rng.uniform(0.05, 3.0, (rows, cols, 3))
+    K4[..., 3] = rng.choice([0.0, 5e-6, 1.1e-5, 0.01, 0.3, 1.0, 4.0, 40.0], (rows, cols)) * \
+        rng.uniform(0.5, 1.5, (rows, cols))
+    S4[..., 3] = rng.uniform(0.0, 2.0, (rows, cols))
+    R4[..., :3] = rng.uniform(0.0, 1.0, (rows, cols, 3))
+    R4[..., 3] = 1.0
+    tiny = rng.random((rows, cols)) < 0.05
+    S4[tiny, 0] = 1e-7
+    zeroK = rng.random((rows, cols)) < 0.05
+    K4[zeroK, 1] = 0.0
+    return K4, S4, R4
+
+
+def _same(a, b):
+    return np.array_equal(np.asarray(a), np.asarray(b), equal_nan=True)
+
+
+def test_compose_matches_painty_shader(oracle, glsl_ref):
+    """ComposeLayerOnSubstrate.compute.glsl: the restatement equals painty's shader source
+    compiled as C++, bit for bit, on a canvas whose size is not a multiple of the 16 x 16
+    work group."""
+    rng = np.random.default_rng(21)
+    K4, S4, R4 = _gl_canvas(rng, 37, 53)
+    assert _same(oracle.glsl_compose(K4, S4, R4), glsl_ref.compose(K4, S4, R4))
+
+
+@pytest.mark.parametrize("portion", [0.0, 5e-6, 0.05, 0.5, 5.0])
+def test_dry_step_matches_painty_shader(oracle, glsl_ref, portion):
+    """DryingStep.compute.glsl: K4 (V) and R4 after one step, bit for bit."""
+    rng = np.random.default_rng(22)
+    K4, S4, R4 = _gl_canvas(rng, 29, 41)
+    ko, ro = oracle.glsl_dry_step(K4, S4, R4, portion)
+    kr, rr = glsl_ref.dry_step(K4, S4, R4, portion)
+    assert _same(ko, kr) and _same(ro, rr)
+
+
+@pytest.mark.parametrize("x0,y0,aoi_w,aoi_h", [(0, 0, 53, 37), (3, 2, 17, 9), (-5, -3, 20, 33),
+                                                (40, 30, 30, 30), (-20, 10, 5, 1),
+                                                (60, 0, 4, 4)])
+def test_imprint_and_clear_match_painty_shaders(oracle, glsl_ref, x0, y0, aoi_w, aoi_h):
+    """PaintTextureFootprintOnCanvas.compute.glsl and ClearTextureFootprint.compute.glsl over
+    an area of interest (offset, whole 16 x 16 tiles, the flipped texture rows, the canvas
+    bounds), on canvases with empty pixels and an empty texture in places, bit for bit."""
+    rng = np.random.default_rng(abs(23 + x0 + 7 * y0))
+    rows, cols = 37, 53
+    K4, S4, _ = _gl_canvas(rng, rows, cols)
+    K4[rng.random((rows, cols)) < 0.3, 3] = 0.0
+    warped = rng.uniform(0.0, 1.0, (rows, cols)).astype(np.float32)
+    warped[rng.random((rows, cols)) < 0.3] = 0.0
+    Kb, Sb = rng.uniform(0.01, 5, 3), rng.uniform(0.05, 3, 3)
+    for scale in (0.0, 0.7, 2.5):
+        ko, so = oracle.glsl_imprint(warped, K4, S4, x0, y0, aoi_w, aoi_h, Kb, Sb, scale)
+        kr, sr = glsl_ref.imprint(warped, K4, S4, x0, y0, aoi_w, aoi_h, Kb, Sb, scale)
+        assert _same(ko, kr) and _same(so, sr), scale
+    assert _same(oracle.glsl_clear(warped, x0, y0, aoi_w, aoi_h),
+                 glsl_ref.clear(warped, x0, y0, aoi_w, aoi_h))
 
 
 def _glsl_reflectance_np(K, S, r0, d):
