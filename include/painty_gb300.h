@@ -335,7 +335,7 @@ painty_status painty_texture_dictionary_add(painty_texture_dictionary* dict,
                                             uint32_t radius_class, uint32_t length_class,
                                             const double* height, int32_t rows, int32_t cols,
                                             int32_t* index_out);
-/* replaces lookup(path, brushSize) (TextureBrushDictionary.cxx:66-110) */
+/* replaces lookup(path, brushSize) (TextureBrushDictionary.cxx:25-69) */
 painty_status painty_texture_dictionary_lookup(painty_texture_dictionary* dict,
                                                const double* path_xy, int32_t n,
                                                double brush_size, int32_t* index_out);

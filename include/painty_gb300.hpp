@@ -418,7 +418,7 @@ class TextureBrushDictionary {
                                         rows, cols, &i));
     return i;
   }
-  // lookup(path, brushSize) (TextureBrushDictionary.cxx:66-110): the chosen texture's index
+  // lookup(path, brushSize) (TextureBrushDictionary.cxx:25-69): the chosen texture's index
   int32_t lookup(const std::vector<vec2>& path, double brushSize) {
     const auto xy = detail::flatten(path);
     int32_t i = -1;

@@ -7,7 +7,7 @@
 //   painty/renderer/src/TextureBrushGpu.cxx:48-246                      (setRadius, paintStroke,
 //        generateWarpedTexture) with BrushTextureWarp.{vert,frag}.glsl,
 //        PaintTextureFootprintOnCanvas.compute.glsl:17-53 and ClearTextureFootprint.compute.glsl
-//   painty/renderer/src/TextureBrushDictionary.cxx:66-180               (lookup, texture classes)
+//   painty/renderer/src/TextureBrushDictionary.cxx:21-181               (lookup, texture classes)
 // A GL canvas is K4 / S4 / R4: rows*cols pixels of 4 floats (painty's rgba32f textures, V in
 // K.a, the lighting volume in S.a), row-major with a top-left origin (the GpuMat upload flips
 // rows into GL's bottom-up textures; the shaders address those flipped rows, so in image
@@ -246,6 +246,18 @@ orc_tdict* orc_tdict_create(uint32_t seed) {
 }
 void orc_tdict_destroy(orc_tdict* d) { delete d; }
 
+// Entry `index`'s GL texture (rows x cols floats, GL row order): copies it into `out` when
+// not NULL; returns 0, or -1 for an index out of range.
+int32_t orc_tdict_texture(const orc_tdict* d, int32_t index, int32_t* rows, int32_t* cols,
+                          float* out) {
+  if (index < 0 || static_cast<size_t>(index) >= d->entries.size()) return -1;
+  const TexEntry& e = d->entries[static_cast<size_t>(index)];
+  *rows = e.rows;
+  *cols = e.cols;
+  if (out) std::memcpy(out, e.gl.data(), e.gl.size() * sizeof(float));
+  return 0;
+}
+
 // createBrushTexturesFromFolder (TextureBrushDictionary.cxx:112-126): loadHeightMap normalises
 // min-max, the GPU copy is normalised again, flipped to GL rows and converted to float
 int32_t orc_tdict_add(orc_tdict* d, uint32_t radius_class, uint32_t length_class,
@@ -267,8 +279,8 @@ int32_t orc_tdict_add(orc_tdict* d, uint32_t radius_class, uint32_t length_class
   return static_cast<int32_t>(d->entries.size() - 1);
 }
 
-// lookup (TextureBrushDictionary.cxx:66-110). The reference scans length classes with the
-// count of size classes (:88); here the scan stops at the chosen size's length classes. Its
+// lookup (TextureBrushDictionary.cxx:25-69). The reference scans length classes with the
+// count of size classes (:46); here the scan stops at the chosen size's length classes. Its
 // random pick (std::random_device) is a seeded std::mt19937 draw mapped by multiply-shift.
 int32_t orc_tdict_lookup(orc_tdict* d, const double* path, int32_t n, double brushSize) {
   if (d->entries.empty() || n < 1) return -1;

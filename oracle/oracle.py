@@ -4,7 +4,8 @@ Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this mo
 results. It loads oracle/_build/liboracle.so (the double-precision restatement of painty's
 paint path, oracle/painty_oracle.cpp) and, where they were built, oracle/_ref/libpainty_ref.so
 (painty's own headers compiled against the repository's Eigen/OpenCV stand-ins) and
-oracle/_ref/libglsl_ref.so (painty's GL compute shaders compiled as C++, oracle/glsl_ref.cpp).
+oracle/_ref/libglsl_ref.so (painty's GL compute shaders compiled as C++, oracle/glsl_ref.cpp)
+and oracle/_ref/libtdict_ref.so (painty's TextureBrushDictionary.cxx, oracle/tdict_ref.cpp).
 """
 from __future__ import annotations
 
@@ -19,6 +20,7 @@ HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liboracle.so"
 REF_LIB = HERE / "_ref" / "libpainty_ref.so"
 GLSL_LIB = HERE / "_ref" / "libglsl_ref.so"
+TDICT_LIB = HERE / "_ref" / "libtdict_ref.so"
 # the reference checkout (only the reference-header build reads it)
 REFERENCE_ROOT = Path(os.environ.get("PAINTY_REFERENCE_ROOT", "/root/reference"))
 
@@ -34,7 +36,7 @@ def build(ref: bool = False) -> None:
 
 def _load(path: Path):
     if not path.exists():
-        build(ref=path in (REF_LIB, GLSL_LIB))
+        build(ref=path in (REF_LIB, GLSL_LIB, TDICT_LIB))
     return C.CDLL(str(path))
 
 
@@ -281,6 +283,7 @@ class _TDict:
 
     def __init__(self, lib, seed: int):
         L = _Lib(lib, "orc")
+        self._lib = lib
         self._destroy = L.f("tdict_destroy", _P)
         self._add = L.f("tdict_add", _P, C.c_uint32, C.c_uint32, _P, _I32, _I32, res=_I32)
         self._lookup = L.f("tdict_lookup", _P, _P, _I32, _D, res=_I32)
@@ -298,6 +301,17 @@ class _TDict:
     def lookup(self, path, brush_size):
         p = np.ascontiguousarray(path, dtype=np.float64)
         return self._lookup(self.h, _p(p), len(p), float(brush_size))
+
+    def texture(self, index):
+        """Entry `index`'s GL texture (float32, GL row order)."""
+        f = _Lib(self._lib, "orc").f("tdict_texture", _P, _I32, C.POINTER(_I32),
+                                     C.POINTER(_I32), _P, res=_I32)
+        rows, cols = _I32(0), _I32(0)
+        if f(self.h, int(index), C.byref(rows), C.byref(cols), None) != 0:
+            raise IndexError(index)
+        out = np.empty((rows.value, cols.value), np.float32)
+        f(self.h, int(index), C.byref(rows), C.byref(cols), _p(out))
+        return out
 
 
 class _GTBrush:
@@ -510,6 +524,65 @@ class GlslReference:
     def clear(self, warped, x0, y0, aoi_w, aoi_h):
         """ClearTextureFootprint on a copy of the warped texture."""
         return _glsl_clear(self.L, "clear", warped, x0, y0, aoi_w, aoi_h)
+
+
+class TDictReference:
+    """painty's own TextureBrushDictionary.cxx (oracle/tdict_ref.cpp, prefix tref_). `build`
+    writes empty files <radius>_<length>_<k>.tex into root/data/textures, registers each one's
+    height map for painty's imRead and lets painty's constructor scan the folder."""
+
+    def __init__(self):
+        self.L = _Lib(_load(TDICT_LIB), "tref")
+        self.h = None
+
+    @staticmethod
+    def available() -> bool:
+        if TDICT_LIB.exists():
+            return True
+        if not (REFERENCE_ROOT / "painty").is_dir():
+            return False
+        try:
+            build(ref=True)
+        except Exception:
+            return False
+        return TDICT_LIB.exists()
+
+    def build(self, root: Path, entries):
+        """entries: (radius_class, length_class, height map) in insertion order. Returns the
+        relative path painty reads for each entry."""
+        folder = Path(root) / "data" / "textures"
+        folder.mkdir(parents=True, exist_ok=True)
+        self.L.f("clear_registry")()
+        reg = self.L.f("register", C.c_char_p, _P, _I32, _I32)
+        names = []
+        for k, (rc, lc, tex) in enumerate(entries):
+            rel = f"data/textures/{int(rc)}_{int(lc)}_{k}.tex"
+            (Path(root) / rel).write_bytes(b"")
+            h = np.ascontiguousarray(tex, dtype=np.float64)
+            reg(rel.encode(), _p(h), h.shape[0], h.shape[1])
+            names.append(rel)
+        self.h = self.L.f("create", C.c_char_p, res=_P)(str(root).encode())
+        if not self.h:
+            raise RuntimeError("painty's TextureBrushDictionary could not be built")
+        return names
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.f("destroy", _P)(self.h)
+            self.h = None
+
+    def lookup(self, path, brush_size):
+        """(source path, GL texture) of painty's pick."""
+        p = np.ascontiguousarray(path, dtype=np.float64)
+        f = self.L.f("lookup", _P, _P, _I32, _D, C.c_char_p, _I32, C.POINTER(_I32),
+                     C.POINTER(_I32), _P, res=_I32)
+        src = C.create_string_buffer(512)
+        rows, cols = _I32(0), _I32(0)
+        buf = np.empty(1 << 20, np.float32)
+        if f(self.h, _p(p), len(p), float(brush_size), src, 512, C.byref(rows), C.byref(cols),
+             _p(buf)) != 0:
+            raise RuntimeError("painty's lookup threw")
+        return src.value.decode(), buf[:rows.value * cols.value].reshape(rows.value, cols.value)
 
 
 class Reference:

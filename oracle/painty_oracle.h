@@ -151,6 +151,8 @@ void orc_tdict_destroy(orc_tdict* d);
 int32_t orc_tdict_add(orc_tdict* d, uint32_t radius_class, uint32_t length_class,
                       const double* height, int32_t rows, int32_t cols);
 int32_t orc_tdict_lookup(orc_tdict* d, const double* path_xy, int32_t n, double brush_size);
+int32_t orc_tdict_texture(const orc_tdict* d, int32_t index, int32_t* rows, int32_t* cols,
+                          float* out);
 /* TextureBrushGpu (smudge off) */
 typedef struct orc_gtbrush orc_gtbrush;
 orc_gtbrush* orc_gtbrush_create(void);

@@ -225,10 +225,10 @@ void normalize_minmax(std::vector<double>& v) {
   for (double& x : v) x = x * scale + shift;
 }
 
-// TextureBrushDictionary::lookup (TextureBrushDictionary.cxx:66-110) over the classes its
+// TextureBrushDictionary::lookup (TextureBrushDictionary.cxx:25-69) over the classes its
 // constructor builds (:128-179): size classes by radius token and length classes by length
 // token, ascending, with their mean texture rows and cols. The length scan stops at the chosen
-// size's length classes (painty bounds it by the number of size classes, :88). The pick is a
+// size's length classes (painty bounds it by the number of size classes, :46). The pick is a
 // seeded std::mt19937 draw mapped by multiply-shift (painty seeds from std::random_device).
 int32_t dict_lookup(painty_texture_dictionary* d, const double* path, int32_t n,
                     double brushSize) {

@@ -213,3 +213,79 @@ def test_gpu_texture_brush_rounds_the_dispatch_up(oracle):
     # bounds x 7..17 (width 11 -> one tile: x 7..22), y 7..13 (one tile: y 7..22)
     assert S4[20, 21, 3] == 0.5 and S4[20, 23, 3] == 0.0 and S4[23, 20, 3] == 0.0
     assert S4[6, 10, 3] == 0.0
+
+
+@pytest.fixture(scope="module")
+def tdict_ref():
+    from oracle.oracle import TDictReference
+    if not TDictReference.available():
+        pytest.skip("reference checkout not present (oracle/_ref cannot be built here)")
+    return TDictReference()
+
+
+def _length_class(avg_lengths, n_size, length, truncate):
+    """lookup's length scan (TextureBrushDictionary.cxx:45-53): the initial best "distance" is
+    the first class's mean length and the initial index 1; `truncate` takes the distance as
+    abs(int(x)), the abs(int) overload."""
+    ml, i1 = avg_lengths[0], 1
+    for i in range(n_size):
+        x = avg_lengths[i] - length
+        d = float(abs(int(x))) if truncate else abs(x)
+        if d < ml:
+            ml, i1 = d, i
+    return i1
+
+
+def test_texture_dictionary_matches_painty(oracle, tdict_ref, tmp_path):
+    """painty's own TextureBrushDictionary.cxx (file-name classes, class averages, the two
+    min-max normalisations, the flip into GL rows, lookup's class choice) against the oracle:
+    the same class for every lookup and the same GL texture for every entry painty picks.
+
+    Two kinds of input are left out, where painty's code has no single meaning. With fewer
+    length classes than size classes the length scan runs past them (TextureBrushDictionary.cxx:
+    45-53). And the scan takes an unqualified abs() of a double (:48): libstdc++ without the
+    C++ <math.h> resolves it to abs(int), which truncates the distance (as this build does),
+    other standard libraries to the double overload (as the oracle does); lookups whose class
+    depends on that choice are checked against the truncating reading only. painty's random
+    pick among a class's candidates (std::random_device) is not reproducible, so picks are
+    compared by class."""
+    rng = np.random.default_rng(31)
+    entries = []
+    for rc, rows in ((3, 6), (9, 18), (27, 54)):
+        for lc, cols in ((20, 30), (90, 100), (300, 320)):
+            for k in range(2 if (rc, lc) in ((9, 90), (27, 20)) else 1):
+                entries.append((rc, lc, rng.random((rows + 2 * k, cols + 3 * k))))
+    names = tdict_ref.build(tmp_path, entries)
+    o = oracle.texture_dictionary(5)
+    for rc, lc, tex in entries:
+        o.add(rc, lc, tex)
+    cls = {n: (rc, lc) for n, (rc, lc, _) in zip(names, entries)}
+    sizes, lengths = (3, 9, 27), (20, 90, 300)
+    avg_rows = [np.mean([t.shape[0] for r, _, t in entries if r == rc]) for rc in sizes]
+    avg_cols = [[np.mean([t.shape[1] for r, l, t in entries if r == rc and l == lc])
+                 for lc in lengths] for rc in sizes]
+    cases = [(float(rng.uniform(1.0, 700.0)), float(rng.uniform(1.0, 90.0))) for _ in range(600)]
+    for i0 in range(len(sizes)):  # lengths whose class depends on the abs() overload
+        grid = [L for L in np.arange(1.0, 700.0, 0.05)
+                if _length_class(avg_cols[i0], len(sizes), L, False) !=
+                _length_class(avg_cols[i0], len(sizes), L, True)]
+        cases += [(float(L), float(avg_rows[i0])) for L in grid[::max(1, len(grid) // 5)]]
+    checked = ambiguous = 0
+    for length, size in cases:
+        path = np.array([[3.0, 4.0], [3.0 + length, 4.0]])
+        src, tex = tdict_ref.lookup(path, size)
+        mr, i0 = avg_rows[0], 0
+        for i, a in enumerate(avg_rows):
+            if abs(a - size) < mr:
+                mr, i0 = abs(a - size), i
+        wide = _length_class(avg_cols[i0], len(sizes), length, truncate=False)
+        narrow = _length_class(avg_cols[i0], len(sizes), length, truncate=True)
+        if wide != narrow:
+            assert cls[src] == (sizes[i0], lengths[narrow]), (length, size)
+            ambiguous += 1
+            continue
+        k = o.lookup(path, size)
+        assert cls[src] == entries[k][:2] == (sizes[i0], lengths[wide]), (length, size)
+        assert np.array_equal(tex, o.texture(names.index(src))), (length, size)
+        checked += 1
+    assert checked > 450 and ambiguous > 0
