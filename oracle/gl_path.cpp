@@ -357,22 +357,14 @@ int32_t orc_gtbrush_paint_stroke(orc_gtbrush* b, orc_tdict* dict, int32_t rows, 
     b->wrows = rows;
     b->wcols = cols;
   }
+  std::vector<float> xy(static_cast<size_t>(4) * n), uv(static_cast<size_t>(4) * n);
+  orc_gl_strip_vertices(path, n, b->radius, xy.data(), uv.data());
   std::vector<float> vx, vy, tu, tv;
-  for (int32_t i = 0; i < n; i++) {
-    const double u = static_cast<double>(i) / static_cast<double>(n - 1);
-    const V2d c = spline(v, u, false);
-    const V2d t = normalized(spline(v, u, true));
-    const V2d d = {-t.y, t.x};
-    const V2d l = {c.x - b->radius * d.x, c.y - b->radius * d.y};
-    const V2d r = {c.x + b->radius * d.x, c.y + b->radius * d.y};
-    vx.push_back(static_cast<float>(r.x));
-    vy.push_back(static_cast<float>(r.y));
-    vx.push_back(static_cast<float>(l.x));
-    vy.push_back(static_cast<float>(l.y));
-    tu.push_back(static_cast<float>(u));
-    tv.push_back(0.0f);
-    tu.push_back(static_cast<float>(u));
-    tv.push_back(1.0f);
+  for (int32_t i = 0; i < 2 * n; i++) {
+    vx.push_back(xy[static_cast<size_t>(2 * i)]);
+    vy.push_back(xy[static_cast<size_t>(2 * i + 1)]);
+    tu.push_back(uv[static_cast<size_t>(2 * i)]);
+    tv.push_back(uv[static_cast<size_t>(2 * i + 1)]);
   }
   const int32_t tex = orc_tdict_lookup(dict, path, n, 2.0 * b->radius);
   if (tex < 0) return -1;
@@ -446,6 +438,33 @@ int32_t orc_gtbrush_paint_stroke(orc_gtbrush* b, orc_tdict* dict, int32_t rows, 
                    static_cast<float>(b->thicknessScale));
   orc_glsl_clear(rows, cols, b->warped.data(), x0, y0, aoiW, aoiH);
   return 0;
+}
+
+// The triangle strip of generateWarpedTexture (TextureBrushGpu.cxx:183-207): for each of the
+// n control points, u = i / (n - 1), the spine's Catmull-Rom point c and unit tangent t
+// (SplineEval), and the vertices c + radius * (-t.y, t.x) then c - radius * (-t.y, t.x) as
+// floats, with texture coordinates (u, 0) and (u, 1). xy and uv receive 2n pairs each.
+void orc_gl_strip_vertices(const double* path, int32_t n, double radius, float* xy, float* uv) {
+  std::vector<V2d> v(static_cast<size_t>(n));
+  for (int32_t i = 0; i < n; i++) v[static_cast<size_t>(i)] = {path[2 * i], path[2 * i + 1]};
+  for (int32_t i = 0; i < n; i++) {
+    const double u = static_cast<double>(i) / static_cast<double>(n - 1);
+    const V2d c = spline(v, u, false);
+    const V2d t = normalized(spline(v, u, true));
+    const V2d d = {-t.y, t.x};
+    const V2d l = {c.x - radius * d.x, c.y - radius * d.y};
+    const V2d r = {c.x + radius * d.x, c.y + radius * d.y};
+    float* p = xy + 4 * i;
+    float* q = uv + 4 * i;
+    p[0] = static_cast<float>(r.x);
+    p[1] = static_cast<float>(r.y);
+    p[2] = static_cast<float>(l.x);
+    p[3] = static_cast<float>(l.y);
+    q[0] = static_cast<float>(u);
+    q[1] = 0.0f;
+    q[2] = static_cast<float>(u);
+    q[3] = 1.0f;
+  }
 }
 
 // PaintTextureFootprintOnCanvas.compute.glsl:17-53 over the area of interest (aoi_w x aoi_h

@@ -216,6 +216,10 @@ class Oracle:
         """TextureBrushGpu's clear pass on a copy of the warped texture."""
         return _glsl_clear(_Lib(self.lib, "orc"), "glsl_clear", warped, x0, y0, aoi_w, aoi_h)
 
+    def gl_strip_vertices(self, path, radius):
+        """TextureBrushGpu's triangle strip: ((2n, 2) float32 vertices, (2n, 2) texcoords)."""
+        return _strip(_Lib(self.lib, "orc"), path, radius)
+
     def texture_dictionary(self, seed: int):
         return _TDict(self.lib, seed)
 
@@ -461,6 +465,14 @@ class OBrush:
         return a.reshape(shape).copy()
 
 
+def _strip(L, path, radius):
+    p = np.ascontiguousarray(path, dtype=np.float64)
+    n = len(p)
+    xy, uv = np.empty((2 * n, 2), np.float32), np.empty((2 * n, 2), np.float32)
+    L.f("gl_strip_vertices", _P, _I32, _D, _P, _P)(_p(p), n, float(radius), _p(xy), _p(uv))
+    return xy, uv
+
+
 def _glsl_imprint(L, name, warped, K4, S4, x0, y0, aoi_w, aoi_h, Kb, Sb, scale):
     warped = np.ascontiguousarray(warped, dtype=np.float32)
     K4, S4 = (np.array(x, dtype=np.float32, order="C") for x in (K4, S4))
@@ -630,6 +642,10 @@ class Reference:
         except Exception:
             return False
         return REF_LIB.exists()
+
+    def gl_strip_vertices(self, path, radius):
+        """TextureBrushGpu's triangle strip over painty's SplineEval."""
+        return _strip(_Lib(self.lib, "ref"), path, radius)
 
     def compute_reflectance(self, K, S, R0, d):
         K, S, R0 = (np.ascontiguousarray(x, dtype=np.float64) for x in (K, S, R0))

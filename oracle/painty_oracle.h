@@ -137,6 +137,10 @@ void orc_glsl_compose(int64_t npix, const float* K4, const float* S4, const floa
                       float* out4);
 /* CanvasGpu::dryStep(portion) */
 void orc_glsl_dry_step(int64_t npix, float* K4, const float* S4, float* R4, float portion);
+/* TextureBrushGpu's triangle strip for an n-point path: 2n vertices (xy) and texture
+ * coordinates (uv), float pairs */
+void orc_gl_strip_vertices(const double* path_xy, int32_t n, double radius, float* xy,
+                           float* uv);
 /* TextureBrushGpu's imprint and clear passes over an area of interest of aoi_w x aoi_h pixels
  * from (x0, y0), dispatched as whole 16 x 16 tiles; warped: rows*cols floats (R32F) */
 void orc_glsl_imprint(int32_t rows, int32_t cols, const float* warped, float* K4, float* S4,

@@ -104,6 +104,31 @@ void ref_spline_catmull_rom(const double* pts, int32_t n, double u, double out[2
   out[1] = r[1];
 }
 
+// The triangle strip of TextureBrushGpu::generateWarpedTexture (TextureBrushGpu.cxx:183-207)
+// over painty's SplineEval. That loop sits in a .cxx built around prgl's GL objects, so the
+// harness repeats its few lines of vertex arithmetic; the spline is painty's.
+void ref_gl_strip_vertices(const double* pts, int32_t n, double radius, float* xy, float* uv) {
+  std::vector<vec2> v;
+  for (int i = 0; i < n; i++) v.emplace_back(pts[2 * i], pts[2 * i + 1]);
+  painty::SplineEval<std::vector<vec2>::const_iterator> spine(v.cbegin(), v.cend());
+  for (int32_t i = 0; i < n; i++) {
+    const auto u = static_cast<double>(i) / static_cast<double>(v.size() - 1);
+    const auto c = spine.catmullRom(u);
+    auto t = spine.catmullRomDerivativeFirst(u).normalized();
+    const vec2 d = {-t[1], t[0]};
+    const vec2 l = c - radius * d;
+    const vec2 r = c + radius * d;
+    xy[4 * i + 0] = static_cast<float>(r[0U]);
+    xy[4 * i + 1] = static_cast<float>(r[1U]);
+    xy[4 * i + 2] = static_cast<float>(l[0U]);
+    xy[4 * i + 3] = static_cast<float>(l[1U]);
+    uv[4 * i + 0] = static_cast<float>(u);
+    uv[4 * i + 1] = static_cast<float>(0.0);
+    uv[4 * i + 2] = static_cast<float>(u);
+    uv[4 * i + 3] = static_cast<float>(1.0);
+  }
+}
+
 double ref_interpolate(const double* img, int32_t rows, int32_t cols, double x, double y) {
   painty::Mat<double> m(rows, cols);
   for (int i = 0; i < rows * cols; i++) m(i) = img[i];

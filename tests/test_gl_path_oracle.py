@@ -289,3 +289,17 @@ def test_texture_dictionary_matches_painty(oracle, tdict_ref, tmp_path):
         assert np.array_equal(tex, o.texture(names.index(src))), (length, size)
         checked += 1
     assert checked > 450 and ambiguous > 0
+
+
+def test_strip_vertices_match_painty_spline(oracle, reference):
+    """TextureBrushGpu's triangle strip (spine points and unit tangents from painty's own
+    SplineEval, offset by the radius, as floats) equals the oracle's, bit for bit, for paths of
+    2 to 9 points, straight, random and with repeated points."""
+    rng = np.random.default_rng(41)
+    paths = [np.array([[0.0, 0.0], [10.0, 0.0]]), np.array([[5.0, 5.0], [5.0, 5.0], [9.0, 2.0]])]
+    paths += [rng.uniform(-50, 400, (int(rng.integers(2, 10)), 2)) for _ in range(40)]
+    for path in paths:
+        for radius in (0.5, 3.7, 25.0):
+            xo, uo = oracle.gl_strip_vertices(path, radius)
+            xr, ur = reference.gl_strip_vertices(path, radius)
+            assert _same(xo, xr) and _same(uo, ur), (path, radius)
