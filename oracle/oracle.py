@@ -643,6 +643,16 @@ class Reference:
             return False
         return REF_LIB.exists()
 
+    def mix_single_paint(self, weights, K, S):
+        """painty's own PaintMixer::mixSinglePaint over the palette (K, S: n x 3)."""
+        w = np.ascontiguousarray(weights, dtype=np.float64)
+        K, S = (np.ascontiguousarray(x, dtype=np.float64) for x in (K, S))
+        ok, os_ = np.zeros(3), np.zeros(3)
+        f = _Lib(self.lib, "ref").f("mix_single_paint", _P, _I32, _P, _P, _P, _P, res=_I32)
+        if f(_p(w), len(w), _p(K), _p(S), _p(ok), _p(os_)) != 0:
+            raise ValueError("painty's mixSinglePaint threw")
+        return ok, os_
+
     def gl_strip_vertices(self, path, radius):
         """TextureBrushGpu's triangle strip over painty's SplineEval."""
         return _strip(_Lib(self.lib, "ref"), path, radius)

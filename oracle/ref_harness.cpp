@@ -8,7 +8,8 @@
 //
 // What is the reference's code here: KubelkaMunk.hxx, Math.hxx (coth), Spline.hxx,
 // Color.hxx (CIEDE2000), image/Mat.hxx (Interpolate, PaddedMat), renderer/PaintLayer.hxx,
-// Canvas.hxx, FootprintBrush.hxx, Renderer.hxx. What is the harness's: the footprint
+// Canvas.hxx, FootprintBrush.hxx, Renderer.hxx, and mixer/src/PaintMixer.cxx (its Ceres
+// fitting routines compiled against oracle/ref_shim/ceres, not run). What is the harness's: the footprint
 // "image" source (painty::io::imRead below returns the registered full-size footprint),
 // and the stroke loop of FootprintBrush::paintStroke, re-driven here over the reference's
 // own CatmullRom/imprint because that loop reads path[SIZE_MAX] at i = 0
@@ -23,7 +24,9 @@
 #include "painty/core/KubelkaMunk.hxx"
 #include "painty/core/Math.hxx"
 #include "painty/core/Spline.hxx"
+#include "painty/image/ColorExtraction.hxx"
 #include "painty/image/Mat.hxx"
+#include "painty/mixer/PaintMixer.hxx"
 #include "painty/renderer/Canvas.hxx"
 #include "painty/renderer/FootprintBrush.hxx"
 #include "painty/renderer/PaintLayer.hxx"
@@ -57,6 +60,13 @@ namespace painty {
 namespace io {
 void imRead(const std::string&, Mat<double>& gray, bool) { gray = g_footprint_full.clone(); }
 }  // namespace io
+
+// PaintMixer.cxx (linked for mixSinglePaint) also references the palette extraction of
+// painty/image/src/ColorExtraction.cxx, which needs OpenCV's clustering; the oracle build never
+// calls it.
+void ExtractColorPaletteAharoni(const Mat<vec3>&, std::vector<vec3>&, uint32_t) {
+  throw std::logic_error("ExtractColorPaletteAharoni is not part of the oracle build");
+}
 
 // The harness's stand-ins for the two out-of-line classes TextureBrush.hxx needs
 // (painty/renderer/src/BrushStrokeSample.cxx, painty/image/src/TextureWarp.cxx load stroke
@@ -127,6 +137,30 @@ void ref_gl_strip_vertices(const double* pts, int32_t n, double radius, float* x
     uv[4 * i + 2] = static_cast<float>(u);
     uv[4 * i + 3] = static_cast<float>(1.0);
   }
+}
+
+// PaintMixer::mixSinglePaint (painty/mixer/src/PaintMixer.cxx:327-355) over a palette of n
+// paints (K, S: n x 3); 0, or -1 when painty throws.
+int32_t ref_mix_single_paint(const double* weights, int32_t n, const double* K, const double* S,
+                             double out_K[3], double out_S[3]) {
+  painty::Palette palette(static_cast<size_t>(n));
+  for (int32_t i = 0; i < n; i++)
+    for (int c = 0; c < 3; c++) {
+      palette[static_cast<size_t>(i)].K[c] = K[3 * i + c];
+      palette[static_cast<size_t>(i)].S[c] = S[3 * i + c];
+    }
+  try {
+    const painty::PaintMixer mixer(palette);
+    const painty::PaintCoeff p =
+      mixer.mixSinglePaint(std::vector<double>(weights, weights + n));
+    for (int c = 0; c < 3; c++) {
+      out_K[c] = p.K[c];
+      out_S[c] = p.S[c];
+    }
+  } catch (...) {
+    return -1;
+  }
+  return 0;
 }
 
 double ref_interpolate(const double* img, int32_t rows, int32_t cols, double x, double y) {

@@ -149,3 +149,23 @@ def test_brush_below_setup_radius(oracle, reference):
             assert np.array_equal(u, v)
     with_tiny, without = _tiny_brush_scenario(reference, True), _tiny_brush_scenario(reference, False)
     assert not all(np.array_equal(u, v) for u, v in zip(with_tiny[2], without[2]))
+
+
+def test_mix_single_paint_bitexact(oracle, reference, pg):
+    """PaintMixer::mixSinglePaint (painty's own PaintMixer.cxx, its Ceres fitting routines
+    compiled against a stand-in and not run) against the oracle and the library's host code:
+    weights that sum to one, that do not (normalised when more than painty's Eps away), and
+    sparse ones, bit for bit."""
+    K, S = workloads.pigments()
+    rng = np.random.default_rng(8)
+    cases = [rng.dirichlet(np.full(len(K), a)) for a in (0.1, 0.3, 1.0, 5.0) for _ in range(5)]
+    cases += [c * s for c in cases[:6] for s in (0.5, 1.0 + 1e-12, 2.0, 1e-3)]
+    one_hot = np.zeros(len(K))
+    one_hot[3] = 1.0
+    cases += [one_hot, np.zeros(len(K))]
+    for w in cases:
+        kr, sr = reference.mix_single_paint(w, K, S)
+        ko, so = oracle.mix_single_paint(w, K, S)
+        kl, sl = pg.mix_single_paint(w, K, S)
+        for a, b in ((kr, ko), (sr, so), (kr, kl), (sr, sl)):
+            assert np.array_equal(a, b, equal_nan=True), w
