@@ -643,6 +643,26 @@ class Reference:
             return False
         return REF_LIB.exists()
 
+    def load_palette(self, text: str):
+        """painty's LoadPalette of a JSON text: [(K, S)] as float64 arrays."""
+        f = _Lib(self.lib, "ref").f("load_palette", C.c_char_p, _P, _P, _I32, res=_I32)
+        cap = 4096
+        K, S = np.zeros((cap, 3)), np.zeros((cap, 3))
+        n = f(text.encode(), _p(K), _p(S), cap)
+        if n < 0:
+            raise ValueError("painty's LoadPalette threw")
+        return [(K[i].copy(), S[i].copy()) for i in range(min(n, cap))]
+
+    def visualize_palette(self, palette, thickness):
+        """painty's VisualizePalette: (200, 100 n, 3) float64 sRGB."""
+        n = len(palette)
+        K = np.ascontiguousarray([k for k, _ in palette], dtype=np.float64).reshape(n, 3)
+        S = np.ascontiguousarray([s for _, s in palette], dtype=np.float64).reshape(n, 3)
+        out = np.zeros((200, 100 * n, 3))
+        f = _Lib(self.lib, "ref").f("visualize_palette", _P, _P, _I32, _D, _P)
+        f(_p(K), _p(S), n, float(thickness), _p(out))
+        return out
+
     def mix_single_paint(self, weights, K, S):
         """painty's own PaintMixer::mixSinglePaint over the palette (K, S: n x 3)."""
         w = np.ascontiguousarray(weights, dtype=np.float64)

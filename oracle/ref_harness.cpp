@@ -8,8 +8,9 @@
 //
 // What is the reference's code here: KubelkaMunk.hxx, Math.hxx (coth), Spline.hxx,
 // Color.hxx (CIEDE2000), image/Mat.hxx (Interpolate, PaddedMat), renderer/PaintLayer.hxx,
-// Canvas.hxx, FootprintBrush.hxx, Renderer.hxx, and mixer/src/PaintMixer.cxx (its Ceres
-// fitting routines compiled against oracle/ref_shim/ceres, not run). What is the harness's: the footprint
+// Canvas.hxx, FootprintBrush.hxx, Renderer.hxx, mixer/src/PaintMixer.cxx (its Ceres fitting
+// routines compiled against oracle/ref_shim/ceres, not run) and mixer/src/Serialization.cxx
+// (palette JSON through oracle/ref_shim/nlohmann, the palette swatch image). What is the harness's: the footprint
 // "image" source (painty::io::imRead below returns the registered full-size footprint),
 // and the stroke loop of FootprintBrush::paintStroke, re-driven here over the reference's
 // own CatmullRom/imprint because that loop reads path[SIZE_MAX] at i = 0
@@ -17,6 +18,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <sstream>
 #include <string>
 #include <vector>
 
@@ -27,6 +29,7 @@
 #include "painty/image/ColorExtraction.hxx"
 #include "painty/image/Mat.hxx"
 #include "painty/mixer/PaintMixer.hxx"
+#include "painty/mixer/Serialization.hxx"
 #include "painty/renderer/Canvas.hxx"
 #include "painty/renderer/FootprintBrush.hxx"
 #include "painty/renderer/PaintLayer.hxx"
@@ -161,6 +164,41 @@ int32_t ref_mix_single_paint(const double* weights, int32_t n, const double* K, 
     return -1;
   }
   return 0;
+}
+
+// LoadPalette (painty/mixer/src/Serialization.cxx:38-44) of a JSON text: the number of paints,
+// their K and S (n x 3) copied out up to `cap` paints; -1 when painty throws.
+int32_t ref_load_palette(const char* text, double* K, double* S, int32_t cap) {
+  painty::Palette palette;
+  try {
+    std::istringstream in(text);
+    painty::LoadPalette(in, palette);
+  } catch (...) {
+    return -1;
+  }
+  for (size_t i = 0; i < palette.size() && static_cast<int32_t>(i) < cap; i++)
+    for (int c = 0; c < 3; c++) {
+      K[3 * i + c] = palette[i].K[c];
+      S[3 * i + c] = palette[i].S[c];
+    }
+  return static_cast<int32_t>(palette.size());
+}
+
+// VisualizePalette (Serialization.cxx:64-137) of n paints at `thickness`: 200 x 100n x 3
+// doubles (sRGB) into `out`.
+void ref_visualize_palette(const double* K, const double* S, int32_t n, double thickness,
+                           double* out) {
+  painty::Palette palette(static_cast<size_t>(n));
+  for (int32_t i = 0; i < n; i++)
+    for (int c = 0; c < 3; c++) {
+      palette[static_cast<size_t>(i)].K[c] = K[3 * i + c];
+      palette[static_cast<size_t>(i)].S[c] = S[3 * i + c];
+    }
+  const painty::Mat<vec3> img = painty::VisualizePalette(palette, thickness);
+  for (int32_t y = 0; y < img.rows; y++)
+    for (int32_t x = 0; x < img.cols; x++)
+      for (int c = 0; c < 3; c++)
+        out[(static_cast<size_t>(y) * img.cols + x) * 3 + c] = img(y, x)[c];
 }
 
 double ref_interpolate(const double* img, int32_t rows, int32_t cols, double x, double y) {

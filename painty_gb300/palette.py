@@ -2,7 +2,7 @@
 
 LoadPalette / SavePalette (painty/mixer/src/Serialization.cxx:38-53) read and write a JSON
 array of {"K": [r, g, b], "S": [r, g, b]} objects (nlohmann::json, keys sorted, compact);
-VisualizePalette (:64-135) paints each paint's Kubelka-Munk reflectance at a given thickness
+VisualizePalette (:64-137) paints each paint's Kubelka-Munk reflectance at a given thickness
 on white and on black into a 200 x 100n swatch image (sRGB). The reflectances come from the
 library's composite kernel on an F64 layer (painty's ComputeReflectance arithmetic).
 """
@@ -10,6 +10,7 @@ from __future__ import annotations
 
 import io
 import json
+import math
 import os
 from typing import IO, Iterable
 
@@ -57,10 +58,20 @@ def dumps_palette(palette: Iterable) -> str:
 
 
 def rgb2srgb(lin: np.ndarray) -> np.ndarray:
-    """ColorConverter::rgb2srgb (painty/core/Color.hxx:198-206)."""
+    """ColorConverter::rgb2srgb (painty/core/Color.hxx:198-206), value by value with the C
+    library's pow (math.pow), as painty's std::pow: numpy's vectorised power can differ from it
+    in the last bit. NaN stays NaN."""
     lin = np.asarray(lin, dtype=np.float64)
-    return np.where(lin <= 0.00313066844250063, lin * 12.92,
-                    1.055 * np.power(np.maximum(lin, 0.0), 1.0 / 2.4) - 0.055)
+    out = np.empty_like(lin)
+    flat, res = lin.reshape(-1), out.reshape(-1)
+    for i, v in enumerate(flat.tolist()):
+        if v <= 0.00313066844250063:
+            res[i] = v * 12.92
+        elif v == v:
+            res[i] = 1.055 * math.pow(v, 1.0 / 2.4) - 0.055
+        else:
+            res[i] = v
+    return out
 
 
 def palette_reflectance(palette: Palette, thickness: float, background) -> np.ndarray:
@@ -81,7 +92,7 @@ def palette_reflectance(palette: Palette, thickness: float, background) -> np.nd
 
 
 def visualize_palette(palette: Palette, applied_thickness: float) -> np.ndarray:
-    """VisualizePalette (Serialization.cxx:64-135): (200, 100 n, 3) sRGB swatches -- per paint
+    """VisualizePalette (Serialization.cxx:64-137): (200, 100 n, 3) sRGB swatches -- per paint
     a white band, the paint on white, white, black, the paint on black, black."""
     n = len(palette)
     img = np.zeros((200, 100 * n, 3))

@@ -1,5 +1,5 @@
 """Palette JSON I/O (LoadPalette / SavePalette, Serialization.cxx:38-53) and the swatch image
-(VisualizePalette, :64-135)."""
+(VisualizePalette, :64-137)."""
 import io
 import os
 from pathlib import Path
@@ -66,3 +66,49 @@ def test_visualize_palette_vs_oracle(pg, oracle):
         assert (img[:20, x] == 1.0).all() and (img[80:100, x] == 1.0).all()
         assert (img[100:120, x] == 0.0).all() and (img[180:, x] == 0.0).all()
         np.testing.assert_array_equal(img[20:80, x], np.broadcast_to(img[50, x], (60, 3)))
+
+
+@pytest.fixture(scope="module")
+def painty_ref():
+    from oracle.oracle import Reference
+    if not Reference.available():
+        pytest.skip("reference checkout not present (oracle/_ref cannot be built here)")
+    return Reference()
+
+
+def test_load_palette_matches_painty(painty_ref):
+    """painty's own LoadPalette (Serialization.cxx:38-44, its JSON library replaced by a
+    stand-in that reads numbers as nlohmann does) and load_palette read the same paints, bit for
+    bit: painty's palette files, and texts with integers, exponents, extra keys and spacing."""
+    texts = ['[{"K":[1,2,3],"S":[4,5,6]}]',
+             '[ {"S": [0.2, 3e-3, 1E2], "K": [0.1, -0.5, 7.25e+1], "name": "x"} ,\n'
+             '  {"K":[0.30000000000000004,1e-320,123456789012],"S":[1,0.5,0.25]} ]',
+             '[]']
+    root = Path(os.environ.get("PAINTY_REFERENCE_ROOT", "/root/reference")) / "data" / "paint_palettes"
+    if root.is_dir():
+        texts += [f.read_text() for f in sorted(root.glob("*.json"))]
+    for text in texts:
+        ours = P.load_palette(io.StringIO(text))
+        theirs = painty_ref.load_palette(text)
+        assert len(ours) == len(theirs)
+        for (K, S), (K2, S2) in zip(ours, theirs):
+            assert np.array_equal(K, K2) and np.array_equal(S, S2), text[:60]
+
+
+def test_visualize_palette_layout_matches_painty(painty_ref, oracle, monkeypatch):
+    """visualize_palette's bands, widths and sRGB conversion against painty's own
+    VisualizePalette (Serialization.cxx:64-137), bit for bit, with the reflectances taken from
+    the oracle (painty's ComputeReflectance, bit for bit) instead of the GPU composite."""
+    def reflectance(palette, thickness, background):
+        bg = np.asarray(background, dtype=np.float64)
+        return np.array([oracle.compute_reflectance(K, S, bg, thickness) for K, S in palette])
+
+    monkeypatch.setattr(P, "palette_reflectance", reflectance)
+    rng = np.random.default_rng(12)
+    palettes = [SMALL, SMALL[:1],
+                [(rng.uniform(0.01, 5, 3), rng.uniform(0.05, 3, 3)) for _ in range(7)]]
+    for pal in palettes:
+        for t in (0.05, 0.5, 3.0):
+            # NaN where K = 0: painty's formula (0 * coth 0) kept as it is
+            assert np.array_equal(P.visualize_palette(pal, t), painty_ref.visualize_palette(pal, t),
+                                  equal_nan=True)
