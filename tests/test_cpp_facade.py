@@ -124,3 +124,23 @@ def test_facade_texture_brush_and_render(demo, pg, tmp_path):
         assert np.array_equal(got[o:o + npx * nch], want), p
         o += npx * nch
     assert np.array_equal(got[o:o + npx * 3], pg.Renderer().render(c).download().ravel())
+
+
+def test_facade_reads_painty_palettes_as_painty_does(demo, tmp_path):
+    """The facade's LoadPalette on painty's own palette files gives painty's own LoadPalette's
+    values (Serialization.cxx:38-44 compiled in the oracle's reference build), bit for bit."""
+    from oracle.oracle import Reference
+    from painty_gb300 import palette as P
+    root = Path(os.environ.get("PAINTY_REFERENCE_ROOT", "/root/reference")) / "data" / "paint_palettes"
+    if not root.is_dir() or not Reference.available():
+        pytest.skip("reference checkout not present")
+    ref = Reference()
+    for src in sorted(root.glob("*.json")):
+        dst = tmp_path / src.name
+        r = subprocess.run([str(demo), "palette", str(src), str(dst)], capture_output=True,
+                           text=True, timeout=120)
+        assert r.returncode == 0, r.stdout + r.stderr
+        ours, theirs = P.load_palette(dst), ref.load_palette(src.read_text())
+        assert len(ours) == len(theirs) > 0
+        for (K, S), (K2, S2) in zip(ours, theirs):
+            assert np.array_equal(K, K2) and np.array_equal(S, S2), src.name
